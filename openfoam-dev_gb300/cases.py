@@ -1,0 +1,225 @@
+"""Seeded synthetic LDU systems (ctypes front end of ``lib/libcfxcase.so``).
+
+Each system is a dict of numpy arrays in OpenFOAM's LDU layout:
+``l``/``u`` (int32 lowerAddr/upperAddr, upper-triangular face order),
+``diag``, ``upper``, ``lower`` (float64; ``lower`` is None when symmetric),
+``source`` and, for geometric agglomeration, ``Sf`` (internal face-area
+vectors, [nFaces, 3]).
+
+The workloads match the solver benchmarks:
+
+* ``pcg_cube``        uniform n^3 unit cube, -laplacian(1,T), Dirichlet T=0
+                      on x=0, zero-gradient elsewhere, source U[-1,1]
+* ``gamg_cube``       the same on a cube with interior vertices jittered by
+                      U[-j*h, j*h] per axis (non-orthogonal, no corrections)
+* ``bicgstab_cube``   jittered cube, upwind div(phi,T) - laplacian(1e-3,T)
+                      with |U| = 1 in a seeded random direction, cells
+                      randomly permuted then renumbered by Cuthill-McKee
+* ``box``             an nx*ny*nz box of given aspect, Dirichlet on one face
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import LIB_DIR
+
+_lib = None
+
+PATCHES = ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")
+
+i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(LIB_DIR, "libcfxcase.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run __graft_entry__.build()")
+        L = ctypes.CDLL(path)
+        i64 = ctypes.c_int64
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        L.cfxc_box_counts.argtypes = [ctypes.c_int] * 3 + [i64p] * 4
+        L.cfxc_box_points.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_uint64, f64p]
+        L.cfxc_box_faces.argtypes = [ctypes.c_int] * 3 + [i32p] * 4
+        L.cfxc_face_geometry.argtypes = [i64, i32p, f64p, f64p, f64p, f64p]
+        L.cfxc_cell_geometry.argtypes = [i64, i64, i64, i32p, i32p, f64p, f64p, f64p, f64p]
+        L.cfxc_laplacian.argtypes = [i64, i64, i64, i32p, i32p, i32p, f64p, f64p, f64p,
+                                     ctypes.c_double, ctypes.c_int, f64p, f64p]
+        L.cfxc_convection_diffusion.argtypes = [i64, i64, i64, i32p, i32p, i32p, f64p, f64p, f64p,
+                                                f64p, f64p, ctypes.c_double, ctypes.c_int,
+                                                f64p, f64p, f64p]
+        L.cfxc_uniform.argtypes = [ctypes.c_uint64, i64, ctypes.c_double, ctypes.c_double, f64p]
+        L.cfxc_random_order.argtypes = [ctypes.c_uint64, i64, i32p]
+        L.cfxc_cuthill_mckee.argtypes = [i64, i64, i32p, i32p, i32p]
+        L.cfxc_renumber.argtypes = [i64, i64, i32p, i32p, i32p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _chk(rc, what):
+    if rc != 0:
+        raise ValueError(f"{what} failed ({rc})")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def box_mesh(nx, ny, nz, L=(1.0, 1.0, 1.0), jitter=0.0, seed=0):
+    """Hex box mesh with OpenFOAM face geometry (points, faces, owner, ...)."""
+    L_ = lib()
+    c = [ctypes.c_int64() for _ in range(4)]
+    _chk(L_.cfxc_box_counts(nx, ny, nz, *[ctypes.byref(x) for x in c]), "box_counts")
+    nP, nC, nI, nB = (x.value for x in c)
+    nF = nI + nB
+    pts = np.empty(3 * nP)
+    _chk(L_.cfxc_box_points(nx, ny, nz, L[0], L[1], L[2], jitter, seed, pts), "box_points")
+    faces = np.empty(4 * nF, np.int32)
+    owner = np.empty(nF, np.int32)
+    nei = np.empty(max(nI, 1), np.int32)
+    ps = np.empty(7, np.int32)
+    _chk(L_.cfxc_box_faces(nx, ny, nz, faces, owner, nei, ps), "box_faces")
+    nei = nei[:nI]
+    Sf = np.empty(3 * nF)
+    Cf = np.empty(3 * nF)
+    magSf = np.empty(nF)
+    _chk(L_.cfxc_face_geometry(nF, faces, pts, Sf, Cf, magSf), "face_geometry")
+    C = np.empty(3 * nC)
+    V = np.empty(nC)
+    _chk(L_.cfxc_cell_geometry(nC, nF, nI, owner, np.ascontiguousarray(nei) if nI else np.zeros(1, np.int32),
+                               Sf, Cf, C, V), "cell_geometry")
+    return dict(nx=nx, ny=ny, nz=nz, nCells=nC, nInternalFaces=nI, nFaces=nF,
+                points=pts, faces=faces, owner=owner, neighbour=nei, patchStart=ps,
+                Sf=Sf, Cf=Cf, magSf=magSf, C=C, V=V)
+
+
+def _mask(dirichlet):
+    m = 0
+    for p in dirichlet:
+        m |= 1 << PATCHES.index(p)
+    return m
+
+
+def laplacian(mesh, gamma=1.0, dirichlet=("xmin",)):
+    """Symmetric -laplacian(gamma,T): returns l, u, diag, upper (lower None)."""
+    L_ = lib()
+    nC, nI, nF = mesh["nCells"], mesh["nInternalFaces"], mesh["nFaces"]
+    diag = np.empty(nC)
+    upper = np.empty(max(nI, 1))
+    nei = mesh["neighbour"] if nI else np.zeros(1, np.int32)
+    _chk(L_.cfxc_laplacian(nC, nF, nI, mesh["owner"], np.ascontiguousarray(nei), mesh["patchStart"],
+                           mesh["magSf"], mesh["Cf"], mesh["C"], gamma, _mask(dirichlet),
+                           diag, upper), "laplacian")
+    return dict(l=mesh["owner"][:nI].copy(), u=mesh["neighbour"].copy(), diag=diag,
+                upper=upper[:nI].copy(), lower=None,
+                Sf=mesh["Sf"][: 3 * nI].reshape(nI, 3).copy())
+
+
+def convection_diffusion(mesh, U, gamma, dirichlet=("xmin",)):
+    """Asymmetric upwind div(phi,T) - laplacian(gamma,T)."""
+    L_ = lib()
+    nC, nI, nF = mesh["nCells"], mesh["nInternalFaces"], mesh["nFaces"]
+    diag = np.empty(nC)
+    upper = np.empty(nI)
+    lower = np.empty(nI)
+    Uv = np.asarray(U, dtype=np.float64)
+    _chk(L_.cfxc_convection_diffusion(nC, nF, nI, mesh["owner"], mesh["neighbour"], mesh["patchStart"],
+                                      mesh["Sf"], mesh["magSf"], mesh["Cf"], mesh["C"], Uv, gamma,
+                                      _mask(dirichlet), diag, upper, lower), "convection_diffusion")
+    return dict(l=mesh["owner"][:nI].copy(), u=mesh["neighbour"].copy(), diag=diag,
+                upper=upper, lower=lower, Sf=mesh["Sf"][: 3 * nI].reshape(nI, 3).copy())
+
+
+def uniform(seed, n, lo=-1.0, hi=1.0):
+    out = np.empty(n)
+    _chk(lib().cfxc_uniform(seed, n, lo, hi, out), "uniform")
+    return out
+
+
+def random_order(seed, n):
+    out = np.empty(n, np.int32)
+    _chk(lib().cfxc_random_order(seed, n, out), "random_order")
+    return out
+
+
+def cuthill_mckee(sys_):
+    n = sys_["diag"].size
+    out = np.empty(n, np.int32)
+    _chk(lib().cfxc_cuthill_mckee(n, sys_["l"].size, sys_["l"], sys_["u"], out), "cuthill_mckee")
+    return out
+
+
+def renumber(sys_, new_order):
+    """Renumber a system in place (cells by new_order, faces re-sorted)."""
+    n, nf = sys_["diag"].size, sys_["l"].size
+    fo = np.empty(nf, np.int32)
+    ff = np.empty(nf, np.int32)
+    _chk(lib().cfxc_renumber(n, nf, np.ascontiguousarray(new_order, np.int32), sys_["l"], sys_["u"],
+                             _ptr(sys_["diag"]), _ptr(sys_["upper"]), _ptr(sys_.get("lower")),
+                             _ptr(fo), _ptr(ff)), "renumber")
+    if sys_.get("Sf") is not None:
+        Sf = sys_["Sf"][fo]
+        Sf[ff == 1] *= -1.0
+        sys_["Sf"] = np.ascontiguousarray(Sf)
+    if sys_.get("source") is not None:
+        sys_["source"] = sys_["source"][new_order].copy()
+    return sys_
+
+
+def pcg_cube(n=64, seed=1):
+    """C1: uniform n^3 unit cube Laplacian, Dirichlet x=0, source U[-1,1]."""
+    s = laplacian(box_mesh(n, n, n, jitter=0.0, seed=seed))
+    s["source"] = uniform(seed, s["diag"].size)
+    s["name"] = f"laplacian-cube-{n}"
+    return s
+
+
+def gamg_cube(n=256, jitter=0.2, seed=1):
+    """C2: jittered n^3 cube Laplacian, Dirichlet x=0, source U[-1,1]."""
+    s = laplacian(box_mesh(n, n, n, jitter=jitter, seed=seed))
+    s["source"] = uniform(seed + 1000, s["diag"].size)
+    s["name"] = f"laplacian-jittered-cube-{n}"
+    return s
+
+
+def bicgstab_cube(n=128, jitter=0.2, seed=1, gamma=1e-3):
+    """C3: jittered cube, upwind convection-diffusion, random + CM order."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=3)
+    U = d / np.linalg.norm(d)
+    s = convection_diffusion(box_mesh(n, n, n, jitter=jitter, seed=seed), U, gamma)
+    renumber(s, random_order(seed + 7, s["diag"].size))
+    renumber(s, cuthill_mckee(s))
+    s["source"] = uniform(seed + 2000, s["diag"].size)
+    s["name"] = f"upwind-convection-diffusion-cube-{n}"
+    s["U"] = U
+    return s
+
+
+def box(nx, ny, nz, dirichlet="xmin", seed=1):
+    """C4 member: box of nx*ny*nz cells (cell size 1/max(n)), one Dirichlet face."""
+    h = 1.0 / max(nx, ny, nz)
+    s = laplacian(box_mesh(nx, ny, nz, L=(nx * h, ny * h, nz * h), seed=seed), dirichlet=(dirichlet,))
+    s["source"] = uniform(seed, s["diag"].size)
+    s["name"] = f"laplacian-box-{nx}x{ny}x{nz}"
+    return s
+
+
+def batch_boxes(count=512, lo=4096, hi=500000, seed=1):
+    """C4: box shapes with cell counts log-uniform in [lo, hi], aspect U[1,4]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        N = math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        a = rng.uniform(1.0, 4.0, size=3)
+        scale = (N / np.prod(a)) ** (1.0 / 3.0)
+        dims = [max(2, int(round(x * scale))) for x in a]
+        face = PATCHES[int(rng.integers(0, 6))]
+        out.append((dims[0], dims[1], dims[2], face, int(seed * 100003 + k)))
+    return out

@@ -1,0 +1,847 @@
+/*
+ * ldu_oracle.c - CPU restatement of OpenFOAM-dev's lduMatrix solver path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker; see ldu_oracle.h).  Compile with
+ * -ffp-contract=off: every loop keeps the reference's operation order so the
+ * results equal the reference's x86-64 (non-FMA) build bit for bit.
+ */
+#include "ldu_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* OpenFOAM doubleScalar constants (src/OpenFOAM/primitives/Scalar/doubleScalar/doubleScalar.H:55-66)
+ * and SolverPerformance great_/small_/vsmall_ (SolverPerformance.H:285-291). */
+#define VSMALL DBL_MIN
+#define GREAT (1.0 / DBL_EPSILON)
+#define SP_GREAT 1e20
+#define SP_SMALL 1e-20
+
+static void* xmalloc(size_t n) { return malloc(n ? n : 1); }
+
+/* ---------------------------------------------------------------- addressing */
+
+/* lduAddressing::calcLosort (lduAddressing.C:32-90): faces grouped by
+ * neighbour (upperAddr), each group in face order.  losortStart is the
+ * group offset array (calcLosortStart, lduAddressing.C:130-170).
+ * calcOwnerStart (lduAddressing.C:93-127): offsets of the owner-sorted faces. */
+int ldu_init_addr(ldu_matrix* m) {
+    const int n = m->nCells, nf = m->nFaces;
+    m->ownerStart = (int*)xmalloc(sizeof(int) * (n + 1));
+    m->losort = (int*)xmalloc(sizeof(int) * nf);
+    m->losortStart = (int*)xmalloc(sizeof(int) * (n + 1));
+    int* cnt = (int*)calloc(n + 1, sizeof(int));
+    for (int f = 0; f < nf; ++f) cnt[m->u[f] + 1]++;
+    m->losortStart[0] = 0;
+    for (int c = 0; c < n; ++c) m->losortStart[c + 1] = m->losortStart[c] + cnt[c + 1];
+    memset(cnt, 0, sizeof(int) * (n + 1));
+    for (int f = 0; f < nf; ++f) {
+        const int c = m->u[f];
+        m->losort[m->losortStart[c] + cnt[c]++] = f;
+    }
+    for (int c = 0; c <= n; ++c) m->ownerStart[c] = nf;
+    m->ownerStart[0] = 0;
+    int nOwnStart = 0, i = 1;
+    for (int f = 0; f < nf; ++f) {
+        const int curOwn = m->l[f];
+        if (curOwn > nOwnStart) {
+            while (i <= curOwn) m->ownerStart[i++] = f;
+            nOwnStart = curOwn;
+        }
+    }
+    free(cnt);
+    return 0;
+}
+
+void ldu_free_addr(ldu_matrix* m) {
+    free(m->ownerStart);
+    free(m->losort);
+    free(m->losortStart);
+    m->ownerStart = m->losort = m->losortStart = NULL;
+}
+
+static const double* lowerOf(const ldu_matrix* m) { return m->lower ? m->lower : m->upper; }
+
+/* ------------------------------------------------------------- matrix ops */
+
+/* lduMatrix::Amul, lduMatrixATmul.C:34-92 (no interfaces) */
+void ldu_amul(const ldu_matrix* m, const double* x, double* y) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) y[c] = m->diag[c] * x[c];
+    for (int f = 0; f < m->nFaces; ++f) {
+        y[m->u[f]] += lo[f] * x[m->l[f]];
+        y[m->l[f]] += m->upper[f] * x[m->u[f]];
+    }
+}
+
+/* lduMatrix::Tmul, lduMatrixATmul.C:95-151 */
+void ldu_tmul(const ldu_matrix* m, const double* x, double* y) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) y[c] = m->diag[c] * x[c];
+    for (int f = 0; f < m->nFaces; ++f) {
+        y[m->u[f]] += m->upper[f] * x[m->l[f]];
+        y[m->l[f]] += lo[f] * x[m->u[f]];
+    }
+}
+
+/* lduMatrix::sumA, lduMatrixATmul.C:154-200 */
+void ldu_sumA(const ldu_matrix* m, double* s) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) s[c] = m->diag[c];
+    for (int f = 0; f < m->nFaces; ++f) {
+        s[m->u[f]] += lo[f];
+        s[m->l[f]] += m->upper[f];
+    }
+}
+
+/* lduMatrix::residual, lduMatrixATmul.C:203-280 */
+void ldu_residual(const ldu_matrix* m, const double* x, const double* b, double* r) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) r[c] = b[c] - m->diag[c] * x[c];
+    for (int f = 0; f < m->nFaces; ++f) {
+        r[m->u[f]] -= lo[f] * x[m->l[f]];
+        r[m->l[f]] -= m->upper[f] * x[m->u[f]];
+    }
+}
+
+/* ------------------------------------------------------------- reductions */
+/* FieldReductionFunctions.C: sequential sums in index order (serial reduce is
+ * a no-op, src/Pstream/dummy/UPstream.C). */
+double ldu_sum(int n, const double* a) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += a[i];
+    return s;
+}
+double ldu_sum_mag(int n, const double* a) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += fabs(a[i]);
+    return s;
+}
+double ldu_sum_sqr(int n, const double* a) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += a[i] * a[i];
+    return s;
+}
+double ldu_sum_prod(int n, const double* a, const double* b) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+/* gAverage, FieldReductionFunctions.C:334-357 */
+double ldu_average(int n, const double* a) { return n > 0 ? ldu_sum(n, a) / n : 0.0; }
+
+/* lduMatrix::solver::normFactor, lduMatrixSolver.C:174-197 */
+double ldu_norm_factor(const ldu_matrix* m, const double* psi, const double* b,
+                       const double* Apsi, double* tmp) {
+    const int n = m->nCells;
+    ldu_sumA(m, tmp);
+    const double avg = ldu_average(n, psi);
+    for (int i = 0; i < n; ++i) tmp[i] *= avg;
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += fabs(Apsi[i] - tmp[i]) + fabs(b[i] - tmp[i]);
+    return s + SP_SMALL;
+}
+
+/* --------------------------------------------------------- preconditioners */
+
+/* DICPreconditioner::calcReciprocalD, DICPreconditioner.C:57-84 (rD = diag on entry
+ * in the reference ctor, :40-54) */
+void ldu_dic_rD(const ldu_matrix* m, double* rD) {
+    for (int c = 0; c < m->nCells; ++c) rD[c] = m->diag[c];
+    for (int f = 0; f < m->nFaces; ++f)
+        rD[m->u[f]] -= m->upper[f] * m->upper[f] / rD[m->l[f]];
+    for (int c = 0; c < m->nCells; ++c) rD[c] = 1.0 / rD[c];
+}
+
+/* DICPreconditioner::precondition, DICPreconditioner.C:87-123 */
+void ldu_dic_precondition(const ldu_matrix* m, const double* rD, const double* r, double* w) {
+    for (int c = 0; c < m->nCells; ++c) w[c] = rD[c] * r[c];
+    for (int f = 0; f < m->nFaces; ++f)
+        w[m->u[f]] -= rD[m->u[f]] * m->upper[f] * w[m->l[f]];
+    for (int f = m->nFaces - 1; f >= 0; --f)
+        w[m->l[f]] -= rD[m->l[f]] * m->upper[f] * w[m->u[f]];
+}
+
+/* DILUPreconditioner::calcReciprocalD, DILUPreconditioner.C:57-85 */
+void ldu_dilu_rD(const ldu_matrix* m, double* rD) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) rD[c] = m->diag[c];
+    for (int f = 0; f < m->nFaces; ++f)
+        rD[m->u[f]] -= m->upper[f] * lo[f] / rD[m->l[f]];
+    for (int c = 0; c < m->nCells; ++c) rD[c] = 1.0 / rD[c];
+}
+
+/* DILUPreconditioner::precondition, DILUPreconditioner.C:88-135 */
+void ldu_dilu_precondition(const ldu_matrix* m, const double* rD, const double* r, double* w) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) w[c] = rD[c] * r[c];
+    for (int k = 0; k < m->nFaces; ++k) {
+        const int f = m->losort[k];
+        w[m->u[f]] -= rD[m->u[f]] * lo[f] * w[m->l[f]];
+    }
+    for (int f = m->nFaces - 1; f >= 0; --f)
+        w[m->l[f]] -= rD[m->l[f]] * m->upper[f] * w[m->u[f]];
+}
+
+/* DILUPreconditioner::preconditionT, DILUPreconditioner.C:138-185 */
+void ldu_dilu_preconditionT(const ldu_matrix* m, const double* rD, const double* r, double* w) {
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < m->nCells; ++c) w[c] = rD[c] * r[c];
+    for (int f = 0; f < m->nFaces; ++f)
+        w[m->u[f]] -= rD[m->u[f]] * m->upper[f] * w[m->l[f]];
+    for (int k = m->nFaces - 1; k >= 0; --k) {
+        const int f = m->losort[k];
+        w[m->l[f]] -= rD[m->l[f]] * lo[f] * w[m->u[f]];
+    }
+}
+
+typedef struct {
+    int kind;
+    double* rD;
+} precon;
+
+static void precon_init(precon* p, const ldu_matrix* m, int kind) {
+    p->kind = kind;
+    p->rD = NULL;
+    if (kind == LDU_PRE_NONE) return;
+    p->rD = (double*)xmalloc(sizeof(double) * m->nCells);
+    if (kind == LDU_PRE_DIAGONAL) {
+        /* diagonalPreconditioner.C ctor: rD = 1/diag */
+        for (int c = 0; c < m->nCells; ++c) p->rD[c] = 1.0 / m->diag[c];
+    } else if (kind == LDU_PRE_DIC) {
+        ldu_dic_rD(m, p->rD);
+    } else {
+        ldu_dilu_rD(m, p->rD);
+    }
+}
+
+static void precon_apply(const precon* p, const ldu_matrix* m, double* w, const double* r) {
+    switch (p->kind) {
+        case LDU_PRE_NONE:
+            memcpy(w, r, sizeof(double) * m->nCells);
+            break;
+        case LDU_PRE_DIAGONAL:
+            for (int c = 0; c < m->nCells; ++c) w[c] = p->rD[c] * r[c];
+            break;
+        case LDU_PRE_DIC:
+            ldu_dic_precondition(m, p->rD, r, w);
+            break;
+        default:
+            ldu_dilu_precondition(m, p->rD, r, w);
+            break;
+    }
+}
+
+/* --------------------------------------------------------------- smoothers */
+
+/* GaussSeidelSmoother::smooth, GaussSeidelSmoother.C:66-187 (no interfaces) */
+void ldu_gs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweeps) {
+    const int n = m->nCells;
+    const double* lo = lowerOf(m);
+    double* bPrime = (double*)xmalloc(sizeof(double) * n);
+    for (int sweep = 0; sweep < nSweeps; ++sweep) {
+        memcpy(bPrime, b, sizeof(double) * n);
+        int fEnd = m->ownerStart[0];
+        for (int c = 0; c < n; ++c) {
+            const int fStart = fEnd;
+            fEnd = m->ownerStart[c + 1];
+            double psii = bPrime[c];
+            for (int f = fStart; f < fEnd; ++f) psii -= m->upper[f] * psi[m->u[f]];
+            psii /= m->diag[c];
+            for (int f = fStart; f < fEnd; ++f) bPrime[m->u[f]] -= lo[f] * psii;
+            psi[c] = psii;
+        }
+    }
+    free(bPrime);
+}
+
+/* DICSmoother::smooth, DICSmoother.C:67-116 */
+void ldu_dic_smooth(const ldu_matrix* m, const double* rD, double* psi, const double* b, int nSweeps) {
+    const int n = m->nCells;
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    for (int sweep = 0; sweep < nSweeps; ++sweep) {
+        ldu_residual(m, psi, b, rA);
+        for (int c = 0; c < n; ++c) rA[c] *= rD[c];
+        for (int f = 0; f < m->nFaces; ++f) {
+            const int u = m->u[f];
+            rA[u] -= rD[u] * m->upper[f] * rA[m->l[f]];
+        }
+        for (int f = m->nFaces - 1; f >= 0; --f) {
+            const int l = m->l[f];
+            rA[l] -= rD[l] * m->upper[f] * rA[m->u[f]];
+        }
+        for (int c = 0; c < n; ++c) psi[c] += rA[c];
+    }
+    free(rA);
+}
+
+/* ----------------------------------------------------------------- solvers */
+
+/* SolverPerformance::checkConvergence, SolverPerformance.C:60-92 */
+static int check_convergence(ldu_perf* p, const ldu_controls* c) {
+    p->converged = (p->finalResidual < c->tolerance ||
+                    (c->relTol > SP_SMALL && p->finalResidual < c->relTol * p->initialResidual));
+    return p->converged;
+}
+
+/* SolverPerformance::checkSingularity, SolverPerformance.C:32-44 */
+static int check_singularity(ldu_perf* p, double v) {
+    p->singular = v < VSMALL;
+    return p->singular;
+}
+
+/* PCG::solve, PCG.C:65-193 */
+int ldu_pcg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
+            int precond, ldu_perf* perf) {
+    const int n = m->nCells;
+    double* pA = (double*)xmalloc(sizeof(double) * n);
+    double* wA = (double*)xmalloc(sizeof(double) * n);
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    memset(perf, 0, sizeof(*perf));
+    double wArA = SP_GREAT, wArAold = wArA;
+    ldu_amul(m, psi, wA);
+    for (int i = 0; i < n; ++i) rA[i] = b[i] - wA[i];
+    const double normFactor = ldu_norm_factor(m, psi, b, wA, pA);
+    perf->initialResidual = ldu_sum_mag(n, rA) / normFactor;
+    perf->finalResidual = perf->initialResidual;
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        precon P;
+        precon_init(&P, m, precond);
+        do {
+            wArAold = wArA;
+            precon_apply(&P, m, wA, rA);
+            wArA = ldu_sum_prod(n, wA, rA);
+            if (perf->nIterations == 0) {
+                for (int i = 0; i < n; ++i) pA[i] = wA[i];
+            } else {
+                const double beta = wArA / wArAold;
+                for (int i = 0; i < n; ++i) pA[i] = wA[i] + beta * pA[i];
+            }
+            ldu_amul(m, pA, wA);
+            const double wApA = ldu_sum_prod(n, wA, pA);
+            if (check_singularity(perf, fabs(wApA) / normFactor)) break;
+            const double alpha = wArA / wApA;
+            for (int i = 0; i < n; ++i) {
+                psi[i] += alpha * pA[i];
+                rA[i] -= alpha * wA[i];
+            }
+            perf->finalResidual = ldu_sum_mag(n, rA) / normFactor;
+        } while ((++perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        free(P.rD);
+    }
+    free(pA);
+    free(wA);
+    free(rA);
+    return 0;
+}
+
+/* PBiCGStab::solve, PBiCGStab.C:68-254 */
+int ldu_pbicgstab(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
+                  int precond, ldu_perf* perf) {
+    const int n = m->nCells;
+    double* pA = (double*)xmalloc(sizeof(double) * n);
+    double* yA = (double*)xmalloc(sizeof(double) * n);
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    memset(perf, 0, sizeof(*perf));
+    ldu_amul(m, psi, yA);
+    for (int i = 0; i < n; ++i) rA[i] = b[i] - yA[i];
+    const double normFactor = ldu_norm_factor(m, psi, b, yA, pA);
+    perf->initialResidual = ldu_sum_mag(n, rA) / normFactor;
+    perf->finalResidual = perf->initialResidual;
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        double* AyA = (double*)xmalloc(sizeof(double) * n);
+        double* sA = (double*)xmalloc(sizeof(double) * n);
+        double* zA = (double*)xmalloc(sizeof(double) * n);
+        double* tA = (double*)xmalloc(sizeof(double) * n);
+        double* rA0 = (double*)xmalloc(sizeof(double) * n);
+        memcpy(rA0, rA, sizeof(double) * n);
+        double rA0rA = 0, alpha = 0, omega = 0;
+        precon P;
+        precon_init(&P, m, precond);
+        do {
+            const double rA0rAold = rA0rA;
+            rA0rA = ldu_sum_prod(n, rA0, rA);
+            if (check_singularity(perf, fabs(rA0rA))) break;
+            if (perf->nIterations == 0) {
+                for (int i = 0; i < n; ++i) pA[i] = rA[i];
+            } else {
+                if (check_singularity(perf, fabs(omega))) break;
+                const double beta = (rA0rA / rA0rAold) * (alpha / omega);
+                for (int i = 0; i < n; ++i) pA[i] = rA[i] + beta * (pA[i] - omega * AyA[i]);
+            }
+            precon_apply(&P, m, yA, pA);
+            ldu_amul(m, yA, AyA);
+            const double rA0AyA = ldu_sum_prod(n, rA0, AyA);
+            alpha = rA0rA / rA0AyA;
+            for (int i = 0; i < n; ++i) sA[i] = rA[i] - alpha * AyA[i];
+            perf->finalResidual = ldu_sum_mag(n, sA) / normFactor;
+            if (++perf->nIterations >= c->minIter && check_convergence(perf, c)) {
+                for (int i = 0; i < n; ++i) psi[i] += alpha * yA[i];
+                break;
+            }
+            precon_apply(&P, m, zA, sA);
+            ldu_amul(m, zA, tA);
+            const double tAtA = ldu_sum_sqr(n, tA);
+            omega = ldu_sum_prod(n, tA, sA) / tAtA;
+            for (int i = 0; i < n; ++i) {
+                psi[i] += alpha * yA[i] + omega * zA[i];
+                rA[i] = sA[i] - omega * tA[i];
+            }
+            perf->finalResidual = ldu_sum_mag(n, rA) / normFactor;
+        } while ((perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        free(P.rD);
+        free(AyA);
+        free(sA);
+        free(zA);
+        free(tA);
+        free(rA0);
+    }
+    free(pA);
+    free(yA);
+    free(rA);
+    return 0;
+}
+
+/* ------------------------------------------------------------ agglomeration */
+
+/* pairGAMGAgglomeration::agglomerate (one level), pairGAMGAgglomerate.C:123-301 */
+int ldu_pair_agglomerate(int nFine, int nFaces, const int* l, const int* u,
+                         const double* w, int* forward, int* map) {
+    int* off = (int*)calloc(nFine + 1, sizeof(int));
+    int* cnt = (int*)calloc(nFine + 1, sizeof(int));
+    int* cellFaces = (int*)xmalloc(sizeof(int) * 2 * (size_t)nFaces);
+    for (int f = 0; f < nFaces; ++f) cnt[u[f]]++;
+    for (int f = 0; f < nFaces; ++f) cnt[l[f]]++;
+    off[0] = 0;
+    for (int c = 0; c < nFine; ++c) off[c + 1] = off[c] + cnt[c];
+    memset(cnt, 0, sizeof(int) * (nFine + 1));
+    for (int f = 0; f < nFaces; ++f) cellFaces[off[u[f]] + cnt[u[f]]++] = f;
+    for (int f = 0; f < nFaces; ++f) cellFaces[off[l[f]] + cnt[l[f]]++] = f;
+
+    for (int c = 0; c < nFine; ++c) map[c] = -1;
+    int nCoarse = 0;
+    const int fwd = *forward;
+    for (int cf = 0; cf < nFine; ++cf) {
+        const int c = fwd ? cf : nFine - cf - 1;
+        if (map[c] >= 0) continue;
+        int match = -1;
+        double maxW = -GREAT;
+        for (int k = off[c]; k < off[c + 1]; ++k) {
+            const int f = cellFaces[k];
+            if (map[u[f]] < 0 && map[l[f]] < 0 && w[f] > maxW) {
+                match = f;
+                maxW = w[f];
+            }
+        }
+        if (match >= 0) {
+            map[u[match]] = nCoarse;
+            map[l[match]] = nCoarse;
+            nCoarse++;
+        } else {
+            int cmatch = -1;
+            double cmax = -GREAT;
+            for (int k = off[c]; k < off[c + 1]; ++k) {
+                const int f = cellFaces[k];
+                if (w[f] > cmax) {
+                    cmatch = f;
+                    cmax = w[f];
+                }
+            }
+            if (cmatch >= 0) {
+                const int a = map[u[cmatch]], b = map[l[cmatch]];
+                map[c] = a > b ? a : b;
+            }
+        }
+    }
+    for (int cf = 0; cf < nFine; ++cf) {
+        const int c = fwd ? cf : nFine - cf - 1;
+        if (map[c] < 0) map[c] = nCoarse++;
+    }
+    if (!fwd) {
+        nCoarse--;
+        for (int c = 0; c < nFine; ++c) map[c] = nCoarse - map[c];
+        nCoarse++;
+    }
+    *forward = !fwd;
+    free(off);
+    free(cnt);
+    free(cellFaces);
+    return nCoarse;
+}
+
+/* GAMGAgglomeration::agglomerateLduAddressing, GAMGAgglomerateLduAddressing.C:32-222 */
+int ldu_agglomerate_addressing(int nCells, int nFaces, const int* l, const int* u,
+                               const int* rm, int nCoarse, int* cl, int* cu,
+                               int* fra, int* flip) {
+    (void)nCells;
+    int maxNnbrs = 10;
+    int* cCellnFaces = (int*)calloc(nCoarse, sizeof(int));
+    int* cCellFaces = (int*)xmalloc(sizeof(int) * (size_t)maxNnbrs * nCoarse);
+    int* initNeighb = (int*)xmalloc(sizeof(int) * nFaces);
+    int nCoarseFaces = 0;
+    for (int f = 0; f < nFaces; ++f) {
+        const int rU = rm[u[f]], rL = rm[l[f]];
+        if (rU == rL) {
+            fra[f] = -(rU + 1);
+            continue;
+        }
+        int cOwn = rU, cNei = rL;
+        if (rU > rL) {
+            cOwn = rL;
+            cNei = rU;
+        }
+        int* cc = &cCellFaces[(size_t)maxNnbrs * cOwn];
+        int found = 0;
+        for (int i = 0; i < cCellnFaces[cOwn]; ++i) {
+            if (initNeighb[cc[i]] == cNei) {
+                found = 1;
+                fra[f] = cc[i];
+                break;
+            }
+        }
+        if (!found) {
+            if (cCellnFaces[cOwn] >= maxNnbrs) {
+                const int oldMax = maxNnbrs;
+                maxNnbrs *= 2;
+                int* grown = (int*)xmalloc(sizeof(int) * (size_t)maxNnbrs * nCoarse);
+                for (int i = 0; i < nCoarse; ++i)
+                    for (int j = 0; j < cCellnFaces[i]; ++j)
+                        grown[(size_t)maxNnbrs * i + j] = cCellFaces[(size_t)oldMax * i + j];
+                free(cCellFaces);
+                cCellFaces = grown;
+                cc = &cCellFaces[(size_t)maxNnbrs * cOwn];
+            }
+            cc[cCellnFaces[cOwn]] = nCoarseFaces;
+            initNeighb[nCoarseFaces] = cNei;
+            fra[f] = nCoarseFaces;
+            cCellnFaces[cOwn]++;
+            nCoarseFaces++;
+        }
+    }
+    /* renumber into upper-triangular order */
+    int* coarseFaceMap = (int*)xmalloc(sizeof(int) * (nCoarseFaces ? nCoarseFaces : 1));
+    int cf = 0;
+    for (int cc = 0; cc < nCoarse; ++cc) {
+        const int* faces = &cCellFaces[(size_t)maxNnbrs * cc];
+        for (int i = 0; i < cCellnFaces[cc]; ++i) {
+            cl[cf] = cc;
+            cu[cf] = initNeighb[faces[i]];
+            coarseFaceMap[faces[i]] = cf;
+            cf++;
+        }
+    }
+    for (int f = 0; f < nFaces; ++f)
+        if (fra[f] >= 0) fra[f] = coarseFaceMap[fra[f]];
+    for (int f = 0; f < nFaces; ++f) {
+        flip[f] = 0;
+        const int c = fra[f];
+        if (c >= 0) {
+            const int rU = rm[u[f]], rL = rm[l[f]];
+            if (cl[c] == rU && cu[c] == rL) flip[f] = 1;
+        }
+    }
+    free(cCellnFaces);
+    free(cCellFaces);
+    free(initNeighb);
+    free(coarseFaceMap);
+    return nCoarseFaces;
+}
+
+/* faceAreaPairGAMGAgglomeration.C:55-80: mag(cmptMultiply(Sf/sqrt(magSf), (1,1.01,1.02)))
+ * with magSf = max(mag(Sf), rootVSmall) (primitiveMeshFaceCentresAndAreas.C:93). */
+void ldu_face_area_pair_weights(int nFaces, const double* Sf, double* w) {
+    const double rootVSmall = sqrt(DBL_MIN);
+    for (int f = 0; f < nFaces; ++f) {
+        const double x = Sf[3 * f], y = Sf[3 * f + 1], z = Sf[3 * f + 2];
+        double m = sqrt(x * x + y * y + z * z);
+        if (m < rootVSmall) m = rootVSmall;
+        const double s = sqrt(m);
+        const double a = (x / s) * 1.0, b = (y / s) * 1.01, c = (z / s) * 1.02;
+        w[f] = sqrt(a * a + b * b + c * c);
+    }
+}
+
+/* pairGAMGAgglomeration::agglomerate(mesh, weights), pairGAMGAgglomerate.C:31-118,
+ * with continueAgglomerating (GAMGAgglomeration.C:205-230) and restrictFaceField
+ * (GAMGAgglomerationTemplates.C:138-167). */
+int ldu_gamg_agglomerate(int nCells, int nFaces, const int* l, const int* u,
+                         const double* weights, int nCellsInCoarsestLevel, int forwardStart,
+                         ldu_agglomeration* agg) {
+    memset(agg, 0, sizeof(*agg));
+    const int maxLevels = 50;
+    int forward = forwardStart;
+    int fn = nCells, fnf = nFaces;
+    const int *fl = l, *fu = u;
+    double* fw = (double*)xmalloc(sizeof(double) * nFaces);
+    memcpy(fw, weights, sizeof(double) * nFaces);
+    int nCreated = 0;
+    while (nCreated < maxLevels - 1) {
+        int* map = (int*)xmalloc(sizeof(int) * fn);
+        const int nCoarse = ldu_pair_agglomerate(fn, fnf, fl, fu, fw, &forward, map);
+        if (!(nCoarse >= nCellsInCoarsestLevel && nCoarse < fn)) {
+            free(map);
+            break;
+        }
+        int* cl = (int*)xmalloc(sizeof(int) * (fnf ? fnf : 1));
+        int* cu = (int*)xmalloc(sizeof(int) * (fnf ? fnf : 1));
+        int* fra = (int*)xmalloc(sizeof(int) * (fnf ? fnf : 1));
+        int* flip = (int*)xmalloc(sizeof(int) * (fnf ? fnf : 1));
+        const int ncf = ldu_agglomerate_addressing(fn, fnf, fl, fu, map, nCoarse, cl, cu, fra, flip);
+        double* cw = (double*)calloc(ncf ? ncf : 1, sizeof(double));
+        for (int f = 0; f < fnf; ++f)
+            if (fra[f] >= 0) cw[fra[f]] += fw[f];
+        free(fw);
+        fw = cw;
+        agg->nCells[nCreated] = nCoarse;
+        agg->nFaces[nCreated] = ncf;
+        agg->restrictAddr[nCreated] = map;
+        agg->faceRestrict[nCreated] = fra;
+        agg->faceFlip[nCreated] = flip;
+        agg->cl[nCreated] = cl;
+        agg->cu[nCreated] = cu;
+        fn = nCoarse;
+        fnf = ncf;
+        fl = cl;
+        fu = cu;
+        nCreated++;
+    }
+    free(fw);
+    agg->nLevels = nCreated;
+    return nCreated > 0 ? 0 : -1;
+}
+
+void ldu_gamg_free(ldu_agglomeration* agg) {
+    for (int i = 0; i < agg->nLevels; ++i) {
+        free(agg->restrictAddr[i]);
+        free(agg->faceRestrict[i]);
+        free(agg->faceFlip[i]);
+        free(agg->cl[i]);
+        free(agg->cu[i]);
+    }
+    agg->nLevels = 0;
+}
+
+/* GAMGSolver::agglomerateMatrix, GAMGSolverAgglomerateMatrix.C:33-193 */
+void ldu_gamg_coarse_matrix(int nFineCells, int nFineFaces, const double* fdiag,
+                            const double* fupper, const double* flower,
+                            const int* ra, const int* fra, const int* flip,
+                            int nCoarseCells, int nCoarseFaces, double* cdiag, double* cupper,
+                            double* clower) {
+    for (int c = 0; c < nCoarseCells; ++c) cdiag[c] = 0;
+    for (int i = 0; i < nFineCells; ++i) cdiag[ra[i]] += fdiag[i];
+    for (int f = 0; f < nCoarseFaces; ++f) cupper[f] = 0;
+    if (flower) {
+        for (int f = 0; f < nCoarseFaces; ++f) clower[f] = 0;
+        for (int f = 0; f < nFineFaces; ++f) {
+            const int c = fra[f];
+            if (c >= 0) {
+                if (!flip[f]) {
+                    cupper[c] += fupper[f];
+                    clower[c] += flower[f];
+                } else {
+                    cupper[c] += flower[f];
+                    clower[c] += fupper[f];
+                }
+            } else {
+                cdiag[-1 - c] += fupper[f] + flower[f];
+            }
+        }
+    } else {
+        for (int f = 0; f < nFineFaces; ++f) {
+            const int c = fra[f];
+            if (c >= 0)
+                cupper[c] += fupper[f];
+            else
+                cdiag[-1 - c] += 2 * fupper[f];
+        }
+    }
+}
+
+/* -------------------------------------------------------------------- GAMG */
+
+void ldu_gamg_default_controls(ldu_gamg_controls* g) {
+    /* GAMGSolver.C:70-80 */
+    g->nPreSweeps = 0;
+    g->preSweepsLevelMultiplier = 1;
+    g->maxPreSweeps = 4;
+    g->nPostSweeps = 2;
+    g->postSweepsLevelMultiplier = 1;
+    g->maxPostSweeps = 4;
+    g->nFinestSweeps = 2;
+    g->scaleCorrection = -1;
+    g->smoother = LDU_SMOOTH_GS;
+}
+
+typedef struct {
+    ldu_matrix m;
+    double* diag;
+    double* upper;
+    double* lower;
+    double* rD; /* DIC smoother */
+} level_matrix;
+
+static void smooth(const ldu_matrix* m, const double* rD, int kind, double* psi, const double* b, int n) {
+    if (kind == LDU_SMOOTH_DIC)
+        ldu_dic_smooth(m, rD, psi, b, n);
+    else
+        ldu_gs_smooth(m, psi, b, n);
+}
+
+/* GAMGSolver::scale, GAMGSolverScale.C:31-76 */
+static void gamg_scale(const ldu_matrix* A, double* field, double* Acf, const double* source) {
+    const int n = A->nCells;
+    ldu_amul(A, field, Acf);
+    double num = 0, den = 0;
+    for (int i = 0; i < n; ++i) {
+        num += source[i] * field[i];
+        den += Acf[i] * field[i];
+    }
+    /* stabilise(den, vSmall), src/OpenFOAM/primitives/Scalar/Scalar.H:367-377 */
+    const double st = den >= 0 ? den + VSMALL : den - VSMALL;
+    const double sf = num / st;
+    for (int i = 0; i < n; ++i) field[i] = sf * field[i] + (source[i] - sf * Acf[i]) / A->diag[i];
+}
+
+static int imin(int a, int b) { return a < b ? a : b; }
+
+/* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
+ * GAMGSolverSolve.C:31-552 (interpolateCorrection off, no interfaces). */
+int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
+             const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
+    const int n = m->nCells;
+    const int nl = agg->nLevels;
+    if (nl < 1) return -1;
+    const int sym = m->lower == NULL;
+    const int scaleCorrection = gc->scaleCorrection < 0 ? sym : gc->scaleCorrection;
+    memset(perf, 0, sizeof(*perf));
+
+    /* coarse matrices (GAMGSolver ctor, GAMGSolver.C:204-206) */
+    level_matrix* lv = (level_matrix*)calloc(nl, sizeof(level_matrix));
+    const ldu_matrix* fine = m;
+    int maxSize = n;
+    for (int i = 0; i < nl; ++i) {
+        const int nc = agg->nCells[i], ncf = agg->nFaces[i];
+        if (nc > maxSize) maxSize = nc;
+        lv[i].diag = (double*)xmalloc(sizeof(double) * nc);
+        lv[i].upper = (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
+        lv[i].lower = sym ? NULL : (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
+        ldu_gamg_coarse_matrix(fine->nCells, fine->nFaces, fine->diag, fine->upper,
+                               sym ? NULL : fine->lower, agg->restrictAddr[i], agg->faceRestrict[i],
+                               agg->faceFlip[i], nc, ncf, lv[i].diag, lv[i].upper, lv[i].lower);
+        lv[i].m.nCells = nc;
+        lv[i].m.nFaces = ncf;
+        lv[i].m.l = agg->cl[i];
+        lv[i].m.u = agg->cu[i];
+        lv[i].m.diag = lv[i].diag;
+        lv[i].m.upper = lv[i].upper;
+        lv[i].m.lower = lv[i].lower;
+        ldu_init_addr(&lv[i].m);
+        fine = &lv[i].m;
+    }
+    const int coarsest = nl - 1;
+
+    double* Apsi = (double*)xmalloc(sizeof(double) * maxSize);
+    double* finestCorrection = (double*)xmalloc(sizeof(double) * maxSize);
+    double* finestResidual = (double*)xmalloc(sizeof(double) * n);
+    ldu_amul(m, psi, Apsi);
+    const double normFactor = ldu_norm_factor(m, psi, b, Apsi, finestCorrection);
+    for (int i = 0; i < n; ++i) finestResidual[i] = b[i] - Apsi[i];
+    perf->initialResidual = ldu_sum_mag(n, finestResidual) / normFactor;
+    perf->finalResidual = perf->initialResidual;
+
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        /* initVcycle, GAMGSolverSolve.C:446-517 */
+        double** corr = (double**)calloc(nl, sizeof(double*));
+        double** src = (double**)calloc(nl, sizeof(double*));
+        double* rD0 = NULL;
+        if (gc->smoother == LDU_SMOOTH_DIC) {
+            rD0 = (double*)xmalloc(sizeof(double) * n);
+            ldu_dic_rD(m, rD0);
+        }
+        for (int i = 0; i < nl; ++i) {
+            corr[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
+            src[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
+            if (gc->smoother == LDU_SMOOTH_DIC) {
+                lv[i].rD = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
+                ldu_dic_rD(&lv[i].m, lv[i].rD);
+            }
+        }
+        ldu_controls cc = {c->tolerance, c->relTol, 1000, 0};
+        do {
+            /* Vcycle, GAMGSolverSolve.C:148-443 */
+            double* scratch1 = Apsi;
+            double* scratch2 = finestCorrection;
+            /* restrictField(coarseSources[0], finestResidual, 0) */
+            for (int k = 0; k < agg->nCells[0]; ++k) src[0][k] = 0;
+            for (int k = 0; k < n; ++k) src[0][agg->restrictAddr[0][k]] += finestResidual[k];
+            for (int li = 0; li < coarsest; ++li) {
+                const int nc = agg->nCells[li];
+                if (gc->nPreSweeps) {
+                    for (int k = 0; k < nc; ++k) corr[li][k] = 0;
+                    smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
+                           imin(gc->nPreSweeps + gc->preSweepsLevelMultiplier * li, gc->maxPreSweeps));
+                    if (scaleCorrection && li < coarsest - 1)
+                        gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
+                    ldu_amul(&lv[li].m, corr[li], scratch1);
+                    for (int k = 0; k < nc; ++k) src[li][k] -= scratch1[k];
+                }
+                const int nn = agg->nCells[li + 1];
+                for (int k = 0; k < nn; ++k) src[li + 1][k] = 0;
+                for (int k = 0; k < nc; ++k) src[li + 1][agg->restrictAddr[li + 1][k]] += src[li][k];
+            }
+            /* solveCoarsestLevel, GAMGSolverSolve.C:520-552 */
+            {
+                ldu_perf cp;
+                for (int k = 0; k < agg->nCells[coarsest]; ++k) corr[coarsest][k] = 0;
+                if (sym)
+                    ldu_pcg(&lv[coarsest].m, corr[coarsest], src[coarsest], &cc, LDU_PRE_DIC, &cp);
+                else
+                    ldu_pbicgstab(&lv[coarsest].m, corr[coarsest], src[coarsest], &cc, LDU_PRE_DILU, &cp);
+            }
+            for (int li = coarsest - 1; li >= 0; --li) {
+                const int nc = agg->nCells[li];
+                double* pre = scratch2;
+                if (gc->nPreSweeps) memcpy(pre, corr[li], sizeof(double) * nc);
+                for (int k = 0; k < nc; ++k) corr[li][k] = corr[li + 1][agg->restrictAddr[li + 1][k]];
+                if (scaleCorrection && li < coarsest - 1)
+                    gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
+                if (gc->nPreSweeps)
+                    for (int k = 0; k < nc; ++k) corr[li][k] += pre[k];
+                smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
+                       imin(gc->nPostSweeps + gc->postSweepsLevelMultiplier * li, gc->maxPostSweeps));
+            }
+            for (int k = 0; k < n; ++k) finestCorrection[k] = corr[0][agg->restrictAddr[0][k]];
+            if (scaleCorrection) gamg_scale(m, finestCorrection, Apsi, finestResidual);
+            for (int k = 0; k < n; ++k) psi[k] += finestCorrection[k];
+            smooth(m, rD0, gc->smoother, psi, b, gc->nFinestSweeps);
+
+            ldu_amul(m, psi, Apsi);
+            for (int k = 0; k < n; ++k) finestResidual[k] = b[k] - Apsi[k];
+            perf->finalResidual = ldu_sum_mag(n, finestResidual) / normFactor;
+        } while ((++perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        for (int i = 0; i < nl; ++i) {
+            free(corr[i]);
+            free(src[i]);
+            free(lv[i].rD);
+        }
+        free(corr);
+        free(src);
+        free(rD0);
+    }
+    for (int i = 0; i < nl; ++i) {
+        free(lv[i].diag);
+        free(lv[i].upper);
+        free(lv[i].lower);
+        ldu_free_addr(&lv[i].m);
+    }
+    free(lv);
+    free(Apsi);
+    free(finestCorrection);
+    free(finestResidual);
+    return 0;
+}

@@ -1,0 +1,141 @@
+/*
+ * ldu_oracle.h - CPU restatement of OpenFOAM-dev's lduMatrix solver path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA solver library is
+ * compared against; nothing in the product links or calls it.  Each function
+ * follows the reference loop it cites (file:line relative to the OpenFOAM-dev
+ * tree) with the same operation order, so that compiled with
+ * -ffp-contract=off it reproduces the reference's x86-64 build bit for bit.
+ * It is pinned against the reference itself (oracle/_ref, built from source
+ * by oracle/build_ref.py) through the golden vectors in tests/golden/.
+ *
+ * Labels are int32 (WM_LABEL_SIZE=32), scalars double (WM_DP).
+ */
+#ifndef LDU_ORACLE_H
+#define LDU_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int nCells, nFaces;
+    const int *l, *u;            /* lowerAddr, upperAddr */
+    const double *diag, *upper;  /* lower == NULL -> symmetric */
+    const double *lower;
+    int *ownerStart;             /* [nCells+1] */
+    int *losort;                 /* [nFaces] */
+    int *losortStart;            /* [nCells+1] */
+} ldu_matrix;
+
+typedef struct {
+    double initialResidual, finalResidual;
+    int nIterations, converged, singular;
+} ldu_perf;
+
+typedef struct {
+    double tolerance, relTol;
+    int maxIter, minIter;
+} ldu_controls;
+
+/* lduAddressing.C:32-170 (losort, ownerStart, losortStart).  Allocates the
+ * three derived arrays inside m; release with ldu_free_addr. */
+int ldu_init_addr(ldu_matrix* m);
+void ldu_free_addr(ldu_matrix* m);
+
+/* lduMatrixATmul.C */
+void ldu_amul(const ldu_matrix* m, const double* x, double* y);
+void ldu_tmul(const ldu_matrix* m, const double* x, double* y);
+void ldu_sumA(const ldu_matrix* m, double* s);
+void ldu_residual(const ldu_matrix* m, const double* x, const double* b, double* r);
+
+/* FieldReductionFunctions.C */
+double ldu_sum(int n, const double* a);
+double ldu_sum_mag(int n, const double* a);
+double ldu_sum_sqr(int n, const double* a);
+double ldu_sum_prod(int n, const double* a, const double* b);
+double ldu_average(int n, const double* a);
+
+/* lduMatrixSolver.C:174-197 */
+double ldu_norm_factor(const ldu_matrix* m, const double* psi, const double* b,
+                       const double* Apsi, double* tmp);
+
+/* Preconditioners: 0 none, 1 diagonal, 2 DIC, 3 DILU */
+enum { LDU_PRE_NONE = 0, LDU_PRE_DIAGONAL = 1, LDU_PRE_DIC = 2, LDU_PRE_DILU = 3 };
+void ldu_dic_rD(const ldu_matrix* m, double* rD);
+void ldu_dic_precondition(const ldu_matrix* m, const double* rD, const double* r, double* w);
+void ldu_dilu_rD(const ldu_matrix* m, double* rD);
+void ldu_dilu_precondition(const ldu_matrix* m, const double* rD, const double* r, double* w);
+void ldu_dilu_preconditionT(const ldu_matrix* m, const double* rD, const double* r, double* w);
+
+/* Smoothers: 0 GaussSeidel, 1 DIC */
+enum { LDU_SMOOTH_GS = 0, LDU_SMOOTH_DIC = 1 };
+void ldu_gs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweeps);
+void ldu_dic_smooth(const ldu_matrix* m, const double* rD, double* psi, const double* b, int nSweeps);
+
+/* PCG.C:65-193, PBiCGStab.C:68-254.  Return 0 or a negative error. */
+int ldu_pcg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
+            int precond, ldu_perf* perf);
+int ldu_pbicgstab(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
+                  int precond, ldu_perf* perf);
+
+/* pairGAMGAgglomerate.C:123-301: one level of pairwise agglomeration.
+ * *forward is the direction flag (pairGAMGAgglomeration::forward_), toggled
+ * on return.  Returns nCoarseCells. */
+int ldu_pair_agglomerate(int nCells, int nFaces, const int* l, const int* u,
+                         const double* weights, int* forward, int* restrictMap);
+
+/* GAMGAgglomerateLduAddressing.C:32-197: coarse l/u, faceRestrictAddr and
+ * faceFlipMap of one level.  cl/cu must hold nFaces entries.  Returns
+ * nCoarseFaces. */
+int ldu_agglomerate_addressing(int nCells, int nFaces, const int* l, const int* u,
+                               const int* restrictMap, int nCoarseCells, int* cl, int* cu,
+                               int* faceRestrict, int* faceFlip);
+
+/* GAMG agglomeration hierarchy (pairGAMGAgglomerate.C:31-118 with
+ * mergeLevels 1, GAMGAgglomeration.C:205-230 stop rule, maxLevels 50). */
+typedef struct {
+    int nLevels;                 /* number of coarse levels */
+    int nCells[50], nFaces[50];  /* coarse sizes per level */
+    int* restrictAddr[50];       /* [fine nCells of level i] */
+    int* faceRestrict[50];       /* [fine nFaces of level i] */
+    int* faceFlip[50];
+    int* cl[50];                 /* coarse lowerAddr [nFaces[i]] */
+    int* cu[50];
+} ldu_agglomeration;
+
+int ldu_gamg_agglomerate(int nCells, int nFaces, const int* l, const int* u,
+                         const double* weights, int nCellsInCoarsestLevel, int forwardStart,
+                         ldu_agglomeration* agg);
+void ldu_gamg_free(ldu_agglomeration* agg);
+
+/* faceAreaPairGAMGAgglomeration.C:55-80 weights from face-area vectors. */
+void ldu_face_area_pair_weights(int nFaces, const double* Sf, double* w);
+
+/* GAMGSolverAgglomerateMatrix.C:33-193: coarse diag/upper/lower of level i. */
+void ldu_gamg_coarse_matrix(int nFineCells, int nFineFaces, const double* fdiag,
+                            const double* fupper, const double* flower,
+                            const int* restrictAddr, const int* faceRestrict, const int* faceFlip,
+                            int nCoarseCells, int nCoarseFaces, double* cdiag, double* cupper,
+                            double* clower);
+
+typedef struct {
+    int nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps;
+    int nPostSweeps, postSweepsLevelMultiplier, maxPostSweeps;
+    int nFinestSweeps;
+    int scaleCorrection;  /* -1: default (= symmetric) */
+    int smoother;         /* LDU_SMOOTH_* */
+} ldu_gamg_controls;
+
+void ldu_gamg_default_controls(ldu_gamg_controls* g);
+
+/* GAMGSolverSolve.C:31-552 with GAMGSolverScale.C:31-76.  The agglomeration
+ * must have been built for m's addressing. */
+int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
+             const ldu_controls* c, const ldu_gamg_controls* g, ldu_perf* perf);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

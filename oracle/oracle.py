@@ -1,0 +1,277 @@
+"""ctypes front end of the C oracle (``oracle/_build/libldu_oracle.so``).
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA solver library.  Used by
+tests/, ``__graft_entry__.smoke()`` and bench.py's CPU baseline; never by the
+product.  Systems are dicts in the layout of ``cases.py`` (l, u, diag, upper,
+lower or None, source, Sf).
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libldu_oracle.so")
+
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+SMOOTHERS = {"GaussSeidel": 0, "DIC": 1}
+
+i32p = ctypes.POINTER(ctypes.c_int)
+f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class LduMatrix(ctypes.Structure):
+    _fields_ = [("nCells", ctypes.c_int), ("nFaces", ctypes.c_int),
+                ("l", i32p), ("u", i32p), ("diag", f64p), ("upper", f64p), ("lower", f64p),
+                ("ownerStart", i32p), ("losort", i32p), ("losortStart", i32p)]
+
+
+class LduPerf(ctypes.Structure):
+    _fields_ = [("initialResidual", ctypes.c_double), ("finalResidual", ctypes.c_double),
+                ("nIterations", ctypes.c_int), ("converged", ctypes.c_int), ("singular", ctypes.c_int)]
+
+
+class LduControls(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("relTol", ctypes.c_double),
+                ("maxIter", ctypes.c_int), ("minIter", ctypes.c_int)]
+
+
+class LduAgglomeration(ctypes.Structure):
+    _fields_ = [("nLevels", ctypes.c_int), ("nCells", ctypes.c_int * 50), ("nFaces", ctypes.c_int * 50),
+                ("restrictAddr", i32p * 50), ("faceRestrict", i32p * 50), ("faceFlip", i32p * 50),
+                ("cl", i32p * 50), ("cu", i32p * 50)]
+
+
+class LduGamgControls(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in (
+        "nPreSweeps", "preSweepsLevelMultiplier", "maxPreSweeps", "nPostSweeps",
+        "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "scaleCorrection", "smoother")]
+
+
+@dataclass
+class Perf:
+    initialResidual: float
+    finalResidual: float
+    nIterations: int
+    converged: bool
+    singular: bool
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"{LIB} missing: run `make -C oracle`")
+        _lib = ctypes.CDLL(LIB)
+        for name in ("ldu_sum", "ldu_sum_mag", "ldu_sum_sqr", "ldu_average"):
+            getattr(_lib, name).restype = ctypes.c_double
+        _lib.ldu_sum_prod.restype = ctypes.c_double
+        _lib.ldu_norm_factor.restype = ctypes.c_double
+    return _lib
+
+
+def _p(a, t=f64p):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Matrix:
+    """Holds a system's arrays and the C view (with derived addressing)."""
+
+    def __init__(self, s):
+        self.l = np.ascontiguousarray(s["l"], np.int32)
+        self.u = np.ascontiguousarray(s["u"], np.int32)
+        self.diag = np.ascontiguousarray(s["diag"], np.float64)
+        self.upper = np.ascontiguousarray(s["upper"], np.float64)
+        lo = s.get("lower")
+        self.lower = None if lo is None else np.ascontiguousarray(lo, np.float64)
+        self.c = LduMatrix(self.diag.size, self.l.size, _p(self.l, i32p), _p(self.u, i32p),
+                           _p(self.diag), _p(self.upper), _p(self.lower), None, None, None)
+        lib().ldu_init_addr(ctypes.byref(self.c))
+        self.n = self.diag.size
+
+    def __del__(self):
+        try:
+            lib().ldu_free_addr(ctypes.byref(self.c))
+        except Exception:
+            pass
+
+    def addr(self):
+        n, nf = self.n, self.l.size
+        return (np.ctypeslib.as_array(self.c.ownerStart, (n + 1,)).copy(),
+                np.ctypeslib.as_array(self.c.losort, (max(nf, 1),))[:nf].copy(),
+                np.ctypeslib.as_array(self.c.losortStart, (n + 1,)).copy())
+
+    def _vec_op(self, fn, *vecs):
+        out = np.empty(self.n)
+        args = [np.ascontiguousarray(v, np.float64) for v in vecs]
+        fn(ctypes.byref(self.c), *[_p(a) for a in args], _p(out))
+        return out
+
+    def amul(self, x):
+        return self._vec_op(lib().ldu_amul, x)
+
+    def tmul(self, x):
+        return self._vec_op(lib().ldu_tmul, x)
+
+    def residual(self, x, b):
+        return self._vec_op(lib().ldu_residual, x, b)
+
+    def sumA(self):
+        out = np.empty(self.n)
+        lib().ldu_sumA(ctypes.byref(self.c), _p(out))
+        return out
+
+    def norm_factor(self, psi, b):
+        Apsi = self.amul(psi)
+        tmp = np.empty(self.n)
+        psi = np.ascontiguousarray(psi, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        return lib().ldu_norm_factor(ctypes.byref(self.c), _p(psi), _p(b), _p(Apsi), _p(tmp))
+
+    def dic_rD(self):
+        out = np.empty(self.n)
+        lib().ldu_dic_rD(ctypes.byref(self.c), _p(out))
+        return out
+
+    def dilu_rD(self):
+        out = np.empty(self.n)
+        lib().ldu_dilu_rD(ctypes.byref(self.c), _p(out))
+        return out
+
+    def dic_precondition(self, r):
+        return self._vec_op(lib().ldu_dic_precondition, self.dic_rD(), r)
+
+    def dilu_precondition(self, r):
+        return self._vec_op(lib().ldu_dilu_precondition, self.dilu_rD(), r)
+
+    def dilu_preconditionT(self, r):
+        return self._vec_op(lib().ldu_dilu_preconditionT, self.dilu_rD(), r)
+
+    def gs_smooth(self, psi, b, n_sweeps):
+        psi = np.ascontiguousarray(psi, np.float64).copy()
+        b = np.ascontiguousarray(b, np.float64)
+        lib().ldu_gs_smooth(ctypes.byref(self.c), _p(psi), _p(b), n_sweeps)
+        return psi
+
+    def dic_smooth(self, psi, b, n_sweeps):
+        psi = np.ascontiguousarray(psi, np.float64).copy()
+        b = np.ascontiguousarray(b, np.float64)
+        rD = self.dic_rD()
+        lib().ldu_dic_smooth(ctypes.byref(self.c), _p(rD), _p(psi), _p(b), n_sweeps)
+        return psi
+
+
+def _perf(p):
+    return Perf(p.initialResidual, p.finalResidual, p.nIterations, bool(p.converged), bool(p.singular))
+
+
+def _controls(tol, rel_tol, max_iter, min_iter):
+    return LduControls(tol, rel_tol, max_iter, min_iter)
+
+
+def pcg(s, psi, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, precond="DIC"):
+    """PCG::solve; psi (float64, contiguous) is updated in place."""
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    lib().ldu_pcg(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c),
+                  PRECONDITIONERS[precond], ctypes.byref(perf))
+    return _perf(perf)
+
+
+def pbicgstab(s, psi, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, precond="DILU"):
+    """PBiCGStab::solve; psi is updated in place."""
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    lib().ldu_pbicgstab(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c),
+                        PRECONDITIONERS[precond], ctypes.byref(perf))
+    return _perf(perf)
+
+
+def face_area_pair_weights(Sf):
+    Sf = np.ascontiguousarray(Sf, np.float64).reshape(-1)
+    w = np.empty(Sf.size // 3)
+    lib().ldu_face_area_pair_weights(w.size, _p(Sf), _p(w))
+    return w
+
+
+class Agglomeration:
+    def __init__(self, s, weights=None, n_coarsest=10, forward=True):
+        if weights is None:
+            weights = face_area_pair_weights(s["Sf"])
+        self.w = np.ascontiguousarray(weights, np.float64)
+        self.l = np.ascontiguousarray(s["l"], np.int32)
+        self.u = np.ascontiguousarray(s["u"], np.int32)
+        self.c = LduAgglomeration()
+        rc = lib().ldu_gamg_agglomerate(s["diag"].size, self.l.size, _p(self.l, i32p), _p(self.u, i32p),
+                                        _p(self.w), n_coarsest, int(forward), ctypes.byref(self.c))
+        if rc != 0:
+            raise ValueError("no coarse level created")
+        self.nCellsFine = s["diag"].size
+        self.nFacesFine = self.l.size
+
+    def __del__(self):
+        try:
+            lib().ldu_gamg_free(ctypes.byref(self.c))
+        except Exception:
+            pass
+
+    @property
+    def n_levels(self):
+        return self.c.nLevels
+
+    def level(self, i):
+        """(restrictAddr, faceRestrict, faceFlip, nCells, nFaces, coarse l, coarse u)."""
+        nf_cells = self.nCellsFine if i == 0 else self.c.nCells[i - 1]
+        nf_faces = self.nFacesFine if i == 0 else self.c.nFaces[i - 1]
+        nc, ncf = self.c.nCells[i], self.c.nFaces[i]
+        A = np.ctypeslib.as_array
+        return (A(self.c.restrictAddr[i], (nf_cells,)).copy(),
+                A(self.c.faceRestrict[i], (max(nf_faces, 1),))[:nf_faces].copy(),
+                A(self.c.faceFlip[i], (max(nf_faces, 1),))[:nf_faces].copy(),
+                nc, ncf,
+                A(self.c.cl[i], (max(ncf, 1),))[:ncf].copy(),
+                A(self.c.cu[i], (max(ncf, 1),))[:ncf].copy())
+
+
+def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smoother="GaussSeidel",
+         nPreSweeps=0, nPostSweeps=2, nFinestSweeps=2, maxPreSweeps=4, maxPostSweeps=4,
+         preSweepsLevelMultiplier=1, postSweepsLevelMultiplier=1, scaleCorrection=None,
+         nCellsInCoarsestLevel=10):
+    """GAMGSolver::solve with faceAreaPair agglomeration; psi updated in place."""
+    if agg is None:
+        agg = Agglomeration(s, n_coarsest=nCellsInCoarsestLevel)
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    g = LduGamgControls(nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps, nPostSweeps,
+                        postSweepsLevelMultiplier, maxPostSweeps, nFinestSweeps,
+                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother])
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    rc = lib().ldu_gamg(ctypes.byref(m.c), ctypes.byref(agg.c), _p(psi), _p(b), ctypes.byref(c),
+                        ctypes.byref(g), ctypes.byref(perf))
+    if rc != 0:
+        raise ValueError("GAMG failed")
+    return _perf(perf)
+
+
+def coarse_matrix(fine, agg, i):
+    """Coarse (diag, upper, lower) of level i from the fine system dict."""
+    ra, fra, flip, nc, ncf, _, _ = agg.level(i)
+    cd = np.empty(nc)
+    cu = np.empty(max(ncf, 1))
+    lo = fine.get("lower")
+    cl = None if lo is None else np.empty(max(ncf, 1))
+    lib().ldu_gamg_coarse_matrix(fine["diag"].size, fra.size, _p(np.ascontiguousarray(fine["diag"])),
+                                 _p(np.ascontiguousarray(fine["upper"])),
+                                 _p(None if lo is None else np.ascontiguousarray(lo)),
+                                 _p(ra, i32p), _p(fra, i32p), _p(flip, i32p), nc, ncf,
+                                 _p(cd), _p(cu), _p(cl))
+    return cd, cu[:ncf], (None if cl is None else cl[:ncf])

@@ -1,0 +1,462 @@
+/*---------------------------------------------------------------------------*\
+  ref_harness.C - drives the reference's own lduMatrix solver code.
+
+  Test infrastructure only (golden-vector generator).  Linked against
+  oracle/_ref/libOpenFOAM.so, which build_ref.py compiles from the
+  reference sources.  It reads one record file, runs the reference code named
+  by its "mode" record and writes the results to a record file:
+
+    geom   polyMesh from (points, faces, owner, neighbour, patches):
+           faceAreas, faceCentres, magFaceAreas, cellCentres, cellVolumes
+           (primitiveMeshFaceCentresAndAreas.C, primitiveMeshCellCentresAndVols.C)
+    ops    single operations on an lduMatrix: Amul, Tmul, residual, sumA,
+           normFactor, DIC/DILU reciprocal diagonals and preconditioning,
+           GaussSeidel and DIC smoothing, gSum* reductions
+    solve  lduMatrix::solver::New(...)->solve(psi, source) for the solver
+           dictionary given as text; for GAMG, an agglomeration built by
+           pairGAMGAgglomeration::agglomerate from the given face weights is
+           registered first (the faceAreaPair weights need an fvMesh; the
+           pairing itself is the reference code path), and the level
+           hierarchy and coarse matrices are written too.
+
+  Record file: "CFXREC1\n", then records of
+    char name[32]; char dtype[8] ("i4"|"f8"|"s"); int64 count; data
+\*---------------------------------------------------------------------------*/
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <limits>
+#include <list>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "Time.H"
+#include "polyMesh.H"
+#include "polyPatch.H"
+#include "FieldField.H"
+#include "lduMatrix.H"
+#include "lduPrimitiveMesh.H"
+#include "DICPreconditioner.H"
+#include "DILUPreconditioner.H"
+#include "pairGAMGAgglomeration.H"
+#include "PCG.H"
+#include "PBiCGStab.H"
+#include "IStringStream.H"
+#include "SolverPerformance.H"
+#include "GAMGSolver.H"
+
+using namespace Foam;
+
+// The coarse-level matrices are a private member of GAMGSolver; the harness
+// reads them (to pin the device-side coarse assembly) through the standard
+// explicit-instantiation access rule.
+namespace
+{
+template<class Tag, typename Tag::type M>
+struct memberAccess
+{
+    friend typename Tag::type get(Tag) { return M; }
+};
+struct GAMGmatrixLevels
+{
+    typedef PtrList<lduMatrix> GAMGSolver::*type;
+    friend type get(GAMGmatrixLevels);
+};
+template struct memberAccess<GAMGmatrixLevels, &GAMGSolver::matrixLevels_>;
+}
+
+namespace
+{
+
+struct Rec
+{
+    std::string dtype;
+    std::vector<char> data;
+    int64_t count = 0;
+};
+
+typedef std::map<std::string, Rec> RecMap;
+
+RecMap readRecs(const char* path)
+{
+    RecMap m;
+    FILE* fh = std::fopen(path, "rb");
+    if (!fh) { std::fprintf(stderr, "cannot open %s\n", path); std::exit(2); }
+    char magic[8];
+    if (std::fread(magic, 1, 8, fh) != 8 || std::memcmp(magic, "CFXREC1\n", 8))
+    {
+        std::fprintf(stderr, "bad record file\n"); std::exit(2);
+    }
+    while (true)
+    {
+        char name[33] = {0}, dt[9] = {0};
+        int64_t n;
+        if (std::fread(name, 1, 32, fh) != 32) break;
+        if (std::fread(dt, 1, 8, fh) != 8) break;
+        if (std::fread(&n, 8, 1, fh) != 1) break;
+        Rec r;
+        r.dtype = dt;
+        r.count = n;
+        size_t es = r.dtype == "f8" ? 8 : r.dtype == "i4" ? 4 : 1;
+        r.data.resize(es*n);
+        if (n && std::fread(r.data.data(), es, n, fh) != size_t(n)) break;
+        m[name] = r;
+    }
+    std::fclose(fh);
+    return m;
+}
+
+struct Writer
+{
+    FILE* fh;
+    explicit Writer(const char* path) : fh(std::fopen(path, "wb"))
+    {
+        std::fwrite("CFXREC1\n", 1, 8, fh);
+    }
+    ~Writer() { std::fclose(fh); }
+    void put(const std::string& name, const char* dt, const void* p, int64_t n, size_t es)
+    {
+        char nm[32] = {0}, d[8] = {0};
+        std::strncpy(nm, name.c_str(), 31);
+        std::strncpy(d, dt, 7);
+        std::fwrite(nm, 1, 32, fh);
+        std::fwrite(d, 1, 8, fh);
+        std::fwrite(&n, 8, 1, fh);
+        if (n) std::fwrite(p, es, n, fh);
+    }
+    void f8(const std::string& name, const scalarUList& v) { put(name, "f8", v.cdata(), v.size(), 8); }
+    void f8(const std::string& name, double v) { put(name, "f8", &v, 1, 8); }
+    void i4(const std::string& name, const labelUList& v) { put(name, "i4", v.cdata(), v.size(), 4); }
+    void i4(const std::string& name, int v) { put(name, "i4", &v, 1, 4); }
+    void vec(const std::string& name, const vectorField& v)
+    {
+        put(name, "f8", v.cdata(), 3*v.size(), 8);
+    }
+};
+
+labelList getL(const RecMap& m, const char* k)
+{
+    const Rec& r = m.at(k);
+    labelList out(r.count);
+    std::memcpy(out.data(), r.data.data(), 4*r.count);
+    return out;
+}
+
+scalarField getF(const RecMap& m, const char* k)
+{
+    const Rec& r = m.at(k);
+    scalarField out(r.count);
+    std::memcpy(out.data(), r.data.data(), 8*r.count);
+    return out;
+}
+
+std::string getS(const RecMap& m, const char* k)
+{
+    const Rec& r = m.at(k);
+    return std::string(r.data.begin(), r.data.end());
+}
+
+bool has(const RecMap& m, const char* k) { return m.count(k) > 0; }
+
+
+// An lduMesh that owns its addressing and can answer db(), which GAMG needs
+// to cache its agglomeration (lduMesh::db() is NotImplemented in the base).
+class harnessMesh
+:
+    public lduPrimitiveMesh
+{
+    const objectRegistry& db_;
+
+public:
+
+    harnessMesh(const objectRegistry& db, label n, labelList& l, labelList& u)
+    :
+        lduPrimitiveMesh(n, l, u, UPstream::worldComm, false),
+        db_(db)
+    {}
+
+    virtual const objectRegistry& db() const { return db_; }
+};
+
+
+// pairGAMGAgglomeration driven by explicit face weights: the faceAreaPair
+// weights (faceAreaPairGAMGAgglomeration.C:55-80) computed from the given
+// face-area vectors, then the reference pairing (pairGAMGAgglomerate.C).
+class harnessAgglomeration
+:
+    public pairGAMGAgglomeration
+{
+public:
+
+    harnessAgglomeration
+    (
+        const lduMesh& mesh,
+        const scalarField& weights,
+        const dictionary& dict
+    )
+    :
+        pairGAMGAgglomeration(mesh, dict)
+    {
+        // pairGAMGAgglomeration::forward_ is a process-global static that
+        // starts true; one agglomeration per harness process keeps it so.
+        agglomerate(mesh, weights);
+    }
+};
+
+
+int runGeom(const RecMap& in, Writer& out, Time& runTime)
+{
+    const scalarField P(getF(in, "points"));
+    const labelList F(getL(in, "faces"));
+    labelList own(getL(in, "owner"));
+    labelList nei(getL(in, "neighbour"));
+    const labelList ps(getL(in, "patchStart"));
+
+    pointField points(P.size()/3);
+    forAll(points, i) points[i] = point(P[3*i], P[3*i+1], P[3*i+2]);
+    faceList faces(F.size()/4);
+    forAll(faces, i)
+    {
+        face f(4);
+        for (int q = 0; q < 4; q++) f[q] = F[4*i+q];
+        faces[i] = f;
+    }
+
+    polyMesh mesh
+    (
+        IOobject(polyMesh::defaultRegion, runTime.name(), runTime,
+                 IOobject::NO_READ, IOobject::NO_WRITE),
+        std::move(points), std::move(faces), std::move(own), std::move(nei),
+        false
+    );
+
+    List<polyPatch*> patches(ps.size() - 1);
+    forAll(patches, p)
+    {
+        patches[p] = new polyPatch
+        (
+            "patch" + Foam::name(p), ps[p+1] - ps[p], ps[p], p, mesh.boundary()
+        );
+    }
+    mesh.addPatches(patches, false);
+
+    out.vec("Sf", mesh.faceAreas());
+    out.vec("Cf", mesh.faceCentres());
+    out.f8("magSf", mesh.magFaceAreas());
+    out.vec("C", mesh.cellCentres());
+    out.f8("V", mesh.cellVolumes());
+    return 0;
+}
+
+
+void buildMatrix(lduMatrix& A, const RecMap& in, label nCells, label nFaces)
+{
+    A.diag(nCells) = getF(in, "diag");
+    A.upper(nFaces) = getF(in, "upper");
+    if (has(in, "lower")) A.lower(nFaces) = getF(in, "lower");
+}
+
+
+int runOps(const RecMap& in, Writer& out, Time& runTime)
+{
+    labelList l(getL(in, "l")), u(getL(in, "u"));
+    const scalarField x(getF(in, "x")), b(getF(in, "b"));
+    const label nCells = x.size(), nFaces = l.size();
+    harnessMesh mesh(runTime, nCells, l, u);
+    lduMatrix A(mesh);
+    buildMatrix(A, in, nCells, nFaces);
+
+    Field<Field<scalar>> bou(0), intc(0);
+    lduInterfaceFieldPtrsList ifs(0);
+
+    scalarField y(nCells);
+    A.Amul(y, x, bou, ifs, 0);
+    out.f8("Amul", y);
+    A.Tmul(y, x, bou, ifs, 0);
+    out.f8("Tmul", y);
+    A.residual(y, x, b, bou, ifs, 0);
+    out.f8("residual", y);
+    A.sumA(y, bou, ifs);
+    out.f8("sumA", y);
+
+    out.f8("sumMag", gSumMag(b));
+    out.f8("sumProd", gSumProd(x, b));
+    out.f8("sumSqr", gSumSqr(b));
+    out.f8("sum", gSum(b));
+    out.f8("average", gAverage(x));
+
+    // normFactor via a throw-away solver object (the base implementation)
+    {
+        IStringStream is
+        (
+            A.symmetric()
+          ? "{ solver PCG; preconditioner none; }"
+          : "{ solver PBiCGStab; preconditioner none; }"
+        );
+        dictionary d(is);
+        autoPtr<lduMatrix::solver> s =
+            lduMatrix::solver::New("x", A, bou, intc, ifs, d);
+        scalarField Ax(nCells), tmp(nCells);
+        A.Amul(Ax, x, bou, ifs, 0);
+        out.f8("normFactor", s->normFactor(x, b, Ax, tmp));
+    }
+
+    if (A.symmetric())
+    {
+        scalarField rD(A.diag());
+        DICPreconditioner::calcReciprocalD(rD, A);
+        out.f8("DIC_rD", rD);
+        IStringStream is("{ solver PCG; preconditioner DIC; }");
+        dictionary d(is);
+        autoPtr<lduMatrix::solver> s =
+            lduMatrix::solver::New("x", A, bou, intc, ifs, d);
+        autoPtr<lduMatrix::preconditioner> p =
+            lduMatrix::preconditioner::New(s(), d);
+        p->precondition(y, b, 0);
+        out.f8("DIC_precondition", y);
+
+        IStringStream is2("{ smoother DIC; }");
+        dictionary d2(is2);
+        autoPtr<lduMatrix::smoother> sm =
+            lduMatrix::smoother::New("x", A, bou, intc, ifs, d2);
+        scalarField psi(x);
+        sm->smooth(psi, b, 0, 2);
+        out.f8("DIC_smooth2", psi);
+    }
+    else
+    {
+        scalarField rD(A.diag());
+        DILUPreconditioner::calcReciprocalD(rD, A);
+        out.f8("DILU_rD", rD);
+        IStringStream is("{ solver PBiCGStab; preconditioner DILU; }");
+        dictionary d(is);
+        autoPtr<lduMatrix::solver> s =
+            lduMatrix::solver::New("x", A, bou, intc, ifs, d);
+        autoPtr<lduMatrix::preconditioner> p =
+            lduMatrix::preconditioner::New(s(), d);
+        p->precondition(y, b, 0);
+        out.f8("DILU_precondition", y);
+        p->preconditionT(y, b, 0);
+        out.f8("DILU_preconditionT", y);
+    }
+
+    {
+        IStringStream is("{ smoother GaussSeidel; }");
+        dictionary d(is);
+        autoPtr<lduMatrix::smoother> sm =
+            lduMatrix::smoother::New("x", A, bou, intc, ifs, d);
+        scalarField psi(x);
+        sm->smooth(psi, b, 0, 1);
+        out.f8("GS_smooth1", psi);
+        sm->smooth(psi, b, 0, 2);
+        out.f8("GS_smooth3", psi);
+    }
+
+    out.i4("ownerStart", mesh.lduAddr().ownerStartAddr());
+    out.i4("losort", mesh.lduAddr().losortAddr());
+    out.i4("losortStart", mesh.lduAddr().losortStartAddr());
+    return 0;
+}
+
+
+int runSolve(const RecMap& in, Writer& out, Time& runTime)
+{
+    labelList l(getL(in, "l")), u(getL(in, "u"));
+    const scalarField source(getF(in, "source"));
+    scalarField psi(getF(in, "psi"));
+    const label nCells = source.size(), nFaces = l.size();
+    harnessMesh mesh(runTime, nCells, l, u);
+    lduMatrix A(mesh);
+    buildMatrix(A, in, nCells, nFaces);
+
+    IStringStream is(getS(in, "dict"));
+    dictionary dict(is);
+
+    Field<Field<scalar>> bou(0), intc(0);
+    lduInterfaceFieldPtrsList ifs(0);
+
+    const word solverName(dict.lookup("solver"));
+    if (solverName == "GAMG")
+    {
+        const scalarField w(getF(in, "weights"));
+        harnessAgglomeration* agg = new harnessAgglomeration(mesh, w, dict);
+        regIOobject::store(static_cast<GAMGAgglomeration*>(agg));
+    }
+
+    autoPtr<lduMatrix::solver> s =
+        lduMatrix::solver::New("psi", A, bou, intc, ifs, dict);
+    solverPerformance perf = s->solve(psi, source, 0);
+
+    out.f8("psi", psi);
+    out.f8("initialResidual", perf.initialResidual());
+    out.f8("finalResidual", perf.finalResidual());
+    out.i4("nIterations", perf.nIterations());
+    out.i4("converged", perf.converged() ? 1 : 0);
+    out.i4("singular", perf.singular() ? 1 : 0);
+    out.put("solverName", "s", perf.solverName().c_str(), perf.solverName().size(), 1);
+
+    if (solverName == "GAMG")
+    {
+        const GAMGSolver& g = refCast<const GAMGSolver>(s());
+        const GAMGAgglomeration& agg =
+            mesh.db().lookupObject<GAMGAgglomeration>(GAMGAgglomeration::typeName);
+        out.i4("nLevels", agg.size());
+        for (label i = 0; i < agg.size(); i++)
+        {
+            const std::string k = std::to_string(i);
+            out.i4("restrict" + k, agg.restrictAddressing(i));
+            out.i4("faceRestrict" + k, agg.faceRestrictAddressing(i));
+            const boolList& fl = agg.faceFlipMap(i);
+            labelList fli(fl.size());
+            forAll(fl, j) fli[j] = fl[j] ? 1 : 0;
+            out.i4("faceFlip" + k, fli);
+            out.i4("nCells" + k, agg.nCells(i));
+            out.i4("nFaces" + k, agg.nFaces(i));
+            const lduAddressing& ca = agg.meshLevel(i + 1).lduAddr();
+            out.i4("coarseL" + k, ca.lowerAddr());
+            out.i4("coarseU" + k, ca.upperAddr());
+            const lduMatrix& cm = (g.*get(GAMGmatrixLevels()))[i];
+            out.f8("coarseDiag" + k, cm.diag());
+            out.f8("coarseUpper" + k, cm.upper());
+            if (cm.hasLower()) out.f8("coarseLower" + k, cm.lower());
+        }
+    }
+    return 0;
+}
+
+} // namespace
+
+
+int main(int argc, char* argv[])
+{
+    if (argc != 3)
+    {
+        std::fprintf(stderr, "usage: ref_harness in.rec out.rec\n");
+        return 2;
+    }
+    const RecMap in = readRecs(argv[1]);
+    const std::string mode = getS(in, "mode");
+
+    const char* tmp = std::getenv("CFX_HARNESS_ROOT");
+    const fileName root(tmp ? tmp : "/tmp");
+    Time runTime(root, "cfxcase", false);
+
+    Writer out(argv[2]);
+    if (mode == "geom") return runGeom(in, out, runTime);
+    if (mode == "ops") return runOps(in, out, runTime);
+    if (mode == "solve") return runSolve(in, out, runTime);
+    std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 2;
+}

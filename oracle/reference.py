@@ -1,0 +1,70 @@
+"""Run the reference's own solver code (oracle/_ref/ref_harness) on a system.
+
+TEST INFRASTRUCTURE ONLY, and only where the reference sources are mounted
+(the harness links oracle/_ref/libOpenFOAM.so built by build_ref.py).  Used
+to pin the C oracle and to write the golden fixtures in tests/golden/.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from . import records
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+REF_ROOT = "/root/reference"
+
+
+def available():
+    return os.path.exists(HARNESS) and os.path.isdir(os.path.join(REF_ROOT, "etc"))
+
+
+def run(recs):
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.rec"), os.path.join(td, "out.rec")
+        records.write(fin, recs)
+        env = dict(os.environ, WM_PROJECT_DIR=REF_ROOT, WM_PROJECT="OpenFOAM",
+                   WM_PROJECT_VERSION="dev", CFX_HARNESS_ROOT=td)
+        os.makedirs(os.path.join(td, "cfxcase"), exist_ok=True)
+        r = subprocess.run([HARNESS, fin, fout], env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference harness failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
+        return records.read(fout)
+
+
+def _ldu(s):
+    d = dict(l=s["l"], u=s["u"], diag=s["diag"], upper=s["upper"])
+    if s.get("lower") is not None:
+        d["lower"] = s["lower"]
+    return d
+
+
+def geometry(mesh):
+    return run(dict(mode="geom", points=mesh["points"], faces=mesh["faces"], owner=mesh["owner"],
+                    neighbour=mesh["neighbour"], patchStart=mesh["patchStart"]))
+
+
+def ops(s, x, b):
+    return run(dict(mode="ops", x=x, b=b, **_ldu(s)))
+
+
+def dict_text(ctl):
+    parts = []
+    for k, v in ctl.items():
+        if isinstance(v, bool):
+            v = "true" if v else "false"
+        elif isinstance(v, float):
+            v = repr(v)
+        parts.append(f"{k} {v};")
+    return "{ " + " ".join(parts) + " }"
+
+
+def solve(s, ctl, psi0=None, weights=None):
+    recs = dict(mode="solve", source=s["source"],
+                psi=np.zeros_like(s["source"]) if psi0 is None else psi0,
+                dict=dict_text(ctl), **_ldu(s))
+    if weights is not None:
+        recs["weights"] = weights
+    return run(recs)

@@ -1,0 +1,183 @@
+/*
+ * cfx.h - C ABI of libcudaLduSolvers.so, the GB300 (sm_103a) lduMatrix solvers.
+ *
+ * The library replaces, for one GPU, the reference's lduMatrix::solver path:
+ * an OpenFOAM plugin class (cudaPCG, cudaPBiCGStab, cudaGAMG deriving
+ * Foam::lduMatrix::solver) holds a cfx_mesh per lduMesh,
+ * re-uploads coefficients on every solve and calls cfx_solve().  All entry
+ * points take plain pointers and sizes; labels are int32 (WM_LABEL_SIZE=32)
+ * and scalars double (WM_DP).  Every function returns a cfx_status.
+ *
+ * Reference interfaces replaced (paths relative to the OpenFOAM-dev tree):
+ *   lduAddressing                src/OpenFOAM/matrices/lduMatrix/lduAddressing/lduAddressing.H:172-194
+ *   lduMatrix coefficients       src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrix.H:86-87
+ *   lduMatrix::solver::New/solve src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrix.H:187-255,
+ *                                src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrixSolver.C:40-130
+ *   SolverPerformance            src/OpenFOAM/matrices/LduMatrix/LduMatrix/SolverPerformance.H:79-304
+ *   lduMatrix::Amul / residual   src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrixATmul.C:34-92, 203-280
+ *   preconditioner::precondition src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrix.H:420-430
+ *   smoother::smooth             src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrix.H:316-330
+ *   GAMGAgglomeration            src/OpenFOAM/matrices/lduMatrix/solvers/GAMG/GAMGAgglomerations/
+ *                                GAMGAgglomeration/GAMGAgglomeration.H:325-380
+ */
+#ifndef CFX_H
+#define CFX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CFX_OK = 0,
+    CFX_ERR_ARG = -1,         /* bad argument (null pointer, size, enum) */
+    CFX_ERR_ADDRESSING = -2,  /* l/u not upper-triangular, out of range */
+    CFX_ERR_CUDA = -3,        /* CUDA runtime error (message: cfx_last_error) */
+    CFX_ERR_NOMEM = -4,       /* device allocation failed */
+    CFX_ERR_ADMISSION = -5,   /* request exceeds the server's HBM budget */
+    CFX_ERR_TIMEOUT = -6,     /* a bounded device wait expired */
+    CFX_ERR_CONFIG = -7,      /* unknown solver/preconditioner/smoother name */
+    CFX_ERR_STATE = -8        /* call out of order (e.g. GAMG without levels) */
+} cfx_status;
+
+typedef struct cfx_ctx cfx_ctx;        /* device, stream, scratch */
+typedef struct cfx_mesh cfx_mesh;      /* resident addressing + schedules + GAMG levels */
+typedef struct cfx_matrix cfx_matrix;  /* coefficients on a mesh */
+
+/* SolverPerformance<scalar> (SolverPerformance.H:79-304) */
+typedef struct {
+    char solverName[32];   /* e.g. "DICPCG", "DILUPBiCGStab", "GAMG" */
+    double initialResidual;
+    double finalResidual;
+    int nIterations;
+    int converged;
+    int singular;
+    int status;            /* cfx_status of the solve */
+    int nOuter;            /* mixed precision: refinement steps; else 0 */
+    int pad;
+} cfx_perf;
+
+enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2 };
+enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3 };
+enum { CFX_SMOOTH_GS = 0, CFX_SMOOTH_DIC = 1 };
+enum { CFX_FP64 = 0, CFX_MIXED = 1 };
+
+/* Solver controls: lduMatrix::solver::readControls (lduMatrixSolver.C:158-164)
+ * and GAMGSolver::readControls (GAMGSolver.C:348-388); use cfx_default_controls. */
+typedef struct {
+    int solver;            /* CFX_SOLVER_* */
+    int preconditioner;    /* CFX_PRE_* (PCG, PBiCGStab) */
+    double tolerance;      /* default 1e-6 */
+    double relTol;         /* default 0 */
+    int maxIter;           /* default 1000 */
+    int minIter;           /* default 0 */
+    /* GAMG */
+    int smoother;          /* CFX_SMOOTH_* (default GaussSeidel) */
+    int nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps;       /* 0, 1, 4 */
+    int nPostSweeps, postSweepsLevelMultiplier, maxPostSweeps;    /* 2, 1, 4 */
+    int nFinestSweeps;     /* 2 */
+    int scaleCorrection;   /* -1: default = matrix symmetric */
+    int nCellsInCoarsestLevel; /* 10 */
+    /* precision: CFX_FP64, or CFX_MIXED = FP32 inner solve in an FP64
+     * iterative-refinement loop (outer residual, solution, normFactor and
+     * convergence in FP64) */
+    int precision;
+    int pad;
+} cfx_controls;
+
+void cfx_default_controls(cfx_controls* c);
+
+/* Human-readable text of the last error on this thread. */
+const char* cfx_last_error(void);
+int cfx_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+cfx_status cfx_ctx_create(int device, cfx_ctx** ctx);
+cfx_status cfx_ctx_destroy(cfx_ctx* ctx);
+/* The cudaStream_t all work of this context is enqueued on. */
+cfx_status cfx_ctx_stream(cfx_ctx* ctx, void** stream);
+cfx_status cfx_ctx_synchronize(cfx_ctx* ctx);
+/* Number of kernels this context has launched (for launch accounting). */
+cfx_status cfx_ctx_launch_count(cfx_ctx* ctx, int64_t* count);
+
+/* ---- mesh (lduAddressing) ----------------------------------------------- */
+/* Validates that (l, u) is upper-triangular (l < u, sorted by l then u, as
+ * lduPrimitiveMesh::checkUpperTriangular, lduPrimitiveMesh.C:60-95), builds
+ * losort/ownerStart/losortStart and the forward/backward level schedules of
+ * the lower/upper dependency DAG, and keeps them resident. */
+cfx_status cfx_mesh_create(cfx_ctx* ctx, int nCells, int nFaces, const int32_t* l,
+                           const int32_t* u, cfx_mesh** mesh);
+cfx_status cfx_mesh_destroy(cfx_mesh* mesh);
+/* Level-schedule depth of the forward (lower) DAG. */
+cfx_status cfx_mesh_info(cfx_mesh* mesh, int* nFwdLevels, int* nBwdLevels);
+
+/* faceAreaPair weights |(Sf/sqrt|Sf|) * (1, 1.01, 1.02)|
+ * (faceAreaPairGAMGAgglomeration.C:55-80) from face-area vectors Sf[nFaces*3]. */
+cfx_status cfx_face_area_pair_weights(int nFaces, const double* Sf, double* weights);
+
+/* GAMG level hierarchy by pairwise agglomeration of the given face weights
+ * (pairGAMGAgglomerate.C:31-301, GAMGAgglomerateLduAddressing.C:32-222) on
+ * the host, then uploaded.  forwardStart is the initial cell-loop direction
+ * (pairGAMGAgglomeration::forward_, true in a fresh process). */
+cfx_status cfx_gamg_agglomerate(cfx_mesh* mesh, const double* faceWeights,
+                                int nCellsInCoarsestLevel, int forwardStart);
+/* Same, from an agglomeration computed by the caller (e.g. the reference's
+ * own cached GAMGAgglomeration): restrictAddr[i] has the cell count of level
+ * i (level 0 = this mesh) and maps to nCoarseCells[i] cells. */
+cfx_status cfx_gamg_set_levels(cfx_mesh* mesh, int nLevels, const int32_t* const* restrictAddr,
+                               const int32_t* nCoarseCells);
+/* Level sizes; restrictAddr/coarse l,u of level i copied out when non-null. */
+cfx_status cfx_gamg_level_info(cfx_mesh* mesh, int level, int* nCells, int* nFaces,
+                               int32_t* restrictAddr, int32_t* faceRestrict, int32_t* faceFlip,
+                               int32_t* coarseL, int32_t* coarseU);
+cfx_status cfx_gamg_n_levels(cfx_mesh* mesh, int* nLevels);
+
+/* ---- matrix (lduMatrix coefficients) ------------------------------------ */
+/* Host coefficients; lower == NULL means symmetric (lduMatrix::symmetric()). */
+cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* upper,
+                             const double* lower, cfx_matrix** mat);
+/* Re-upload coefficients (a new fvMatrix on the same mesh, every solve). */
+cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper,
+                             const double* lower);
+/* Same with device pointers (coefficients already in HBM). */
+cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* d_diag, const double* d_upper,
+                                    const double* d_lower);
+cfx_status cfx_matrix_destroy(cfx_matrix* mat);
+/* Coarse-level coefficients assembled on the device (level >= 1), copied out. */
+cfx_status cfx_matrix_coarse(cfx_matrix* mat, int level, double* diag, double* upper, double* lower);
+
+/* ---- solve (lduMatrix::solver::solve) ------------------------------------ */
+/* psi (in/out) and source are host arrays of nCells doubles. */
+cfx_status cfx_solve(cfx_matrix* mat, const cfx_controls* ctl, double* psi, const double* source,
+                     cfx_perf* perf);
+/* Same with device pointers: nothing crosses PCIe/C2C except the perf record. */
+cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_psi,
+                            const double* d_source, cfx_perf* perf);
+
+/* ---- tuning (process-wide knobs; no reference counterpart) ---------------
+ * CFX_TUNE_SMALL_SWEEP: meshes with at most this many cells run their
+ * triangular sweeps in one CTA with block barriers; larger ones use the
+ * persistent multi-CTA level scheduler (default 200000). */
+enum { CFX_TUNE_SMALL_SWEEP = 0 };
+cfx_status cfx_tune_set(int key, int value);
+cfx_status cfx_tune_get(int key, int* value);
+
+/* ---- single operations, device pointers (parity tests, building blocks) -- */
+cfx_status cfx_amul(cfx_matrix* mat, const double* d_x, double* d_y);
+cfx_status cfx_tmul(cfx_matrix* mat, const double* d_x, double* d_y);
+cfx_status cfx_residual(cfx_matrix* mat, const double* d_x, const double* d_b, double* d_r);
+cfx_status cfx_sumA(cfx_matrix* mat, double* d_s);
+/* which: 0 sum, 1 sumMag, 2 sumSqr, 3 sumProd(a, b) -> *out (host). */
+cfx_status cfx_reduce(cfx_ctx* ctx, int which, int n, const double* d_a, const double* d_b, double* out);
+cfx_status cfx_norm_factor(cfx_matrix* mat, const double* d_psi, const double* d_b, double* out);
+/* kind CFX_PRE_*; transpose != 0 applies DILU preconditionT. */
+cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const double* d_r, double* d_w);
+cfx_status cfx_reciprocal_d(cfx_matrix* mat, int kind, double* d_rD);
+cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* d_psi, const double* d_b, int nSweeps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

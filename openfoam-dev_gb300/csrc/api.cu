@@ -1,0 +1,1365 @@
+// api.cu - the C ABI (include/cfx.h): contexts, resident meshes and matrices,
+// and the host drivers of cudaPCG / cudaPBiCGStab / cudaGAMG.
+//
+// The drivers enqueue device work only; the host reads the device SolveState
+// once per batch of iterations (Krylov) or once per V-cycle (GAMG).  One
+// iteration (or one V-cycle) is captured once into a CUDA graph and replayed,
+// so launch overhead is paid once per graph, not per kernel.
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+
+#include "internal.h"
+#include "solvers.h"
+
+namespace cfx {
+
+namespace {
+thread_local std::string g_err;
+}
+
+void set_error(const std::string& msg) { g_err = msg; }
+const char* last_error() { return g_err.c_str(); }
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
+        throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+#define CK(x) ck((x), #x)
+
+// Owner of a set of device allocations.
+struct Arena {
+    std::vector<void*> ptrs;
+    size_t bytes = 0;
+    template <class T>
+    T* get(size_t n) {
+        void* p = nullptr;
+        const size_t b = std::max<size_t>(n, 1) * sizeof(T);
+        CK(cudaMalloc(&p, b));
+        ptrs.push_back(p);
+        bytes += b;
+        return static_cast<T*>(p);
+    }
+    template <class T>
+    T* upload(const std::vector<T>& v, cudaStream_t s) {
+        T* p = get<T>(v.size());
+        if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        return p;
+    }
+    void release() {
+        for (void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+        bytes = 0;
+    }
+    ~Arena() { release(); }
+};
+
+}  // namespace cfx
+
+using namespace cfx;
+
+// ------------------------------------------------------------------ objects
+struct cfx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    Scratch sc;
+    SolveState* d_state = nullptr;  // [4]: outer, inner, spare
+    SolveState* h_state = nullptr;  // pinned mirror
+    int* d_status = nullptr;
+    double* d_red = nullptr;        // [8] reduction outputs
+    double* h_red = nullptr;        // pinned
+};
+
+struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key = 0;
+    }
+    ~GraphCache() { reset(); }
+};
+
+struct cfx_mesh {
+    cfx_ctx* ctx = nullptr;
+    Arena arena;
+    std::vector<HostLevel> host;   // [0] = the mesh, then GAMG coarse levels
+    std::vector<LevelMesh> dev;
+    int nCoarseLevels = 0;         // GAMG levels below the mesh (0: none)
+    uint64_t version = 1;          // bumped when the level hierarchy changes
+};
+
+// Named device work vectors of one precision; slot i keeps its allocation
+// (grown when a larger size is asked for), so captured graphs stay valid.
+template <class T>
+struct Work {
+    Arena arena;
+    int n = 0;
+    std::vector<T*> v;
+    std::vector<int> sz;
+    T* get(int i, int nn) {
+        if ((int)v.size() <= i) {
+            v.resize(i + 1, nullptr);
+            sz.resize(i + 1, 0);
+        }
+        if (!v[i] || sz[i] < nn) {
+            v[i] = arena.template get<T>(nn);
+            sz[i] = nn;
+        }
+        return v[i];
+    }
+};
+
+struct cfx_matrix {
+    cfx_mesh* mesh = nullptr;
+    Arena arena;
+    bool sym = true;
+    std::vector<LevelCoeffs<double>> c64;   // per level
+    std::vector<LevelCoeffs<float>> c32;
+    bool coarse64 = false, coarse32 = false, fine32 = false;
+    // host<->device staging and work vectors
+    double *d_psi = nullptr, *d_src = nullptr;
+    Work<double> w64;
+    Work<float> w32;
+    std::vector<Work<double>> lv64;  // per-level GAMG vectors
+    std::vector<Work<float>> lv32;
+    Arena blockArena;
+    BlockSys<double>* d_blk64 = nullptr;
+    BlockSys<float>* d_blk32 = nullptr;
+    GraphCache gPCG, gBiCG, gGAMG, gMixed;
+};
+
+// --------------------------------------------------------------- utilities
+namespace {
+
+template <class F>
+cfx_status guard(F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        set_error("device or host allocation failed");
+        return CFX_ERR_NOMEM;
+    } catch (const CudaError& e) {
+        set_error(e.what());
+        return CFX_ERR_CUDA;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return CFX_ERR_ARG;
+    }
+}
+
+void upload_schedule(Arena& ar, cudaStream_t s, const std::vector<int>& cells, const std::vector<int>& levelStart,
+                     Schedule& sch) {
+    const int nl = int(levelStart.size()) - 1;
+    std::vector<int> chunkStart{0}, chunkLevel, levelChunks(std::max(nl, 0), 0);
+    int maxw = 0;
+    for (int L = 0; L < nl; ++L) {
+        const int b = levelStart[L], e = levelStart[L + 1];
+        maxw = std::max(maxw, e - b);
+        for (int i = b; i < e; i += SWEEP_CHUNK) {
+            chunkStart.push_back(std::min(i + SWEEP_CHUNK, e));
+            chunkLevel.push_back(L);
+            levelChunks[L]++;
+        }
+    }
+    sch.nLevels = nl;
+    sch.nCells = int(cells.size());
+    sch.nChunks = int(chunkLevel.size());
+    sch.maxLevelWidth = maxw;
+    sch.cells = ar.upload(cells, s);
+    sch.levelStart = ar.upload(levelStart, s);
+    sch.chunkStart = ar.upload(chunkStart, s);
+    sch.chunkLevel = ar.upload(chunkLevel, s);
+    sch.levelChunks = ar.upload(levelChunks, s);
+    sch.sync = ar.get<int>(2 + std::max(nl, 1));
+    CK(cudaMemsetAsync(sch.sync, 0, sizeof(int) * (2 + std::max(nl, 1)), s));
+}
+
+void upload_level(Arena& ar, cudaStream_t s, const HostLevel& h, LevelMesh& m) {
+    m.n = h.n;
+    m.nf = h.nf;
+    m.l = ar.upload(h.l, s);
+    m.u = ar.upload(h.u, s);
+    m.ownerStart = ar.upload(h.ownerStart, s);
+    m.losortStart = ar.upload(h.losortStart, s);
+    m.losort = ar.upload(h.losort, s);
+    m.losortL = ar.upload(h.losortL, s);
+    upload_schedule(ar, s, h.fwdCells, h.fwdLevelStart, m.fwd);
+    upload_schedule(ar, s, h.bwdCells, h.bwdLevelStart, m.bwd);
+}
+
+// Inverse restriction maps of level h (fine) -> coarse, for the gathers.
+void upload_restriction(Arena& ar, cudaStream_t s, const HostLevel& h, LevelMesh& m) {
+    const int n = h.n, nf = h.nf, nc = h.nCoarse, ncf = h.nCoarseFaces;
+    m.nCoarse = nc;
+    m.nCoarseFaces = ncf;
+    auto group = [](int nKeys, const std::vector<int>& key, std::vector<int>& start, std::vector<int>& items,
+                     bool negative) {
+        start.assign(nKeys + 1, 0);
+        for (size_t i = 0; i < key.size(); ++i) {
+            const int k = key[i];
+            if (negative ? k < 0 : k >= 0) start[(negative ? -1 - k : k) + 1]++;
+        }
+        for (int c = 0; c < nKeys; ++c) start[c + 1] += start[c];
+        items.resize(start[nKeys]);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (size_t i = 0; i < key.size(); ++i) {
+            const int k = key[i];
+            if (negative ? k < 0 : k >= 0) items[fill[negative ? -1 - k : k]++] = int(i);
+        }
+    };
+    std::vector<int> ccStart, ccFine, cfStart, cfFine, ifStart, ifFine;
+    group(nc, h.restrictAddr, ccStart, ccFine, false);
+    group(ncf, h.faceRestrict, cfStart, cfFine, false);
+    group(nc, h.faceRestrict, ifStart, ifFine, true);
+    (void)n;
+    (void)nf;
+    m.restrictAddr = ar.upload(h.restrictAddr, s);
+    m.coarseCellStart = ar.upload(ccStart, s);
+    m.coarseCellFine = ar.upload(ccFine, s);
+    m.faceRestrict = ar.upload(h.faceRestrict, s);
+    m.faceFlip = ar.upload(h.faceFlip, s);
+    m.coarseFaceStart = ar.upload(cfStart, s);
+    m.coarseFaceFine = ar.upload(cfFine, s);
+    m.intFaceStart = ar.upload(ifStart, s);
+    m.intFaceFine = ar.upload(ifFine, s);
+}
+
+template <class T>
+void alloc_coeffs(Arena& ar, const LevelMesh& m, bool sym, LevelCoeffs<T>& c) {
+    c.sym = sym;
+    c.diag = ar.get<T>(m.n);
+    c.upper = ar.get<T>(m.nf);
+    c.lower = sym ? nullptr : ar.get<T>(m.nf);
+    c.lowerPerm = ar.get<T>(m.nf);
+    c.upperPerm = sym ? nullptr : ar.get<T>(m.nf);
+    c.rD = ar.get<T>(m.n);
+}
+
+// GAMG hierarchy from level-0 restriction maps (host), then upload.
+cfx_status build_hierarchy(cfx_mesh* mesh, const std::vector<std::vector<int>>& maps, const std::vector<int>& nCoarse) {
+    cudaStream_t s = mesh->ctx->stream;
+    mesh->host.resize(1);
+    for (size_t i = 0; i < maps.size(); ++i) {
+        HostLevel& f = mesh->host[i];
+        if ((int)maps[i].size() != f.n) {
+            set_error("restrict map " + std::to_string(i) + " has wrong size");
+            return CFX_ERR_ARG;
+        }
+        for (int v : maps[i])
+            if (v < 0 || v >= nCoarse[i]) {
+                set_error("restrict map " + std::to_string(i) + " out of range");
+                return CFX_ERR_ARG;
+            }
+        std::vector<int> cl, cu, fra, flip;
+        const int ncf = agglomerate_addressing(f.nf, f.l.data(), f.u.data(), maps[i], nCoarse[i], cl, cu, fra, flip);
+        f.restrictAddr = maps[i];
+        f.nCoarse = nCoarse[i];
+        f.nCoarseFaces = ncf;
+        f.faceRestrict = std::move(fra);
+        f.faceFlip = std::move(flip);
+        HostLevel c;
+        CFX_TRY(build_host_level(nCoarse[i], ncf, cl.data(), cu.data(), c, false));
+        mesh->host.push_back(std::move(c));
+    }
+    mesh->nCoarseLevels = int(maps.size());
+    mesh->version++;
+    // upload: keep level 0's device mesh, rebuild the rest
+    mesh->dev.resize(1);
+    upload_restriction(mesh->arena, s, mesh->host[0], mesh->dev[0]);
+    for (size_t i = 1; i < mesh->host.size(); ++i) {
+        LevelMesh m;
+        upload_level(mesh->arena, s, mesh->host[i], m);
+        if (mesh->host[i].nCoarse > 0) upload_restriction(mesh->arena, s, mesh->host[i], m);
+        mesh->dev.push_back(m);
+    }
+    return CFX_OK;
+}
+
+void set_state(cfx_ctx* ctx, int slot, const cfx_controls& c, double tol, double relTol, int maxIter, int minIter) {
+    SolveState h{};
+    h.tolerance = tol;
+    h.relTol = relTol;
+    h.maxIter = maxIter;
+    h.minIter = minIter;
+    (void)c;
+    ctx->h_state[slot] = h;
+    CK(cudaMemcpyAsync(ctx->d_state + slot, ctx->h_state + slot, sizeof(SolveState), cudaMemcpyHostToDevice,
+                       ctx->stream));
+}
+
+SolveState read_state(cfx_ctx* ctx, int slot) {
+    CK(cudaMemcpyAsync(ctx->h_state + slot, ctx->d_state + slot, sizeof(SolveState), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ctx->h_state[slot];
+}
+
+int read_status(cfx_ctx* ctx) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return h;
+}
+
+// Capture `body` into the cache's executable graph once (keyed), then launch.
+template <class F>
+void graph_launch(GraphCache& g, uint64_t key, cudaStream_t s, F&& body) {
+    if (!g.exec || g.key != key) {
+        g.reset();
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        body();
+        CK(cudaStreamEndCapture(s, &graph));
+        CK(cudaGraphInstantiate(&g.exec, graph, 0));
+        cudaGraphDestroy(graph);
+        g.key = key;
+    }
+    CK(cudaGraphLaunch(g.exec, s));
+}
+
+uint64_t hkey(std::initializer_list<uint64_t> v) {
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t x : v) {
+        h ^= x;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+template <class T>
+LevelCoeffs<T>& coeffs(cfx_matrix* mat, int lv);
+template <>
+LevelCoeffs<double>& coeffs<double>(cfx_matrix* mat, int lv) {
+    return mat->c64[lv];
+}
+template <>
+LevelCoeffs<float>& coeffs<float>(cfx_matrix* mat, int lv) {
+    return mat->c32[lv];
+}
+
+// Ensure coefficients of all levels exist in precision T (coarse assembly on
+// device from the level-0 FP64 coefficients; FP32 copies are cast from FP64).
+void prepare_levels(cfx_matrix* mat, bool want32) {
+    cfx_mesh* mesh = mat->mesh;
+    cudaStream_t s = mesh->ctx->stream;
+    const int nl = int(mesh->dev.size());
+    if ((int)mat->c64.size() < nl) {
+        for (int i = int(mat->c64.size()); i < nl; ++i) {
+            LevelCoeffs<double> c;
+            alloc_coeffs(mat->arena, mesh->dev[i], mat->sym, c);
+            mat->c64.push_back(c);
+        }
+        mat->coarse64 = false;
+    }
+    if (!mat->coarse64) {
+        for (int i = 1; i < nl; ++i) Ops<double>::coarsen(s, mesh->dev[i - 1], mat->c64[i - 1], mesh->dev[i], mat->c64[i]);
+        mat->coarse64 = true;
+    }
+    if (want32) {
+        if ((int)mat->c32.size() < nl) {
+            for (int i = int(mat->c32.size()); i < nl; ++i) {
+                LevelCoeffs<float> c;
+                alloc_coeffs(mat->arena, mesh->dev[i], mat->sym, c);
+                mat->c32.push_back(c);
+            }
+            mat->fine32 = mat->coarse32 = false;
+        }
+        if (!mat->fine32 || !mat->coarse32) {
+            for (int i = 0; i < nl; ++i) {
+                const LevelMesh& m = mesh->dev[i];
+                launch_cast_d2f(s, m.n, mat->c64[i].diag, mat->c32[i].diag);
+                launch_cast_d2f(s, m.nf, mat->c64[i].upper, mat->c32[i].upper);
+                launch_cast_d2f(s, m.nf, mat->c64[i].lowerPerm, mat->c32[i].lowerPerm);
+                if (!mat->sym) {
+                    launch_cast_d2f(s, m.nf, mat->c64[i].lower, mat->c32[i].lower);
+                    launch_cast_d2f(s, m.nf, mat->c64[i].upperPerm, mat->c32[i].upperPerm);
+                }
+                count_launch(mat->sym ? 3 : 5);
+            }
+            mat->fine32 = mat->coarse32 = true;
+        }
+    }
+}
+
+void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, const double* lower,
+                      cudaMemcpyKind kind) {
+    cfx_mesh* mesh = mat->mesh;
+    cudaStream_t s = mesh->ctx->stream;
+    const LevelMesh& m = mesh->dev[0];
+    LevelCoeffs<double>& c = mat->c64[0];
+    CK(cudaMemcpyAsync(c.diag, diag, sizeof(double) * m.n, kind, s));
+    if (m.nf) CK(cudaMemcpyAsync(c.upper, upper, sizeof(double) * m.nf, kind, s));
+    if (!mat->sym && m.nf) CK(cudaMemcpyAsync(c.lower, lower, sizeof(double) * m.nf, kind, s));
+    Ops<double>::permute(s, m, c);
+    mat->coarse64 = mat->coarse32 = mat->fine32 = false;
+}
+
+// rD of DIC / DILU (DICPreconditioner.C:57-84, DILUPreconditioner.C:57-85):
+// pivot sweep in level order, then the reciprocal.
+template <class T>
+cfx_status compute_rD(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c) {
+    SweepArgs<T> a{};
+    a.diag = c.diag;
+    a.lp = c.lowerPerm;
+    a.up = c.sym ? c.lowerPerm : c.upperPerm;
+    a.x = c.rD;
+    CFX_TRY(run_sweep<T>(ctx->stream, m, m.fwd, SW_RD, a, ctx->d_status));
+    Ops<T>::reciprocal(ctx->stream, m.n, c.rD);
+    return CFX_OK;
+}
+
+template <class T>
+void diag_reciprocal(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c) {
+    Kern<T>::copy(ctx->stream, m.n, c.diag, c.rD, nullptr);
+    Ops<T>::reciprocal(ctx->stream, m.n, c.rD);
+}
+
+// w = M^-1 r with the w.r dot partials in ctx->sc.chunkPartials.  Returns the
+// number of partials.
+template <class T>
+int precondition(cfx_ctx* ctx, const LevelMesh& m, const LevelCoeffs<T>& c, int kind, const T* r, T* w,
+                 const int* done, bool dot) {
+    cudaStream_t s = ctx->stream;
+    if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
+        SweepArgs<T> a{};
+        a.rD = c.rD;
+        a.lp = c.lowerPerm;
+        a.upper = c.upper;
+        a.in = r;
+        a.x = w;
+        a.done = done;
+        if (run_sweep<T>(s, m, m.fwd, SW_DIC_FWD, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
+        a.dotWith = dot ? r : nullptr;
+        a.chunkPartials = ctx->sc.chunkPartials;
+        if (run_sweep<T>(s, m, m.bwd, SW_BWD, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
+        return sweep_partials(m, m.bwd);
+    }
+    Kern<T>::precond_pointwise(s, m.n, kind == CFX_PRE_DIAGONAL ? c.rD : nullptr, r, w, ctx->sc.chunkPartials,
+                               done);
+    int g = (m.n + RED_NT - 1) / RED_NT;
+    return std::max(1, std::min(g, RED_MAXB));
+}
+
+void ensure_chunk_partials(cfx_ctx* ctx, const LevelMesh& m) {
+    const size_t need = std::max<size_t>(std::max(m.fwd.nChunks, m.bwd.nChunks), RED_MAXB) + 16;
+    if (ctx->sc.chunkPartialsCap < need) {
+        ctx->sc.chunkPartials = ctx->arena.get<double>(need);
+        ctx->sc.chunkPartialsCap = need;
+    }
+}
+
+template <class T>
+void setup_preconditioner(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c, int kind) {
+    if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
+        if (compute_rD<T>(ctx, m, c) != CFX_OK) throw CudaError(last_error());
+    } else if (kind == CFX_PRE_DIAGONAL) {
+        diag_reciprocal<T>(ctx, m, c);
+    }
+}
+
+// ----------------------------------------------------------- PCG / PBiCGStab
+// One Krylov solve in precision T on level lv of the matrix.  psi/b are T
+// device vectors; state in slot.
+template <class T>
+cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solver, int precond, T* psi, const T* b,
+                  int slot, double tol, double relTol, int maxIter, int minIter, const cfx_controls& ctl,
+                  SolveState* out) {
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const LevelMesh& m = mat->mesh->dev[lv];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    const int n = m.n;
+    W.n = std::max(W.n, n);
+    ensure_chunk_partials(ctx, m);
+    SolveState* st = ctx->d_state + slot;
+    set_state(ctx, slot, ctl, tol, relTol, maxIter, minIter);
+    T* r = W.get(0, n);
+    T* w = W.get(1, n);
+    T* p = W.get(2, n);
+    T* r0 = solver == CFX_SOLVER_PBICGSTAB ? W.get(3, n) : nullptr;
+    // Apsi into w; normFactor; r = b - Apsi
+    launch_reduce<T>(s, ctx->sc, 0, n, psi, nullptr, &st->red0);
+    count_launch();
+    Ops<T>::amul(s, m, c, psi, w);
+    Kern<T>::norm_init(s, ctx->sc, m, c, w, b, r, r0, st);
+    setup_preconditioner<T>(ctx, m, c, precond);
+    const int* done = &st->done;
+    int iters = 0;
+    if (solver == CFX_SOLVER_PBICGSTAB)
+        for (int i = 4; i < 8; ++i) W.get(i, n);
+    const uint64_t key = hkey({mat->mesh->version, uint64_t(small_sweep_threshold()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+                               reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
+                               reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD)});
+    auto body = [&]() {
+        if (solver == CFX_SOLVER_PCG) {
+            const int np = precondition<T>(ctx, m, c, precond, r, w, done, true);
+            Kern<T>::pcg_beta(s, np, ctx->sc.chunkPartials, st);
+            Kern<T>::pcg_p(s, n, w, p, st);
+            Kern<T>::pcg_amul(s, ctx->sc, m, c, p, w, st);
+            Kern<T>::pcg_update(s, ctx->sc, n, p, w, psi, r, st);
+        } else {
+            T* AyA = W.get(4, n);
+            T* sA = W.get(5, n);
+            T* zA = W.get(6, n);
+            T* tA = W.get(7, n);
+            T* yA = w;
+            Kern<T>::bicg_rho(s, ctx->sc, n, r0, r, st);
+            Kern<T>::bicg_p(s, n, r, AyA, p, st);
+            precondition<T>(ctx, m, c, precond, p, yA, done, false);
+            Kern<T>::bicg_amul_alpha(s, ctx->sc, m, c, yA, AyA, r0, st);
+            Kern<T>::bicg_s(s, ctx->sc, n, r, AyA, sA, st);
+            Kern<T>::bicg_early(s, n, yA, psi, st);
+            precondition<T>(ctx, m, c, precond, sA, zA, done, false);
+            Kern<T>::bicg_amul_omega(s, ctx->sc, m, c, zA, tA, sA, st);
+            Kern<T>::bicg_update(s, ctx->sc, n, yA, zA, sA, tA, psi, r, st);
+        }
+    };
+    // first read: was it converged at start?
+    SolveState h = read_state(ctx, slot);
+    int batch = 4;
+    while (!h.done) {
+        for (int k = 0; k < batch; ++k) graph_launch(gc, key, s, body);
+        iters += batch;
+        h = read_state(ctx, slot);
+        const int stc = read_status(ctx);
+        if (stc != 0) return cfx_status(stc);
+        batch = std::min(64, std::max(4, h.nIterations / 4));
+        if (iters > 4 * maxIter + 1024) {
+            set_error("iteration loop did not terminate");
+            return CFX_ERR_STATE;
+        }
+    }
+    *out = h;
+    return CFX_OK;
+}
+
+// ---------------------------------------------------------------------- GAMG
+template <class T>
+void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b, int nSweeps, Work<T>& LW) {
+    const LevelMesh& m = mat->mesh->dev[lv];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    cudaStream_t s = ctx->stream;
+    for (int k = 0; k < nSweeps; ++k) {
+        if (kind == CFX_SMOOTH_GS) {
+            // GaussSeidelSmoother.C:125-177
+            SweepArgs<T> a{};
+            a.diag = c.diag;
+            a.lp = c.lowerPerm;
+            a.upper = c.upper;
+            a.in = b;
+            a.x = psi;
+            if (run_sweep<T>(s, m, m.fwd, SW_GS, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
+        } else {
+            // DICSmoother.C:86-115: rA = b - A psi; rA = M^-1 rA; psi += rA
+            T* rA = LW.get(0, m.n);
+            T* wA = LW.get(1, m.n);
+            Ops<T>::residual(s, m, c, psi, b, rA);
+            precondition<T>(ctx, m, c, CFX_PRE_DIC, rA, wA, nullptr, false);
+            Kern<T>::axpy(s, m.n, T(1), wA, psi, nullptr);
+        }
+    }
+}
+
+// GAMGSolver::scale (GAMGSolverScale.C:31-76), optionally adding `pre`.
+template <class T>
+void scale(cfx_ctx* ctx, cfx_matrix* mat, int lv, T* field, T* Acf, const T* source, const T* pre, SolveState* st) {
+    const LevelMesh& m = mat->mesh->dev[lv];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    Kern<T>::gamg_scale_sf(ctx->stream, ctx->sc, m, c, field, Acf, source, st);
+    Kern<T>::gamg_scale_apply(ctx->stream, m.n, field, Acf, source, c.diag, pre, st);
+}
+
+template <class T>
+struct GamgCycle {
+    cfx_ctx* ctx;
+    cfx_matrix* mat;
+    const cfx_controls* ctl;
+    int coarsest;         // index of the coarsest coarse level li (matrix level coarsest+1)
+    bool scaleCorr;
+    std::vector<T*> corr, src;
+    T *Apsi, *fcorr, *scratch2;
+    BlockSys<T>* d_blk;
+    SolveState* st;
+
+    // One V-cycle (GAMGSolverSolve.C:148-443) for psi with source b and
+    // current finest residual fres.
+    void enqueue(T* psi, const T* b, const T* fres) {
+        cudaStream_t s = ctx->stream;
+        cfx_mesh* mesh = mat->mesh;
+        const int smoother = ctl->smoother;
+        Ops<T>::restrict_field(s, mesh->dev[0], fres, src[0]);
+        for (int li = 0; li < coarsest; ++li) {
+            const int lv = li + 1;
+            const int nc = mesh->dev[lv].n;
+            if (ctl->nPreSweeps) {
+                Kern<T>::fill(s, nc, T(0), corr[li], nullptr);
+                smooth<T>(ctx, mat, lv, smoother, corr[li], src[li],
+                          std::min(ctl->nPreSweeps + ctl->preSweepsLevelMultiplier * li, ctl->maxPreSweeps),
+                          workFor(lv));
+                if (scaleCorr && li < coarsest - 1) scale<T>(ctx, mat, lv, corr[li], Apsi, src[li], nullptr, st);
+                Ops<T>::amul(s, mesh->dev[lv], coeffs<T>(mat, lv), corr[li], Apsi);
+                Kern<T>::axpy(s, nc, T(-1), Apsi, src[li], nullptr);
+            }
+            Ops<T>::restrict_field(s, mesh->dev[lv], src[li], src[li + 1]);
+        }
+        // solveCoarsestLevel (GAMGSolverSolve.C:520-552): PCG+DIC or
+        // PBiCGStab+DILU from zero at the GAMG tolerances, one CTA.
+        Kern<T>::fill(s, mesh->dev[coarsest + 1].n, T(0), corr[coarsest], nullptr);
+        Kern<T>::block_solve(s, d_blk, 1, nullptr);
+        for (int li = coarsest - 1; li >= 0; --li) {
+            const int lv = li + 1;
+            const int nc = mesh->dev[lv].n;
+            T* pre = nullptr;
+            if (ctl->nPreSweeps) {
+                Kern<T>::copy(s, nc, corr[li], scratch2, nullptr);
+                pre = scratch2;
+            }
+            Ops<T>::prolong_field(s, mesh->dev[lv], corr[li + 1], corr[li]);
+            if (scaleCorr && li < coarsest - 1) {
+                scale<T>(ctx, mat, lv, corr[li], Apsi, src[li], pre, st);
+            } else if (pre) {
+                Kern<T>::axpy(s, nc, T(1), pre, corr[li], nullptr);
+            }
+            smooth<T>(ctx, mat, lv, smoother, corr[li], src[li],
+                      std::min(ctl->nPostSweeps + ctl->postSweepsLevelMultiplier * li, ctl->maxPostSweeps),
+                      workFor(lv));
+        }
+        Ops<T>::prolong_field(s, mesh->dev[0], corr[0], fcorr);
+        if (scaleCorr) scale<T>(ctx, mat, 0, fcorr, Apsi, fres, nullptr, st);
+    }
+
+    Work<T>& workFor(int lv);
+};
+
+template <>
+Work<double>& GamgCycle<double>::workFor(int lv) {
+    return mat->lv64[lv];
+}
+template <>
+Work<float>& GamgCycle<float>::workFor(int lv) {
+    return mat->lv32[lv];
+}
+
+template <class T>
+BlockSys<T>* block_sys(cfx_matrix* mat);
+template <>
+BlockSys<double>* block_sys<double>(cfx_matrix* mat) {
+    if (!mat->d_blk64) mat->d_blk64 = mat->blockArena.get<BlockSys<double>>(1);
+    return mat->d_blk64;
+}
+template <>
+BlockSys<float>* block_sys<float>(cfx_matrix* mat) {
+    if (!mat->d_blk32) mat->d_blk32 = mat->blockArena.get<BlockSys<float>>(1);
+    return mat->d_blk32;
+}
+
+constexpr int G0 = 1000;  // GAMG work-vector slots (apart from the Krylov ones)
+
+template <class T>
+void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Work<T>& W, SolveState* st) {
+    cfx_mesh* mesh = mat->mesh;
+    cfx_ctx* ctx = mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const int nl = int(mesh->dev.size());
+    cy.ctx = ctx;
+    cy.mat = mat;
+    cy.ctl = ctl;
+    cy.coarsest = nl - 2;
+    cy.scaleCorr = ctl->scaleCorrection < 0 ? mat->sym : ctl->scaleCorrection != 0;
+    cy.st = st;
+    int maxSize = 0;
+    for (int i = 0; i < nl; ++i) maxSize = std::max(maxSize, mesh->dev[i].n);
+    W.n = std::max(W.n, maxSize);
+    cy.corr.assign(nl - 1, nullptr);
+    cy.src.assign(nl - 1, nullptr);
+    for (int li = 0; li < nl - 1; ++li) {
+        cy.corr[li] = W.get(G0 + 10 + 2 * li, mesh->dev[li + 1].n);
+        cy.src[li] = W.get(G0 + 11 + 2 * li, mesh->dev[li + 1].n);
+    }
+    cy.Apsi = W.get(G0 + 0, maxSize);
+    cy.fcorr = W.get(G0 + 1, maxSize);
+    cy.scratch2 = W.get(G0 + 2, maxSize);
+    // smoother / coarsest-solver set-up on every level (initVcycle: the
+    // smoothers are constructed per solve, so DIC rD is recomputed)
+    for (int lv = 0; lv < nl; ++lv) {
+        ensure_chunk_partials(ctx, mesh->dev[lv]);
+        if (ctl->smoother == CFX_SMOOTH_DIC) {
+            if (compute_rD<T>(ctx, mesh->dev[lv], coeffs<T>(mat, lv)) != CFX_OK) throw CudaError(last_error());
+            cy.workFor(lv).get(0, mesh->dev[lv].n);  // allocated before graph capture
+            cy.workFor(lv).get(1, mesh->dev[lv].n);
+        }
+    }
+    const int lc = nl - 1;
+    const LevelMesh& m = mesh->dev[lc];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lc);
+    if (ctl->smoother != CFX_SMOOTH_DIC)
+        if (compute_rD<T>(ctx, m, c) != CFX_OK) throw CudaError(last_error());
+    BlockSys<T> h{};
+    h.n = m.n;
+    h.nf = m.nf;
+    h.ownerStart = m.ownerStart;
+    h.losortStart = m.losortStart;
+    h.losortL = m.losortL;
+    h.u = m.u;
+    h.fwdCells = m.fwd.cells;
+    h.fwdLevelStart = m.fwd.levelStart;
+    h.nFwd = m.fwd.nLevels;
+    h.bwdCells = m.bwd.cells;
+    h.bwdLevelStart = m.bwd.levelStart;
+    h.nBwd = m.bwd.nLevels;
+    h.diag = c.diag;
+    h.lp = c.lowerPerm;
+    h.upper = c.upper;
+    h.rD = c.rD;
+    h.b = cy.src[lc - 1];
+    h.psi = cy.corr[lc - 1];
+    h.r = W.get(G0 + 3, m.n);
+    h.w = W.get(G0 + 4, m.n);
+    h.p = W.get(G0 + 5, m.n);
+    h.q = W.get(G0 + 6, m.n);
+    h.s = W.get(G0 + 7, m.n);
+    h.t = W.get(G0 + 8, m.n);
+    h.r0 = W.get(G0 + 9, m.n);
+    h.tolerance = ctl->tolerance;
+    h.relTol = ctl->relTol;
+    h.maxIter = 1000;  // lduMatrix::solver::defaultMaxIter_ (lduMatrix.C:38)
+    h.minIter = 0;
+    h.precond = mat->sym ? CFX_PRE_DIC : CFX_PRE_DILU;
+    h.solver = mat->sym ? CFX_SOLVER_PCG : CFX_SOLVER_PBICGSTAB;
+    cy.d_blk = block_sys<T>(mat);
+    CK(cudaMemcpyAsync(cy.d_blk, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // h is a stack object
+}
+
+cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, const double* b, cfx_perf* perf) {
+    cfx_mesh* mesh = mat->mesh;
+    cfx_ctx* ctx = mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    if (mesh->nCoarseLevels < 1) {
+        set_error("No coarse levels created, either matrix too small for GAMG or nCellsInCoarsestLevel too large");
+        return CFX_ERR_STATE;
+    }
+    const bool mixed = ctl.precision == CFX_MIXED;
+    prepare_levels(mat, mixed);
+    const int nl = int(mesh->dev.size());
+    if ((int)mat->lv64.size() < nl) mat->lv64.resize(nl);
+    if ((int)mat->lv32.size() < nl) mat->lv32.resize(nl);
+    const LevelMesh& m0 = mesh->dev[0];
+    const int n = m0.n;
+    SolveState* st = ctx->d_state;
+    set_state(ctx, 0, ctl, ctl.tolerance, ctl.relTol, ctl.maxIter, ctl.minIter);
+    Work<double>& W = mat->w64;
+    W.n = std::max(W.n, n);
+    double* Apsi = W.get(200, n);
+    double* fres = W.get(201, n);
+    launch_reduce<double>(s, ctx->sc, 0, n, psi, nullptr, &st->red0);
+    count_launch();
+    Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
+    Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+                         uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
+                         uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
+                         uint64_t(ctl.scaleCorrection + 7), uint64_t(mixed), reinterpret_cast<uint64_t>(psi),
+                         reinterpret_cast<uint64_t>(b)});
+    SolveState h = read_state(ctx, 0);
+    if (!mixed) {
+        GamgCycle<double> cy;
+        setup_cycle<double>(cy, mat, &ctl, mat->w64, st);
+        auto body = [&]() {
+            cy.enqueue(psi, b, fres);
+            // psi += finestCorrection; smoothers[0].smooth(nFinestSweeps)
+            Kern<double>::axpy(s, n, 1.0, cy.fcorr, psi, nullptr);
+            smooth<double>(ctx, mat, 0, ctl.smoother, psi, b, ctl.nFinestSweeps, mat->lv64[0]);
+            Kern<double>::gamg_residual_check(s, ctx->sc, m0, mat->c64[0], psi, b, fres, st);
+        };
+        while (!h.done) {
+            graph_launch(mat->gGAMG, key, s, body);
+            h = read_state(ctx, 0);
+            const int stc = read_status(ctx);
+            if (stc != 0) return cfx_status(stc);
+        }
+    } else {
+        // FP32 V-cycle on the residual equation A e = r inside an FP64
+        // refinement loop: e = S(0 + C(r)) equals the FP64 cycle's
+        // psi_new - psi in exact arithmetic (Gauss-Seidel is affine).
+        GamgCycle<float> cy;
+        setup_cycle<float>(cy, mat, &ctl, mat->w32, st);
+        Work<float>& W32 = mat->w32;
+        float* r32 = W32.get(201, n);
+        float* e32 = cy.fcorr;
+        auto body = [&]() {
+            launch_cast_pred(s, n, fres, r32, nullptr);
+            cy.enqueue(nullptr, nullptr, r32);
+            smooth<float>(ctx, mat, 0, ctl.smoother, e32, r32, ctl.nFinestSweeps, mat->lv32[0]);
+            launch_add_f2d(s, n, e32, psi, nullptr);
+            Kern<double>::gamg_residual_check(s, ctx->sc, m0, mat->c64[0], psi, b, fres, st);
+        };
+        while (!h.done) {
+            graph_launch(mat->gMixed, key, s, body);
+            h = read_state(ctx, 0);
+            const int stc = read_status(ctx);
+            if (stc != 0) return cfx_status(stc);
+        }
+    }
+    std::snprintf(perf->solverName, sizeof(perf->solverName), "GAMG");
+    perf->initialResidual = h.initialResidual;
+    perf->finalResidual = h.finalResidual;
+    perf->nIterations = h.nIterations;
+    perf->converged = h.converged;
+    perf->singular = h.singular;
+    perf->nOuter = mixed ? h.nIterations : 0;
+    return CFX_OK;
+}
+
+const char* pre_name(int p) {
+    switch (p) {
+        case CFX_PRE_NONE: return "none";
+        case CFX_PRE_DIAGONAL: return "diagonal";
+        case CFX_PRE_DIC: return "DIC";
+        default: return "DILU";
+    }
+}
+
+cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, const double* b, cfx_perf* perf) {
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = mat->mesh->dev[0].n;
+    SolveState h{};
+    if (ctl.precision != CFX_MIXED) {
+        CFX_TRY(krylov<double>(mat, mat->w64, ctl.solver == CFX_SOLVER_PCG ? mat->gPCG : mat->gBiCG, 0, ctl.solver,
+                               ctl.preconditioner, psi, b, 0, ctl.tolerance, ctl.relTol, ctl.maxIter, ctl.minIter,
+                               ctl, &h));
+        perf->nOuter = 0;
+    } else {
+        // FP64 iterative refinement around an FP32 Krylov solve of A e = r:
+        // the outer residual, solution, normFactor and convergence test are
+        // FP64 (the reference's definitions); the inner solve reduces the
+        // residual by innerRelTol.
+        prepare_levels(mat, true);
+        const LevelMesh& m = mat->mesh->dev[0];
+        Work<double>& W = mat->w64;
+        W.n = std::max(W.n, n);
+        double* Apsi = W.get(300, n);
+        double* r64 = W.get(301, n);
+        float* r32 = mat->w32.get(300, n);
+        float* e32 = mat->w32.get(301, n);
+        SolveState* st = ctx->d_state;
+        set_state(ctx, 0, ctl, ctl.tolerance, ctl.relTol, ctl.maxIter, ctl.minIter);
+        launch_reduce<double>(s, ctx->sc, 0, n, psi, nullptr, &st->red0);
+        count_launch();
+        Ops<double>::amul(s, m, mat->c64[0], psi, Apsi);
+        Kern<double>::norm_init(s, ctx->sc, m, mat->c64[0], Apsi, b, r64, nullptr, st);
+        h = read_state(ctx, 0);
+        int inner = 0, outer = 0;
+        const double innerRelTol = 1e-3;
+        while (!h.done) {
+            launch_cast_d2f(s, n, r64, r32);
+            Kern<float>::fill(s, n, 0.0f, e32, nullptr);
+            SolveState hi{};
+            CFX_TRY(krylov<float>(mat, mat->w32, ctl.solver == CFX_SOLVER_PCG ? mat->gPCG : mat->gBiCG, 0, ctl.solver,
+                                  ctl.preconditioner, e32, r32, 1, 0.0, innerRelTol, ctl.maxIter, 0, ctl, &hi));
+            inner += hi.nIterations;
+            launch_add_f2d(s, n, e32, psi, nullptr);
+            // outer: r = b - A psi, |r|/normFactor, one refinement step
+            Kern<double>::gamg_residual_check(s, ctx->sc, m, mat->c64[0], psi, b, r64, st);
+            h = read_state(ctx, 0);
+            ++outer;
+            if (hi.singular || hi.nIterations == 0) break;
+        }
+        h.nIterations = inner;
+        perf->nOuter = outer;
+    }
+    const char* base = ctl.solver == CFX_SOLVER_PCG ? "PCG" : "PBiCGStab";
+    std::snprintf(perf->solverName, sizeof(perf->solverName), "%s%s", pre_name(ctl.preconditioner), base);
+    perf->initialResidual = h.initialResidual;
+    perf->finalResidual = h.finalResidual;
+    perf->nIterations = h.nIterations;
+    perf->converged = h.converged;
+    perf->singular = h.singular;
+    return CFX_OK;
+}
+
+cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
+    if (!c) {
+        set_error("null controls");
+        return CFX_ERR_ARG;
+    }
+    if (c->solver < 0 || c->solver > 2 || c->preconditioner < 0 || c->preconditioner > 3 || c->smoother < 0 ||
+        c->smoother > 1 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
+        set_error("unknown solver, preconditioner, smoother or precision");
+        return CFX_ERR_CONFIG;
+    }
+    // lduMatrix::solver::New (lduMatrixSolver.C:67-120): PCG is registered
+    // for symmetric matrices only; DIC only for symmetric, DILU for asymmetric.
+    if (c->solver == CFX_SOLVER_PCG && !mat->sym) {
+        set_error("Unknown asymmetric matrix solver cudaPCG");
+        return CFX_ERR_CONFIG;
+    }
+    if (c->solver != CFX_SOLVER_GAMG) {
+        if (c->preconditioner == CFX_PRE_DIC && !mat->sym) {
+            set_error("Unknown asymmetric matrix preconditioner DIC");
+            return CFX_ERR_CONFIG;
+        }
+        if (c->preconditioner == CFX_PRE_DILU && mat->sym) {
+            set_error("Unknown symmetric matrix preconditioner DILU");
+            return CFX_ERR_CONFIG;
+        }
+    } else if (c->smoother == CFX_SMOOTH_DIC && !mat->sym) {
+        set_error("Unknown asymmetric matrix smoother DIC");
+        return CFX_ERR_CONFIG;
+    }
+    return CFX_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+void cfx_default_controls(cfx_controls* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->solver = CFX_SOLVER_PCG;
+    c->preconditioner = CFX_PRE_DIC;
+    c->tolerance = 1e-6;
+    c->relTol = 0.0;
+    c->maxIter = 1000;
+    c->minIter = 0;
+    c->smoother = CFX_SMOOTH_GS;
+    c->nPreSweeps = 0;
+    c->preSweepsLevelMultiplier = 1;
+    c->maxPreSweeps = 4;
+    c->nPostSweeps = 2;
+    c->postSweepsLevelMultiplier = 1;
+    c->maxPostSweeps = 4;
+    c->nFinestSweeps = 2;
+    c->scaleCorrection = -1;
+    c->nCellsInCoarsestLevel = 10;
+    c->precision = CFX_FP64;
+}
+
+const char* cfx_last_error(void) { return cfx::last_error(); }
+int cfx_version(void) { return 100; }
+
+cfx_status cfx_ctx_create(int device, cfx_ctx** out) {
+    if (!out) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        auto ctx = std::make_unique<cfx_ctx>();
+        ctx->device = device;
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        set_num_sms(sms);
+        ctx->sc.partials = ctx->arena.get<double>(RED_MAXB * 4);
+        ctx->sc.counters = ctx->arena.get<unsigned>(16);
+        ctx->sc.result = ctx->arena.get<double>(16);
+        CK(cudaMemset(ctx->sc.counters, 0, 16 * sizeof(unsigned)));
+        ctx->d_state = ctx->arena.get<SolveState>(4);
+        ctx->d_status = ctx->arena.get<int>(1);
+        CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+        ctx->d_red = ctx->arena.get<double>(8);
+        CK(cudaMallocHost(&ctx->h_state, 4 * sizeof(SolveState)));
+        CK(cudaMallocHost(&ctx->h_red, 8 * sizeof(double)));
+        *out = ctx.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_ctx_destroy(cfx_ctx* ctx) {
+    if (!ctx) return CFX_ERR_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFreeHost(ctx->h_state);
+    cudaFreeHost(ctx->h_red);
+    ctx->arena.release();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CFX_OK;
+}
+
+cfx_status cfx_ctx_stream(cfx_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return CFX_ERR_ARG;
+    *stream = ctx->stream;
+    return CFX_OK;
+}
+
+cfx_status cfx_ctx_synchronize(cfx_ctx* ctx) {
+    if (!ctx) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        CK(cudaStreamSynchronize(ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_ctx_launch_count(cfx_ctx* ctx, int64_t* count) {
+    if (!ctx || !count) return CFX_ERR_ARG;
+    *count = launch_count();
+    return CFX_OK;
+}
+
+cfx_status cfx_mesh_create(cfx_ctx* ctx, int nCells, int nFaces, const int32_t* l, const int32_t* u,
+                           cfx_mesh** out) {
+    if (!ctx || !out || nCells < 1) {
+        set_error("cfx_mesh_create: bad argument");
+        return CFX_ERR_ARG;
+    }
+    return guard([&]() -> cfx_status {
+        auto mesh = std::make_unique<cfx_mesh>();
+        mesh->ctx = ctx;
+        HostLevel h;
+        CFX_TRY(build_host_level(nCells, nFaces, l, u, h, true));
+        mesh->host.push_back(std::move(h));
+        LevelMesh m;
+        upload_level(mesh->arena, ctx->stream, mesh->host[0], m);
+        mesh->dev.push_back(m);
+        CK(cudaStreamSynchronize(ctx->stream));
+        *out = mesh.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_mesh_destroy(cfx_mesh* mesh) {
+    if (!mesh) return CFX_ERR_ARG;
+    cudaStreamSynchronize(mesh->ctx->stream);
+    delete mesh;
+    return CFX_OK;
+}
+
+cfx_status cfx_mesh_info(cfx_mesh* mesh, int* nFwd, int* nBwd) {
+    if (!mesh) return CFX_ERR_ARG;
+    if (nFwd) *nFwd = mesh->dev[0].fwd.nLevels;
+    if (nBwd) *nBwd = mesh->dev[0].bwd.nLevels;
+    return CFX_OK;
+}
+
+cfx_status cfx_face_area_pair_weights(int nFaces, const double* Sf, double* w) {
+    if (nFaces < 0 || (nFaces && (!Sf || !w))) return CFX_ERR_ARG;
+    face_area_pair_weights(nFaces, Sf, w);
+    return CFX_OK;
+}
+
+cfx_status cfx_gamg_agglomerate(cfx_mesh* mesh, const double* weights, int nCellsInCoarsestLevel, int forwardStart) {
+    if (!mesh || (!weights && mesh->host[0].nf)) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        // pairGAMGAgglomeration::agglomerate (pairGAMGAgglomerate.C:31-118),
+        // mergeLevels 1, maxLevels 50, continueAgglomerating (GAMGAgglomeration.C:205-230)
+        std::vector<std::vector<int>> maps;
+        std::vector<int> nCoarse;
+        bool forward = forwardStart != 0;
+        std::vector<double> w(weights, weights + mesh->host[0].nf);
+        int fn = mesh->host[0].n;
+        std::vector<int> fl = mesh->host[0].l, fu = mesh->host[0].u;
+        while (int(maps.size()) < MAX_LEVELS - 1) {
+            std::vector<int> map;
+            const int nc = pair_agglomerate(fn, int(fl.size()), fl.data(), fu.data(), w.data(), forward, map);
+            if (!(nc >= nCellsInCoarsestLevel && nc < fn)) break;
+            std::vector<int> cl, cu, fra, flip;
+            const int ncf = agglomerate_addressing(int(fl.size()), fl.data(), fu.data(), map, nc, cl, cu, fra, flip);
+            std::vector<double> cw(ncf, 0.0);
+            for (size_t f = 0; f < fra.size(); ++f)
+                if (fra[f] >= 0) cw[fra[f]] += w[f];
+            maps.push_back(std::move(map));
+            nCoarse.push_back(nc);
+            w.swap(cw);
+            fl.swap(cl);
+            fu.swap(cu);
+            fn = nc;
+        }
+        if (maps.empty()) {
+            set_error("No coarse levels created, either matrix too small for GAMG or nCellsInCoarsestLevel too large");
+            return CFX_ERR_STATE;
+        }
+        CFX_TRY(build_hierarchy(mesh, maps, nCoarse));
+        CK(cudaStreamSynchronize(mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_gamg_set_levels(cfx_mesh* mesh, int nLevels, const int32_t* const* restrictAddr,
+                               const int32_t* nCoarseCells) {
+    if (!mesh || nLevels < 1 || nLevels >= MAX_LEVELS || !restrictAddr || !nCoarseCells) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        std::vector<std::vector<int>> maps;
+        std::vector<int> nCoarse;
+        int fn = mesh->host[0].n;
+        for (int i = 0; i < nLevels; ++i) {
+            maps.emplace_back(restrictAddr[i], restrictAddr[i] + fn);
+            nCoarse.push_back(nCoarseCells[i]);
+            fn = nCoarseCells[i];
+        }
+        CFX_TRY(build_hierarchy(mesh, maps, nCoarse));
+        CK(cudaStreamSynchronize(mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_gamg_n_levels(cfx_mesh* mesh, int* n) {
+    if (!mesh || !n) return CFX_ERR_ARG;
+    *n = mesh->nCoarseLevels;
+    return CFX_OK;
+}
+
+cfx_status cfx_gamg_level_info(cfx_mesh* mesh, int level, int* nCells, int* nFaces, int32_t* restrictAddr,
+                               int32_t* faceRestrict, int32_t* faceFlip, int32_t* coarseL, int32_t* coarseU) {
+    if (!mesh || level < 0 || level >= mesh->nCoarseLevels) return CFX_ERR_ARG;
+    const HostLevel& f = mesh->host[level];
+    const HostLevel& c = mesh->host[level + 1];
+    if (nCells) *nCells = c.n;
+    if (nFaces) *nFaces = c.nf;
+    if (restrictAddr) std::copy(f.restrictAddr.begin(), f.restrictAddr.end(), restrictAddr);
+    if (faceRestrict) std::copy(f.faceRestrict.begin(), f.faceRestrict.end(), faceRestrict);
+    if (faceFlip) std::copy(f.faceFlip.begin(), f.faceFlip.end(), faceFlip);
+    if (coarseL) std::copy(c.l.begin(), c.l.end(), coarseL);
+    if (coarseU) std::copy(c.u.begin(), c.u.end(), coarseU);
+    return CFX_OK;
+}
+
+cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* upper, const double* lower,
+                             cfx_matrix** out) {
+    if (!mesh || !out || !diag || (!upper && mesh->host[0].nf)) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        auto mat = std::make_unique<cfx_matrix>();
+        mat->mesh = mesh;
+        mat->sym = lower == nullptr;
+        LevelCoeffs<double> c;
+        alloc_coeffs(mat->arena, mesh->dev[0], mat->sym, c);
+        mat->c64.push_back(c);
+        const int n = mesh->dev[0].n;
+        mat->d_psi = mat->arena.get<double>(n);
+        mat->d_src = mat->arena.get<double>(n);
+        set_coefficients(mat.get(), diag, upper, lower, cudaMemcpyHostToDevice);
+        CK(cudaStreamSynchronize(mesh->ctx->stream));
+        *out = mat.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper, const double* lower) {
+    if (!mat || !diag || (mat->sym != (lower == nullptr))) {
+        set_error("cfx_matrix_update: symmetry of the coefficients changed or null diag");
+        return CFX_ERR_ARG;
+    }
+    return guard([&]() -> cfx_status {
+        set_coefficients(mat, diag, upper, lower, cudaMemcpyHostToDevice);
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* diag, const double* upper, const double* lower) {
+    if (!mat || !diag || (mat->sym != (lower == nullptr))) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        set_coefficients(mat, diag, upper, lower, cudaMemcpyDeviceToDevice);
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_matrix_destroy(cfx_matrix* mat) {
+    if (!mat) return CFX_ERR_ARG;
+    cudaStreamSynchronize(mat->mesh->ctx->stream);
+    delete mat;
+    return CFX_OK;
+}
+
+cfx_status cfx_matrix_coarse(cfx_matrix* mat, int level, double* diag, double* upper, double* lower) {
+    if (!mat || level < 1 || level > mat->mesh->nCoarseLevels) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        prepare_levels(mat, false);
+        const LevelMesh& m = mat->mesh->dev[level];
+        cudaStream_t s = mat->mesh->ctx->stream;
+        const LevelCoeffs<double>& c = mat->c64[level];
+        if (diag) CK(cudaMemcpyAsync(diag, c.diag, sizeof(double) * m.n, cudaMemcpyDeviceToHost, s));
+        if (upper && m.nf) CK(cudaMemcpyAsync(upper, c.upper, sizeof(double) * m.nf, cudaMemcpyDeviceToHost, s));
+        if (lower && !mat->sym && m.nf)
+            CK(cudaMemcpyAsync(lower, c.lower, sizeof(double) * m.nf, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_psi, const double* d_source,
+                            cfx_perf* perf) {
+    if (!mat || !d_psi || !d_source || !perf) return CFX_ERR_ARG;
+    CFX_TRY(check_controls(mat, ctl));
+    std::memset(perf, 0, sizeof(*perf));
+    const cfx_status st = guard([&]() -> cfx_status {
+        CK(cudaMemsetAsync(mat->mesh->ctx->d_status, 0, sizeof(int), mat->mesh->ctx->stream));
+        if (ctl->solver == CFX_SOLVER_GAMG) return gamg_solve(mat, *ctl, d_psi, d_source, perf);
+        return krylov_solve(mat, *ctl, d_psi, d_source, perf);
+    });
+    perf->status = st;
+    return st;
+}
+
+cfx_status cfx_solve(cfx_matrix* mat, const cfx_controls* ctl, double* psi, const double* source, cfx_perf* perf) {
+    if (!mat || !psi || !source || !perf) return CFX_ERR_ARG;
+    const int n = mat->mesh->dev[0].n;
+    cudaStream_t s = mat->mesh->ctx->stream;
+    cfx_status st = guard([&]() -> cfx_status {
+        CK(cudaMemcpyAsync(mat->d_psi, psi, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(mat->d_src, source, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        return CFX_OK;
+    });
+    if (st != CFX_OK) return st;
+    st = cfx_solve_device(mat, ctl, mat->d_psi, mat->d_src, perf);
+    const cfx_status st2 = guard([&]() -> cfx_status {
+        CK(cudaMemcpyAsync(psi, mat->d_psi, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        return CFX_OK;
+    });
+    return st != CFX_OK ? st : st2;
+}
+
+cfx_status cfx_tune_set(int key, int value) {
+    if (key != CFX_TUNE_SMALL_SWEEP || value < 0) return CFX_ERR_ARG;
+    set_small_sweep_threshold(value);
+    return CFX_OK;
+}
+
+cfx_status cfx_tune_get(int key, int* value) {
+    if (key != CFX_TUNE_SMALL_SWEEP || !value) return CFX_ERR_ARG;
+    *value = small_sweep_threshold();
+    return CFX_OK;
+}
+
+// ---------------------------------------------------------- single operations
+cfx_status cfx_amul(cfx_matrix* mat, const double* x, double* y) {
+    if (!mat || !x || !y) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        Ops<double>::amul(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, y);
+        CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_tmul(cfx_matrix* mat, const double* x, double* y) {
+    if (!mat || !x || !y) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        Ops<double>::tmul(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, y);
+        CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_residual(cfx_matrix* mat, const double* x, const double* b, double* r) {
+    if (!mat || !x || !b || !r) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        Ops<double>::residual(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, b, r);
+        CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_sumA(cfx_matrix* mat, double* s) {
+    if (!mat || !s) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        Ops<double>::sumA(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], s);
+        CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_reduce(cfx_ctx* ctx, int which, int n, const double* a, const double* b, double* out) {
+    if (!ctx || !a || !out || which < 0 || which > 3 || (which == 3 && !b) || n < 0) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        launch_reduce<double>(ctx->stream, ctx->sc, which, n, a, b, ctx->d_red);
+        count_launch();
+        CK(cudaMemcpyAsync(ctx->h_red, ctx->d_red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        *out = ctx->h_red[0];
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_norm_factor(cfx_matrix* mat, const double* psi, const double* b, double* out) {
+    if (!mat || !psi || !b || !out) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        cudaStream_t s = ctx->stream;
+        const LevelMesh& m = mat->mesh->dev[0];
+        Work<double>& W = mat->w64;
+        W.n = std::max(W.n, m.n);
+        double* Apsi = W.get(400, m.n);
+        double* r = W.get(401, m.n);
+        cfx_controls c;
+        cfx_default_controls(&c);
+        set_state(ctx, 2, c, 0.0, 0.0, 1, 0);
+        SolveState* st = ctx->d_state + 2;
+        launch_reduce<double>(s, ctx->sc, 0, m.n, psi, nullptr, &st->red0);
+        count_launch();
+        Ops<double>::amul(s, m, mat->c64[0], psi, Apsi);
+        Kern<double>::norm_init(s, ctx->sc, m, mat->c64[0], Apsi, b, r, nullptr, st);
+        *out = read_state(ctx, 2).normFactor;
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_reciprocal_d(cfx_matrix* mat, int kind, double* rD) {
+    if (!mat || !rD) return CFX_ERR_ARG;
+    if ((kind == CFX_PRE_DIC && !mat->sym) || (kind == CFX_PRE_DILU && mat->sym) ||
+        (kind != CFX_PRE_DIC && kind != CFX_PRE_DILU && kind != CFX_PRE_DIAGONAL))
+        return CFX_ERR_CONFIG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        const LevelMesh& m = mat->mesh->dev[0];
+        ensure_chunk_partials(ctx, m);
+        setup_preconditioner<double>(ctx, m, mat->c64[0], kind);
+        CK(cudaMemcpyAsync(rD, mat->c64[0].rD, sizeof(double) * m.n, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        const int stc = read_status(ctx);
+        return stc ? cfx_status(stc) : CFX_OK;
+    });
+}
+
+cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const double* r, double* w) {
+    if (!mat || !r || !w) return CFX_ERR_ARG;
+    if (transpose) {
+        set_error("preconditionT is used by PBiCG only, which this library does not provide");
+        return CFX_ERR_CONFIG;
+    }
+    if ((kind == CFX_PRE_DIC && !mat->sym) || (kind == CFX_PRE_DILU && mat->sym) || kind < 0 || kind > 3)
+        return CFX_ERR_CONFIG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        const LevelMesh& m = mat->mesh->dev[0];
+        ensure_chunk_partials(ctx, m);
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        setup_preconditioner<double>(ctx, m, mat->c64[0], kind);
+        precondition<double>(ctx, m, mat->c64[0], kind, r, w, nullptr, false);
+        CK(cudaStreamSynchronize(ctx->stream));
+        const int stc = read_status(ctx);
+        return stc ? cfx_status(stc) : CFX_OK;
+    });
+}
+
+cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, int nSweeps) {
+    if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
+    if (kind != CFX_SMOOTH_GS && kind != CFX_SMOOTH_DIC) return CFX_ERR_CONFIG;
+    if (kind == CFX_SMOOTH_DIC && !mat->sym) return CFX_ERR_CONFIG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        const LevelMesh& m = mat->mesh->dev[0];
+        ensure_chunk_partials(ctx, m);
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        if ((int)mat->lv64.size() < 1) mat->lv64.resize(1);
+        if (kind == CFX_SMOOTH_DIC) setup_preconditioner<double>(ctx, m, mat->c64[0], CFX_PRE_DIC);
+        smooth<double>(ctx, mat, 0, kind, psi, b, nSweeps, mat->lv64[0]);
+        CK(cudaStreamSynchronize(ctx->stream));
+        const int stc = read_status(ctx);
+        return stc ? cfx_status(stc) : CFX_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,222 @@
+// host.cpp - host-side addressing: validation, derived LDU addressing, level
+// schedules, pairwise agglomeration and coarse-level addressing.
+//
+// The agglomeration is sequential by nature (each pairing decision depends on
+// the previous ones) and runs once per mesh, as in the reference where the
+// GAMGAgglomeration is cached in the mesh registry; everything per solve runs
+// on the device.
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+#include "internal.h"
+
+namespace cfx {
+
+// Derived addressing of lduAddressing (lduAddressing.C:32-170) plus the
+// lower-neighbour of each losort slot.  With validate, (l, u) must satisfy
+// 0 <= l < u < n and l non-decreasing (the owner-sorted order that
+// lduAddressing::calcOwnerStart and every face-order loop rely on).
+cfx_status build_host_level(int n, int nf, const int* l, const int* u, HostLevel& h, bool validate) {
+    if (n < 0 || nf < 0) {
+        set_error("negative size");
+        return CFX_ERR_ARG;
+    }
+    if (nf > 0 && (!l || !u)) {
+        set_error("null addressing");
+        return CFX_ERR_ARG;
+    }
+    if (validate) {
+        for (int f = 0; f < nf; ++f) {
+            if (l[f] < 0 || u[f] >= n || l[f] >= u[f]) {
+                set_error("face " + std::to_string(f) + ": need 0 <= l < u < nCells (l=" +
+                          std::to_string(l[f]) + " u=" + std::to_string(u[f]) + ")");
+                return CFX_ERR_ADDRESSING;
+            }
+            if (f > 0 && l[f - 1] > l[f]) {
+                set_error("lower not in incremental cell order at face " + std::to_string(f));
+                return CFX_ERR_ADDRESSING;
+            }
+        }
+    }
+    h.n = n;
+    h.nf = nf;
+    h.l.assign(l, l + nf);
+    h.u.assign(u, u + nf);
+    h.ownerStart.assign(n + 1, 0);
+    h.losortStart.assign(n + 1, 0);
+    for (int f = 0; f < nf; ++f) {
+        h.ownerStart[l[f] + 1]++;
+        h.losortStart[u[f] + 1]++;
+    }
+    for (int c = 0; c < n; ++c) {
+        h.ownerStart[c + 1] += h.ownerStart[c];
+        h.losortStart[c + 1] += h.losortStart[c];
+    }
+    h.losort.resize(nf);
+    h.losortL.resize(nf);
+    std::vector<int> fill(h.losortStart.begin(), h.losortStart.end() - 1);
+    for (int f = 0; f < nf; ++f) {
+        const int k = fill[u[f]]++;
+        h.losort[k] = f;
+        h.losortL[k] = l[f];
+    }
+    build_schedules(h);
+    return CFX_OK;
+}
+
+// Level schedules.  Forward: level(u) = 1 + max level(l) over the faces
+// (l, u); a face's owner is final when the face is reached because faces are
+// owner-sorted and l < u.  Backward: level(l) = 1 + max level(u), faces in
+// reverse.  Cells are grouped by level, ascending index within a level.
+static void group_by_level(const std::vector<int>& lev, int n, std::vector<int>& cells,
+                           std::vector<int>& start) {
+    int nl = 0;
+    for (int c = 0; c < n; ++c) nl = std::max(nl, lev[c] + 1);
+    start.assign(nl + 1, 0);
+    for (int c = 0; c < n; ++c) start[lev[c] + 1]++;
+    for (int i = 0; i < nl; ++i) start[i + 1] += start[i];
+    cells.resize(n);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int c = 0; c < n; ++c) cells[fill[lev[c]]++] = c;
+}
+
+void build_schedules(HostLevel& h) {
+    const int n = h.n, nf = h.nf;
+    std::vector<int> lev(n, 0);
+    for (int f = 0; f < nf; ++f) lev[h.u[f]] = std::max(lev[h.u[f]], lev[h.l[f]] + 1);
+    group_by_level(lev, n, h.fwdCells, h.fwdLevelStart);
+    std::fill(lev.begin(), lev.end(), 0);
+    for (int f = nf - 1; f >= 0; --f) lev[h.l[f]] = std::max(lev[h.l[f]], lev[h.u[f]] + 1);
+    group_by_level(lev, n, h.bwdCells, h.bwdLevelStart);
+}
+
+// pairGAMGAgglomeration::agglomerate, one level (pairGAMGAgglomerate.C:123-301).
+// Cell faces list, per cell, the faces where it is the neighbour (upperAddr)
+// then those where it is the owner, each in face order; ties in weight keep
+// the first face (strict >).  forward is toggled on return.
+int pair_agglomerate(int nFine, int nFaces, const int* l, const int* u, const double* w,
+                     bool& forward, std::vector<int>& map) {
+    const double great = 1.0 / std::numeric_limits<double>::epsilon();
+    std::vector<int> off(nFine + 1, 0), cnt(nFine, 0), cellFaces(2 * size_t(nFaces));
+    for (int f = 0; f < nFaces; ++f) {
+        off[u[f] + 1]++;
+        off[l[f] + 1]++;
+    }
+    for (int c = 0; c < nFine; ++c) off[c + 1] += off[c];
+    for (int f = 0; f < nFaces; ++f) cellFaces[off[u[f]] + cnt[u[f]]++] = f;
+    for (int f = 0; f < nFaces; ++f) cellFaces[off[l[f]] + cnt[l[f]]++] = f;
+    map.assign(nFine, -1);
+    int nCoarse = 0;
+    const bool fwd = forward;
+    for (int cf = 0; cf < nFine; ++cf) {
+        const int c = fwd ? cf : nFine - cf - 1;
+        if (map[c] >= 0) continue;
+        int match = -1;
+        double maxW = -great;
+        for (int k = off[c]; k < off[c + 1]; ++k) {
+            const int f = cellFaces[k];
+            if (map[u[f]] < 0 && map[l[f]] < 0 && w[f] > maxW) {
+                match = f;
+                maxW = w[f];
+            }
+        }
+        if (match >= 0) {
+            map[u[match]] = nCoarse;
+            map[l[match]] = nCoarse;
+            nCoarse++;
+        } else {
+            int cmatch = -1;
+            double cmax = -great;
+            for (int k = off[c]; k < off[c + 1]; ++k) {
+                const int f = cellFaces[k];
+                if (w[f] > cmax) {
+                    cmatch = f;
+                    cmax = w[f];
+                }
+            }
+            if (cmatch >= 0) map[c] = std::max(map[u[cmatch]], map[l[cmatch]]);
+        }
+    }
+    for (int cf = 0; cf < nFine; ++cf) {
+        const int c = fwd ? cf : nFine - cf - 1;
+        if (map[c] < 0) map[c] = nCoarse++;
+    }
+    if (!fwd) {
+        nCoarse--;
+        for (int c = 0; c < nFine; ++c) map[c] = nCoarse - map[c];
+        nCoarse++;
+    }
+    forward = !fwd;
+    return nCoarse;
+}
+
+// GAMGAgglomeration::agglomerateLduAddressing (GAMGAgglomerateLduAddressing.C:32-222):
+// coarse faces are created in fine-face order, then numbered by coarse owner
+// (creation order within an owner); faceFlip marks fine faces whose coarse
+// owner comes from the fine upper cell.
+int agglomerate_addressing(int nFaces, const int* l, const int* u, const std::vector<int>& rm,
+                           int nCoarse, std::vector<int>& cl, std::vector<int>& cu,
+                           std::vector<int>& fra, std::vector<int>& flip) {
+    std::vector<std::vector<int>> cCellFaces(nCoarse);
+    std::vector<int> initNeighb;
+    initNeighb.reserve(nFaces / 2 + 1);
+    fra.assign(nFaces, 0);
+    for (int f = 0; f < nFaces; ++f) {
+        const int rU = rm[u[f]], rL = rm[l[f]];
+        if (rU == rL) {
+            fra[f] = -(rU + 1);
+            continue;
+        }
+        const int cOwn = std::min(rU, rL), cNei = std::max(rU, rL);
+        bool found = false;
+        for (int cf : cCellFaces[cOwn]) {
+            if (initNeighb[cf] == cNei) {
+                fra[f] = cf;
+                found = true;
+                break;
+            }
+        }
+        if (!found) {
+            const int cf = int(initNeighb.size());
+            cCellFaces[cOwn].push_back(cf);
+            initNeighb.push_back(cNei);
+            fra[f] = cf;
+        }
+    }
+    const int ncf = int(initNeighb.size());
+    cl.resize(ncf);
+    cu.resize(ncf);
+    std::vector<int> coarseFaceMap(ncf);
+    int k = 0;
+    for (int c = 0; c < nCoarse; ++c)
+        for (int cf : cCellFaces[c]) {
+            cl[k] = c;
+            cu[k] = initNeighb[cf];
+            coarseFaceMap[cf] = k++;
+        }
+    flip.assign(nFaces, 0);
+    for (int f = 0; f < nFaces; ++f) {
+        if (fra[f] >= 0) {
+            fra[f] = coarseFaceMap[fra[f]];
+            if (cl[fra[f]] == rm[u[f]] && cu[fra[f]] == rm[l[f]]) flip[f] = 1;
+        }
+    }
+    return ncf;
+}
+
+// faceAreaPairGAMGAgglomeration.C:55-80 with magSf = max(|Sf|, rootVSmall)
+// (primitiveMeshFaceCentresAndAreas.C:93).  Compiled without FMA contraction.
+void face_area_pair_weights(int nFaces, const double* Sf, double* w) {
+    const double rootVSmall = std::sqrt(std::numeric_limits<double>::min());
+    for (int f = 0; f < nFaces; ++f) {
+        const double x = Sf[3 * f], y = Sf[3 * f + 1], z = Sf[3 * f + 2];
+        const double m = std::max(std::sqrt(x * x + y * y + z * z), rootVSmall);
+        const double s = std::sqrt(m);
+        const double a = (x / s) * 1.0, b = (y / s) * 1.01, c = (z / s) * 1.02;
+        w[f] = std::sqrt(a * a + b * b + c * c);
+    }
+}
+
+}  // namespace cfx

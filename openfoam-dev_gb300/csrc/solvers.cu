@@ -1,0 +1,786 @@
+// solvers.cu - fused kernels of the Krylov and GAMG drivers.
+//
+// Every scalar of the iteration (normFactor, wArA, alpha, beta, omega, the
+// residuals, nIterations, converged/singular) lives in a device SolveState;
+// the last block of each reduction kernel finishes the reduction in a fixed
+// order and applies the reference's scalar logic, so the host never waits
+// inside an iteration.  Once `done` is set every later kernel returns at
+// entry, which lets the host enqueue iterations ahead of the convergence test.
+//
+// Reference loops restated here (paths relative to the OpenFOAM-dev tree):
+//   PCG::solve              src/OpenFOAM/matrices/lduMatrix/solvers/PCG/PCG.C:65-193
+//   PBiCGStab::solve        src/OpenFOAM/matrices/lduMatrix/solvers/PBiCGStab/PBiCGStab.C:68-254
+//   solver::normFactor      src/OpenFOAM/matrices/lduMatrix/lduMatrix/lduMatrixSolver.C:174-197
+//   checkConvergence / checkSingularity
+//                           src/OpenFOAM/matrices/LduMatrix/LduMatrix/SolverPerformance.C:32-92
+//   GAMGSolver::scale       src/OpenFOAM/matrices/lduMatrix/solvers/GAMG/GAMGSolverScale.C:31-76
+//   GAMGSolver::solve       src/OpenFOAM/matrices/lduMatrix/solvers/GAMG/GAMGSolverSolve.C:31-145
+
+#include <atomic>
+#include <cfloat>
+
+#include "device.cuh"
+#include "solvers.h"
+
+namespace cfx {
+
+namespace {
+
+std::atomic<int64_t> g_launches{0};
+
+constexpr double VSMALL = DBL_MIN;  // doubleScalarVSmall
+constexpr double SP_SMALL = 1e-20;  // SolverPerformance::small_
+constexpr double SP_GREAT = 1e20;   // SolverPerformance::great_
+
+inline int grid_for(int64_t n) {
+    int64_t b = (n + RED_NT - 1) / RED_NT;
+    if (b < 1) b = 1;
+    if (b > RED_MAXB) b = RED_MAXB;
+    return int(b);
+}
+
+__device__ __forceinline__ int check_convergence(SolveState* st) {
+    const int c = st->finalResidual < st->tolerance ||
+                  (st->relTol > SP_SMALL && st->finalResidual < st->relTol * st->initialResidual);
+    st->converged = c;
+    return c;
+}
+
+// do { ... } while ((++nIter < maxIter && !converged) || nIter < minIter)
+__device__ __forceinline__ void loop_test(SolveState* st) {
+    ++st->nIterations;
+    bool cont = false;
+    if (st->nIterations < st->maxIter) cont = !check_convergence(st);
+    cont = cont || st->nIterations < st->minIter;
+    if (!cont) st->done = 1;
+}
+
+// Two fixed-order partial sums per block, finished by the last block.
+struct Red2 {
+    double* partials;
+    unsigned* counter;
+};
+
+template <int NT>
+__device__ __forceinline__ bool reduce2(double a, double b, Red2 r, double& outA, double& outB) {
+    __shared__ double sh[NT / 32];
+    a = block_sum<NT>(a, sh);
+    b = block_sum<NT>(b, sh);
+    if (threadIdx.x == 0) {
+        r.partials[blockIdx.x] = a;
+        r.partials[RED_MAXB + blockIdx.x] = b;
+    }
+    if (!last_block(r.counter)) return false;
+    double sa = 0.0, sb = 0.0;
+    for (int i = threadIdx.x; i < gridDim.x; i += NT) {
+        sa += __ldcg(r.partials + i);
+        sb += __ldcg(r.partials + RED_MAXB + i);
+    }
+    sa = block_sum<NT>(sa, sh);
+    sb = block_sum<NT>(sb, sh);
+    outA = sa;
+    outB = sb;
+    return true;  // valid in thread 0
+}
+
+template <class T>
+__device__ __forceinline__ T row_amul(int c, const int* __restrict__ os, const int* __restrict__ ls,
+                                      const int* __restrict__ lL, const int* __restrict__ u,
+                                      const T* __restrict__ diag, const T* __restrict__ lp,
+                                      const T* __restrict__ upper, const T* __restrict__ x) {
+    T acc = diag[c] * x[c];
+    const int k1 = ls[c + 1];
+    for (int k = ls[c]; k < k1; ++k) acc += lp[k] * x[lL[k]];
+    const int f1 = os[c + 1];
+    for (int f = os[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
+    return acc;
+}
+
+// normFactor (lduMatrixSolver.C:174-197): sumA*gAverage(psi), then
+// sum(|Apsi - t| + |b - t|) + small_; also r = b - Apsi and sum|r|.
+template <class T>
+__global__ void __launch_bounds__(RED_NT) norm_init_k(int n, const int* os, const int* ls, const int* u,
+                                                      const T* diag, const T* lp, const T* upper,
+                                                      const T* __restrict__ Apsi, const T* __restrict__ b,
+                                                      T* __restrict__ r, T* __restrict__ r0, SolveState* st,
+                                                      Red2 red) {
+    const double avg = n > 0 ? st->red0 / n : 0.0;
+    double nf = 0.0, mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        T sA = diag[c];
+        for (int k = ls[c]; k < ls[c + 1]; ++k) sA += lp[k];
+        for (int f = os[c]; f < os[c + 1]; ++f) sA += upper[f];
+        const T t = sA * T(avg);
+        nf += double(fabs(Apsi[c] - t) + fabs(b[c] - t));
+        const T rc = b[c] - Apsi[c];
+        r[c] = rc;
+        if (r0) r0[c] = rc;
+        mg += fabs(double(rc));
+    }
+    double snf, smg;
+    if (reduce2<RED_NT>(nf, mg, red, snf, smg) && threadIdx.x == 0) {
+        st->normFactor = snf + SP_SMALL;
+        st->initialResidual = smg / st->normFactor;
+        st->finalResidual = st->initialResidual;
+        st->nIterations = 0;
+        st->singular = 0;
+        st->phase = 0;
+        st->wArA = SP_GREAT;
+        st->rA0rA = 0.0;
+        st->alpha = 0.0;
+        st->omega = 0.0;
+        const int conv = check_convergence(st);
+        st->done = !(st->minIter > 0 || !conv);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) precond_pointwise_k(int n, const T* __restrict__ rD,
+                                                              const T* __restrict__ r, T* __restrict__ w,
+                                                              double* partials, const int* done) {
+    __shared__ double sh[RED_NT / 32];
+    if (*done) return;
+    double d = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = rD ? rD[c] * r[c] : r[c];
+        w[c] = v;
+        d += double(v) * double(r[c]);
+    }
+    d = block_sum<RED_NT>(d, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = d;
+}
+
+// wArAold = wArA; wArA = sum of the preconditioner's dot partials; beta.
+__global__ void pcg_beta_k(int nPartials, const double* partials, SolveState* st) {
+    __shared__ double sh[RED_NT / 32];
+    if (st->done) return;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nPartials; i += RED_NT) s += partials[i];
+    s = block_sum<RED_NT>(s, sh);
+    if (threadIdx.x == 0) {
+        st->wArAold = st->wArA;
+        st->wArA = s;
+        st->beta = st->wArA / st->wArAold;
+    }
+}
+
+template <class T>
+__global__ void pcg_p_k(int n, const T* __restrict__ w, T* __restrict__ p, const SolveState* st) {
+    if (st->done) return;
+    const bool first = st->nIterations == 0;
+    const T beta = T(st->beta);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        p[c] = first ? w[c] : w[c] + beta * p[c];
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) pcg_amul_k(int n, const int* os, const int* ls, const int* lL,
+                                                     const int* u, const T* diag, const T* lp, const T* upper,
+                                                     const T* __restrict__ p, T* __restrict__ wA, SolveState* st,
+                                                     Red2 red) {
+    if (st->done) return;
+    double d = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, p);
+        wA[c] = v;
+        d += double(v) * double(p[c]);
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(d, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        // PCG.C:161-168: singularity test, then alpha
+        st->singular = fabs(s) / st->normFactor < VSMALL;
+        if (st->singular) {
+            st->done = 1;
+        } else {
+            st->alpha = st->wArA / s;
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) pcg_update_k(int n, const T* __restrict__ p, const T* __restrict__ wA,
+                                                       T* __restrict__ psi, T* __restrict__ r, SolveState* st,
+                                                       Red2 red) {
+    if (st->done) return;
+    const T alpha = T(st->alpha);
+    double mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        psi[c] += alpha * p[c];
+        const T rc = r[c] - alpha * wA[c];
+        r[c] = rc;
+        mg += fabs(double(rc));
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->finalResidual = s / st->normFactor;
+        loop_test(st);
+    }
+}
+
+// PBiCGStab.C:141-171
+template <class T>
+__global__ void __launch_bounds__(RED_NT) bicg_rho_k(int n, const T* __restrict__ r0, const T* __restrict__ r,
+                                                     SolveState* st, Red2 red) {
+    if (st->done) return;
+    double d = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) d += double(r0[c]) * double(r[c]);
+    double s, dummy;
+    if (reduce2<RED_NT>(d, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->rA0rAold = st->rA0rA;
+        st->rA0rA = s;
+        st->singular = fabs(s) < VSMALL;
+        if (st->singular) {
+            st->done = 1;
+            return;
+        }
+        if (st->nIterations > 0) {
+            st->singular = fabs(st->omega) < VSMALL;
+            if (st->singular) {
+                st->done = 1;
+                return;
+            }
+            st->beta = (st->rA0rA / st->rA0rAold) * (st->alpha / st->omega);
+        }
+    }
+}
+
+template <class T>
+__global__ void bicg_p_k(int n, const T* __restrict__ r, const T* __restrict__ AyA, T* __restrict__ p,
+                         const SolveState* st) {
+    if (st->done) return;
+    const bool first = st->nIterations == 0;
+    const T beta = T(st->beta), omega = T(st->omega);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        p[c] = first ? r[c] : r[c] + beta * (p[c] - omega * AyA[c]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) bicg_amul_alpha_k(int n, const int* os, const int* ls, const int* lL,
+                                                            const int* u, const T* diag, const T* lp,
+                                                            const T* upper, const T* __restrict__ yA,
+                                                            T* __restrict__ AyA, const T* __restrict__ r0,
+                                                            SolveState* st, Red2 red) {
+    if (st->done) return;
+    double d = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, yA);
+        AyA[c] = v;
+        d += double(r0[c]) * double(v);
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(d, 0.0, red, s, dummy) && threadIdx.x == 0) st->alpha = st->rA0rA / s;
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) bicg_s_k(int n, const T* __restrict__ r, const T* __restrict__ AyA,
+                                                   T* __restrict__ sA, SolveState* st, Red2 red) {
+    if (st->done) return;
+    const T alpha = T(st->alpha);
+    double mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = r[c] - alpha * AyA[c];
+        sA[c] = v;
+        mg += fabs(double(v));
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->finalResidual = s / st->normFactor;
+        // if (++nIterations >= minIter && checkConvergence) { psi += alpha*yA; return }
+        if (++st->nIterations >= st->minIter && check_convergence(st)) {
+            st->phase = 1;
+            st->done = 1;
+        }
+    }
+}
+
+template <class T>
+__global__ void bicg_early_k(int n, const T* __restrict__ yA, T* __restrict__ psi, SolveState* st) {
+    if (st->phase != 1) return;
+    const T alpha = T(st->alpha);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) psi[c] += alpha * yA[c];
+}
+
+__global__ void bicg_phase_k(SolveState* st) {
+    if (st->phase == 1) st->phase = 2;
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) bicg_amul_omega_k(int n, const int* os, const int* ls, const int* lL,
+                                                            const int* u, const T* diag, const T* lp,
+                                                            const T* upper, const T* __restrict__ zA,
+                                                            T* __restrict__ tA, const T* __restrict__ sA,
+                                                            SolveState* st, Red2 red) {
+    if (st->done) return;
+    double tt = 0.0, ts = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, zA);
+        tA[c] = v;
+        tt += double(v) * double(v);
+        ts += double(v) * double(sA[c]);
+    }
+    double stt, sts;
+    if (reduce2<RED_NT>(tt, ts, red, stt, sts) && threadIdx.x == 0) {
+        st->tAtA = stt;
+        st->omega = sts / stt;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) bicg_update_k(int n, const T* __restrict__ yA, const T* __restrict__ zA,
+                                                        const T* __restrict__ sA, const T* __restrict__ tA,
+                                                        T* __restrict__ psi, T* __restrict__ r, SolveState* st,
+                                                        Red2 red) {
+    if (st->done) return;
+    const T alpha = T(st->alpha), omega = T(st->omega);
+    double mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        psi[c] += alpha * yA[c] + omega * zA[c];
+        const T v = sA[c] - omega * tA[c];
+        r[c] = v;
+        mg += fabs(double(v));
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->finalResidual = s / st->normFactor;
+        // while ((nIter < maxIter && !converged) || nIter < minIter)
+        bool cont = false;
+        if (st->nIterations < st->maxIter) cont = !check_convergence(st);
+        cont = cont || st->nIterations < st->minIter;
+        if (!cont) st->done = 1;
+    }
+}
+
+// GAMGSolverScale.C:42-75
+template <class T>
+__global__ void __launch_bounds__(RED_NT) gamg_scale_sf_k(int n, const int* os, const int* ls, const int* lL,
+                                                          const int* u, const T* diag, const T* lp, const T* upper,
+                                                          const T* __restrict__ field, T* __restrict__ Acf,
+                                                          const T* __restrict__ source, SolveState* st, Red2 red) {
+    if (st->done) return;
+    double num = 0.0, den = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, field);
+        Acf[c] = v;
+        num += double(source[c]) * double(field[c]);
+        den += double(v) * double(field[c]);
+    }
+    double sn, sd;
+    if (reduce2<RED_NT>(num, den, red, sn, sd) && threadIdx.x == 0) {
+        const double stab = sd >= 0 ? sd + VSMALL : sd - VSMALL;  // stabilise(den, vSmall)
+        st->sf = sn / stab;
+    }
+}
+
+template <class T>
+__global__ void gamg_scale_apply_k(int n, T* __restrict__ field, const T* __restrict__ Acf,
+                                   const T* __restrict__ source, const T* __restrict__ D, const T* __restrict__ pre,
+                                   const SolveState* st) {
+    if (st->done) return;
+    const T sf = T(st->sf);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        T v = sf * field[c] + (source[c] - sf * Acf[c]) / D[c];
+        if (pre) v += pre[c];
+        field[c] = v;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int* os, const int* ls, const int* lL,
+                                                                const int* u, const T* diag, const T* lp,
+                                                                const T* upper, const T* __restrict__ psi,
+                                                                const T* __restrict__ b, T* __restrict__ r,
+                                                                SolveState* st, Red2 red) {
+    if (st->done) return;
+    double mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        // finestResidual = source - Apsi (GAMGSolverSolve.C:116-118)
+        const T v = b[c] - row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi);
+        r[c] = v;
+        mg += fabs(double(v));
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->finalResidual = s / st->normFactor;
+        loop_test(st);
+    }
+}
+
+template <class T>
+__global__ void axpy_k(int n, T a, const T* __restrict__ x, T* __restrict__ y, const int* done) {
+    if (done && *done) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) y[c] += a * x[c];
+}
+
+template <class T>
+__global__ void copy_k(int n, const T* __restrict__ x, T* __restrict__ y, const int* done) {
+    if (done && *done) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) y[c] = x[c];
+}
+
+template <class T>
+__global__ void fill_k(int n, T v, T* __restrict__ y, const int* done) {
+    if (done && *done) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) y[c] = v;
+}
+
+__global__ void add_f2d_k(int n, const float* __restrict__ e, double* __restrict__ psi, const int* done) {
+    if (done && *done) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) psi[c] += double(e[c]);
+}
+
+__global__ void cast_pred_k(int n, const double* __restrict__ in, float* __restrict__ out, const int* done) {
+    if (done && *done) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) out[c] = float(in[c]);
+}
+
+// ---------------------------------------------------------------- block solver
+constexpr int BLK_NT = 256;
+
+template <class T>
+__device__ __forceinline__ double bsum(double v, double* sh, double* bc) {
+    v = block_sum<BLK_NT>(v, sh);
+    if (threadIdx.x == 0) *bc = v;
+    __syncthreads();
+    v = *bc;
+    __syncthreads();
+    return v;
+}
+
+template <class T>
+__device__ void blk_amul(const BlockSys<T>& S, const T* x, T* y) {
+    for (int c = threadIdx.x; c < S.n; c += BLK_NT)
+        y[c] = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, x);
+    __syncthreads();
+}
+
+// w = M^-1 r: DIC/DILU forward then backward level sweeps, block barriers.
+template <class T>
+__device__ void blk_precondition(const BlockSys<T>& S, const T* r, T* w) {
+    if (S.precond == CFX_PRE_DIC || S.precond == CFX_PRE_DILU) {
+        for (int L = 0; L < S.nFwd; ++L) {
+            for (int i = S.fwdLevelStart[L] + threadIdx.x; i < S.fwdLevelStart[L + 1]; i += BLK_NT) {
+                const int c = S.fwdCells[i];
+                const T rDc = S.rD[c];
+                T v = rDc * r[c];
+                for (int k = S.losortStart[c]; k < S.losortStart[c + 1]; ++k) v -= (rDc * S.lp[k]) * w[S.losortL[k]];
+                w[c] = v;
+            }
+            __syncthreads();
+        }
+        for (int L = 0; L < S.nBwd; ++L) {
+            for (int i = S.bwdLevelStart[L] + threadIdx.x; i < S.bwdLevelStart[L + 1]; i += BLK_NT) {
+                const int c = S.bwdCells[i];
+                const T rDc = S.rD[c];
+                T v = w[c];
+                for (int f = S.ownerStart[c + 1] - 1; f >= S.ownerStart[c]; --f) v -= (rDc * S.upper[f]) * w[S.u[f]];
+                w[c] = v;
+            }
+            __syncthreads();
+        }
+    } else {
+        for (int c = threadIdx.x; c < S.n; c += BLK_NT) w[c] = S.precond == CFX_PRE_DIAGONAL ? S.rD[c] * r[c] : r[c];
+        __syncthreads();
+    }
+}
+
+template <class T>
+__device__ __forceinline__ bool blk_check(BlockSys<T>& S, double fin, double ini) {
+    return fin < S.tolerance || (S.relTol > SP_SMALL && fin < S.relTol * ini);
+}
+
+template <class T>
+__global__ void __launch_bounds__(BLK_NT) block_solve_k(BlockSys<T>* systems, const int* done) {
+    __shared__ double sh[BLK_NT / 32];
+    __shared__ double bc;
+    if (done && *done) return;
+    BlockSys<T>& S = systems[blockIdx.x];
+    const int n = S.n;
+    T* psi = S.psi;
+    // Apsi into q
+    double s0 = 0.0;
+    for (int c = threadIdx.x; c < n; c += BLK_NT) s0 += double(psi[c]);
+    const double avg = n > 0 ? bsum<T>(s0, sh, &bc) / n : 0.0;
+    blk_amul(S, psi, S.q);
+    double nf = 0.0, mg = 0.0;
+    for (int c = threadIdx.x; c < n; c += BLK_NT) {
+        T sA = S.diag[c];
+        for (int k = S.losortStart[c]; k < S.losortStart[c + 1]; ++k) sA += S.lp[k];
+        for (int f = S.ownerStart[c]; f < S.ownerStart[c + 1]; ++f) sA += S.upper[f];
+        const T t = sA * T(avg);
+        nf += double(fabs(S.q[c] - t) + fabs(S.b[c] - t));
+        const T rc = S.b[c] - S.q[c];
+        S.r[c] = rc;
+        if (S.r0) S.r0[c] = rc;
+        mg += fabs(double(rc));
+    }
+    const double normFactor = bsum<T>(nf, sh, &bc) + SP_SMALL;
+    const double initial = bsum<T>(mg, sh, &bc) / normFactor;
+    double fin = initial;
+    int nIter = 0, converged = blk_check(S, fin, initial), singular = 0;
+    if (S.minIter > 0 || !converged) {
+        if (S.solver == CFX_SOLVER_PCG) {
+            double wArA = SP_GREAT, wArAold;
+            do {
+                wArAold = wArA;
+                blk_precondition(S, S.r, S.w);
+                double d = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.w[c]) * double(S.r[c]);
+                wArA = bsum<T>(d, sh, &bc);
+                const T beta = T(wArA / wArAold);
+                for (int c = threadIdx.x; c < n; c += BLK_NT) S.p[c] = nIter == 0 ? S.w[c] : S.w[c] + beta * S.p[c];
+                __syncthreads();
+                blk_amul(S, S.p, S.w);
+                d = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.w[c]) * double(S.p[c]);
+                const double wApA = bsum<T>(d, sh, &bc);
+                singular = fabs(wApA) / normFactor < VSMALL;
+                if (singular) break;
+                const T alpha = T(wArA / wApA);
+                mg = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) {
+                    psi[c] += alpha * S.p[c];
+                    const T rc = S.r[c] - alpha * S.w[c];
+                    S.r[c] = rc;
+                    mg += fabs(double(rc));
+                }
+                fin = bsum<T>(mg, sh, &bc) / normFactor;
+                bool cont = false;
+                if (++nIter < S.maxIter) {
+                    converged = blk_check(S, fin, initial);
+                    cont = !converged;
+                }
+                if (!(cont || nIter < S.minIter)) break;
+            } while (true);
+        } else {
+            double rA0rA = 0.0, alpha = 0.0, omega = 0.0;
+            do {
+                const double rA0rAold = rA0rA;
+                double d = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.r0[c]) * double(S.r[c]);
+                rA0rA = bsum<T>(d, sh, &bc);
+                singular = fabs(rA0rA) < VSMALL;
+                if (singular) break;
+                if (nIter == 0) {
+                    for (int c = threadIdx.x; c < n; c += BLK_NT) S.p[c] = S.r[c];
+                } else {
+                    singular = fabs(omega) < VSMALL;
+                    if (singular) break;
+                    const T beta = T((rA0rA / rA0rAold) * (alpha / omega));
+                    for (int c = threadIdx.x; c < n; c += BLK_NT)
+                        S.p[c] = S.r[c] + beta * (S.p[c] - T(omega) * S.q[c]);
+                }
+                __syncthreads();
+                blk_precondition(S, S.p, S.w);  // yA = w
+                blk_amul(S, S.w, S.q);          // AyA = q
+                d = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.r0[c]) * double(S.q[c]);
+                alpha = rA0rA / bsum<T>(d, sh, &bc);
+                mg = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) {
+                    const T v = S.r[c] - T(alpha) * S.q[c];
+                    S.s[c] = v;
+                    mg += fabs(double(v));
+                }
+                fin = bsum<T>(mg, sh, &bc) / normFactor;
+                if (++nIter >= S.minIter && (converged = blk_check(S, fin, initial))) {
+                    for (int c = threadIdx.x; c < n; c += BLK_NT) psi[c] += T(alpha) * S.w[c];
+                    __syncthreads();
+                    break;
+                }
+                // zA into r0-free slot: use t for tA, reuse p? keep z in S.t's partner
+                blk_precondition(S, S.s, S.t);  // zA = t
+                // tA = A zA -> stored in r (r is rewritten below from s and tA)
+                double tt = 0.0, ts = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) {
+                    const T v = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, S.t);
+                    S.r[c] = v;
+                    tt += double(v) * double(v);
+                    ts += double(v) * double(S.s[c]);
+                }
+                const double tAtA = bsum<T>(tt, sh, &bc);
+                omega = bsum<T>(ts, sh, &bc) / tAtA;
+                mg = 0.0;
+                for (int c = threadIdx.x; c < n; c += BLK_NT) {
+                    psi[c] += T(alpha) * S.w[c] + T(omega) * S.t[c];
+                    const T v = S.s[c] - T(omega) * S.r[c];
+                    S.r[c] = v;
+                    mg += fabs(double(v));
+                }
+                fin = bsum<T>(mg, sh, &bc) / normFactor;
+                bool cont = false;
+                if (nIter < S.maxIter) {
+                    converged = blk_check(S, fin, initial);
+                    cont = !converged;
+                }
+                if (!(cont || nIter < S.minIter)) break;
+            } while (true);
+        }
+    }
+    if (threadIdx.x == 0) {
+        S.initialResidual = initial;
+        S.finalResidual = fin;
+        S.nIterations = nIter;
+        S.converged = converged;
+        S.singular = singular;
+    }
+}
+
+}  // namespace
+
+void count_launch(int k) { g_launches += k; }
+int64_t launch_count() { return g_launches.load(); }
+
+template <class T>
+void Kern<T>::norm_init(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* Apsi,
+                        const T* b, T* r, T* r0, SolveState* st) {
+    norm_init_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.u, a.diag, a.lowerPerm,
+                                                    a.upper, Apsi, b, r, r0, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::precond_pointwise(cudaStream_t s, int n, const T* rD, const T* r, T* w, double* partials,
+                                const int* done) {
+    precond_pointwise_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, rD, r, w, partials, done);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pcg_beta(cudaStream_t s, int nPartials, const double* partials, SolveState* st) {
+    pcg_beta_k<<<1, RED_NT, 0, s>>>(nPartials, partials, st);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pcg_p(cudaStream_t s, int n, const T* w, T* p, const SolveState* st) {
+    pcg_p_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, w, p, st);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pcg_amul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* p, T* wA,
+                       SolveState* st) {
+    pcg_amul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+                                                   a.lowerPerm, a.upper, p, wA, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pcg_update(cudaStream_t s, Scratch& sc, int n, const T* p, const T* wA, T* psi, T* r, SolveState* st) {
+    pcg_update_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, p, wA, psi, r, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_rho(cudaStream_t s, Scratch& sc, int n, const T* r0, const T* r, SolveState* st) {
+    bicg_rho_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, r0, r, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_p(cudaStream_t s, int n, const T* r, const T* AyA, T* p, const SolveState* st) {
+    bicg_p_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, r, AyA, p, st);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_amul_alpha(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* yA,
+                              T* AyA, const T* r0, SolveState* st) {
+    bicg_amul_alpha_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+                                                          a.lowerPerm, a.upper, yA, AyA, r0, st,
+                                                          Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_s(cudaStream_t s, Scratch& sc, int n, const T* r, const T* AyA, T* sA, SolveState* st) {
+    bicg_s_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, r, AyA, sA, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_early(cudaStream_t s, int n, const T* yA, T* psi, SolveState* st) {
+    bicg_early_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, yA, psi, st);
+    bicg_phase_k<<<1, 1, 0, s>>>(st);
+    count_launch(2);
+}
+
+template <class T>
+void Kern<T>::bicg_amul_omega(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* zA,
+                              T* tA, const T* sA, SolveState* st) {
+    bicg_amul_omega_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+                                                          a.lowerPerm, a.upper, zA, tA, sA, st,
+                                                          Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::bicg_update(cudaStream_t s, Scratch& sc, int n, const T* yA, const T* zA, const T* sA, const T* tA,
+                          T* psi, T* r, SolveState* st) {
+    bicg_update_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, yA, zA, sA, tA, psi, r, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::gamg_scale_sf(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* field,
+                            T* Acf, const T* source, SolveState* st) {
+    gamg_scale_sf_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+                                                        a.lowerPerm, a.upper, field, Acf, source, st,
+                                                        Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::gamg_scale_apply(cudaStream_t s, int n, T* field, const T* Acf, const T* source, const T* diag,
+                               const T* pre, const SolveState* st) {
+    gamg_scale_apply_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, field, Acf, source, diag, pre, st);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a,
+                                  const T* psi, const T* b, T* r, SolveState* st) {
+    gamg_residual_check_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u,
+                                                              a.diag, a.lowerPerm, a.upper, psi, b, r, st,
+                                                              Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::block_solve(cudaStream_t s, BlockSys<T>* d_sys, int nSys, const int* done) {
+    block_solve_k<T><<<nSys, BLK_NT, 0, s>>>(d_sys, done);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::axpy(cudaStream_t s, int n, T a, const T* x, T* y, const int* done) {
+    axpy_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, a, x, y, done);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::copy(cudaStream_t s, int n, const T* x, T* y, const int* done) {
+    copy_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, x, y, done);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::fill(cudaStream_t s, int n, T v, T* y, const int* done) {
+    fill_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, v, y, done);
+    count_launch();
+}
+
+void launch_add_f2d(cudaStream_t s, int n, const float* e, double* psi, const int* done) {
+    add_f2d_k<<<grid_for(n), RED_NT, 0, s>>>(n, e, psi, done);
+    count_launch();
+}
+
+void launch_cast_pred(cudaStream_t s, int n, const double* in, float* out, const int* done) {
+    cast_pred_k<<<grid_for(n), RED_NT, 0, s>>>(n, in, out, done);
+    count_launch();
+}
+
+template struct Kern<double>;
+template struct Kern<float>;
+
+}  // namespace cfx

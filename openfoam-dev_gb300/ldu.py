@@ -1,0 +1,466 @@
+"""Python front end of libcudaLduSolvers.so, mirroring OpenFOAM's interface.
+
+    mesh   = LduMesh(ctx, nCells, lowerAddr, upperAddr)          # lduAddressing
+    A      = LduMatrix(mesh, diag, upper, lower=None)             # lduMatrix
+    solver = solver_new("T", A, {"solver": "cudaPCG",             # lduMatrix::solver::New
+                                 "preconditioner": "DIC",
+                                 "tolerance": 1e-8, "relTol": 0})
+    perf   = solver.solve(psi, source)                            # SolverPerformance
+
+Names, defaults and errors follow the reference (lduMatrixSolver.C:40-164,
+GAMGSolver.C:48-388, SolverPerformance.C:96-126): an unknown solver name
+raises ``FatalError`` with "Unknown symmetric matrix solver <name>"; numerical
+failure is reported through ``perf.singular`` / ``perf.converged``.  Solver
+names are the plugin's (``cudaPCG``, ``cudaPBiCGStab``, ``cudaGAMG``); the
+reference names ``PCG``/``PBiCGStab``/``GAMG`` are accepted as aliases.
+
+Everything runs on the GPU through the C ABI in include/cfx.h.  There is no
+CPU fallback: without the shared library, or without a CUDA device, every
+call raises.
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import LIB_DIR
+
+LIB_PATH = os.path.join(LIB_DIR, "libcudaLduSolvers.so")
+
+SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG = 0, 1, 2
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+SMOOTHERS = {"GaussSeidel": 0, "DIC": 1}
+SOLVERS = {"cudaPCG": SOLVER_PCG, "cudaPBiCGStab": SOLVER_PBICGSTAB, "cudaGAMG": SOLVER_GAMG,
+           "PCG": SOLVER_PCG, "PBiCGStab": SOLVER_PBICGSTAB, "GAMG": SOLVER_GAMG}
+SYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaPCG")
+ASYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab")
+
+STATUS = {0: "ok", -1: "bad argument", -2: "bad addressing", -3: "CUDA error", -4: "out of memory",
+          -5: "admission refused", -6: "device wait timed out", -7: "bad configuration", -8: "bad state"}
+
+
+class FatalError(RuntimeError):
+    """The reference's FatalError / FatalIOError (configuration errors)."""
+
+
+class CfxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Perf(ctypes.Structure):
+    _fields_ = [("solverName", ctypes.c_char * 32), ("initialResidual", ctypes.c_double),
+                ("finalResidual", ctypes.c_double), ("nIterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("singular", ctypes.c_int), ("status", ctypes.c_int), ("nOuter", ctypes.c_int),
+                ("pad", ctypes.c_int)]
+
+
+class Controls(ctypes.Structure):
+    _fields_ = [("solver", ctypes.c_int), ("preconditioner", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("relTol", ctypes.c_double), ("maxIter", ctypes.c_int), ("minIter", ctypes.c_int),
+                ("smoother", ctypes.c_int), ("nPreSweeps", ctypes.c_int),
+                ("preSweepsLevelMultiplier", ctypes.c_int), ("maxPreSweeps", ctypes.c_int),
+                ("nPostSweeps", ctypes.c_int), ("postSweepsLevelMultiplier", ctypes.c_int),
+                ("maxPostSweeps", ctypes.c_int), ("nFinestSweeps", ctypes.c_int),
+                ("scaleCorrection", ctypes.c_int), ("nCellsInCoarsestLevel", ctypes.c_int),
+                ("precision", ctypes.c_int), ("pad", ctypes.c_int)]
+
+
+# exported symbols and their signatures (every declaration of include/cfx.h)
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+_SIG = {
+    "cfx_default_controls": (None, [ctypes.POINTER(Controls)]),
+    "cfx_last_error": (ctypes.c_char_p, []),
+    "cfx_version": (_i, []),
+    "cfx_ctx_create": (_i, [_i, ctypes.POINTER(_vp)]),
+    "cfx_ctx_destroy": (_i, [_vp]),
+    "cfx_ctx_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "cfx_ctx_synchronize": (_i, [_vp]),
+    "cfx_ctx_launch_count": (_i, [_vp, ctypes.POINTER(ctypes.c_int64)]),
+    "cfx_mesh_create": (_i, [_vp, _i, _i, _vp, _vp, ctypes.POINTER(_vp)]),
+    "cfx_mesh_destroy": (_i, [_vp]),
+    "cfx_mesh_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "cfx_face_area_pair_weights": (_i, [_i, _vp, _vp]),
+    "cfx_gamg_agglomerate": (_i, [_vp, _vp, _i, _i]),
+    "cfx_gamg_set_levels": (_i, [_vp, _i, _vp, _vp]),
+    "cfx_gamg_level_info": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp, _vp, _vp, _vp, _vp]),
+    "cfx_gamg_n_levels": (_i, [_vp, ctypes.POINTER(_i)]),
+    "cfx_matrix_create": (_i, [_vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "cfx_matrix_update": (_i, [_vp, _vp, _vp, _vp]),
+    "cfx_matrix_update_device": (_i, [_vp, _vp, _vp, _vp]),
+    "cfx_matrix_destroy": (_i, [_vp]),
+    "cfx_matrix_coarse": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "cfx_solve": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, ctypes.POINTER(Perf)]),
+    "cfx_solve_device": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, ctypes.POINTER(Perf)]),
+    "cfx_tune_set": (_i, [_i, _i]),
+    "cfx_tune_get": (_i, [_i, ctypes.POINTER(_i)]),
+    "cfx_amul": (_i, [_vp, _vp, _vp]),
+    "cfx_tmul": (_i, [_vp, _vp, _vp]),
+    "cfx_residual": (_i, [_vp, _vp, _vp, _vp]),
+    "cfx_sumA": (_i, [_vp, _vp]),
+    "cfx_reduce": (_i, [_vp, _i, _i, _vp, _vp, ctypes.POINTER(_d)]),
+    "cfx_norm_factor": (_i, [_vp, _vp, _vp, ctypes.POINTER(_d)]),
+    "cfx_precondition": (_i, [_vp, _i, _i, _vp, _vp]),
+    "cfx_reciprocal_d": (_i, [_vp, _i, _vp]),
+    "cfx_smooth": (_i, [_vp, _i, _vp, _vp, _i]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the solver library (raises when it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() (no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIG.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIG)
+
+
+def _check(rc, what=""):
+    if rc != 0:
+        msg = lib().cfx_last_error().decode(errors="replace")
+        if rc == -7:
+            raise FatalError(msg)
+        raise CfxError(rc, f"{what}: {msg}")
+
+
+def _hp(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _dp(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Context:
+    """A device context: one CUDA stream on one GPU."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().cfx_ctx_create(device, ctypes.byref(h)), "cfx_ctx_create")
+        self.h = h
+        self.device = device
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(lib().cfx_ctx_stream(self.h, ctypes.byref(s)), "cfx_ctx_stream")
+        return s.value
+
+    def synchronize(self):
+        _check(lib().cfx_ctx_synchronize(self.h), "cfx_ctx_synchronize")
+
+    def launch_count(self):
+        c = ctypes.c_int64()
+        _check(lib().cfx_ctx_launch_count(self.h, ctypes.byref(c)), "launch_count")
+        return c.value
+
+    def reduce(self, which, a, b=None):
+        out = ctypes.c_double()
+        _check(lib().cfx_reduce(self.h, which, a.numel(), _dp(a), _dp(b), ctypes.byref(out)), "cfx_reduce")
+        return out.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cfx_ctx_destroy(self.h)
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class LduMesh:
+    """lduAddressing resident on the device (with level schedules)."""
+
+    def __init__(self, ctx, nCells, lowerAddr, upperAddr):
+        self.ctx = ctx
+        self.l = np.ascontiguousarray(lowerAddr, np.int32)
+        self.u = np.ascontiguousarray(upperAddr, np.int32)
+        self.nCells = int(nCells)
+        h = ctypes.c_void_p()
+        _check(lib().cfx_mesh_create(ctx.h, self.nCells, self.l.size, _hp(self.l), _hp(self.u), ctypes.byref(h)),
+               "cfx_mesh_create")
+        self.h = h
+        self.gamg_key = None
+
+    def schedule_depth(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cfx_mesh_info(self.h, ctypes.byref(a), ctypes.byref(b)), "cfx_mesh_info")
+        return a.value, b.value
+
+    def agglomerate(self, weights=None, Sf=None, nCellsInCoarsestLevel=10, forward=True):
+        """faceAreaPair agglomeration (weights from Sf when not given)."""
+        if weights is None:
+            weights = face_area_pair_weights(Sf)
+        w = np.ascontiguousarray(weights, np.float64)
+        _check(lib().cfx_gamg_agglomerate(self.h, _hp(w), int(nCellsInCoarsestLevel), int(bool(forward))),
+               "cfx_gamg_agglomerate")
+        self.gamg_key = ("faceAreaPair", int(nCellsInCoarsestLevel))
+
+    def set_levels(self, restrict_maps):
+        """Use a caller's agglomeration: list of fine->coarse maps."""
+        maps = [np.ascontiguousarray(m, np.int32) for m in restrict_maps]
+        nco = np.array([int(m.max()) + 1 for m in maps], np.int32)
+        arr = (ctypes.c_void_p * len(maps))(*[m.ctypes.data for m in maps])
+        _check(lib().cfx_gamg_set_levels(self.h, len(maps), arr, _hp(nco)), "cfx_gamg_set_levels")
+        self.gamg_key = ("given", len(maps))
+
+    def n_levels(self):
+        n = ctypes.c_int()
+        _check(lib().cfx_gamg_n_levels(self.h, ctypes.byref(n)), "cfx_gamg_n_levels")
+        return n.value
+
+    def level(self, i, fine_cells, fine_faces):
+        nc, ncf = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cfx_gamg_level_info(self.h, i, ctypes.byref(nc), ctypes.byref(ncf), None, None, None, None,
+                                         None), "level_info")
+        ra = np.empty(fine_cells, np.int32)
+        fra = np.empty(fine_faces, np.int32)
+        fl = np.empty(fine_faces, np.int32)
+        cl = np.empty(ncf.value, np.int32)
+        cu = np.empty(ncf.value, np.int32)
+        _check(lib().cfx_gamg_level_info(self.h, i, None, None, _hp(ra), _hp(fra), _hp(fl), _hp(cl), _hp(cu)),
+               "level_info")
+        return ra, fra, fl, nc.value, ncf.value, cl, cu
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cfx_mesh_destroy(self.h)
+        except Exception:
+            pass
+
+
+class LduMatrix:
+    """lduMatrix: diag/upper(/lower) coefficients on an LduMesh."""
+
+    def __init__(self, mesh, diag, upper, lower=None):
+        self.mesh = mesh
+        self.diag = np.ascontiguousarray(diag, np.float64)
+        self.upper = np.ascontiguousarray(upper, np.float64)
+        self.lower = None if lower is None else np.ascontiguousarray(lower, np.float64)
+        h = ctypes.c_void_p()
+        _check(lib().cfx_matrix_create(mesh.h, _hp(self.diag), _hp(self.upper), _hp(self.lower), ctypes.byref(h)),
+               "cfx_matrix_create")
+        self.h = h
+
+    def symmetric(self):
+        return self.lower is None
+
+    def asymmetric(self):
+        return self.lower is not None
+
+    def update(self, diag, upper, lower=None):
+        self.diag = np.ascontiguousarray(diag, np.float64)
+        self.upper = np.ascontiguousarray(upper, np.float64)
+        self.lower = None if lower is None else np.ascontiguousarray(lower, np.float64)
+        _check(lib().cfx_matrix_update(self.h, _hp(self.diag), _hp(self.upper), _hp(self.lower)), "update")
+
+    # single operations on torch CUDA tensors (float64)
+    def Amul(self, x, y):
+        _check(lib().cfx_amul(self.h, _dp(x), _dp(y)), "cfx_amul")
+
+    def Tmul(self, x, y):
+        _check(lib().cfx_tmul(self.h, _dp(x), _dp(y)), "cfx_tmul")
+
+    def residual(self, x, b, r):
+        _check(lib().cfx_residual(self.h, _dp(x), _dp(b), _dp(r)), "cfx_residual")
+
+    def sumA(self, s):
+        _check(lib().cfx_sumA(self.h, _dp(s)), "cfx_sumA")
+
+    def normFactor(self, psi, b):
+        out = ctypes.c_double()
+        _check(lib().cfx_norm_factor(self.h, _dp(psi), _dp(b), ctypes.byref(out)), "normFactor")
+        return out.value
+
+    def precondition(self, kind, r, w, transpose=False):
+        _check(lib().cfx_precondition(self.h, PRECONDITIONERS[kind], int(transpose), _dp(r), _dp(w)), "precondition")
+
+    def reciprocalD(self, kind, rD):
+        _check(lib().cfx_reciprocal_d(self.h, PRECONDITIONERS[kind], _dp(rD)), "reciprocalD")
+
+    def smooth(self, kind, psi, b, nSweeps):
+        _check(lib().cfx_smooth(self.h, SMOOTHERS[kind], _dp(psi), _dp(b), int(nSweeps)), "smooth")
+
+    def coarse(self, level, nCells, nFaces):
+        d = np.empty(nCells)
+        up = np.empty(nFaces)
+        lo = None if self.symmetric() else np.empty(nFaces)
+        _check(lib().cfx_matrix_coarse(self.h, level, _hp(d), _hp(up), _hp(lo)), "coarse")
+        return d, up, lo
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().cfx_matrix_destroy(self.h)
+        except Exception:
+            pass
+
+
+@dataclass
+class SolverPerformance:
+    solverName: str
+    fieldName: str
+    initialResidual: float
+    finalResidual: float
+    nIterations: int
+    converged: bool
+    singular: bool
+    nOuter: int = 0
+
+    def __str__(self):
+        # SolverPerformance::print (SolverPerformance.C:96-126)
+        if self.singular:
+            return f"{self.solverName}:  Solving for {self.fieldName}:  solution singularity"
+        return (f"{self.solverName}:  Solving for {self.fieldName}, Initial residual = {self.initialResidual:g}, "
+                f"Final residual = {self.finalResidual:g}, No Iterations {self.nIterations}")
+
+
+TUNE_SMALL_SWEEP = 0
+
+
+def tune_set(key, value):
+    _check(lib().cfx_tune_set(int(key), int(value)), "cfx_tune_set")
+
+
+def tune_get(key):
+    v = ctypes.c_int()
+    _check(lib().cfx_tune_get(int(key), ctypes.byref(v)), "cfx_tune_get")
+    return v.value
+
+
+def face_area_pair_weights(Sf):
+    Sf = np.ascontiguousarray(Sf, np.float64).reshape(-1)
+    w = np.empty(Sf.size // 3)
+    _check(lib().cfx_face_area_pair_weights(w.size, _hp(Sf), _hp(w)), "weights")
+    return w
+
+
+def _controls(d, sym):
+    c = Controls()
+    lib().cfx_default_controls(ctypes.byref(c))
+    name = d.get("solver")
+    if name is None:
+        raise FatalError("keyword solver is undefined in dictionary")
+    table = SYM_SOLVERS if sym else ASYM_SOLVERS
+    if name not in SOLVERS or SOLVERS[name] not in [SOLVERS[t] for t in table]:
+        kind = "symmetric" if sym else "asymmetric"
+        raise FatalError(f"Unknown {kind} matrix solver {name}\n\nValid {kind} matrix solvers are : {list(table)}")
+    c.solver = SOLVERS[name]
+    if c.solver != SOLVER_GAMG:
+        pre = d.get("preconditioner", "none")
+        if isinstance(pre, dict):
+            pre = pre.get("preconditioner", "none")
+        if pre not in PRECONDITIONERS:
+            raise FatalError(f"Unknown {'symmetric' if sym else 'asymmetric'} matrix preconditioner {pre}")
+        c.preconditioner = PRECONDITIONERS[pre]
+    c.tolerance = float(d.get("tolerance", 1e-6))
+    c.relTol = float(d.get("relTol", 0.0))
+    c.maxIter = int(d.get("maxIter", 1000))
+    c.minIter = int(d.get("minIter", 0))
+    sm = d.get("smoother", "GaussSeidel")
+    if c.solver == SOLVER_GAMG and sm not in SMOOTHERS:
+        raise FatalError(f"Unknown {'symmetric' if sym else 'asymmetric'} matrix smoother {sm}")
+    c.smoother = SMOOTHERS.get(sm, 0)
+    for k in ("nPreSweeps", "preSweepsLevelMultiplier", "maxPreSweeps", "nPostSweeps",
+              "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "nCellsInCoarsestLevel"):
+        if k in d:
+            setattr(c, k, int(d[k]))
+    if "minCellsPerProcessor" in d:
+        c.nCellsInCoarsestLevel = int(d["minCellsPerProcessor"])
+    if "scaleCorrection" in d:
+        c.scaleCorrection = int(bool(d["scaleCorrection"]))
+    if d.get("interpolateCorrection", False):
+        raise FatalError("interpolateCorrection is not supported by cudaGAMG")
+    if d.get("agglomerator", "faceAreaPair") != "faceAreaPair":
+        raise FatalError(f"Unknown GAMGAgglomeration type {d['agglomerator']}")
+    prec = str(d.get("precision", "FP64"))
+    if prec not in ("FP64", "mixed"):
+        raise FatalError(f"Unknown precision {prec} (FP64 or mixed)")
+    c.precision = 1 if prec == "mixed" else 0
+    return c
+
+
+class Solver:
+    """lduMatrix::solver for cudaPCG / cudaPBiCGStab / cudaGAMG."""
+
+    def __init__(self, fieldName, matrix, controls):
+        self.fieldName = fieldName
+        self.matrix = matrix
+        self.controlDict = dict(controls)
+        self.c = _controls(self.controlDict, matrix.symmetric())
+
+    def read(self, controls):
+        self.controlDict = dict(controls)
+        self.c = _controls(self.controlDict, self.matrix.symmetric())
+
+    def _perf(self, p):
+        return SolverPerformance(p.solverName.decode(), self.fieldName, p.initialResidual, p.finalResidual,
+                                 p.nIterations, bool(p.converged), bool(p.singular), p.nOuter)
+
+    def solve(self, psi, source):
+        """psi: float64 numpy array (updated in place) or CUDA tensor."""
+        p = Perf()
+        if isinstance(psi, np.ndarray):
+            if psi.dtype != np.float64 or not psi.flags["C_CONTIGUOUS"]:
+                raise TypeError("psi must be a contiguous float64 array")
+            src = np.ascontiguousarray(source, np.float64)
+            rc = lib().cfx_solve(self.matrix.h, ctypes.byref(self.c), _hp(psi), _hp(src), ctypes.byref(p))
+        else:
+            rc = lib().cfx_solve_device(self.matrix.h, ctypes.byref(self.c), _dp(psi), _dp(source), ctypes.byref(p))
+        _check(rc, "solve")
+        return self._perf(p)
+
+
+def solver_new(fieldName, matrix, controls):
+    """lduMatrix::solver::New (lduMatrixSolver.C:40-130)."""
+    return Solver(fieldName, matrix, controls)
+
+
+# ---------------------------------------------------------------- convenience
+_PRE_FOR = {"PCG": "DIC", "PBiCGStab": "DILU"}
+
+
+def system_matrix(s, ctx=None):
+    """(LduMesh, LduMatrix) for a system dict of cases.py, cached on the dict."""
+    if "_cfx" not in s:
+        ctx = ctx or default_context()
+        mesh = LduMesh(ctx, s["diag"].size, s["l"], s["u"])
+        A = LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
+        s["_cfx"] = (mesh, A)
+    return s["_cfx"]
+
+
+def solve(s, psi, controls, field="psi"):
+    """Solve system dict s (cases.py layout) with a controls dict."""
+    mesh, A = system_matrix(s)
+    name = controls["solver"]
+    if SOLVERS.get(name) == SOLVER_GAMG:
+        key = ("faceAreaPair", int(controls.get("nCellsInCoarsestLevel", 10)))
+        if mesh.gamg_key != key:
+            mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=key[1])
+    return solver_new(field, A, controls).solve(psi, s["source"])

@@ -1,0 +1,121 @@
+"""Write the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a container where the OpenFOAM-dev sources are mounted and
+``python oracle/build_ref.py`` has built oracle/_ref (libOpenFOAM.so and the
+harness).  Every fixture is produced by the reference's own code:
+
+* geom_*.npz   polyMesh face areas/centres and cell centres/volumes of a
+               jittered hex box (primitiveMesh geometry)
+* ops_*.npz    lduMatrix::Amul/Tmul/residual/sumA, normFactor, gSum*, the
+               DIC/DILU reciprocal diagonals and preconditioners, the
+               GaussSeidel and DIC smoothers, lduAddressing losort/ownerStart
+* solve_*.npz  lduMatrix::solver::New(...)->solve for PCG, PBiCGStab and GAMG
+               (with the agglomeration levels and coarse matrices)
+
+Inputs are regenerated by the tests from the stored case parameters with
+openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
+
+Usage:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+import __graft_entry__ as ge  # noqa: E402
+
+ge.load_package()
+from openfoam_dev_gb300 import cases  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+from oracle import reference as ref  # noqa: E402
+
+# Case specs: (kind, params).  Shared with tests/golden_cases.py via JSON.
+SYSTEMS = {
+    "cube6": ("pcg_cube", dict(n=6, seed=2)),
+    "cube12": ("pcg_cube", dict(n=12, seed=2)),
+    "jcube7": ("gamg_cube", dict(n=7, jitter=0.3, seed=3)),
+    "jcube14": ("gamg_cube", dict(n=14, jitter=0.2, seed=5)),
+    "jcube16": ("gamg_cube", dict(n=16, jitter=0.2, seed=9)),
+    "cd6": ("bicgstab_cube", dict(n=6, seed=4)),
+    "cd10": ("bicgstab_cube", dict(n=10, seed=4)),
+    "box": ("box", dict(nx=9, ny=5, nz=13, dirichlet="zmax", seed=11)),
+}
+
+SOLVES = {
+    "pcg_dic": ("cube12", dict(solver="PCG", preconditioner="DIC", tolerance=1e-8, relTol=0.0, maxIter=2000)),
+    "pcg_diag": ("cube12", dict(solver="PCG", preconditioner="diagonal", tolerance=1e-8, relTol=0.0)),
+    "pcg_none": ("box", dict(solver="PCG", preconditioner="none", tolerance=1e-7, relTol=0.0)),
+    "pcg_reltol": ("jcube14", dict(solver="PCG", preconditioner="DIC", tolerance=0.0, relTol=1e-3)),
+    "pcg_maxiter": ("jcube14", dict(solver="PCG", preconditioner="DIC", tolerance=1e-12, relTol=0.0, maxIter=7)),
+    "pcg_miniter": ("cube6", dict(solver="PCG", preconditioner="DIC", tolerance=1.0, relTol=0.0, minIter=3)),
+    "bicgstab_dilu": ("cd10", dict(solver="PBiCGStab", preconditioner="DILU", tolerance=1e-8, relTol=0.0,
+                                   maxIter=2000)),
+    "bicgstab_sym": ("jcube14", dict(solver="PBiCGStab", preconditioner="DIC", tolerance=1e-8, relTol=0.0)),
+    "gamg_gs": ("jcube14", dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-8, relTol=0.0,
+                                nCellsInCoarsestLevel=10)),
+    "gamg_gs_pre": ("jcube16", dict(solver="GAMG", smoother="GaussSeidel", nPreSweeps=2, nPostSweeps=2,
+                                    tolerance=1e-8, relTol=0.0, nCellsInCoarsestLevel=10)),
+    "gamg_dic": ("jcube14", dict(solver="GAMG", smoother="DIC", tolerance=1e-8, relTol=0.0)),
+    "gamg_box": ("box", dict(solver="GAMG", smoother="GaussSeidel", nPreSweeps=1, tolerance=1e-9, relTol=0.0,
+                             nCellsInCoarsestLevel=4)),
+}
+
+
+def build(kind, params):
+    return getattr(cases, kind)(**params)
+
+
+def checksum(s):
+    h = hashlib.sha256()
+    for k in ("l", "u", "diag", "upper", "lower", "source"):
+        if s.get(k) is not None:
+            h.update(np.ascontiguousarray(s[k]).tobytes())
+    return h.hexdigest()
+
+
+def main():
+    if not ref.available():
+        print("reference harness not built (python oracle/build_ref.py) or sources absent")
+        return 1
+    specs = {"systems": SYSTEMS, "solves": SOLVES}
+    with open(os.path.join(HERE, "specs.json"), "w") as fh:
+        json.dump(specs, fh, indent=1, sort_keys=True)
+
+    # geometry of a jittered box
+    m = cases.box_mesh(5, 6, 7, jitter=0.3, seed=11)
+    g = ref.geometry(m)
+    np.savez_compressed(os.path.join(HERE, "geom_box567.npz"), nx=5, ny=6, nz=7, jitter=0.3, seed=11,
+                        **{k: g[k] for k in ("Sf", "Cf", "magSf", "C", "V")})
+
+    sums = {}
+    for name in ("cube6", "jcube7", "cd6", "box"):
+        s = build(*SYSTEMS[name])
+        sums[name] = checksum(s)
+        x = cases.uniform(99, s["diag"].size)
+        r = ref.ops(s, x, s["source"])
+        r = {k: v for k, v in r.items() if not isinstance(v, str)}
+        np.savez_compressed(os.path.join(HERE, f"ops_{name}.npz"), x=x, **r)
+
+    for name, (sysname, ctl) in SOLVES.items():
+        s = build(*SYSTEMS[sysname])
+        sums[sysname] = checksum(s)
+        w = orc.face_area_pair_weights(s["Sf"]) if ctl["solver"] == "GAMG" else None
+        r = ref.solve(s, ctl, weights=w)
+        out = {k: v for k, v in r.items() if not isinstance(v, str)}
+        out["solverName"] = np.frombuffer(r["solverName"].encode(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **out)
+        print(name, r["solverName"], int(r["nIterations"][0]), float(r["finalResidual"][0]))
+
+    with open(os.path.join(HERE, "checksums.json"), "w") as fh:
+        json.dump(sums, fh, indent=1, sort_keys=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,194 @@
+"""Solver parity on the GPU through the C ABI.
+
+Against the reference's own results (golden fixtures) and the oracle:
+* FP64 cudaPCG / cudaPBiCGStab / cudaGAMG: solution within relative L2
+  1e-10 of the reference's, iteration count within +-1, same solverName and
+  initial residual (to rounding; the GPU sums reductions in a fixed tree
+  instead of sequentially);
+* the GAMG agglomeration (restriction maps, coarse addressing, face maps) is
+  bit-exact and the device-assembled coarse matrices are bit-exact;
+* results are reproducible bit for bit from run to run;
+* FP32-inner / FP64-refined solves reach the same residual tolerance, and
+  their error against an FP64 solution converged to 1e-12 is stated and
+  bounded (mixed: relative L2 <= 1e-6 at tolerance 1e-8).
+"""
+import numpy as np
+import pytest
+
+from golden_cases import SPECS, solve_case
+from oracle import oracle as orc
+from openfoam_dev_gb300 import cases, ldu
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+RTOL_FP64 = 1e-10
+
+
+def _ctl(ctl):
+    c = dict(ctl)
+    c["solver"] = "cuda" + c["solver"]
+    return c
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("name", sorted(SPECS["solves"]))
+def test_golden_solves(name):
+    s, ctl, g = solve_case(name)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, _ctl(ctl))
+    assert perf.solverName == g["solverName"]
+    assert abs(perf.nIterations - int(g["nIterations"][0])) <= 1, (perf, int(g["nIterations"][0]))
+    assert perf.initialResidual == pytest.approx(float(g["initialResidual"][0]), rel=1e-12)
+    assert perf.converged == bool(g["converged"][0])
+    assert not perf.singular
+    if perf.nIterations == int(g["nIterations"][0]):
+        assert _rel(psi, g["psi"]) <= RTOL_FP64, _rel(psi, g["psi"])
+    else:
+        # one iteration more or less: the solutions differ by at most one
+        # iteration's update, bounded by the tolerance
+        assert _rel(psi, g["psi"]) <= 1e-6
+
+
+@pytest.mark.parametrize("name", [n for n, (_, c) in sorted(SPECS["solves"].items()) if c["solver"] == "GAMG"])
+def test_gamg_levels_and_coarse_matrices_exact(name):
+    s, ctl, g = solve_case(name)
+    mesh, A = ldu.system_matrix(s)
+    mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=ctl.get("nCellsInCoarsestLevel", 10))
+    assert mesh.n_levels() == int(g["nLevels"][0])
+    nc_f, nf_f = s["diag"].size, s["l"].size
+    for i in range(mesh.n_levels()):
+        ra, fra, fl, nc, ncf, cl, cu = mesh.level(i, nc_f, nf_f)
+        np.testing.assert_array_equal(ra, g[f"restrict{i}"])
+        np.testing.assert_array_equal(fra, g[f"faceRestrict{i}"])
+        np.testing.assert_array_equal(fl, g[f"faceFlip{i}"])
+        np.testing.assert_array_equal(cl, g[f"coarseL{i}"])
+        np.testing.assert_array_equal(cu, g[f"coarseU{i}"])
+        d, up, _ = A.coarse(i + 1, nc, ncf)
+        np.testing.assert_array_equal(d, g[f"coarseDiag{i}"])
+        np.testing.assert_array_equal(up, g[f"coarseUpper{i}"])
+        nc_f, nf_f = nc, ncf
+    mesh.gamg_key = None
+
+
+def test_gamg_given_levels_equal_own_agglomeration():
+    s, ctl, g = solve_case("gamg_gs")
+    maps = [g[f"restrict{i}"] for i in range(int(g["nLevels"][0]))]
+    mesh = ldu.LduMesh(ldu.default_context(), s["diag"].size, s["l"], s["u"])
+    A = ldu.LduMatrix(mesh, s["diag"], s["upper"])
+    mesh.set_levels(maps)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solver_new("T", A, _ctl(ctl)).solve(psi, s["source"])
+    assert perf.nIterations == int(g["nIterations"][0]) or abs(perf.nIterations - int(g["nIterations"][0])) <= 1
+    assert _rel(psi, g["psi"]) <= 1e-6
+
+
+def _oracle(s, solver, tol, **kw):
+    psi = np.zeros_like(s["source"])
+    if solver == "PCG":
+        p = orc.pcg(s, psi, tol=tol, max_iter=4000, precond="DIC")
+    elif solver == "PBiCGStab":
+        p = orc.pbicgstab(s, psi, tol=tol, max_iter=4000, precond="DILU")
+    else:
+        p = orc.gamg(s, psi, tol=tol, max_iter=1000, **kw)
+    return psi, p
+
+
+@pytest.mark.parametrize("form", ["small", "multi"])
+def test_pcg_cube_against_oracle(form):
+    """C1 shape (uniform cube Laplacian, Dirichlet x=0) at 40^3."""
+    old = ldu.tune_get(ldu.TUNE_SMALL_SWEEP)
+    ldu.tune_set(ldu.TUNE_SMALL_SWEEP, 1 << 30 if form == "small" else 0)
+    try:
+        s = cases.pcg_cube(40, seed=1)
+        ref, rp = _oracle(s, "PCG", 1e-8)
+        psi = np.zeros_like(s["source"])
+        perf = ldu.solve(s, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-8,
+                                  "relTol": 0, "maxIter": 2000})
+    finally:
+        ldu.tune_set(ldu.TUNE_SMALL_SWEEP, old)
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= RTOL_FP64
+
+
+def test_pbicgstab_cd_against_oracle():
+    """C3 shape (jittered, upwind convection-diffusion, random+CM order) at 16^3."""
+    s = cases.bicgstab_cube(16, seed=2)
+    ref, rp = _oracle(s, "PBiCGStab", 1e-8)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, {"solver": "cudaPBiCGStab", "preconditioner": "DILU", "tolerance": 1e-8,
+                              "relTol": 0, "maxIter": 2000})
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= RTOL_FP64 if perf.nIterations == rp.nIterations else _rel(psi, ref) <= 1e-6
+
+
+@pytest.mark.parametrize("npre", [0, 2])
+def test_gamg_jittered_against_oracle(npre):
+    """C2 shape (jittered cube, faceAreaPair, GaussSeidel) at 32^3."""
+    s = cases.gamg_cube(32, jitter=0.2, seed=3)
+    kw = dict(smoother="GaussSeidel", nPreSweeps=npre, nPostSweeps=2)
+    ref, rp = _oracle(s, "GAMG", 1e-8, **kw)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, {"solver": "cudaGAMG", "tolerance": 1e-8, "relTol": 0, **kw})
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= RTOL_FP64 if perf.nIterations == rp.nIterations else _rel(psi, ref) <= 1e-6
+
+
+def test_deterministic_repeat():
+    s = cases.gamg_cube(20, jitter=0.2, seed=7)
+    out = []
+    for _ in range(2):
+        psi = np.zeros_like(s["source"])
+        ldu.solve(s, psi, {"solver": "cudaGAMG", "tolerance": 1e-8, "relTol": 0, "nPreSweeps": 2})
+        out.append(psi)
+        psi = np.zeros_like(s["source"])
+        ldu.solve(s, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-8, "relTol": 0})
+        out.append(psi)
+    np.testing.assert_array_equal(out[0], out[2])
+    np.testing.assert_array_equal(out[1], out[3])
+
+
+@pytest.mark.parametrize("solver", ["cudaGAMG", "cudaPCG"])
+def test_mixed_precision_reaches_tolerance(solver):
+    """FP32 inner / FP64 refinement: residual 1e-8 in the reference's
+    normalisation; error vs the FP64 oracle converged to 1e-12 <= 1e-6."""
+    s = cases.gamg_cube(32, jitter=0.2, seed=4)
+    tight, _ = _oracle(s, "GAMG", 1e-12, smoother="GaussSeidel", nPreSweeps=2)
+    ctl = {"solver": solver, "tolerance": 1e-8, "relTol": 0, "precision": "mixed", "nPreSweeps": 2,
+           "preconditioner": "DIC", "maxIter": 2000}
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, ctl)
+    assert perf.converged and perf.finalResidual < 1e-8
+    # independent FP64 check of the residual with the oracle
+    m = orc.Matrix(s)
+    r = m.residual(psi, s["source"])
+    nf = m.norm_factor(np.zeros_like(psi), s["source"])
+    assert np.abs(r).sum() / nf < 1.5e-8
+    assert _rel(psi, tight) <= 1e-6
+    ctl64 = dict(ctl, precision="FP64")
+    psi64 = np.zeros_like(s["source"])
+    p64 = ldu.solve(s, psi64, ctl64)
+    if solver == "cudaGAMG":
+        assert abs(perf.nIterations - p64.nIterations) <= 2
+
+
+def test_asymmetric_rejects_pcg_and_dic():
+    s = cases.bicgstab_cube(6, seed=1)
+    _, A = ldu.system_matrix(s)
+    with pytest.raises(ldu.FatalError):
+        ldu.solver_new("T", A, {"solver": "cudaPCG", "preconditioner": "DIC"}).solve(np.zeros(216), s["source"])
+    with pytest.raises(ldu.FatalError):
+        ldu.solver_new("T", A, {"solver": "cudaPBiCGStab", "preconditioner": "DIC"}).solve(np.zeros(216),
+                                                                                          s["source"])
+
+
+def test_converged_at_start_runs_no_iteration():
+    s = cases.pcg_cube(8, seed=1)
+    s2 = dict(s)
+    s2["source"] = np.zeros_like(s["source"])
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s2, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-6})
+    assert perf.nIterations == 0 and perf.converged and np.all(psi == 0)

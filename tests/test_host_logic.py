@@ -1,0 +1,115 @@
+"""Host-side logic that needs no GPU: the C ABI's exports, control parsing
+with the reference's error behaviour, and the case generator's invariants."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from openfoam_dev_gb300 import INCLUDE_DIR, cases, ldu
+
+
+def _declared_symbols():
+    with open(os.path.join(INCLUDE_DIR, "cfx.h")) as fh:
+        text = fh.read()
+    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(cfx_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(ldu.LIB_PATH)
+    declared = _declared_symbols()
+    assert len(declared) >= 30
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(ldu.exported_symbols()) == declared
+
+
+def test_default_controls_are_the_reference_defaults():
+    c = ldu.Controls()
+    ldu.lib().cfx_default_controls(ctypes.byref(c))
+    # lduMatrixSolver.C:158-164, lduMatrix.C:38, GAMGSolver.C:70-80, GAMGAgglomeration.C:250-257
+    assert (c.tolerance, c.relTol, c.maxIter, c.minIter) == (1e-6, 0.0, 1000, 0)
+    assert (c.nPreSweeps, c.preSweepsLevelMultiplier, c.maxPreSweeps) == (0, 1, 4)
+    assert (c.nPostSweeps, c.postSweepsLevelMultiplier, c.maxPostSweeps, c.nFinestSweeps) == (2, 1, 4, 2)
+    assert c.scaleCorrection == -1 and c.nCellsInCoarsestLevel == 10
+
+
+class _FakeMatrix:
+    def __init__(self, sym):
+        self.lower = None if sym else np.zeros(1)
+
+    def symmetric(self):
+        return self.lower is None
+
+
+def test_unknown_solver_is_fatal_like_the_reference():
+    with pytest.raises(ldu.FatalError, match="Unknown symmetric matrix solver smoothSolver"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "smoothSolver"})
+    with pytest.raises(ldu.FatalError, match="Unknown asymmetric matrix solver cudaPCG"):
+        ldu.solver_new("U", _FakeMatrix(False), {"solver": "cudaPCG", "preconditioner": "DILU"})
+    with pytest.raises(ldu.FatalError, match="keyword solver is undefined"):
+        ldu.solver_new("p", _FakeMatrix(True), {"tolerance": 1e-6})
+    with pytest.raises(ldu.FatalError, match="preconditioner"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaPCG", "preconditioner": "ILU0"})
+    with pytest.raises(ldu.FatalError, match="smoother"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "smoother": "symGaussSeidel"})
+    with pytest.raises(ldu.FatalError, match="GAMGAgglomeration"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "agglomerator": "algebraicPair"})
+
+
+def test_controls_parse():
+    s = ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "tolerance": 1e-8, "relTol": 0.01,
+                                                "nPreSweeps": 2, "smoother": "DIC", "precision": "mixed",
+                                                "minCellsPerProcessor": 20})
+    c = s.c
+    assert c.solver == ldu.SOLVER_GAMG and c.tolerance == 1e-8 and c.relTol == 0.01
+    assert c.nPreSweeps == 2 and c.smoother == 1 and c.precision == 1 and c.nCellsInCoarsestLevel == 20
+
+
+def test_solver_performance_print_format():
+    p = ldu.SolverPerformance("DICPCG", "T", 1.0, 5e-9, 32, True, False)
+    assert str(p) == "DICPCG:  Solving for T, Initial residual = 1, Final residual = 5e-09, No Iterations 32"
+    p.singular = True
+    assert str(p) == "DICPCG:  Solving for T:  solution singularity"
+
+
+def test_weights_match_oracle():
+    s = cases.gamg_cube(9, jitter=0.3, seed=4)
+    np.testing.assert_array_equal(ldu.face_area_pair_weights(s["Sf"]), orc.face_area_pair_weights(s["Sf"]))
+
+
+def test_renumbering_keeps_upper_triangular_order_and_operator():
+    s = cases.bicgstab_cube(7, seed=3)
+    l, u = s["l"], s["u"]
+    assert np.all(l < u)
+    assert np.all(np.diff(l) >= 0)
+    same = np.diff(l) == 0
+    assert np.all(np.diff(u)[same] > 0)
+    # the renumbered operator is a permutation of the original one
+    s0 = cases.convection_diffusion(cases.box_mesh(7, 7, 7, jitter=0.2, seed=3), s["U"], 1e-3)
+    order = cases.random_order(3 + 7, s0["diag"].size)
+    s1 = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s0.items()}
+    cases.renumber(s1, order)
+    x = np.random.default_rng(0).uniform(-1, 1, s0["diag"].size)
+    y0 = orc.Matrix(s0).amul(x)
+    y1 = orc.Matrix(s1).amul(x[order])
+    np.testing.assert_allclose(y1, y0[order], rtol=0, atol=1e-14)
+
+
+def test_cuthill_mckee_is_a_permutation_and_reduces_bandwidth():
+    s = cases.convection_diffusion(cases.box_mesh(6, 6, 6, seed=1), [1.0, 0.0, 0.0], 1e-3)
+    cases.renumber(s, cases.random_order(5, s["diag"].size))
+    bw0 = int(np.max(s["u"] - s["l"]))
+    order = cases.cuthill_mckee(s)
+    assert np.array_equal(np.sort(order), np.arange(s["diag"].size))
+    cases.renumber(s, order)
+    assert int(np.max(s["u"] - s["l"])) < bw0
+
+
+def test_batch_box_shapes_log_uniform():
+    boxes = cases.batch_boxes(64, seed=3)
+    n = np.array([a * b * c for a, b, c, _, _ in boxes])
+    assert n.min() >= 2000 and n.max() <= 700000
+    assert len({f for *_, f, _ in boxes}) > 1

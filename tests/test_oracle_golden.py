@@ -1,0 +1,105 @@
+"""The C oracle against the reference's own outputs (golden fixtures).
+
+The fixtures were produced by the reference code built from source
+(tests/golden/make_golden.py); the oracle must reproduce them bit for bit:
+same operation order, no FMA contraction.  This pins the oracle that every
+GPU parity test compares against.
+"""
+import numpy as np
+import pytest
+
+from golden_cases import CHECKSUMS, SPECS, checksum, gamg_kwargs, load, solve_case, system
+from oracle import oracle as orc
+from openfoam_dev_gb300 import cases
+
+
+def test_case_inputs_unchanged():
+    for name, digest in CHECKSUMS.items():
+        assert checksum(system(name)) == digest, name
+
+
+def test_geometry_matches_polymesh():
+    g = load("geom_box567.npz")
+    m = cases.box_mesh(int(g["nx"]), int(g["ny"]), int(g["nz"]), jitter=float(g["jitter"]), seed=int(g["seed"]))
+    for k in ("Sf", "Cf", "magSf", "C", "V"):
+        np.testing.assert_array_equal(m[k], g[k], err_msg=k)
+
+
+@pytest.mark.parametrize("name", ["cube6", "jcube7", "cd6", "box"])
+def test_single_operations(name):
+    s = system(name)
+    g = load(f"ops_{name}.npz")
+    m = orc.Matrix(s)
+    x, b = g["x"], s["source"]
+    os_, lo, ls = m.addr()
+    np.testing.assert_array_equal(os_, g["ownerStart"])
+    np.testing.assert_array_equal(lo, g["losort"])
+    np.testing.assert_array_equal(ls, g["losortStart"])
+    np.testing.assert_array_equal(m.amul(x), g["Amul"])
+    np.testing.assert_array_equal(m.tmul(x), g["Tmul"])
+    np.testing.assert_array_equal(m.residual(x, b), g["residual"])
+    np.testing.assert_array_equal(m.sumA(), g["sumA"])
+    assert m.norm_factor(x, b) == g["normFactor"][0]
+    L = orc.lib()
+    bp = b.ctypes.data_as(orc.f64p)
+    xp = x.ctypes.data_as(orc.f64p)
+    assert L.ldu_sum_mag(b.size, bp) == g["sumMag"][0]
+    assert L.ldu_sum_prod(b.size, xp, bp) == g["sumProd"][0]
+    assert L.ldu_sum_sqr(b.size, bp) == g["sumSqr"][0]
+    assert L.ldu_sum(b.size, bp) == g["sum"][0]
+    assert L.ldu_average(x.size, xp) == g["average"][0]
+    if s.get("lower") is None:
+        np.testing.assert_array_equal(m.dic_rD(), g["DIC_rD"])
+        np.testing.assert_array_equal(m.dic_precondition(b), g["DIC_precondition"])
+        np.testing.assert_array_equal(m.dic_smooth(x, b, 2), g["DIC_smooth2"])
+    else:
+        np.testing.assert_array_equal(m.dilu_rD(), g["DILU_rD"])
+        np.testing.assert_array_equal(m.dilu_precondition(b), g["DILU_precondition"])
+        np.testing.assert_array_equal(m.dilu_preconditionT(b), g["DILU_preconditionT"])
+    np.testing.assert_array_equal(m.gs_smooth(x, b, 1), g["GS_smooth1"])
+    np.testing.assert_array_equal(m.gs_smooth(x, b, 3), g["GS_smooth3"])
+
+
+def _run_oracle(s, ctl):
+    psi = np.zeros_like(s["source"])
+    kw = dict(tol=ctl.get("tolerance", 1e-6), rel_tol=ctl.get("relTol", 0.0), max_iter=ctl.get("maxIter", 1000),
+              min_iter=ctl.get("minIter", 0))
+    if ctl["solver"] == "PCG":
+        p = orc.pcg(s, psi, precond=ctl["preconditioner"], **kw)
+    elif ctl["solver"] == "PBiCGStab":
+        p = orc.pbicgstab(s, psi, precond=ctl["preconditioner"], **kw)
+    else:
+        p = orc.gamg(s, psi, **kw, **gamg_kwargs(ctl))
+    return psi, p
+
+
+@pytest.mark.parametrize("name", sorted(SPECS["solves"]))
+def test_solvers_bit_exact(name):
+    s, ctl, g = solve_case(name)
+    psi, p = _run_oracle(s, ctl)
+    np.testing.assert_array_equal(psi, g["psi"])
+    assert p.nIterations == g["nIterations"][0]
+    assert p.initialResidual == g["initialResidual"][0]
+    assert p.finalResidual == g["finalResidual"][0]
+    assert p.converged == bool(g["converged"][0])
+    assert p.singular == bool(g["singular"][0])
+
+
+@pytest.mark.parametrize("name", [n for n, (_, c) in sorted(SPECS["solves"].items()) if c["solver"] == "GAMG"])
+def test_agglomeration_and_coarse_matrices(name):
+    s, ctl, g = solve_case(name)
+    agg = orc.Agglomeration(s, n_coarsest=ctl.get("nCellsInCoarsestLevel", 10))
+    assert agg.n_levels == g["nLevels"][0]
+    fine = s
+    for i in range(agg.n_levels):
+        ra, fra, flip, nc, ncf, cl, cu = agg.level(i)
+        np.testing.assert_array_equal(ra, g[f"restrict{i}"])
+        np.testing.assert_array_equal(fra, g[f"faceRestrict{i}"])
+        np.testing.assert_array_equal(flip, g[f"faceFlip{i}"])
+        np.testing.assert_array_equal(cl, g[f"coarseL{i}"])
+        np.testing.assert_array_equal(cu, g[f"coarseU{i}"])
+        assert nc == g[f"nCells{i}"][0] and ncf == g[f"nFaces{i}"][0]
+        cd, cup, clo = orc.coarse_matrix(fine, agg, i)
+        np.testing.assert_array_equal(cd, g[f"coarseDiag{i}"])
+        np.testing.assert_array_equal(cup, g[f"coarseUpper{i}"])
+        fine = dict(l=cl, u=cu, diag=cd, upper=cup, lower=clo)

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -99,6 +100,20 @@ struct cfx_mesh {
     std::vector<LevelMesh> dev;
     int nCoarseLevels = 0;         // GAMG levels below the mesh (0: none)
     uint64_t version = 1;          // bumped when the level hierarchy changes
+    // packed sweep schedules per level, built on first use
+    struct Scheds {
+        DevSched fwd, bwd;
+        bool hasFwd = false, hasBwd = false;
+        std::map<int, DevSched> gs;
+    };
+    std::vector<Scheds> sched;
+    Arena schedArena;
+};
+
+template <class T>
+struct LevelPack {
+    Packed<T> rd, fwd, bwd;
+    std::map<int, Packed<T>> gs;
 };
 
 // Named device work vectors of one precision; slot i keeps its allocation
@@ -136,6 +151,8 @@ struct cfx_matrix {
     std::vector<Work<double>> lv64;  // per-level GAMG vectors
     std::vector<Work<float>> lv32;
     Arena blockArena;
+    std::vector<LevelPack<double>> p64;
+    std::vector<LevelPack<float>> p32;
     BlockSys<double>* d_blk64 = nullptr;
     BlockSys<float>* d_blk32 = nullptr;
     GraphCache gPCG, gBiCG, gGAMG, gMixed;
@@ -394,6 +411,8 @@ void prepare_levels(cfx_matrix* mat, bool want32) {
     }
 }
 
+void invalidate_packs(cfx_matrix* mat);
+
 void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, const double* lower,
                       cudaMemcpyKind kind) {
     cfx_mesh* mesh = mat->mesh;
@@ -405,20 +424,131 @@ void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, 
     if (!mat->sym && m.nf) CK(cudaMemcpyAsync(c.lower, lower, sizeof(double) * m.nf, kind, s));
     Ops<double>::permute(s, m, c);
     mat->coarse64 = mat->coarse32 = mat->fine32 = false;
+    invalidate_packs(mat);
+}
+
+// ---- packed sweep schedules and coefficients ------------------------------
+DevSched upload_sched(Arena& ar, cudaStream_t s, const HostSched& h) {
+    DevSched d;
+    d.kind = h.kind;
+    d.nSweeps = h.nSweeps;
+    d.nLevels = h.nLevels;
+    d.n = h.n;
+    d.maxK = h.maxK;
+    d.nSlots = int(h.cell.size());
+    d.nEntries = int(h.nb.size());
+    d.nGroups = int(h.groupEntry.size()) - 1;
+    d.nChunks = int(h.chunkLevel.size());
+    d.maxLevelBytes8 = h.maxLevelBytes8;
+    d.levelSlot = ar.upload(h.levelSlot, s);
+    d.levelEntry = ar.upload(h.levelEntry, s);
+    d.groupEntry = ar.upload(h.groupEntry, s);
+    d.cell = ar.upload(h.cell, s);
+    d.cnt = ar.upload(h.cnt, s);
+    d.nb = ar.upload(h.nb, s);
+    d.src = ar.upload(h.src, s);
+    d.chunkGroup = ar.upload(h.chunkGroup, s);
+    d.chunkLevel = ar.upload(h.chunkLevel, s);
+    d.levelChunks = ar.upload(h.levelChunks, s);
+    d.sync = ar.get<int>(2 + std::max(h.nLevels, 1));
+    CK(cudaMemsetAsync(d.sync, 0, sizeof(int) * (2 + std::max(h.nLevels, 1)), s));
+    return d;
+}
+
+// Schedule of level lv (kind SCHED_*, S combined Gauss-Seidel sweeps).
+const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
+    if ((int)mesh->sched.size() < (int)mesh->host.size()) mesh->sched.resize(mesh->host.size());
+    cfx_mesh::Scheds& sc = mesh->sched[lv];
+    cudaStream_t s = mesh->ctx->stream;
+    if (kind == SCHED_FWD) {
+        if (!sc.hasFwd) {
+            HostSched h;
+            build_sched(mesh->host[lv], SCHED_FWD, 1, h);
+            sc.fwd = upload_sched(mesh->schedArena, s, h);
+            sc.hasFwd = true;
+        }
+        return sc.fwd;
+    }
+    if (kind == SCHED_BWD) {
+        if (!sc.hasBwd) {
+            HostSched h;
+            build_sched(mesh->host[lv], SCHED_BWD, 1, h);
+            sc.bwd = upload_sched(mesh->schedArena, s, h);
+            sc.hasBwd = true;
+        }
+        return sc.bwd;
+    }
+    auto it = sc.gs.find(S);
+    if (it == sc.gs.end()) {
+        HostSched h;
+        build_sched(mesh->host[lv], SCHED_GS, S, h);
+        it = sc.gs.emplace(S, upload_sched(mesh->schedArena, s, h)).first;
+    }
+    return it->second;
+}
+
+template <class T>
+std::vector<LevelPack<T>>& packs_of(cfx_matrix* mat);
+template <>
+std::vector<LevelPack<double>>& packs_of<double>(cfx_matrix* mat) {
+    return mat->p64;
+}
+template <>
+std::vector<LevelPack<float>>& packs_of<float>(cfx_matrix* mat) {
+    return mat->p32;
+}
+
+template <class T>
+Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd) {
+    auto& v = packs_of<T>(mat);
+    if ((int)v.size() <= lv) v.resize(lv + 1);
+    LevelPack<T>& lp = v[lv];
+    Packed<T>* p = op == OP_RD ? &lp.rd : op == OP_FWD ? &lp.fwd : op == OP_BWD ? &lp.bwd : &lp.gs[S];
+    if (!p->coef) {
+        p->coef = mat->arena.get<T>(sd.nEntries);
+        p->scalar = mat->arena.get<T>(sd.nSlots);
+    }
+    return *p;
+}
+
+void invalidate_packs(cfx_matrix* mat) {
+    for (auto& l : mat->p64) {
+        l.rd.valid = l.fwd.valid = l.bwd.valid = false;
+        for (auto& kv : l.gs) kv.second.valid = false;
+    }
+    for (auto& l : mat->p32) {
+        l.rd.valid = l.fwd.valid = l.bwd.valid = false;
+        for (auto& kv : l.gs) kv.second.valid = false;
+    }
+}
+
+void ensure_chunk_partials(cfx_ctx* ctx, size_t chunks) {
+    const size_t need = std::max<size_t>(chunks, RED_MAXB) + 16;
+    if (ctx->sc.chunkPartialsCap < need) {
+        ctx->sc.chunkPartials = ctx->arena.get<double>(need);
+        ctx->sc.chunkPartialsCap = need;
+    }
 }
 
 // rD of DIC / DILU (DICPreconditioner.C:57-84, DILUPreconditioner.C:57-85):
-// pivot sweep in level order, then the reciprocal.
+// pivot sweep in level order, then the reciprocal; then the forward and
+// backward coefficients (rD_c*lower, rD_c*upper) are packed.
 template <class T>
-cfx_status compute_rD(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c) {
-    SweepArgs<T> a{};
-    a.diag = c.diag;
-    a.lp = c.lowerPerm;
-    a.up = c.sym ? c.lowerPerm : c.upperPerm;
-    a.x = c.rD;
-    CFX_TRY(run_sweep<T>(ctx->stream, m, m.fwd, SW_RD, a, ctx->d_status));
-    Ops<T>::reciprocal(ctx->stream, m.n, c.rD);
-    return CFX_OK;
+void compute_rD(cfx_matrix* mat, int lv) {
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const LevelMesh& m = mat->mesh->dev[lv];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
+    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    ensure_chunk_partials(ctx, std::max(f.nChunks, b.nChunks));
+    Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f);
+    pack_sweep<T>(s, f, OP_RD, c, prd);
+    if (run_sweep<T>(s, f, OP_RD, prd, nullptr, c.rD, nullptr, nullptr, nullptr, ctx->d_status) != CFX_OK)
+        throw CudaError(last_error());
+    Ops<T>::reciprocal(s, m.n, c.rD);
+    pack_sweep<T>(s, f, OP_FWD, c, packed<T>(mat, lv, OP_FWD, 1, f));
+    pack_sweep<T>(s, b, OP_BWD, c, packed<T>(mat, lv, OP_BWD, 1, b));
 }
 
 template <class T>
@@ -427,25 +557,25 @@ void diag_reciprocal(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c) {
     Ops<T>::reciprocal(ctx->stream, m.n, c.rD);
 }
 
-// w = M^-1 r with the w.r dot partials in ctx->sc.chunkPartials.  Returns the
-// number of partials.
+// w = M^-1 r with the w.r dot partials in ctx->sc.chunkPartials when dot.
+// Returns the number of partials.  DIC/DILU packs must be current
+// (compute_rD).
 template <class T>
-int precondition(cfx_ctx* ctx, const LevelMesh& m, const LevelCoeffs<T>& c, int kind, const T* r, T* w,
-                 const int* done, bool dot) {
+int precondition(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int* done, bool dot) {
+    cfx_ctx* ctx = mat->mesh->ctx;
     cudaStream_t s = ctx->stream;
+    const LevelMesh& m = mat->mesh->dev[lv];
+    LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
-        SweepArgs<T> a{};
-        a.rD = c.rD;
-        a.lp = c.lowerPerm;
-        a.upper = c.upper;
-        a.in = r;
-        a.x = w;
-        a.done = done;
-        if (run_sweep<T>(s, m, m.fwd, SW_DIC_FWD, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
-        a.dotWith = dot ? r : nullptr;
-        a.chunkPartials = ctx->sc.chunkPartials;
-        if (run_sweep<T>(s, m, m.bwd, SW_BWD, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
-        return sweep_partials(m, m.bwd);
+        const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
+        const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+        if (run_sweep<T>(s, f, OP_FWD, packed<T>(mat, lv, OP_FWD, 1, f), r, w, nullptr, nullptr, done,
+                         ctx->d_status) != CFX_OK)
+            throw CudaError(last_error());
+        if (run_sweep<T>(s, b, OP_BWD, packed<T>(mat, lv, OP_BWD, 1, b), nullptr, w, dot ? r : nullptr,
+                         ctx->sc.chunkPartials, done, ctx->d_status) != CFX_OK)
+            throw CudaError(last_error());
+        return sweep_partials<T>(b);
     }
     Kern<T>::precond_pointwise(s, m.n, kind == CFX_PRE_DIAGONAL ? c.rD : nullptr, r, w, ctx->sc.chunkPartials,
                                done);
@@ -453,22 +583,26 @@ int precondition(cfx_ctx* ctx, const LevelMesh& m, const LevelCoeffs<T>& c, int 
     return std::max(1, std::min(g, RED_MAXB));
 }
 
-void ensure_chunk_partials(cfx_ctx* ctx, const LevelMesh& m) {
-    const size_t need = std::max<size_t>(std::max(m.fwd.nChunks, m.bwd.nChunks), RED_MAXB) + 16;
-    if (ctx->sc.chunkPartialsCap < need) {
-        ctx->sc.chunkPartials = ctx->arena.get<double>(need);
-        ctx->sc.chunkPartialsCap = need;
+template <class T>
+void setup_preconditioner(cfx_matrix* mat, int lv, int kind) {
+    cfx_ctx* ctx = mat->mesh->ctx;
+    if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
+        compute_rD<T>(mat, lv);
+    } else if (kind == CFX_PRE_DIAGONAL) {
+        diag_reciprocal<T>(ctx, mat->mesh->dev[lv], coeffs<T>(mat, lv));
     }
+    ensure_chunk_partials(ctx, RED_MAXB);
 }
 
+// Gauss-Seidel coefficients for S fused sweeps on level lv.
 template <class T>
-void setup_preconditioner(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c, int kind) {
-    if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
-        if (compute_rD<T>(ctx, m, c) != CFX_OK) throw CudaError(last_error());
-    } else if (kind == CFX_PRE_DIAGONAL) {
-        diag_reciprocal<T>(ctx, m, c);
-    }
+void prepare_gs(cfx_matrix* mat, int lv, int S) {
+    const DevSched& g = sched(mat->mesh, lv, SCHED_GS, S);
+    Packed<T>& p = packed<T>(mat, lv, OP_GS, S, g);
+    if (!p.valid) pack_sweep<T>(mat->mesh->ctx->stream, g, OP_GS, coeffs<T>(mat, lv), p);
 }
+
+constexpr int MAX_FUSED_SWEEPS = 4;
 
 // ----------------------------------------------------------- PCG / PBiCGStab
 // One Krylov solve in precision T on level lv of the matrix.  psi/b are T
@@ -483,7 +617,6 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     const int n = m.n;
     W.n = std::max(W.n, n);
-    ensure_chunk_partials(ctx, m);
     SolveState* st = ctx->d_state + slot;
     set_state(ctx, slot, ctl, tol, relTol, maxIter, minIter);
     T* r = W.get(0, n);
@@ -495,7 +628,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     count_launch();
     Ops<T>::amul(s, m, c, psi, w);
     Kern<T>::norm_init(s, ctx->sc, m, c, w, b, r, r0, st);
-    setup_preconditioner<T>(ctx, m, c, precond);
+    setup_preconditioner<T>(mat, lv, precond);
     const int* done = &st->done;
     int iters = 0;
     if (solver == CFX_SOLVER_PBICGSTAB)
@@ -505,7 +638,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD)});
     auto body = [&]() {
         if (solver == CFX_SOLVER_PCG) {
-            const int np = precondition<T>(ctx, m, c, precond, r, w, done, true);
+            const int np = precondition<T>(mat, lv, precond, r, w, done, true);
             Kern<T>::pcg_beta(s, np, ctx->sc.chunkPartials, st);
             Kern<T>::pcg_p(s, n, w, p, st);
             Kern<T>::pcg_amul(s, ctx->sc, m, c, p, w, st);
@@ -518,11 +651,11 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
             T* yA = w;
             Kern<T>::bicg_rho(s, ctx->sc, n, r0, r, st);
             Kern<T>::bicg_p(s, n, r, AyA, p, st);
-            precondition<T>(ctx, m, c, precond, p, yA, done, false);
+            precondition<T>(mat, lv, precond, p, yA, done, false);
             Kern<T>::bicg_amul_alpha(s, ctx->sc, m, c, yA, AyA, r0, st);
             Kern<T>::bicg_s(s, ctx->sc, n, r, AyA, sA, st);
             Kern<T>::bicg_early(s, n, yA, psi, st);
-            precondition<T>(ctx, m, c, precond, sA, zA, done, false);
+            precondition<T>(mat, lv, precond, sA, zA, done, false);
             Kern<T>::bicg_amul_omega(s, ctx->sc, m, c, zA, tA, sA, st);
             Kern<T>::bicg_update(s, ctx->sc, n, yA, zA, sA, tA, psi, r, st);
         }
@@ -547,29 +680,47 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
 }
 
 // ---------------------------------------------------------------------- GAMG
+// nSweeps of GaussSeidel (fused in passes of up to MAX_FUSED_SWEEPS, packs
+// prepared by prepare_gs) or DIC (packs prepared by compute_rD).
 template <class T>
 void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b, int nSweeps, Work<T>& LW) {
     const LevelMesh& m = mat->mesh->dev[lv];
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     cudaStream_t s = ctx->stream;
-    for (int k = 0; k < nSweeps; ++k) {
-        if (kind == CFX_SMOOTH_GS) {
-            // GaussSeidelSmoother.C:125-177
-            SweepArgs<T> a{};
-            a.diag = c.diag;
-            a.lp = c.lowerPerm;
-            a.upper = c.upper;
-            a.in = b;
-            a.x = psi;
-            if (run_sweep<T>(s, m, m.fwd, SW_GS, a, ctx->d_status) != CFX_OK) throw CudaError(last_error());
-        } else {
-            // DICSmoother.C:86-115: rA = b - A psi; rA = M^-1 rA; psi += rA
-            T* rA = LW.get(0, m.n);
-            T* wA = LW.get(1, m.n);
-            Ops<T>::residual(s, m, c, psi, b, rA);
-            precondition<T>(ctx, m, c, CFX_PRE_DIC, rA, wA, nullptr, false);
-            Kern<T>::axpy(s, m.n, T(1), wA, psi, nullptr);
+    if (kind == CFX_SMOOTH_GS) {
+        // GaussSeidelSmoother.C:125-177
+        for (int left = nSweeps; left > 0;) {
+            const int S = std::min(left, MAX_FUSED_SWEEPS);
+            const DevSched& g = sched(mat->mesh, lv, SCHED_GS, S);
+            if (run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, S, g), b, psi, nullptr, nullptr, nullptr,
+                             ctx->d_status) != CFX_OK)
+                throw CudaError(last_error());
+            left -= S;
         }
+        return;
+    }
+    for (int k = 0; k < nSweeps; ++k) {
+        // DICSmoother.C:86-115: rA = b - A psi; rA = M^-1 rA; psi += rA
+        T* rA = LW.get(0, m.n);
+        T* wA = LW.get(1, m.n);
+        Ops<T>::residual(s, m, c, psi, b, rA);
+        precondition<T>(mat, lv, CFX_PRE_DIC, rA, wA, nullptr, false);
+        Kern<T>::axpy(s, m.n, T(1), wA, psi, nullptr);
+    }
+}
+
+// Set up what smooth() needs on level lv for nSweeps (outside graph capture).
+template <class T>
+void prepare_smooth(cfx_matrix* mat, int lv, int kind, int nSweeps, Work<T>& LW) {
+    if (kind == CFX_SMOOTH_GS) {
+        for (int left = nSweeps; left > 0;) {
+            const int S = std::min(left, MAX_FUSED_SWEEPS);
+            prepare_gs<T>(mat, lv, S);
+            left -= S;
+        }
+    } else {
+        LW.get(0, mat->mesh->dev[lv].n);
+        LW.get(1, mat->mesh->dev[lv].n);
     }
 }
 
@@ -694,19 +845,27 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     cy.scratch2 = W.get(G0 + 2, maxSize);
     // smoother / coarsest-solver set-up on every level (initVcycle: the
     // smoothers are constructed per solve, so DIC rD is recomputed)
-    for (int lv = 0; lv < nl; ++lv) {
-        ensure_chunk_partials(ctx, mesh->dev[lv]);
-        if (ctl->smoother == CFX_SMOOTH_DIC) {
-            if (compute_rD<T>(ctx, mesh->dev[lv], coeffs<T>(mat, lv)) != CFX_OK) throw CudaError(last_error());
-            cy.workFor(lv).get(0, mesh->dev[lv].n);  // allocated before graph capture
-            cy.workFor(lv).get(1, mesh->dev[lv].n);
+    // sweep counts used on each level (Vcycle, GAMGSolverSolve.C:179-390)
+    for (int lv = 0; lv < nl - 1; ++lv) {
+        if (ctl->smoother == CFX_SMOOTH_DIC) compute_rD<T>(mat, lv);
+        if (lv == 0) {
+            prepare_smooth<T>(mat, 0, ctl->smoother, ctl->nFinestSweeps, cy.workFor(0));
+            continue;
         }
+        const int li = lv - 1;
+        if (ctl->nPreSweeps)
+            prepare_smooth<T>(mat, lv, ctl->smoother,
+                              std::min(ctl->nPreSweeps + ctl->preSweepsLevelMultiplier * li, ctl->maxPreSweeps),
+                              cy.workFor(lv));
+        prepare_smooth<T>(mat, lv, ctl->smoother,
+                          std::min(ctl->nPostSweeps + ctl->postSweepsLevelMultiplier * li, ctl->maxPostSweeps),
+                          cy.workFor(lv));
     }
+    ensure_chunk_partials(ctx, RED_MAXB);
     const int lc = nl - 1;
     const LevelMesh& m = mesh->dev[lc];
     LevelCoeffs<T>& c = coeffs<T>(mat, lc);
-    if (ctl->smoother != CFX_SMOOTH_DIC)
-        if (compute_rD<T>(ctx, m, c) != CFX_OK) throw CudaError(last_error());
+    compute_rD<T>(mat, lc);  // coarsest PCG+DIC / PBiCGStab+DILU
     BlockSys<T> h{};
     h.n = m.n;
     h.nf = m.nf;
@@ -963,7 +1122,7 @@ cfx_status cfx_ctx_create(int device, cfx_ctx** out) {
         CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        set_num_sms(sms);
+        sweeps_init(sms);
         ctx->sc.partials = ctx->arena.get<double>(RED_MAXB * 4);
         ctx->sc.counters = ctx->arena.get<unsigned>(16);
         ctx->sc.result = ctx->arena.get<double>(16);
@@ -1314,8 +1473,8 @@ cfx_status cfx_reciprocal_d(cfx_matrix* mat, int kind, double* rD) {
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
         const LevelMesh& m = mat->mesh->dev[0];
-        ensure_chunk_partials(ctx, m);
-        setup_preconditioner<double>(ctx, m, mat->c64[0], kind);
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        setup_preconditioner<double>(mat, 0, kind);
         CK(cudaMemcpyAsync(rD, mat->c64[0].rD, sizeof(double) * m.n, cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);
@@ -1333,11 +1492,9 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
         return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
-        const LevelMesh& m = mat->mesh->dev[0];
-        ensure_chunk_partials(ctx, m);
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-        setup_preconditioner<double>(ctx, m, mat->c64[0], kind);
-        precondition<double>(ctx, m, mat->c64[0], kind, r, w, nullptr, false);
+        setup_preconditioner<double>(mat, 0, kind);
+        precondition<double>(mat, 0, kind, r, w, nullptr, false);
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);
         return stc ? cfx_status(stc) : CFX_OK;
@@ -1350,11 +1507,10 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, i
     if (kind == CFX_SMOOTH_DIC && !mat->sym) return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
-        const LevelMesh& m = mat->mesh->dev[0];
-        ensure_chunk_partials(ctx, m);
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
         if ((int)mat->lv64.size() < 1) mat->lv64.resize(1);
-        if (kind == CFX_SMOOTH_DIC) setup_preconditioner<double>(ctx, m, mat->c64[0], CFX_PRE_DIC);
+        if (kind == CFX_SMOOTH_DIC) setup_preconditioner<double>(mat, 0, CFX_PRE_DIC);
+        prepare_smooth<double>(mat, 0, kind, nSweeps, mat->lv64[0]);
         smooth<double>(ctx, mat, 0, kind, psi, b, nSweeps, mat->lv64[0]);
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);

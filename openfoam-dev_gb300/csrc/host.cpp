@@ -220,3 +220,130 @@ void face_area_pair_weights(int nFaces, const double* Sf, double* w) {
 }
 
 }  // namespace cfx
+
+namespace cfx {
+
+// Packed sweep schedules.  A slot is one cell update (for a combined
+// Gauss-Seidel schedule: one cell in one sweep); slots are grouped by DAG
+// level, levels padded to whole groups of 32 slots, entries of a group stored
+// column-major (entry k of lane j at groupEntry[g] + 32*k + j) so a warp loads
+// them coalesced.  src encodes where each entry's coefficient comes from:
+// a losort slot k (lower side) or, with SRC_UPPER set, an owner face f.
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o) {
+    const int n = h.n;
+    const int S = kind == SCHED_GS ? std::max(1, nSweeps) : 1;
+    // level of every (cell, sweep)
+    std::vector<int> lev(size_t(n) * S, 0);
+    if (kind == SCHED_BWD) {
+        for (int f = h.nf - 1; f >= 0; --f) lev[h.l[f]] = std::max(lev[h.l[f]], lev[h.u[f]] + 1);
+    } else {
+        for (int s = 0; s < S; ++s) {
+            int* L = lev.data() + size_t(s) * n;
+            const int* P = s > 0 ? lev.data() + size_t(s - 1) * n : nullptr;
+            if (P) {
+                for (int c = 0; c < n; ++c) L[c] = P[c] + 1;
+                // c^(s) after the previous sweep of its upper neighbours
+                for (int f = 0; f < h.nf; ++f) L[h.l[f]] = std::max(L[h.l[f]], P[h.u[f]] + 1);
+            }
+            for (int f = 0; f < h.nf; ++f) L[h.u[f]] = std::max(L[h.u[f]], L[h.l[f]] + 1);
+        }
+    }
+    int nl = 0;
+    for (int v : lev) nl = std::max(nl, v + 1);
+    if (n == 0) nl = 0;
+    // bucket (sweep-major, ascending cell) by level
+    std::vector<int> cntL(nl + 1, 0);
+    for (int v : lev) cntL[v + 1]++;
+    std::vector<int> start(nl + 1, 0);
+    for (int i = 0; i < nl; ++i) start[i + 1] = start[i] + cntL[i + 1];
+    std::vector<int> order(lev.size());
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (size_t i = 0; i < lev.size(); ++i) order[fill[lev[i]]++] = int(i);
+    }
+    o.kind = kind;
+    o.nSweeps = S;
+    o.nLevels = nl;
+    o.n = n;
+    o.levelSlot.assign(nl + 1, 0);
+    o.levelEntry.assign(nl + 1, 0);
+    o.cell.clear();
+    o.cnt.clear();
+    o.nb.clear();
+    o.src.clear();
+    o.groupEntry.assign(1, 0);
+    o.chunkGroup.assign(1, 0);
+    o.chunkLevel.clear();
+    o.levelChunks.assign(nl, 0);
+    o.maxK = 0;
+    o.maxLevelBytes8 = 0;
+    auto entries_of = [&](int c, std::vector<int>& nbs, std::vector<int>& srcs) {
+        nbs.clear();
+        srcs.clear();
+        if (kind == SCHED_FWD || kind == SCHED_GS) {
+            for (int k = h.losortStart[c]; k < h.losortStart[c + 1]; ++k) {
+                nbs.push_back(h.losortL[k]);
+                srcs.push_back(k);
+            }
+        }
+        if (kind == SCHED_GS) {
+            for (int f = h.ownerStart[c]; f < h.ownerStart[c + 1]; ++f) {
+                nbs.push_back(h.u[f]);
+                srcs.push_back(f | SRC_UPPER);
+            }
+        }
+        if (kind == SCHED_BWD) {
+            for (int f = h.ownerStart[c + 1] - 1; f >= h.ownerStart[c]; --f) {
+                nbs.push_back(h.u[f]);
+                srcs.push_back(f | SRC_UPPER);
+            }
+        }
+    };
+    std::vector<int> nbs, srcs;
+    std::vector<std::vector<int>> gnb(32), gsrc(32);
+    for (int L = 0; L < nl; ++L) {
+        o.levelSlot[L] = int(o.cell.size());
+        o.levelEntry[L] = int(o.nb.size());
+        const int b = start[L], e = start[L + 1];
+        int groupsInChunk = 0;
+        for (int g0 = b; g0 < e; g0 += 32) {
+            int K = 0;
+            for (int j = 0; j < 32; ++j) {
+                const int i = g0 + j;
+                if (i < e) {
+                    const int c = order[i] % n;
+                    entries_of(c, gnb[j], gsrc[j]);
+                    o.cell.push_back(c);
+                    o.cnt.push_back(int(gnb[j].size()));
+                    K = std::max(K, int(gnb[j].size()));
+                } else {
+                    gnb[j].clear();
+                    gsrc[j].clear();
+                    o.cell.push_back(-1);
+                    o.cnt.push_back(0);
+                }
+            }
+            for (int k = 0; k < K; ++k)
+                for (int j = 0; j < 32; ++j) {
+                    const bool has = k < int(gnb[j].size());
+                    o.nb.push_back(has ? gnb[j][k] : 0);
+                    o.src.push_back(has ? gsrc[j][k] : -1);
+                }
+            o.maxK = std::max(o.maxK, K);
+            o.groupEntry.push_back(int(o.nb.size()));
+            if (++groupsInChunk == SCHED_CHUNK_GROUPS || g0 + 32 >= e) {
+                o.chunkGroup.push_back(int(o.groupEntry.size()) - 1);
+                o.chunkLevel.push_back(L);
+                o.levelChunks[L]++;
+                groupsInChunk = 0;
+            }
+        }
+        const int64_t slots = int64_t(o.cell.size()) - o.levelSlot[L];
+        const int64_t ents = int64_t(o.nb.size()) - o.levelEntry[L];
+        o.maxLevelBytes8 = std::max<int64_t>(o.maxLevelBytes8, slots * 16 + ents * 12);
+    }
+    o.levelSlot[nl] = int(o.cell.size());
+    o.levelEntry[nl] = int(o.nb.size());
+}
+
+}  // namespace cfx

@@ -150,42 +150,66 @@ void launch_cast_f2d(cudaStream_t s, int64_t n, const float* in, double* out);
 template <class T>
 void launch_reduce(cudaStream_t s, Scratch& sc, int which, int n, const T* a, const T* b, double* out);
 
+// ---- packed sweep schedules (host.cpp builds, sweeps.cu runs) -------------
+enum { SCHED_FWD = 0, SCHED_BWD = 1, SCHED_GS = 2 };
+constexpr int SRC_UPPER = 1 << 30;       // entry coefficient from upper[f]
+constexpr int SCHED_CHUNK_GROUPS = 8;    // groups of 32 slots per grid chunk
+
+struct HostSched {
+    int kind = 0, nSweeps = 1, nLevels = 0, n = 0, maxK = 0;
+    int64_t maxLevelBytes8 = 0;          // largest level's staged bytes (FP64)
+    std::vector<int> levelSlot, levelEntry, groupEntry, cell, cnt, nb, src;
+    std::vector<int> chunkGroup, chunkLevel, levelChunks;
+};
+
+struct DevSched {
+    int kind = 0, nSweeps = 1, nLevels = 0, n = 0, maxK = 0;
+    int nSlots = 0, nEntries = 0, nGroups = 0, nChunks = 0;
+    int64_t maxLevelBytes8 = 0;
+    int *levelSlot = nullptr, *levelEntry = nullptr, *groupEntry = nullptr;
+    int *cell = nullptr, *cnt = nullptr, *nb = nullptr, *src = nullptr;
+    int *chunkGroup = nullptr, *chunkLevel = nullptr, *levelChunks = nullptr;
+    int* sync = nullptr;                 // [2 + nLevels]: abort, pad, done[level]
+};
+
+// coefficients packed for one schedule and one operation
+template <class T>
+struct Packed {
+    T* coef = nullptr;    // [nEntries]
+    T* scalar = nullptr;  // [nSlots]
+    bool valid = false;
+};
+
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o);
+
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {
-    SW_DIC_FWD = 0,   // w = rD*r, then w_u -= (rD_u*lp)*w_l in losort order
-    SW_BWD = 1,       // w_l -= (rD_l*upper)*w_u, owner faces in reverse order
-    SW_GS = 2,        // psi_c = (b - sum lp*psi_l - sum upper*psi_u)/diag
-    SW_RD = 3,        // D_u -= (up*lp)/D_l (pivots; reciprocal afterwards)
-    SW_T_FWD = 4,     // DILU preconditionT forward: w_u -= (rD_u*upperPerm)*w_l
+    OP_FWD = 0,   // w_c = rD_c*r_c - sum (rD_c*lower)*w_l   (losort order)
+    OP_BWD = 1,   // w_c -= sum (rD_c*upper)*w_u              (owner faces, reverse)
+    OP_GS = 2,    // psi_c = (b_c - sum lower*psi_l - sum upper*psi_u)/diag_c
+    OP_RD = 3,    // D_c = diag_c - sum (upper*lower)/D_l     (pivots; 1/D after)
 };
 
+void sweeps_init(int numSms);
 template <class T>
-struct SweepArgs {
-    const T* rD;        // reciprocal diagonal (DIC/DILU) or nullptr
-    const T* diag;      // GS
-    const T* lp;        // lowerPerm
-    const T* up;        // upperPerm (SW_RD asym, SW_T_FWD)
-    const T* upper;     // owner-side coefficients
-    const T* in;        // r (fwd) or b (GS) ; D initial for SW_RD = diag
-    T* x;               // in/out vector
-    // fused dot of the backward sweep result with `dotWith` (per-chunk partials)
-    const T* dotWith;
-    double* chunkPartials;
-    // when non-null and *done != 0 the sweep returns at once (solver predicate)
-    const int* done;
-};
-
+bool sweep_is_grid(const DevSched& s);
+// number of dot partials a fused backward sweep writes
 template <class T>
-cfx_status run_sweep(cudaStream_t s, const LevelMesh& m, const Schedule& sch, int op,
-                     const SweepArgs<T>& a, int* status, bool forceSmall = false);
+int sweep_partials(const DevSched& s);
+template <class T>
+cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
+                     const T* dotWith, double* partials, const int* done, int* status);
+template <class T>
+void pack_sweep(cudaStream_t st, const DevSched& s, int op, const LevelCoeffs<T>& c, Packed<T>& p);
 
-// Number of dot partials a fused sweep writes (1 for the single-CTA form).
-int sweep_partials(const LevelMesh& m, const Schedule& s, bool forceSmall = false);
-
-// Threshold (cells) below which sweeps run in one CTA with block barriers.
+// meshes with at most this many cells sweep in one CTA even when the vector
+// does not fit in shared memory
 int small_sweep_threshold();
 void set_small_sweep_threshold(int n);
-void set_num_sms(int n);
+size_t sweep_smem_cap();
+void set_sweep_smem_cap(size_t b);
+int sweep_cluster_size();
+void set_sweep_cluster_size(int cs);
 
 // ---- host addressing (host.cpp) ----------------------------------------------
 cfx_status build_host_level(int n, int nf, const int* l, const int* u, HostLevel& h, bool validate);

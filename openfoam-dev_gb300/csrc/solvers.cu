@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(RED_NT) precond_pointwise_k(int n, const T* __
                                                               const T* __restrict__ r, T* __restrict__ w,
                                                               double* partials, const int* done) {
     __shared__ double sh[RED_NT / 32];
-    if (*done) return;
+    if (done && *done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
         const T v = rD ? rD[c] * r[c] : r[c];

@@ -1,28 +1,46 @@
-// sweeps.cu - level-scheduled triangular sweeps (DIC/DILU preconditioning,
-// their reciprocal diagonals, Gauss-Seidel smoothing).
+// sweeps.cu - level-scheduled triangular sweeps on packed schedules: DIC/DILU
+// forward and backward preconditioning, their reciprocal diagonals, and
+// Gauss-Seidel smoothing (several sweeps fused into one pass).
 //
 // The reference runs these as sequential face loops (DICPreconditioner.C:71-122,
 // DILUPreconditioner.C:71-134, GaussSeidelSmoother.C:125-177).  Every cell's
 // result depends only on its lower neighbours (forward) or upper neighbours
-// (backward), so cells of one level of that dependency DAG are independent.
-// Each cell gathers its contributions in the reference's per-cell face order:
+// (backward), so all cells of one level of that dependency DAG are
+// independent.  Each slot gathers its contributions in the reference's
+// per-cell face order:
 //   forward:  losort slots of the cell (faces where it is the neighbour, in
-//             face order), the order in which the face loop reaches it;
-//   backward: owner faces in decreasing face index (the reverse face loop);
-//   GS:       losort slots with new values, then owner faces with old values.
-// With --fmad=false the results equal the sequential sweeps bit for bit.
+//             face order), coefficient rD_c*lower;
+//   backward: owner faces in decreasing face index, coefficient rD_c*upper;
+//   GS:       losort slots with this sweep's values, then owner faces with the
+//             previous sweep's values, divided by the diagonal.
+// Products such as rD_c*lower are rounded exactly as the reference rounds
+// them, and the library is built with --fmad=false, so every result equals
+// the sequential sweep bit for bit.
 //
-// Two execution forms:
-//   sweep_small_k  one CTA walks all levels with block barriers (small or
-//                  coarse meshes: a block barrier costs ~0.1 us);
-//   sweep_multi_k  persistent CTAs take chunks of <= SWEEP_CHUNK cells in
-//                  level order from an atomic ticket; a chunk of level L waits
-//                  (bounded spin) until every chunk of level L-1 has released
-//                  its done-counter.  A CTA only waits on chunks with smaller
-//                  tickets, which are held by running CTAs, so the kernel needs
-//                  no co-residency guarantee.  A wait that exceeds its deadline
-//                  sets the abort flag and an error status; every CTA then
-//                  returns.
+// Several Gauss-Seidel sweeps run as one pass over the combined DAG: cell c in
+// sweep s waits for its lower neighbours in sweep s and its upper neighbours
+// in sweep s-1, so S sweeps take D + 2(S-1) levels instead of S*D.
+//
+// Execution forms:
+//   sweep_cta_k   one CTA of 1024 threads walks the levels with block
+//                 barriers; the vector lives in shared memory when it fits.
+//                 Used for coarse levels and small meshes.
+//   sweep_cluster_k  a cluster of up to 16 CTAs (one GPC) holds the vector in
+//                 distributed shared memory (cell c in CTA c / per) and
+//                 separates levels with the hardware cluster barrier; each
+//                 warp prefetches its next group's packed data into registers
+//                 before the barrier.  Used up to ~16x the single-CTA size.
+//   sweep_grid_k  persistent CTAs, chunk J (8 groups of 32 slots, level
+//                 order) on CTA J mod grid; each CTA loads its next chunk's
+//                 packed data, then waits (bounded spin, acquire) for every
+//                 chunk of the previous level to release its done-counter.
+//                 Launched cooperatively so all CTAs are resident.  A wait
+//                 that exceeds its deadline sets the abort flag and an error
+//                 status; every CTA then returns.
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
 
 #include "device.cuh"
 #include "internal.h"
@@ -33,98 +51,94 @@ namespace cfx {
 namespace {
 
 constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
-int g_small_threshold = 200000;
-int g_num_sms = 152;
+constexpr int GRID_NT = 256;                            // 8 warps = one chunk
+constexpr int CTA_NT = 512;
+constexpr int CL_NT = 512;                              // threads per cluster CTA
+constexpr int PF = 8;                                   // entries held in registers (grid)
+namespace cg = cooperative_groups;
 
-struct AddrPtrs {
-    const int* __restrict__ ownerStart;
-    const int* __restrict__ losortStart;
-    const int* __restrict__ losortL;
-    const int* __restrict__ u;
+int g_num_sms = 152;
+int g_cluster = 0;          // CTAs per cluster of sweep_cluster_k (0: unavailable)
+int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
+int g_grid[2][8];           // resident CTAs of sweep_grid_k per (precision, op)
+size_t g_smem_cap = 200 * 1024;
+
+template <class T>
+struct SweepCtx {
+    const T* coef;
+    const T* scalar;
+    const T* in;
+    T* x;
+    const T* dotWith;
+    double* partials;
+    const int* done;
 };
 
-template <class T, int OP>
-__device__ __forceinline__ T sweep_cell(int c, const AddrPtrs& m, const SweepArgs<T>& a) {
-    if (OP == SW_DIC_FWD || OP == SW_T_FWD) {
-        const T* cf = OP == SW_DIC_FWD ? a.lp : a.up;
-        const T rDc = a.rD[c];
-        T w = rDc * a.in[c];
-        const int k1 = m.losortStart[c + 1];
-        for (int k = m.losortStart[c]; k < k1; ++k) w -= (rDc * cf[k]) * ldcg(a.x + m.losortL[k]);
-        return w;
-    } else if (OP == SW_BWD) {
-        const T rDc = a.rD[c];
-        T w = ldcg(a.x + c);
-        const int f0 = m.ownerStart[c];
-        for (int f = m.ownerStart[c + 1] - 1; f >= f0; --f) w -= (rDc * a.upper[f]) * ldcg(a.x + m.u[f]);
-        return w;
-    } else if (OP == SW_GS) {
-        T v = a.in[c];
-        const int k1 = m.losortStart[c + 1];
-        for (int k = m.losortStart[c]; k < k1; ++k) v -= a.lp[k] * ldcg(a.x + m.losortL[k]);
-        const int f1 = m.ownerStart[c + 1];
-        for (int f = m.ownerStart[c]; f < f1; ++f) v -= a.upper[f] * ldcg(a.x + m.u[f]);
-        return v / a.diag[c];
-    } else {  // SW_RD: pivots D (reciprocal taken afterwards)
-        T D = a.diag[c];
-        const int k1 = m.losortStart[c + 1];
-        for (int k = m.losortStart[c]; k < k1; ++k) D -= (a.up[k] * a.lp[k]) / ldcg(a.x + m.losortL[k]);
-        return D;
-    }
+template <int OP, class T>
+__device__ __forceinline__ T sw_init(T sc, T in, T xc) {
+    if (OP == OP_FWD) return sc * in;
+    if (OP == OP_BWD) return xc;
+    if (OP == OP_GS) return in;
+    return sc;  // OP_RD: pivot starts at the diagonal
+}
+
+template <int OP, class T>
+__device__ __forceinline__ T sw_step(T acc, T cf, T xn) {
+    if (OP == OP_RD) return acc - cf / xn;
+    return acc - cf * xn;
+}
+
+template <int OP, class T>
+__device__ __forceinline__ T sw_fini(T acc, T sc) {
+    if (OP == OP_GS) return acc / sc;
+    return acc;
 }
 
 template <class T, int OP>
-__global__ void __launch_bounds__(SMALL_NT) sweep_small_k(AddrPtrs m, SweepArgs<T> a, const int* __restrict__ cells,
-                                                          const int* __restrict__ levelStart, int nLevels) {
-    __shared__ double sh[SMALL_NT / 32];
+__global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> a, int* status) {
+    __shared__ double sh[GRID_NT / 32];
+    __shared__ int sh_ok;
     if (a.done && *a.done) return;
-    double dot = 0.0;
-    for (int L = 0; L < nLevels; ++L) {
-        const int e = levelStart[L + 1];
-        for (int i = levelStart[L] + threadIdx.x; i < e; i += SMALL_NT) {
-            const int c = cells[i];
-            const T v = sweep_cell<T, OP>(c, m, a);
-            a.x[c] = v;
-            if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
-        }
-        __syncthreads();
-    }
-    if (a.dotWith) {
-        dot = block_sum<SMALL_NT>(dot, sh);
-        if (threadIdx.x == 0) a.chunkPartials[0] = dot;
-    }
-}
-
-template <class T, int OP>
-__global__ void __launch_bounds__(SWEEP_NT) sweep_multi_k(AddrPtrs m, SweepArgs<T> a, Schedule s, int* status) {
-    __shared__ int sh_chunk, sh_ok;
-    __shared__ double sh[SWEEP_NT / 32];
-    int* ticket = s.sync;
-    int* abortf = s.sync + 1;
+    int* abortf = s.sync;
     int* done = s.sync + 2;
-    if (a.done && *a.done) return;
-    for (;;) {
-        if (threadIdx.x == 0) sh_chunk = atomicAdd(ticket, 1);
-        __syncthreads();
-        const int chunk = sh_chunk;
-        if (chunk >= s.nChunks) return;
-        const int level = s.chunkLevel[chunk];
-        const int i = s.chunkStart[chunk] + threadIdx.x;
-        const int c = i < s.chunkStart[chunk + 1] ? s.cells[i] : -1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int J = blockIdx.x; J < s.nChunks; J += gridDim.x) {
+        const int L = s.chunkLevel[J];
+        const int g = s.chunkGroup[J] + w;
+        int c = -1, n = 0, e0 = 0;
+        T sc = T(0), in = T(0);
+        int nbr[PF];
+        T cf[PF];
+        if (g < s.chunkGroup[J + 1]) {
+            const int slot = g * 32 + lane;
+            c = s.cell[slot];
+            if (c >= 0) {
+                n = s.cnt[slot];
+                e0 = s.groupEntry[g] + lane;
+                sc = a.scalar[slot];
+                if (OP == OP_FWD || OP == OP_GS) in = a.in[c];
+#pragma unroll
+                for (int k = 0; k < PF; ++k)
+                    if (k < n) {
+                        nbr[k] = s.nb[e0 + 32 * k];
+                        cf[k] = a.coef[e0 + 32 * k];
+                    }
+            }
+        }
         if (threadIdx.x == 0) {
             int ok = 1;
-            if (level > 0) {
-                const int target = s.levelChunks[level - 1];
-                const int* d = done + level - 1;
+            if (L > 0) {
+                const int target = s.levelChunks[L - 1];
+                const int* d = done + L - 1;
                 uint64_t t0 = 0;
                 unsigned spins = 0;
-                while (ld_acquire(d) < target) {
+                // relaxed poll, then a fence: the acquire pattern
+                while (*(volatile const int*)d < target) {
                     if (*(volatile int*)abortf) {
                         ok = 0;
                         break;
                     }
-                    __nanosleep(32);
-                    if ((++spins & 255u) == 0) {
+                    if ((++spins & 63u) == 0) {
                         const uint64_t t = globaltimer_ns();
                         if (t0 == 0) {
                             t0 = t;
@@ -136,6 +150,7 @@ __global__ void __launch_bounds__(SWEEP_NT) sweep_multi_k(AddrPtrs m, SweepArgs<
                         }
                     }
                 }
+                __threadfence();
             } else if (*(volatile int*)abortf) {
                 ok = 0;
             }
@@ -145,66 +160,415 @@ __global__ void __launch_bounds__(SWEEP_NT) sweep_multi_k(AddrPtrs m, SweepArgs<
         if (!sh_ok) return;
         T v = T(0);
         if (c >= 0) {
-            v = sweep_cell<T, OP>(c, m, a);
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
+#pragma unroll
+            for (int k = 0; k < PF; ++k)
+                if (k < n) acc = sw_step<OP>(acc, cf[k], ldcg(a.x + nbr[k]));
+            for (int k = PF; k < n; ++k) acc = sw_step<OP>(acc, a.coef[e0 + 32 * k], ldcg(a.x + s.nb[e0 + 32 * k]));
+            v = sw_fini<OP>(acc, sc);
             a.x[c] = v;
         }
         if (a.dotWith) {
             double p = c >= 0 ? double(v) * double(a.dotWith[c]) : 0.0;
-            p = block_sum<SWEEP_NT>(p, sh);
-            if (threadIdx.x == 0) a.chunkPartials[chunk] = p;
+            p = block_sum<GRID_NT>(p, sh);
+            if (threadIdx.x == 0) a.partials[J] = p;
         }
         __syncthreads();
-        if (threadIdx.x == 0) red_release_add(done + level, 1);
+        if (threadIdx.x == 0) red_release_add(done + L, 1);
+    }
+}
+
+// Element c of the vector distributed over the cluster (c in CTA c / per).
+template <class T>
+__device__ __forceinline__ T* cl_ref(cg::cluster_group& cl, T* Xl, int per, int c) {
+    const int o = c / per;
+    return cl.map_shared_rank(Xl, o) + (c - o * per);
+}
+
+// Packed data of one group slot held in registers.
+template <class T>
+struct SlotRegs {
+    int c, n, e0;
+    T sc, in;
+    int nbr[PF];
+    T cf[PF];
+};
+
+template <class T, int OP>
+__device__ __forceinline__ void load_slot(const DevSched& s, const SweepCtx<T>& a, int g, int lane, SlotRegs<T>& r) {
+    const int slot = g * 32 + lane;
+    r.c = s.cell[slot];
+    r.n = 0;
+    if (r.c < 0) return;
+    r.n = s.cnt[slot];
+    r.e0 = s.groupEntry[g] + lane;
+    r.sc = a.scalar[slot];
+    r.in = (OP == OP_FWD || OP == OP_GS) ? a.in[r.c] : T(0);
+#pragma unroll
+    for (int k = 0; k < PF; ++k)
+        if (k < r.n) {
+            r.nbr[k] = s.nb[r.e0 + 32 * k];
+            r.cf[k] = a.coef[r.e0 + 32 * k];
+        }
+}
+
+// Entries k >= k0 of one slot, loaded in batches of 8 independent loads so
+// the latency is paid once per batch, then applied in order.
+template <class T, int OP, class XF>
+__device__ __forceinline__ T tail_entries(const DevSched& s, const T* coef, int e0, int k0, int n, T acc, XF xat) {
+    for (int kb = k0; kb < n; kb += 8) {
+        int nb[8];
+        T cf[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (kb + j < n) {
+                nb[j] = s.nb[e0 + 32 * (kb + j)];
+                cf[j] = coef[e0 + 32 * (kb + j)];
+            }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (kb + j < n) acc = sw_step<OP>(acc, cf[j], xat(nb[j]));
+    }
+    return acc;
+}
+
+// One CTA; X = shared-memory copy of the vector when XS, else global.  Each
+// warp loads its first group of the next level into registers before the
+// block barrier, so the global-memory latency overlaps the barrier.
+template <class T, int OP, bool XS>
+__global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double sh[CTA_NT / 32];
+    if (a.done && *a.done) return;
+    T* X = XS ? reinterpret_cast<T*>(smem_raw) : a.x;
+    const int n = s.n;
+    if (XS && (OP == OP_BWD || OP == OP_GS)) {
+        for (int i = threadIdx.x; i < n; i += CTA_NT) X[i] = a.x[i];
+    }
+    constexpr int WARPS = CTA_NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    auto xat = [&](int c) -> T { return XS ? X[c] : ldcg(a.x + c); };
+    SlotRegs<T> cur;
+    cur.c = -1;
+    cur.n = 0;
+    if (s.nLevels > 0) {
+        const int g = (s.levelSlot[0] >> 5) + w;
+        if (g < (s.levelSlot[1] >> 5)) load_slot<T, OP>(s, a, g, lane, cur);
+    }
+    __syncthreads();
+    double dot = 0.0;
+    for (int L = 0; L < s.nLevels; ++L) {
+        const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
+        if (cur.c >= 0) {
+            T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? xat(cur.c) : T(0));
+#pragma unroll
+            for (int k = 0; k < PF; ++k)
+                if (k < cur.n) acc = sw_step<OP>(acc, cur.cf[k], xat(cur.nbr[k]));
+            acc = tail_entries<T, OP>(s, a.coef, cur.e0, PF, cur.n, acc, xat);
+            const T v = sw_fini<OP>(acc, cur.sc);
+            X[cur.c] = v;
+            if (a.dotWith) dot += double(v) * double(a.dotWith[cur.c]);
+        }
+        for (int g = g0 + w + WARPS; g < g1; g += WARPS) {
+            const int slot = g * 32 + lane;
+            const int c = s.cell[slot];
+            if (c < 0) continue;
+            const int cnt = s.cnt[slot];
+            const int e0 = s.groupEntry[g] + lane;
+            const T sc = a.scalar[slot];
+            const T in = (OP == OP_FWD || OP == OP_GS) ? a.in[c] : T(0);
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? xat(c) : T(0));
+            acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
+            const T v = sw_fini<OP>(acc, sc);
+            X[c] = v;
+            if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
+        }
+        cur.c = -1;
+        cur.n = 0;
+        if (L + 1 < s.nLevels) {
+            const int gn = (s.levelSlot[L + 1] >> 5) + w;
+            if (gn < (s.levelSlot[L + 2] >> 5)) load_slot<T, OP>(s, a, gn, lane, cur);
+        }
+        __syncthreads();
+    }
+    if (XS)
+        for (int i = threadIdx.x; i < n; i += CTA_NT) a.x[i] = X[i];
+    if (a.dotWith) {
+        dot = block_sum<CTA_NT>(dot, sh);
+        if (threadIdx.x == 0) a.partials[0] = dot;
     }
 }
 
 template <class T, int OP>
-cfx_status launch_op(cudaStream_t st, const LevelMesh& m, const Schedule& s, const SweepArgs<T>& a, int* status,
-                     bool small) {
-    AddrPtrs p{m.ownerStart, m.losortStart, m.losortL, m.u};
-    if (s.nCells == 0) return CFX_OK;
-    if (small) {
-        sweep_small_k<T, OP><<<1, SMALL_NT, 0, st>>>(p, a, s.cells, s.levelStart, s.nLevels);
-        count_launch();
-    } else {
-        // More CTAs than fit at once are harmless (tickets are taken only by
-        // running CTAs); 8 x 256 threads fill an SM at <= 32 registers.
-        const int grid = g_num_sms * 8;
-        CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
-        const int g = s.nChunks < grid ? s.nChunks : grid;
-        sweep_multi_k<T, OP><<<g, SWEEP_NT, 0, st>>>(p, a, s, status);
-        count_launch();
+__global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T> a, int per) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double sh[CL_NT / 32];
+    if (a.done && *a.done) return;
+    cg::cluster_group cl = cg::this_cluster();
+    const int CS = int(cl.num_blocks());
+    const int rank = int(cl.block_rank());
+    T* Xl = reinterpret_cast<T*>(smem_raw);
+    const int n = s.n;
+    const int base = rank * per;
+    if (OP == OP_BWD || OP == OP_GS)
+        for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) Xl[i] = a.x[base + i];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int WARPS = CL_NT / 32;
+    // level groups g0.., this CTA takes g0 + rank + CS*j, warp w takes j = w, w + WARPS, ...
+    SlotRegs<T> cur;
+    cur.c = -1;
+    cur.n = 0;
+    if (s.nLevels > 0) {
+        const int g = (s.levelSlot[0] >> 5) + rank + CS * w;
+        if (g < (s.levelSlot[1] >> 5)) load_slot<T, OP>(s, a, g, lane, cur);
     }
+    cl.sync();
+    double dot = 0.0;
+    for (int L = 0; L < s.nLevels; ++L) {
+        const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
+        // prefetched first group
+        if (cur.c >= 0) {
+            T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? *cl_ref(cl, Xl, per, cur.c) : T(0));
+#pragma unroll
+            for (int k = 0; k < PF; ++k)
+                if (k < cur.n) acc = sw_step<OP>(acc, cur.cf[k], *cl_ref(cl, Xl, per, cur.nbr[k]));
+            acc = tail_entries<T, OP>(s, a.coef, cur.e0, PF, cur.n, acc,
+                                      [&](int c) -> T { return *cl_ref(cl, Xl, per, c); });
+            const T v = sw_fini<OP>(acc, cur.sc);
+            *cl_ref(cl, Xl, per, cur.c) = v;
+            if (a.dotWith) dot += double(v) * double(a.dotWith[cur.c]);
+        }
+        // further groups of this warp in wide levels
+        for (int g = g0 + rank + CS * (w + WARPS); g < g1; g += CS * WARPS) {
+            const int slot = g * 32 + lane;
+            const int c = s.cell[slot];
+            if (c < 0) continue;
+            const int cnt = s.cnt[slot];
+            const int e0 = s.groupEntry[g] + lane;
+            const T sc = a.scalar[slot];
+            const T in = (OP == OP_FWD || OP == OP_GS) ? a.in[c] : T(0);
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? *cl_ref(cl, Xl, per, c) : T(0));
+            acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc,
+                                      [&](int cc) -> T { return *cl_ref(cl, Xl, per, cc); });
+            const T v = sw_fini<OP>(acc, sc);
+            *cl_ref(cl, Xl, per, c) = v;
+            if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
+        }
+        // arrive (release: this level's writes), prefetch the next level's
+        // packed data while the other CTAs finish, then wait (acquire)
+        cl.barrier_arrive();
+        cur.c = -1;
+        cur.n = 0;
+        if (L + 1 < s.nLevels) {
+            const int gn = (s.levelSlot[L + 1] >> 5) + rank + CS * w;
+            if (gn < (s.levelSlot[L + 2] >> 5)) load_slot<T, OP>(s, a, gn, lane, cur);
+        }
+        cl.barrier_wait();
+    }
+    for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) a.x[base + i] = Xl[i];
+    if (a.dotWith) {
+        dot = block_sum<CL_NT>(dot, sh);
+        if (threadIdx.x == 0) a.partials[rank] = dot;
+    }
+}
+
+// Coefficients of a schedule for one operation (per matrix update).
+template <class T>
+__global__ void pack_k(DevSched s, int op, const T* __restrict__ lp, const T* __restrict__ up,
+                       const T* __restrict__ upper, const T* __restrict__ diag, const T* __restrict__ rD,
+                       T* __restrict__ coef, T* __restrict__ scalar) {
+    const int nThreads = s.nGroups * 32;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nThreads; t += gridDim.x * blockDim.x) {
+        const int g = t >> 5, lane = t & 31;
+        const int c = s.cell[t];
+        const int K = (s.groupEntry[g + 1] - s.groupEntry[g]) >> 5;
+        const int e0 = s.groupEntry[g] + lane;
+        const int n = c >= 0 ? s.cnt[t] : 0;
+        scalar[t] = c < 0 ? T(0) : ((op == OP_FWD || op == OP_BWD) ? rD[c] : diag[c]);
+        for (int k = 0; k < K; ++k) {
+            const int e = e0 + 32 * k;
+            T v = T(0);
+            if (k < n) {
+                const int src = s.src[e];
+                const int i = src & (SRC_UPPER - 1);
+                if (op == OP_FWD) v = rD[c] * lp[i];
+                else if (op == OP_BWD) v = rD[c] * upper[i];
+                else if (op == OP_GS) v = (src & SRC_UPPER) ? upper[i] : lp[i];
+                else v = up[i] * lp[i];  // OP_RD: upper*upper (DIC) / upper*lower (DILU)
+            }
+            coef[e] = v;
+        }
+    }
+}
+
+template <class T>
+inline int prec_index();
+template <>
+inline int prec_index<double>() { return 0; }
+template <>
+inline int prec_index<float>() { return 1; }
+
+template <class T, int OP>
+cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+    if (s.nSlots == 0) return CFX_OK;
+    const size_t xbytes = sizeof(T) * size_t(s.n);
+    const int per = g_cluster ? (s.n + g_cluster - 1) / g_cluster : 0;
+    if (xbytes <= g_smem_cap) {
+        sweep_cta_k<T, OP, true><<<1, CTA_NT, xbytes, st>>>(s, a);
+    } else if (g_cluster && sizeof(T) * size_t(per) <= g_smem_cap) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g_cluster);
+        cfg.blockDim = dim3(CL_NT);
+        cfg.dynamicSmemBytes = sizeof(T) * size_t(per);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = g_cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP>, s, a, per));
+    } else if (s.n <= g_small_threshold) {
+        sweep_cta_k<T, OP, false><<<1, CTA_NT, 0, st>>>(s, a);
+    } else {
+        CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
+        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP]);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(GRID_NT);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_grid_k<T, OP>, s, a, status));
+    }
+    count_launch();
     return CFX_OK;
+}
+
+template <class T, int OP>
+void init_op() {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP>, GRID_NT, 0);
+    g_grid[prec_index<T>()][OP] = g_num_sms * (per > 0 ? per : 1);
+    cudaFuncSetAttribute(sweep_cta_k<T, OP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+// Largest cluster (16, else 8) that can be resident with a full-size
+// shared-memory partition per CTA; 0 when none can.
+int probe_cluster() {
+    for (int cs : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(CL_NT);
+        cfg.dynamicSmemBytes = g_smem_cap;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int num = 0;
+        if (cudaOccupancyMaxActiveClusters(&num, sweep_cluster_k<double, OP_GS>, &cfg) == cudaSuccess && num > 0)
+            return cs;
+        cudaGetLastError();
+    }
+    return 0;
+}
+
+template <class T>
+void init_attrs() {
+    init_op<T, OP_FWD>();
+    init_op<T, OP_BWD>();
+    init_op<T, OP_GS>();
+    init_op<T, OP_RD>();
 }
 
 }  // namespace
 
-int small_sweep_threshold() { return g_small_threshold; }
-void set_num_sms(int n) { g_num_sms = n > 0 ? n : 152; }
-
-int sweep_partials(const LevelMesh& m, const Schedule& s, bool forceSmall) {
-    return (forceSmall || m.n <= g_small_threshold) ? 1 : s.nChunks;
+void sweeps_init(int numSms) {
+    g_num_sms = numSms > 0 ? numSms : 152;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // leave room for the CTA kernel's static shared memory
+    if (optin > 4096) g_smem_cap = size_t(optin) - 4096;
+    init_attrs<double>();
+    init_attrs<float>();
+    g_cluster = probe_cluster();
 }
+
+int sweep_cluster_size() { return g_cluster; }
+void set_sweep_cluster_size(int cs) { g_cluster = cs; }
+
+int small_sweep_threshold() { return g_small_threshold; }
 void set_small_sweep_threshold(int n) { g_small_threshold = n; }
+size_t sweep_smem_cap() { return g_smem_cap; }
+void set_sweep_smem_cap(size_t b) { g_smem_cap = b; }
 
 template <class T>
-cfx_status run_sweep(cudaStream_t st, const LevelMesh& m, const Schedule& s, int op, const SweepArgs<T>& a,
-                     int* status, bool forceSmall) {
-    const bool small = forceSmall || m.n <= g_small_threshold;
+static bool uses_cluster(const DevSched& s) {
+    if (sizeof(T) * size_t(s.n) <= g_smem_cap || !g_cluster) return false;
+    const int per = (s.n + g_cluster - 1) / g_cluster;
+    return sizeof(T) * size_t(per) <= g_smem_cap;
+}
+
+template <class T>
+bool sweep_is_grid(const DevSched& s) {
+    return !(sizeof(T) * size_t(s.n) <= g_smem_cap || uses_cluster<T>(s) || s.n <= g_small_threshold);
+}
+
+template <class T>
+int sweep_partials(const DevSched& s) {
+    if (sweep_is_grid<T>(s)) return s.nChunks;
+    return uses_cluster<T>(s) ? g_cluster : 1;
+}
+
+template <class T>
+cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
+                     const T* dotWith, double* partials, const int* done, int* status) {
+    SweepCtx<T> a{p.coef, p.scalar, in, x, dotWith, partials, done};
     switch (op) {
-        case SW_DIC_FWD: return launch_op<T, SW_DIC_FWD>(st, m, s, a, status, small);
-        case SW_BWD: return launch_op<T, SW_BWD>(st, m, s, a, status, small);
-        case SW_GS: return launch_op<T, SW_GS>(st, m, s, a, status, small);
-        case SW_RD: return launch_op<T, SW_RD>(st, m, s, a, status, small);
-        case SW_T_FWD: return launch_op<T, SW_T_FWD>(st, m, s, a, status, small);
+        case OP_FWD: return launch<T, OP_FWD>(st, s, a, status);
+        case OP_BWD: return launch<T, OP_BWD>(st, s, a, status);
+        case OP_GS: return launch<T, OP_GS>(st, s, a, status);
+        case OP_RD: return launch<T, OP_RD>(st, s, a, status);
         default: set_error("unknown sweep"); return CFX_ERR_ARG;
     }
 }
 
-template cfx_status run_sweep<double>(cudaStream_t, const LevelMesh&, const Schedule&, int, const SweepArgs<double>&,
-                                      int*, bool);
-template cfx_status run_sweep<float>(cudaStream_t, const LevelMesh&, const Schedule&, int, const SweepArgs<float>&,
-                                     int*, bool);
+template <class T>
+void pack_sweep(cudaStream_t st, const DevSched& s, int op, const LevelCoeffs<T>& c, Packed<T>& p) {
+    if (s.nGroups == 0) {
+        p.valid = true;
+        return;
+    }
+    const T* up = c.sym ? c.lowerPerm : c.upperPerm;
+    const int threads = 256;
+    int blocks = (s.nGroups * 32 + threads - 1) / threads;
+    if (blocks > 4096) blocks = 4096;
+    pack_k<T><<<blocks, threads, 0, st>>>(s, op, c.lowerPerm, up, c.upper, c.diag, c.rD, p.coef, p.scalar);
+    count_launch();
+    p.valid = true;
+}
+
+template bool sweep_is_grid<double>(const DevSched&);
+template bool sweep_is_grid<float>(const DevSched&);
+template int sweep_partials<double>(const DevSched&);
+template int sweep_partials<float>(const DevSched&);
+template cfx_status run_sweep<double>(cudaStream_t, const DevSched&, int, const Packed<double>&, const double*,
+                                      double*, const double*, double*, const int*, int*);
+template cfx_status run_sweep<float>(cudaStream_t, const DevSched&, int, const Packed<float>&, const float*, float*,
+                                     const float*, double*, const int*, int*);
+template void pack_sweep<double>(cudaStream_t, const DevSched&, int, const LevelCoeffs<double>&, Packed<double>&);
+template void pack_sweep<float>(cudaStream_t, const DevSched&, int, const LevelCoeffs<float>&, Packed<float>&);
 
 }  // namespace cfx

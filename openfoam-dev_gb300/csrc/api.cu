@@ -507,6 +507,7 @@ Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd) {
     if (!p->coef) {
         p->coef = mat->arena.get<T>(sd.nEntries);
         p->scalar = mat->arena.get<T>(sd.nSlots);
+        p->inS = mat->arena.get<T>(sd.nSlots);
     }
     return *p;
 }

@@ -177,6 +177,7 @@ template <class T>
 struct Packed {
     T* coef = nullptr;    // [nEntries]
     T* scalar = nullptr;  // [nSlots]
+    T* inS = nullptr;     // [nSlots] right-hand side in slot order (scratch)
     bool valid = false;
 };
 

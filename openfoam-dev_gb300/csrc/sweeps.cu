@@ -52,8 +52,8 @@ namespace {
 
 constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
 constexpr int GRID_NT = 256;                            // 8 warps = one chunk
-constexpr int CTA_NT = 512;
-constexpr int CL_NT = 512;                              // threads per cluster CTA
+constexpr int CTA_NT = 256;
+constexpr int CL_NT = 256;                              // threads per cluster CTA
 constexpr int PF = 8;                                   // entries held in registers (grid)
 namespace cg = cooperative_groups;
 
@@ -67,7 +67,8 @@ template <class T>
 struct SweepCtx {
     const T* coef;
     const T* scalar;
-    const T* in;
+    const T* in;     // right-hand side by cell (r or b)
+    const T* inS;    // the same gathered into slot order
     T* x;
     const T* dotWith;
     double* partials;
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
                 n = s.cnt[slot];
                 e0 = s.groupEntry[g] + lane;
                 sc = a.scalar[slot];
-                if (OP == OP_FWD || OP == OP_GS) in = a.in[c];
+                if (OP == OP_FWD || OP == OP_GS) in = a.inS[slot];
 #pragma unroll
                 for (int k = 0; k < PF; ++k)
                     if (k < n) {
@@ -203,7 +204,7 @@ __device__ __forceinline__ void load_slot(const DevSched& s, const SweepCtx<T>& 
     r.n = s.cnt[slot];
     r.e0 = s.groupEntry[g] + lane;
     r.sc = a.scalar[slot];
-    r.in = (OP == OP_FWD || OP == OP_GS) ? a.in[r.c] : T(0);
+    r.in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
 #pragma unroll
     for (int k = 0; k < PF; ++k)
         if (k < r.n) {
@@ -248,16 +249,16 @@ __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a)
     constexpr int WARPS = CTA_NT / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     auto xat = [&](int c) -> T { return XS ? X[c] : ldcg(a.x + c); };
-    SlotRegs<T> cur;
-    cur.c = -1;
-    cur.n = 0;
-    if (s.nLevels > 0) {
-        const int g = (s.levelSlot[0] >> 5) + w;
-        if (g < (s.levelSlot[1] >> 5)) load_slot<T, OP>(s, a, g, lane, cur);
-    }
-    __syncthreads();
+    auto prefetch = [&](int L, SlotRegs<T>& r) {
+        r.c = -1;
+        r.n = 0;
+        if (L < s.nLevels) {
+            const int g = (s.levelSlot[L] >> 5) + w;
+            if (g < (s.levelSlot[L + 1] >> 5)) load_slot<T, OP>(s, a, g, lane, r);
+        }
+    };
     double dot = 0.0;
-    for (int L = 0; L < s.nLevels; ++L) {
+    auto level = [&](int L, SlotRegs<T>& cur) {
         const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
         if (cur.c >= 0) {
             T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? xat(cur.c) : T(0));
@@ -276,20 +277,25 @@ __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a)
             const int cnt = s.cnt[slot];
             const int e0 = s.groupEntry[g] + lane;
             const T sc = a.scalar[slot];
-            const T in = (OP == OP_FWD || OP == OP_GS) ? a.in[c] : T(0);
+            const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
             T acc = sw_init<OP>(sc, in, OP == OP_BWD ? xat(c) : T(0));
             acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
             const T v = sw_fini<OP>(acc, sc);
             X[c] = v;
             if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
         }
-        cur.c = -1;
-        cur.n = 0;
-        if (L + 1 < s.nLevels) {
-            const int gn = (s.levelSlot[L + 1] >> 5) + w;
-            if (gn < (s.levelSlot[L + 2] >> 5)) load_slot<T, OP>(s, a, gn, lane, cur);
-        }
+        // the level after next into the registers just consumed
+        prefetch(L + 2, cur);
         __syncthreads();
+    };
+    // two register sets, two levels ahead (no register copies between levels)
+    SlotRegs<T> A, B;
+    prefetch(0, A);
+    prefetch(1, B);
+    __syncthreads();
+    for (int L = 0; L < s.nLevels; L += 2) {
+        level(L, A);
+        if (L + 1 < s.nLevels) level(L + 1, B);
     }
     if (XS)
         for (int i = threadIdx.x; i < n; i += CTA_NT) a.x[i] = X[i];
@@ -314,31 +320,29 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
         for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) Xl[i] = a.x[base + i];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int WARPS = CL_NT / 32;
+    auto xat = [&](int c) -> T { return *cl_ref(cl, Xl, per, c); };
     // level groups g0.., this CTA takes g0 + rank + CS*j, warp w takes j = w, w + WARPS, ...
-    SlotRegs<T> cur;
-    cur.c = -1;
-    cur.n = 0;
-    if (s.nLevels > 0) {
-        const int g = (s.levelSlot[0] >> 5) + rank + CS * w;
-        if (g < (s.levelSlot[1] >> 5)) load_slot<T, OP>(s, a, g, lane, cur);
-    }
-    cl.sync();
+    auto prefetch = [&](int L, SlotRegs<T>& r) {
+        r.c = -1;
+        r.n = 0;
+        if (L < s.nLevels) {
+            const int g = (s.levelSlot[L] >> 5) + rank + CS * w;
+            if (g < (s.levelSlot[L + 1] >> 5)) load_slot<T, OP>(s, a, g, lane, r);
+        }
+    };
     double dot = 0.0;
-    for (int L = 0; L < s.nLevels; ++L) {
+    auto level = [&](int L, SlotRegs<T>& cur) {
         const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
-        // prefetched first group
         if (cur.c >= 0) {
-            T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? *cl_ref(cl, Xl, per, cur.c) : T(0));
+            T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? xat(cur.c) : T(0));
 #pragma unroll
             for (int k = 0; k < PF; ++k)
-                if (k < cur.n) acc = sw_step<OP>(acc, cur.cf[k], *cl_ref(cl, Xl, per, cur.nbr[k]));
-            acc = tail_entries<T, OP>(s, a.coef, cur.e0, PF, cur.n, acc,
-                                      [&](int c) -> T { return *cl_ref(cl, Xl, per, c); });
+                if (k < cur.n) acc = sw_step<OP>(acc, cur.cf[k], xat(cur.nbr[k]));
+            acc = tail_entries<T, OP>(s, a.coef, cur.e0, PF, cur.n, acc, xat);
             const T v = sw_fini<OP>(acc, cur.sc);
             *cl_ref(cl, Xl, per, cur.c) = v;
             if (a.dotWith) dot += double(v) * double(a.dotWith[cur.c]);
         }
-        // further groups of this warp in wide levels
         for (int g = g0 + rank + CS * (w + WARPS); g < g1; g += CS * WARPS) {
             const int slot = g * 32 + lane;
             const int c = s.cell[slot];
@@ -346,29 +350,43 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
             const int cnt = s.cnt[slot];
             const int e0 = s.groupEntry[g] + lane;
             const T sc = a.scalar[slot];
-            const T in = (OP == OP_FWD || OP == OP_GS) ? a.in[c] : T(0);
-            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? *cl_ref(cl, Xl, per, c) : T(0));
-            acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc,
-                                      [&](int cc) -> T { return *cl_ref(cl, Xl, per, cc); });
+            const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? xat(c) : T(0));
+            acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
             const T v = sw_fini<OP>(acc, sc);
             *cl_ref(cl, Xl, per, c) = v;
             if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
         }
-        // arrive (release: this level's writes), prefetch the next level's
-        // packed data while the other CTAs finish, then wait (acquire)
+        // arrive (release: this level's writes), prefetch the level after
+        // next while the other CTAs finish, then wait (acquire)
         cl.barrier_arrive();
-        cur.c = -1;
-        cur.n = 0;
-        if (L + 1 < s.nLevels) {
-            const int gn = (s.levelSlot[L + 1] >> 5) + rank + CS * w;
-            if (gn < (s.levelSlot[L + 2] >> 5)) load_slot<T, OP>(s, a, gn, lane, cur);
-        }
+        prefetch(L + 2, cur);
         cl.barrier_wait();
+    };
+    SlotRegs<T> A, B;
+    prefetch(0, A);
+    prefetch(1, B);
+    cl.sync();
+    for (int L = 0; L < s.nLevels; L += 2) {
+        level(L, A);
+        if (L + 1 < s.nLevels) level(L + 1, B);
     }
     for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) a.x[base + i] = Xl[i];
     if (a.dotWith) {
         dot = block_sum<CL_NT>(dot, sh);
         if (threadIdx.x == 0) a.partials[rank] = dot;
+    }
+}
+
+// Right-hand side gathered into slot order, so the sweeps load it without
+// first loading the slot's cell index.
+template <class T>
+__global__ void gather_slots_k(int nSlots, const int* __restrict__ cell, const T* __restrict__ in,
+                               T* __restrict__ inS, const int* done) {
+    if (done && *done) return;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nSlots; t += gridDim.x * blockDim.x) {
+        const int c = cell[t];
+        inS[t] = c >= 0 ? in[c] : T(0);
     }
 }
 
@@ -535,7 +553,13 @@ int sweep_partials(const DevSched& s) {
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
                      const T* dotWith, double* partials, const int* done, int* status) {
-    SweepCtx<T> a{p.coef, p.scalar, in, x, dotWith, partials, done};
+    if ((op == OP_FWD || op == OP_GS) && s.nSlots > 0) {
+        int blocks = (s.nSlots + 255) / 256;
+        if (blocks > 4096) blocks = 4096;
+        gather_slots_k<T><<<blocks, 256, 0, st>>>(s.nSlots, s.cell, in, p.inS, done);
+        count_launch();
+    }
+    SweepCtx<T> a{p.coef, p.scalar, in, p.inS, x, dotWith, partials, done};
     switch (op) {
         case OP_FWD: return launch<T, OP_FWD>(st, s, a, status);
         case OP_BWD: return launch<T, OP_BWD>(st, s, a, status);

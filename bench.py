@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Benchmark of the lduMatrix solver path on one GB300 (or N replicas).
+
+Workload (the headline configuration): cudaGAMG with faceAreaPair
+agglomeration, GaussSeidel smoother, nPreSweeps 2, nPostSweeps 2,
+nCellsInCoarsestLevel 10, tolerance 1e-8, relTol 0, on the Laplacian of a
+256^3 hex cube (16.8M cells) with vertices jittered by U[-0.2h, 0.2h], Dirichlet
+T=0 on x=0, source U[-1,1] (seeded, synthetic).
+
+One step is one complete solve from psi = 0 to the 1e-8 residual.  The
+headline value is the FP32-inner / FP64-refined solve's time-to-1e-8; the
+plain FP64 solve is timed too (fp64_time_s, mixed_speedup).  Device timing uses
+CUDA events on the library's stream with the system resident in HBM (its
+arrays are larger than the 129 MB L2, so no flush is needed).  e2e times the
+reference-facing call a plugin makes per solve: coefficient upload, psi and
+source host->device from pinned memory, the solve, psi device->host.
+
+--impl reference times the C restatement of the reference solver (oracle/,
+the reference itself is not built on this machine) on the host cores.
+
+Multi-GPU: replicas only (one independent system per rank, no collective on
+the data path); launch with torchrun, value = max over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "time-to-1e-8 (FP32-refined vs FP64) of cudaGAMG"
+TOL = 1e-8
+GAMG = {"solver": "cudaGAMG", "tolerance": TOL, "relTol": 0.0, "smoother": "GaussSeidel",
+        "nPreSweeps": 2, "nPostSweeps": 2, "nCellsInCoarsestLevel": 10, "maxIter": 200}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=256, help="cube cells per axis")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as tdist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        tdist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = tdist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def reduce_max(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(n):
+    return {"workload": f"cudaGAMG faceAreaPair GaussSeidel nPre2/nPost2, Laplacian of a {n}^3 cube jittered "
+                        f"+-20%, Dirichlet x=0, tolerance 1e-8 relTol 0",
+            "n_cells": n ** 3, "n_faces": 3 * n * n * (n - 1), "solve": "psi=0 to residual 1e-8",
+            "l2": "inputs larger than L2 (no flush): the resident system is several GB"}
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_sample(s, cycles_hint=None):
+    """The oracle (C restatement of GAMGSolver, serial) on a bounded sample of
+    the same workload: agglomeration plus 2 V-cycles, extrapolated to the
+    V-cycles a full solve takes (from the observed per-cycle reduction, or the
+    GPU solve's count, which matches the reference's within one)."""
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    agg = orc.Agglomeration(s, n_coarsest=10)
+    t_agg = time.perf_counter() - t0
+    psi = np.zeros_like(s["source"])
+    kw = dict(tol=TOL, rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=2, nPostSweeps=2)
+    t0 = time.perf_counter()
+    p1 = orc.gamg(s, psi, agg, max_iter=1, **kw)
+    t1 = time.perf_counter() - t0
+    psi = np.zeros_like(s["source"])
+    t0 = time.perf_counter()
+    p2 = orc.gamg(s, psi, agg, max_iter=2, **kw)
+    t2 = time.perf_counter() - t0
+    t_cycle = max(t2 - t1, 1e-9)
+    if cycles_hint:
+        cycles = int(cycles_hint)
+    else:
+        rho = p2.finalResidual / max(p1.finalResidual, 1e-300)
+        cycles = 2 + max(0, math.ceil(math.log(TOL / p2.finalResidual) / math.log(rho))) if rho < 1 else 1000
+    # setup (coarse matrices, smoother set-up) is t1 - t_cycle
+    total = (t1 - t_cycle) + cycles * t_cycle
+    return {"value": total, "cycles": cycles, "t_cycle": t_cycle, "t_setup": t1 - t_cycle,
+            "t_agglomeration": t_agg, "sample_s": t_agg + t1 + t2}
+
+
+def run_reference(args, rank, world, pg):
+    if rank != 0:
+        return 0
+    ge.load_package()
+    from openfoam_dev_gb300 import cases
+    s = cases.gamg_cube(args.n, jitter=0.2, seed=1)
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_reference_sample(s)
+        if i >= args.warmup:
+            samples.append(r)
+    v = statistics.median([r["value"] for r in samples])
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload(args.n),
+            "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "oracle/ldu_oracle.c GAMG (serial C restatement of GAMGSolver, "
+                                       "bit-exact with the reference built from source): agglomeration + "
+                                       f"1 and 2 V-cycles at {args.n}^3, extrapolated to "
+                                       f"{samples[-1]['cycles']} V-cycles; the reference is serial "
+                                       "(no MPI on this host)"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": samples[-1]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local, pg):
+    import torch
+    torch.cuda.set_device(local)
+    ge.load_package()
+    from openfoam_dev_gb300 import cases, ldu
+    n = args.n
+    s = cases.gamg_cube(n, jitter=0.2, seed=1 + rank)
+    ctx = ldu.Context(local)
+    mesh = ldu.LduMesh(ctx, s["diag"].size, s["l"], s["u"])
+    A = ldu.LduMatrix(mesh, s["diag"], s["upper"])
+    mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=10)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    N, F = s["diag"].size, s["l"].size
+    d_src = torch.from_numpy(s["source"]).to(f"cuda:{local}")
+    d_psi = torch.zeros_like(d_src)
+    mixed = ldu.solver_new("T", A, dict(GAMG, precision="mixed"))
+    fp64 = ldu.solver_new("T", A, dict(GAMG, precision="FP64"))
+
+    def device_solve(solver):
+        with torch.cuda.stream(stream):
+            d_psi.zero_()
+        return solver.solve(d_psi, d_src)
+
+    def timed(solver, steps):
+        evs = []
+        perf = None
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            perf = device_solve(solver)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) / 1e3 for a, b in evs], perf
+
+    for _ in range(args.warmup):
+        device_solve(mixed)
+        device_solve(fp64)
+    torch.cuda.synchronize()
+
+    barrier(pg)
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count()
+    with Clocks(local) as clk:
+        t_mixed, p_mixed = timed(mixed, args.steps)
+    launches = ctx.launch_count() - launches0
+    torch.cuda.synchronize()
+    barrier(pg)
+    t_fp64, p_fp64 = timed(fp64, args.steps)
+    barrier(pg)
+
+    # e2e: what a plugin does per fvMatrix::solve, host buffers (pinned)
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    h_diag, h_upper, h_src = pin(s["diag"]), pin(s["upper"]), pin(s["source"])
+    h_psi = torch.zeros(N, dtype=torch.float64).pin_memory().numpy()
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        h_psi[:] = 0.0
+        t0 = time.perf_counter()
+        A.update(h_diag, h_upper)
+        mixed.solve(h_psi, h_src)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e.append(dt)
+
+    # roofline of the largest single kernel: the fused 2-sweep Gauss-Seidel of
+    # the finest level (gather of b into slot order + the level-scheduled
+    # sweep), FP64, timed alone with events on the library's stream
+    d_b = d_src.clone()
+    d_x = torch.zeros_like(d_src)
+    A.smooth("GaussSeidel", d_x, d_b, 2)
+    torch.cuda.synchronize()
+    reps = 5
+    gs = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.smooth("GaussSeidel", d_x, d_b, 2)
+        e1.record(stream)
+        gs.append((e0, e1))
+    torch.cuda.synchronize()
+    t_gs = statistics.median([a.elapsed_time(b) / 1e3 for a, b in gs])
+    # algorithmic bytes of one GS sweep (7sN + sF + 4F + 4N, s = 8): diag, b,
+    # psi read+write, bPrime, upper once, upperAddr, ownerStart
+    gs_bytes = 2 * (7 * 8 * N + 8 * F + 4 * F + 4 * N)
+
+    tm = reduce_max(pg, statistics.median(t_mixed))
+    t64 = reduce_max(pg, statistics.median(t_fp64))
+    te = reduce_max(pg, statistics.median(e2e))
+    if rank != 0:
+        return 0
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = gs_bytes / t_gs / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
+            tr = json.load(fh)
+        traffic = tr.get(f"gs2_finest_{n}")
+    except (OSError, ValueError):
+        pass
+    line = {"metric": METRIC, "value": tm, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tm * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-inner/f64-refined", "data": "synthetic (seeded)",
+            "config": dict(workload(n), parallelism="replicas" if world > 1 else "1 GPU"),
+            "fp64_time_s": t64, "mixed_speedup": t64 / tm, "v_cycles_mixed": p_mixed.nIterations,
+            "v_cycles_fp64": p_fp64.nIterations, "final_residual_mixed": p_mixed.finalResidual,
+            "final_residual_fp64": p_fp64.finalResidual,
+            "e2e": {"value": te, "unit": "s", "h2d_bytes_per_step": 8 * (N + F) + 16 * N,
+                    "d2h_bytes_per_step": 8 * N},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "fused 2-sweep GaussSeidel, finest level (FP64)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "algorithmic_bytes": gs_bytes, "launch_s": t_gs,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline and world == 1:
+        r = cpu_reference_sample(s, cycles_hint=p_fp64.nIterations)
+        line["cpu_baseline"] = {
+            "value": r["value"], "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"oracle GAMG (serial C restatement, bit-exact with the reference build) at {n}^3: "
+                      f"agglomeration + 1 and 2 V-cycles timed, extrapolated to the {r['cycles']} V-cycles "
+                      f"of the FP64 solve ({r['sample_s']:.1f} s of CPU work)",
+            "detail": r}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist()
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world, pg)
+    else:
+        rc = run_ours(args, rank, world, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -156,10 +156,17 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
                             const double* d_source, cfx_perf* perf);
 
 /* ---- tuning (process-wide knobs; no reference counterpart) ---------------
- * CFX_TUNE_SMALL_SWEEP: meshes with at most this many cells run their
- * triangular sweeps in one CTA with block barriers; larger ones use the
- * persistent multi-CTA level scheduler (default 200000). */
-enum { CFX_TUNE_SMALL_SWEEP = 0 };
+ * How triangular sweeps run, by mesh size.  A mesh whose vector fits one
+ * CTA's shared memory sweeps in one CTA; one that fits a cluster's
+ * distributed shared memory sweeps in one cluster; otherwise:
+ *   CFX_TUNE_SMALL_SWEEP    <= this many cells: one CTA, vector in global
+ *                           memory (default 0)
+ *   CFX_TUNE_CLUSTER_GLOBAL <= this many cells: one cluster, vector in global
+ *                           memory, cluster barriers between levels
+ *   larger: the persistent grid-wide level scheduler.
+ *   CFX_TUNE_CLUSTER_SIZE   CTAs per cluster (16 or 8 as the GPU allows; 0
+ *                           disables the cluster forms). */
+enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_SIZE = 2 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

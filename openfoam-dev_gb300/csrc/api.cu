@@ -85,10 +85,12 @@ struct cfx_ctx {
 struct GraphCache {
     cudaGraphExec_t exec = nullptr;
     uint64_t key = 0;
+    int64_t kernels = 0;  // kernel nodes per replay (launch accounting)
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
         key = 0;
+        kernels = 0;
     }
     ~GraphCache() { reset(); }
 };
@@ -337,14 +339,19 @@ void graph_launch(GraphCache& g, uint64_t key, cudaStream_t s, F&& body) {
     if (!g.exec || g.key != key) {
         g.reset();
         cudaGraph_t graph;
+        // kernels are counted when a replay runs them, not when captured
+        const int64_t before = launch_count();
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         body();
         CK(cudaStreamEndCapture(s, &graph));
+        g.kernels = launch_count() - before;
+        count_launch(-int(g.kernels));
         CK(cudaGraphInstantiate(&g.exec, graph, 0));
         cudaGraphDestroy(graph);
         g.key = key;
     }
     CK(cudaGraphLaunch(g.exec, s));
+    count_launch(int(g.kernels));
 }
 
 uint64_t hkey(std::initializer_list<uint64_t> v) {
@@ -634,7 +641,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     int iters = 0;
     if (solver == CFX_SOLVER_PBICGSTAB)
         for (int i = 4; i < 8; ++i) W.get(i, n);
-    const uint64_t key = hkey({mat->mesh->version, uint64_t(small_sweep_threshold()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD)});
     auto body = [&]() {
@@ -929,7 +936,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(mixed), reinterpret_cast<uint64_t>(psi),
@@ -1383,15 +1390,26 @@ cfx_status cfx_solve(cfx_matrix* mat, const cfx_controls* ctl, double* psi, cons
 }
 
 cfx_status cfx_tune_set(int key, int value) {
-    if (key != CFX_TUNE_SMALL_SWEEP || value < 0) return CFX_ERR_ARG;
-    set_small_sweep_threshold(value);
-    return CFX_OK;
+    if (value < 0) return CFX_ERR_ARG;
+    switch (key) {
+        case CFX_TUNE_SMALL_SWEEP: set_small_sweep_threshold(value); return CFX_OK;
+        case CFX_TUNE_CLUSTER_GLOBAL: set_cluster_global_cells(value); return CFX_OK;
+        case CFX_TUNE_CLUSTER_SIZE:
+            if (value != 0 && value != 8 && value != 16 && value != 4 && value != 2) return CFX_ERR_ARG;
+            set_sweep_cluster_size(value);
+            return CFX_OK;
+        default: return CFX_ERR_ARG;
+    }
 }
 
 cfx_status cfx_tune_get(int key, int* value) {
-    if (key != CFX_TUNE_SMALL_SWEEP || !value) return CFX_ERR_ARG;
-    *value = small_sweep_threshold();
-    return CFX_OK;
+    if (!value) return CFX_ERR_ARG;
+    switch (key) {
+        case CFX_TUNE_SMALL_SWEEP: *value = small_sweep_threshold(); return CFX_OK;
+        case CFX_TUNE_CLUSTER_GLOBAL: *value = cluster_global_cells(); return CFX_OK;
+        case CFX_TUNE_CLUSTER_SIZE: *value = sweep_cluster_size(); return CFX_OK;
+        default: return CFX_ERR_ARG;
+    }
 }
 
 // ---------------------------------------------------------- single operations

@@ -211,6 +211,8 @@ size_t sweep_smem_cap();
 void set_sweep_smem_cap(size_t b);
 int sweep_cluster_size();
 void set_sweep_cluster_size(int cs);
+int cluster_global_cells();
+void set_cluster_global_cells(int n);
 
 // ---- host addressing (host.cpp) ----------------------------------------------
 cfx_status build_host_level(int n, int nf, const int* l, const int* u, HostLevel& h, bool validate);

@@ -60,6 +60,7 @@ namespace cg = cooperative_groups;
 int g_num_sms = 152;
 int g_cluster = 0;          // CTAs per cluster of sweep_cluster_k (0: unavailable)
 int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
+int g_cluster_global = 0;   // <= this many cells: one cluster with the vector in global memory
 int g_grid[2][8];           // resident CTAs of sweep_grid_k per (precision, op)
 size_t g_smem_cap = 200 * 1024;
 
@@ -305,7 +306,9 @@ __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a)
     }
 }
 
-template <class T, int OP>
+// DS: vector in distributed shared memory; otherwise in global memory (L2),
+// read with L2-coherent loads, and only the barrier is the cluster's.
+template <class T, int OP, bool DS>
 __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T> a, int per) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double sh[CL_NT / 32];
@@ -316,11 +319,17 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
     T* Xl = reinterpret_cast<T*>(smem_raw);
     const int n = s.n;
     const int base = rank * per;
-    if (OP == OP_BWD || OP == OP_GS)
+    if (DS && (OP == OP_BWD || OP == OP_GS))
         for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) Xl[i] = a.x[base + i];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int WARPS = CL_NT / 32;
-    auto xat = [&](int c) -> T { return *cl_ref(cl, Xl, per, c); };
+    auto xat = [&](int c) -> T { return DS ? *cl_ref(cl, Xl, per, c) : ldcg(a.x + c); };
+    auto xset = [&](int c, T v) {
+        if (DS)
+            *cl_ref(cl, Xl, per, c) = v;
+        else
+            a.x[c] = v;
+    };
     // level groups g0.., this CTA takes g0 + rank + CS*j, warp w takes j = w, w + WARPS, ...
     auto prefetch = [&](int L, SlotRegs<T>& r) {
         r.c = -1;
@@ -340,7 +349,7 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
                 if (k < cur.n) acc = sw_step<OP>(acc, cur.cf[k], xat(cur.nbr[k]));
             acc = tail_entries<T, OP>(s, a.coef, cur.e0, PF, cur.n, acc, xat);
             const T v = sw_fini<OP>(acc, cur.sc);
-            *cl_ref(cl, Xl, per, cur.c) = v;
+            xset(cur.c, v);
             if (a.dotWith) dot += double(v) * double(a.dotWith[cur.c]);
         }
         for (int g = g0 + rank + CS * (w + WARPS); g < g1; g += CS * WARPS) {
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
             T acc = sw_init<OP>(sc, in, OP == OP_BWD ? xat(c) : T(0));
             acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
             const T v = sw_fini<OP>(acc, sc);
-            *cl_ref(cl, Xl, per, c) = v;
+            xset(c, v);
             if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
         }
         // arrive (release: this level's writes), prefetch the level after
@@ -371,7 +380,8 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
         level(L, A);
         if (L + 1 < s.nLevels) level(L + 1, B);
     }
-    for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) a.x[base + i] = Xl[i];
+    if (DS)
+        for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) a.x[base + i] = Xl[i];
     if (a.dotWith) {
         dot = block_sum<CL_NT>(dot, sh);
         if (threadIdx.x == 0) a.partials[rank] = dot;
@@ -426,18 +436,38 @@ inline int prec_index<double>() { return 0; }
 template <>
 inline int prec_index<float>() { return 1; }
 
+enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4 };
+
+// Execution form of a schedule: the vector in one CTA's shared memory, in a
+// cluster's distributed shared memory, or in global memory with a single CTA,
+// one cluster, or the whole grid separating the levels.
+template <class T>
+int mode_of(const DevSched& s) {
+    const size_t xbytes = sizeof(T) * size_t(s.n);
+    if (xbytes <= g_smem_cap) return M_CTA;
+    if (g_cluster) {
+        const int per = (s.n + g_cluster - 1) / g_cluster;
+        if (sizeof(T) * size_t(per) <= g_smem_cap) return M_CLUSTER_DS;
+    }
+    if (s.n <= g_small_threshold) return M_CTA_GLOBAL;
+    if (g_cluster && s.n <= g_cluster_global) return M_CLUSTER_GLOBAL;
+    return M_GRID;
+}
+
 template <class T, int OP>
 cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
     if (s.nSlots == 0) return CFX_OK;
     const size_t xbytes = sizeof(T) * size_t(s.n);
     const int per = g_cluster ? (s.n + g_cluster - 1) / g_cluster : 0;
-    if (xbytes <= g_smem_cap) {
+    const int m = mode_of<T>(s);
+    if (m == M_CTA) {
         sweep_cta_k<T, OP, true><<<1, CTA_NT, xbytes, st>>>(s, a);
-    } else if (g_cluster && sizeof(T) * size_t(per) <= g_smem_cap) {
+    } else if (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) {
+        const bool ds = m == M_CLUSTER_DS;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g_cluster);
         cfg.blockDim = dim3(CL_NT);
-        cfg.dynamicSmemBytes = sizeof(T) * size_t(per);
+        cfg.dynamicSmemBytes = ds ? sizeof(T) * size_t(per) : 0;
         cfg.stream = st;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -446,8 +476,11 @@ cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int*
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP>, s, a, per));
-    } else if (s.n <= g_small_threshold) {
+        if (ds)
+            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, true>, s, a, per));
+        else
+            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, false>, s, a, per));
+    } else if (m == M_CTA_GLOBAL) {
         sweep_cta_k<T, OP, false><<<1, CTA_NT, 0, st>>>(s, a);
     } else {
         CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
@@ -474,8 +507,9 @@ void init_op() {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP>, GRID_NT, 0);
     g_grid[prec_index<T>()][OP] = g_num_sms * (per > 0 ? per : 1);
     cudaFuncSetAttribute(sweep_cta_k<T, OP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
-    cudaFuncSetAttribute(sweep_cluster_k<T, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
-    cudaFuncSetAttribute(sweep_cluster_k<T, OP>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 }
 
 // Largest cluster (16, else 8) that can be resident with a full-size
@@ -494,7 +528,7 @@ int probe_cluster() {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int num = 0;
-        if (cudaOccupancyMaxActiveClusters(&num, sweep_cluster_k<double, OP_GS>, &cfg) == cudaSuccess && num > 0)
+        if (cudaOccupancyMaxActiveClusters(&num, sweep_cluster_k<double, OP_GS, true>, &cfg) == cudaSuccess && num > 0)
             return cs;
         cudaGetLastError();
     }
@@ -533,22 +567,19 @@ size_t sweep_smem_cap() { return g_smem_cap; }
 void set_sweep_smem_cap(size_t b) { g_smem_cap = b; }
 
 template <class T>
-static bool uses_cluster(const DevSched& s) {
-    if (sizeof(T) * size_t(s.n) <= g_smem_cap || !g_cluster) return false;
-    const int per = (s.n + g_cluster - 1) / g_cluster;
-    return sizeof(T) * size_t(per) <= g_smem_cap;
-}
-
-template <class T>
 bool sweep_is_grid(const DevSched& s) {
-    return !(sizeof(T) * size_t(s.n) <= g_smem_cap || uses_cluster<T>(s) || s.n <= g_small_threshold);
+    return mode_of<T>(s) == M_GRID;
 }
 
 template <class T>
 int sweep_partials(const DevSched& s) {
-    if (sweep_is_grid<T>(s)) return s.nChunks;
-    return uses_cluster<T>(s) ? g_cluster : 1;
+    const int m = mode_of<T>(s);
+    if (m == M_GRID) return s.nChunks;
+    return (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) ? g_cluster : 1;
 }
+
+int cluster_global_cells() { return g_cluster_global; }
+void set_cluster_global_cells(int n) { g_cluster_global = n; }
 
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,

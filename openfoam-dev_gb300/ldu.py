@@ -340,7 +340,7 @@ class SolverPerformance:
                 f"Final residual = {self.finalResidual:g}, No Iterations {self.nIterations}")
 
 
-TUNE_SMALL_SWEEP = 0
+TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE = 0, 1, 2
 
 
 def tune_set(key, value):

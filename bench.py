@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=256, help="cube cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", choices=["gs"], default=None,
+                    help="only run the finest-level fused 2-sweep Gauss-Seidel (for profiling)")
     return ap.parse_args()
 
 
@@ -333,8 +335,31 @@ def run_ours(args, rank, world, local, pg):
     return 0
 
 
+def run_kernel_only(args):
+    """The finest-level fused 2-sweep GaussSeidel alone, warmup + steps times."""
+    import torch
+    ge.load_package()
+    from openfoam_dev_gb300 import cases, ldu
+    s = cases.gamg_cube(args.n, jitter=0.2, seed=1)
+    mesh, A = ldu.system_matrix(s)
+    d_b = torch.from_numpy(s["source"]).cuda()
+    d_x = torch.zeros_like(d_b)
+    t = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        A.smooth("GaussSeidel", d_x, d_b, 2)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            t.append(time.perf_counter() - t0)
+    print(json.dumps({"kernel": "gs2_finest", "n": args.n, "s": statistics.median(t)}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.kernel_only:
+        return run_kernel_only(args)
     rank, world, local, pg = dist()
     if args.impl == "reference":
         rc = run_reference(args, rank, world, pg)

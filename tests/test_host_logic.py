@@ -113,3 +113,18 @@ def test_batch_box_shapes_log_uniform():
     n = np.array([a * b * c for a, b, c, _, _ in boxes])
     assert n.min() >= 2000 and n.max() <= 700000
     assert len({f for *_, f, _ in boxes}) > 1
+
+
+REF_FARM = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "lnInclude")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_FARM, "OpenFOAM")),
+                    reason="reference headers (oracle/_ref) not built here")
+def test_plugin_compiles_against_reference_headers():
+    import subprocess
+    src = os.path.join(os.path.dirname(INCLUDE_DIR), "openfoam-dev_gb300", "plugin", "cudaLduSolvers.C")
+    r = subprocess.run(["g++", "-std=c++14", "-fsyntax-only", "-DWM_DP", "-DWM_LABEL_SIZE=32", "-DNoRepository",
+                        "-Dlinux64", "-ftemplate-depth-256", "-w", "-I" + os.path.join(REF_FARM, "OpenFOAM"),
+                        "-I" + os.path.join(REF_FARM, "POSIX"), "-I" + INCLUDE_DIR, src],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

@@ -183,6 +183,21 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
 cfx_status cfx_reciprocal_d(cfx_matrix* mat, int kind, double* d_rD);
 cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* d_psi, const double* d_b, int nSweeps);
 
+/* ---- reduction that allocates nothing ------------------------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot call cudaMalloc (code enqueuing work during CUDA-graph stream
+ * capture, hosts that give all GPU memory to their own pool).  Same
+ * operations as cfx_reduce (which: 0 sum, 1 sumMag, 2 sumSqr, 3 sumProd), no
+ * context: d_a, d_b (device, n doubles) in, the result to the device double
+ * d_out, enqueued on `stream` (a cudaStream_t; NULL = the default stream)
+ * without synchronizing.  Its only scratch is a static device array of 4096
+ * block partials, so n <= 33,554,432 (larger n returns CFX_ERR_ARG).  The
+ * first call on a device looks up that array's address (make it before any
+ * stream capture); calls on one device share the array, so calls that
+ * overlap on the GPU race. */
+cfx_status cfx_reduce_noalloc(int which, int n, const double* d_a, const double* d_b, double* d_out,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ _SIG = {
     "cfx_precondition": (_i, [_vp, _i, _i, _vp, _vp]),
     "cfx_reciprocal_d": (_i, [_vp, _i, _vp]),
     "cfx_smooth": (_i, [_vp, _i, _vp, _vp, _i]),
+    "cfx_reduce_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -166,9 +166,58 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
  *   larger: the persistent grid-wide level scheduler.
  *   CFX_TUNE_CLUSTER_SIZE   CTAs per cluster (16 or 8 as the GPU allows; 0
  *                           disables the cluster forms). */
-enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_SIZE = 2 };
+enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_SIZE = 2,
+       /* FP32 inner solves of mixed-precision batches (cfx_batch_*) reduce
+        * the residual by 10^-value (default 3) per refinement step */
+       CFX_TUNE_BATCH_INNER_DIGITS = 3 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
+
+/* ---- batched solves of many small systems --------------------------------
+ * No counterpart in the reference: many independent lduMatrix systems (an
+ * ensemble of small cases, a parameter sweep) solved by one kernel launch,
+ * one CTA per system.  Each system follows lduMatrix::solver::solve exactly
+ * as cfx_solve does (PCG with symmetric, PBiCGStab with either matrix; any
+ * preconditioner of cfx_controls), or, with precision CFX_MIXED, FP32 inner
+ * solves inside FP64 iterative refinement (normFactor, residuals and the
+ * convergence test in FP64).  The launch hands systems to persistent CTAs
+ * largest first and is replayed from a CUDA graph.  Systems are numbered in
+ * creation order; psi and source vectors are the systems' vectors
+ * concatenated in that order (offsets: prefix sums of nCells). */
+typedef struct cfx_batch cfx_batch;
+/* l[i], u[i]: addressing of system i (as cfx_mesh_create). */
+cfx_status cfx_batch_create(cfx_ctx* ctx, int nSystems, const int32_t* nCells, const int32_t* nFaces,
+                            const int32_t* const* l, const int32_t* const* u, cfx_batch** batch);
+cfx_status cfx_batch_destroy(cfx_batch* batch);
+/* Host coefficients of system i; lower == NULL means symmetric. */
+cfx_status cfx_batch_set_matrix(cfx_batch* batch, int i, const double* diag, const double* upper,
+                                const double* lower);
+/* psi (in/out) and source: host arrays of sum(nCells) doubles; perf[nSystems]. */
+cfx_status cfx_batch_solve(cfx_batch* batch, const cfx_controls* ctl, double* psi, const double* source,
+                           cfx_perf* perf);
+/* The batch's resident device vectors (psi, source, each sum(nCells)
+ * doubles) and the nSystems+1 cell offsets; any pointer may be NULL. */
+cfx_status cfx_batch_vectors(cfx_batch* batch, double** d_psi, double** d_source, int64_t* offsets);
+/* Solve with the resident device vectors; only perf crosses to the host. */
+cfx_status cfx_batch_solve_device(cfx_batch* batch, const cfx_controls* ctl, cfx_perf* perf);
+/* Start and end of each system's solve in the last launch, in ms from the
+ * first start (device clock), creation order; arrays of nSystems. */
+cfx_status cfx_batch_timings(cfx_batch* batch, double* startMs, double* endMs);
+/* Persistent CTAs per SM (0: as many as fit). */
+cfx_status cfx_batch_set_ctas_per_sm(cfx_batch* batch, int ctasPerSm);
+/* Large systems on thread-block clusters: systems of at least bigCells cells
+ * are each solved by a whole cluster of clusterSize CTAs (2..16), the rest
+ * by one CTA each; clusterSize 0 turns clusters off (the default).  A
+ * system's result depends on whether it ran on a cluster (the sums' order
+ * changes), not on the rest of the batch. */
+cfx_status cfx_batch_set_groups(cfx_batch* batch, int clusterSize, int bigCells);
+cfx_status cfx_batch_get_groups(cfx_batch* batch, int* clusterSize, int* nBig, int* ctasPerSm);
+/* Autotuned packing: times resident solves from the current psi (restored
+ * afterwards) with one CTA per system, then with the systems whose solve
+ * outlasted half the balanced share of the batch on clusters of 4, 8 and 16
+ * CTAs, and keeps the fastest.  best = chosen cluster size (0: none);
+ * bestMs = its time.  Either may be NULL. */
+cfx_status cfx_batch_tune(cfx_batch* batch, const cfx_controls* ctl, int* best, float* bestMs);
 
 /* ---- single operations, device pointers (parity tests, building blocks) -- */
 cfx_status cfx_amul(cfx_matrix* mat, const double* d_x, double* d_y);

@@ -15,6 +15,8 @@
 #include <stdexcept>
 
 #include "internal.h"
+#include "batch.h"
+#include "objects.h"
 #include "solvers.h"
 
 namespace cfx {
@@ -26,74 +28,12 @@ thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
 const char* last_error() { return g_err.c_str(); }
 
-struct CudaError : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-
-inline void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) {
-        if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
-        throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
-#define CK(x) ck((x), #x)
-
-// Owner of a set of device allocations.
-struct Arena {
-    std::vector<void*> ptrs;
-    size_t bytes = 0;
-    template <class T>
-    T* get(size_t n) {
-        void* p = nullptr;
-        const size_t b = std::max<size_t>(n, 1) * sizeof(T);
-        CK(cudaMalloc(&p, b));
-        ptrs.push_back(p);
-        bytes += b;
-        return static_cast<T*>(p);
-    }
-    template <class T>
-    T* upload(const std::vector<T>& v, cudaStream_t s) {
-        T* p = get<T>(v.size());
-        if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-        return p;
-    }
-    void release() {
-        for (void* p : ptrs) cudaFree(p);
-        ptrs.clear();
-        bytes = 0;
-    }
-    ~Arena() { release(); }
-};
 
 }  // namespace cfx
 
 using namespace cfx;
 
 // ------------------------------------------------------------------ objects
-struct cfx_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    Arena arena;
-    Scratch sc;
-    SolveState* d_state = nullptr;  // [4]: outer, inner, spare
-    SolveState* h_state = nullptr;  // pinned mirror
-    int* d_status = nullptr;
-    double* d_red = nullptr;        // [8] reduction outputs
-    double* h_red = nullptr;        // pinned
-};
-
-struct GraphCache {
-    cudaGraphExec_t exec = nullptr;
-    uint64_t key = 0;
-    int64_t kernels = 0;  // kernel nodes per replay (launch accounting)
-    void reset() {
-        if (exec) cudaGraphExecDestroy(exec);
-        exec = nullptr;
-        key = 0;
-        kernels = 0;
-    }
-    ~GraphCache() { reset(); }
-};
 
 struct cfx_mesh {
     cfx_ctx* ctx = nullptr;
@@ -163,21 +103,6 @@ struct cfx_matrix {
 // --------------------------------------------------------------- utilities
 namespace {
 
-template <class F>
-cfx_status guard(F&& f) {
-    try {
-        return f();
-    } catch (const std::bad_alloc&) {
-        set_error("device or host allocation failed");
-        return CFX_ERR_NOMEM;
-    } catch (const CudaError& e) {
-        set_error(e.what());
-        return CFX_ERR_CUDA;
-    } catch (const std::exception& e) {
-        set_error(e.what());
-        return CFX_ERR_ARG;
-    }
-}
 
 void upload_schedule(Arena& ar, cudaStream_t s, const std::vector<int>& cells, const std::vector<int>& levelStart,
                      Schedule& sch) {
@@ -333,26 +258,6 @@ int read_status(cfx_ctx* ctx) {
     return h;
 }
 
-// Capture `body` into the cache's executable graph once (keyed), then launch.
-template <class F>
-void graph_launch(GraphCache& g, uint64_t key, cudaStream_t s, F&& body) {
-    if (!g.exec || g.key != key) {
-        g.reset();
-        cudaGraph_t graph;
-        // kernels are counted when a replay runs them, not when captured
-        const int64_t before = launch_count();
-        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        body();
-        CK(cudaStreamEndCapture(s, &graph));
-        g.kernels = launch_count() - before;
-        count_launch(-int(g.kernels));
-        CK(cudaGraphInstantiate(&g.exec, graph, 0));
-        cudaGraphDestroy(graph);
-        g.key = key;
-    }
-    CK(cudaGraphLaunch(g.exec, s));
-    count_launch(int(g.kernels));
-}
 
 uint64_t hkey(std::initializer_list<uint64_t> v) {
     uint64_t h = 1469598103934665603ull;
@@ -1398,6 +1303,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value != 0 && value != 8 && value != 16 && value != 4 && value != 2) return CFX_ERR_ARG;
             set_sweep_cluster_size(value);
             return CFX_OK;
+        case CFX_TUNE_BATCH_INNER_DIGITS:
+            if (value < 1 || value > 7) return CFX_ERR_ARG;
+            batch_set_inner_digits(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -1408,6 +1317,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_SMALL_SWEEP: *value = small_sweep_threshold(); return CFX_OK;
         case CFX_TUNE_CLUSTER_GLOBAL: *value = cluster_global_cells(); return CFX_OK;
         case CFX_TUNE_CLUSTER_SIZE: *value = sweep_cluster_size(); return CFX_OK;
+        case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

@@ -4,7 +4,31 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cfloat>
+
 namespace cfx {
+
+constexpr double VSMALL = DBL_MIN;  // doubleScalarVSmall
+constexpr double SP_SMALL = 1e-20;  // SolverPerformance::small_
+constexpr double SP_GREAT = 1e20;   // SolverPerformance::great_
+
+// One row of A x in the reference's per-cell face order (Amul,
+// lduMatrixATmul.C:34-92, seen from cell c): diag, then the lower
+// coefficients of the faces where c is the neighbour (losort order), then
+// the upper coefficients of the faces c owns.
+template <class T>
+__device__ __forceinline__ T row_amul(int c, const int* __restrict__ os, const int* __restrict__ ls,
+                                      const int* __restrict__ lL, const int* __restrict__ u,
+                                      const T* __restrict__ diag, const T* __restrict__ lp,
+                                      const T* __restrict__ upper, const T* __restrict__ x) {
+    T acc = diag[c] * x[c];
+    const int k1 = ls[c + 1];
+    for (int k = ls[c]; k < k1; ++k) acc += lp[k] * x[lL[k]];
+    const int f1 = os[c + 1];
+    for (int f = os[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
+    return acc;
+}
+
 
 // Fixed-order warp tree (xor-free shuffle down): the same inputs always give
 // the same sum, whatever the launch.

@@ -28,9 +28,6 @@ namespace {
 
 std::atomic<int64_t> g_launches{0};
 
-constexpr double VSMALL = DBL_MIN;  // doubleScalarVSmall
-constexpr double SP_SMALL = 1e-20;  // SolverPerformance::small_
-constexpr double SP_GREAT = 1e20;   // SolverPerformance::great_
 
 inline int grid_for(int64_t n) {
     int64_t b = (n + RED_NT - 1) / RED_NT;
@@ -83,18 +80,6 @@ __device__ __forceinline__ bool reduce2(double a, double b, Red2 r, double& outA
     return true;  // valid in thread 0
 }
 
-template <class T>
-__device__ __forceinline__ T row_amul(int c, const int* __restrict__ os, const int* __restrict__ ls,
-                                      const int* __restrict__ lL, const int* __restrict__ u,
-                                      const T* __restrict__ diag, const T* __restrict__ lp,
-                                      const T* __restrict__ upper, const T* __restrict__ x) {
-    T acc = diag[c] * x[c];
-    const int k1 = ls[c + 1];
-    for (int k = ls[c]; k < k1; ++k) acc += lp[k] * x[lL[k]];
-    const int f1 = os[c + 1];
-    for (int f = os[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
-    return acc;
-}
 
 // normFactor (lduMatrixSolver.C:174-197): sumA*gAverage(psi), then
 // sum(|Apsi - t| + |b - t|) + small_; also r = b - Apsi and sum|r|.
@@ -433,197 +418,6 @@ __global__ void cast_pred_k(int n, const double* __restrict__ in, float* __restr
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) out[c] = float(in[c]);
 }
 
-// ---------------------------------------------------------------- block solver
-constexpr int BLK_NT = 256;
-
-template <class T>
-__device__ __forceinline__ double bsum(double v, double* sh, double* bc) {
-    v = block_sum<BLK_NT>(v, sh);
-    if (threadIdx.x == 0) *bc = v;
-    __syncthreads();
-    v = *bc;
-    __syncthreads();
-    return v;
-}
-
-template <class T>
-__device__ void blk_amul(const BlockSys<T>& S, const T* x, T* y) {
-    for (int c = threadIdx.x; c < S.n; c += BLK_NT)
-        y[c] = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, x);
-    __syncthreads();
-}
-
-// w = M^-1 r: DIC/DILU forward then backward level sweeps, block barriers.
-template <class T>
-__device__ void blk_precondition(const BlockSys<T>& S, const T* r, T* w) {
-    if (S.precond == CFX_PRE_DIC || S.precond == CFX_PRE_DILU) {
-        for (int L = 0; L < S.nFwd; ++L) {
-            for (int i = S.fwdLevelStart[L] + threadIdx.x; i < S.fwdLevelStart[L + 1]; i += BLK_NT) {
-                const int c = S.fwdCells[i];
-                const T rDc = S.rD[c];
-                T v = rDc * r[c];
-                for (int k = S.losortStart[c]; k < S.losortStart[c + 1]; ++k) v -= (rDc * S.lp[k]) * w[S.losortL[k]];
-                w[c] = v;
-            }
-            __syncthreads();
-        }
-        for (int L = 0; L < S.nBwd; ++L) {
-            for (int i = S.bwdLevelStart[L] + threadIdx.x; i < S.bwdLevelStart[L + 1]; i += BLK_NT) {
-                const int c = S.bwdCells[i];
-                const T rDc = S.rD[c];
-                T v = w[c];
-                for (int f = S.ownerStart[c + 1] - 1; f >= S.ownerStart[c]; --f) v -= (rDc * S.upper[f]) * w[S.u[f]];
-                w[c] = v;
-            }
-            __syncthreads();
-        }
-    } else {
-        for (int c = threadIdx.x; c < S.n; c += BLK_NT) w[c] = S.precond == CFX_PRE_DIAGONAL ? S.rD[c] * r[c] : r[c];
-        __syncthreads();
-    }
-}
-
-template <class T>
-__device__ __forceinline__ bool blk_check(BlockSys<T>& S, double fin, double ini) {
-    return fin < S.tolerance || (S.relTol > SP_SMALL && fin < S.relTol * ini);
-}
-
-template <class T>
-__global__ void __launch_bounds__(BLK_NT) block_solve_k(BlockSys<T>* systems, const int* done) {
-    __shared__ double sh[BLK_NT / 32];
-    __shared__ double bc;
-    if (done && *done) return;
-    BlockSys<T>& S = systems[blockIdx.x];
-    const int n = S.n;
-    T* psi = S.psi;
-    // Apsi into q
-    double s0 = 0.0;
-    for (int c = threadIdx.x; c < n; c += BLK_NT) s0 += double(psi[c]);
-    const double avg = n > 0 ? bsum<T>(s0, sh, &bc) / n : 0.0;
-    blk_amul(S, psi, S.q);
-    double nf = 0.0, mg = 0.0;
-    for (int c = threadIdx.x; c < n; c += BLK_NT) {
-        T sA = S.diag[c];
-        for (int k = S.losortStart[c]; k < S.losortStart[c + 1]; ++k) sA += S.lp[k];
-        for (int f = S.ownerStart[c]; f < S.ownerStart[c + 1]; ++f) sA += S.upper[f];
-        const T t = sA * T(avg);
-        nf += double(fabs(S.q[c] - t) + fabs(S.b[c] - t));
-        const T rc = S.b[c] - S.q[c];
-        S.r[c] = rc;
-        if (S.r0) S.r0[c] = rc;
-        mg += fabs(double(rc));
-    }
-    const double normFactor = bsum<T>(nf, sh, &bc) + SP_SMALL;
-    const double initial = bsum<T>(mg, sh, &bc) / normFactor;
-    double fin = initial;
-    int nIter = 0, converged = blk_check(S, fin, initial), singular = 0;
-    if (S.minIter > 0 || !converged) {
-        if (S.solver == CFX_SOLVER_PCG) {
-            double wArA = SP_GREAT, wArAold;
-            do {
-                wArAold = wArA;
-                blk_precondition(S, S.r, S.w);
-                double d = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.w[c]) * double(S.r[c]);
-                wArA = bsum<T>(d, sh, &bc);
-                const T beta = T(wArA / wArAold);
-                for (int c = threadIdx.x; c < n; c += BLK_NT) S.p[c] = nIter == 0 ? S.w[c] : S.w[c] + beta * S.p[c];
-                __syncthreads();
-                blk_amul(S, S.p, S.w);
-                d = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.w[c]) * double(S.p[c]);
-                const double wApA = bsum<T>(d, sh, &bc);
-                singular = fabs(wApA) / normFactor < VSMALL;
-                if (singular) break;
-                const T alpha = T(wArA / wApA);
-                mg = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) {
-                    psi[c] += alpha * S.p[c];
-                    const T rc = S.r[c] - alpha * S.w[c];
-                    S.r[c] = rc;
-                    mg += fabs(double(rc));
-                }
-                fin = bsum<T>(mg, sh, &bc) / normFactor;
-                bool cont = false;
-                if (++nIter < S.maxIter) {
-                    converged = blk_check(S, fin, initial);
-                    cont = !converged;
-                }
-                if (!(cont || nIter < S.minIter)) break;
-            } while (true);
-        } else {
-            double rA0rA = 0.0, alpha = 0.0, omega = 0.0;
-            do {
-                const double rA0rAold = rA0rA;
-                double d = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.r0[c]) * double(S.r[c]);
-                rA0rA = bsum<T>(d, sh, &bc);
-                singular = fabs(rA0rA) < VSMALL;
-                if (singular) break;
-                if (nIter == 0) {
-                    for (int c = threadIdx.x; c < n; c += BLK_NT) S.p[c] = S.r[c];
-                } else {
-                    singular = fabs(omega) < VSMALL;
-                    if (singular) break;
-                    const T beta = T((rA0rA / rA0rAold) * (alpha / omega));
-                    for (int c = threadIdx.x; c < n; c += BLK_NT)
-                        S.p[c] = S.r[c] + beta * (S.p[c] - T(omega) * S.q[c]);
-                }
-                __syncthreads();
-                blk_precondition(S, S.p, S.w);  // yA = w
-                blk_amul(S, S.w, S.q);          // AyA = q
-                d = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) d += double(S.r0[c]) * double(S.q[c]);
-                alpha = rA0rA / bsum<T>(d, sh, &bc);
-                mg = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) {
-                    const T v = S.r[c] - T(alpha) * S.q[c];
-                    S.s[c] = v;
-                    mg += fabs(double(v));
-                }
-                fin = bsum<T>(mg, sh, &bc) / normFactor;
-                if (++nIter >= S.minIter && (converged = blk_check(S, fin, initial))) {
-                    for (int c = threadIdx.x; c < n; c += BLK_NT) psi[c] += T(alpha) * S.w[c];
-                    __syncthreads();
-                    break;
-                }
-                // zA into r0-free slot: use t for tA, reuse p? keep z in S.t's partner
-                blk_precondition(S, S.s, S.t);  // zA = t
-                // tA = A zA -> stored in r (r is rewritten below from s and tA)
-                double tt = 0.0, ts = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) {
-                    const T v = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, S.t);
-                    S.r[c] = v;
-                    tt += double(v) * double(v);
-                    ts += double(v) * double(S.s[c]);
-                }
-                const double tAtA = bsum<T>(tt, sh, &bc);
-                omega = bsum<T>(ts, sh, &bc) / tAtA;
-                mg = 0.0;
-                for (int c = threadIdx.x; c < n; c += BLK_NT) {
-                    psi[c] += T(alpha) * S.w[c] + T(omega) * S.t[c];
-                    const T v = S.s[c] - T(omega) * S.r[c];
-                    S.r[c] = v;
-                    mg += fabs(double(v));
-                }
-                fin = bsum<T>(mg, sh, &bc) / normFactor;
-                bool cont = false;
-                if (nIter < S.maxIter) {
-                    converged = blk_check(S, fin, initial);
-                    cont = !converged;
-                }
-                if (!(cont || nIter < S.minIter)) break;
-            } while (true);
-        }
-    }
-    if (threadIdx.x == 0) {
-        S.initialResidual = initial;
-        S.finalResidual = fin;
-        S.nIterations = nIter;
-        S.converged = converged;
-        S.singular = singular;
-    }
-}
 
 }  // namespace
 
@@ -743,12 +537,6 @@ void Kern<T>::gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& 
     gamg_residual_check_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u,
                                                               a.diag, a.lowerPerm, a.upper, psi, b, r, st,
                                                               Red2{sc.partials, sc.counters});
-    count_launch();
-}
-
-template <class T>
-void Kern<T>::block_solve(cudaStream_t s, BlockSys<T>* d_sys, int nSys, const int* done) {
-    block_solve_k<T><<<nSys, BLK_NT, 0, s>>>(d_sys, done);
     count_launch();
 }
 

@@ -13,6 +13,7 @@ struct BlockSys {
     const int *fwdCells, *fwdLevelStart, *bwdCells, *bwdLevelStart;
     int nFwd, nBwd;
     const T *diag, *lp, *upper, *rD;
+    const T* upPerm;  // upper[losort] for the DILU reciprocal diagonal (null: lp)
     const T* b;
     T* psi;
     T *r, *w, *p, *q, *s, *t, *r0;  // work vectors (s, t, r0: PBiCGStab)
@@ -69,6 +70,52 @@ struct Kern {
     static void copy(cudaStream_t s, int n, const T* x, T* y, const int* done);
     static void fill(cudaStream_t s, int n, T v, T* y, const int* done);
 };
+
+// A system of a batch in slot order: slot p holds cell cellOf[p], slots
+// ordered by forward (lower-DAG) level, so each level of the DIC/DILU
+// forward sweep is a contiguous slot range.  Neighbours are kept in ELL
+// form, column-major ([j*n + p], padded with p): the faces where the cell is
+// the neighbour (losort order; lower coefficients) and the faces it owns
+// (face order; upper coefficients).  cnt[p] = nLower | nUpper << 16.  The
+// operator and every per-cell face order are the reference's; only the
+// storage order of the vectors differs.
+template <class T>
+struct SlotSys {
+    int n, wLo, wUp, nFwd, nBwd;
+    int bwdMirror;  // backward level L = forward level nFwd-1-L, same order
+    const int *cnt, *loSrc, *upSrc, *cellOf;
+    const int *fwdLevelStart, *bwdSlot, *bwdLevelStart;
+    const T *diag, *lo, *up;  // slot order; lo/up [w*n]
+    const T* upLo;            // upper[losort] in lo layout (asymmetric DILU pivots; null: lo)
+    T* rD;
+    T *b, *psi;               // slot order
+    T *r, *w, *p, *q, *s, *t, *r0;
+    const double* bCell;      // cell order (FP64 record): source in,
+    double* psiCell;          // solution in/out
+    double tolerance, relTol;
+    int maxIter, minIter;
+    int precond, solver;
+    double initialResidual, finalResidual;
+    int nIterations, converged, singular, nOuter;
+    unsigned long long tStart, tEnd;  // %globaltimer at the system's start / end (ns)
+};
+
+// Batched solves of independent systems: nCta persistent CTAs take systems
+// in array order from the counter next[1] (zero at launch), one CTA per
+// system.  Preconditioner set-up runs in the kernel.  mixed: FP32 inner
+// solves in FP64 iterative refinement (nOuter = refinement steps).
+void launch_batch(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nCta, int mixed,
+                  double innerRelTol, int maxOuter, unsigned* next);
+// resident batch CTAs per SM (occupancy of the batch kernel)
+int batch_ctas_per_sm();
+// Cluster form: the first nBig systems (in array order) are solved by whole
+// clusters of clusterSize CTAs, the rest by single CTAs; nClusters
+// persistent clusters; next[0], next[1] zero at launch.
+cudaError_t launch_batch_cluster(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nBig,
+                                 int clusterSize, int nClusters, int mixed, double innerRelTol, int maxOuter,
+                                 unsigned* next);
+// co-resident clusters of the cluster form (0: clusters unavailable)
+int batch_max_clusters(int clusterSize);
 
 // Mixed precision: e (float) -> psi (double) += e; r64 -> r32.
 void launch_add_f2d(cudaStream_t s, int n, const float* e, double* psi, const int* done);

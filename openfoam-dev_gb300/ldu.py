@@ -18,8 +18,10 @@ Everything runs on the GPU through the C ABI in include/cfx.h.  There is no
 CPU fallback: without the shared library, or without a CUDA device, every
 call raises.
 """
+import atexit
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -108,9 +110,39 @@ _SIG = {
     "cfx_reciprocal_d": (_i, [_vp, _i, _vp]),
     "cfx_smooth": (_i, [_vp, _i, _vp, _vp, _i]),
     "cfx_reduce_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
+    "cfx_batch_create": (_i, [_vp, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "cfx_batch_destroy": (_i, [_vp]),
+    "cfx_batch_set_matrix": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "cfx_batch_solve": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, _vp]),
+    "cfx_batch_vectors": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),
+    "cfx_batch_solve_device": (_i, [_vp, ctypes.POINTER(Controls), _vp]),
+    "cfx_batch_timings": (_i, [_vp, _vp, _vp]),
+    "cfx_batch_set_ctas_per_sm": (_i, [_vp, _i]),
+    "cfx_batch_set_groups": (_i, [_vp, _i, _i]),
+    "cfx_batch_get_groups": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "cfx_batch_tune": (_i, [_vp, ctypes.POINTER(Controls), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_float)]),
 }
 
 _lib = None
+
+# Live handles by kind, closed at interpreter exit in dependency order
+# (batches and matrices before the meshes they use, meshes before their
+# context), while the library and the CUDA runtime are still intact.
+_LIVE = {k: weakref.WeakSet() for k in ("batch", "matrix", "mesh", "ctx")}
+
+
+def _track(kind, obj):
+    _LIVE[kind].add(obj)
+
+
+@atexit.register
+def _close_all():
+    for kind in ("batch", "matrix", "mesh", "ctx"):
+        for obj in list(_LIVE[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
 
 
 def lib():
@@ -156,6 +188,7 @@ class Context:
         _check(lib().cfx_ctx_create(device, ctypes.byref(h)), "cfx_ctx_create")
         self.h = h
         self.device = device
+        _track("ctx", self)
 
     def stream(self):
         s = ctypes.c_void_p()
@@ -175,10 +208,14 @@ class Context:
         _check(lib().cfx_reduce(self.h, which, a.numel(), _dp(a), _dp(b), ctypes.byref(out)), "cfx_reduce")
         return out.value
 
+    def close(self):
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            lib().cfx_ctx_destroy(h)
+
     def __del__(self):
         try:
-            if getattr(self, "h", None):
-                lib().cfx_ctx_destroy(self.h)
+            self.close()
         except Exception:
             pass
 
@@ -206,6 +243,7 @@ class LduMesh:
                "cfx_mesh_create")
         self.h = h
         self.gamg_key = None
+        _track("mesh", self)
 
     def schedule_depth(self):
         a, b = ctypes.c_int(), ctypes.c_int()
@@ -247,10 +285,14 @@ class LduMesh:
                "level_info")
         return ra, fra, fl, nc.value, ncf.value, cl, cu
 
+    def close(self):
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            lib().cfx_mesh_destroy(h)
+
     def __del__(self):
         try:
-            if getattr(self, "h", None):
-                lib().cfx_mesh_destroy(self.h)
+            self.close()
         except Exception:
             pass
 
@@ -267,6 +309,7 @@ class LduMatrix:
         _check(lib().cfx_matrix_create(mesh.h, _hp(self.diag), _hp(self.upper), _hp(self.lower), ctypes.byref(h)),
                "cfx_matrix_create")
         self.h = h
+        _track("matrix", self)
 
     def symmetric(self):
         return self.lower is None
@@ -314,10 +357,14 @@ class LduMatrix:
         _check(lib().cfx_matrix_coarse(self.h, level, _hp(d), _hp(up), _hp(lo)), "coarse")
         return d, up, lo
 
+    def close(self):
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            lib().cfx_matrix_destroy(h)
+
     def __del__(self):
         try:
-            if getattr(self, "h", None):
-                lib().cfx_matrix_destroy(self.h)
+            self.close()
         except Exception:
             pass
 
@@ -341,7 +388,7 @@ class SolverPerformance:
                 f"Final residual = {self.finalResidual:g}, No Iterations {self.nIterations}")
 
 
-TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE = 0, 1, 2
+TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS = 0, 1, 2, 3
 
 
 def tune_set(key, value):
@@ -465,3 +512,107 @@ def solve(s, psi, controls, field="psi"):
         if mesh.gamg_key != key:
             mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=key[1])
     return solver_new(field, A, controls).solve(psi, s["source"])
+
+
+class Batch:
+    """Many independent systems solved by one launch (cfx_batch_*).
+
+    ``systems``: list of dicts with ``l``, ``u``, ``diag``, ``upper`` and
+    optionally ``lower`` (cases.py layout).  ``solve(psi, source, controls)``
+    takes the concatenated vectors (numpy, float64) and returns one
+    SolverPerformance per system; ``solve_device`` uses the resident device
+    vectors (``vectors()``)."""
+
+    def __init__(self, ctx, systems):
+        self.ctx = ctx
+        n = len(systems)
+        self.nCells = np.array([s["diag"].size for s in systems], np.int32)
+        self.nFaces = np.array([s["l"].size for s in systems], np.int32)
+        self._l = [np.ascontiguousarray(s["l"], np.int32) for s in systems]
+        self._u = [np.ascontiguousarray(s["u"], np.int32) for s in systems]
+        la = (ctypes.c_void_p * n)(*[a.ctypes.data for a in self._l])
+        ua = (ctypes.c_void_p * n)(*[a.ctypes.data for a in self._u])
+        h = ctypes.c_void_p()
+        _check(lib().cfx_batch_create(ctx.h, n, _hp(self.nCells), _hp(self.nFaces), la, ua, ctypes.byref(h)),
+               "cfx_batch_create")
+        self.h = h
+        self.n = n
+        self.sym = []
+        _track("batch", self)
+        for i, s in enumerate(systems):
+            self.set_matrix(i, s["diag"], s["upper"], s.get("lower"))
+        self.offsets = np.concatenate([[0], np.cumsum(self.nCells, dtype=np.int64)])
+
+    def set_matrix(self, i, diag, upper, lower=None):
+        d = np.ascontiguousarray(diag, np.float64)
+        up = np.ascontiguousarray(upper, np.float64)
+        lo = None if lower is None else np.ascontiguousarray(lower, np.float64)
+        _check(lib().cfx_batch_set_matrix(self.h, int(i), _hp(d), _hp(up), _hp(lo)), "cfx_batch_set_matrix")
+        if len(self.sym) <= i:
+            self.sym.extend([True] * (i + 1 - len(self.sym)))
+        self.sym[i] = lo is None
+
+    def _c(self, controls):
+        c = _controls(controls, all(self.sym))
+        if not all(self.sym) and c.solver == SOLVER_PCG:
+            raise FatalError("Unknown asymmetric matrix solver cudaPCG")
+        return c
+
+    def _perfs(self, arr, field):
+        return [SolverPerformance(p.solverName.decode(), field, p.initialResidual, p.finalResidual, p.nIterations,
+                                  bool(p.converged), bool(p.singular), p.nOuter) for p in arr]
+
+    def solve(self, psi, source, controls, field="psi"):
+        if psi.dtype != np.float64 or not psi.flags["C_CONTIGUOUS"] or psi.size != self.offsets[-1]:
+            raise TypeError("psi must be a contiguous float64 array of sum(nCells)")
+        src = np.ascontiguousarray(source, np.float64)
+        arr = (Perf * self.n)()
+        c = self._c(controls)
+        _check(lib().cfx_batch_solve(self.h, ctypes.byref(c), _hp(psi), _hp(src), arr), "cfx_batch_solve")
+        return self._perfs(arr, field)
+
+    def vectors(self):
+        p, b = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().cfx_batch_vectors(self.h, ctypes.byref(p), ctypes.byref(b), None), "cfx_batch_vectors")
+        return p.value, b.value
+
+    def solve_device(self, controls, field="psi"):
+        arr = (Perf * self.n)()
+        c = self._c(controls)
+        _check(lib().cfx_batch_solve_device(self.h, ctypes.byref(c), arr), "cfx_batch_solve_device")
+        return self._perfs(arr, field)
+
+    def timings(self):
+        """(start, end) in ms of each system's solve in the last launch."""
+        a = np.empty(self.n)
+        b = np.empty(self.n)
+        _check(lib().cfx_batch_timings(self.h, _hp(a), _hp(b)), "cfx_batch_timings")
+        return a, b
+
+    def set_ctas_per_sm(self, k):
+        _check(lib().cfx_batch_set_ctas_per_sm(self.h, int(k)), "cfx_batch_set_ctas_per_sm")
+
+    def set_groups(self, cluster_size, big_cells):
+        _check(lib().cfx_batch_set_groups(self.h, int(cluster_size), int(big_cells)), "cfx_batch_set_groups")
+
+    def groups(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().cfx_batch_get_groups(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "groups")
+        return a.value, b.value, c.value
+
+    def tune(self, controls):
+        k, ms = ctypes.c_int(), ctypes.c_float()
+        c = self._c(controls)
+        _check(lib().cfx_batch_tune(self.h, ctypes.byref(c), ctypes.byref(k), ctypes.byref(ms)), "cfx_batch_tune")
+        return k.value, ms.value
+
+    def close(self):
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            lib().cfx_batch_destroy(h)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

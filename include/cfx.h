@@ -219,6 +219,71 @@ cfx_status cfx_batch_get_groups(cfx_batch* batch, int* clusterSize, int* nBig, i
  * bestMs = its time.  Either may be NULL. */
 cfx_status cfx_batch_tune(cfx_batch* batch, const cfx_controls* ctl, int* best, float* bestMs);
 
+/* ---- solve server ----------------------------------------------------------
+ * No counterpart in the reference: an in-process server for many clients
+ * (solver instances of several cases, a parametric study driver, a service
+ * front end).  Matrices are registered once and stay resident in HBM;
+ * requests bring a right-hand side (and initial psi) for a resident matrix,
+ * so re-solving one (a PISO corrector) uploads two vectors.  One worker
+ * thread drives the GPU: requests on small matrices are solved together in
+ * one persistent launch whenever the GPU is free (continuous batching, one
+ * precision per launch, at most one request per matrix at a time, up to
+ * maxBatch); requests on large matrices (more than largeCells cells) run
+ * alone through the whole-GPU drivers, with cudaGAMG when the matrix was
+ * registered with face weights.  Admission: resident matrices and the
+ * requests' device vectors count against hbmBudget bytes; a matrix that does
+ * not fit, or a request that alone exceeds the budget, is refused with
+ * CFX_ERR_ADMISSION; a request that does not fit now blocks the submitting
+ * thread until completions free space.  All functions are thread-safe. */
+typedef struct cfx_server cfx_server;
+typedef struct {
+    int64_t hbmBudget;          /* bytes (default 150e9) */
+    int largeCells;             /* larger matrices are solved alone (default 1,000,000) */
+    int maxBatch;               /* systems per launch (default 1024) */
+    int nCellsInCoarsestLevel;  /* GAMG agglomeration of large matrices (default 10) */
+    int groupCells;             /* small matrices of at least this many cells are solved by */
+    int groupSize;              /* a thread-block cluster of groupSize CTAs (defaults 100,000 and 4;
+                                 * 0: one CTA each); a result depends on its matrix only, never on
+                                 * the rest of the launch */
+} cfx_server_config;
+typedef struct {
+    int64_t submitted, completed, cancelled, failed, refused;
+    int64_t batches, batchedSolves, largeSolves;
+    int64_t queueDepth, running, residentMatrices;
+    int64_t hbmInUse, hbmBudget;
+    double elapsedS, solvesPerS;   /* since creation or the last reset */
+    double p50Ms, p99Ms, meanMs, maxMs;  /* submit-to-completion latency */
+} cfx_server_stats_t;
+void cfx_server_default_config(cfx_server_config* cfg);
+/* cfg NULL: defaults.  The server runs on ctx's device. */
+cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_server** server);
+/* Stops the worker after the running launch; frees everything. */
+cfx_status cfx_server_destroy(cfx_server* server);
+/* Registers a matrix (host arrays; lower NULL = symmetric; faceWeights
+ * [nFaces] or NULL: large matrices given weights get a faceAreaPair GAMG
+ * hierarchy).  matrixId identifies it in requests. */
+cfx_status cfx_server_add_matrix(cfx_server* server, int nCells, int nFaces, const int32_t* l, const int32_t* u,
+                                 const double* diag, const double* upper, const double* lower,
+                                 const double* faceWeights, int64_t* matrixId);
+/* Frees the matrix once no request uses it. */
+cfx_status cfx_server_remove_matrix(cfx_server* server, int64_t matrixId);
+/* Queues a solve (psi0 NULL: zero initial guess); the host arrays are copied
+ * before the call returns. */
+cfx_status cfx_server_submit(cfx_server* server, int64_t matrixId, const cfx_controls* ctl, const double* psi0,
+                             const double* source, int64_t* requestId);
+/* Waits up to timeoutMs (< 0: forever) for a request, copies psi (if non-NULL)
+ * and perf out and frees the request.  CFX_ERR_TIMEOUT leaves it pending;
+ * a cancelled request returns CFX_ERR_STATE. */
+cfx_status cfx_server_wait(cfx_server* server, int64_t requestId, int timeoutMs, double* psi, cfx_perf* perf);
+/* Removes a queued request (its wait returns CFX_ERR_STATE); CFX_ERR_STATE if
+ * it is already running or finished. */
+cfx_status cfx_server_cancel(cfx_server* server, int64_t requestId);
+/* The client gives the request up (disconnect): queued -> cancelled;
+ * running -> freed when it completes; finished -> freed now. */
+cfx_status cfx_server_release(cfx_server* server, int64_t requestId);
+cfx_status cfx_server_stats(cfx_server* server, cfx_server_stats_t* stats);
+cfx_status cfx_server_reset_stats(cfx_server* server);
+
 /* ---- single operations, device pointers (parity tests, building blocks) -- */
 cfx_status cfx_amul(cfx_matrix* mat, const double* d_x, double* d_y);
 cfx_status cfx_tmul(cfx_matrix* mat, const double* d_x, double* d_y);

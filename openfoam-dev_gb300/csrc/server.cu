@@ -1,0 +1,684 @@
+// server.cu - the solve server (cfx_server_*): an in-process component that
+// keeps matrices resident in HBM and serves solve requests from any number of
+// client threads with continuous batching.
+//
+//   * Matrices are registered once (cfx_server_add_matrix) and stay resident
+//     until removed: small ones as slot-ordered batch systems, large ones
+//     (more than largeCells cells) as a cfx_mesh + cfx_matrix with their GAMG
+//     hierarchy.  A request names a matrix and brings a new right-hand side
+//     (and initial psi), so re-solving a resident matrix (a PISO corrector)
+//     uploads two vectors only.
+//   * Admission: every resident matrix and every request's device vectors
+//     count against an HBM budget.  A matrix or request that alone exceeds
+//     the budget is refused (CFX_ERR_ADMISSION); one that does not fit now
+//     waits (the submitting thread blocks) until completions free space.
+//   * One worker thread runs the GPU.  Whenever it is free it takes every
+//     queued small request (at most one per matrix, up to maxBatch) and
+//     solves them in one persistent launch, one CTA or one thread-block
+//     cluster per system; requests that arrive meanwhile go into the next
+//     launch.  Large requests run alone through the whole-GPU drivers.
+//   * Completion is signalled per request; a request can be cancelled while
+//     it is queued (or its result dropped later), and requests whose client
+//     never collects them are freed at release or shutdown.
+// Latency (submit to completion) and throughput counters are kept for
+// cfx_server_stats.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+#include "batch.h"
+
+using namespace cfx;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+enum ReqState { Q_WAITING = 0, Q_RUNNING = 1, Q_DONE = 2, Q_CANCELLED = 3, Q_FAILED = 4 };
+
+struct SrvMatrix {
+    int64_t id = 0;
+    int n = 0, nf = 0;
+    bool large = false, sym = true;
+    std::unique_ptr<BSys> bs;
+    cfx_mesh* mesh = nullptr;
+    cfx_matrix* mat = nullptr;
+    size_t bytes = 0;
+    bool busy = false;      // a request on it is running
+    bool removing = false;  // remove requested; freed when idle
+    int pending = 0;        // queued or running requests
+};
+
+struct SrvRequest {
+    int64_t id = 0, matrixId = 0;
+    cfx_controls ctl{};
+    double *d_psi = nullptr, *d_b = nullptr;
+    size_t bytes = 0;
+    int n = 0;
+    ReqState state = Q_WAITING;
+    bool detached = false;  // released by its client: freed when it completes
+    cfx_status status = CFX_OK;
+    std::string error;
+    cfx_perf perf{};
+    Clock::time_point tSubmit, tDone;
+};
+
+}  // namespace
+
+struct cfx_server {
+    cfx_ctx* ctx = nullptr;           // batches run on its stream
+    cfx_ctx* ctxLarge = nullptr;      // large matrices: their uploads and solves
+    cudaStream_t copyStream = nullptr;  // request vectors and small-matrix uploads
+    cfx_server_config cfg{};
+    int sms = 0;
+    std::mutex mu;
+    std::condition_variable cvWork;   // worker: something to do
+    std::condition_variable cvDone;   // clients: a request finished / space freed
+    std::map<int64_t, std::unique_ptr<SrvMatrix>> mats;
+    std::map<int64_t, std::unique_ptr<SrvRequest>> reqs;
+    std::deque<int64_t> queue;        // waiting requests, arrival order
+    int64_t nextMat = 1, nextReq = 1;
+    size_t used = 0;                  // bytes admitted (matrices + request vectors)
+    bool stop = false;
+    std::thread worker;
+    // launch buffers
+    SlotSys<double>* d64 = nullptr;
+    SlotSys<float>* d32 = nullptr;
+    SlotSys<double>* h64 = nullptr;
+    SlotSys<float>* h32 = nullptr;
+    unsigned* d_next = nullptr;
+    int cap = 0;
+    std::map<int, int> maxClusters;
+    // statistics
+    Clock::time_point t0;
+    int64_t submitted = 0, completed = 0, cancelled = 0, failed = 0, refused = 0;
+    int64_t batches = 0, batchedSolves = 0, largeSolves = 0, running = 0;
+    std::vector<double> latMs;
+};
+
+namespace {
+
+size_t large_estimate(int n, int nf) {
+    // fine level + GAMG hierarchy (< the fine level again), FP64 and FP32
+    // coefficients, schedules and the drivers' work vectors
+    return size_t(n) * 420 + size_t(nf) * 96 + (size_t(64) << 20);
+}
+
+int max_clusters(cfx_server* sv, int cs) {
+    auto it = sv->maxClusters.find(cs);
+    if (it == sv->maxClusters.end()) it = sv->maxClusters.emplace(cs, batch_max_clusters(cs)).first;
+    return it->second;
+}
+
+void finish(cfx_server* sv, SrvRequest& r, ReqState st) {
+    r.state = st;
+    r.tDone = Clock::now();
+    if (st == Q_DONE) {
+        ++sv->completed;
+        sv->latMs.push_back(std::chrono::duration<double, std::milli>(r.tDone - r.tSubmit).count());
+    } else if (st == Q_FAILED) {
+        ++sv->failed;
+    }
+    auto m = sv->mats.find(r.matrixId);
+    if (m != sv->mats.end()) {
+        m->second->busy = false;
+        m->second->pending--;
+    }
+}
+
+void free_request_buffers(cfx_server* sv, SrvRequest& r) {
+    if (r.d_psi) cudaFreeAsync(r.d_psi, sv->copyStream);
+    if (r.d_b) cudaFreeAsync(r.d_b, sv->copyStream);
+    r.d_psi = r.d_b = nullptr;
+    sv->used -= r.bytes;
+    r.bytes = 0;
+}
+
+// Drops finished requests that no client will collect.
+void drop_detached(cfx_server* sv) {
+    for (auto it = sv->reqs.begin(); it != sv->reqs.end();) {
+        SrvRequest& r = *it->second;
+        if (r.detached && r.state != Q_WAITING && r.state != Q_RUNNING) {
+            free_request_buffers(sv, r);
+            it = sv->reqs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+void free_matrix(cfx_server* sv, SrvMatrix& m) {
+    if (m.mat) cfx_matrix_destroy(m.mat);
+    if (m.mesh) cfx_mesh_destroy(m.mesh);
+    m.mat = nullptr;
+    m.mesh = nullptr;
+    m.bs.reset();
+    sv->used -= m.bytes;
+}
+
+// Matrices whose removal was requested go once no request uses them.
+void reap(cfx_server* sv) {
+    for (auto it = sv->mats.begin(); it != sv->mats.end();) {
+        if (it->second->removing && it->second->pending == 0) {
+            free_matrix(sv, *it->second);
+            it = sv->mats.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+void ensure_cap(cfx_server* sv, int k) {
+    if (k <= sv->cap) return;
+    const int c = std::max(k, 2 * sv->cap);
+    if (sv->d64) cudaFree(sv->d64);
+    if (sv->d32) cudaFree(sv->d32);
+    if (sv->h64) cudaFreeHost(sv->h64);
+    if (sv->h32) cudaFreeHost(sv->h32);
+    sv->d64 = nullptr;
+    sv->d32 = nullptr;
+    sv->h64 = nullptr;
+    sv->h32 = nullptr;
+    sv->cap = 0;
+    CK(cudaMalloc(&sv->d64, sizeof(SlotSys<double>) * c));
+    CK(cudaMalloc(&sv->d32, sizeof(SlotSys<float>) * c));
+    CK(cudaMallocHost(&sv->h64, sizeof(SlotSys<double>) * c));
+    CK(cudaMallocHost(&sv->h32, sizeof(SlotSys<float>) * c));
+    sv->cap = c;
+}
+
+// Runs one batch of small requests (worker thread, lock not held): systems
+// of at least groupCells cells on clusters of groupSize CTAs, the others one
+// CTA each, largest first.
+void run_batch(cfx_server* sv, std::vector<SrvRequest*>& rs, std::vector<SrvMatrix*>& ms) {
+    const int k = int(rs.size());
+    std::vector<int> order(k);
+    for (int i = 0; i < k; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ms[a]->n > ms[b]->n; });
+    ensure_cap(sv, k);
+    int mixed = 0;
+    for (int j = 0; j < k; ++j) {
+        const int i = order[j];
+        bsys_records(*ms[i]->bs, rs[i]->ctl, rs[i]->d_psi, rs[i]->d_b, sv->h64[j], sv->h32[j]);
+        mixed |= rs[i]->ctl.precision == CFX_MIXED;
+    }
+    cudaStream_t s = sv->ctx->stream;
+    CK(cudaMemcpyAsync(sv->d64, sv->h64, sizeof(SlotSys<double>) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sv->d32, sv->h32, sizeof(SlotSys<float>) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(sv->d_next, 0, 2 * sizeof(unsigned), s));
+    // group size by system size alone, so that a request's result does not
+    // depend on what else is in the launch
+    int cs = 0, nBig = 0;
+    if (sv->cfg.groupSize > 1 && max_clusters(sv, sv->cfg.groupSize) > 0) {
+        for (int j = 0; j < k; ++j)
+            if (ms[order[j]]->n >= sv->cfg.groupCells) nBig = j + 1;
+        if (nBig) cs = sv->cfg.groupSize;
+    }
+    const double innerRelTol = std::pow(10.0, -double(batch_inner_digits()));
+    // a mixed launch solves every system of it in mixed precision; the
+    // worker only batches requests of one precision together
+    if (cs)
+        CK(launch_batch_cluster(s, sv->d64, mixed ? sv->d32 : nullptr, k, nBig, cs, max_clusters(sv, cs), mixed,
+                                innerRelTol, 50, sv->d_next));
+    else
+        launch_batch(s, sv->d64, mixed ? sv->d32 : nullptr, k, std::min(k, sv->sms * batch_ctas_per_sm()), mixed,
+                     innerRelTol, 50, sv->d_next);
+    CK(cudaMemcpyAsync(sv->h64, sv->d64, sizeof(SlotSys<double>) * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int j = 0; j < k; ++j) {
+        const SlotSys<double>& r = sv->h64[j];
+        SrvRequest& q = *rs[order[j]];
+        std::memset(&q.perf, 0, sizeof(q.perf));
+        std::snprintf(q.perf.solverName, sizeof(q.perf.solverName), "%s", bsys_solver_name(q.ctl));
+        q.perf.initialResidual = r.initialResidual;
+        q.perf.finalResidual = r.finalResidual;
+        q.perf.nIterations = r.nIterations;
+        q.perf.converged = r.converged;
+        q.perf.singular = r.singular;
+        q.perf.nOuter = mixed ? r.nOuter : 0;
+    }
+}
+
+}  // namespace
+
+namespace {
+
+// The worker: large requests alone, small ones batched (one precision per
+// launch, at most one request per matrix), until stopped.
+void worker_loop(cfx_server* sv) {
+    cudaSetDevice(sv->ctx->device);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        sv->cvWork.wait(lk, [&] { return sv->stop || !sv->queue.empty(); });
+        if (sv->stop) return;
+        // the oldest request decides: large -> alone; small -> a batch of
+        // its precision
+        SrvRequest* head = sv->reqs[sv->queue.front()].get();
+        SrvMatrix* hm = sv->mats[head->matrixId].get();
+        std::vector<SrvRequest*> rs;
+        std::vector<SrvMatrix*> ms;
+        if (hm->large) {
+            if (hm->busy) {  // cannot happen with one worker, kept for clarity
+                sv->cvWork.wait_for(lk, std::chrono::milliseconds(1));
+                continue;
+            }
+            rs.push_back(head);
+            ms.push_back(hm);
+            sv->queue.pop_front();
+        } else {
+            const int prec = head->ctl.precision;
+            std::deque<int64_t> keep;
+            while (!sv->queue.empty()) {
+                const int64_t id = sv->queue.front();
+                sv->queue.pop_front();
+                SrvRequest* r = sv->reqs[id].get();
+                SrvMatrix* m = sv->mats[r->matrixId].get();
+                if (!m->large && !m->busy && r->ctl.precision == prec && int(rs.size()) < sv->cfg.maxBatch) {
+                    m->busy = true;
+                    rs.push_back(r);
+                    ms.push_back(m);
+                } else {
+                    keep.push_back(id);
+                }
+            }
+            sv->queue.swap(keep);
+        }
+        for (SrvRequest* r : rs) r->state = Q_RUNNING;
+        sv->running = int64_t(rs.size());
+        lk.unlock();
+        cfx_status st = CFX_OK;
+        std::string err;
+        try {
+            if (ms[0]->large) {
+                cfx_perf perf;
+                std::memset(&perf, 0, sizeof(perf));
+                st = cfx_solve_device(ms[0]->mat, &rs[0]->ctl, rs[0]->d_psi, rs[0]->d_b, &perf);
+                if (st != CFX_OK) err = cfx_last_error();
+                rs[0]->perf = perf;
+            } else {
+                run_batch(sv, rs, ms);
+            }
+        } catch (const std::exception& e) {
+            st = CFX_ERR_CUDA;
+            err = e.what();
+        }
+        lk.lock();
+        sv->running = 0;
+        if (ms[0]->large) {
+            ++sv->largeSolves;
+        } else {
+            ++sv->batches;
+            sv->batchedSolves += int64_t(rs.size());
+        }
+        for (SrvRequest* r : rs) {
+            r->status = st;
+            r->error = err;
+            r->perf.status = st;
+            finish(sv, *r, st == CFX_OK ? Q_DONE : Q_FAILED);
+        }
+        drop_detached(sv);
+        reap(sv);
+        sv->cvDone.notify_all();
+    }
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+void cfx_server_default_config(cfx_server_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->hbmBudget = int64_t(150) * 1000 * 1000 * 1000;
+    c->largeCells = 1000000;
+    c->maxBatch = 1024;
+    c->nCellsInCoarsestLevel = 10;
+    c->groupCells = 100000;
+    c->groupSize = 4;
+}
+
+cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_server** out) {
+    if (!ctx || !out) {
+        set_error("cfx_server_create: bad argument");
+        return CFX_ERR_ARG;
+    }
+    return guard([&]() -> cfx_status {
+        auto sv = std::make_unique<cfx_server>();
+        sv->ctx = ctx;
+        if (cfg) {
+            sv->cfg = *cfg;
+        } else {
+            cfx_server_default_config(&sv->cfg);
+        }
+        if (sv->cfg.hbmBudget <= 0 || sv->cfg.largeCells < 1 || sv->cfg.maxBatch < 1 || sv->cfg.groupSize < 0 ||
+            sv->cfg.groupSize > 16) {
+            set_error("cfx_server_create: bad configuration");
+            return CFX_ERR_ARG;
+        }
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaDeviceGetAttribute(&sv->sms, cudaDevAttrMultiProcessorCount, ctx->device));
+        CK(cudaStreamCreateWithFlags(&sv->copyStream, cudaStreamNonBlocking));
+        CFX_TRY(cfx_ctx_create(ctx->device, &sv->ctxLarge));
+        CK(cudaMalloc(&sv->d_next, 2 * sizeof(unsigned)));
+        sv->t0 = Clock::now();
+        sv->worker = std::thread(worker_loop, sv.get());
+        *out = sv.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_server_destroy(cfx_server* sv) {
+    if (!sv) return CFX_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cvWork.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    cudaStreamSynchronize(sv->ctx->stream);
+    for (auto& kv : sv->reqs) free_request_buffers(sv, *kv.second);
+    sv->reqs.clear();
+    for (auto& kv : sv->mats) free_matrix(sv, *kv.second);
+    sv->mats.clear();
+    cudaStreamSynchronize(sv->copyStream);
+    if (sv->d64) cudaFree(sv->d64);
+    if (sv->d32) cudaFree(sv->d32);
+    if (sv->h64) cudaFreeHost(sv->h64);
+    if (sv->h32) cudaFreeHost(sv->h32);
+    if (sv->d_next) cudaFree(sv->d_next);
+    cudaStreamDestroy(sv->copyStream);
+    if (sv->ctxLarge) cfx_ctx_destroy(sv->ctxLarge);
+    sv->cvDone.notify_all();
+    delete sv;
+    return CFX_OK;
+}
+
+cfx_status cfx_server_add_matrix(cfx_server* sv, int nCells, int nFaces, const int32_t* l, const int32_t* u,
+                                 const double* diag, const double* upper, const double* lower,
+                                 const double* faceWeights, int64_t* matrixId) {
+    if (!sv || !matrixId || nCells < 1 || nFaces < 0 || !diag || (nFaces > 0 && (!l || !u || !upper))) {
+        set_error("cfx_server_add_matrix: bad argument");
+        return CFX_ERR_ARG;
+    }
+    const bool large = nCells > sv->cfg.largeCells;
+    const bool sym = lower == nullptr;
+    const size_t est = large ? large_estimate(nCells, nFaces) : bsys_bytes_estimate(nCells, nFaces, sym);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (int64_t(est) > sv->cfg.hbmBudget || int64_t(sv->used + est) > sv->cfg.hbmBudget) {
+            ++sv->refused;
+            set_error("cfx_server_add_matrix: " + std::to_string(est) + " bytes do not fit the HBM budget (" +
+                      std::to_string(sv->used) + " of " + std::to_string(sv->cfg.hbmBudget) + " in use)");
+            return CFX_ERR_ADMISSION;
+        }
+        sv->used += est;  // reserved while the matrix is built
+    }
+    auto m = std::make_unique<SrvMatrix>();
+    m->n = nCells;
+    m->nf = nFaces;
+    m->large = large;
+    m->sym = sym;
+    cfx_status st = guard([&]() -> cfx_status {
+        if (large) {
+            CFX_TRY(cfx_mesh_create(sv->ctxLarge, nCells, nFaces, l, u, &m->mesh));
+            if (faceWeights)
+                CFX_TRY(cfx_gamg_agglomerate(m->mesh, faceWeights, sv->cfg.nCellsInCoarsestLevel, 1));
+            CFX_TRY(cfx_matrix_create(m->mesh, diag, upper, lower, &m->mat));
+            m->bytes = est;
+        } else {
+            m->bs = std::make_unique<BSys>();
+            CFX_TRY(bsys_create(sv->copyStream, nCells, nFaces, l, u, *m->bs));
+            bsys_set_coeffs(sv->copyStream, *m->bs, diag, upper, lower);
+            m->bytes = m->bs->addrBytes + m->bs->coefBytes;
+        }
+        return CFX_OK;
+    });
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->used -= est;
+    if (st != CFX_OK) {
+        if (m->mat) cfx_matrix_destroy(m->mat);
+        if (m->mesh) cfx_mesh_destroy(m->mesh);
+        return st;
+    }
+    sv->used += m->bytes;
+    m->id = sv->nextMat++;
+    *matrixId = m->id;
+    sv->mats[m->id] = std::move(m);
+    return CFX_OK;
+}
+
+cfx_status cfx_server_remove_matrix(cfx_server* sv, int64_t matrixId) {
+    if (!sv) return CFX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->mats.find(matrixId);
+    if (it == sv->mats.end() || it->second->removing) {
+        set_error("cfx_server_remove_matrix: unknown matrix " + std::to_string(matrixId));
+        return CFX_ERR_ARG;
+    }
+    it->second->removing = true;
+    reap(sv);
+    sv->cvDone.notify_all();
+    return CFX_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+cfx_status cfx_server_submit(cfx_server* sv, int64_t matrixId, const cfx_controls* ctl, const double* psi0,
+                             const double* source, int64_t* requestId) {
+    if (!sv || !ctl || !source || !requestId) {
+        set_error("cfx_server_submit: bad argument");
+        return CFX_ERR_ARG;
+    }
+    auto r = std::make_unique<SrvRequest>();
+    r->tSubmit = Clock::now();
+    r->ctl = *ctl;
+    r->matrixId = matrixId;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->mats.find(matrixId);
+    if (it == sv->mats.end() || it->second->removing) {
+        set_error("cfx_server_submit: unknown matrix " + std::to_string(matrixId));
+        return CFX_ERR_ARG;
+    }
+    SrvMatrix* m = it->second.get();
+    if (!m->large) {
+        const cfx_status st = bsys_check_controls(ctl, m->sym);
+        if (st != CFX_OK) return st;
+    } else if (ctl->solver == CFX_SOLVER_GAMG) {
+        int nl = 0;
+        if (cfx_gamg_n_levels(m->mesh, &nl) != CFX_OK || nl < 1) {
+            set_error("cfx_server_submit: cudaGAMG on a matrix registered without face weights");
+            return CFX_ERR_STATE;
+        }
+    }
+    r->n = m->n;
+    r->bytes = 2 * sizeof(double) * size_t(m->n);
+    if (int64_t(r->bytes) > sv->cfg.hbmBudget) {
+        ++sv->refused;
+        set_error("cfx_server_submit: request vectors exceed the HBM budget");
+        return CFX_ERR_ADMISSION;
+    }
+    // admission: wait for space (completions free request vectors)
+    sv->cvDone.wait(lk, [&] { return sv->stop || int64_t(sv->used + r->bytes) <= sv->cfg.hbmBudget; });
+    if (sv->stop) {
+        set_error("cfx_server_submit: server stopping");
+        return CFX_ERR_STATE;
+    }
+    sv->used += r->bytes;
+    m->pending++;
+    r->id = sv->nextReq++;
+    SrvRequest* rp = r.get();
+    sv->reqs[r->id] = std::move(r);
+    ++sv->submitted;
+    lk.unlock();
+    // device vectors and uploads outside the lock (the request is not queued yet)
+    const cfx_status st = guard([&]() -> cfx_status {
+        const size_t b = sizeof(double) * size_t(rp->n);
+        CK(cudaMallocAsync(&rp->d_psi, b, sv->copyStream));
+        CK(cudaMallocAsync(&rp->d_b, b, sv->copyStream));
+        if (psi0)
+            CK(cudaMemcpyAsync(rp->d_psi, psi0, b, cudaMemcpyHostToDevice, sv->copyStream));
+        else
+            CK(cudaMemsetAsync(rp->d_psi, 0, b, sv->copyStream));
+        CK(cudaMemcpyAsync(rp->d_b, source, b, cudaMemcpyHostToDevice, sv->copyStream));
+        CK(cudaStreamSynchronize(sv->copyStream));
+        return CFX_OK;
+    });
+    lk.lock();
+    if (st != CFX_OK) {
+        rp->status = st;
+        rp->error = cfx_last_error();
+        finish(sv, *rp, Q_FAILED);
+        free_request_buffers(sv, *rp);
+        sv->reqs.erase(rp->id);
+        return st;
+    }
+    *requestId = rp->id;
+    sv->queue.push_back(rp->id);
+    sv->cvWork.notify_one();
+    return CFX_OK;
+}
+
+cfx_status cfx_server_wait(cfx_server* sv, int64_t requestId, int timeoutMs, double* psi, cfx_perf* perf) {
+    if (!sv) return CFX_ERR_ARG;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(requestId);
+    if (it == sv->reqs.end() || it->second->detached) {
+        set_error("cfx_server_wait: unknown request " + std::to_string(requestId));
+        return CFX_ERR_ARG;
+    }
+    SrvRequest* r = it->second.get();
+    auto ready = [&] { return r->state != Q_WAITING && r->state != Q_RUNNING; };
+    if (timeoutMs < 0) {
+        sv->cvDone.wait(lk, ready);
+    } else if (!sv->cvDone.wait_for(lk, std::chrono::milliseconds(timeoutMs), ready)) {
+        set_error("cfx_server_wait: request " + std::to_string(requestId) + " not finished after " +
+                  std::to_string(timeoutMs) + " ms");
+        return CFX_ERR_TIMEOUT;
+    }
+    cfx_status st = r->status;
+    if (r->state == Q_CANCELLED) {
+        set_error("cfx_server_wait: request " + std::to_string(requestId) + " was cancelled");
+        st = CFX_ERR_STATE;
+    } else if (r->state == Q_FAILED) {
+        set_error(r->error);
+    } else {
+        if (perf) *perf = r->perf;
+        if (psi) {
+            st = guard([&]() -> cfx_status {
+                CK(cudaMemcpyAsync(psi, r->d_psi, sizeof(double) * size_t(r->n), cudaMemcpyDeviceToHost,
+                                   sv->copyStream));
+                CK(cudaStreamSynchronize(sv->copyStream));
+                return CFX_OK;
+            });
+        }
+    }
+    free_request_buffers(sv, *r);
+    sv->reqs.erase(it);
+    sv->cvDone.notify_all();
+    return st;
+}
+
+cfx_status cfx_server_cancel(cfx_server* sv, int64_t requestId) {
+    if (!sv) return CFX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(requestId);
+    if (it == sv->reqs.end()) {
+        set_error("cfx_server_cancel: unknown request " + std::to_string(requestId));
+        return CFX_ERR_ARG;
+    }
+    SrvRequest& r = *it->second;
+    if (r.state == Q_WAITING) {
+        sv->queue.erase(std::remove(sv->queue.begin(), sv->queue.end(), requestId), sv->queue.end());
+        ++sv->cancelled;
+        finish(sv, r, Q_CANCELLED);
+        free_request_buffers(sv, r);
+        if (r.detached) sv->reqs.erase(it);
+        reap(sv);
+        sv->cvDone.notify_all();
+        return CFX_OK;
+    }
+    // running: it completes; finished: nothing to stop
+    set_error("cfx_server_cancel: request " + std::to_string(requestId) + " is already running or finished");
+    return CFX_ERR_STATE;
+}
+
+cfx_status cfx_server_release(cfx_server* sv, int64_t requestId) {
+    if (!sv) return CFX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(requestId);
+    if (it == sv->reqs.end()) {
+        set_error("cfx_server_release: unknown request " + std::to_string(requestId));
+        return CFX_ERR_ARG;
+    }
+    SrvRequest& r = *it->second;
+    r.detached = true;
+    if (r.state == Q_WAITING) {
+        sv->queue.erase(std::remove(sv->queue.begin(), sv->queue.end(), requestId), sv->queue.end());
+        ++sv->cancelled;
+        finish(sv, r, Q_CANCELLED);
+    }
+    drop_detached(sv);
+    reap(sv);
+    sv->cvDone.notify_all();
+    return CFX_OK;
+}
+
+cfx_status cfx_server_stats(cfx_server* sv, cfx_server_stats_t* o) {
+    if (!sv || !o) return CFX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    std::memset(o, 0, sizeof(*o));
+    o->submitted = sv->submitted;
+    o->completed = sv->completed;
+    o->cancelled = sv->cancelled;
+    o->failed = sv->failed;
+    o->refused = sv->refused;
+    o->batches = sv->batches;
+    o->batchedSolves = sv->batchedSolves;
+    o->largeSolves = sv->largeSolves;
+    o->queueDepth = int64_t(sv->queue.size());
+    o->running = sv->running;
+    o->residentMatrices = int64_t(sv->mats.size());
+    o->hbmInUse = int64_t(sv->used);
+    o->hbmBudget = sv->cfg.hbmBudget;
+    o->elapsedS = std::chrono::duration<double>(Clock::now() - sv->t0).count();
+    o->solvesPerS = o->elapsedS > 0 ? double(sv->completed) / o->elapsedS : 0.0;
+    if (!sv->latMs.empty()) {
+        std::vector<double> v = sv->latMs;
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) {
+            const size_t i = std::min(v.size() - 1, size_t(std::ceil(q * double(v.size()))) - (q > 0 ? 1 : 0));
+            return v[i];
+        };
+        o->p50Ms = pct(0.50);
+        o->p99Ms = pct(0.99);
+        o->maxMs = v.back();
+        double sum = 0.0;
+        for (double x : v) sum += x;
+        o->meanMs = sum / double(v.size());
+    }
+    return CFX_OK;
+}
+
+cfx_status cfx_server_reset_stats(cfx_server* sv) {
+    if (!sv) return CFX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->t0 = Clock::now();
+    sv->submitted = sv->completed = sv->cancelled = sv->failed = sv->refused = 0;
+    sv->batches = sv->batchedSolves = sv->largeSolves = 0;
+    sv->latMs.clear();
+    return CFX_OK;
+}
+
+}  // extern "C"

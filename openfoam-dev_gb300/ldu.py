@@ -70,6 +70,21 @@ class Controls(ctypes.Structure):
                 ("precision", ctypes.c_int), ("pad", ctypes.c_int)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbmBudget", ctypes.c_int64), ("largeCells", ctypes.c_int), ("maxBatch", ctypes.c_int),
+                ("nCellsInCoarsestLevel", ctypes.c_int), ("groupCells", ctypes.c_int), ("groupSize", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "cancelled", "failed", "refused", "batches",
+                                              "batchedSolves", "largeSolves", "queueDepth", "running",
+                                              "residentMatrices", "hbmInUse", "hbmBudget")] + \
+               [(k, ctypes.c_double) for k in ("elapsedS", "solvesPerS", "p50Ms", "p99Ms", "meanMs", "maxMs")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # exported symbols and their signatures (every declaration of include/cfx.h)
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -119,6 +134,18 @@ _SIG = {
     "cfx_batch_timings": (_i, [_vp, _vp, _vp]),
     "cfx_batch_set_ctas_per_sm": (_i, [_vp, _i]),
     "cfx_batch_set_groups": (_i, [_vp, _i, _i]),
+    "cfx_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
+    "cfx_server_create": (_i, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "cfx_server_destroy": (_i, [_vp]),
+    "cfx_server_add_matrix": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
+    "cfx_server_remove_matrix": (_i, [_vp, ctypes.c_int64]),
+    "cfx_server_submit": (_i, [_vp, ctypes.c_int64, ctypes.POINTER(Controls), _vp, _vp,
+                               ctypes.POINTER(ctypes.c_int64)]),
+    "cfx_server_wait": (_i, [_vp, ctypes.c_int64, _i, _vp, ctypes.POINTER(Perf)]),
+    "cfx_server_cancel": (_i, [_vp, ctypes.c_int64]),
+    "cfx_server_release": (_i, [_vp, ctypes.c_int64]),
+    "cfx_server_stats": (_i, [_vp, ctypes.POINTER(ServerStats)]),
+    "cfx_server_reset_stats": (_i, [_vp]),
     "cfx_batch_get_groups": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cfx_batch_tune": (_i, [_vp, ctypes.POINTER(Controls), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_float)]),
 }
@@ -128,7 +155,7 @@ _lib = None
 # Live handles by kind, closed at interpreter exit in dependency order
 # (batches and matrices before the meshes they use, meshes before their
 # context), while the library and the CUDA runtime are still intact.
-_LIVE = {k: weakref.WeakSet() for k in ("batch", "matrix", "mesh", "ctx")}
+_LIVE = {k: weakref.WeakSet() for k in ("server", "batch", "matrix", "mesh", "ctx")}
 
 
 def _track(kind, obj):
@@ -137,7 +164,7 @@ def _track(kind, obj):
 
 @atexit.register
 def _close_all():
-    for kind in ("batch", "matrix", "mesh", "ctx"):
+    for kind in ("server", "batch", "matrix", "mesh", "ctx"):
         for obj in list(_LIVE[kind]):
             try:
                 obj.close()
@@ -610,6 +637,100 @@ class Batch:
         h, self.h = getattr(self, "h", None), None
         if h:
             lib().cfx_batch_destroy(h)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The solve server (cfx_server_*): resident matrices, continuous batching,
+    HBM admission.  ``add_matrix(system)`` registers a cases.py system dict
+    (face weights from its Sf when large and ``gamg``); ``submit`` returns a
+    request id; ``wait`` returns (psi, SolverPerformance).  Thread-safe: the
+    ctypes calls release the GIL, so client threads submit and wait
+    concurrently."""
+
+    def __init__(self, ctx=None, **cfg):
+        self.ctx = ctx or default_context()
+        c = ServerConfig()
+        lib().cfx_server_default_config(ctypes.byref(c))
+        for k, v in cfg.items():
+            setattr(c, k, int(v))
+        self.config = c
+        h = ctypes.c_void_p()
+        _check(lib().cfx_server_create(self.ctx.h, ctypes.byref(c), ctypes.byref(h)), "cfx_server_create")
+        self.h = h
+        self._n = {}
+        self._sym = {}
+        _track("server", self)
+
+    def add_matrix(self, s, gamg=False):
+        l = np.ascontiguousarray(s["l"], np.int32)
+        u = np.ascontiguousarray(s["u"], np.int32)
+        d = np.ascontiguousarray(s["diag"], np.float64)
+        up = np.ascontiguousarray(s["upper"], np.float64)
+        lo = None if s.get("lower") is None else np.ascontiguousarray(s["lower"], np.float64)
+        w = face_area_pair_weights(s["Sf"]) if gamg else None
+        mid = ctypes.c_int64()
+        _check(lib().cfx_server_add_matrix(self.h, d.size, l.size, _hp(l), _hp(u), _hp(d), _hp(up), _hp(lo), _hp(w),
+                                           ctypes.byref(mid)), "cfx_server_add_matrix")
+        self._n[mid.value] = d.size
+        self._sym[mid.value] = lo is None
+        return mid.value
+
+    def remove_matrix(self, mid):
+        _check(lib().cfx_server_remove_matrix(self.h, ctypes.c_int64(mid)), "cfx_server_remove_matrix")
+
+    def submit(self, mid, source, controls, psi0=None):
+        c = _controls(controls, self._sym[mid])
+        src = np.ascontiguousarray(source, np.float64)
+        p0 = None if psi0 is None else np.ascontiguousarray(psi0, np.float64)
+        rid = ctypes.c_int64()
+        _check(lib().cfx_server_submit(self.h, ctypes.c_int64(mid), ctypes.byref(c), _hp(p0), _hp(src),
+                                       ctypes.byref(rid)), "cfx_server_submit")
+        self._n[("r", rid.value)] = self._n[mid]
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1, field="psi"):
+        n = self._n.pop(("r", rid), None)
+        psi = np.empty(n if n is not None else 0)
+        p = Perf()
+        rc = lib().cfx_server_wait(self.h, ctypes.c_int64(rid), int(timeout_ms), _hp(psi) if n else None,
+                                   ctypes.byref(p))
+        if rc == -6 and n is not None:
+            self._n[("r", rid)] = n
+        _check(rc, "cfx_server_wait")
+        return psi, SolverPerformance(p.solverName.decode(), field, p.initialResidual, p.finalResidual,
+                                      p.nIterations, bool(p.converged), bool(p.singular), p.nOuter)
+
+    def cancel(self, rid):
+        _check(lib().cfx_server_cancel(self.h, ctypes.c_int64(rid)), "cfx_server_cancel")
+
+    def release(self, rid):
+        self._n.pop(("r", rid), None)
+        _check(lib().cfx_server_release(self.h, ctypes.c_int64(rid)), "cfx_server_release")
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().cfx_server_stats(self.h, ctypes.byref(st)), "cfx_server_stats")
+        return st.as_dict()
+
+    def metrics_json(self):
+        """One JSON line of the server's metrics (solves/s, p50/p99, queue
+        depth, HBM in use)."""
+        import json
+        return json.dumps(self.stats(), sort_keys=True)
+
+    def reset_stats(self):
+        _check(lib().cfx_server_reset_stats(self.h), "cfx_server_reset_stats")
+
+    def close(self):
+        h, self.h = getattr(self, "h", None), None
+        if h:
+            lib().cfx_server_destroy(h)
 
     def __del__(self):
         try:

@@ -54,6 +54,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", choices=["gs"], default=None,
                     help="only run the finest-level fused 2-sweep Gauss-Seidel (for profiling)")
+    ap.add_argument("--workload", choices=["all", "gamg", "batch", "serve"], default="all",
+                    help="all: the GAMG headline line with the batch and serving measurements added")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--serve-duration", type=float, default=15.0, help="seconds of Poisson arrivals per precision")
+    ap.add_argument("--serve-rate", type=float, default=0.0, help="requests/s (0: 60%% of the estimated capacity)")
+    ap.add_argument("--serve-sweep", action="store_true", help="sweep the rate for the largest with p99 <= 2x unloaded")
+    ap.add_argument("--serve-large", type=int, default=200, help="cells per axis of the large GAMG requests")
     return ap.parse_args()
 
 
@@ -335,6 +342,92 @@ def run_ours(args, rank, world, local, pg):
     return 0
 
 
+def cpu_batch_sample(count, seed=1, per_core=2):
+    """Oracle PCG+DIC (serial C restatement) on an even sample of the batch,
+    one process per host core: solves/s of the host cores."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    k = min(count, per_core * cores)
+    idx = [int(round(i * (count - 1) / max(k - 1, 1))) for i in range(k)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.starmap(_cpu_batch_one, [(seed, count, i) for i in idx])
+    wall = time.perf_counter() - t0
+    return {"value": k / wall, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"{k} of the {count} systems (evenly spaced), oracle PCG+DIC FP64 to 1e-8, one process per "
+                      f"core; {wall:.1f} s wall, {sum(r[1] for r in res):.1f} s of CPU work",
+            "converged": all(r[0] for r in res)}
+
+
+def _cpu_batch_one(seed, count, i):
+    ge.load_package()
+    from oracle import oracle as orc
+    from openfoam_dev_gb300 import cases
+    nx, ny, nz, f, sd = cases.batch_boxes(count, seed=seed)[i]
+    s = cases.box(nx, ny, nz, dirichlet=f, seed=sd)
+    x = np.zeros(s["diag"].size)
+    t0 = time.process_time()
+    p = orc.pcg(s, x, tol=1e-8, max_iter=2000)
+    return bool(p.converged), time.process_time() - t0
+
+
+def run_batch_serve(args, local, want_batch, want_serve):
+    """The batched (512 independent systems) and serving measurements."""
+    import torch
+    ge.load_package()
+    from openfoam_dev_gb300 import cases, ldu, loadgen
+    out = {}
+    ctx = ldu.Context(local)
+    if want_batch:
+        systems = loadgen.batch_systems(args.batch_count, seed=1)
+        b = {"workload": f"{args.batch_count} independent PCG+DIC Laplacian box systems (cells log-uniform in "
+                         f"[4096, 500000], aspect U[1,4], Dirichlet on one seeded face), tolerance 1e-8, one "
+                         f"persistent launch, autotuned packing"}
+        for prec in ("mixed", "FP64"):
+            b[prec] = loadgen.bench_batch(ctx, systems, steps=args.steps, warmup=1, precision=prec)
+        del systems
+        if not args.no_cpu_baseline:
+            b["cpu_baseline"] = cpu_batch_sample(args.batch_count)
+        out["batch"] = b
+    if want_serve:
+        pool = loadgen.batch_systems(64, seed=5)
+        large = cases.gamg_cube(args.serve_large, jitter=0.2, seed=9)
+        sv = ldu.Server(ctx)
+        mix = loadgen.ServeMix(sv, pool, large, resident=16, seed=3)
+        srv = {"workload": f"Poisson arrivals: 90% batch-like systems (30% of all requests re-solve one of 16 "
+                           f"resident matrices with a new source; the rest register one of 64 pool systems, "
+                           f"solve, remove), 10% GAMG on a {args.serve_large}^3 jittered cube "
+                           f"({args.serve_large ** 3} cells, resident); HBM budget "
+                           f"{sv.config.hbmBudget / 1e9:.0f} GB"}
+        for prec in ("mixed", "FP64"):
+            mix.run(mix.draw(), prec)  # warm the drivers
+            mix.run(("large", None, 1), prec)
+            un = loadgen.serve_unloaded(mix, 24, prec)
+            t_large = un["by_kind_p50_ms"].get("large", 1000.0) / 1e3
+            rate = args.serve_rate or 0.6 / (0.1 * t_large + 0.9 * 0.01)
+            r = {"unloaded": un}
+            if args.serve_sweep:
+                sweep = []
+                for f in (0.4, 0.6, 0.8, 1.0, 1.2):
+                    q = loadgen.serve_stream(mix, rate / 0.6 * f, args.serve_duration, prec)
+                    q["p99_over_unloaded"] = q["p99_ms"] / un["p99_ms"]
+                    sweep.append(q)
+                ok = [q for q in sweep if q["p99_over_unloaded"] <= 2.0]
+                r["sweep"] = sweep
+                r["max_sustainable_solves_per_s"] = max((q["solves_per_s"] for q in ok), default=None)
+            else:
+                q = loadgen.serve_stream(mix, rate, args.serve_duration, prec)
+                q["p99_over_unloaded"] = q["p99_ms"] / un["p99_ms"]
+                r["stream"] = q
+            srv[prec] = r
+        sv.close()
+        out["serve"] = srv
+    ctx.close()
+    torch.cuda.synchronize()
+    return out
+
+
 def run_kernel_only(args):
     """The finest-level fused 2-sweep GaussSeidel alone, warmup + steps times."""
     import torch
@@ -361,6 +454,12 @@ def main():
     if args.kernel_only:
         return run_kernel_only(args)
     rank, world, local, pg = dist()
+    if args.impl == "ours" and args.workload in ("batch", "serve"):
+        import torch
+        torch.cuda.set_device(local)
+        extra = run_batch_serve(args, local, args.workload == "batch", args.workload == "serve")
+        print(json.dumps(dict(extra, workload=args.workload)), flush=True)
+        return 0
     if args.impl == "reference":
         rc = run_reference(args, rank, world, pg)
     else:

@@ -338,6 +338,8 @@ def run_ours(args, rank, world, local, pg):
                       f"agglomeration + 1 and 2 V-cycles timed, extrapolated to the {r['cycles']} V-cycles "
                       f"of the FP64 solve ({r['sample_s']:.1f} s of CPU work)",
             "detail": r}
+    if world == 1 and args.workload == "all":
+        line.update(run_batch_serve(args, local, True, True))
     print(json.dumps(line), flush=True)
     return 0
 

@@ -164,12 +164,17 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
  *   CFX_TUNE_CLUSTER_GLOBAL <= this many cells: one cluster, vector in global
  *                           memory, cluster barriers between levels
  *   larger: the persistent grid-wide level scheduler.
- *   CFX_TUNE_CLUSTER_SIZE   CTAs per cluster (16 or 8 as the GPU allows; 0
- *                           disables the cluster forms). */
+ *   CFX_TUNE_CLUSTER_SIZE   CTAs per cluster (16 or 8 as the GPU allows; 0,
+ *                           the default, disables the cluster forms: on GB300
+ *                           the grid form sweeps mid-size levels faster). */
 enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_SIZE = 2,
        /* FP32 inner solves of mixed-precision batches (cfx_batch_*) reduce
         * the residual by 10^-value (default 3) per refinement step */
-       CFX_TUNE_BATCH_INNER_DIGITS = 3 };
+       CFX_TUNE_BATCH_INNER_DIGITS = 3,
+       /* bytes of the swept vector one CTA may hold in shared memory (the
+        * single-CTA form and a cluster CTA's share); default the device's
+        * opt-in limit less the kernels' static use; 0 forces global forms */
+       CFX_TUNE_SMEM_BYTES = 4 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -1307,6 +1307,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value < 1 || value > 7) return CFX_ERR_ARG;
             batch_set_inner_digits(value);
             return CFX_OK;
+        case CFX_TUNE_SMEM_BYTES:
+            if (size_t(value) > sweep_smem_cap_max()) return CFX_ERR_ARG;
+            set_sweep_smem_cap(size_t(value));
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -1318,6 +1322,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_CLUSTER_GLOBAL: *value = cluster_global_cells(); return CFX_OK;
         case CFX_TUNE_CLUSTER_SIZE: *value = sweep_cluster_size(); return CFX_OK;
         case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
+        case CFX_TUNE_SMEM_BYTES: *value = int(sweep_smem_cap()); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

@@ -208,6 +208,7 @@ void pack_sweep(cudaStream_t st, const DevSched& s, int op, const LevelCoeffs<T>
 int small_sweep_threshold();
 void set_small_sweep_threshold(int n);
 size_t sweep_smem_cap();
+size_t sweep_smem_cap_max();
 void set_sweep_smem_cap(size_t b);
 int sweep_cluster_size();
 void set_sweep_cluster_size(int cs);

@@ -54,15 +54,17 @@ constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
 constexpr int GRID_NT = 256;                            // 8 warps = one chunk
 constexpr int CTA_NT = 256;
 constexpr int CL_NT = 256;                              // threads per cluster CTA
-constexpr int PF = 8;                                   // entries held in registers (grid)
+constexpr int PF_SMALL = 8, PF_LARGE = 16;              // entries held in registers per slot
 namespace cg = cooperative_groups;
 
 int g_num_sms = 152;
-int g_cluster = 0;          // CTAs per cluster of sweep_cluster_k (0: unavailable)
+int g_cluster = 0;          // CTAs per cluster of sweep_cluster_k (0: not used)
+int g_cluster_avail = 0;    // largest cluster the GPU can hold (16 or 8; 0: none)
 int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
 int g_cluster_global = 0;   // <= this many cells: one cluster with the vector in global memory
-int g_grid[2][8];           // resident CTAs of sweep_grid_k per (precision, op)
+int g_grid[2][8][2];        // resident CTAs of sweep_grid_k per (precision, op, PF_LARGE)
 size_t g_smem_cap = 200 * 1024;
+size_t g_smem_cap_max = 200 * 1024;
 
 template <class T>
 struct SweepCtx {
@@ -96,7 +98,27 @@ __device__ __forceinline__ T sw_fini(T acc, T sc) {
     return acc;
 }
 
-template <class T, int OP>
+// Entries k >= k0 of one slot, loaded in batches of 8 independent loads so
+// the latency is paid once per batch, then applied in order.
+template <class T, int OP, class XF>
+__device__ __forceinline__ T tail_entries(const DevSched& s, const T* coef, int e0, int k0, int n, T acc, XF xat) {
+    for (int kb = k0; kb < n; kb += 8) {
+        int nb[8];
+        T cf[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (kb + j < n) {
+                nb[j] = s.nb[e0 + 32 * (kb + j)];
+                cf[j] = coef[e0 + 32 * (kb + j)];
+            }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (kb + j < n) acc = sw_step<OP>(acc, cf[j], xat(nb[j]));
+    }
+    return acc;
+}
+
+template <class T, int OP, int PF>
 __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> a, int* status) {
     __shared__ double sh[GRID_NT / 32];
     __shared__ int sh_ok;
@@ -166,7 +188,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
 #pragma unroll
             for (int k = 0; k < PF; ++k)
                 if (k < n) acc = sw_step<OP>(acc, cf[k], ldcg(a.x + nbr[k]));
-            for (int k = PF; k < n; ++k) acc = sw_step<OP>(acc, a.coef[e0 + 32 * k], ldcg(a.x + s.nb[e0 + 32 * k]));
+            acc = tail_entries<T, OP>(s, a.coef, e0, PF, n, acc, [&](int cc) { return ldcg(a.x + cc); });
             v = sw_fini<OP>(acc, sc);
             a.x[c] = v;
         }
@@ -187,8 +209,9 @@ __device__ __forceinline__ T* cl_ref(cg::cluster_group& cl, T* Xl, int per, int 
     return cl.map_shared_rank(Xl, o) + (c - o * per);
 }
 
-// Packed data of one group slot held in registers.
-template <class T>
+// Packed data of one group slot held in registers: the header (cell, entry
+// count, entry offset, scalar, right-hand side) and the first PF entries.
+template <class T, int PF>
 struct SlotRegs {
     int c, n, e0;
     T sc, in;
@@ -196,71 +219,77 @@ struct SlotRegs {
     T cf[PF];
 };
 
-template <class T, int OP>
-__device__ __forceinline__ void load_slot(const DevSched& s, const SweepCtx<T>& a, int g, int lane, SlotRegs<T>& r) {
-    const int slot = g * 32 + lane;
-    r.c = s.cell[slot];
+// Header of slot (g, lane): independent loads, and no branch on their
+// values, so issuing them never waits for memory.
+template <class T, int OP, int PF>
+__device__ __forceinline__ void load_header(const DevSched& s, const SweepCtx<T>& a, int g, bool ok, int lane,
+                                            SlotRegs<T, PF>& r) {
+    r.c = -1;
     r.n = 0;
-    if (r.c < 0) return;
-    r.n = s.cnt[slot];
-    r.e0 = s.groupEntry[g] + lane;
-    r.sc = a.scalar[slot];
-    r.in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+    if (ok) {
+        const int slot = g * 32 + lane;
+        r.c = s.cell[slot];
+        r.n = s.cnt[slot];  // 0 for padding slots
+        r.e0 = s.groupEntry[g] + lane;
+        r.sc = a.scalar[slot];
+        r.in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+    }
+}
+
+// The first PF entries of a slot whose header was issued a level earlier.
+template <class T, int PF>
+__device__ __forceinline__ void load_entries(const DevSched& s, const T* coef, SlotRegs<T, PF>& r) {
 #pragma unroll
     for (int k = 0; k < PF; ++k)
         if (k < r.n) {
             r.nbr[k] = s.nb[r.e0 + 32 * k];
-            r.cf[k] = a.coef[r.e0 + 32 * k];
+            r.cf[k] = coef[r.e0 + 32 * k];
         }
 }
 
-// Entries k >= k0 of one slot, loaded in batches of 8 independent loads so
-// the latency is paid once per batch, then applied in order.
-template <class T, int OP, class XF>
-__device__ __forceinline__ T tail_entries(const DevSched& s, const T* coef, int e0, int k0, int n, T acc, XF xat) {
-    for (int kb = k0; kb < n; kb += 8) {
-        int nb[8];
-        T cf[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (kb + j < n) {
-                nb[j] = s.nb[e0 + 32 * (kb + j)];
-                cf[j] = coef[e0 + 32 * (kb + j)];
-            }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (kb + j < n) acc = sw_step<OP>(acc, cf[j], xat(nb[j]));
-    }
-    return acc;
-}
+// Level bounds (levelSlot) of the first LS_CACHE levels are copied to shared
+// memory at kernel start, so level loops read no global memory for them.
+constexpr int LS_CACHE = 4096;
 
-// One CTA; X = shared-memory copy of the vector when XS, else global.  Each
-// warp loads its first group of the next level into registers before the
-// block barrier, so the global-memory latency overlaps the barrier.
-template <class T, int OP, bool XS>
+// Pipeline of the single-CTA and cluster forms.  While level L is computed
+// from register set X (header and entries in place), the entries of level
+// L+1 are issued into set Y (its header arrived during level L-1) and the
+// header of level L+2 into X: no load in the level loop waits for memory
+// except the neighbour values of the level being computed.  A warp's further
+// groups in a wide level are loaded directly.
+
+// One CTA; X = shared-memory copy of the vector when XS, else global.
+template <class T, int OP, bool XS, int PF>
 __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double sh[CTA_NT / 32];
+    __shared__ int lsl[LS_CACHE + 1];
     if (a.done && *a.done) return;
     T* X = XS ? reinterpret_cast<T*>(smem_raw) : a.x;
     const int n = s.n;
+    const int nL = s.nLevels;
+    const int nc = nL + 1 < LS_CACHE + 1 ? nL + 1 : LS_CACHE + 1;
+    for (int i = threadIdx.x; i < nc; i += CTA_NT) lsl[i] = s.levelSlot[i];
     if (XS && (OP == OP_BWD || OP == OP_GS)) {
         for (int i = threadIdx.x; i < n; i += CTA_NT) X[i] = a.x[i];
     }
+    __syncthreads();
     constexpr int WARPS = CTA_NT / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    auto lslot = [&](int L) -> int { return L < nc ? lsl[L] : s.levelSlot[L]; };
     auto xat = [&](int c) -> T { return XS ? X[c] : ldcg(a.x + c); };
-    auto prefetch = [&](int L, SlotRegs<T>& r) {
-        r.c = -1;
-        r.n = 0;
-        if (L < s.nLevels) {
-            const int g = (s.levelSlot[L] >> 5) + w;
-            if (g < (s.levelSlot[L + 1] >> 5)) load_slot<T, OP>(s, a, g, lane, r);
+    auto header = [&](int L, SlotRegs<T, PF>& r) {
+        int g = 0;
+        bool ok = false;
+        if (L < nL) {
+            g = (lslot(L) >> 5) + w;
+            ok = g < (lslot(L + 1) >> 5);
         }
+        load_header<T, OP, PF>(s, a, g, ok, lane, r);
     };
     double dot = 0.0;
-    auto level = [&](int L, SlotRegs<T>& cur) {
-        const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
+    auto level = [&](int L, SlotRegs<T, PF>& cur, SlotRegs<T, PF>& nxt) {
+        const int g0 = lslot(L) >> 5, g1 = lslot(L + 1) >> 5;
         if (cur.c >= 0) {
             T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? xat(cur.c) : T(0));
 #pragma unroll
@@ -285,18 +314,17 @@ __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a)
             X[c] = v;
             if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
         }
-        // the level after next into the registers just consumed
-        prefetch(L + 2, cur);
+        load_entries<T, PF>(s, a.coef, nxt);
+        header(L + 2, cur);
         __syncthreads();
     };
-    // two register sets, two levels ahead (no register copies between levels)
-    SlotRegs<T> A, B;
-    prefetch(0, A);
-    prefetch(1, B);
-    __syncthreads();
-    for (int L = 0; L < s.nLevels; L += 2) {
-        level(L, A);
-        if (L + 1 < s.nLevels) level(L + 1, B);
+    SlotRegs<T, PF> A, B;
+    header(0, A);
+    header(1, B);
+    load_entries<T, PF>(s, a.coef, A);
+    for (int L = 0; L < nL; L += 2) {
+        level(L, A, B);
+        if (L + 1 < nL) level(L + 1, B, A);
     }
     if (XS)
         for (int i = threadIdx.x; i < n; i += CTA_NT) a.x[i] = X[i];
@@ -307,22 +335,31 @@ __global__ void __launch_bounds__(CTA_NT) sweep_cta_k(DevSched s, SweepCtx<T> a)
 }
 
 // DS: vector in distributed shared memory; otherwise in global memory (L2),
-// read with L2-coherent loads, and only the barrier is the cluster's.
-template <class T, int OP, bool DS>
+// read with L2-coherent loads, and only the barrier is the cluster's.  The
+// groups of a level go round the CTAs: CTA r takes g0 + r + CS*j, its warp w
+// the j = w, w + WARPS, ...  Between levels the barrier is split: arrive
+// (release: this level's writes), issue the pipeline's loads, wait (acquire).
+template <class T, int OP, bool DS, int PF>
 __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T> a, int per) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double sh[CL_NT / 32];
+    __shared__ int lsl[LS_CACHE + 1];
     if (a.done && *a.done) return;
     cg::cluster_group cl = cg::this_cluster();
     const int CS = int(cl.num_blocks());
     const int rank = int(cl.block_rank());
     T* Xl = reinterpret_cast<T*>(smem_raw);
     const int n = s.n;
+    const int nL = s.nLevels;
+    const int nc = nL + 1 < LS_CACHE + 1 ? nL + 1 : LS_CACHE + 1;
+    for (int i = threadIdx.x; i < nc; i += CL_NT) lsl[i] = s.levelSlot[i];
     const int base = rank * per;
     if (DS && (OP == OP_BWD || OP == OP_GS))
         for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) Xl[i] = a.x[base + i];
+    __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int WARPS = CL_NT / 32;
+    auto lslot = [&](int L) -> int { return L < nc ? lsl[L] : s.levelSlot[L]; };
     auto xat = [&](int c) -> T { return DS ? *cl_ref(cl, Xl, per, c) : ldcg(a.x + c); };
     auto xset = [&](int c, T v) {
         if (DS)
@@ -330,18 +367,18 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
         else
             a.x[c] = v;
     };
-    // level groups g0.., this CTA takes g0 + rank + CS*j, warp w takes j = w, w + WARPS, ...
-    auto prefetch = [&](int L, SlotRegs<T>& r) {
-        r.c = -1;
-        r.n = 0;
-        if (L < s.nLevels) {
-            const int g = (s.levelSlot[L] >> 5) + rank + CS * w;
-            if (g < (s.levelSlot[L + 1] >> 5)) load_slot<T, OP>(s, a, g, lane, r);
+    auto header = [&](int L, SlotRegs<T, PF>& r) {
+        int g = 0;
+        bool ok = false;
+        if (L < nL) {
+            g = (lslot(L) >> 5) + rank + CS * w;
+            ok = g < (lslot(L + 1) >> 5);
         }
+        load_header<T, OP, PF>(s, a, g, ok, lane, r);
     };
     double dot = 0.0;
-    auto level = [&](int L, SlotRegs<T>& cur) {
-        const int g0 = s.levelSlot[L] >> 5, g1 = s.levelSlot[L + 1] >> 5;
+    auto level = [&](int L, SlotRegs<T, PF>& cur, SlotRegs<T, PF>& nxt) {
+        const int g0 = lslot(L) >> 5, g1 = lslot(L + 1) >> 5;
         if (cur.c >= 0) {
             T acc = sw_init<OP>(cur.sc, cur.in, OP == OP_BWD ? xat(cur.c) : T(0));
 #pragma unroll
@@ -366,19 +403,19 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
             xset(c, v);
             if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
         }
-        // arrive (release: this level's writes), prefetch the level after
-        // next while the other CTAs finish, then wait (acquire)
         cl.barrier_arrive();
-        prefetch(L + 2, cur);
+        load_entries<T, PF>(s, a.coef, nxt);
+        header(L + 2, cur);
         cl.barrier_wait();
     };
-    SlotRegs<T> A, B;
-    prefetch(0, A);
-    prefetch(1, B);
+    SlotRegs<T, PF> A, B;
+    header(0, A);
+    header(1, B);
+    load_entries<T, PF>(s, a.coef, A);
     cl.sync();
-    for (int L = 0; L < s.nLevels; L += 2) {
-        level(L, A);
-        if (L + 1 < s.nLevels) level(L + 1, B);
+    for (int L = 0; L < nL; L += 2) {
+        level(L, A, B);
+        if (L + 1 < nL) level(L + 1, B, A);
     }
     if (DS)
         for (int i = threadIdx.x; i < per && base + i < n; i += CL_NT) a.x[base + i] = Xl[i];
@@ -454,14 +491,14 @@ int mode_of(const DevSched& s) {
     return M_GRID;
 }
 
-template <class T, int OP>
-cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+template <class T, int OP, int PF>
+cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
     if (s.nSlots == 0) return CFX_OK;
     const size_t xbytes = sizeof(T) * size_t(s.n);
     const int per = g_cluster ? (s.n + g_cluster - 1) / g_cluster : 0;
     const int m = mode_of<T>(s);
     if (m == M_CTA) {
-        sweep_cta_k<T, OP, true><<<1, CTA_NT, xbytes, st>>>(s, a);
+        sweep_cta_k<T, OP, true, PF><<<1, CTA_NT, xbytes, st>>>(s, a);
     } else if (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) {
         const bool ds = m == M_CLUSTER_DS;
         cudaLaunchConfig_t cfg = {};
@@ -477,14 +514,14 @@ cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int*
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         if (ds)
-            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, true>, s, a, per));
+            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, true, PF>, s, a, per));
         else
-            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, false>, s, a, per));
+            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, false, PF>, s, a, per));
     } else if (m == M_CTA_GLOBAL) {
-        sweep_cta_k<T, OP, false><<<1, CTA_NT, 0, st>>>(s, a);
+        sweep_cta_k<T, OP, false, PF><<<1, CTA_NT, 0, st>>>(s, a);
     } else {
         CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
-        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP]);
+        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP][PF == PF_LARGE]);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
         cfg.blockDim = dim3(GRID_NT);
@@ -495,21 +532,37 @@ cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int*
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_grid_k<T, OP>, s, a, status));
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_grid_k<T, OP, PF>, s, a, status));
     }
     count_launch();
     return CFX_OK;
 }
 
+// Slots with at most PF_SMALL entries (hexahedral fine levels) take the
+// lighter register set; agglomerated levels, whose cells have many more
+// neighbours, hold PF_LARGE entries per slot in registers.
+template <class T, int OP>
+cfx_status launch(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+    if (s.maxK <= PF_SMALL) return launch_pf<T, OP, PF_SMALL>(st, s, a, status);
+    return launch_pf<T, OP, PF_LARGE>(st, s, a, status);
+}
+
+template <class T, int OP, int PF>
+void init_op_pf() {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP, PF>, GRID_NT, 0);
+    g_grid[prec_index<T>()][OP][PF == PF_LARGE] = g_num_sms * (per > 0 ? per : 1);
+    cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(g_smem_cap));
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(sweep_cluster_k<T, OP, false, PF>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
 template <class T, int OP>
 void init_op() {
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP>, GRID_NT, 0);
-    g_grid[prec_index<T>()][OP] = g_num_sms * (per > 0 ? per : 1);
-    cudaFuncSetAttribute(sweep_cta_k<T, OP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
-    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
-    cudaFuncSetAttribute(sweep_cluster_k<T, OP, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    cudaFuncSetAttribute(sweep_cluster_k<T, OP, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    init_op_pf<T, OP, PF_SMALL>();
+    init_op_pf<T, OP, PF_LARGE>();
 }
 
 // Largest cluster (16, else 8) that can be resident with a full-size
@@ -528,7 +581,7 @@ int probe_cluster() {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int num = 0;
-        if (cudaOccupancyMaxActiveClusters(&num, sweep_cluster_k<double, OP_GS, true>, &cfg) == cudaSuccess && num > 0)
+        if (cudaOccupancyMaxActiveClusters(&num, sweep_cluster_k<double, OP_GS, true, PF_LARGE>, &cfg) == cudaSuccess && num > 0)
             return cs;
         cudaGetLastError();
     }
@@ -551,19 +604,26 @@ void sweeps_init(int numSms) {
     cudaGetDevice(&dev);
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    // leave room for the CTA kernel's static shared memory
-    if (optin > 4096) g_smem_cap = size_t(optin) - 4096;
+    // leave room for the kernels' static shared memory (level bounds cache)
+    constexpr int reserve = 4096 + 4 * (LS_CACHE + 1);
+    if (optin > reserve) g_smem_cap = size_t(optin) - reserve;
+    g_smem_cap_max = g_smem_cap;
     init_attrs<double>();
     init_attrs<float>();
-    g_cluster = probe_cluster();
+    // The cluster forms are kept behind CFX_TUNE_CLUSTER_SIZE: on GB300 the
+    // persistent grid form sweeps the mid-size levels faster (a cluster
+    // barrier per level costs more than the grid's per-level counters).
+    g_cluster_avail = probe_cluster();
+    g_cluster = 0;
 }
 
 int sweep_cluster_size() { return g_cluster; }
-void set_sweep_cluster_size(int cs) { g_cluster = cs; }
+void set_sweep_cluster_size(int cs) { g_cluster = cs <= g_cluster_avail ? cs : g_cluster_avail; }
 
 int small_sweep_threshold() { return g_small_threshold; }
 void set_small_sweep_threshold(int n) { g_small_threshold = n; }
 size_t sweep_smem_cap() { return g_smem_cap; }
+size_t sweep_smem_cap_max() { return g_smem_cap_max; }
 void set_sweep_smem_cap(size_t b) { g_smem_cap = b; }
 
 template <class T>

@@ -415,7 +415,7 @@ class SolverPerformance:
                 f"Final residual = {self.finalResidual:g}, No Iterations {self.nIterations}")
 
 
-TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS = 0, 1, 2, 3
+TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS, TUNE_SMEM_BYTES = 0, 1, 2, 3, 4
 
 
 def tune_set(key, value):

@@ -1,0 +1,31 @@
+"""The execution forms of the level-scheduled sweeps, forced through the
+library's tuning knobs so every form is checked on small systems:
+
+* small   -- one CTA, vector in global memory
+* cta     -- one CTA, vector in shared memory (the default for small levels)
+* cluster -- a 16-CTA cluster, vector in distributed shared memory
+* grid    -- the persistent grid-wide level scheduler (vector in global memory)
+"""
+import contextlib
+
+from openfoam_dev_gb300 import ldu
+
+FORMS = {
+    "small": {ldu.TUNE_SMALL_SWEEP: 1 << 30, ldu.TUNE_SMEM_BYTES: 0},
+    "cta": {},
+    "cluster": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 8192},
+    "grid": {ldu.TUNE_SMEM_BYTES: 0},
+}
+KNOBS = (ldu.TUNE_SMALL_SWEEP, ldu.TUNE_CLUSTER_GLOBAL, ldu.TUNE_CLUSTER_SIZE, ldu.TUNE_SMEM_BYTES)
+
+
+@contextlib.contextmanager
+def sweep_form(name):
+    old = {k: ldu.tune_get(k) for k in KNOBS}
+    try:
+        for k, v in FORMS[name].items():
+            ldu.tune_set(k, v)
+        yield name
+    finally:
+        for k in KNOBS:
+            ldu.tune_set(k, old[k])

@@ -13,6 +13,7 @@ import pytest
 
 from golden_cases import system
 from oracle import oracle as orc
+from sweep_forms import FORMS, sweep_form as form_ctx
 from openfoam_dev_gb300 import cases, ldu
 
 pytestmark = pytest.mark.gpu
@@ -46,12 +47,10 @@ SYSTEMS = {
 }
 
 
-@pytest.fixture(params=["small", "multi"])
+@pytest.fixture(params=sorted(FORMS))
 def sweep_form(request):
-    old = ldu.tune_get(ldu.TUNE_SMALL_SWEEP)
-    ldu.tune_set(ldu.TUNE_SMALL_SWEEP, 1 << 30 if request.param == "small" else 0)
-    yield request.param
-    ldu.tune_set(ldu.TUNE_SMALL_SWEEP, old)
+    with form_ctx(request.param):
+        yield request.param
 
 
 def _fresh(s):

@@ -17,6 +17,7 @@ import pytest
 
 from golden_cases import SPECS, solve_case
 from oracle import oracle as orc
+from sweep_forms import FORMS, sweep_form
 from openfoam_dev_gb300 import cases, ldu
 
 pytestmark = pytest.mark.gpu
@@ -117,19 +118,15 @@ def _oracle(s, solver, tol, **kw):
     return psi, p
 
 
-@pytest.mark.parametrize("form", ["small", "multi"])
+@pytest.mark.parametrize("form", sorted(FORMS))
 def test_pcg_cube_against_oracle(form):
-    """C1 shape (uniform cube Laplacian, Dirichlet x=0) at 40^3."""
-    old = ldu.tune_get(ldu.TUNE_SMALL_SWEEP)
-    ldu.tune_set(ldu.TUNE_SMALL_SWEEP, 1 << 30 if form == "small" else 0)
-    try:
+    """C1 shape (uniform cube Laplacian, Dirichlet x=0) at 40^3, every sweep form."""
+    with sweep_form(form):
         s = cases.pcg_cube(40, seed=1)
         ref, rp = _oracle(s, "PCG", 1e-8)
         psi = np.zeros_like(s["source"])
         perf = ldu.solve(s, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-8,
                                   "relTol": 0, "maxIter": 2000})
-    finally:
-        ldu.tune_set(ldu.TUNE_SMALL_SWEEP, old)
     assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
     assert _rel(psi, ref) <= RTOL_FP64
 

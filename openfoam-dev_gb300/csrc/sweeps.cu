@@ -54,7 +54,7 @@ constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
 constexpr int GRID_NT = 256;                            // 8 warps = one chunk
 constexpr int CTA_NT = 256;
 constexpr int CL_NT = 256;                              // threads per cluster CTA
-constexpr int PF_SMALL = 8, PF_LARGE = 16;              // entries held in registers per slot
+constexpr int PF_SMALL = 8, PF_LARGE = 16, PF_GRID_XL = 32;  // entries held in registers per slot
 namespace cg = cooperative_groups;
 
 int g_num_sms = 152;
@@ -62,7 +62,7 @@ int g_cluster = 0;          // CTAs per cluster of sweep_cluster_k (0: not used)
 int g_cluster_avail = 0;    // largest cluster the GPU can hold (16 or 8; 0: none)
 int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
 int g_cluster_global = 0;   // <= this many cells: one cluster with the vector in global memory
-int g_grid[2][8][2];        // resident CTAs of sweep_grid_k per (precision, op, PF_LARGE)
+int g_grid[2][8][3];        // resident CTAs of sweep_grid_k per (precision, op, PF 8/16/32)
 size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
 
@@ -491,6 +491,11 @@ int mode_of(const DevSched& s) {
     return M_GRID;
 }
 
+constexpr int pf_index(int pf) { return pf == PF_SMALL ? 0 : pf == PF_LARGE ? 1 : 2; }
+
+template <class T, int OP, int PF>
+cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status);
+
 template <class T, int OP, int PF>
 cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
     if (s.nSlots == 0) return CFX_OK;
@@ -519,9 +524,22 @@ cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, i
             CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_cluster_k<T, OP, false, PF>, s, a, per));
     } else if (m == M_CTA_GLOBAL) {
         sweep_cta_k<T, OP, false, PF><<<1, CTA_NT, 0, st>>>(s, a);
+    } else if (sizeof(T) == 4 && PF == PF_LARGE && s.maxK > PF_LARGE) {
+        // FP32: the grid form holds up to PF_GRID_XL entries (one register
+        // set).  In FP64 the larger set costs more in occupancy than it saves.
+        return launch_grid<T, OP, (sizeof(T) == 4 ? PF_GRID_XL : PF_LARGE)>(st, s, a, status);
     } else {
+        return launch_grid<T, OP, PF>(st, s, a, status);
+    }
+    count_launch();
+    return CFX_OK;
+}
+
+template <class T, int OP, int PF>
+cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+    {
         CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
-        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP][PF == PF_LARGE]);
+        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP][pf_index(PF)]);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
         cfg.blockDim = dim3(GRID_NT);
@@ -551,7 +569,7 @@ template <class T, int OP, int PF>
 void init_op_pf() {
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP, PF>, GRID_NT, 0);
-    g_grid[prec_index<T>()][OP][PF == PF_LARGE] = g_num_sms * (per > 0 ? per : 1);
+    g_grid[prec_index<T>()][OP][pf_index(PF)] = g_num_sms * (per > 0 ? per : 1);
     cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(g_smem_cap));
@@ -563,6 +581,12 @@ template <class T, int OP>
 void init_op() {
     init_op_pf<T, OP, PF_SMALL>();
     init_op_pf<T, OP, PF_LARGE>();
+    if (sizeof(T) == 4) {
+        constexpr int XL = sizeof(T) == 4 ? PF_GRID_XL : PF_LARGE;
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP, XL>, GRID_NT, 0);
+        g_grid[prec_index<T>()][OP][pf_index(XL)] = g_num_sms * (per > 0 ? per : 1);
+    }
 }
 
 // Largest cluster (16, else 8) that can be resident with a full-size

@@ -174,7 +174,11 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
        /* bytes of the swept vector one CTA may hold in shared memory (the
         * single-CTA form and a cluster CTA's share); default the device's
         * opt-in limit less the kernels' static use; 0 forces global forms */
-       CFX_TUNE_SMEM_BYTES = 4 };
+       CFX_TUNE_SMEM_BYTES = 4,
+       /* grid form: 1 = wavefront, each 32-slot group waits only for the
+        * groups it reads; 0 (default) = whole-level counters, faster on GB300
+        * for the fused multi-sweep Gauss-Seidel of the coarse levels */
+       CFX_TUNE_GRID_WAVE = 5 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -362,6 +362,10 @@ DevSched upload_sched(Arena& ar, cudaStream_t s, const HostSched& h) {
     d.chunkGroup = ar.upload(h.chunkGroup, s);
     d.chunkLevel = ar.upload(h.chunkLevel, s);
     d.levelChunks = ar.upload(h.levelChunks, s);
+    d.depStart = ar.upload(h.depStart, s);
+    d.dep = ar.upload(h.dep, s);
+    d.gdone = ar.get<int>(std::max(d.nGroups, 1));
+    d.waveOk = h.waveOk ? 1 : 0;
     d.sync = ar.get<int>(2 + std::max(h.nLevels, 1));
     CK(cudaMemsetAsync(d.sync, 0, sizeof(int) * (2 + std::max(h.nLevels, 1)), s));
     return d;
@@ -1311,6 +1315,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (size_t(value) > sweep_smem_cap_max()) return CFX_ERR_ARG;
             set_sweep_smem_cap(size_t(value));
             return CFX_OK;
+        case CFX_TUNE_GRID_WAVE:
+            if (value > 1) return CFX_ERR_ARG;
+            set_sweep_wave(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -1323,6 +1331,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_CLUSTER_SIZE: *value = sweep_cluster_size(); return CFX_OK;
         case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
         case CFX_TUNE_SMEM_BYTES: *value = int(sweep_smem_cap()); return CFX_OK;
+        case CFX_TUNE_GRID_WAVE: *value = sweep_wave(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

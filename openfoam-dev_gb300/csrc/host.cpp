@@ -344,6 +344,48 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o) {
     }
     o.levelSlot[nl] = int(o.cell.size());
     o.levelEntry[nl] = int(o.nb.size());
+    // group dependencies: the groups holding every (cell, sweep) a group's
+    // slots read (lower neighbours in the same sweep; for Gauss-Seidel the
+    // upper neighbours and the cell itself in the previous sweep)
+    std::vector<int> slotOf(size_t(n) * S, -1);
+    for (int L = 0; L < nl; ++L)
+        for (int i = start[L]; i < start[L + 1]; ++i) slotOf[order[i]] = o.levelSlot[L] + (i - start[L]);
+    const int nGroups = int(o.groupEntry.size()) - 1;
+    o.depStart.assign(1, 0);
+    o.dep.clear();
+    o.waveOk = true;
+    std::vector<int> ds;
+    int L = 0;  // level of group g (groups are in level order)
+    for (int g = 0; g < nGroups; ++g) {
+        ds.clear();
+        while (o.levelSlot[L + 1] <= g * 32) ++L;
+        for (int j = 0; j < 32; ++j) {
+            const int slot = g * 32 + j;
+            const int c = o.cell[slot];
+            if (c < 0) continue;
+            // the sweep of this slot: its index in the (sweep, cell) order
+            int sw = 0;
+            if (S > 1) {
+                sw = order[start[L] + (slot - o.levelSlot[L])] / n;
+                if (sw > 0) ds.push_back(slotOf[size_t(sw - 1) * n + c] / 32);
+            }
+            for (int k = 0; k < o.cnt[slot]; ++k) {
+                const int e = o.groupEntry[g] + 32 * k + j;
+                const int nb = o.nb[e];
+                const bool prev = kind == SCHED_GS && (o.src[e] & SRC_UPPER);
+                const int s2 = prev ? sw - 1 : sw;
+                if (s2 < 0) continue;
+                ds.push_back(slotOf[size_t(s2) * n + nb] / 32);
+            }
+        }
+        std::sort(ds.begin(), ds.end());
+        ds.erase(std::unique(ds.begin(), ds.end()), ds.end());
+        // every source lies on an earlier level, hence in an earlier group:
+        // the wavefront form's waits rely on it, so a violation disables it
+        if (!ds.empty() && ds.back() >= g) o.waveOk = false;
+        for (int d : ds) o.dep.push_back(d);
+        o.depStart.push_back(int(o.dep.size()));
+    }
 }
 
 }  // namespace cfx

@@ -160,6 +160,10 @@ struct HostSched {
     int64_t maxLevelBytes8 = 0;          // largest level's staged bytes (FP64)
     std::vector<int> levelSlot, levelEntry, groupEntry, cell, cnt, nb, src;
     std::vector<int> chunkGroup, chunkLevel, levelChunks;
+    // groups each group's slots read from (CSR, ascending): the wavefront
+    // form waits on exactly these
+    std::vector<int> depStart, dep;
+    bool waveOk = false;
 };
 
 struct DevSched {
@@ -170,6 +174,9 @@ struct DevSched {
     int *cell = nullptr, *cnt = nullptr, *nb = nullptr, *src = nullptr;
     int *chunkGroup = nullptr, *chunkLevel = nullptr, *levelChunks = nullptr;
     int* sync = nullptr;                 // [2 + nLevels]: abort, pad, done[level]
+    int *depStart = nullptr, *dep = nullptr;  // group dependencies (wavefront form)
+    int* gdone = nullptr;                // [nGroups] group finished flags
+    int waveOk = 0;                      // dependencies verified to point backwards
 };
 
 // coefficients packed for one schedule and one operation
@@ -209,6 +216,8 @@ int small_sweep_threshold();
 void set_small_sweep_threshold(int n);
 size_t sweep_smem_cap();
 size_t sweep_smem_cap_max();
+int sweep_wave();
+void set_sweep_wave(int on);
 void set_sweep_smem_cap(size_t b);
 int sweep_cluster_size();
 void set_sweep_cluster_size(int cs);

@@ -63,6 +63,8 @@ int g_cluster_avail = 0;    // largest cluster the GPU can hold (16 or 8; 0: non
 int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
 int g_cluster_global = 0;   // <= this many cells: one cluster with the vector in global memory
 int g_grid[2][8][3];        // resident CTAs of sweep_grid_k per (precision, op, PF 8/16/32)
+int g_wave_grid[2][8][3];   // resident CTAs of sweep_wave_k, the same
+int g_wave = 0;             // grid form: wavefront (1) or whole-level counters (0, default)
 size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
 
@@ -207,6 +209,94 @@ template <class T>
 __device__ __forceinline__ T* cl_ref(cg::cluster_group& cl, T* Xl, int per, int c) {
     const int o = c / per;
     return cl.map_shared_rank(Xl, o) + (c - o * per);
+}
+
+// Wavefront form (persistent, cooperative): warp-sized chunks.  Warp W of the
+// grid takes groups W, W + NW, ... in order; before computing a group it
+// waits only for the groups its slots read (the dependency lists built with
+// the schedule: lower neighbours in the same sweep, and for Gauss-Seidel the
+// upper neighbours and the cell itself in the previous sweep), each lane
+// polling one of them with an acquire load, then publishes its own flag with
+// a release store.  No block barrier, no whole-level counter: a group starts
+// as soon as its own inputs exist.  Groups only depend on groups of earlier
+// levels, which come earlier in every warp's order, and all warps are
+// resident (cooperative launch), so the waits always end; every wait is
+// bounded by SWEEP_TIMEOUT_NS on %globaltimer (abort flag + CFX_ERR_TIMEOUT,
+// then every warp returns).  The dot partial (when requested) is summed per
+// warp in its fixed group order, then per CTA: nPartials = gridDim.x.
+template <class T, int OP, int PF>
+__global__ void __launch_bounds__(GRID_NT) sweep_wave_k(DevSched s, SweepCtx<T> a, int* status) {
+    __shared__ double sh[GRID_NT / 32];
+    if (a.done && *a.done) return;
+    int* abortf = s.sync;
+    const int lane = threadIdx.x & 31;
+    const int W = blockIdx.x * (GRID_NT / 32) + (threadIdx.x >> 5);
+    const int NW = gridDim.x * (GRID_NT / 32);
+    double dot = 0.0;
+    bool ok = true;
+    for (int g = W; g < s.nGroups && ok; g += NW) {
+        const int slot = g * 32 + lane;
+        const int c = s.cell[slot];
+        const int n = s.cnt[slot];
+        const int e0 = s.groupEntry[g] + lane;
+        T sc = T(0), in = T(0);
+        int nbr[PF];
+        T cf[PF];
+        if (c >= 0) {
+            sc = a.scalar[slot];
+            if (OP == OP_FWD || OP == OP_GS) in = a.inS[slot];
+        }
+#pragma unroll
+        for (int k = 0; k < PF; ++k)
+            if (k < n) {
+                nbr[k] = s.nb[e0 + 32 * k];
+                cf[k] = a.coef[e0 + 32 * k];
+            }
+        // wait for the groups this one reads, each lane polling one of them
+        bool mine = true;
+        const int d1 = s.depStart[g + 1];
+        for (int k = s.depStart[g] + lane; k < d1 && mine; k += 32) {
+            const int* f = s.gdone + s.dep[k];
+            uint64_t t0 = 0;
+            unsigned spins = 0;
+            while (ld_acquire(f) == 0) {
+                if ((++spins & 63u) == 0) {
+                    if (*(volatile int*)abortf) {
+                        mine = false;
+                        break;
+                    }
+                    const uint64_t t = globaltimer_ns();
+                    if (t0 == 0) {
+                        t0 = t;
+                    } else if (t - t0 > SWEEP_TIMEOUT_NS) {
+                        atomicExch(abortf, 1);
+                        atomicExch(status, int(CFX_ERR_TIMEOUT));
+                        mine = false;
+                        break;
+                    }
+                }
+            }
+        }
+        ok = __all_sync(0xffffffffu, mine);
+        if (!ok) break;
+        T v = T(0);
+        if (c >= 0) {
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
+#pragma unroll
+            for (int k = 0; k < PF; ++k)
+                if (k < n) acc = sw_step<OP>(acc, cf[k], ldcg(a.x + nbr[k]));
+            acc = tail_entries<T, OP>(s, a.coef, e0, PF, n, acc, [&](int cc) { return ldcg(a.x + cc); });
+            v = sw_fini<OP>(acc, sc);
+            a.x[c] = v;
+            if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
+        }
+        __syncwarp();
+        if (lane == 0) st_release(s.gdone + g, 1);
+    }
+    if (a.dotWith) {
+        dot = block_sum<GRID_NT>(dot, sh);
+        if (threadIdx.x == 0) a.partials[blockIdx.x] = dot;
+    }
 }
 
 // Packed data of one group slot held in registers: the header (cell, entry
@@ -535,8 +625,37 @@ cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, i
     return CFX_OK;
 }
 
+// CTAs of a wavefront launch: the smallest residency over the operations
+// (so a schedule's dot-partial count does not depend on the operation), at
+// most one warp per group.
+int wave_ctas(int prec, int pf, int nGroups) {
+    int r = 1 << 30;
+    for (int op = 0; op < 4; ++op) r = std::min(r, g_wave_grid[prec][op][pf_index(pf)]);
+    const int need = (nGroups + GRID_NT / 32 - 1) / (GRID_NT / 32);
+    r = std::min(r, need);
+    return r > 0 ? r : 1;
+}
+
 template <class T, int OP, int PF>
 cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+    if (g_wave && s.waveOk) {
+        CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * 2, st));
+        CFX_CUDA(cudaMemsetAsync(s.gdone, 0, sizeof(int) * size_t(s.nGroups), st));
+        const int grid = wave_ctas(prec_index<T>(), PF, s.nGroups);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid > 0 ? grid : 1);
+        cfg.blockDim = dim3(GRID_NT);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_wave_k<T, OP, PF>, s, a, status));
+        count_launch();
+        return CFX_OK;
+    }
     {
         CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
         const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP][pf_index(PF)]);
@@ -570,6 +689,9 @@ void init_op_pf() {
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP, PF>, GRID_NT, 0);
     g_grid[prec_index<T>()][OP][pf_index(PF)] = g_num_sms * (per > 0 ? per : 1);
+    per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_wave_k<T, OP, PF>, GRID_NT, 0);
+    g_wave_grid[prec_index<T>()][OP][pf_index(PF)] = g_num_sms * (per > 0 ? per : 1);
     cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(g_smem_cap));
@@ -586,6 +708,9 @@ void init_op() {
         int per = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_grid_k<T, OP, XL>, GRID_NT, 0);
         g_grid[prec_index<T>()][OP][pf_index(XL)] = g_num_sms * (per > 0 ? per : 1);
+        per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_wave_k<T, OP, XL>, GRID_NT, 0);
+        g_wave_grid[prec_index<T>()][OP][pf_index(XL)] = g_num_sms * (per > 0 ? per : 1);
     }
 }
 
@@ -650,6 +775,16 @@ size_t sweep_smem_cap() { return g_smem_cap; }
 size_t sweep_smem_cap_max() { return g_smem_cap_max; }
 void set_sweep_smem_cap(size_t b) { g_smem_cap = b; }
 
+// CTAs of the wavefront launch for s (its dot partial count)
+template <class T>
+int wave_grid(const DevSched& s) {
+    const int pf = s.maxK <= PF_SMALL ? PF_SMALL : (sizeof(T) == 4 && s.maxK > PF_LARGE ? PF_GRID_XL : PF_LARGE);
+    return wave_ctas(prec_index<T>(), pf, s.nGroups);
+}
+
+int sweep_wave() { return g_wave; }
+void set_sweep_wave(int on) { g_wave = on ? 1 : 0; }
+
 template <class T>
 bool sweep_is_grid(const DevSched& s) {
     return mode_of<T>(s) == M_GRID;
@@ -658,7 +793,7 @@ bool sweep_is_grid(const DevSched& s) {
 template <class T>
 int sweep_partials(const DevSched& s) {
     const int m = mode_of<T>(s);
-    if (m == M_GRID) return s.nChunks;
+    if (m == M_GRID) return g_wave && s.waveOk ? wave_grid<T>(s) : s.nChunks;
     return (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) ? g_cluster : 1;
 }
 

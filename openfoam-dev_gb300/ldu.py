@@ -416,6 +416,7 @@ class SolverPerformance:
 
 
 TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS, TUNE_SMEM_BYTES = 0, 1, 2, 3, 4
+TUNE_GRID_WAVE = 5
 
 
 def tune_set(key, value):

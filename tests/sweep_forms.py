@@ -4,7 +4,9 @@ library's tuning knobs so every form is checked on small systems:
 * small   -- one CTA, vector in global memory
 * cta     -- one CTA, vector in shared memory (the default for small levels)
 * cluster -- a 16-CTA cluster, vector in distributed shared memory
-* grid    -- the persistent grid-wide level scheduler (vector in global memory)
+* grid    -- the persistent grid, wavefront: each 32-slot group waits for the
+             groups it reads (vector in global memory)
+* levels  -- the persistent grid with whole-level counters (the default grid form)
 """
 import contextlib
 
@@ -14,9 +16,11 @@ FORMS = {
     "small": {ldu.TUNE_SMALL_SWEEP: 1 << 30, ldu.TUNE_SMEM_BYTES: 0},
     "cta": {},
     "cluster": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 8192},
-    "grid": {ldu.TUNE_SMEM_BYTES: 0},
+    "grid": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 1},
+    "levels": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 0},
 }
-KNOBS = (ldu.TUNE_SMALL_SWEEP, ldu.TUNE_CLUSTER_GLOBAL, ldu.TUNE_CLUSTER_SIZE, ldu.TUNE_SMEM_BYTES)
+KNOBS = (ldu.TUNE_SMALL_SWEEP, ldu.TUNE_CLUSTER_GLOBAL, ldu.TUNE_CLUSTER_SIZE, ldu.TUNE_SMEM_BYTES,
+         ldu.TUNE_GRID_WAVE)
 
 
 @contextlib.contextmanager

@@ -379,7 +379,7 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     if (kind == SCHED_FWD) {
         if (!sc.hasFwd) {
             HostSched h;
-            build_sched(mesh->host[lv], SCHED_FWD, 1, h);
+            build_sched(mesh->host[lv], SCHED_FWD, 1, h, sweep_wave() != 0);
             sc.fwd = upload_sched(mesh->schedArena, s, h);
             sc.hasFwd = true;
         }
@@ -388,7 +388,7 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     if (kind == SCHED_BWD) {
         if (!sc.hasBwd) {
             HostSched h;
-            build_sched(mesh->host[lv], SCHED_BWD, 1, h);
+            build_sched(mesh->host[lv], SCHED_BWD, 1, h, sweep_wave() != 0);
             sc.bwd = upload_sched(mesh->schedArena, s, h);
             sc.hasBwd = true;
         }
@@ -397,7 +397,7 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     auto it = sc.gs.find(S);
     if (it == sc.gs.end()) {
         HostSched h;
-        build_sched(mesh->host[lv], SCHED_GS, S, h);
+        build_sched(mesh->host[lv], SCHED_GS, S, h, sweep_wave() != 0);
         it = sc.gs.emplace(S, upload_sched(mesh->schedArena, s, h)).first;
     }
     return it->second;

@@ -229,7 +229,7 @@ namespace cfx {
 // column-major (entry k of lane j at groupEntry[g] + 32*k + j) so a warp loads
 // them coalesced.  src encodes where each entry's coefficient comes from:
 // a losort slot k (lower side) or, with SRC_UPPER set, an owner face f.
-void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o) {
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps) {
     const int n = h.n;
     const int S = kind == SCHED_GS ? std::max(1, nSweeps) : 1;
     // level of every (cell, sweep)
@@ -344,9 +344,13 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o) {
     }
     o.levelSlot[nl] = int(o.cell.size());
     o.levelEntry[nl] = int(o.nb.size());
-    // group dependencies: the groups holding every (cell, sweep) a group's
+    // group dependencies (only for the wavefront form): the groups holding every (cell, sweep) a group's
     // slots read (lower neighbours in the same sweep; for Gauss-Seidel the
     // upper neighbours and the cell itself in the previous sweep)
+    o.depStart.clear();
+    o.dep.clear();
+    o.waveOk = false;
+    if (!withDeps) return;
     std::vector<int> slotOf(size_t(n) * S, -1);
     for (int L = 0; L < nl; ++L)
         for (int i = start[L]; i < start[L + 1]; ++i) slotOf[order[i]] = o.levelSlot[L] + (i - start[L]);

@@ -188,7 +188,8 @@ struct Packed {
     bool valid = false;
 };
 
-void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o);
+// withDeps: also the group dependency lists of the wavefront form
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps);
 
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {

@@ -295,6 +295,29 @@ def run_ours(args, rank, world, local, pg):
     # psi read+write, bPrime, upper once, upperAddr, ownerStart
     gs_bytes = 2 * (7 * 8 * N + 8 * F + 4 * F + 4 * N)
 
+    # the streaming kernels of the path (HBM-bound, no level chain), FP64 at
+    # the same size, each timed alone: Amul (3sN + sF + 8F), residual
+    # (4sN + sF + 8F), and a dot product (2sN)
+    d_y = torch.empty_like(d_src)
+
+    def ev_time(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            out.append((e0, e1))
+        torch.cuda.synchronize()
+        return statistics.median([a.elapsed_time(b) / 1e3 for a, b in out])
+
+    streaming = {
+        "amul": (ev_time(lambda: A.Amul(d_b, d_y)), 3 * 8 * N + 8 * F + 8 * F),
+        "residual": (ev_time(lambda: A.residual(d_b, d_src, d_y)), 4 * 8 * N + 8 * F + 8 * F),
+    }
+
     tm = reduce_max(pg, statistics.median(t_mixed))
     t64 = reduce_max(pg, statistics.median(t_fp64))
     te = reduce_max(pg, statistics.median(e2e))
@@ -325,6 +348,9 @@ def run_ours(args, rank, world, local, pg):
             "e2e": {"value": te, "unit": "s", "h2d_bytes_per_step": 8 * (N + F) + 16 * N,
                     "d2h_bytes_per_step": 8 * N},
             "gpu_launches": int(launches),
+            "streaming_kernels": {k: {"s": t, "algorithmic_bytes": b, "GB_s": b / t / 1e9,
+                                      "frac": b / t / 1e9 / float(peaks.get("hbm_gbs", 6800.0))}
+                                  for k, (t, b) in streaming.items()},
             "roofline": {"bound": "hbm", "kernel": "fused 2-sweep GaussSeidel, finest level (FP64)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes": gs_bytes, "launch_s": t_gs,

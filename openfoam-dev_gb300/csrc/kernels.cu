@@ -19,6 +19,14 @@ namespace cfx {
 
 namespace {
 
+// one element per thread (streaming kernels without block partials)
+inline int grid_all(int64_t n, int nt = RED_NT) {
+    int64_t b = (n + nt - 1) / nt;
+    if (b < 1) b = 1;
+    if (b > (int64_t(1) << 30)) b = int64_t(1) << 30;
+    return int(b);
+}
+
 inline int grid_for(int64_t n, int nt = RED_NT) {
     int64_t b = (n + nt - 1) / nt;
     if (b < 1) b = 1;
@@ -191,7 +199,7 @@ __global__ void __launch_bounds__(RED_NT) reduce_k(int n, const T* __restrict__ 
 
 template <class T>
 void Ops<T>::amul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
-    amul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+    amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                a.lowerPerm, a.upper, x, y);
     count_launch();
 }
@@ -199,7 +207,7 @@ void Ops<T>::amul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, c
 template <class T>
 void Ops<T>::tmul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
     // Tmul (lduMatrixATmul.C:95-151): y[u] += upper*x[l]; y[l] += lower*x[u]
-    amul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+    amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower, x, y);
     count_launch();
 }
@@ -207,7 +215,7 @@ void Ops<T>::tmul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, c
 template <class T>
 void Ops<T>::residual(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, const T* b,
                       T* r) {
-    residual_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+    residual_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                    a.lowerPerm, a.upper, x, b, r);
     count_launch();
 }

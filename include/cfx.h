@@ -321,6 +321,16 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* d_psi, const double* d_
 cfx_status cfx_reduce_noalloc(int which, int n, const double* d_a, const double* d_b, double* d_out,
                               void* stream);
 
+/* ---- diagnostics (no reference counterpart) -------------------------------
+ * Exercises the failure path of the bounded device waits without any fault:
+ * one Gauss-Seidel sweep of the matrix in the persistent grid form with the
+ * level-0 completion count started one short, so level 1 waits on a count
+ * nothing will reach.  Each wait gives up after timeoutMs (1..10000), the
+ * kernel raises its abort flag, every CTA returns, and *status receives the
+ * device status (CFX_ERR_TIMEOUT).  The context and the matrix stay usable;
+ * the matrix needs at least two forward levels. */
+cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1444,6 +1444,32 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
     });
 }
 
+cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status) {
+    if (!mat || !status || timeoutMs < 1 || timeoutMs > 10000) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        cudaStream_t s = ctx->stream;
+        const int n = mat->mesh->dev[0].n;
+        prepare_gs<double>(mat, 0, 1);
+        const DevSched& g = sched(mat->mesh, 0, SCHED_GS, 1);
+        Packed<double>& p = packed<double>(mat, 0, OP_GS, 1, g);
+        double* b = mat->w64.get(990, n);
+        double* x = mat->w64.get(991, n);
+        CK(cudaMemsetAsync(b, 0, sizeof(double) * n, s));
+        CK(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s));
+        const cfx_status st = run_sweep_stalled<double>(s, g, p, b, x, 1000000ull * unsigned(timeoutMs),
+                                                        ctx->d_status);
+        if (st != CFX_OK) return st;
+        CK(cudaStreamSynchronize(s));
+        *status = read_status(ctx);
+        // the context stays usable: clear the status for the next solve
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s));
+        CK(cudaStreamSynchronize(s));
+        return CFX_OK;
+    });
+}
+
 cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, int nSweeps) {
     if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
     if (kind != CFX_SMOOTH_GS && kind != CFX_SMOOTH_DIC) return CFX_ERR_CONFIG;

@@ -208,6 +208,10 @@ int sweep_partials(const DevSched& s);
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
                      const T* dotWith, double* partials, const int* done, int* status);
+// Failure-path exercise of the grid form's bounded waits (see sweeps.cu).
+template <class T>
+cfx_status run_sweep_stalled(cudaStream_t st, const DevSched& s, const Packed<T>& p, const T* in, T* x,
+                             unsigned long long timeoutNs, int* status);
 template <class T>
 void pack_sweep(cudaStream_t st, const DevSched& s, int op, const LevelCoeffs<T>& c, Packed<T>& p);
 

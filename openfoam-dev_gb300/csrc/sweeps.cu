@@ -78,6 +78,7 @@ struct SweepCtx {
     const T* dotWith;
     double* partials;
     const int* done;
+    unsigned long long timeoutNs;  // bound of every wait of the grid forms
 };
 
 template <int OP, class T>
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
                         const uint64_t t = globaltimer_ns();
                         if (t0 == 0) {
                             t0 = t;
-                        } else if (t - t0 > SWEEP_TIMEOUT_NS) {
+                        } else if (t - t0 > a.timeoutNs) {
                             atomicExch(abortf, 1);
                             atomicExch(status, int(CFX_ERR_TIMEOUT));
                             ok = 0;
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_wave_k(DevSched s, SweepCtx<T> 
                     const uint64_t t = globaltimer_ns();
                     if (t0 == 0) {
                         t0 = t;
-                    } else if (t - t0 > SWEEP_TIMEOUT_NS) {
+                    } else if (t - t0 > a.timeoutNs) {
                         atomicExch(abortf, 1);
                         atomicExch(status, int(CFX_ERR_TIMEOUT));
                         mine = false;
@@ -809,7 +810,7 @@ cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>
         gather_slots_k<T><<<blocks, 256, 0, st>>>(s.nSlots, s.cell, in, p.inS, done);
         count_launch();
     }
-    SweepCtx<T> a{p.coef, p.scalar, in, p.inS, x, dotWith, partials, done};
+    SweepCtx<T> a{p.coef, p.scalar, in, p.inS, x, dotWith, partials, done, SWEEP_TIMEOUT_NS};
     switch (op) {
         case OP_FWD: return launch<T, OP_FWD>(st, s, a, status);
         case OP_BWD: return launch<T, OP_BWD>(st, s, a, status);
@@ -817,6 +818,44 @@ cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>
         case OP_RD: return launch<T, OP_RD>(st, s, a, status);
         default: set_error("unknown sweep"); return CFX_ERR_ARG;
     }
+}
+
+// A Gauss-Seidel sweep in the level-counter grid form whose level-0
+// completion counter starts one short, so every chunk of level 1 waits on a
+// count that is never reached: each wait expires after timeoutNs, the kernel
+// sets the abort flag and CFX_ERR_TIMEOUT in *status, and every CTA returns.
+// Exercises the failure path of the bounded waits without any fault.
+template <class T>
+cfx_status run_sweep_stalled(cudaStream_t st, const DevSched& s, const Packed<T>& p, const T* in, T* x,
+                             unsigned long long timeoutNs, int* status) {
+    if (s.nLevels < 2 || s.nSlots == 0) {
+        set_error("stalled sweep: the schedule needs at least two levels");
+        return CFX_ERR_ARG;
+    }
+    int blocks = (s.nSlots + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    gather_slots_k<T><<<blocks, 256, 0, st>>>(s.nSlots, s.cell, in, p.inS, nullptr);
+    count_launch();
+    SweepCtx<T> a{p.coef, p.scalar, in, p.inS, x, nullptr, nullptr, nullptr, timeoutNs};
+    CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
+    CFX_CUDA(cudaMemsetAsync(s.sync + 2, 0xff, sizeof(int), st));  // done[0] = -1
+    auto go = [&](auto kern, int pf) -> cfx_status {
+        const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP_GS][pf_index(pf)]);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid > 0 ? grid : 1);
+        cfg.blockDim = dim3(GRID_NT);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, kern, s, a, status));
+        count_launch();
+        return CFX_OK;
+    };
+    if (s.maxK <= PF_SMALL) return go(sweep_grid_k<T, OP_GS, PF_SMALL>, PF_SMALL);
+    return go(sweep_grid_k<T, OP_GS, PF_LARGE>, PF_LARGE);
 }
 
 template <class T>
@@ -842,6 +881,8 @@ template cfx_status run_sweep<double>(cudaStream_t, const DevSched&, int, const 
                                       double*, const double*, double*, const int*, int*);
 template cfx_status run_sweep<float>(cudaStream_t, const DevSched&, int, const Packed<float>&, const float*, float*,
                                      const float*, double*, const int*, int*);
+template cfx_status run_sweep_stalled<double>(cudaStream_t, const DevSched&, const Packed<double>&,
+                                               const double*, double*, unsigned long long, int*);
 template void pack_sweep<double>(cudaStream_t, const DevSched&, int, const LevelCoeffs<double>&, Packed<double>&);
 template void pack_sweep<float>(cudaStream_t, const DevSched&, int, const LevelCoeffs<float>&, Packed<float>&);
 

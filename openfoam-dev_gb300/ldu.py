@@ -124,6 +124,7 @@ _SIG = {
     "cfx_precondition": (_i, [_vp, _i, _i, _vp, _vp]),
     "cfx_reciprocal_d": (_i, [_vp, _i, _vp]),
     "cfx_smooth": (_i, [_vp, _i, _vp, _vp, _i]),
+    "cfx_diag_sweep_stall": (_i, [_vp, _i, ctypes.POINTER(_i)]),
     "cfx_reduce_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
     "cfx_batch_create": (_i, [_vp, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "cfx_batch_destroy": (_i, [_vp]),
@@ -376,6 +377,12 @@ class LduMatrix:
 
     def smooth(self, kind, psi, b, nSweeps):
         _check(lib().cfx_smooth(self.h, SMOOTHERS[kind], _dp(psi), _dp(b), int(nSweeps)), "smooth")
+
+    def diag_sweep_stall(self, timeout_ms):
+        """Device status of a sweep whose bounded waits are made to expire."""
+        st = ctypes.c_int()
+        _check(lib().cfx_diag_sweep_stall(self.h, int(timeout_ms), ctypes.byref(st)), "cfx_diag_sweep_stall")
+        return st.value
 
     def coarse(self, level, nCells, nFaces):
         d = np.empty(nCells)

@@ -277,6 +277,100 @@ void ldu_dic_smooth(const ldu_matrix* m, const double* rD, double* psi, const do
     free(rA);
 }
 
+/* symGaussSeidelSmoother::smooth, symGaussSeidelSmoother.C:66-204 (no
+ * interfaces): per sweep bPrime = source, a forward pass as GaussSeidel, then
+ * a backward pass over the cells in reverse order that starts from the bPrime
+ * the forward pass left (the lower contributions of the forward values). */
+void ldu_symgs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweeps) {
+    const int n = m->nCells;
+    const double* lo = lowerOf(m);
+    double* bPrime = (double*)xmalloc(sizeof(double) * n);
+    for (int sweep = 0; sweep < nSweeps; ++sweep) {
+        memcpy(bPrime, b, sizeof(double) * n);
+        int fEnd = m->ownerStart[0];
+        for (int c = 0; c < n; ++c) {
+            const int fStart = fEnd;
+            fEnd = m->ownerStart[c + 1];
+            double psii = bPrime[c];
+            for (int f = fStart; f < fEnd; ++f) psii -= m->upper[f] * psi[m->u[f]];
+            psii /= m->diag[c];
+            for (int f = fStart; f < fEnd; ++f) bPrime[m->u[f]] -= lo[f] * psii;
+            psi[c] = psii;
+        }
+        int fStart = m->ownerStart[n];
+        for (int c = n - 1; c >= 0; --c) {
+            const int fE = fStart;
+            fStart = m->ownerStart[c];
+            double psii = bPrime[c];
+            for (int f = fStart; f < fE; ++f) psii -= m->upper[f] * psi[m->u[f]];
+            psii /= m->diag[c];
+            for (int f = fStart; f < fE; ++f) bPrime[m->u[f]] -= lo[f] * psii;
+            psi[c] = psii;
+        }
+    }
+    free(bPrime);
+}
+
+/* DILUSmoother::smooth, DILUSmoother.C:67-118 */
+void ldu_dilu_smooth(const ldu_matrix* m, const double* rD, double* psi, const double* b, int nSweeps) {
+    const int n = m->nCells;
+    const double* lo = lowerOf(m);
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    for (int sweep = 0; sweep < nSweeps; ++sweep) {
+        ldu_residual(m, psi, b, rA);
+        for (int c = 0; c < n; ++c) rA[c] *= rD[c];
+        for (int f = 0; f < m->nFaces; ++f) {
+            const int u = m->u[f];
+            rA[u] -= rD[u] * lo[f] * rA[m->l[f]];
+        }
+        for (int f = m->nFaces - 1; f >= 0; --f) {
+            const int l = m->l[f];
+            rA[l] -= rD[l] * m->upper[f] * rA[m->u[f]];
+        }
+        for (int c = 0; c < n; ++c) psi[c] += rA[c];
+    }
+    free(rA);
+}
+
+/* lduMatrix::smoother by name: GaussSeidel, symGaussSeidel, DIC (symmetric),
+ * DILU (asymmetric), DICGaussSeidel and DILUGaussSeidel
+ * (DICGaussSeidelSmoother.C:79-92, DILUGaussSeidelSmoother.C:79-92: the
+ * incomplete-factorisation smoother's sweeps, then Gauss-Seidel's).  rD: the
+ * DIC/DILU reciprocal diagonal (unused otherwise). */
+static void smoother_apply(const ldu_matrix* m, int smoother, const double* rD, double* psi, const double* b,
+                           int nSweeps) {
+    switch (smoother) {
+        case LDU_SMOOTH_GS: ldu_gs_smooth(m, psi, b, nSweeps); break;
+        case LDU_SMOOTH_SYMGS: ldu_symgs_smooth(m, psi, b, nSweeps); break;
+        case LDU_SMOOTH_DIC: ldu_dic_smooth(m, rD, psi, b, nSweeps); break;
+        case LDU_SMOOTH_DILU: ldu_dilu_smooth(m, rD, psi, b, nSweeps); break;
+        case LDU_SMOOTH_DICGS:
+            ldu_dic_smooth(m, rD, psi, b, nSweeps);
+            ldu_gs_smooth(m, psi, b, nSweeps);
+            break;
+        default:
+            ldu_dilu_smooth(m, rD, psi, b, nSweeps);
+            ldu_gs_smooth(m, psi, b, nSweeps);
+            break;
+    }
+}
+
+static double* smoother_rD(const ldu_matrix* m, int smoother) {
+    if (smoother == LDU_SMOOTH_GS || smoother == LDU_SMOOTH_SYMGS) return NULL;
+    double* rD = (double*)xmalloc(sizeof(double) * m->nCells);
+    if (smoother == LDU_SMOOTH_DIC || smoother == LDU_SMOOTH_DICGS)
+        ldu_dic_rD(m, rD);
+    else
+        ldu_dilu_rD(m, rD);
+    return rD;
+}
+
+void ldu_smooth(const ldu_matrix* m, int smoother, double* psi, const double* b, int nSweeps) {
+    double* rD = smoother_rD(m, smoother);
+    smoother_apply(m, smoother, rD, psi, b, nSweeps);
+    free(rD);
+}
+
 /* ----------------------------------------------------------------- solvers */
 
 /* SolverPerformance::checkConvergence, SolverPerformance.C:60-92 */
@@ -403,6 +497,40 @@ int ldu_pbicgstab(const ldu_matrix* m, double* psi, const double* b, const ldu_c
     free(pA);
     free(yA);
     free(rA);
+    return 0;
+}
+
+/* smoothSolver::solve, smoothSolver.C:77-196.  nSweeps < 0: that many sweeps,
+ * no residuals, nIterations = -nSweeps. */
+int ldu_smooth_solve(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c, int smoother,
+                     int nSweeps, ldu_perf* perf) {
+    const int n = m->nCells;
+    memset(perf, 0, sizeof(*perf));
+    if (nSweeps < 0) {
+        ldu_smooth(m, smoother, psi, b, -nSweeps);
+        perf->nIterations -= nSweeps;
+        return 0;
+    }
+    double* Apsi = (double*)xmalloc(sizeof(double) * n);
+    double* tmp = (double*)xmalloc(sizeof(double) * n);
+    ldu_amul(m, psi, Apsi);
+    const double normFactor = ldu_norm_factor(m, psi, b, Apsi, tmp);
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += fabs(b[i] - Apsi[i]);
+    perf->initialResidual = s / normFactor;
+    perf->finalResidual = perf->initialResidual;
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        double* rD = smoother_rD(m, smoother);
+        do {
+            smoother_apply(m, smoother, rD, psi, b, nSweeps);
+            ldu_residual(m, psi, b, tmp);
+            perf->finalResidual = ldu_sum_mag(n, tmp) / normFactor;
+        } while (((perf->nIterations += nSweeps) < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        free(rD);
+    }
+    free(Apsi);
+    free(tmp);
     return 0;
 }
 

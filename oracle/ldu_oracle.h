@@ -72,6 +72,14 @@ void ldu_dilu_preconditionT(const ldu_matrix* m, const double* rD, const double*
 enum { LDU_SMOOTH_GS = 0, LDU_SMOOTH_DIC = 1 };
 void ldu_gs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweeps);
 void ldu_dic_smooth(const ldu_matrix* m, const double* rD, double* psi, const double* b, int nSweeps);
+void ldu_symgs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweeps);
+void ldu_dilu_smooth(const ldu_matrix* m, const double* rD, double* psi, const double* b, int nSweeps);
+/* smoothers beyond GaussSeidel and DIC (the values above) */
+enum { LDU_SMOOTH_SYMGS = 2, LDU_SMOOTH_DILU = 3, LDU_SMOOTH_DICGS = 4, LDU_SMOOTH_DILUGS = 5 };
+/* the named smoother, nSweeps sweeps (DIC/DILU pivots computed inside) */
+void ldu_smooth(const ldu_matrix* m, int smoother, double* psi, const double* b, int nSweeps);
+int ldu_smooth_solve(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c, int smoother,
+                     int nSweeps, ldu_perf* perf);
 
 /* PCG.C:65-193, PBiCGStab.C:68-254.  Return 0 or a negative error. */
 int ldu_pcg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,

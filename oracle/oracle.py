@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libldu_oracle.so")
 
 PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
-SMOOTHERS = {"GaussSeidel": 0, "DIC": 1}
+SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "symGaussSeidel": 2, "DILU": 3, "DICGaussSeidel": 4,
+             "DILUGaussSeidel": 5}
 
 i32p = ctypes.POINTER(ctypes.c_int)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -164,6 +165,14 @@ class Matrix:
         lib().ldu_dic_smooth(ctypes.byref(self.c), _p(rD), _p(psi), _p(b), n_sweeps)
         return psi
 
+    def smooth(self, smoother, psi, b, n_sweeps):
+        """lduMatrix::smoother by name (GaussSeidel, symGaussSeidel, DIC, DILU,
+        DICGaussSeidel, DILUGaussSeidel), n_sweeps sweeps."""
+        psi = np.ascontiguousarray(psi, np.float64).copy()
+        b = np.ascontiguousarray(b, np.float64)
+        lib().ldu_smooth(ctypes.byref(self.c), SMOOTHERS[smoother], _p(psi), _p(b), int(n_sweeps))
+        return psi
+
 
 def _perf(p):
     return Perf(p.initialResidual, p.finalResidual, p.nIterations, bool(p.converged), bool(p.singular))
@@ -181,6 +190,17 @@ def pcg(s, psi, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, precond="DIC")
     c = _controls(tol, rel_tol, max_iter, min_iter)
     lib().ldu_pcg(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c),
                   PRECONDITIONERS[precond], ctypes.byref(perf))
+    return _perf(perf)
+
+
+def smooth_solve(s, psi, smoother="GaussSeidel", n_sweeps=1, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0):
+    """smoothSolver::solve (smoothSolver.C:77-196); psi is updated in place."""
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    lib().ldu_smooth_solve(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c), SMOOTHERS[smoother],
+                           int(n_sweeps), ctypes.byref(perf))
     return _perf(perf)
 
 

@@ -364,6 +364,31 @@ int runOps(const RecMap& in, Writer& out, Time& runTime)
         out.f8("GS_smooth3", psi);
     }
 
+    // the other smoothers of the run-time table, 2 sweeps from x
+    {
+        std::vector<std::string> names;
+        names.push_back("symGaussSeidel");
+        if (A.symmetric())
+        {
+            names.push_back("DICGaussSeidel");
+        }
+        else
+        {
+            names.push_back("DILU");
+            names.push_back("DILUGaussSeidel");
+        }
+        for (const std::string& nm : names)
+        {
+            IStringStream is("{ smoother " + nm + "; }");
+            dictionary d(is);
+            autoPtr<lduMatrix::smoother> sm =
+                lduMatrix::smoother::New("x", A, bou, intc, ifs, d);
+            scalarField psi(x);
+            sm->smooth(psi, b, 0, 2);
+            out.f8(nm + "_smooth2", psi);
+        }
+    }
+
     out.i4("ownerStart", mesh.lduAddr().ownerStartAddr());
     out.i4("losort", mesh.lduAddr().losortAddr());
     out.i4("losortStart", mesh.lduAddr().losortStartAddr());

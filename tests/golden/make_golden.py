@@ -8,9 +8,11 @@ harness).  Every fixture is produced by the reference's own code:
                jittered hex box (primitiveMesh geometry)
 * ops_*.npz    lduMatrix::Amul/Tmul/residual/sumA, normFactor, gSum*, the
                DIC/DILU reciprocal diagonals and preconditioners, the
-               GaussSeidel and DIC smoothers, lduAddressing losort/ownerStart
-* solve_*.npz  lduMatrix::solver::New(...)->solve for PCG, PBiCGStab and GAMG
-               (with the agglomeration levels and coarse matrices)
+               GaussSeidel, symGaussSeidel, DIC, DILU, DICGaussSeidel and
+               DILUGaussSeidel smoothers, lduAddressing losort/ownerStart
+* solve_*.npz  lduMatrix::solver::New(...)->solve for PCG, PBiCGStab, GAMG
+               (with the agglomeration levels and coarse matrices) and
+               smoothSolver with each smoother of the run-time table
 
 Inputs are regenerated by the tests from the stored case parameters with
 openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
@@ -64,6 +66,24 @@ SOLVES = {
     "gamg_dic": ("jcube14", dict(solver="GAMG", smoother="DIC", tolerance=1e-8, relTol=0.0)),
     "gamg_box": ("box", dict(solver="GAMG", smoother="GaussSeidel", nPreSweeps=1, tolerance=1e-9, relTol=0.0,
                              nCellsInCoarsestLevel=4)),
+    "smooth_gs": ("cube12", dict(solver="smoothSolver", smoother="GaussSeidel", tolerance=1e-6, relTol=0.0,
+                                 maxIter=5000)),
+    "smooth_symgs": ("jcube14", dict(solver="smoothSolver", smoother="symGaussSeidel", nSweeps=2,
+                                     tolerance=1e-7, relTol=0.0, maxIter=5000)),
+    "smooth_dic": ("cube12", dict(solver="smoothSolver", smoother="DIC", tolerance=1e-7, relTol=0.0,
+                                  maxIter=5000)),
+    "smooth_dicgs": ("jcube14", dict(solver="smoothSolver", smoother="DICGaussSeidel", tolerance=1e-7,
+                                     relTol=0.0, maxIter=5000)),
+    "smooth_dilu": ("cd10", dict(solver="smoothSolver", smoother="DILU", tolerance=1e-9, relTol=0.0)),
+    "smooth_dilugs": ("cd10", dict(solver="smoothSolver", smoother="DILUGaussSeidel", nSweeps=2, tolerance=1e-9,
+                                   relTol=0.0)),
+    "smooth_symgs_asym": ("cd10", dict(solver="smoothSolver", smoother="symGaussSeidel", tolerance=1e-9,
+                                       relTol=0.0)),
+    "smooth_fixed": ("box", dict(solver="smoothSolver", smoother="symGaussSeidel", nSweeps=-5)),
+    "smooth_maxiter": ("box", dict(solver="smoothSolver", smoother="GaussSeidel", nSweeps=3, tolerance=1e-12,
+                                   relTol=0.0, maxIter=7)),
+    "smooth_reltol": ("jcube14", dict(solver="smoothSolver", smoother="DICGaussSeidel", tolerance=0.0,
+                                      relTol=1e-2)),
 }
 
 

@@ -58,6 +58,10 @@ def test_single_operations(name):
         np.testing.assert_array_equal(m.dilu_preconditionT(b), g["DILU_preconditionT"])
     np.testing.assert_array_equal(m.gs_smooth(x, b, 1), g["GS_smooth1"])
     np.testing.assert_array_equal(m.gs_smooth(x, b, 3), g["GS_smooth3"])
+    others = ("symGaussSeidel", "DICGaussSeidel") if s.get("lower") is None else \
+        ("symGaussSeidel", "DILU", "DILUGaussSeidel")
+    for sm in others:
+        np.testing.assert_array_equal(m.smooth(sm, x, b, 2), g[f"{sm}_smooth2"], err_msg=sm)
 
 
 def _run_oracle(s, ctl):
@@ -68,6 +72,8 @@ def _run_oracle(s, ctl):
         p = orc.pcg(s, psi, precond=ctl["preconditioner"], **kw)
     elif ctl["solver"] == "PBiCGStab":
         p = orc.pbicgstab(s, psi, precond=ctl["preconditioner"], **kw)
+    elif ctl["solver"] == "smoothSolver":
+        p = orc.smooth_solve(s, psi, ctl["smoother"], ctl.get("nSweeps", 1), **kw)
     else:
         p = orc.gamg(s, psi, **kw, **gamg_kwargs(ctl))
     return psi, p

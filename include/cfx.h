@@ -58,9 +58,14 @@ typedef struct {
     int pad;
 } cfx_perf;
 
-enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2 };
+/* CFX_SOLVER_SMOOTH: smoothSolver (smoothSolver.C:77-196) */
+enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2, CFX_SOLVER_SMOOTH = 3 };
 enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3 };
-enum { CFX_SMOOTH_GS = 0, CFX_SMOOTH_DIC = 1 };
+/* lduMatrix::smoother run-time table (GAMG's smoother, smoothSolver's):
+ * GaussSeidel, DIC (symmetric), symGaussSeidel, DILU (asymmetric),
+ * DICGaussSeidel (symmetric), DILUGaussSeidel (asymmetric) */
+enum { CFX_SMOOTH_GS = 0, CFX_SMOOTH_DIC = 1, CFX_SMOOTH_SYMGS = 2, CFX_SMOOTH_DILU = 3, CFX_SMOOTH_DICGS = 4,
+       CFX_SMOOTH_DILUGS = 5 };
 enum { CFX_FP64 = 0, CFX_MIXED = 1 };
 
 /* Solver controls: lduMatrix::solver::readControls (lduMatrixSolver.C:158-164)
@@ -73,7 +78,7 @@ typedef struct {
     int maxIter;           /* default 1000 */
     int minIter;           /* default 0 */
     /* GAMG */
-    int smoother;          /* CFX_SMOOTH_* (default GaussSeidel) */
+    int smoother;          /* CFX_SMOOTH_* (default GaussSeidel; GAMG and smoothSolver) */
     int nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps;       /* 0, 1, 4 */
     int nPostSweeps, postSweepsLevelMultiplier, maxPostSweeps;    /* 2, 1, 4 */
     int nFinestSweeps;     /* 2 */
@@ -83,7 +88,9 @@ typedef struct {
      * iterative-refinement loop (outer residual, solution, normFactor and
      * convergence in FP64) */
     int precision;
-    int pad;
+    /* smoothSolver: sweeps between residual checks (default 1; negative: that
+     * many sweeps and no residuals, smoothSolver.C:93-116) */
+    int nSweeps;
 } cfx_controls;
 
 void cfx_default_controls(cfx_controls* c);

@@ -394,10 +394,15 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
         }
         return sc.bwd;
     }
+    // Gauss-Seidel schedules by sweep count; key -1 = the backward pass
+    if (kind == SCHED_GSB) S = -1;
     auto it = sc.gs.find(S);
     if (it == sc.gs.end()) {
         HostSched h;
-        build_sched(mesh->host[lv], SCHED_GS, S, h, sweep_wave() != 0);
+        if (S < 0)
+            build_sched(mesh->host[lv], SCHED_GSB, 1, h, sweep_wave() != 0);
+        else
+            build_sched(mesh->host[lv], SCHED_GS, S, h, sweep_wave() != 0);
         it = sc.gs.emplace(S, upload_sched(mesh->schedArena, s, h)).first;
     }
     return it->second;
@@ -604,6 +609,27 @@ void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b,
     const LevelMesh& m = mat->mesh->dev[lv];
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     cudaStream_t s = ctx->stream;
+    if (kind == CFX_SMOOTH_DICGS || kind == CFX_SMOOTH_DILUGS) {
+        // DICGaussSeidelSmoother.C:79-92, DILUGaussSeidelSmoother.C:79-92
+        smooth<T>(ctx, mat, lv, kind == CFX_SMOOTH_DICGS ? CFX_SMOOTH_DIC : CFX_SMOOTH_DILU, psi, b, nSweeps, LW);
+        smooth<T>(ctx, mat, lv, CFX_SMOOTH_GS, psi, b, nSweeps, LW);
+        return;
+    }
+    if (kind == CFX_SMOOTH_SYMGS) {
+        // symGaussSeidelSmoother.C:130-199: a forward pass, then a backward
+        // pass over the reverse order starting from the forward bPrime, which
+        // is the same per-cell formula on the upper-neighbour DAG
+        const DevSched& f = sched(mat->mesh, lv, SCHED_GS, 1);
+        const DevSched& g = sched(mat->mesh, lv, SCHED_GSB, 1);
+        for (int k = 0; k < nSweeps; ++k) {
+            if (run_sweep<T>(s, f, OP_GS, packed<T>(mat, lv, OP_GS, 1, f), b, psi, nullptr, nullptr, nullptr,
+                             ctx->d_status) != CFX_OK ||
+                run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, -1, g), b, psi, nullptr, nullptr, nullptr,
+                             ctx->d_status) != CFX_OK)
+                throw CudaError(last_error());
+        }
+        return;
+    }
     if (kind == CFX_SMOOTH_GS) {
         // GaussSeidelSmoother.C:125-177
         for (int left = nSweeps; left > 0;) {
@@ -617,11 +643,12 @@ void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b,
         return;
     }
     for (int k = 0; k < nSweeps; ++k) {
-        // DICSmoother.C:86-115: rA = b - A psi; rA = M^-1 rA; psi += rA
+        // DICSmoother.C:86-115, DILUSmoother.C:86-117: rA = b - A psi;
+        // rA = M^-1 rA; psi += rA
         T* rA = LW.get(0, m.n);
         T* wA = LW.get(1, m.n);
         Ops<T>::residual(s, m, c, psi, b, rA);
-        precondition<T>(mat, lv, CFX_PRE_DIC, rA, wA, nullptr, false);
+        precondition<T>(mat, lv, kind == CFX_SMOOTH_DILU ? CFX_PRE_DILU : CFX_PRE_DIC, rA, wA, nullptr, false);
         Kern<T>::axpy(s, m.n, T(1), wA, psi, nullptr);
     }
 }
@@ -629,6 +656,18 @@ void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b,
 // Set up what smooth() needs on level lv for nSweeps (outside graph capture).
 template <class T>
 void prepare_smooth(cfx_matrix* mat, int lv, int kind, int nSweeps, Work<T>& LW) {
+    if (kind == CFX_SMOOTH_DICGS || kind == CFX_SMOOTH_DILUGS) {
+        prepare_smooth<T>(mat, lv, kind == CFX_SMOOTH_DICGS ? CFX_SMOOTH_DIC : CFX_SMOOTH_DILU, nSweeps, LW);
+        prepare_smooth<T>(mat, lv, CFX_SMOOTH_GS, nSweeps, LW);
+        return;
+    }
+    if (kind == CFX_SMOOTH_SYMGS) {
+        prepare_gs<T>(mat, lv, 1);
+        const DevSched& g = sched(mat->mesh, lv, SCHED_GSB, 1);
+        Packed<T>& p = packed<T>(mat, lv, OP_GS, -1, g);
+        if (!p.valid) pack_sweep<T>(mat->mesh->ctx->stream, g, OP_GS, coeffs<T>(mat, lv), p);
+        return;
+    }
     if (kind == CFX_SMOOTH_GS) {
         for (int left = nSweeps; left > 0;) {
             const int S = std::min(left, MAX_FUSED_SWEEPS);
@@ -764,7 +803,9 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     // smoothers are constructed per solve, so DIC rD is recomputed)
     // sweep counts used on each level (Vcycle, GAMGSolverSolve.C:179-390)
     for (int lv = 0; lv < nl - 1; ++lv) {
-        if (ctl->smoother == CFX_SMOOTH_DIC) compute_rD<T>(mat, lv);
+        if (ctl->smoother == CFX_SMOOTH_DIC || ctl->smoother == CFX_SMOOTH_DILU || ctl->smoother == CFX_SMOOTH_DICGS ||
+            ctl->smoother == CFX_SMOOTH_DILUGS)
+            compute_rD<T>(mat, lv);  // DIC pivots when symmetric, DILU otherwise
         if (lv == 0) {
             prepare_smooth<T>(mat, 0, ctl->smoother, ctl->nFinestSweeps, cy.workFor(0));
             continue;
@@ -968,13 +1009,73 @@ cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, c
     return CFX_OK;
 }
 
+// smoothSolver::solve (smoothSolver.C:77-196) in FP64: normFactor and the
+// initial residual |source - A psi|, then sweeps of the smoother with the
+// residual (lduMatrix::residual) checked every nSweeps; nIterations counts
+// sweeps.  The scalar loop test runs on the device (gamg_residual_check with
+// an increment of nSweeps); the host reads the state once per check.
+cfx_status smooth_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, const double* b, cfx_perf* perf) {
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const LevelMesh& m = mat->mesh->dev[0];
+    LevelCoeffs<double>& c = mat->c64[0];
+    const int n = m.n;
+    if ((int)mat->lv64.size() < 1) mat->lv64.resize(1);
+    Work<double>& LW = mat->lv64[0];
+    std::snprintf(perf->solverName, sizeof(perf->solverName), "smoothSolver");
+    const bool fact = ctl.smoother != CFX_SMOOTH_GS && ctl.smoother != CFX_SMOOTH_SYMGS;
+    if (ctl.nSweeps < 0) {
+        if (fact) compute_rD<double>(mat, 0);
+        prepare_smooth<double>(mat, 0, ctl.smoother, -ctl.nSweeps, LW);
+        smooth<double>(ctx, mat, 0, ctl.smoother, psi, b, -ctl.nSweeps, LW);
+        CK(cudaStreamSynchronize(s));
+        const int stc = read_status(ctx);
+        if (stc) return cfx_status(stc);
+        perf->nIterations = -ctl.nSweeps;
+        return CFX_OK;
+    }
+    const int slot = 0;
+    set_state(ctx, slot, ctl, ctl.tolerance, ctl.relTol, ctl.maxIter, ctl.minIter);
+    SolveState* st = ctx->d_state + slot;
+    double* Apsi = mat->w64.get(0, n);
+    double* r = mat->w64.get(1, n);
+    launch_reduce<double>(s, ctx->sc, 0, n, psi, nullptr, &st->red0);
+    count_launch();
+    Ops<double>::amul(s, m, c, psi, Apsi);
+    Kern<double>::norm_init(s, ctx->sc, m, c, Apsi, b, r, nullptr, st);
+    SolveState h = read_state(ctx, slot);
+    if (!h.done) {
+        if (fact) compute_rD<double>(mat, 0);
+        const int ns = std::max(ctl.nSweeps, 1);
+        prepare_smooth<double>(mat, 0, ctl.smoother, ns, LW);
+        int checks = 0;
+        while (!h.done) {
+            smooth<double>(ctx, mat, 0, ctl.smoother, psi, b, ns, LW);
+            Kern<double>::gamg_residual_check(s, ctx->sc, m, c, psi, b, r, st, ns);
+            h = read_state(ctx, slot);
+            const int stc = read_status(ctx);
+            if (stc) return cfx_status(stc);
+            if (++checks > ctl.maxIter + ctl.minIter + 16) {
+                set_error("smoothing loop did not terminate");
+                return CFX_ERR_STATE;
+            }
+        }
+    }
+    perf->initialResidual = h.initialResidual;
+    perf->finalResidual = h.finalResidual;
+    perf->nIterations = h.nIterations;
+    perf->converged = h.converged;
+    perf->singular = 0;
+    return CFX_OK;
+}
+
 cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
     if (!c) {
         set_error("null controls");
         return CFX_ERR_ARG;
     }
-    if (c->solver < 0 || c->solver > 2 || c->preconditioner < 0 || c->preconditioner > 3 || c->smoother < 0 ||
-        c->smoother > 1 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
+    if (c->solver < 0 || c->solver > 3 || c->preconditioner < 0 || c->preconditioner > 3 || c->smoother < 0 ||
+        c->smoother > 5 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
         set_error("unknown solver, preconditioner, smoother or precision");
         return CFX_ERR_CONFIG;
     }
@@ -984,7 +1085,22 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("Unknown asymmetric matrix solver cudaPCG");
         return CFX_ERR_CONFIG;
     }
-    if (c->solver != CFX_SOLVER_GAMG) {
+    if (c->solver == CFX_SOLVER_SMOOTH && c->precision == CFX_MIXED) {
+        set_error("precision mixed is not available for cudaSmoothSolver");
+        return CFX_ERR_CONFIG;
+    }
+    if (c->solver == CFX_SOLVER_GAMG || c->solver == CFX_SOLVER_SMOOTH) {
+        // smoother tables (the smoothers' *ConstructorToTable registrations)
+        const bool symOnly = c->smoother == CFX_SMOOTH_DIC || c->smoother == CFX_SMOOTH_DICGS;
+        const bool asymOnly = c->smoother == CFX_SMOOTH_DILU || c->smoother == CFX_SMOOTH_DILUGS;
+        static const char* names[] = {"GaussSeidel", "DIC", "symGaussSeidel", "DILU", "DICGaussSeidel",
+                                      "DILUGaussSeidel"};
+        if ((symOnly && !mat->sym) || (asymOnly && mat->sym)) {
+            set_error(std::string("Unknown ") + (mat->sym ? "symmetric" : "asymmetric") + " matrix smoother " +
+                      names[c->smoother]);
+            return CFX_ERR_CONFIG;
+        }
+    } else {
         if (c->preconditioner == CFX_PRE_DIC && !mat->sym) {
             set_error("Unknown asymmetric matrix preconditioner DIC");
             return CFX_ERR_CONFIG;
@@ -993,9 +1109,6 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
             set_error("Unknown symmetric matrix preconditioner DILU");
             return CFX_ERR_CONFIG;
         }
-    } else if (c->smoother == CFX_SMOOTH_DIC && !mat->sym) {
-        set_error("Unknown asymmetric matrix smoother DIC");
-        return CFX_ERR_CONFIG;
     }
     return CFX_OK;
 }
@@ -1025,6 +1138,7 @@ void cfx_default_controls(cfx_controls* c) {
     c->scaleCorrection = -1;
     c->nCellsInCoarsestLevel = 10;
     c->precision = CFX_FP64;
+    c->nSweeps = 1;
 }
 
 const char* cfx_last_error(void) { return cfx::last_error(); }
@@ -1273,6 +1387,7 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
     const cfx_status st = guard([&]() -> cfx_status {
         CK(cudaMemsetAsync(mat->mesh->ctx->d_status, 0, sizeof(int), mat->mesh->ctx->stream));
         if (ctl->solver == CFX_SOLVER_GAMG) return gamg_solve(mat, *ctl, d_psi, d_source, perf);
+        if (ctl->solver == CFX_SOLVER_SMOOTH) return smooth_solve(mat, *ctl, d_psi, d_source, perf);
         return krylov_solve(mat, *ctl, d_psi, d_source, perf);
     });
     perf->status = st;
@@ -1472,13 +1587,15 @@ cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status) {
 
 cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, int nSweeps) {
     if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
-    if (kind != CFX_SMOOTH_GS && kind != CFX_SMOOTH_DIC) return CFX_ERR_CONFIG;
-    if (kind == CFX_SMOOTH_DIC && !mat->sym) return CFX_ERR_CONFIG;
+    if (kind < CFX_SMOOTH_GS || kind > CFX_SMOOTH_DILUGS) return CFX_ERR_CONFIG;
+    if ((kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) && !mat->sym) return CFX_ERR_CONFIG;
+    if ((kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) && mat->sym) return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
         if ((int)mat->lv64.size() < 1) mat->lv64.resize(1);
-        if (kind == CFX_SMOOTH_DIC) setup_preconditioner<double>(mat, 0, CFX_PRE_DIC);
+        if (kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) setup_preconditioner<double>(mat, 0, CFX_PRE_DIC);
+        if (kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) setup_preconditioner<double>(mat, 0, CFX_PRE_DILU);
         prepare_smooth<double>(mat, 0, kind, nSweeps, mat->lv64[0]);
         smooth<double>(ctx, mat, 0, kind, psi, b, nSweeps, mat->lv64[0]);
         CK(cudaStreamSynchronize(ctx->stream));

@@ -234,7 +234,7 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
     const int S = kind == SCHED_GS ? std::max(1, nSweeps) : 1;
     // level of every (cell, sweep)
     std::vector<int> lev(size_t(n) * S, 0);
-    if (kind == SCHED_BWD) {
+    if (kind == SCHED_BWD || kind == SCHED_GSB) {
         for (int f = h.nf - 1; f >= 0; --f) lev[h.l[f]] = std::max(lev[h.l[f]], lev[h.u[f]] + 1);
     } else {
         for (int s = 0; s < S; ++s) {
@@ -280,13 +280,13 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
     auto entries_of = [&](int c, std::vector<int>& nbs, std::vector<int>& srcs) {
         nbs.clear();
         srcs.clear();
-        if (kind == SCHED_FWD || kind == SCHED_GS) {
+        if (kind == SCHED_FWD || kind == SCHED_GS || kind == SCHED_GSB) {
             for (int k = h.losortStart[c]; k < h.losortStart[c + 1]; ++k) {
                 nbs.push_back(h.losortL[k]);
                 srcs.push_back(k);
             }
         }
-        if (kind == SCHED_GS) {
+        if (kind == SCHED_GS || kind == SCHED_GSB) {
             for (int f = h.ownerStart[c]; f < h.ownerStart[c + 1]; ++f) {
                 nbs.push_back(h.u[f]);
                 srcs.push_back(f | SRC_UPPER);
@@ -376,6 +376,9 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
             for (int k = 0; k < o.cnt[slot]; ++k) {
                 const int e = o.groupEntry[g] + 32 * k + j;
                 const int nb = o.nb[e];
+                // the backward pass reads its lower neighbours' values from
+                // before the kernel: no dependency
+                if (kind == SCHED_GSB && !(o.src[e] & SRC_UPPER)) continue;
                 const bool prev = kind == SCHED_GS && (o.src[e] & SRC_UPPER);
                 const int s2 = prev ? sw - 1 : sw;
                 if (s2 < 0) continue;

@@ -151,7 +151,9 @@ template <class T>
 void launch_reduce(cudaStream_t s, Scratch& sc, int which, int n, const T* a, const T* b, double* out);
 
 // ---- packed sweep schedules (host.cpp builds, sweeps.cu runs) -------------
-enum { SCHED_FWD = 0, SCHED_BWD = 1, SCHED_GS = 2 };
+// SCHED_GSB: the backward Gauss-Seidel pass of symGaussSeidel (the GS
+// entries, levels of the upper-neighbour DAG, cells in reverse order)
+enum { SCHED_FWD = 0, SCHED_BWD = 1, SCHED_GS = 2, SCHED_GSB = 3 };
 constexpr int SRC_UPPER = 1 << 30;       // entry coefficient from upper[f]
 constexpr int SCHED_CHUNK_GROUPS = 8;    // groups of 32 slots per grid chunk
 

@@ -44,8 +44,8 @@ __device__ __forceinline__ int check_convergence(SolveState* st) {
 }
 
 // do { ... } while ((++nIter < maxIter && !converged) || nIter < minIter)
-__device__ __forceinline__ void loop_test(SolveState* st) {
-    ++st->nIterations;
+__device__ __forceinline__ void loop_test(SolveState* st, int inc = 1) {
+    st->nIterations += inc;
     bool cont = false;
     if (st->nIterations < st->maxIter) cont = !check_convergence(st);
     cont = cont || st->nIterations < st->minIter;
@@ -369,24 +369,35 @@ __global__ void gamg_scale_apply_k(int n, T* __restrict__ field, const T* __rest
     }
 }
 
-template <class T>
+// RES false: GAMG's finestResidual = source - Apsi (GAMGSolverSolve.C:116-118);
+// RES true: lduMatrix::residual (lduMatrixATmul.C:203-280: source - diag psi,
+// then minus the neighbour products), as smoothSolver checks it.  The loop
+// counter advances by inc.
+template <class T, bool RES>
 __global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int* os, const int* ls, const int* lL,
                                                                 const int* u, const T* diag, const T* lp,
                                                                 const T* upper, const T* __restrict__ psi,
                                                                 const T* __restrict__ b, T* __restrict__ r,
-                                                                SolveState* st, Red2 red) {
+                                                                SolveState* st, Red2 red, int inc) {
     if (st->done) return;
     double mg = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        // finestResidual = source - Apsi (GAMGSolverSolve.C:116-118)
-        const T v = b[c] - row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi);
+        T v;
+        if (RES) {
+            T acc = b[c] - diag[c] * psi[c];
+            for (int k = ls[c]; k < ls[c + 1]; ++k) acc -= lp[k] * psi[lL[k]];
+            for (int f = os[c]; f < os[c + 1]; ++f) acc -= upper[f] * psi[u[f]];
+            v = acc;
+        } else {
+            v = b[c] - row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi);
+        }
         r[c] = v;
         mg += fabs(double(v));
     }
     double s, dummy;
     if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
         st->finalResidual = s / st->normFactor;
-        loop_test(st);
+        loop_test(st, inc);
     }
 }
 
@@ -533,10 +544,15 @@ void Kern<T>::gamg_scale_apply(cudaStream_t s, int n, T* field, const T* Acf, co
 
 template <class T>
 void Kern<T>::gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a,
-                                  const T* psi, const T* b, T* r, SolveState* st) {
-    gamg_residual_check_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u,
-                                                              a.diag, a.lowerPerm, a.upper, psi, b, r, st,
-                                                              Red2{sc.partials, sc.counters});
+                                  const T* psi, const T* b, T* r, SolveState* st, int inc) {
+    if (inc > 0)
+        gamg_residual_check_k<T, true><<<grid_for(m.n), RED_NT, 0, s>>>(
+            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
+            Red2{sc.partials, sc.counters}, inc);
+    else
+        gamg_residual_check_k<T, false><<<grid_for(m.n), RED_NT, 0, s>>>(
+            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
+            Red2{sc.partials, sc.counters}, 1);
     count_launch();
 }
 

@@ -60,9 +60,10 @@ struct Kern {
     // field = sf*field + (source - sf*Acf)/diag (+ pre when non-null)
     static void gamg_scale_apply(cudaStream_t s, int n, T* field, const T* Acf, const T* source, const T* diag,
                                  const T* pre, const SolveState* st);
-    // r = b - A psi; final = sum|r|/normFactor; nIterations++; loop test
+    // r = b - A psi; final = sum|r|/normFactor; nIterations++; loop test.
+    // inc > 0: r = lduMatrix::residual and nIterations += inc (smoothSolver)
     static void gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a,
-                                    const T* psi, const T* b, T* r, SolveState* st);
+                                    const T* psi, const T* b, T* r, SolveState* st, int inc = 0);
     // single-CTA whole solve of one or more small systems (blockIdx = system)
     static void block_solve(cudaStream_t s, BlockSys<T>* d_sys, int nSys, const int* done);
     // y (+)= x, predicated

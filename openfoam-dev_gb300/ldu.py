@@ -30,13 +30,18 @@ from . import LIB_DIR
 
 LIB_PATH = os.path.join(LIB_DIR, "libcudaLduSolvers.so")
 
-SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG = 0, 1, 2
+SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG, SOLVER_SMOOTH = 0, 1, 2, 3
 PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
-SMOOTHERS = {"GaussSeidel": 0, "DIC": 1}
+SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "symGaussSeidel": 2, "DILU": 3, "DICGaussSeidel": 4,
+             "DILUGaussSeidel": 5}
+# the smoothers' run-time tables by matrix symmetry
+SYM_SMOOTHERS = ("DIC", "DICGaussSeidel", "GaussSeidel", "symGaussSeidel")
+ASYM_SMOOTHERS = ("DILU", "DILUGaussSeidel", "GaussSeidel", "symGaussSeidel")
 SOLVERS = {"cudaPCG": SOLVER_PCG, "cudaPBiCGStab": SOLVER_PBICGSTAB, "cudaGAMG": SOLVER_GAMG,
-           "PCG": SOLVER_PCG, "PBiCGStab": SOLVER_PBICGSTAB, "GAMG": SOLVER_GAMG}
-SYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaPCG")
-ASYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab")
+           "cudaSmoothSolver": SOLVER_SMOOTH,
+           "PCG": SOLVER_PCG, "PBiCGStab": SOLVER_PBICGSTAB, "GAMG": SOLVER_GAMG, "smoothSolver": SOLVER_SMOOTH}
+SYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaPCG", "cudaSmoothSolver")
+ASYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaSmoothSolver")
 
 STATUS = {0: "ok", -1: "bad argument", -2: "bad addressing", -3: "CUDA error", -4: "out of memory",
           -5: "admission refused", -6: "device wait timed out", -7: "bad configuration", -8: "bad state"}
@@ -67,7 +72,7 @@ class Controls(ctypes.Structure):
                 ("nPostSweeps", ctypes.c_int), ("postSweepsLevelMultiplier", ctypes.c_int),
                 ("maxPostSweeps", ctypes.c_int), ("nFinestSweeps", ctypes.c_int),
                 ("scaleCorrection", ctypes.c_int), ("nCellsInCoarsestLevel", ctypes.c_int),
-                ("precision", ctypes.c_int), ("pad", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("nSweeps", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -466,9 +471,12 @@ def _controls(d, sym):
     c.maxIter = int(d.get("maxIter", 1000))
     c.minIter = int(d.get("minIter", 0))
     sm = d.get("smoother", "GaussSeidel")
-    if c.solver == SOLVER_GAMG and sm not in SMOOTHERS:
-        raise FatalError(f"Unknown {'symmetric' if sym else 'asymmetric'} matrix smoother {sm}")
+    if c.solver in (SOLVER_GAMG, SOLVER_SMOOTH) and sm not in (SYM_SMOOTHERS if sym else ASYM_SMOOTHERS):
+        kind = "symmetric" if sym else "asymmetric"
+        table = list(SYM_SMOOTHERS if sym else ASYM_SMOOTHERS)
+        raise FatalError(f"Unknown {kind} matrix smoother {sm}\n\nValid {kind} matrix smoothers are : {table}")
     c.smoother = SMOOTHERS.get(sm, 0)
+    c.nSweeps = int(d.get("nSweeps", 1))
     for k in ("nPreSweeps", "preSweepsLevelMultiplier", "maxPreSweeps", "nPostSweeps",
               "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "nCellsInCoarsestLevel"):
         if k in d:

@@ -1,6 +1,7 @@
 /*---------------------------------------------------------------------------*\
   cudaLduSolvers.C - OpenFOAM run-time selectable solvers cudaPCG,
-  cudaPBiCGStab and cudaGAMG backed by libcudaLduSolvers.so (include/cfx.h).
+  cudaPBiCGStab, cudaGAMG and cudaSmoothSolver backed by
+  libcudaLduSolvers.so (include/cfx.h).
 
   Build into libcudaLduSolvers_OpenFOAM.so with wmake (Make/files: this file;
   Make/options: -I<repo>/include, -L<repo>/openfoam-dev_gb300/lib
@@ -14,8 +15,8 @@
           tolerance 1e-8; relTol 0; precision mixed; }
 
   Registration follows the reference's solvers (PCG.C:30-36,
-  PBiCGStab.C:30-39, GAMGSolver.C:34-43): cudaPCG in the symmetric table,
-  cudaPBiCGStab and cudaGAMG in both.  The solver object is constructed per
+  PBiCGStab.C:30-39, GAMGSolver.C:34-43, smoothSolver.C:32-38): cudaPCG in
+  the symmetric table, cudaPBiCGStab, cudaGAMG and cudaSmoothSolver in both.  The solver object is constructed per
   fvMatrix::solve (fvScalarMatrix.C:162-170); the device copies of the
   addressing, level schedules and GAMG hierarchy live in a process-wide
   cache keyed by the lduMesh, and the coefficients are re-uploaded on every
@@ -169,7 +170,14 @@ protected:
         (
             controlDict_.lookupOrDefault<word>("smoother", "GaussSeidel")
         );
-        c.smoother = sm == "DIC" ? CFX_SMOOTH_DIC : CFX_SMOOTH_GS;
+        c.smoother =
+            sm == "DIC" ? CFX_SMOOTH_DIC
+          : sm == "symGaussSeidel" ? CFX_SMOOTH_SYMGS
+          : sm == "DILU" ? CFX_SMOOTH_DILU
+          : sm == "DICGaussSeidel" ? CFX_SMOOTH_DICGS
+          : sm == "DILUGaussSeidel" ? CFX_SMOOTH_DILUGS
+          : CFX_SMOOTH_GS;
+        c.nSweeps = controlDict_.lookupOrDefault<label>("nSweeps", 1);
         c.nPreSweeps = controlDict_.lookupOrDefault<label>("nPreSweeps", 0);
         c.preSweepsLevelMultiplier =
             controlDict_.lookupOrDefault<label>("preSweepsLevelMultiplier", 1);
@@ -272,10 +280,12 @@ public:                                                                        \
 CUDA_LDU_SOLVER(cudaPCG, CFX_SOLVER_PCG)
 CUDA_LDU_SOLVER(cudaPBiCGStab, CFX_SOLVER_PBICGSTAB)
 CUDA_LDU_SOLVER(cudaGAMG, CFX_SOLVER_GAMG)
+CUDA_LDU_SOLVER(cudaSmoothSolver, CFX_SOLVER_SMOOTH)
 
 defineTypeNameAndDebug(cudaPCG, 0);
 defineTypeNameAndDebug(cudaPBiCGStab, 0);
 defineTypeNameAndDebug(cudaGAMG, 0);
+defineTypeNameAndDebug(cudaSmoothSolver, 0);
 
 lduMatrix::solver::addsymMatrixConstructorToTable<cudaPCG>
     addcudaPCGSymMatrixConstructorToTable_;
@@ -287,6 +297,10 @@ lduMatrix::solver::addsymMatrixConstructorToTable<cudaGAMG>
     addcudaGAMGSymMatrixConstructorToTable_;
 lduMatrix::solver::addasymMatrixConstructorToTable<cudaGAMG>
     addcudaGAMGAsymMatrixConstructorToTable_;
+lduMatrix::solver::addsymMatrixConstructorToTable<cudaSmoothSolver>
+    addcudaSmoothSolverSymMatrixConstructorToTable_;
+lduMatrix::solver::addasymMatrixConstructorToTable<cudaSmoothSolver>
+    addcudaSmoothSolverAsymMatrixConstructorToTable_;
 
 
 solverPerformance cudaPCG::solve
@@ -310,6 +324,18 @@ solverPerformance cudaPBiCGStab::solve
 {
     Entry& e = deviceMatrix();
     return run(e, controls(CFX_SOLVER_PBICGSTAB), psi, source);
+}
+
+
+solverPerformance cudaSmoothSolver::solve
+(
+    scalarField& psi,
+    const scalarField& source,
+    const direction
+) const
+{
+    Entry& e = deviceMatrix();
+    return run(e, controls(CFX_SOLVER_SMOOTH), psi, source);
 }
 
 

@@ -812,11 +812,9 @@ typedef struct {
     double* rD; /* DIC smoother */
 } level_matrix;
 
+/* GAMG's smoother on one level (any smoother of the table; rD as smoother_rD) */
 static void smooth(const ldu_matrix* m, const double* rD, int kind, double* psi, const double* b, int n) {
-    if (kind == LDU_SMOOTH_DIC)
-        ldu_dic_smooth(m, rD, psi, b, n);
-    else
-        ldu_gs_smooth(m, psi, b, n);
+    smoother_apply(m, kind, rD, psi, b, n);
 }
 
 /* GAMGSolver::scale, GAMGSolverScale.C:31-76 */
@@ -885,18 +883,11 @@ int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, con
         /* initVcycle, GAMGSolverSolve.C:446-517 */
         double** corr = (double**)calloc(nl, sizeof(double*));
         double** src = (double**)calloc(nl, sizeof(double*));
-        double* rD0 = NULL;
-        if (gc->smoother == LDU_SMOOTH_DIC) {
-            rD0 = (double*)xmalloc(sizeof(double) * n);
-            ldu_dic_rD(m, rD0);
-        }
+        double* rD0 = smoother_rD(m, gc->smoother);
         for (int i = 0; i < nl; ++i) {
             corr[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
             src[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
-            if (gc->smoother == LDU_SMOOTH_DIC) {
-                lv[i].rD = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
-                ldu_dic_rD(&lv[i].m, lv[i].rD);
-            }
+            lv[i].rD = smoother_rD(&lv[i].m, gc->smoother);
         }
         ldu_controls cc = {c->tolerance, c->relTol, 1000, 0};
         do {

@@ -104,6 +104,12 @@ def test_sweeps_exact(name, sweep_form):
     psi = dev(x)
     A.smooth("GaussSeidel", psi, db, 3)
     np.testing.assert_array_equal(host(psi), m.gs_smooth(x, b, 3))
+    # the rest of the smoother table (symGaussSeidel, DIC/DILU + GaussSeidel, DILU)
+    others = ("symGaussSeidel", "DICGaussSeidel") if A.symmetric() else ("symGaussSeidel", "DILU", "DILUGaussSeidel")
+    for sm in others:
+        psi = dev(x)
+        A.smooth(sm, psi, db, 2)
+        np.testing.assert_array_equal(host(psi), m.smooth(sm, x, b, 2), err_msg=sm)
     A.precondition("diagonal", db, w)
     np.testing.assert_array_equal(host(w), (1.0 / s["diag"]) * b)
 

@@ -26,13 +26,17 @@ torch = pytest.importorskip("torch")
 RTOL_FP64 = 1e-10
 
 
-def _iters_ok(solver, ours, ref):
+def _iters_ok(solver, ours, ref, n_sweeps=1):
     """PCG and GAMG: +-1 iteration.  PBiCGStab on the asymmetric upwind
     matrix is sensitive to the order of its six reductions per iteration
     (the GPU sums in a fixed tree, the reference sequentially), so its count
     may move by a few: within 10% (and 4) of the reference's."""
     if solver == "PBiCGStab":
         return abs(ours - ref) <= max(4, ref // 10)
+    if solver == "smoothSolver":
+        # sweeps are bit-exact; the residual check sums in a tree, so the
+        # last check may fall one check (nSweeps sweeps) either side
+        return abs(ours - ref) <= abs(n_sweeps)
     return abs(ours - ref) <= 1
 
 
@@ -43,9 +47,13 @@ def _residual_ok(s, psi, tol):
     assert np.abs(r).sum() / nf < 1.5 * tol
 
 
+_PLUGIN_NAMES = {"PCG": "cudaPCG", "PBiCGStab": "cudaPBiCGStab", "GAMG": "cudaGAMG",
+                 "smoothSolver": "cudaSmoothSolver"}
+
+
 def _ctl(ctl):
     c = dict(ctl)
-    c["solver"] = "cuda" + c["solver"]
+    c["solver"] = _PLUGIN_NAMES[c["solver"]]
     return c
 
 
@@ -59,7 +67,8 @@ def test_golden_solves(name):
     psi = np.zeros_like(s["source"])
     perf = ldu.solve(s, psi, _ctl(ctl))
     assert perf.solverName == g["solverName"]
-    assert _iters_ok(ctl["solver"], perf.nIterations, int(g["nIterations"][0])), (perf, int(g["nIterations"][0]))
+    assert _iters_ok(ctl["solver"], perf.nIterations, int(g["nIterations"][0]), ctl.get("nSweeps", 1)), \
+        (perf, int(g["nIterations"][0]))
     assert perf.initialResidual == pytest.approx(float(g["initialResidual"][0]), rel=1e-12)
     assert perf.converged == bool(g["converged"][0])
     assert not perf.singular
@@ -210,3 +219,35 @@ def test_converged_at_start_runs_no_iteration():
     psi = np.zeros_like(s["source"])
     perf = ldu.solve(s2, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-6})
     assert perf.nIterations == 0 and perf.converged and np.all(psi == 0)
+
+
+@pytest.mark.parametrize("smoother", ["symGaussSeidel", "DICGaussSeidel", "DIC"])
+def test_gamg_with_other_smoothers_against_oracle(smoother):
+    """cudaGAMG with the rest of the smoother table (the oracle's GAMG is
+    bit-exact with the reference's for the smoothers it shares)."""
+    s = cases.gamg_cube(16, jitter=0.2, seed=5)
+    ref = np.zeros_like(s["source"])
+    rp = orc.gamg(s, ref, tol=1e-8, smoother=smoother, nPreSweeps=1)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, {"solver": "cudaGAMG", "smoother": smoother, "nPreSweeps": 1, "tolerance": 1e-8,
+                              "relTol": 0})
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= (RTOL_FP64 if perf.nIterations == rp.nIterations else 1e-6)
+
+
+@pytest.mark.parametrize("smoother", ["GaussSeidel", "symGaussSeidel", "DICGaussSeidel"])
+def test_smooth_solver_every_form(smoother):
+    """cudaSmoothSolver on a 12^3 cube in every sweep form against the oracle."""
+    s = cases.pcg_cube(12, seed=4)
+    ref = np.zeros_like(s["source"])
+    rp = orc.smooth_solve(s, ref, smoother, 2, tol=1e-6, max_iter=4000)
+    for form in sorted(FORMS):
+        with sweep_form(form):
+            s2 = cases.pcg_cube(12, seed=4)
+            psi = np.zeros_like(s2["source"])
+            perf = ldu.solve(s2, psi, {"solver": "cudaSmoothSolver", "smoother": smoother, "nSweeps": 2,
+                                       "tolerance": 1e-6, "relTol": 0, "maxIter": 4000})
+        assert perf.solverName == "smoothSolver" and perf.converged
+        assert abs(perf.nIterations - rp.nIterations) <= 2, (form, perf.nIterations, rp.nIterations)
+        if perf.nIterations == rp.nIterations:
+            np.testing.assert_array_equal(psi, ref)

@@ -45,8 +45,8 @@ class _FakeMatrix:
 
 
 def test_unknown_solver_is_fatal_like_the_reference():
-    with pytest.raises(ldu.FatalError, match="Unknown symmetric matrix solver smoothSolver"):
-        ldu.solver_new("p", _FakeMatrix(True), {"solver": "smoothSolver"})
+    with pytest.raises(ldu.FatalError, match="Unknown symmetric matrix solver PBiCG"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "PBiCG"})
     with pytest.raises(ldu.FatalError, match="Unknown asymmetric matrix solver cudaPCG"):
         ldu.solver_new("U", _FakeMatrix(False), {"solver": "cudaPCG", "preconditioner": "DILU"})
     with pytest.raises(ldu.FatalError, match="keyword solver is undefined"):
@@ -54,9 +54,19 @@ def test_unknown_solver_is_fatal_like_the_reference():
     with pytest.raises(ldu.FatalError, match="preconditioner"):
         ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaPCG", "preconditioner": "ILU0"})
     with pytest.raises(ldu.FatalError, match="smoother"):
-        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "smoother": "symGaussSeidel"})
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "smoother": "DILU"})
+    with pytest.raises(ldu.FatalError, match="Unknown asymmetric matrix smoother DICGaussSeidel"):
+        ldu.solver_new("U", _FakeMatrix(False), {"solver": "cudaSmoothSolver", "smoother": "DICGaussSeidel"})
     with pytest.raises(ldu.FatalError, match="GAMGAgglomeration"):
         ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "agglomerator": "algebraicPair"})
+
+
+def test_smooth_solver_controls_parse():
+    s = ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaSmoothSolver", "smoother": "symGaussSeidel",
+                                                "nSweeps": 2, "tolerance": 1e-7})
+    assert s.c.solver == ldu.SOLVER_SMOOTH and s.c.smoother == 2 and s.c.nSweeps == 2
+    s = ldu.solver_new("U", _FakeMatrix(False), {"solver": "smoothSolver", "smoother": "DILUGaussSeidel"})
+    assert s.c.smoother == 5 and s.c.nSweeps == 1
 
 
 def test_controls_parse():

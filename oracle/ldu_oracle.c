@@ -834,133 +834,234 @@ static void gamg_scale(const ldu_matrix* A, double* field, double* Acf, const do
 
 static int imin(int a, int b) { return a < b ? a : b; }
 
-/* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
- * GAMGSolverSolve.C:31-552 (interpolateCorrection off, no interfaces). */
-int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
-             const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
+/* The GAMG hierarchy of one solve: coarse matrices (GAMGSolver ctor,
+ * GAMGSolver.C:204-206), the smoothers' reciprocal diagonals and the coarse
+ * correction and source fields (initVcycle, GAMGSolverSolve.C:446-517). */
+typedef struct {
+    const ldu_matrix* m;
+    const ldu_agglomeration* agg;
+    const ldu_gamg_controls* gc;
+    int nl, coarsest, sym, scaleCorrection, maxSize;
+    level_matrix* lv;
+    double **corr, **src;
+    double* rD0;
+} gamg_hier;
+
+static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeration* agg,
+                       const ldu_gamg_controls* gc) {
     const int n = m->nCells;
     const int nl = agg->nLevels;
-    if (nl < 1) return -1;
-    const int sym = m->lower == NULL;
-    const int scaleCorrection = gc->scaleCorrection < 0 ? sym : gc->scaleCorrection;
-    memset(perf, 0, sizeof(*perf));
-
-    /* coarse matrices (GAMGSolver ctor, GAMGSolver.C:204-206) */
-    level_matrix* lv = (level_matrix*)calloc(nl, sizeof(level_matrix));
+    H->m = m;
+    H->agg = agg;
+    H->gc = gc;
+    H->nl = nl;
+    H->coarsest = nl - 1;
+    H->sym = m->lower == NULL;
+    H->scaleCorrection = gc->scaleCorrection < 0 ? H->sym : gc->scaleCorrection;
+    H->lv = (level_matrix*)calloc(nl, sizeof(level_matrix));
     const ldu_matrix* fine = m;
     int maxSize = n;
     for (int i = 0; i < nl; ++i) {
         const int nc = agg->nCells[i], ncf = agg->nFaces[i];
         if (nc > maxSize) maxSize = nc;
-        lv[i].diag = (double*)xmalloc(sizeof(double) * nc);
-        lv[i].upper = (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
-        lv[i].lower = sym ? NULL : (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
+        level_matrix* L = &H->lv[i];
+        L->diag = (double*)xmalloc(sizeof(double) * nc);
+        L->upper = (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
+        L->lower = H->sym ? NULL : (double*)xmalloc(sizeof(double) * (ncf ? ncf : 1));
         ldu_gamg_coarse_matrix(fine->nCells, fine->nFaces, fine->diag, fine->upper,
-                               sym ? NULL : fine->lower, agg->restrictAddr[i], agg->faceRestrict[i],
-                               agg->faceFlip[i], nc, ncf, lv[i].diag, lv[i].upper, lv[i].lower);
-        lv[i].m.nCells = nc;
-        lv[i].m.nFaces = ncf;
-        lv[i].m.l = agg->cl[i];
-        lv[i].m.u = agg->cu[i];
-        lv[i].m.diag = lv[i].diag;
-        lv[i].m.upper = lv[i].upper;
-        lv[i].m.lower = lv[i].lower;
-        ldu_init_addr(&lv[i].m);
-        fine = &lv[i].m;
+                               H->sym ? NULL : fine->lower, agg->restrictAddr[i], agg->faceRestrict[i],
+                               agg->faceFlip[i], nc, ncf, L->diag, L->upper, L->lower);
+        L->m.nCells = nc;
+        L->m.nFaces = ncf;
+        L->m.l = agg->cl[i];
+        L->m.u = agg->cu[i];
+        L->m.diag = L->diag;
+        L->m.upper = L->upper;
+        L->m.lower = L->lower;
+        ldu_init_addr(&L->m);
+        fine = &L->m;
     }
-    const int coarsest = nl - 1;
+    H->maxSize = maxSize;
+    H->corr = (double**)calloc(nl, sizeof(double*));
+    H->src = (double**)calloc(nl, sizeof(double*));
+    H->rD0 = smoother_rD(m, gc->smoother);
+    for (int i = 0; i < nl; ++i) {
+        H->corr[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
+        H->src[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
+        H->lv[i].rD = smoother_rD(&H->lv[i].m, gc->smoother);
+    }
+}
 
-    double* Apsi = (double*)xmalloc(sizeof(double) * maxSize);
-    double* finestCorrection = (double*)xmalloc(sizeof(double) * maxSize);
+static void gamg_free(gamg_hier* H) {
+    for (int i = 0; i < H->nl; ++i) {
+        free(H->corr[i]);
+        free(H->src[i]);
+        free(H->lv[i].rD);
+        free(H->lv[i].diag);
+        free(H->lv[i].upper);
+        free(H->lv[i].lower);
+        ldu_free_addr(&H->lv[i].m);
+    }
+    free(H->corr);
+    free(H->src);
+    free(H->rD0);
+    free(H->lv);
+}
+
+/* GAMGSolver::Vcycle, GAMGSolverSolve.C:148-443: psi += the coarse-grid
+ * correction of finestResidual, then the finest level's smoothing against
+ * source b.  Apsi, finestCorrection: scratch of maxSize.  cc: the coarsest
+ * level solve's tolerances (the GAMG object's own). */
+static void gamg_vcycle(gamg_hier* H, double* psi, const double* b, double* Apsi, double* finestCorrection,
+                        const double* finestResidual, const ldu_controls* cc) {
+    const ldu_matrix* m = H->m;
+    const ldu_agglomeration* agg = H->agg;
+    const ldu_gamg_controls* gc = H->gc;
+    const int n = m->nCells, coarsest = H->coarsest, scaleCorrection = H->scaleCorrection;
+    level_matrix* lv = H->lv;
+    double** corr = H->corr;
+    double** src = H->src;
+    double* scratch1 = Apsi;
+    double* scratch2 = finestCorrection;
+    /* restrictField(coarseSources[0], finestResidual, 0) */
+    for (int k = 0; k < agg->nCells[0]; ++k) src[0][k] = 0;
+    for (int k = 0; k < n; ++k) src[0][agg->restrictAddr[0][k]] += finestResidual[k];
+    for (int li = 0; li < coarsest; ++li) {
+        const int nc = agg->nCells[li];
+        if (gc->nPreSweeps) {
+            for (int k = 0; k < nc; ++k) corr[li][k] = 0;
+            smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
+                   imin(gc->nPreSweeps + gc->preSweepsLevelMultiplier * li, gc->maxPreSweeps));
+            if (scaleCorrection && li < coarsest - 1) gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
+            ldu_amul(&lv[li].m, corr[li], scratch1);
+            for (int k = 0; k < nc; ++k) src[li][k] -= scratch1[k];
+        }
+        const int nn = agg->nCells[li + 1];
+        for (int k = 0; k < nn; ++k) src[li + 1][k] = 0;
+        for (int k = 0; k < nc; ++k) src[li + 1][agg->restrictAddr[li + 1][k]] += src[li][k];
+    }
+    /* solveCoarsestLevel, GAMGSolverSolve.C:520-552 */
+    {
+        ldu_perf cp;
+        for (int k = 0; k < agg->nCells[coarsest]; ++k) corr[coarsest][k] = 0;
+        if (H->sym)
+            ldu_pcg(&lv[coarsest].m, corr[coarsest], src[coarsest], cc, LDU_PRE_DIC, &cp);
+        else
+            ldu_pbicgstab(&lv[coarsest].m, corr[coarsest], src[coarsest], cc, LDU_PRE_DILU, &cp);
+    }
+    for (int li = coarsest - 1; li >= 0; --li) {
+        const int nc = agg->nCells[li];
+        double* pre = scratch2;
+        if (gc->nPreSweeps) memcpy(pre, corr[li], sizeof(double) * nc);
+        for (int k = 0; k < nc; ++k) corr[li][k] = corr[li + 1][agg->restrictAddr[li + 1][k]];
+        if (scaleCorrection && li < coarsest - 1) gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
+        if (gc->nPreSweeps)
+            for (int k = 0; k < nc; ++k) corr[li][k] += pre[k];
+        smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
+               imin(gc->nPostSweeps + gc->postSweepsLevelMultiplier * li, gc->maxPostSweeps));
+    }
+    for (int k = 0; k < n; ++k) finestCorrection[k] = corr[0][agg->restrictAddr[0][k]];
+    if (scaleCorrection) gamg_scale(m, finestCorrection, Apsi, finestResidual);
+    for (int k = 0; k < n; ++k) psi[k] += finestCorrection[k];
+    smooth(m, H->rD0, gc->smoother, psi, b, gc->nFinestSweeps);
+}
+
+/* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
+ * GAMGSolverSolve.C:31-552 (interpolateCorrection off, no interfaces). */
+int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
+             const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
+    const int n = m->nCells;
+    if (agg->nLevels < 1) return -1;
+    memset(perf, 0, sizeof(*perf));
+    gamg_hier H;
+    gamg_setup(&H, m, agg, gc);
+    double* Apsi = (double*)xmalloc(sizeof(double) * H.maxSize);
+    double* finestCorrection = (double*)xmalloc(sizeof(double) * H.maxSize);
     double* finestResidual = (double*)xmalloc(sizeof(double) * n);
     ldu_amul(m, psi, Apsi);
     const double normFactor = ldu_norm_factor(m, psi, b, Apsi, finestCorrection);
     for (int i = 0; i < n; ++i) finestResidual[i] = b[i] - Apsi[i];
     perf->initialResidual = ldu_sum_mag(n, finestResidual) / normFactor;
     perf->finalResidual = perf->initialResidual;
-
     if (c->minIter > 0 || !check_convergence(perf, c)) {
-        /* initVcycle, GAMGSolverSolve.C:446-517 */
-        double** corr = (double**)calloc(nl, sizeof(double*));
-        double** src = (double**)calloc(nl, sizeof(double*));
-        double* rD0 = smoother_rD(m, gc->smoother);
-        for (int i = 0; i < nl; ++i) {
-            corr[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
-            src[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
-            lv[i].rD = smoother_rD(&lv[i].m, gc->smoother);
-        }
         ldu_controls cc = {c->tolerance, c->relTol, 1000, 0};
         do {
-            /* Vcycle, GAMGSolverSolve.C:148-443 */
-            double* scratch1 = Apsi;
-            double* scratch2 = finestCorrection;
-            /* restrictField(coarseSources[0], finestResidual, 0) */
-            for (int k = 0; k < agg->nCells[0]; ++k) src[0][k] = 0;
-            for (int k = 0; k < n; ++k) src[0][agg->restrictAddr[0][k]] += finestResidual[k];
-            for (int li = 0; li < coarsest; ++li) {
-                const int nc = agg->nCells[li];
-                if (gc->nPreSweeps) {
-                    for (int k = 0; k < nc; ++k) corr[li][k] = 0;
-                    smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
-                           imin(gc->nPreSweeps + gc->preSweepsLevelMultiplier * li, gc->maxPreSweeps));
-                    if (scaleCorrection && li < coarsest - 1)
-                        gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
-                    ldu_amul(&lv[li].m, corr[li], scratch1);
-                    for (int k = 0; k < nc; ++k) src[li][k] -= scratch1[k];
-                }
-                const int nn = agg->nCells[li + 1];
-                for (int k = 0; k < nn; ++k) src[li + 1][k] = 0;
-                for (int k = 0; k < nc; ++k) src[li + 1][agg->restrictAddr[li + 1][k]] += src[li][k];
-            }
-            /* solveCoarsestLevel, GAMGSolverSolve.C:520-552 */
-            {
-                ldu_perf cp;
-                for (int k = 0; k < agg->nCells[coarsest]; ++k) corr[coarsest][k] = 0;
-                if (sym)
-                    ldu_pcg(&lv[coarsest].m, corr[coarsest], src[coarsest], &cc, LDU_PRE_DIC, &cp);
-                else
-                    ldu_pbicgstab(&lv[coarsest].m, corr[coarsest], src[coarsest], &cc, LDU_PRE_DILU, &cp);
-            }
-            for (int li = coarsest - 1; li >= 0; --li) {
-                const int nc = agg->nCells[li];
-                double* pre = scratch2;
-                if (gc->nPreSweeps) memcpy(pre, corr[li], sizeof(double) * nc);
-                for (int k = 0; k < nc; ++k) corr[li][k] = corr[li + 1][agg->restrictAddr[li + 1][k]];
-                if (scaleCorrection && li < coarsest - 1)
-                    gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
-                if (gc->nPreSweeps)
-                    for (int k = 0; k < nc; ++k) corr[li][k] += pre[k];
-                smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
-                       imin(gc->nPostSweeps + gc->postSweepsLevelMultiplier * li, gc->maxPostSweeps));
-            }
-            for (int k = 0; k < n; ++k) finestCorrection[k] = corr[0][agg->restrictAddr[0][k]];
-            if (scaleCorrection) gamg_scale(m, finestCorrection, Apsi, finestResidual);
-            for (int k = 0; k < n; ++k) psi[k] += finestCorrection[k];
-            smooth(m, rD0, gc->smoother, psi, b, gc->nFinestSweeps);
-
+            gamg_vcycle(&H, psi, b, Apsi, finestCorrection, finestResidual, &cc);
             ldu_amul(m, psi, Apsi);
             for (int k = 0; k < n; ++k) finestResidual[k] = b[k] - Apsi[k];
             perf->finalResidual = ldu_sum_mag(n, finestResidual) / normFactor;
         } while ((++perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
                  perf->nIterations < c->minIter);
-        for (int i = 0; i < nl; ++i) {
-            free(corr[i]);
-            free(src[i]);
-            free(lv[i].rD);
-        }
-        free(corr);
-        free(src);
-        free(rD0);
     }
-    for (int i = 0; i < nl; ++i) {
-        free(lv[i].diag);
-        free(lv[i].upper);
-        free(lv[i].lower);
-        ldu_free_addr(&lv[i].m);
-    }
-    free(lv);
+    gamg_free(&H);
     free(Apsi);
     free(finestCorrection);
     free(finestResidual);
+    return 0;
+}
+
+/* PCG::solve (PCG.C:65-193) with GAMGPreconditioner::precondition
+ * (GAMGPreconditioner.C:81-148): wA = 0, nVcycles V-cycles on A wA = rA, the
+ * finest residual rA - A wA recomputed between them.  pc: the preconditioner
+ * dictionary's tolerance/relTol (its coarsest-level solves). */
+int ldu_pcg_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
+                 const ldu_controls* c, const ldu_gamg_controls* gc, const ldu_controls* pc, int nVcycles,
+                 ldu_perf* perf) {
+    const int n = m->nCells;
+    if (agg->nLevels < 1) return -1;
+    double* pA = (double*)xmalloc(sizeof(double) * n);
+    double* wA = (double*)xmalloc(sizeof(double) * n);
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    memset(perf, 0, sizeof(*perf));
+    double wArA = SP_GREAT, wArAold = wArA;
+    ldu_amul(m, psi, wA);
+    for (int i = 0; i < n; ++i) rA[i] = b[i] - wA[i];
+    const double normFactor = ldu_norm_factor(m, psi, b, wA, pA);
+    perf->initialResidual = ldu_sum_mag(n, rA) / normFactor;
+    perf->finalResidual = perf->initialResidual;
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        gamg_hier H;
+        gamg_setup(&H, m, agg, gc);
+        double* AwA = (double*)xmalloc(sizeof(double) * H.maxSize);
+        double* fcorr = (double*)xmalloc(sizeof(double) * H.maxSize);
+        double* fres = (double*)xmalloc(sizeof(double) * n);
+        const ldu_controls cc = {pc->tolerance, pc->relTol, 1000, 0};
+        do {
+            wArAold = wArA;
+            memset(wA, 0, sizeof(double) * n);
+            memcpy(fres, rA, sizeof(double) * n);
+            for (int cycle = 0; cycle < nVcycles; ++cycle) {
+                gamg_vcycle(&H, wA, rA, AwA, fcorr, fres, &cc);
+                if (cycle < nVcycles - 1) {
+                    ldu_amul(m, wA, AwA);
+                    for (int i = 0; i < n; ++i) fres[i] = rA[i] - AwA[i];
+                }
+            }
+            wArA = ldu_sum_prod(n, wA, rA);
+            if (perf->nIterations == 0) {
+                for (int i = 0; i < n; ++i) pA[i] = wA[i];
+            } else {
+                const double beta = wArA / wArAold;
+                for (int i = 0; i < n; ++i) pA[i] = wA[i] + beta * pA[i];
+            }
+            ldu_amul(m, pA, wA);
+            const double wApA = ldu_sum_prod(n, wA, pA);
+            if (check_singularity(perf, fabs(wApA) / normFactor)) break;
+            const double alpha = wArA / wApA;
+            for (int i = 0; i < n; ++i) {
+                psi[i] += alpha * pA[i];
+                rA[i] -= alpha * wA[i];
+            }
+            perf->finalResidual = ldu_sum_mag(n, rA) / normFactor;
+        } while ((++perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        gamg_free(&H);
+        free(AwA);
+        free(fcorr);
+        free(fres);
+    }
+    free(pA);
+    free(wA);
+    free(rA);
     return 0;
 }

@@ -141,6 +141,11 @@ void ldu_gamg_default_controls(ldu_gamg_controls* g);
  * must have been built for m's addressing. */
 int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
              const ldu_controls* c, const ldu_gamg_controls* g, ldu_perf* perf);
+/* PCG with the GAMG preconditioner; pc: the preconditioner dictionary's
+ * tolerance/relTol */
+int ldu_pcg_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
+                 const ldu_controls* c, const ldu_gamg_controls* g, const ldu_controls* pc, int nVcycles,
+                 ldu_perf* perf);
 
 #ifdef __cplusplus
 }

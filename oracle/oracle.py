@@ -282,6 +282,28 @@ def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smo
     return _perf(perf)
 
 
+def pcg_gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, nVcycles=2, pre_tol=1e-6,
+             pre_rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=0, nPostSweeps=2, nFinestSweeps=2,
+             maxPreSweeps=4, maxPostSweeps=4, preSweepsLevelMultiplier=1, postSweepsLevelMultiplier=1,
+             scaleCorrection=None, nCellsInCoarsestLevel=10):
+    """PCG with the GAMG preconditioner (GAMGPreconditioner.C:81-148)."""
+    if agg is None:
+        agg = Agglomeration(s, n_coarsest=nCellsInCoarsestLevel)
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    g = LduGamgControls(nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps, nPostSweeps,
+                        postSweepsLevelMultiplier, maxPostSweeps, nFinestSweeps,
+                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother])
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    pc = _controls(pre_tol, pre_rel_tol, 1000, 0)
+    rc = lib().ldu_pcg_gamg(ctypes.byref(m.c), ctypes.byref(agg.c), _p(psi), _p(b), ctypes.byref(c),
+                            ctypes.byref(g), ctypes.byref(pc), int(nVcycles), ctypes.byref(perf))
+    if rc != 0:
+        raise ValueError("PCG/GAMG failed")
+    return _perf(perf)
+
+
 def coarse_matrix(fine, agg, i):
     """Coarse (diag, upper, lower) of level i from the fine system dict."""
     ra, fra, flip, nc, ncf, _, _ = agg.level(i)

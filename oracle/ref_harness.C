@@ -413,10 +413,19 @@ int runSolve(const RecMap& in, Writer& out, Time& runTime)
     lduInterfaceFieldPtrsList ifs(0);
 
     const word solverName(dict.lookup("solver"));
-    if (solverName == "GAMG")
+    // GAMG, or a solver preconditioned by GAMG (a preconditioner
+    // dictionary with preconditioner GAMG and the GAMG keys): the
+    // agglomeration from the given weights
+    const bool gamgPre =
+        dict.isDict("preconditioner")
+     && word(dict.subDict("preconditioner").lookup("preconditioner")) == "GAMG";
+    if (solverName == "GAMG" || gamgPre)
     {
         const scalarField w(getF(in, "weights"));
-        harnessAgglomeration* agg = new harnessAgglomeration(mesh, w, dict);
+        harnessAgglomeration* agg = new harnessAgglomeration
+        (
+            mesh, w, gamgPre ? dict.subDict("preconditioner") : dict
+        );
         regIOobject::store(static_cast<GAMGAgglomeration*>(agg));
     }
 

@@ -53,6 +53,9 @@ def ops(s, x, b):
 def dict_text(ctl):
     parts = []
     for k, v in ctl.items():
+        if isinstance(v, dict):
+            parts.append(f"{k} {dict_text(v)}")
+            continue
         if isinstance(v, bool):
             v = "true" if v else "false"
         elif isinstance(v, float):

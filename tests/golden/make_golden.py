@@ -84,6 +84,12 @@ SOLVES = {
                                    relTol=0.0, maxIter=7)),
     "smooth_reltol": ("jcube14", dict(solver="smoothSolver", smoother="DICGaussSeidel", tolerance=0.0,
                                       relTol=1e-2)),
+    "pcg_gamg": ("jcube16", dict(solver="PCG", tolerance=1e-8, relTol=0.0,
+                                 preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel", nVcycles=2,
+                                                     nCellsInCoarsestLevel=10))),
+    "pcg_gamg_dicgs": ("jcube14", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
+                                       preconditioner=dict(preconditioner="GAMG", smoother="DICGaussSeidel",
+                                                           nVcycles=1, nPreSweeps=1, tolerance=1e-4))),
 }
 
 
@@ -125,7 +131,9 @@ def main():
     for name, (sysname, ctl) in SOLVES.items():
         s = build(*SYSTEMS[sysname])
         sums[sysname] = checksum(s)
-        w = orc.face_area_pair_weights(s["Sf"]) if ctl["solver"] == "GAMG" else None
+        pre = ctl.get("preconditioner")
+        gamg_pre = isinstance(pre, dict) and pre.get("preconditioner") == "GAMG"
+        w = orc.face_area_pair_weights(s["Sf"]) if ctl["solver"] == "GAMG" or gamg_pre else None
         r = ref.solve(s, ctl, weights=w)
         out = {k: v for k, v in r.items() if not isinstance(v, str)}
         out["solverName"] = np.frombuffer(r["solverName"].encode(), np.uint8)

@@ -68,7 +68,11 @@ def _run_oracle(s, ctl):
     psi = np.zeros_like(s["source"])
     kw = dict(tol=ctl.get("tolerance", 1e-6), rel_tol=ctl.get("relTol", 0.0), max_iter=ctl.get("maxIter", 1000),
               min_iter=ctl.get("minIter", 0))
-    if ctl["solver"] == "PCG":
+    pre = ctl.get("preconditioner")
+    if ctl["solver"] == "PCG" and isinstance(pre, dict):
+        p = orc.pcg_gamg(s, psi, nVcycles=pre.get("nVcycles", 2), pre_tol=pre.get("tolerance", 1e-6),
+                         pre_rel_tol=pre.get("relTol", 0.0), **kw, **gamg_kwargs(pre))
+    elif ctl["solver"] == "PCG":
         p = orc.pcg(s, psi, precond=ctl["preconditioner"], **kw)
     elif ctl["solver"] == "PBiCGStab":
         p = orc.pbicgstab(s, psi, precond=ctl["preconditioner"], **kw)

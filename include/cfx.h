@@ -60,7 +60,10 @@ typedef struct {
 
 /* CFX_SOLVER_SMOOTH: smoothSolver (smoothSolver.C:77-196) */
 enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2, CFX_SOLVER_SMOOTH = 3 };
-enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3 };
+/* CFX_PRE_GAMG: GAMGPreconditioner (GAMGPreconditioner.C:81-148), nVcycles
+ * V-cycles with the controls' GAMG fields (smoother, sweeps) from w = 0; the
+ * mesh needs GAMG levels */
+enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3, CFX_PRE_GAMG = 4 };
 /* lduMatrix::smoother run-time table (GAMG's smoother, smoothSolver's):
  * GaussSeidel, DIC (symmetric), symGaussSeidel, DILU (asymmetric),
  * DICGaussSeidel (symmetric), DILUGaussSeidel (asymmetric) */
@@ -91,6 +94,12 @@ typedef struct {
     /* smoothSolver: sweeps between residual checks (default 1; negative: that
      * many sweeps and no residuals, smoothSolver.C:93-116) */
     int nSweeps;
+    /* GAMG preconditioner: V-cycles per application (default 2) and its own
+     * tolerance / relTol (its coarsest-level solves; defaults 1e-6, 0) */
+    int nVcycles;
+    int pad;
+    double pcTolerance;
+    double pcRelTol;
 } cfx_controls;
 
 void cfx_default_controls(cfx_controls* c);

@@ -79,8 +79,14 @@ struct Work {
     }
 };
 
+namespace cfx {
+struct PcGamg;  // the GAMG preconditioner's cycles (defined with the V-cycle)
+void pc_gamg_free(PcGamg* p);
+}  // namespace cfx
+
 struct cfx_matrix {
     cfx_mesh* mesh = nullptr;
+    PcGamg* pcGamg = nullptr;
     Arena arena;
     bool sym = true;
     std::vector<LevelCoeffs<double>> c64;   // per level
@@ -479,6 +485,11 @@ void diag_reciprocal(cfx_ctx* ctx, const LevelMesh& m, LevelCoeffs<T>& c) {
     Ops<T>::reciprocal(ctx->stream, m.n, c.rD);
 }
 
+template <class T>
+int pc_gamg_apply(cfx_matrix* mat, const T* r, T* w, const int* done, bool dot);
+template <class T>
+void pc_gamg_setup(cfx_matrix* mat);
+
 // w = M^-1 r with the w.r dot partials in ctx->sc.chunkPartials when dot.
 // Returns the number of partials.  DIC/DILU packs must be current
 // (compute_rD).
@@ -488,6 +499,7 @@ int precondition(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int*
     cudaStream_t s = ctx->stream;
     const LevelMesh& m = mat->mesh->dev[lv];
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    if (kind == CFX_PRE_GAMG) return pc_gamg_apply<T>(mat, r, w, done, dot);
     if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
         const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
         const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
@@ -512,6 +524,8 @@ void setup_preconditioner(cfx_matrix* mat, int lv, int kind) {
         compute_rD<T>(mat, lv);
     } else if (kind == CFX_PRE_DIAGONAL) {
         diag_reciprocal<T>(ctx, mat->mesh->dev[lv], coeffs<T>(mat, lv));
+    } else if (kind == CFX_PRE_GAMG) {
+        pc_gamg_setup<T>(mat);
     }
     ensure_chunk_partials(ctx, RED_MAXB);
 }
@@ -555,7 +569,19 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     int iters = 0;
     if (solver == CFX_SOLVER_PBICGSTAB)
         for (int i = 4; i < 8; ++i) W.get(i, n);
-    const uint64_t key = hkey({mat->mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    uint64_t pcKey = 0;
+    if (precond == CFX_PRE_GAMG) {
+        double pt = ctl.pcTolerance, pr = ctl.pcRelTol;
+        uint64_t a = 0, b2 = 0;
+        std::memcpy(&a, &pt, 8);
+        std::memcpy(&b2, &pr, 8);
+        pcKey = hkey({a, b2, uint64_t(ctl.nVcycles), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps),
+                      uint64_t(ctl.nPostSweeps), uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps),
+                      uint64_t(ctl.maxPostSweeps), uint64_t(ctl.preSweepsLevelMultiplier),
+                      uint64_t(ctl.postSweepsLevelMultiplier), uint64_t(ctl.scaleCorrection + 7),
+                      uint64_t(mat->mesh->nCoarseLevels)});
+    }
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD)});
     auto body = [&]() {
@@ -861,6 +887,94 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     CK(cudaStreamSynchronize(s));  // h is a stack object
 }
 
+}  // namespace
+
+namespace cfx {
+// GAMGPreconditioner (GAMGPreconditioner.C:40-148): its own GAMG controls
+// (the preconditioner dictionary's smoother, sweeps, tolerance and relTol)
+// and one V-cycle object per precision.
+struct PcGamg {
+    cfx_controls ctl{};
+    GamgCycle<double> c64{};
+    GamgCycle<float> c32{};
+};
+void pc_gamg_free(PcGamg* p) { delete p; }
+}  // namespace cfx
+
+namespace {
+
+template <class T>
+GamgCycle<T>& pc_cycle(PcGamg* p);
+template <>
+GamgCycle<double>& pc_cycle<double>(PcGamg* p) {
+    return p->c64;
+}
+template <>
+GamgCycle<float>& pc_cycle<float>(PcGamg* p) {
+    return p->c32;
+}
+template <class T>
+Work<T>& work_of(cfx_matrix* mat);
+template <>
+Work<double>& work_of<double>(cfx_matrix* mat) {
+    return mat->w64;
+}
+template <>
+Work<float>& work_of<float>(cfx_matrix* mat) {
+    return mat->w32;
+}
+
+constexpr int PC_SLOT = 3;  // SolveState of the preconditioner's V-cycles
+
+template <class T>
+void pc_gamg_setup(cfx_matrix* mat) {
+    PcGamg* P = mat->pcGamg;
+    cfx_ctx* ctx = mat->mesh->ctx;
+    prepare_levels(mat, sizeof(T) == 4);
+    const int nl = int(mat->mesh->dev.size());
+    if ((int)mat->lv64.size() < nl) mat->lv64.resize(nl);
+    if ((int)mat->lv32.size() < nl) mat->lv32.resize(nl);
+    set_state(ctx, PC_SLOT, P->ctl, P->ctl.tolerance, P->ctl.relTol, 1, 0);
+    setup_cycle<T>(pc_cycle<T>(P), mat, &P->ctl, work_of<T>(mat), ctx->d_state + PC_SLOT);
+    // the finest residual and A wA: allocated here, outside graph capture
+    work_of<T>(mat).get(G0 + 600, mat->mesh->dev[0].n);
+    work_of<T>(mat).get(G0 + 601, mat->mesh->dev[0].n);
+}
+
+// wA = 0; nVcycles V-cycles of A wA = rA, the finest residual rA - A wA
+// recomputed between them (GAMGPreconditioner.C:81-148).  The dot product
+// w.r (PCG's wArA), when asked, lands in chunkPartials[0] (one partial).
+template <class T>
+int pc_gamg_apply(cfx_matrix* mat, const T* r, T* w, const int* done, bool dot) {
+    PcGamg* P = mat->pcGamg;
+    GamgCycle<T>& cy = pc_cycle<T>(P);
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const LevelMesh& m0 = mat->mesh->dev[0];
+    LevelCoeffs<T>& c0 = coeffs<T>(mat, 0);
+    const int n = m0.n;
+    Work<T>& W = work_of<T>(mat);
+    T* fres = W.get(G0 + 600, n);
+    T* Aw = W.get(G0 + 601, n);
+    Kern<T>::fill(s, n, T(0), w, done);
+    Kern<T>::copy(s, n, r, fres, done);
+    for (int cyc = 0; cyc < P->ctl.nVcycles; ++cyc) {
+        cy.enqueue(w, r, fres);
+        Kern<T>::axpy(s, n, T(1), cy.fcorr, w, done);
+        smooth<T>(ctx, mat, 0, P->ctl.smoother, w, r, P->ctl.nFinestSweeps, cy.workFor(0));
+        if (cyc < P->ctl.nVcycles - 1) {
+            // finestResidual = rA; finestResidual -= AwA
+            Ops<T>::amul(s, m0, c0, w, Aw);
+            Kern<T>::copy(s, n, r, fres, done);
+            Kern<T>::axpy(s, n, T(-1), Aw, fres, done);
+        }
+    }
+    if (!dot) return 0;
+    launch_reduce<T>(s, ctx->sc, 3, n, w, r, ctx->sc.chunkPartials);
+    count_launch();
+    return 1;
+}
+
 cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, const double* b, cfx_perf* perf) {
     cfx_mesh* mesh = mat->mesh;
     cfx_ctx* ctx = mesh->ctx;
@@ -946,6 +1060,7 @@ const char* pre_name(int p) {
         case CFX_PRE_NONE: return "none";
         case CFX_PRE_DIAGONAL: return "diagonal";
         case CFX_PRE_DIC: return "DIC";
+        case CFX_PRE_GAMG: return "GAMG";
         default: return "DILU";
     }
 }
@@ -955,6 +1070,26 @@ cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, c
     cudaStream_t s = ctx->stream;
     const int n = mat->mesh->dev[0].n;
     SolveState h{};
+    if (ctl.preconditioner == CFX_PRE_GAMG) {
+        if (mat->mesh->nCoarseLevels < 1) {
+            set_error("GAMG preconditioner: no coarse levels (agglomerate the mesh first)");
+            return CFX_ERR_STATE;
+        }
+        if (!mat->pcGamg) mat->pcGamg = new PcGamg();
+        // coarse coefficients and level work lists before krylov() takes
+        // references into them (prepare_levels grows mat->c64 / c32)
+        prepare_levels(mat, ctl.precision == CFX_MIXED);
+        const int nl = int(mat->mesh->dev.size());
+        if ((int)mat->lv64.size() < nl) mat->lv64.resize(nl);
+        if ((int)mat->lv32.size() < nl) mat->lv32.resize(nl);
+        cfx_controls pc = ctl;
+        pc.solver = CFX_SOLVER_GAMG;
+        pc.tolerance = ctl.pcTolerance;
+        pc.relTol = ctl.pcRelTol;
+        pc.maxIter = 1000;
+        pc.minIter = 0;
+        mat->pcGamg->ctl = pc;
+    }
     if (ctl.precision != CFX_MIXED) {
         CFX_TRY(krylov<double>(mat, mat->w64, ctl.solver == CFX_SOLVER_PCG ? mat->gPCG : mat->gBiCG, 0, ctl.solver,
                                ctl.preconditioner, psi, b, 0, ctl.tolerance, ctl.relTol, ctl.maxIter, ctl.minIter,
@@ -1074,7 +1209,7 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("null controls");
         return CFX_ERR_ARG;
     }
-    if (c->solver < 0 || c->solver > 3 || c->preconditioner < 0 || c->preconditioner > 3 || c->smoother < 0 ||
+    if (c->solver < 0 || c->solver > 3 || c->preconditioner < 0 || c->preconditioner > 4 || c->smoother < 0 ||
         c->smoother > 5 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
         set_error("unknown solver, preconditioner, smoother or precision");
         return CFX_ERR_CONFIG;
@@ -1089,7 +1224,13 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("precision mixed is not available for cudaSmoothSolver");
         return CFX_ERR_CONFIG;
     }
-    if (c->solver == CFX_SOLVER_GAMG || c->solver == CFX_SOLVER_SMOOTH) {
+    const bool pcGamg = (c->solver == CFX_SOLVER_PCG || c->solver == CFX_SOLVER_PBICGSTAB) &&
+                        c->preconditioner == CFX_PRE_GAMG;
+    if (pcGamg && c->nVcycles < 1) {
+        set_error("GAMG preconditioner: nVcycles must be at least 1");
+        return CFX_ERR_CONFIG;
+    }
+    if (c->solver == CFX_SOLVER_GAMG || c->solver == CFX_SOLVER_SMOOTH || pcGamg) {
         // smoother tables (the smoothers' *ConstructorToTable registrations)
         const bool symOnly = c->smoother == CFX_SMOOTH_DIC || c->smoother == CFX_SMOOTH_DICGS;
         const bool asymOnly = c->smoother == CFX_SMOOTH_DILU || c->smoother == CFX_SMOOTH_DILUGS;
@@ -1100,7 +1241,8 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
                       names[c->smoother]);
             return CFX_ERR_CONFIG;
         }
-    } else {
+    }
+    if (c->solver != CFX_SOLVER_GAMG && c->solver != CFX_SOLVER_SMOOTH) {
         if (c->preconditioner == CFX_PRE_DIC && !mat->sym) {
             set_error("Unknown asymmetric matrix preconditioner DIC");
             return CFX_ERR_CONFIG;
@@ -1139,6 +1281,9 @@ void cfx_default_controls(cfx_controls* c) {
     c->nCellsInCoarsestLevel = 10;
     c->precision = CFX_FP64;
     c->nSweeps = 1;
+    c->nVcycles = 2;
+    c->pcTolerance = 1e-6;
+    c->pcRelTol = 0.0;
 }
 
 const char* cfx_last_error(void) { return cfx::last_error(); }
@@ -1359,6 +1504,7 @@ cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* diag, const d
 cfx_status cfx_matrix_destroy(cfx_matrix* mat) {
     if (!mat) return CFX_ERR_ARG;
     cudaStreamSynchronize(mat->mesh->ctx->stream);
+    pc_gamg_free(mat->pcGamg);
     delete mat;
     return CFX_OK;
 }

@@ -31,7 +31,7 @@ from . import LIB_DIR
 LIB_PATH = os.path.join(LIB_DIR, "libcudaLduSolvers.so")
 
 SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG, SOLVER_SMOOTH = 0, 1, 2, 3
-PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3, "GAMG": 4}
 SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "symGaussSeidel": 2, "DILU": 3, "DICGaussSeidel": 4,
              "DILUGaussSeidel": 5}
 # the smoothers' run-time tables by matrix symmetry
@@ -72,7 +72,8 @@ class Controls(ctypes.Structure):
                 ("nPostSweeps", ctypes.c_int), ("postSweepsLevelMultiplier", ctypes.c_int),
                 ("maxPostSweeps", ctypes.c_int), ("nFinestSweeps", ctypes.c_int),
                 ("scaleCorrection", ctypes.c_int), ("nCellsInCoarsestLevel", ctypes.c_int),
-                ("precision", ctypes.c_int), ("nSweeps", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("nSweeps", ctypes.c_int), ("nVcycles", ctypes.c_int),
+                ("pad", ctypes.c_int), ("pcTolerance", ctypes.c_double), ("pcRelTol", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -459,19 +460,28 @@ def _controls(d, sym):
         kind = "symmetric" if sym else "asymmetric"
         raise FatalError(f"Unknown {kind} matrix solver {name}\n\nValid {kind} matrix solvers are : {list(table)}")
     c.solver = SOLVERS[name]
-    if c.solver != SOLVER_GAMG:
+    gd = d  # the dictionary of the GAMG keys (the solver's, or the GAMG preconditioner's)
+    if c.solver not in (SOLVER_GAMG, SOLVER_SMOOTH):
         pre = d.get("preconditioner", "none")
+        pd = None
         if isinstance(pre, dict):
+            pd = pre
             pre = pre.get("preconditioner", "none")
-        if pre not in PRECONDITIONERS:
+        if pre not in PRECONDITIONERS or (pre == "GAMG" and pd is None):
             raise FatalError(f"Unknown {'symmetric' if sym else 'asymmetric'} matrix preconditioner {pre}")
         c.preconditioner = PRECONDITIONERS[pre]
+        if pre == "GAMG":
+            gd = pd
+            c.nVcycles = int(pd.get("nVcycles", 2))
+            c.pcTolerance = float(pd.get("tolerance", 1e-6))
+            c.pcRelTol = float(pd.get("relTol", 0.0))
     c.tolerance = float(d.get("tolerance", 1e-6))
     c.relTol = float(d.get("relTol", 0.0))
     c.maxIter = int(d.get("maxIter", 1000))
     c.minIter = int(d.get("minIter", 0))
-    sm = d.get("smoother", "GaussSeidel")
-    if c.solver in (SOLVER_GAMG, SOLVER_SMOOTH) and sm not in (SYM_SMOOTHERS if sym else ASYM_SMOOTHERS):
+    sm = gd.get("smoother", "GaussSeidel")
+    uses_smoother = c.solver in (SOLVER_GAMG, SOLVER_SMOOTH) or c.preconditioner == PRECONDITIONERS["GAMG"]
+    if uses_smoother and sm not in (SYM_SMOOTHERS if sym else ASYM_SMOOTHERS):
         kind = "symmetric" if sym else "asymmetric"
         table = list(SYM_SMOOTHERS if sym else ASYM_SMOOTHERS)
         raise FatalError(f"Unknown {kind} matrix smoother {sm}\n\nValid {kind} matrix smoothers are : {table}")
@@ -479,16 +489,16 @@ def _controls(d, sym):
     c.nSweeps = int(d.get("nSweeps", 1))
     for k in ("nPreSweeps", "preSweepsLevelMultiplier", "maxPreSweeps", "nPostSweeps",
               "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "nCellsInCoarsestLevel"):
-        if k in d:
-            setattr(c, k, int(d[k]))
-    if "minCellsPerProcessor" in d:
-        c.nCellsInCoarsestLevel = int(d["minCellsPerProcessor"])
-    if "scaleCorrection" in d:
-        c.scaleCorrection = int(bool(d["scaleCorrection"]))
-    if d.get("interpolateCorrection", False):
+        if k in gd:
+            setattr(c, k, int(gd[k]))
+    if "minCellsPerProcessor" in gd:
+        c.nCellsInCoarsestLevel = int(gd["minCellsPerProcessor"])
+    if "scaleCorrection" in gd:
+        c.scaleCorrection = int(bool(gd["scaleCorrection"]))
+    if gd.get("interpolateCorrection", False):
         raise FatalError("interpolateCorrection is not supported by cudaGAMG")
-    if d.get("agglomerator", "faceAreaPair") != "faceAreaPair":
-        raise FatalError(f"Unknown GAMGAgglomeration type {d['agglomerator']}")
+    if gd.get("agglomerator", "faceAreaPair") != "faceAreaPair":
+        raise FatalError(f"Unknown GAMGAgglomeration type {gd['agglomerator']}")
     prec = str(d.get("precision", "FP64"))
     if prec not in ("FP64", "mixed"):
         raise FatalError(f"Unknown precision {prec} (FP64 or mixed)")
@@ -550,8 +560,11 @@ def solve(s, psi, controls, field="psi"):
     """Solve system dict s (cases.py layout) with a controls dict."""
     mesh, A = system_matrix(s)
     name = controls["solver"]
-    if SOLVERS.get(name) == SOLVER_GAMG:
-        key = ("faceAreaPair", int(controls.get("nCellsInCoarsestLevel", 10)))
+    pre = controls.get("preconditioner")
+    gd = pre if isinstance(pre, dict) and pre.get("preconditioner") == "GAMG" else None
+    if SOLVERS.get(name) == SOLVER_GAMG or gd is not None:
+        src = gd if gd is not None else controls
+        key = ("faceAreaPair", int(src.get("nCellsInCoarsestLevel", 10)))
         if mesh.gamg_key != key:
             mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=key[1])
     return solver_new(field, A, controls).solve(psi, s["source"])

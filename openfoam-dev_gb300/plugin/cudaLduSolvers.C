@@ -148,6 +148,41 @@ protected:
         return e;
     }
 
+    //- The preconditioner's dictionary when it is given as one (the
+    //  "preconditioner { preconditioner GAMG; ... }" form read by
+    //  lduMatrix::preconditioner::getName, lduMatrixPreconditioner.C:38-58)
+    const dictionary* preconditionerDict() const
+    {
+        return controlDict_.isDict("preconditioner")
+            ? &controlDict_.subDict("preconditioner")
+            : nullptr;
+    }
+
+    //- The GAMG hierarchy of the entry from the reference's own
+    //  agglomeration (faceAreaPair on an fvMesh), cached in the mesh
+    //  registry (GAMGAgglomeration.C:349-400); its restriction maps define
+    //  the device levels.
+    void gamgLevels(Entry& e, const dictionary& gamgDict) const
+    {
+        if (e.gamg) return;
+        const GAMGAgglomeration& agg =
+            GAMGAgglomeration::New(matrix_, gamgDict);
+        const label nLevels = agg.size();
+        List<const label*> maps(nLevels);
+        labelList nCoarse(nLevels);
+        for (label i = 0; i < nLevels; i++)
+        {
+            maps[i] = agg.restrictAddressing(i).cdata();
+            nCoarse[i] = agg.nCells(i);
+        }
+        check
+        (
+            cfx_gamg_set_levels(e.mesh, nLevels, maps.cdata(), nCoarse.cdata()),
+            "cfx_gamg_set_levels"
+        );
+        e.gamg = true;
+    }
+
     cfx_controls controls(int solverType) const
     {
         cfx_controls c;
@@ -157,18 +192,34 @@ protected:
         c.relTol = relTol_;
         c.maxIter = maxIter_;
         c.minIter = minIter_;
+        const dictionary* pd = preconditionerDict();
         const word pre
         (
-            controlDict_.lookupOrDefault<word>("preconditioner", "none")
+            pd
+          ? pd->lookup<word>("preconditioner")
+          : controlDict_.lookupOrDefault<word>("preconditioner", "none")
         );
         c.preconditioner =
             pre == "DIC" ? CFX_PRE_DIC
           : pre == "DILU" ? CFX_PRE_DILU
           : pre == "diagonal" ? CFX_PRE_DIAGONAL
+          : pre == "GAMG" ? CFX_PRE_GAMG
           : CFX_PRE_NONE;
+        // the GAMG keys: the solver's own, or the GAMG preconditioner's
+        // (GAMGPreconditioner.C:40-79: nVcycles, its tolerance and relTol)
+        const bool pcGamg =
+            pd && c.preconditioner == CFX_PRE_GAMG
+         && solverType != CFX_SOLVER_GAMG;
+        const dictionary& gd = pcGamg ? *pd : controlDict_;
+        if (pcGamg)
+        {
+            c.nVcycles = gd.lookupOrDefault<label>("nVcycles", 2);
+            c.pcTolerance = gd.lookupOrDefault<scalar>("tolerance", 1e-6);
+            c.pcRelTol = gd.lookupOrDefault<scalar>("relTol", 0);
+        }
         const word sm
         (
-            controlDict_.lookupOrDefault<word>("smoother", "GaussSeidel")
+            gd.lookupOrDefault<word>("smoother", "GaussSeidel")
         );
         c.smoother =
             sm == "DIC" ? CFX_SMOOTH_DIC
@@ -178,17 +229,17 @@ protected:
           : sm == "DILUGaussSeidel" ? CFX_SMOOTH_DILUGS
           : CFX_SMOOTH_GS;
         c.nSweeps = controlDict_.lookupOrDefault<label>("nSweeps", 1);
-        c.nPreSweeps = controlDict_.lookupOrDefault<label>("nPreSweeps", 0);
+        c.nPreSweeps = gd.lookupOrDefault<label>("nPreSweeps", 0);
         c.preSweepsLevelMultiplier =
-            controlDict_.lookupOrDefault<label>("preSweepsLevelMultiplier", 1);
-        c.maxPreSweeps = controlDict_.lookupOrDefault<label>("maxPreSweeps", 4);
-        c.nPostSweeps = controlDict_.lookupOrDefault<label>("nPostSweeps", 2);
+            gd.lookupOrDefault<label>("preSweepsLevelMultiplier", 1);
+        c.maxPreSweeps = gd.lookupOrDefault<label>("maxPreSweeps", 4);
+        c.nPostSweeps = gd.lookupOrDefault<label>("nPostSweeps", 2);
         c.postSweepsLevelMultiplier =
-            controlDict_.lookupOrDefault<label>("postSweepsLevelMultiplier", 1);
-        c.maxPostSweeps = controlDict_.lookupOrDefault<label>("maxPostSweeps", 4);
-        c.nFinestSweeps = controlDict_.lookupOrDefault<label>("nFinestSweeps", 2);
+            gd.lookupOrDefault<label>("postSweepsLevelMultiplier", 1);
+        c.maxPostSweeps = gd.lookupOrDefault<label>("maxPostSweeps", 4);
+        c.nFinestSweeps = gd.lookupOrDefault<label>("nFinestSweeps", 2);
         c.scaleCorrection =
-            controlDict_.lookupOrDefault<bool>
+            gd.lookupOrDefault<bool>
             (
                 "scaleCorrection", matrix_.symmetric()
             );
@@ -311,7 +362,9 @@ solverPerformance cudaPCG::solve
 ) const
 {
     Entry& e = deviceMatrix();
-    return run(e, controls(CFX_SOLVER_PCG), psi, source);
+    const cfx_controls c = controls(CFX_SOLVER_PCG);
+    if (c.preconditioner == CFX_PRE_GAMG) gamgLevels(e, *preconditionerDict());
+    return run(e, c, psi, source);
 }
 
 
@@ -323,7 +376,9 @@ solverPerformance cudaPBiCGStab::solve
 ) const
 {
     Entry& e = deviceMatrix();
-    return run(e, controls(CFX_SOLVER_PBICGSTAB), psi, source);
+    const cfx_controls c = controls(CFX_SOLVER_PBICGSTAB);
+    if (c.preconditioner == CFX_PRE_GAMG) gamgLevels(e, *preconditionerDict());
+    return run(e, c, psi, source);
 }
 
 
@@ -347,28 +402,7 @@ solverPerformance cudaGAMG::solve
 ) const
 {
     Entry& e = deviceMatrix();
-    if (!e.gamg)
-    {
-        // The reference's own agglomeration (faceAreaPair on an fvMesh),
-        // cached in the mesh registry (GAMGAgglomeration.C:349-400); its
-        // restriction maps define the device hierarchy.
-        const GAMGAgglomeration& agg =
-            GAMGAgglomeration::New(matrix_, controlDict_);
-        const label nLevels = agg.size();
-        List<const label*> maps(nLevels);
-        labelList nCoarse(nLevels);
-        for (label i = 0; i < nLevels; i++)
-        {
-            maps[i] = agg.restrictAddressing(i).cdata();
-            nCoarse[i] = agg.nCells(i);
-        }
-        check
-        (
-            cfx_gamg_set_levels(e.mesh, nLevels, maps.cdata(), nCoarse.cdata()),
-            "cfx_gamg_set_levels"
-        );
-        e.gamg = true;
-    }
+    gamgLevels(e, controlDict_);
     return run(e, controls(CFX_SOLVER_GAMG), psi, source);
 }
 

@@ -251,3 +251,42 @@ def test_smooth_solver_every_form(smoother):
         assert abs(perf.nIterations - rp.nIterations) <= 2, (form, perf.nIterations, rp.nIterations)
         if perf.nIterations == rp.nIterations:
             np.testing.assert_array_equal(psi, ref)
+
+
+@pytest.mark.parametrize("smoother", ["GaussSeidel", "DIC"])
+def test_pcg_gamg_preconditioner_every_form(smoother):
+    """PCG with the GAMG preconditioner (2 V-cycles per application) on a
+    jittered 16^3 cube in every sweep form against the oracle's GAMGPCG."""
+    s = cases.gamg_cube(16, jitter=0.2, seed=6)
+    ref = np.zeros_like(s["source"])
+    rp = orc.pcg_gamg(s, ref, tol=1e-9, smoother=smoother, nVcycles=2, pre_tol=1e-6)
+    for form in sorted(FORMS):
+        with sweep_form(form):
+            s2 = cases.gamg_cube(16, jitter=0.2, seed=6)
+            psi = np.zeros_like(s2["source"])
+            perf = ldu.solve(s2, psi, {"solver": "cudaPCG", "tolerance": 1e-9, "relTol": 0,
+                                       "preconditioner": {"preconditioner": "GAMG", "smoother": smoother,
+                                                          "nVcycles": 2}})
+        assert perf.solverName == "GAMGPCG" and perf.converged, form
+        assert abs(perf.nIterations - rp.nIterations) <= 1, (form, perf.nIterations, rp.nIterations)
+        assert _rel(psi, ref) <= (RTOL_FP64 if perf.nIterations == rp.nIterations else 1e-6), form
+
+
+def test_gamg_preconditioner_mixed_and_asymmetric():
+    """GAMGPCG with FP32 inner V-cycles reaches the FP64 tolerance; PBiCGStab
+    with the GAMG preconditioner (coarsest level by PBiCGStab+DILU) solves
+    the asymmetric upwind system to its tolerance."""
+    s = cases.gamg_cube(16, jitter=0.2, seed=7)
+    psi = np.zeros_like(s["source"])
+    ctl = {"solver": "cudaPCG", "tolerance": 1e-9, "relTol": 0, "precision": "mixed",
+           "preconditioner": {"preconditioner": "GAMG", "smoother": "GaussSeidel"}}
+    perf = ldu.solve(s, psi, ctl)
+    assert perf.converged and perf.solverName == "GAMGPCG"
+    _residual_ok(s, psi, 1e-9)
+    cd = cases.convection_diffusion(cases.box_mesh(14, 12, 10, jitter=0.1, seed=8), [1.0, 0.3, 0.2], 5e-2)
+    cd["source"] = cases.uniform(31, cd["diag"].size)
+    psi = np.zeros_like(cd["source"])
+    perf = ldu.solve(cd, psi, {"solver": "cudaPBiCGStab", "tolerance": 1e-9, "relTol": 0, "maxIter": 500,
+                               "preconditioner": {"preconditioner": "GAMG", "smoother": "GaussSeidel"}})
+    assert perf.converged and perf.solverName == "GAMGPBiCGStab"
+    _residual_ok(cd, psi, 1e-9)

@@ -78,6 +78,27 @@ def test_controls_parse():
     assert c.nPreSweeps == 2 and c.smoother == 1 and c.precision == 1 and c.nCellsInCoarsestLevel == 20
 
 
+def test_gamg_preconditioner_controls_parse():
+    """The GAMG preconditioner's keys come from its own dictionary
+    (GAMGPreconditioner.C:40-79): nVcycles (default 2), its tolerance
+    (default 1e-6) and relTol, the smoother and sweeps; the solver's own
+    tolerance stays the outer one."""
+    s = ldu.solver_new("p", _FakeMatrix(True), {
+        "solver": "cudaPCG", "tolerance": 1e-9, "nPreSweeps": 3,
+        "preconditioner": {"preconditioner": "GAMG", "smoother": "DICGaussSeidel", "nPreSweeps": 1,
+                           "tolerance": 1e-4, "nVcycles": 1}})
+    c = s.c
+    assert c.preconditioner == ldu.PRECONDITIONERS["GAMG"] and c.tolerance == 1e-9
+    assert (c.pcTolerance, c.pcRelTol, c.nVcycles, c.smoother, c.nPreSweeps) == (1e-4, 0.0, 1, 4, 1)
+    c = ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaPCG",
+                                                "preconditioner": {"preconditioner": "GAMG"}}).c
+    assert (c.pcTolerance, c.nVcycles, c.smoother) == (1e-6, 2, 0)
+    # the word form has no dictionary for the GAMG keys (the reference
+    # constructs GAMGPreconditioner from an empty one): refused here
+    with pytest.raises(ldu.FatalError, match="preconditioner GAMG"):
+        ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaPCG", "preconditioner": "GAMG"})
+
+
 def test_solver_performance_print_format():
     p = ldu.SolverPerformance("DICPCG", "T", 1.0, 5e-9, 32, True, False)
     assert str(p) == "DICPCG:  Solving for T, Initial residual = 1, Final residual = 5e-09, No Iterations 32"

@@ -38,7 +38,8 @@ typedef enum {
     CFX_ERR_ADMISSION = -5,   /* request exceeds the server's HBM budget */
     CFX_ERR_TIMEOUT = -6,     /* a bounded device wait expired */
     CFX_ERR_CONFIG = -7,      /* unknown solver/preconditioner/smoother name */
-    CFX_ERR_STATE = -8        /* call out of order (e.g. GAMG without levels) */
+    CFX_ERR_STATE = -8,       /* call out of order (e.g. GAMG without levels) */
+    CFX_ERR_FATAL = -9        /* the reference's FatalError (e.g. "Singular matrix") */
 } cfx_status;
 
 typedef struct cfx_ctx cfx_ctx;        /* device, stream, scratch */
@@ -97,9 +98,15 @@ typedef struct {
     /* GAMG preconditioner: V-cycles per application (default 2) and its own
      * tolerance / relTol (its coarsest-level solves; defaults 1e-6, 0) */
     int nVcycles;
-    int pad;
+    /* GAMG: interpolateCorrection (GAMGSolverInterpolate.C:30-130; default 0) */
+    int interpolateCorrection;
     double pcTolerance;
     double pcRelTol;
+    /* GAMG: directSolveCoarsest - the coarsest level by a dense LU with
+     * implicit partial pivoting (LUscalarMatrix, GAMGSolver.C:257-267;
+     * default 0); a singular coarsest matrix is CFX_ERR_FATAL */
+    int directSolveCoarsest;
+    int reserved;
 } cfx_controls;
 
 void cfx_default_controls(cfx_controls* c);

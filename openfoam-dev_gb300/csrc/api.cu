@@ -103,6 +103,8 @@ struct cfx_matrix {
     std::vector<LevelPack<float>> p32;
     BlockSys<double>* d_blk64 = nullptr;
     BlockSys<float>* d_blk32 = nullptr;
+    int* luPiv = nullptr;  // directSolveCoarsest pivots
+    int luPivN = 0;
     GraphCache gPCG, gBiCG, gGAMG, gMixed;
 };
 
@@ -579,6 +581,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.nPostSweeps), uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps),
                       uint64_t(ctl.maxPostSweeps), uint64_t(ctl.preSweepsLevelMultiplier),
                       uint64_t(ctl.postSweepsLevelMultiplier), uint64_t(ctl.scaleCorrection + 7),
+                      uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
     const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
@@ -722,6 +725,9 @@ struct GamgCycle {
     const cfx_controls* ctl;
     int coarsest;         // index of the coarsest coarse level li (matrix level coarsest+1)
     bool scaleCorr;
+    bool interp;  // interpolateCorrection
+    T* lu = nullptr;  // directSolveCoarsest: the factorised coarsest matrix
+    int* piv = nullptr;
     std::vector<T*> corr, src;
     T *Apsi, *fcorr, *scratch2;
     BlockSys<T>* d_blk;
@@ -750,8 +756,13 @@ struct GamgCycle {
         }
         // solveCoarsestLevel (GAMGSolverSolve.C:520-552): PCG+DIC or
         // PBiCGStab+DILU from zero at the GAMG tolerances, one CTA.
-        Kern<T>::fill(s, mesh->dev[coarsest + 1].n, T(0), corr[coarsest], nullptr);
-        Kern<T>::block_solve(s, d_blk, 1, nullptr);
+        if (lu) {
+            // LUscalarMatrix::solve (LUscalarMatrixTemplates.C:29-139)
+            Ops<T>::lu_solve(s, mesh->dev[coarsest + 1].n, lu, piv, src[coarsest], corr[coarsest]);
+        } else {
+            Kern<T>::fill(s, mesh->dev[coarsest + 1].n, T(0), corr[coarsest], nullptr);
+            Kern<T>::block_solve(s, d_blk, 1, nullptr);
+        }
         for (int li = coarsest - 1; li >= 0; --li) {
             const int lv = li + 1;
             const int nc = mesh->dev[lv].n;
@@ -761,7 +772,8 @@ struct GamgCycle {
                 pre = scratch2;
             }
             Ops<T>::prolong_field(s, mesh->dev[lv], corr[li + 1], corr[li]);
-            if (scaleCorr && li < coarsest - 1) {
+            if (interp) Ops<T>::interpolate(s, mesh->dev[lv], coeffs<T>(mat, lv), corr[li], Apsi, corr[li + 1]);
+            if (scaleCorr && (interp || li < coarsest - 1)) {
                 scale<T>(ctx, mat, lv, corr[li], Apsi, src[li], pre, st);
             } else if (pre) {
                 Kern<T>::axpy(s, nc, T(1), pre, corr[li], nullptr);
@@ -771,6 +783,7 @@ struct GamgCycle {
                       workFor(lv));
         }
         Ops<T>::prolong_field(s, mesh->dev[0], corr[0], fcorr);
+        if (interp) Ops<T>::interpolate(s, mesh->dev[0], coeffs<T>(mat, 0), fcorr, Apsi, corr[0]);
         if (scaleCorr) scale<T>(ctx, mat, 0, fcorr, Apsi, fres, nullptr, st);
     }
 
@@ -812,6 +825,7 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     cy.ctl = ctl;
     cy.coarsest = nl - 2;
     cy.scaleCorr = ctl->scaleCorrection < 0 ? mat->sym : ctl->scaleCorrection != 0;
+    cy.interp = ctl->interpolateCorrection != 0;
     cy.st = st;
     int maxSize = 0;
     for (int i = 0; i < nl; ++i) maxSize = std::max(maxSize, mesh->dev[i].n);
@@ -849,6 +863,28 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     const int lc = nl - 1;
     const LevelMesh& m = mesh->dev[lc];
     LevelCoeffs<T>& c = coeffs<T>(mat, lc);
+    cy.lu = nullptr;
+    cy.piv = nullptr;
+    if (ctl->directSolveCoarsest) {
+        // GAMGSolver.C:257-267: the coarsest matrix factorised once per
+        // solver construction (here: per solve), in the cycle's precision
+        if (m.n > 8192) throw StatusError(CFX_ERR_CONFIG, "directSolveCoarsest: the coarsest level has more "
+                                                          "than 8192 cells");
+        cy.lu = W.get(G0 + 700, m.n * m.n);
+        T* vv = W.get(G0 + 701, m.n);
+        if (mat->luPivN < m.n) {
+            mat->luPiv = mat->arena.get<int>(m.n);
+            mat->luPivN = m.n;
+        }
+        cy.piv = mat->luPiv;
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s));
+        Ops<T>::lu_factor(s, m, c, cy.lu, vv, cy.piv, ctx->d_status);
+        if (read_status(ctx) == CFX_ERR_FATAL) {
+            CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s));
+            throw StatusError(CFX_ERR_FATAL, "Singular matrix");
+        }
+        return;
+    }
     compute_rD<T>(mat, lc);  // coarsest PCG+DIC / PBiCGStab+DILU
     BlockSys<T> h{};
     h.n = m.n;
@@ -1003,7 +1039,9 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
-                         uint64_t(ctl.scaleCorrection + 7), uint64_t(mixed), reinterpret_cast<uint64_t>(psi),
+                         uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
+                         uint64_t(ctl.directSolveCoarsest), uint64_t(mixed),
+                         reinterpret_cast<uint64_t>(psi),
                          reinterpret_cast<uint64_t>(b)});
     SolveState h = read_state(ctx, 0);
     if (!mixed) {

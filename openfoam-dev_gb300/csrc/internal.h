@@ -140,6 +140,17 @@ struct Ops {
     static void prolong_field(cudaStream_t s, const LevelMesh& fine, const T* cf, T* ff);
     // rD = 1/rD
     static void reciprocal(cudaStream_t s, int n, T* x);
+    // GAMGSolver::interpolate: psi = -(A - D) psi / D on the fine level,
+    // then each coarse cell's diagonal-weighted mean replaced by psiC
+    // (Apsi: scratch of the fine level's size)
+    static void interpolate(cudaStream_t s, const LevelMesh& fine, const LevelCoeffs<T>& a, T* psi, T* Apsi,
+                            const T* psiC);
+    // LUscalarMatrix of the level (dense, row-major A[n*n], pivots piv[n];
+    // vv: scratch [n]); *status = CFX_ERR_FATAL for an all-zero row
+    static void lu_factor(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, T* A, T* vv, int* piv,
+                          int* status);
+    // x = LU^-1 b (LUscalarMatrix::solve)
+    static void lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T* b, T* x);
 };
 
 void launch_cast_d2f(cudaStream_t s, int64_t n, const double* in, float* out);

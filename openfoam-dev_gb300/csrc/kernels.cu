@@ -11,6 +11,8 @@
 // with --fmad=false, so every result equals the reference's sequential loop
 // bit for bit.
 
+#include <cfloat>
+
 #include "device.cuh"
 #include "internal.h"
 #include "solvers.h"
@@ -155,6 +157,185 @@ __global__ void prolong_k(int n, const int* __restrict__ ra, const T* __restrict
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) ff[i] = cf[ra[i]];
 }
 
+// GAMGSolver::interpolate, first part (GAMGSolverInterpolate.C:30-79): the
+// off-diagonal product (A - D) psi from zero, in the per-cell face order of
+// the reference's face loop (neighbour faces in losort order, then owned).
+template <class T>
+__global__ void offdiag_amul_k(int n, const int* __restrict__ ownerStart, const int* __restrict__ losortStart,
+                               const int* __restrict__ losortL, const int* __restrict__ u,
+                               const T* __restrict__ lp, const T* __restrict__ upper, const T* __restrict__ x,
+                               T* __restrict__ y) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        T acc = T(0);
+        const int k1 = losortStart[c + 1];
+        for (int k = losortStart[c]; k < k1; ++k) acc += lp[k] * x[losortL[k]];
+        const int f1 = ownerStart[c + 1];
+        for (int f = ownerStart[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
+        y[c] = acc;
+    }
+}
+
+// GAMGSolverInterpolate.C:69-127 for one coarse cell per thread, over its
+// fine cells in ascending order (the order the reference's cell loop adds
+// them in): psi = -Apsi/diag; corrC = psiC - sum(diag psi)/sum(diag);
+// psi += corrC.
+template <class T>
+__global__ void interp_coarse_k(int nc, const int* __restrict__ ccStart, const int* __restrict__ ccFine,
+                                const T* __restrict__ diag, const T* __restrict__ Apsi, const T* __restrict__ psiC,
+                                T* __restrict__ psi) {
+    for (int C = blockIdx.x * blockDim.x + threadIdx.x; C < nc; C += gridDim.x * blockDim.x) {
+        const int k0 = ccStart[C], k1 = ccStart[C + 1];
+        T corr = T(0), dg = T(0);
+        for (int k = k0; k < k1; ++k) {
+            const int c = ccFine[k];
+            const T d = diag[c];
+            const T p = -Apsi[c] / d;
+            psi[c] = p;
+            corr += d * p;
+            dg += d;
+        }
+        const T cc = psiC[C] - corr / dg;
+        for (int k = k0; k < k1; ++k) {
+            const int c = ccFine[k];
+            psi[c] = psi[c] + cc;
+        }
+    }
+}
+
+// LUscalarMatrix (LUscalarMatrix.C:205-266 convert, scalarMatrices.C:77-180
+// LUDecompose) of one level in one block: the dense row-major matrix, the
+// implicit row scaling, then Crout's column sweep with partial pivoting.
+// Every sum runs in one thread in the reference's k order; the parallel
+// parts (assembly, row scales, rows j..n-1 of a column, the row swap and
+// the column scaling) touch disjoint entries.  An all-zero row sets
+// *status = CFX_ERR_FATAL ("Singular matrix") and stops.
+constexpr int LU_NT = 256;
+
+template <class T>
+__global__ void __launch_bounds__(LU_NT) lu_factor_k(int n, int nf, const int* __restrict__ l,
+                                                     const int* __restrict__ u, const T* __restrict__ diag,
+                                                     const T* __restrict__ upper, const T* __restrict__ lower,
+                                                     T* __restrict__ A, T* __restrict__ vv, int* __restrict__ piv,
+                                                     int* status) {
+    __shared__ int singular, pivRow;
+    const int t = threadIdx.x;
+    const size_t nn = size_t(n) * n;
+    for (size_t i = t; i < nn; i += LU_NT) A[i] = T(0);
+    if (t == 0) singular = 0;
+    __syncthreads();
+    for (int c = t; c < n; c += LU_NT) A[size_t(c) * n + c] = diag[c];
+    for (int f = t; f < nf; f += LU_NT) {
+        A[size_t(u[f]) * n + l[f]] = lower[f];
+        A[size_t(l[f]) * n + u[f]] = upper[f];
+    }
+    __syncthreads();
+    for (int i = t; i < n; i += LU_NT) {
+        T big = T(0);
+        for (int j = 0; j < n; ++j) {
+            const T v = fabs(A[size_t(i) * n + j]);
+            if (v > big) big = v;
+        }
+        if (big == T(0)) singular = 1;
+        vv[i] = T(1) / big;
+    }
+    __syncthreads();
+    if (singular) {
+        if (t == 0) *status = CFX_ERR_FATAL;
+        return;
+    }
+    const T small = sizeof(T) == 8 ? T(DBL_EPSILON) : T(FLT_EPSILON);
+    for (int j = 0; j < n; ++j) {
+        if (t == 0) {
+            // rows above the diagonal: row i reads rows k < i of this column
+            for (int i = 0; i < j; ++i) {
+                T sum = A[size_t(i) * n + j];
+                for (int k = 0; k < i; ++k) sum -= A[size_t(i) * n + k] * A[size_t(k) * n + j];
+                A[size_t(i) * n + j] = sum;
+            }
+        }
+        __syncthreads();
+        for (int i = j + t; i < n; i += LU_NT) {
+            T sum = A[size_t(i) * n + j];
+            for (int k = 0; k < j; ++k) sum -= A[size_t(i) * n + k] * A[size_t(k) * n + j];
+            A[size_t(i) * n + j] = sum;
+        }
+        __syncthreads();
+        if (t == 0) {
+            // the last row of largest scaled magnitude (>=, as the reference)
+            int iMax = 0;
+            T big = T(0);
+            for (int i = j; i < n; ++i) {
+                const T v = vv[i] * fabs(A[size_t(i) * n + j]);
+                if (v >= big) {
+                    big = v;
+                    iMax = i;
+                }
+            }
+            piv[j] = iMax;
+            if (iMax != j) vv[iMax] = vv[j];
+            pivRow = iMax;
+        }
+        __syncthreads();
+        const int iMax = pivRow;
+        if (iMax != j) {
+            for (int k = t; k < n; k += LU_NT) {
+                const T a = A[size_t(j) * n + k];
+                A[size_t(j) * n + k] = A[size_t(iMax) * n + k];
+                A[size_t(iMax) * n + k] = a;
+            }
+        }
+        __syncthreads();
+        T d = A[size_t(j) * n + j];
+        if (d == T(0)) d = small;
+        __syncthreads();
+        if (t == 0) A[size_t(j) * n + j] = d;
+        if (j != n - 1) {
+            const T rDiag = T(1) / d;
+            for (int i = j + 1 + t; i < n; i += LU_NT) A[size_t(i) * n + j] *= rDiag;
+        }
+        __syncthreads();
+    }
+}
+
+// LUBacksubstitute (scalarMatricesTemplates.C:117-163) in one thread, the
+// factors staged in shared memory when they fit (SH).
+template <class T, bool SH>
+__global__ void lu_solve_k(int n, const T* __restrict__ LUg, const int* __restrict__ piv, const T* __restrict__ b,
+                           T* __restrict__ x) {
+    extern __shared__ __align__(16) unsigned char lu_smem[];
+    T* LUs = reinterpret_cast<T*>(lu_smem);
+    T* xs = LUs + size_t(n) * n;
+    if (SH) {
+        for (size_t i = threadIdx.x; i < size_t(n) * n; i += blockDim.x) LUs[i] = LUg[i];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = b[i];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const T* LU = SH ? LUs : LUg;
+    T* X = SH ? xs : x;
+    if (!SH)
+        for (int i = 0; i < n; ++i) X[i] = b[i];
+    int ii = 0;
+    for (int i = 0; i < n; ++i) {
+        const int ip = piv[i];
+        T sum = X[ip];
+        X[ip] = X[i];
+        if (ii != 0) {
+            for (int j = ii - 1; j < i; ++j) sum -= LU[size_t(i) * n + j] * X[j];
+        } else if (sum != T(0)) {
+            ii = i + 1;
+        }
+        X[i] = sum;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        T sum = X[i];
+        for (int j = i + 1; j < n; ++j) sum -= LU[size_t(i) * n + j] * X[j];
+        X[i] = sum / LU[size_t(i) * n + i];
+    }
+    if (SH)
+        for (int i = 0; i < n; ++i) x[i] = X[i];
+}
+
 template <class T>
 __global__ void reciprocal_k(int n, T* x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = T(1) / x[i];
@@ -259,6 +440,34 @@ void Ops<T>::restrict_field(cudaStream_t s, const LevelMesh& f, const T* ff, T* 
 template <class T>
 void Ops<T>::prolong_field(cudaStream_t s, const LevelMesh& f, const T* cf, T* ff) {
     prolong_k<T><<<grid_for(f.n), RED_NT, 0, s>>>(f.n, f.restrictAddr, cf, ff);
+    count_launch();
+}
+
+template <class T>
+void Ops<T>::interpolate(cudaStream_t s, const LevelMesh& f, const LevelCoeffs<T>& a, T* psi, T* Apsi,
+                         const T* psiC) {
+    offdiag_amul_k<T><<<grid_all(f.n), RED_NT, 0, s>>>(f.n, f.ownerStart, f.losortStart, f.losortL, f.u,
+                                                       a.lowerPerm, a.upper, psi, Apsi);
+    interp_coarse_k<T><<<grid_for(f.nCoarse), RED_NT, 0, s>>>(f.nCoarse, f.coarseCellStart, f.coarseCellFine,
+                                                             a.diag, Apsi, psiC, psi);
+    count_launch(2);
+}
+
+template <class T>
+void Ops<T>::lu_factor(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, T* A, T* vv, int* piv,
+                       int* status) {
+    lu_factor_k<T><<<1, LU_NT, 0, s>>>(m.n, m.nf, m.l, m.u, a.diag, a.upper, a.sym ? a.upper : a.lower, A, vv, piv,
+                                       status);
+    count_launch();
+}
+
+template <class T>
+void Ops<T>::lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T* b, T* x) {
+    const size_t sm = (size_t(n) * n + n) * sizeof(T);
+    if (sm <= 48 * 1024)
+        lu_solve_k<T, true><<<1, 128, sm, s>>>(n, A, piv, b, x);
+    else
+        lu_solve_k<T, false><<<1, 32, 0, s>>>(n, A, piv, b, x);
     count_launch();
 }
 

@@ -20,6 +20,13 @@ struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// An error the reference reports as FatalError (or another fixed status),
+// raised from deep inside a solve's set-up.
+struct StatusError : std::runtime_error {
+    cfx_status status;
+    StatusError(cfx_status st, const std::string& what) : std::runtime_error(what), status(st) {}
+};
+
 inline void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {
         if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
@@ -96,6 +103,9 @@ inline cfx_status guard(F&& f) {
     } catch (const CudaError& e) {
         set_error(e.what());
         return CFX_ERR_CUDA;
+    } catch (const StatusError& e) {
+        set_error(e.what());
+        return e.status;
     } catch (const std::exception& e) {
         set_error(e.what());
         return CFX_ERR_ARG;

@@ -73,7 +73,8 @@ class Controls(ctypes.Structure):
                 ("maxPostSweeps", ctypes.c_int), ("nFinestSweeps", ctypes.c_int),
                 ("scaleCorrection", ctypes.c_int), ("nCellsInCoarsestLevel", ctypes.c_int),
                 ("precision", ctypes.c_int), ("nSweeps", ctypes.c_int), ("nVcycles", ctypes.c_int),
-                ("pad", ctypes.c_int), ("pcTolerance", ctypes.c_double), ("pcRelTol", ctypes.c_double)]
+                ("interpolateCorrection", ctypes.c_int), ("pcTolerance", ctypes.c_double),
+                ("pcRelTol", ctypes.c_double), ("directSolveCoarsest", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -201,7 +202,7 @@ def exported_symbols():
 def _check(rc, what=""):
     if rc != 0:
         msg = lib().cfx_last_error().decode(errors="replace")
-        if rc == -7:
+        if rc in (-7, -9):
             raise FatalError(msg)
         raise CfxError(rc, f"{what}: {msg}")
 
@@ -495,8 +496,8 @@ def _controls(d, sym):
         c.nCellsInCoarsestLevel = int(gd["minCellsPerProcessor"])
     if "scaleCorrection" in gd:
         c.scaleCorrection = int(bool(gd["scaleCorrection"]))
-    if gd.get("interpolateCorrection", False):
-        raise FatalError("interpolateCorrection is not supported by cudaGAMG")
+    c.interpolateCorrection = int(bool(gd.get("interpolateCorrection", False)))
+    c.directSolveCoarsest = int(bool(gd.get("directSolveCoarsest", False)))
     if gd.get("agglomerator", "faceAreaPair") != "faceAreaPair":
         raise FatalError(f"Unknown GAMGAgglomeration type {gd['agglomerator']}")
     prec = str(d.get("precision", "FP64"))

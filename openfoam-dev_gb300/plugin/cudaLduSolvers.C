@@ -243,6 +243,10 @@ protected:
             (
                 "scaleCorrection", matrix_.symmetric()
             );
+        c.interpolateCorrection =
+            gd.lookupOrDefault<bool>("interpolateCorrection", false);
+        c.directSolveCoarsest =
+            gd.lookupOrDefault<bool>("directSolveCoarsest", false);
         c.precision =
             controlDict_.lookupOrDefault<word>("precision", "FP64") == "mixed"
           ? CFX_MIXED : CFX_FP64;

@@ -802,6 +802,8 @@ void ldu_gamg_default_controls(ldu_gamg_controls* g) {
     g->nFinestSweeps = 2;
     g->scaleCorrection = -1;
     g->smoother = LDU_SMOOTH_GS;
+    g->interpolateCorrection = 0;
+    g->directSolveCoarsest = 0;
 }
 
 typedef struct {
@@ -837,6 +839,82 @@ static int imin(int a, int b) { return a < b ? a : b; }
 /* The GAMG hierarchy of one solve: coarse matrices (GAMGSolver ctor,
  * GAMGSolver.C:204-206), the smoothers' reciprocal diagonals and the coarse
  * correction and source fields (initVcycle, GAMGSolverSolve.C:446-517). */
+int ldu_lu_decompose(int n, double* A, int* piv) {
+    double* vv = (double*)xmalloc(sizeof(double) * (n ? n : 1));
+    /* implicit scaling: 1 / the largest magnitude of each row */
+    for (int i = 0; i < n; ++i) {
+        double big = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double t = fabs(A[(size_t)i * n + j]);
+            if (t > big) big = t;
+        }
+        if (big == 0.0) {
+            free(vv);
+            return -1;
+        }
+        vv[i] = 1.0 / big;
+    }
+    for (int j = 0; j < n; ++j) {
+        /* U above the diagonal of column j, rows in ascending order */
+        for (int i = 0; i < j; ++i) {
+            double sum = A[(size_t)i * n + j];
+            for (int k = 0; k < i; ++k) sum -= A[(size_t)i * n + k] * A[(size_t)k * n + j];
+            A[(size_t)i * n + j] = sum;
+        }
+        /* the rest of the column; pivot: the last row of largest scaled magnitude */
+        int iMax = 0;
+        double big = 0.0;
+        for (int i = j; i < n; ++i) {
+            double sum = A[(size_t)i * n + j];
+            for (int k = 0; k < j; ++k) sum -= A[(size_t)i * n + k] * A[(size_t)k * n + j];
+            A[(size_t)i * n + j] = sum;
+            const double t = vv[i] * fabs(sum);
+            if (t >= big) {
+                big = t;
+                iMax = i;
+            }
+        }
+        piv[j] = iMax;
+        if (j != iMax) {
+            for (int k = 0; k < n; ++k) {
+                const double t = A[(size_t)j * n + k];
+                A[(size_t)j * n + k] = A[(size_t)iMax * n + k];
+                A[(size_t)iMax * n + k] = t;
+            }
+            vv[iMax] = vv[j];
+        }
+        if (A[(size_t)j * n + j] == 0.0) A[(size_t)j * n + j] = DBL_EPSILON;
+        if (j != n - 1) {
+            const double rDiag = 1.0 / A[(size_t)j * n + j];
+            for (int i = j + 1; i < n; ++i) A[(size_t)i * n + j] *= rDiag;
+        }
+    }
+    free(vv);
+    return 0;
+}
+
+void ldu_lu_backsubstitute(int n, const double* LU, const int* piv, double* x) {
+    /* forward: unit-lower L with the row interchanges; the first nonzero
+     * entry starts the sums (ii) */
+    int ii = 0;
+    for (int i = 0; i < n; ++i) {
+        const int ip = piv[i];
+        double sum = x[ip];
+        x[ip] = x[i];
+        if (ii != 0) {
+            for (int j = ii - 1; j < i; ++j) sum -= LU[(size_t)i * n + j] * x[j];
+        } else if (sum != 0.0) {
+            ii = i + 1;
+        }
+        x[i] = sum;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double sum = x[i];
+        for (int j = i + 1; j < n; ++j) sum -= LU[(size_t)i * n + j] * x[j];
+        x[i] = sum / LU[(size_t)i * n + i];
+    }
+}
+
 typedef struct {
     const ldu_matrix* m;
     const ldu_agglomeration* agg;
@@ -845,7 +923,23 @@ typedef struct {
     level_matrix* lv;
     double **corr, **src;
     double* rD0;
+    double* lu; /* directSolveCoarsest: the factorised coarsest matrix */
+    int* piv;
+    int singular;
 } gamg_hier;
+
+/* LUscalarMatrix::convert (LUscalarMatrix.C:205-266, no interfaces): the
+ * dense row-major matrix of an LDU matrix (lower = upper when symmetric). */
+static void lu_dense(const ldu_matrix* m, double* A) {
+    const int n = m->nCells;
+    const double* lower = m->lower ? m->lower : m->upper;
+    memset(A, 0, sizeof(double) * (size_t)n * n);
+    for (int c = 0; c < n; ++c) A[(size_t)c * n + c] = m->diag[c];
+    for (int f = 0; f < m->nFaces; ++f) {
+        A[(size_t)m->u[f] * n + m->l[f]] = lower[f];
+        A[(size_t)m->l[f] * n + m->u[f]] = m->upper[f];
+    }
+}
 
 static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeration* agg,
                        const ldu_gamg_controls* gc) {
@@ -890,6 +984,17 @@ static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeratio
         H->src[i] = (double*)xmalloc(sizeof(double) * agg->nCells[i]);
         H->lv[i].rD = smoother_rD(&H->lv[i].m, gc->smoother);
     }
+    H->lu = NULL;
+    H->piv = NULL;
+    H->singular = 0;
+    if (gc->directSolveCoarsest) {
+        const level_matrix* L = &H->lv[nl - 1];
+        const int nc = L->m.nCells;
+        H->lu = (double*)xmalloc(sizeof(double) * ((size_t)nc * nc + 1));
+        H->piv = (int*)xmalloc(sizeof(int) * (nc + 1));
+        lu_dense(&L->m, H->lu);
+        H->singular = ldu_lu_decompose(nc, H->lu, H->piv) != 0;
+    }
 }
 
 static void gamg_free(gamg_hier* H) {
@@ -906,6 +1011,35 @@ static void gamg_free(gamg_hier* H) {
     free(H->src);
     free(H->rD0);
     free(H->lv);
+    free(H->lu);
+    free(H->piv);
+}
+
+/* GAMGSolver::interpolate, GAMGSolverInterpolate.C:30-127: one Jacobi step
+ * psi = -(A - D) psi / D (the off-diagonal product from zero, in face
+ * order), then every coarse cell's diagonal-weighted mean of psi is replaced
+ * by psiC (ra: this level's restriction map, nCC coarse cells).  Apsi:
+ * scratch of m's size. */
+static void gamg_interpolate(const ldu_matrix* m, double* psi, double* Apsi, const int* ra, const double* psiC,
+                             int nCC) {
+    const int n = m->nCells;
+    const double* lower = m->lower ? m->lower : m->upper;
+    for (int c = 0; c < n; ++c) Apsi[c] = 0;
+    for (int f = 0; f < m->nFaces; ++f) {
+        Apsi[m->u[f]] += lower[f] * psi[m->l[f]];
+        Apsi[m->l[f]] += m->upper[f] * psi[m->u[f]];
+    }
+    for (int c = 0; c < n; ++c) psi[c] = -Apsi[c] / m->diag[c];
+    double* corrC = (double*)calloc(nCC ? nCC : 1, sizeof(double));
+    double* diagC = (double*)calloc(nCC ? nCC : 1, sizeof(double));
+    for (int c = 0; c < n; ++c) {
+        corrC[ra[c]] += m->diag[c] * psi[c];
+        diagC[ra[c]] += m->diag[c];
+    }
+    for (int k = 0; k < nCC; ++k) corrC[k] = psiC[k] - corrC[k] / diagC[k];
+    for (int c = 0; c < n; ++c) psi[c] += corrC[ra[c]];
+    free(corrC);
+    free(diagC);
 }
 
 /* GAMGSolver::Vcycle, GAMGSolverSolve.C:148-443: psi += the coarse-grid
@@ -941,7 +1075,11 @@ static void gamg_vcycle(gamg_hier* H, double* psi, const double* b, double* Apsi
         for (int k = 0; k < nc; ++k) src[li + 1][agg->restrictAddr[li + 1][k]] += src[li][k];
     }
     /* solveCoarsestLevel, GAMGSolverSolve.C:520-552 */
-    {
+    if (H->lu) {
+        /* LUscalarMatrix::solve: x = source, then the back-substitution */
+        memcpy(corr[coarsest], src[coarsest], sizeof(double) * agg->nCells[coarsest]);
+        ldu_lu_backsubstitute(agg->nCells[coarsest], H->lu, H->piv, corr[coarsest]);
+    } else {
         ldu_perf cp;
         for (int k = 0; k < agg->nCells[coarsest]; ++k) corr[coarsest][k] = 0;
         if (H->sym)
@@ -954,20 +1092,26 @@ static void gamg_vcycle(gamg_hier* H, double* psi, const double* b, double* Apsi
         double* pre = scratch2;
         if (gc->nPreSweeps) memcpy(pre, corr[li], sizeof(double) * nc);
         for (int k = 0; k < nc; ++k) corr[li][k] = corr[li + 1][agg->restrictAddr[li + 1][k]];
-        if (scaleCorrection && li < coarsest - 1) gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
+        if (gc->interpolateCorrection)
+            gamg_interpolate(&lv[li].m, corr[li], scratch1, agg->restrictAddr[li + 1], corr[li + 1],
+                             agg->nCells[li + 1]);
+        if (scaleCorrection && (gc->interpolateCorrection || li < coarsest - 1))
+            gamg_scale(&lv[li].m, corr[li], scratch1, src[li]);
         if (gc->nPreSweeps)
             for (int k = 0; k < nc; ++k) corr[li][k] += pre[k];
         smooth(&lv[li].m, lv[li].rD, gc->smoother, corr[li], src[li],
                imin(gc->nPostSweeps + gc->postSweepsLevelMultiplier * li, gc->maxPostSweeps));
     }
     for (int k = 0; k < n; ++k) finestCorrection[k] = corr[0][agg->restrictAddr[0][k]];
+    if (gc->interpolateCorrection)
+        gamg_interpolate(m, finestCorrection, Apsi, agg->restrictAddr[0], corr[0], agg->nCells[0]);
     if (scaleCorrection) gamg_scale(m, finestCorrection, Apsi, finestResidual);
     for (int k = 0; k < n; ++k) psi[k] += finestCorrection[k];
     smooth(m, H->rD0, gc->smoother, psi, b, gc->nFinestSweeps);
 }
 
 /* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
- * GAMGSolverSolve.C:31-552 (interpolateCorrection off, no interfaces). */
+ * GAMGSolverSolve.C:31-552 (no interfaces). */
 int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
              const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
     const int n = m->nCells;
@@ -975,6 +1119,10 @@ int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, con
     memset(perf, 0, sizeof(*perf));
     gamg_hier H;
     gamg_setup(&H, m, agg, gc);
+    if (H.singular) {
+        gamg_free(&H);
+        return -2;
+    }
     double* Apsi = (double*)xmalloc(sizeof(double) * H.maxSize);
     double* finestCorrection = (double*)xmalloc(sizeof(double) * H.maxSize);
     double* finestResidual = (double*)xmalloc(sizeof(double) * n);

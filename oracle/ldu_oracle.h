@@ -133,12 +133,22 @@ typedef struct {
     int nFinestSweeps;
     int scaleCorrection;  /* -1: default (= symmetric) */
     int smoother;         /* LDU_SMOOTH_* */
+    int interpolateCorrection; /* GAMGSolverInterpolate.C:30-130 (default 0) */
+    int directSolveCoarsest;   /* LU of the coarsest level (GAMGSolver.C:257-267; default 0) */
 } ldu_gamg_controls;
+
+/* LUDecompose (scalarMatrices.C:77-180): in-place Crout factorisation with
+ * implicit partial pivoting of the row-major n x n matrix A; piv[n].
+ * Returns -1 for a matrix with an all-zero row ("Singular matrix"). */
+int ldu_lu_decompose(int n, double* A, int* piv);
+/* LUBacksubstitute (scalarMatricesTemplates.C:117-163): x = A^-1 x. */
+void ldu_lu_backsubstitute(int n, const double* LU, const int* piv, double* x);
 
 void ldu_gamg_default_controls(ldu_gamg_controls* g);
 
 /* GAMGSolverSolve.C:31-552 with GAMGSolverScale.C:31-76.  The agglomeration
- * must have been built for m's addressing. */
+ * must have been built for m's addressing.  Returns -1 without coarse levels,
+ * -2 when the direct coarsest solve meets a singular matrix. */
 int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
              const ldu_controls* c, const ldu_gamg_controls* g, ldu_perf* perf);
 /* PCG with the GAMG preconditioner; pc: the preconditioner dictionary's

@@ -47,7 +47,8 @@ class LduAgglomeration(ctypes.Structure):
 class LduGamgControls(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in (
         "nPreSweeps", "preSweepsLevelMultiplier", "maxPreSweeps", "nPostSweeps",
-        "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "scaleCorrection", "smoother")]
+        "postSweepsLevelMultiplier", "maxPostSweeps", "nFinestSweeps", "scaleCorrection", "smoother",
+        "interpolateCorrection", "directSolveCoarsest")]
 
 
 @dataclass
@@ -77,6 +78,20 @@ def lib():
 
 def _p(a, t=f64p):
     return None if a is None else a.ctypes.data_as(t)
+
+
+def lu_solve(A, b):
+    """LUscalarMatrix: LUDecompose then LUBacksubstitute of a dense matrix
+    (scalarMatrices.C:77-180, scalarMatricesTemplates.C:117-163).  Raises
+    ValueError("Singular matrix") for an all-zero row."""
+    n = A.shape[0]
+    lu = np.ascontiguousarray(A, np.float64).copy()
+    piv = np.zeros(n, np.int32)
+    if lib().ldu_lu_decompose(n, _p(lu), _p(piv, i32p)) != 0:
+        raise ValueError("Singular matrix")
+    x = np.ascontiguousarray(b, np.float64).copy()
+    lib().ldu_lu_backsubstitute(n, _p(lu), _p(piv, i32p), _p(x))
+    return x, lu, piv
 
 
 class Matrix:
@@ -264,7 +279,7 @@ class Agglomeration:
 def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smoother="GaussSeidel",
          nPreSweeps=0, nPostSweeps=2, nFinestSweeps=2, maxPreSweeps=4, maxPostSweeps=4,
          preSweepsLevelMultiplier=1, postSweepsLevelMultiplier=1, scaleCorrection=None,
-         nCellsInCoarsestLevel=10):
+         nCellsInCoarsestLevel=10, interpolateCorrection=False, directSolveCoarsest=False):
     """GAMGSolver::solve with faceAreaPair agglomeration; psi updated in place."""
     if agg is None:
         agg = Agglomeration(s, n_coarsest=nCellsInCoarsestLevel)
@@ -272,11 +287,14 @@ def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smo
     b = np.ascontiguousarray(s["source"], np.float64)
     g = LduGamgControls(nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps, nPostSweeps,
                         postSweepsLevelMultiplier, maxPostSweeps, nFinestSweeps,
-                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother])
+                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother],
+                        int(bool(interpolateCorrection)), int(bool(directSolveCoarsest)))
     perf = LduPerf()
     c = _controls(tol, rel_tol, max_iter, min_iter)
     rc = lib().ldu_gamg(ctypes.byref(m.c), ctypes.byref(agg.c), _p(psi), _p(b), ctypes.byref(c),
                         ctypes.byref(g), ctypes.byref(perf))
+    if rc == -2:
+        raise ValueError("Singular matrix")
     if rc != 0:
         raise ValueError("GAMG failed")
     return _perf(perf)
@@ -285,7 +303,8 @@ def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smo
 def pcg_gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, nVcycles=2, pre_tol=1e-6,
              pre_rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=0, nPostSweeps=2, nFinestSweeps=2,
              maxPreSweeps=4, maxPostSweeps=4, preSweepsLevelMultiplier=1, postSweepsLevelMultiplier=1,
-             scaleCorrection=None, nCellsInCoarsestLevel=10):
+             scaleCorrection=None, nCellsInCoarsestLevel=10, interpolateCorrection=False,
+             directSolveCoarsest=False):
     """PCG with the GAMG preconditioner (GAMGPreconditioner.C:81-148)."""
     if agg is None:
         agg = Agglomeration(s, n_coarsest=nCellsInCoarsestLevel)
@@ -293,7 +312,8 @@ def pcg_gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0,
     b = np.ascontiguousarray(s["source"], np.float64)
     g = LduGamgControls(nPreSweeps, preSweepsLevelMultiplier, maxPreSweeps, nPostSweeps,
                         postSweepsLevelMultiplier, maxPostSweeps, nFinestSweeps,
-                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother])
+                        -1 if scaleCorrection is None else int(scaleCorrection), SMOOTHERS[smoother],
+                        int(bool(interpolateCorrection)), int(bool(directSolveCoarsest)))
     perf = LduPerf()
     c = _controls(tol, rel_tol, max_iter, min_iter)
     pc = _controls(pre_tol, pre_rel_tol, 1000, 0)

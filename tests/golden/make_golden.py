@@ -90,6 +90,22 @@ SOLVES = {
     "pcg_gamg_dicgs": ("jcube14", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
                                        preconditioner=dict(preconditioner="GAMG", smoother="DICGaussSeidel",
                                                            nVcycles=1, nPreSweeps=1, tolerance=1e-4))),
+    "gamg_interp": ("jcube14", dict(solver="GAMG", smoother="GaussSeidel", interpolateCorrection=True,
+                                    tolerance=1e-8, relTol=0.0)),
+    "gamg_interp_pre": ("jcube16", dict(solver="GAMG", smoother="DICGaussSeidel", nPreSweeps=2,
+                                        interpolateCorrection=True, tolerance=1e-9, relTol=0.0)),
+    "gamg_interp_asym": ("cd10", dict(solver="GAMG", smoother="GaussSeidel", nPreSweeps=1,
+                                      interpolateCorrection=True, tolerance=1e-9, relTol=0.0)),
+    "gamg_direct": ("jcube14", dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True,
+                                    tolerance=1e-8, relTol=0.0)),
+    "gamg_direct_big": ("jcube16", dict(solver="GAMG", smoother="DIC", directSolveCoarsest=True,
+                                        nCellsInCoarsestLevel=60, tolerance=1e-9, relTol=0.0)),
+    "gamg_direct_asym": ("cd10", dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True,
+                                      tolerance=1e-9, relTol=0.0)),
+    "pcg_gamg_direct": ("jcube14", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
+                                        preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel",
+                                                            directSolveCoarsest=True,
+                                                            interpolateCorrection=True))),
 }
 
 

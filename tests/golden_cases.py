@@ -42,5 +42,5 @@ def solve_case(name):
 
 def gamg_kwargs(ctl):
     keys = ("smoother", "nPreSweeps", "nPostSweeps", "nFinestSweeps", "maxPreSweeps", "maxPostSweeps",
-            "nCellsInCoarsestLevel")
+            "nCellsInCoarsestLevel", "interpolateCorrection", "directSolveCoarsest")
     return {k: ctl[k] for k in keys if k in ctl}

@@ -290,3 +290,44 @@ def test_gamg_preconditioner_mixed_and_asymmetric():
                                "preconditioner": {"preconditioner": "GAMG", "smoother": "GaussSeidel"}})
     assert perf.converged and perf.solverName == "GAMGPBiCGStab"
     _residual_ok(cd, psi, 1e-9)
+
+
+@pytest.mark.parametrize("form", ["cta", "levels"])
+def test_gamg_interpolate_correction_mixed_and_forms(form):
+    """interpolateCorrection (GAMGSolverInterpolate.C) in FP64 against the
+    oracle in two sweep forms, and with FP32 V-cycles to the FP64 tolerance."""
+    s = cases.gamg_cube(16, jitter=0.2, seed=12)
+    ref = np.zeros_like(s["source"])
+    rp = orc.gamg(s, ref, tol=1e-9, smoother="GaussSeidel", nPreSweeps=1, interpolateCorrection=True)
+    ctl = {"solver": "cudaGAMG", "smoother": "GaussSeidel", "nPreSweeps": 1, "interpolateCorrection": True,
+           "tolerance": 1e-9, "relTol": 0}
+    with sweep_form(form):
+        psi = np.zeros_like(s["source"])
+        perf = ldu.solve(s, psi, ctl)
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= (RTOL_FP64 if perf.nIterations == rp.nIterations else 1e-6)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, dict(ctl, precision="mixed"))
+    assert perf.converged
+    _residual_ok(s, psi, 1e-9)
+
+
+@pytest.mark.parametrize("n_coarsest", [10, 300])
+def test_gamg_direct_coarsest_against_oracle(n_coarsest):
+    """directSolveCoarsest: the coarsest level by the device LU (factors in
+    shared memory for small levels, in global memory for a 300-cell one)
+    against the oracle's LUscalarMatrix, in FP64 and with FP32 V-cycles."""
+    s = cases.gamg_cube(16, jitter=0.2, seed=13)
+    ref = np.zeros_like(s["source"])
+    rp = orc.gamg(s, ref, tol=1e-9, smoother="GaussSeidel", directSolveCoarsest=True,
+                  nCellsInCoarsestLevel=n_coarsest)
+    ctl = {"solver": "cudaGAMG", "smoother": "GaussSeidel", "directSolveCoarsest": True,
+           "nCellsInCoarsestLevel": n_coarsest, "tolerance": 1e-9, "relTol": 0}
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, ctl)
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= (RTOL_FP64 if perf.nIterations == rp.nIterations else 1e-6)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, dict(ctl, precision="mixed"))
+    assert perf.converged
+    _residual_ok(s, psi, 1e-9)

@@ -113,3 +113,19 @@ def test_agglomeration_and_coarse_matrices(name):
         np.testing.assert_array_equal(cd, g[f"coarseDiag{i}"])
         np.testing.assert_array_equal(cup, g[f"coarseUpper{i}"])
         fine = dict(l=cl, u=cu, diag=cd, upper=cup, lower=clo)
+
+
+def test_lu_restatement_solves_and_detects_singular_rows():
+    """The oracle's LUscalarMatrix (pinned bit for bit by the golden
+    directSolveCoarsest solves) solves a pivoting-heavy dense system to
+    rounding and refuses an all-zero row like LUDecompose."""
+    rng = np.random.default_rng(3)
+    A = rng.uniform(-1, 1, (40, 40))
+    A[np.arange(40), np.arange(40)] *= 1e-3  # small diagonals force row interchanges
+    b = rng.uniform(-1, 1, 40)
+    x, _, piv = orc.lu_solve(A, b)
+    assert np.any(piv != np.arange(40))
+    np.testing.assert_allclose(A @ x, b, rtol=0, atol=1e-10)
+    A[7, :] = 0.0
+    with pytest.raises(ValueError, match="Singular matrix"):
+        orc.lu_solve(A, b)

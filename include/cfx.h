@@ -59,17 +59,27 @@ typedef struct {
     int pad;
 } cfx_perf;
 
-/* CFX_SOLVER_SMOOTH: smoothSolver (smoothSolver.C:77-196) */
-enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2, CFX_SOLVER_SMOOTH = 3 };
+/* CFX_SOLVER_SMOOTH: smoothSolver (smoothSolver.C:77-196); CFX_SOLVER_PBICG:
+ * PBiCG (PBiCG.C:65-220, asymmetric matrices; preconditioners with a
+ * preconditionT: none, diagonal, DILU) */
+enum { CFX_SOLVER_PCG = 0, CFX_SOLVER_PBICGSTAB = 1, CFX_SOLVER_GAMG = 2, CFX_SOLVER_SMOOTH = 3,
+       CFX_SOLVER_PBICG = 4 };
 /* CFX_PRE_GAMG: GAMGPreconditioner (GAMGPreconditioner.C:81-148), nVcycles
  * V-cycles with the controls' GAMG fields (smoother, sweeps) from w = 0; the
  * mesh needs GAMG levels */
-enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3, CFX_PRE_GAMG = 4 };
+/* CFX_PRE_FDIC: FDICPreconditioner (FDICPreconditioner.C:40-137, symmetric):
+ * its cached rD[u]*upper products are the ones DIC forms, so it runs the DIC
+ * sweeps and reports "FDIC<solver>" */
+enum { CFX_PRE_NONE = 0, CFX_PRE_DIAGONAL = 1, CFX_PRE_DIC = 2, CFX_PRE_DILU = 3, CFX_PRE_GAMG = 4,
+       CFX_PRE_FDIC = 5 };
 /* lduMatrix::smoother run-time table (GAMG's smoother, smoothSolver's):
  * GaussSeidel, DIC (symmetric), symGaussSeidel, DILU (asymmetric),
- * DICGaussSeidel (symmetric), DILUGaussSeidel (asymmetric) */
+ * DICGaussSeidel (symmetric), DILUGaussSeidel (asymmetric), FDIC (symmetric;
+ * the DIC smoother's arithmetic, FDICSmoother.C:40-160) and
+ * nonBlockingGaussSeidel (GaussSeidel's arithmetic when there are no
+ * coupled interfaces, nonBlockingGaussSeidelSmoother.C:92-233) */
 enum { CFX_SMOOTH_GS = 0, CFX_SMOOTH_DIC = 1, CFX_SMOOTH_SYMGS = 2, CFX_SMOOTH_DILU = 3, CFX_SMOOTH_DICGS = 4,
-       CFX_SMOOTH_DILUGS = 5 };
+       CFX_SMOOTH_DILUGS = 5, CFX_SMOOTH_FDIC = 6, CFX_SMOOTH_NBGS = 7 };
 enum { CFX_FP64 = 0, CFX_MIXED = 1 };
 
 /* Solver controls: lduMatrix::solver::readControls (lduMatrixSolver.C:158-164)
@@ -157,7 +167,12 @@ cfx_status cfx_gamg_level_info(cfx_mesh* mesh, int level, int* nCells, int* nFac
 cfx_status cfx_gamg_n_levels(cfx_mesh* mesh, int* nLevels);
 
 /* ---- matrix (lduMatrix coefficients) ------------------------------------ */
-/* Host coefficients; lower == NULL means symmetric (lduMatrix::symmetric()). */
+/* Host coefficients; lower == NULL means symmetric (lduMatrix::symmetric()).
+ * upper == lower == NULL is a diagonal matrix (lduMatrix::diagonal()): every
+ * solve of it is diagonalSolver's psi = source/diag ("diagonal", 0
+ * iterations, converged), whatever solver the controls name, as
+ * lduMatrix::solver::New selects it (lduMatrixSolver.C:52-66,
+ * diagonalSolver.C:62-81). */
 cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* upper,
                              const double* lower, cfx_matrix** mat);
 /* Re-upload coefficients (a new fvMatrix on the same mesh, every solve). */

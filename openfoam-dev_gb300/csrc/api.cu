@@ -55,6 +55,7 @@ struct cfx_mesh {
 template <class T>
 struct LevelPack {
     Packed<T> rd, fwd, bwd;
+    Packed<T> fwdT, bwdT;  // DILU preconditionT: the packs of the transpose
     std::map<int, Packed<T>> gs;
 };
 
@@ -89,6 +90,7 @@ struct cfx_matrix {
     PcGamg* pcGamg = nullptr;
     Arena arena;
     bool sym = true;
+    bool diagonal = false;  // lduMatrix::diagonal(): no off-diagonal coefficients
     std::vector<LevelCoeffs<double>> c64;   // per level
     std::vector<LevelCoeffs<float>> c32;
     bool coarse64 = false, coarse32 = false, fine32 = false;
@@ -340,7 +342,8 @@ void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, 
     const LevelMesh& m = mesh->dev[0];
     LevelCoeffs<double>& c = mat->c64[0];
     CK(cudaMemcpyAsync(c.diag, diag, sizeof(double) * m.n, kind, s));
-    if (m.nf) CK(cudaMemcpyAsync(c.upper, upper, sizeof(double) * m.nf, kind, s));
+    if (m.nf && upper) CK(cudaMemcpyAsync(c.upper, upper, sizeof(double) * m.nf, kind, s));
+    if (m.nf && !upper) CK(cudaMemsetAsync(c.upper, 0, sizeof(double) * m.nf, s));  // diagonal matrix
     if (!mat->sym && m.nf) CK(cudaMemcpyAsync(c.lower, lower, sizeof(double) * m.nf, kind, s));
     Ops<double>::permute(s, m, c);
     mat->coarse64 = mat->coarse32 = mat->fine32 = false;
@@ -441,13 +444,28 @@ Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd) {
     return *p;
 }
 
+// The transpose's DILU packs (forward: rD*upper of the neighbour faces,
+// backward: rD*lower of the owned faces) for preconditionT.
+template <class T>
+Packed<T>& packedT(cfx_matrix* mat, int lv, int op, const DevSched& sd) {
+    auto& v = packs_of<T>(mat);
+    if ((int)v.size() <= lv) v.resize(lv + 1);
+    Packed<T>* p = op == OP_FWD ? &v[lv].fwdT : &v[lv].bwdT;
+    if (!p->coef) {
+        p->coef = mat->arena.get<T>(sd.nEntries);
+        p->scalar = mat->arena.get<T>(sd.nSlots);
+        p->inS = mat->arena.get<T>(sd.nSlots);
+    }
+    return *p;
+}
+
 void invalidate_packs(cfx_matrix* mat) {
     for (auto& l : mat->p64) {
-        l.rd.valid = l.fwd.valid = l.bwd.valid = false;
+        l.rd.valid = l.fwd.valid = l.bwd.valid = l.fwdT.valid = l.bwdT.valid = false;
         for (auto& kv : l.gs) kv.second.valid = false;
     }
     for (auto& l : mat->p32) {
-        l.rd.valid = l.fwd.valid = l.bwd.valid = false;
+        l.rd.valid = l.fwd.valid = l.bwd.valid = l.fwdT.valid = l.bwdT.valid = false;
         for (auto& kv : l.gs) kv.second.valid = false;
     }
 }
@@ -519,6 +537,48 @@ int precondition(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int*
     return std::max(1, std::min(g, RED_MAXB));
 }
 
+// DILUPreconditioner::preconditionT (DILUPreconditioner.C:138-185) is the
+// DILU sweep pair of the transpose: the forward pass subtracts
+// rD[u]*upper*w[l] per cell in face order (the order the losort forward
+// pass of precondition uses for lower), the backward pass rD[l]*lower*w[u]
+// in the reverse order of the owned faces, and rD (upper*lower products)
+// is the same.  Other preconditioners' preconditionT is precondition.
+template <class T>
+void preconditionT(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int* done) {
+    if (kind != CFX_PRE_DILU) {
+        precondition<T>(mat, lv, kind, r, w, done, false);
+        return;
+    }
+    cfx_ctx* ctx = mat->mesh->ctx;
+    cudaStream_t s = ctx->stream;
+    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
+    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    if (run_sweep<T>(s, f, OP_FWD, packedT<T>(mat, lv, OP_FWD, f), r, w, nullptr, nullptr, done, ctx->d_status) !=
+        CFX_OK)
+        throw CudaError(last_error());
+    if (run_sweep<T>(s, b, OP_BWD, packedT<T>(mat, lv, OP_BWD, b), nullptr, w, nullptr, nullptr, done,
+                     ctx->d_status) != CFX_OK)
+        throw CudaError(last_error());
+}
+
+// Packs for preconditionT of DILU (compute_rD must have run).
+template <class T>
+void setup_preconditioner_t(cfx_matrix* mat, int lv, int kind) {
+    if (kind != CFX_PRE_DILU) return;
+    cudaStream_t s = mat->mesh->ctx->stream;
+    const LevelCoeffs<T>& c = coeffs<T>(mat, lv);
+    LevelCoeffs<T> t = c;  // the transpose: upper <-> lower
+    t.sym = false;
+    t.lower = c.upper;
+    t.upper = c.lower;
+    t.lowerPerm = c.upperPerm;
+    t.upperPerm = c.lowerPerm;
+    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
+    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    pack_sweep<T>(s, f, OP_FWD, t, packedT<T>(mat, lv, OP_FWD, f));
+    pack_sweep<T>(s, b, OP_BWD, t, packedT<T>(mat, lv, OP_BWD, b));
+}
+
 template <class T>
 void setup_preconditioner(cfx_matrix* mat, int lv, int kind) {
     cfx_ctx* ctx = mat->mesh->ctx;
@@ -571,6 +631,19 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     int iters = 0;
     if (solver == CFX_SOLVER_PBICGSTAB)
         for (int i = 4; i < 8; ++i) W.get(i, n);
+    T *rT = nullptr, *wT = nullptr, *pT = nullptr;
+    if (solver == CFX_SOLVER_PBICG) {
+        // PBiCG.C:108-125: rT = source - A^T psi (pT starts at zero; the
+        // first iteration overwrites it)
+        rT = W.get(20, n);
+        wT = W.get(21, n);
+        pT = W.get(22, n);
+        setup_preconditioner_t<T>(mat, lv, precond);
+        Ops<T>::tmul(s, m, c, psi, wT);
+        Kern<T>::copy(s, n, b, rT, nullptr);
+        Kern<T>::axpy(s, n, T(-1), wT, rT, nullptr);
+        Kern<T>::fill(s, n, T(0), pT, nullptr);
+    }
     uint64_t pcKey = 0;
     if (precond == CFX_PRE_GAMG) {
         double pt = ctl.pcTolerance, pr = ctl.pcRelTol;
@@ -594,6 +667,17 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
             Kern<T>::pcg_p(s, n, w, p, st);
             Kern<T>::pcg_amul(s, ctx->sc, m, c, p, w, st);
             Kern<T>::pcg_update(s, ctx->sc, n, p, w, psi, r, st);
+        } else if (solver == CFX_SOLVER_PBICG) {
+            // PBiCG.C:131-200
+            precondition<T>(mat, lv, precond, r, w, done, false);
+            preconditionT<T>(mat, lv, precond, rT, wT, done);
+            launch_reduce<T>(s, ctx->sc, 3, n, w, rT, ctx->sc.chunkPartials);  // wArT
+            count_launch();
+            Kern<T>::pcg_beta(s, 1, ctx->sc.chunkPartials, st);
+            Kern<T>::pbicg_p(s, n, w, wT, p, pT, st);
+            Ops<T>::amul(s, m, c, p, w);
+            Kern<T>::pbicg_tmul(s, ctx->sc, m, c, pT, wT, w, st);
+            Kern<T>::pbicg_update(s, ctx->sc, n, p, w, wT, psi, r, rT, st);
         } else {
             T* AyA = W.get(4, n);
             T* sA = W.get(5, n);
@@ -1172,13 +1256,18 @@ cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, c
         h.nIterations = inner;
         perf->nOuter = outer;
     }
-    const char* base = ctl.solver == CFX_SOLVER_PCG ? "PCG" : "PBiCGStab";
+    const char* base = ctl.solver == CFX_SOLVER_PCG ? "PCG" : ctl.solver == CFX_SOLVER_PBICG ? "PBiCG" : "PBiCGStab";
     std::snprintf(perf->solverName, sizeof(perf->solverName), "%s%s", pre_name(ctl.preconditioner), base);
     perf->initialResidual = h.initialResidual;
     perf->finalResidual = h.finalResidual;
     perf->nIterations = h.nIterations;
     perf->converged = h.converged;
     perf->singular = h.singular;
+    if (ctl.solver == CFX_SOLVER_PBICG && h.nIterations > std::max(1000, ctl.maxIter)) {
+        set_error("PBiCG has failed to converge within the maximum number of iterations " +
+                  std::to_string(std::max(1000, ctl.maxIter)) + "\n    Please try the more robust PBiCGStab solver.");
+        return CFX_ERR_FATAL;
+    }
     return CFX_OK;
 }
 
@@ -1247,8 +1336,8 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("null controls");
         return CFX_ERR_ARG;
     }
-    if (c->solver < 0 || c->solver > 3 || c->preconditioner < 0 || c->preconditioner > 4 || c->smoother < 0 ||
-        c->smoother > 5 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
+    if (c->solver < 0 || c->solver > 4 || c->preconditioner < 0 || c->preconditioner > 5 || c->smoother < 0 ||
+        c->smoother > 7 || (c->precision != CFX_FP64 && c->precision != CFX_MIXED)) {
         set_error("unknown solver, preconditioner, smoother or precision");
         return CFX_ERR_CONFIG;
     }
@@ -1258,22 +1347,36 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("Unknown asymmetric matrix solver cudaPCG");
         return CFX_ERR_CONFIG;
     }
+    if (c->solver == CFX_SOLVER_PBICG && mat->sym) {
+        set_error("Unknown symmetric matrix solver cudaPBiCG");  // PBiCG.C:34-35: asymmetric only
+        return CFX_ERR_CONFIG;
+    }
+    if (c->solver == CFX_SOLVER_PBICG && c->preconditioner == CFX_PRE_GAMG) {
+        // lduMatrix::preconditioner::preconditionT (lduMatrix.H:500-508)
+        set_error("Not implemented: GAMGPreconditioner::preconditionT");
+        return CFX_ERR_FATAL;
+    }
     if (c->solver == CFX_SOLVER_SMOOTH && c->precision == CFX_MIXED) {
         set_error("precision mixed is not available for cudaSmoothSolver");
         return CFX_ERR_CONFIG;
     }
     const bool pcGamg = (c->solver == CFX_SOLVER_PCG || c->solver == CFX_SOLVER_PBICGSTAB) &&
                         c->preconditioner == CFX_PRE_GAMG;
+    if (c->solver == CFX_SOLVER_PBICG && c->precision == CFX_MIXED) {
+        set_error("precision mixed is not available for cudaPBiCG");
+        return CFX_ERR_CONFIG;
+    }
     if (pcGamg && c->nVcycles < 1) {
         set_error("GAMG preconditioner: nVcycles must be at least 1");
         return CFX_ERR_CONFIG;
     }
     if (c->solver == CFX_SOLVER_GAMG || c->solver == CFX_SOLVER_SMOOTH || pcGamg) {
         // smoother tables (the smoothers' *ConstructorToTable registrations)
-        const bool symOnly = c->smoother == CFX_SMOOTH_DIC || c->smoother == CFX_SMOOTH_DICGS;
+        const bool symOnly =
+            c->smoother == CFX_SMOOTH_DIC || c->smoother == CFX_SMOOTH_DICGS || c->smoother == CFX_SMOOTH_FDIC;
         const bool asymOnly = c->smoother == CFX_SMOOTH_DILU || c->smoother == CFX_SMOOTH_DILUGS;
-        static const char* names[] = {"GaussSeidel", "DIC", "symGaussSeidel", "DILU", "DICGaussSeidel",
-                                      "DILUGaussSeidel"};
+        static const char* names[] = {"GaussSeidel",     "DIC",  "symGaussSeidel",        "DILU", "DICGaussSeidel",
+                                      "DILUGaussSeidel", "FDIC", "nonBlockingGaussSeidel"};
         if ((symOnly && !mat->sym) || (asymOnly && mat->sym)) {
             set_error(std::string("Unknown ") + (mat->sym ? "symmetric" : "asymmetric") + " matrix smoother " +
                       names[c->smoother]);
@@ -1281,8 +1384,9 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         }
     }
     if (c->solver != CFX_SOLVER_GAMG && c->solver != CFX_SOLVER_SMOOTH) {
-        if (c->preconditioner == CFX_PRE_DIC && !mat->sym) {
-            set_error("Unknown asymmetric matrix preconditioner DIC");
+        if ((c->preconditioner == CFX_PRE_DIC || c->preconditioner == CFX_PRE_FDIC) && !mat->sym) {
+            set_error(std::string("Unknown asymmetric matrix preconditioner ") +
+                      (c->preconditioner == CFX_PRE_DIC ? "DIC" : "FDIC"));
             return CFX_ERR_CONFIG;
         }
         if (c->preconditioner == CFX_PRE_DILU && mat->sym) {
@@ -1502,11 +1606,12 @@ cfx_status cfx_gamg_level_info(cfx_mesh* mesh, int level, int* nCells, int* nFac
 
 cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* upper, const double* lower,
                              cfx_matrix** out) {
-    if (!mesh || !out || !diag || (!upper && mesh->host[0].nf)) return CFX_ERR_ARG;
+    if (!mesh || !out || !diag || (!upper && lower)) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
         auto mat = std::make_unique<cfx_matrix>();
         mat->mesh = mesh;
         mat->sym = lower == nullptr;
+        mat->diagonal = upper == nullptr;
         LevelCoeffs<double> c;
         alloc_coeffs(mat->arena, mesh->dev[0], mat->sym, c);
         mat->c64.push_back(c);
@@ -1521,7 +1626,7 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
 }
 
 cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper, const double* lower) {
-    if (!mat || !diag || (mat->sym != (lower == nullptr))) {
+    if (!mat || !diag || (mat->sym != (lower == nullptr)) || (mat->diagonal != (upper == nullptr))) {
         set_error("cfx_matrix_update: symmetry of the coefficients changed or null diag");
         return CFX_ERR_ARG;
     }
@@ -1532,7 +1637,8 @@ cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* 
 }
 
 cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* diag, const double* upper, const double* lower) {
-    if (!mat || !diag || (mat->sym != (lower == nullptr))) return CFX_ERR_ARG;
+    if (!mat || !diag || (mat->sym != (lower == nullptr)) || (mat->diagonal != (upper == nullptr)))
+        return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
         set_coefficients(mat, diag, upper, lower, cudaMemcpyDeviceToDevice);
         return CFX_OK;
@@ -1566,14 +1672,39 @@ cfx_status cfx_matrix_coarse(cfx_matrix* mat, int level, double* diag, double* u
 cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_psi, const double* d_source,
                             cfx_perf* perf) {
     if (!mat || !d_psi || !d_source || !perf) return CFX_ERR_ARG;
+    if (mat->diagonal) {
+        // lduMatrix::solver::New picks diagonalSolver for a diagonal matrix
+        // before it looks at the solver name (lduMatrixSolver.C:52-66)
+        if (!ctl) return CFX_ERR_ARG;
+        std::memset(perf, 0, sizeof(*perf));
+        const cfx_status st = guard([&]() -> cfx_status {
+            Ops<double>::diag_solve(mat->mesh->ctx->stream, mat->mesh->dev[0].n, mat->c64[0].diag, d_source, d_psi);
+            return CFX_OK;
+        });
+        std::snprintf(perf->solverName, sizeof(perf->solverName), "diagonal");
+        perf->converged = 1;
+        perf->status = st;
+        return st;
+    }
     CFX_TRY(check_controls(mat, ctl));
     std::memset(perf, 0, sizeof(*perf));
+    // FDIC (preconditioner and smoother) forms DIC's products in DIC's order
+    // (sqr(upper) = upper*upper; rDuUpper = rD[u]*upper is the left factor
+    // DIC multiplies first) and nonBlockingGaussSeidel without coupled
+    // interfaces is GaussSeidel: they run those kernels under their names
+    cfx_controls c = *ctl;
+    if (c.preconditioner == CFX_PRE_FDIC) c.preconditioner = CFX_PRE_DIC;
+    if (c.smoother == CFX_SMOOTH_FDIC) c.smoother = CFX_SMOOTH_DIC;
+    if (c.smoother == CFX_SMOOTH_NBGS) c.smoother = CFX_SMOOTH_GS;
     const cfx_status st = guard([&]() -> cfx_status {
         CK(cudaMemsetAsync(mat->mesh->ctx->d_status, 0, sizeof(int), mat->mesh->ctx->stream));
-        if (ctl->solver == CFX_SOLVER_GAMG) return gamg_solve(mat, *ctl, d_psi, d_source, perf);
-        if (ctl->solver == CFX_SOLVER_SMOOTH) return smooth_solve(mat, *ctl, d_psi, d_source, perf);
-        return krylov_solve(mat, *ctl, d_psi, d_source, perf);
+        if (c.solver == CFX_SOLVER_GAMG) return gamg_solve(mat, c, d_psi, d_source, perf);
+        if (c.solver == CFX_SOLVER_SMOOTH) return smooth_solve(mat, c, d_psi, d_source, perf);
+        return krylov_solve(mat, c, d_psi, d_source, perf);
     });
+    if (ctl->preconditioner == CFX_PRE_FDIC && (c.solver == CFX_SOLVER_PCG || c.solver == CFX_SOLVER_PBICGSTAB))
+        std::snprintf(perf->solverName, sizeof(perf->solverName), "FDIC%s",
+                      c.solver == CFX_SOLVER_PCG ? "PCG" : "PBiCGStab");
     perf->status = st;
     return st;
 }
@@ -1771,7 +1902,10 @@ cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status) {
 
 cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, int nSweeps) {
     if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
-    if (kind < CFX_SMOOTH_GS || kind > CFX_SMOOTH_DILUGS) return CFX_ERR_CONFIG;
+    if (kind < CFX_SMOOTH_GS || kind > CFX_SMOOTH_NBGS) return CFX_ERR_CONFIG;
+    if (kind == CFX_SMOOTH_FDIC && !mat->sym) return CFX_ERR_CONFIG;
+    if (kind == CFX_SMOOTH_FDIC) kind = CFX_SMOOTH_DIC;  // the same arithmetic (FDICSmoother.C:40-160)
+    if (kind == CFX_SMOOTH_NBGS) kind = CFX_SMOOTH_GS;   // no coupled interfaces
     if ((kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) && !mat->sym) return CFX_ERR_CONFIG;
     if ((kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) && mat->sym) return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {

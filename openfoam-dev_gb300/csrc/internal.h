@@ -151,6 +151,8 @@ struct Ops {
                           int* status);
     // x = LU^-1 b (LUscalarMatrix::solve)
     static void lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T* b, T* x);
+    // x = b / diag (diagonalSolver)
+    static void diag_solve(cudaStream_t s, int n, const T* diag, const T* b, T* x);
 };
 
 void launch_cast_d2f(cudaStream_t s, int64_t n, const double* in, float* out);

@@ -337,6 +337,11 @@ __global__ void lu_solve_k(int n, const T* __restrict__ LUg, const int* __restri
 }
 
 template <class T>
+__global__ void diag_solve_k(int n, const T* __restrict__ diag, const T* __restrict__ b, T* __restrict__ x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i] / diag[i];
+}
+
+template <class T>
 __global__ void reciprocal_k(int n, T* x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = T(1) / x[i];
 }
@@ -468,6 +473,12 @@ void Ops<T>::lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T
         lu_solve_k<T, true><<<1, 128, sm, s>>>(n, A, piv, b, x);
     else
         lu_solve_k<T, false><<<1, 32, 0, s>>>(n, A, piv, b, x);
+    count_launch();
+}
+
+template <class T>
+void Ops<T>::diag_solve(cudaStream_t s, int n, const T* diag, const T* b, T* x) {
+    diag_solve_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, diag, b, x);
     count_launch();
 }
 

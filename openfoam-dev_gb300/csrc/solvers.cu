@@ -202,6 +202,72 @@ __global__ void __launch_bounds__(RED_NT) pcg_update_k(int n, const T* __restric
     }
 }
 
+// PBiCG.C:138-158: the search directions of the pair (first iteration: the
+// preconditioned residuals)
+template <class T>
+__global__ void pbicg_p_k(int n, const T* __restrict__ w, const T* __restrict__ wT, T* __restrict__ p,
+                          T* __restrict__ pT, const SolveState* st) {
+    if (st->done) return;
+    const bool first = st->nIterations == 0;
+    const T beta = T(st->beta);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        if (first) {
+            p[c] = w[c];
+            pT[c] = wT[c];
+        } else {
+            p[c] = w[c] + beta * p[c];
+            pT[c] = wT[c] + beta * pT[c];
+        }
+    }
+}
+
+// PBiCG.C:160-172: wT = A^T pT (row gather, lduMatrix::Tmul's per-cell face
+// order) fused with wApT = wA.pT, the singularity test and alpha.
+template <class T>
+__global__ void __launch_bounds__(RED_NT) pbicg_tmul_k(int n, const int* os, const int* ls, const int* lL,
+                                                       const int* u, const T* diag, const T* upPerm, const T* lower,
+                                                       const T* __restrict__ pT, T* __restrict__ wT,
+                                                       const T* __restrict__ wA, SolveState* st, Red2 red) {
+    if (st->done) return;
+    double d = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        wT[c] = row_amul<T>(c, os, ls, lL, u, diag, upPerm, lower, pT);
+        d += double(wA[c]) * double(pT[c]);
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(d, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->singular = fabs(s) / st->normFactor < VSMALL;
+        if (st->singular) {
+            st->done = 1;
+        } else {
+            st->alpha = st->wArA / s;
+        }
+    }
+}
+
+// PBiCG.C:174-200: psi, rA and rT updates, |rA|/normFactor, loop test.
+template <class T>
+__global__ void __launch_bounds__(RED_NT) pbicg_update_k(int n, const T* __restrict__ p, const T* __restrict__ wA,
+                                                         const T* __restrict__ wT, T* __restrict__ psi,
+                                                         T* __restrict__ r, T* __restrict__ rT, SolveState* st,
+                                                         Red2 red) {
+    if (st->done) return;
+    const T alpha = T(st->alpha);
+    double mg = 0.0;
+    for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
+        psi[c] += alpha * p[c];
+        const T rc = r[c] - alpha * wA[c];
+        r[c] = rc;
+        rT[c] -= alpha * wT[c];
+        mg += fabs(double(rc));
+    }
+    double s, dummy;
+    if (reduce2<RED_NT>(mg, 0.0, red, s, dummy) && threadIdx.x == 0) {
+        st->finalResidual = s / st->normFactor;
+        loop_test(st);
+    }
+}
+
 // PBiCGStab.C:141-171
 template <class T>
 __global__ void __launch_bounds__(RED_NT) bicg_rho_k(int n, const T* __restrict__ r0, const T* __restrict__ r,
@@ -473,6 +539,28 @@ void Kern<T>::pcg_amul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const Le
 template <class T>
 void Kern<T>::pcg_update(cudaStream_t s, Scratch& sc, int n, const T* p, const T* wA, T* psi, T* r, SolveState* st) {
     pcg_update_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, p, wA, psi, r, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pbicg_p(cudaStream_t s, int n, const T* w, const T* wT, T* p, T* pT, const SolveState* st) {
+    pbicg_p_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, w, wT, p, pT, st);
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pbicg_tmul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* pT,
+                         T* wT, const T* wA, SolveState* st) {
+    pbicg_tmul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
+                                                     a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower,
+                                                     pT, wT, wA, st, Red2{sc.partials, sc.counters});
+    count_launch();
+}
+
+template <class T>
+void Kern<T>::pbicg_update(cudaStream_t s, Scratch& sc, int n, const T* p, const T* wA, const T* wT, T* psi, T* r,
+                           T* rT, SolveState* st) {
+    pbicg_update_k<T><<<grid_for(n), RED_NT, 0, s>>>(n, p, wA, wT, psi, r, rT, st, Red2{sc.partials, sc.counters});
     count_launch();
 }
 

@@ -42,6 +42,12 @@ struct Kern {
                          T* wA, SolveState* st);
     static void pcg_update(cudaStream_t s, Scratch& sc, int n, const T* p, const T* wA, T* psi, T* r,
                            SolveState* st);
+    // PBiCG (wArA holds wArT)
+    static void pbicg_p(cudaStream_t s, int n, const T* w, const T* wT, T* p, T* pT, const SolveState* st);
+    static void pbicg_tmul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* pT,
+                           T* wT, const T* wA, SolveState* st);
+    static void pbicg_update(cudaStream_t s, Scratch& sc, int n, const T* p, const T* wA, const T* wT, T* psi,
+                             T* r, T* rT, SolveState* st);
     // PBiCGStab
     static void bicg_rho(cudaStream_t s, Scratch& sc, int n, const T* r0, const T* r, SolveState* st);
     static void bicg_p(cudaStream_t s, int n, const T* r, const T* AyA, T* p, const SolveState* st);

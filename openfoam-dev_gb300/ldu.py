@@ -30,21 +30,23 @@ from . import LIB_DIR
 
 LIB_PATH = os.path.join(LIB_DIR, "libcudaLduSolvers.so")
 
-SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG, SOLVER_SMOOTH = 0, 1, 2, 3
-PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3, "GAMG": 4}
+SOLVER_PCG, SOLVER_PBICGSTAB, SOLVER_GAMG, SOLVER_SMOOTH, SOLVER_PBICG = 0, 1, 2, 3, 4
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3, "GAMG": 4, "FDIC": 5}
 SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "symGaussSeidel": 2, "DILU": 3, "DICGaussSeidel": 4,
-             "DILUGaussSeidel": 5}
+             "DILUGaussSeidel": 5, "FDIC": 6, "nonBlockingGaussSeidel": 7}
 # the smoothers' run-time tables by matrix symmetry
-SYM_SMOOTHERS = ("DIC", "DICGaussSeidel", "GaussSeidel", "symGaussSeidel")
-ASYM_SMOOTHERS = ("DILU", "DILUGaussSeidel", "GaussSeidel", "symGaussSeidel")
+SYM_SMOOTHERS = ("DIC", "DICGaussSeidel", "FDIC", "GaussSeidel", "nonBlockingGaussSeidel", "symGaussSeidel")
+ASYM_SMOOTHERS = ("DILU", "DILUGaussSeidel", "GaussSeidel", "nonBlockingGaussSeidel", "symGaussSeidel")
 SOLVERS = {"cudaPCG": SOLVER_PCG, "cudaPBiCGStab": SOLVER_PBICGSTAB, "cudaGAMG": SOLVER_GAMG,
-           "cudaSmoothSolver": SOLVER_SMOOTH,
-           "PCG": SOLVER_PCG, "PBiCGStab": SOLVER_PBICGSTAB, "GAMG": SOLVER_GAMG, "smoothSolver": SOLVER_SMOOTH}
+           "cudaSmoothSolver": SOLVER_SMOOTH, "cudaPBiCG": SOLVER_PBICG,
+           "PCG": SOLVER_PCG, "PBiCGStab": SOLVER_PBICGSTAB, "GAMG": SOLVER_GAMG, "smoothSolver": SOLVER_SMOOTH,
+           "PBiCG": SOLVER_PBICG}
 SYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaPCG", "cudaSmoothSolver")
-ASYM_SOLVERS = ("cudaGAMG", "cudaPBiCGStab", "cudaSmoothSolver")
+ASYM_SOLVERS = ("cudaGAMG", "cudaPBiCG", "cudaPBiCGStab", "cudaSmoothSolver")
 
 STATUS = {0: "ok", -1: "bad argument", -2: "bad addressing", -3: "CUDA error", -4: "out of memory",
-          -5: "admission refused", -6: "device wait timed out", -7: "bad configuration", -8: "bad state"}
+          -5: "admission refused", -6: "device wait timed out", -7: "bad configuration", -8: "bad state",
+          -9: "fatal error"}
 
 
 class FatalError(RuntimeError):
@@ -335,10 +337,11 @@ class LduMesh:
 class LduMatrix:
     """lduMatrix: diag/upper(/lower) coefficients on an LduMesh."""
 
-    def __init__(self, mesh, diag, upper, lower=None):
+    def __init__(self, mesh, diag, upper=None, lower=None):
+        """upper = lower = None: a diagonal matrix (lduMatrix::diagonal())."""
         self.mesh = mesh
         self.diag = np.ascontiguousarray(diag, np.float64)
-        self.upper = np.ascontiguousarray(upper, np.float64)
+        self.upper = None if upper is None else np.ascontiguousarray(upper, np.float64)
         self.lower = None if lower is None else np.ascontiguousarray(lower, np.float64)
         h = ctypes.c_void_p()
         _check(lib().cfx_matrix_create(mesh.h, _hp(self.diag), _hp(self.upper), _hp(self.lower), ctypes.byref(h)),
@@ -346,15 +349,18 @@ class LduMatrix:
         self.h = h
         _track("matrix", self)
 
+    def diagonal(self):
+        return self.upper is None and self.lower is None
+
     def symmetric(self):
-        return self.lower is None
+        return self.upper is not None and self.lower is None
 
     def asymmetric(self):
         return self.lower is not None
 
-    def update(self, diag, upper, lower=None):
+    def update(self, diag, upper=None, lower=None):
         self.diag = np.ascontiguousarray(diag, np.float64)
-        self.upper = np.ascontiguousarray(upper, np.float64)
+        self.upper = None if upper is None else np.ascontiguousarray(upper, np.float64)
         self.lower = None if lower is None else np.ascontiguousarray(lower, np.float64)
         _check(lib().cfx_matrix_update(self.h, _hp(self.diag), _hp(self.upper), _hp(self.lower)), "update")
 
@@ -394,7 +400,7 @@ class LduMatrix:
     def coarse(self, level, nCells, nFaces):
         d = np.empty(nCells)
         up = np.empty(nFaces)
-        lo = None if self.symmetric() else np.empty(nFaces)
+        lo = None if self.lower is None else np.empty(nFaces)
         _check(lib().cfx_matrix_coarse(self.h, level, _hp(d), _hp(up), _hp(lo)), "coarse")
         return d, up, lo
 
@@ -513,11 +519,18 @@ class Solver:
     def __init__(self, fieldName, matrix, controls):
         self.fieldName = fieldName
         self.matrix = matrix
-        self.controlDict = dict(controls)
-        self.c = _controls(self.controlDict, matrix.symmetric())
+        self.read(controls)
 
     def read(self, controls):
         self.controlDict = dict(controls)
+        if getattr(self.matrix, "diagonal", lambda: False)():
+            # diagonalSolver: chosen before the solver name is looked at
+            # (lduMatrixSolver.C:52-66); the keyword must still be present
+            if "solver" not in self.controlDict:
+                raise FatalError("keyword solver is undefined in dictionary")
+            self.c = Controls()
+            lib().cfx_default_controls(ctypes.byref(self.c))
+            return
         self.c = _controls(self.controlDict, self.matrix.symmetric())
 
     def _perf(self, p):

@@ -201,6 +201,7 @@ protected:
         );
         c.preconditioner =
             pre == "DIC" ? CFX_PRE_DIC
+          : pre == "FDIC" ? CFX_PRE_FDIC
           : pre == "DILU" ? CFX_PRE_DILU
           : pre == "diagonal" ? CFX_PRE_DIAGONAL
           : pre == "GAMG" ? CFX_PRE_GAMG
@@ -223,6 +224,8 @@ protected:
         );
         c.smoother =
             sm == "DIC" ? CFX_SMOOTH_DIC
+          : sm == "FDIC" ? CFX_SMOOTH_FDIC
+          : sm == "nonBlockingGaussSeidel" ? CFX_SMOOTH_NBGS
           : sm == "symGaussSeidel" ? CFX_SMOOTH_SYMGS
           : sm == "DILU" ? CFX_SMOOTH_DILU
           : sm == "DICGaussSeidel" ? CFX_SMOOTH_DICGS
@@ -336,11 +339,13 @@ CUDA_LDU_SOLVER(cudaPCG, CFX_SOLVER_PCG)
 CUDA_LDU_SOLVER(cudaPBiCGStab, CFX_SOLVER_PBICGSTAB)
 CUDA_LDU_SOLVER(cudaGAMG, CFX_SOLVER_GAMG)
 CUDA_LDU_SOLVER(cudaSmoothSolver, CFX_SOLVER_SMOOTH)
+CUDA_LDU_SOLVER(cudaPBiCG, CFX_SOLVER_PBICG)
 
 defineTypeNameAndDebug(cudaPCG, 0);
 defineTypeNameAndDebug(cudaPBiCGStab, 0);
 defineTypeNameAndDebug(cudaGAMG, 0);
 defineTypeNameAndDebug(cudaSmoothSolver, 0);
+defineTypeNameAndDebug(cudaPBiCG, 0);
 
 lduMatrix::solver::addsymMatrixConstructorToTable<cudaPCG>
     addcudaPCGSymMatrixConstructorToTable_;
@@ -356,6 +361,9 @@ lduMatrix::solver::addsymMatrixConstructorToTable<cudaSmoothSolver>
     addcudaSmoothSolverSymMatrixConstructorToTable_;
 lduMatrix::solver::addasymMatrixConstructorToTable<cudaSmoothSolver>
     addcudaSmoothSolverAsymMatrixConstructorToTable_;
+// PBiCG.C:34-35: asymmetric matrices only
+lduMatrix::solver::addasymMatrixConstructorToTable<cudaPBiCG>
+    addcudaPBiCGAsymMatrixConstructorToTable_;
 
 
 solverPerformance cudaPCG::solve
@@ -383,6 +391,18 @@ solverPerformance cudaPBiCGStab::solve
     const cfx_controls c = controls(CFX_SOLVER_PBICGSTAB);
     if (c.preconditioner == CFX_PRE_GAMG) gamgLevels(e, *preconditionerDict());
     return run(e, c, psi, source);
+}
+
+
+solverPerformance cudaPBiCG::solve
+(
+    scalarField& psi,
+    const scalarField& source,
+    const direction
+) const
+{
+    Entry& e = deviceMatrix();
+    return run(e, controls(CFX_SOLVER_PBICG), psi, source);
 }
 
 

@@ -432,6 +432,92 @@ int ldu_pcg(const ldu_matrix* m, double* psi, const double* b, const ldu_control
     return 0;
 }
 
+/* DILUPreconditioner::preconditionT, DILUPreconditioner.C:138-185: forward
+ * over the faces in order with the upper coefficients, backward over the
+ * faces in reverse losort order with the lower ones. */
+static void dilu_precondition_t(const ldu_matrix* m, const double* rD, const double* r, double* w) {
+    const int n = m->nCells, nf = m->nFaces;
+    const double* lo = lowerOf(m);
+    for (int c = 0; c < n; ++c) w[c] = rD[c] * r[c];
+    for (int f = 0; f < nf; ++f) w[m->u[f]] -= rD[m->u[f]] * m->upper[f] * w[m->l[f]];
+    for (int f = nf - 1; f >= 0; --f) {
+        const int sf = m->losort[f];
+        w[m->l[sf]] -= rD[m->l[sf]] * lo[sf] * w[m->u[sf]];
+    }
+}
+
+/* preconditionT of none / diagonal is precondition (noPreconditioner.H:89-97,
+ * diagonalPreconditioner.H:97-105) */
+static void precon_apply_t(const precon* p, const ldu_matrix* m, double* w, const double* r) {
+    if (p->kind == LDU_PRE_DILU)
+        dilu_precondition_t(m, p->rD, r, w);
+    else
+        precon_apply(p, m, w, r);
+}
+
+int ldu_pbicg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c, int precond,
+              ldu_perf* perf) {
+    const int n = m->nCells;
+    double* pA = (double*)xmalloc(sizeof(double) * n);
+    double* wA = (double*)xmalloc(sizeof(double) * n);
+    double* rA = (double*)xmalloc(sizeof(double) * n);
+    memset(perf, 0, sizeof(*perf));
+    ldu_amul(m, psi, wA);
+    for (int i = 0; i < n; ++i) rA[i] = b[i] - wA[i];
+    const double normFactor = ldu_norm_factor(m, psi, b, wA, pA);
+    perf->initialResidual = ldu_sum_mag(n, rA) / normFactor;
+    perf->finalResidual = perf->initialResidual;
+    if (c->minIter > 0 || !check_convergence(perf, c)) {
+        double* pT = (double*)calloc(n ? n : 1, sizeof(double));
+        double* wT = (double*)xmalloc(sizeof(double) * n);
+        double* rT = (double*)xmalloc(sizeof(double) * n);
+        ldu_tmul(m, psi, wT);
+        for (int i = 0; i < n; ++i) rT[i] = b[i] - wT[i];
+        double wArT = 0;
+        precon P;
+        precon_init(&P, m, precond);
+        do {
+            const double wArTold = wArT;
+            precon_apply(&P, m, wA, rA);
+            precon_apply_t(&P, m, wT, rT);
+            wArT = ldu_sum_prod(n, wA, rT);
+            if (perf->nIterations == 0) {
+                for (int i = 0; i < n; ++i) {
+                    pA[i] = wA[i];
+                    pT[i] = wT[i];
+                }
+            } else {
+                const double beta = wArT / wArTold;
+                for (int i = 0; i < n; ++i) {
+                    pA[i] = wA[i] + beta * pA[i];
+                    pT[i] = wT[i] + beta * pT[i];
+                }
+            }
+            ldu_amul(m, pA, wA);
+            ldu_tmul(m, pT, wT);
+            const double wApT = ldu_sum_prod(n, wA, pT);
+            if (check_singularity(perf, fabs(wApT) / normFactor)) break;
+            const double alpha = wArT / wApT;
+            for (int i = 0; i < n; ++i) {
+                psi[i] += alpha * pA[i];
+                rA[i] -= alpha * wA[i];
+                rT[i] -= alpha * wT[i];
+            }
+            perf->finalResidual = ldu_sum_mag(n, rA) / normFactor;
+        } while ((++perf->nIterations < c->maxIter && !check_convergence(perf, c)) ||
+                 perf->nIterations < c->minIter);
+        free(P.rD);
+        free(pT);
+        free(wT);
+        free(rT);
+    }
+    free(pA);
+    free(wA);
+    free(rA);
+    const int lim = c->maxIter > 1000 ? c->maxIter : 1000;
+    return perf->nIterations > lim ? -2 : 0;
+}
+
 /* PBiCGStab::solve, PBiCGStab.C:68-254 */
 int ldu_pbicgstab(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
                   int precond, ldu_perf* perf) {

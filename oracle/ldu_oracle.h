@@ -84,6 +84,12 @@ int ldu_smooth_solve(const ldu_matrix* m, double* psi, const double* b, const ld
 /* PCG.C:65-193, PBiCGStab.C:68-254.  Return 0 or a negative error. */
 int ldu_pcg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
             int precond, ldu_perf* perf);
+/* PBiCG::solve (PBiCG.C:65-220; asymmetric matrices): precond LDU_PRE_NONE,
+ * DIAGONAL or DILU, with the preconditioner's preconditionT on the
+ * transpose residual.  Returns -2 when the iteration count passes
+ * max(1000, maxIter) (the reference's FatalError). */
+int ldu_pbicg(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c, int precond,
+              ldu_perf* perf);
 int ldu_pbicgstab(const ldu_matrix* m, double* psi, const double* b, const ldu_controls* c,
                   int precond, ldu_perf* perf);
 

@@ -14,9 +14,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libldu_oracle.so")
 
-PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3}
+# FDIC (preconditioner and smoother) is DIC's arithmetic and
+# nonBlockingGaussSeidel without coupled interfaces is GaussSeidel's: the
+# reference's own FDIC / nonBlockingGaussSeidel golden solves pin the aliases
+PRECONDITIONERS = {"none": 0, "diagonal": 1, "DIC": 2, "DILU": 3, "FDIC": 2}
 SMOOTHERS = {"GaussSeidel": 0, "DIC": 1, "symGaussSeidel": 2, "DILU": 3, "DICGaussSeidel": 4,
-             "DILUGaussSeidel": 5}
+             "DILUGaussSeidel": 5, "FDIC": 1,
+             "nonBlockingGaussSeidel": 0}
 
 i32p = ctypes.POINTER(ctypes.c_int)
 f64p = ctypes.POINTER(ctypes.c_double)
@@ -216,6 +220,19 @@ def smooth_solve(s, psi, smoother="GaussSeidel", n_sweeps=1, tol=1e-6, rel_tol=0
     c = _controls(tol, rel_tol, max_iter, min_iter)
     lib().ldu_smooth_solve(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c), SMOOTHERS[smoother],
                            int(n_sweeps), ctypes.byref(perf))
+    return _perf(perf)
+
+
+def pbicg(s, psi, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, precond="DILU"):
+    """PBiCG::solve (asymmetric matrices); psi is updated in place."""
+    m = Matrix(s)
+    b = np.ascontiguousarray(s["source"], np.float64)
+    perf = LduPerf()
+    c = _controls(tol, rel_tol, max_iter, min_iter)
+    rc = lib().ldu_pbicg(ctypes.byref(m.c), _p(psi), _p(b), ctypes.byref(c), PRECONDITIONERS[precond],
+                         ctypes.byref(perf))
+    if rc == -2:
+        raise ValueError("PBiCG has failed to converge within the maximum number of iterations")
     return _perf(perf)
 
 

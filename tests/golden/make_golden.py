@@ -102,6 +102,20 @@ SOLVES = {
                                         nCellsInCoarsestLevel=60, tolerance=1e-9, relTol=0.0)),
     "gamg_direct_asym": ("cd10", dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True,
                                       tolerance=1e-9, relTol=0.0)),
+    "pcg_fdic": ("jcube14", dict(solver="PCG", preconditioner="FDIC", tolerance=1e-9, relTol=0.0)),
+    "bicgstab_fdic": ("cube6", dict(solver="PBiCGStab", preconditioner="FDIC", tolerance=1e-9, relTol=0.0)),
+    "smooth_fdic": ("cube12", dict(solver="smoothSolver", smoother="FDIC", nSweeps=2, tolerance=1e-7,
+                                   relTol=0.0, maxIter=5000)),
+    "smooth_nbgs_asym": ("cd10", dict(solver="smoothSolver", smoother="nonBlockingGaussSeidel", tolerance=1e-9,
+                                      relTol=0.0)),
+    "gamg_nbgs": ("jcube14", dict(solver="GAMG", smoother="nonBlockingGaussSeidel", nPreSweeps=1,
+                                  tolerance=1e-8, relTol=0.0)),
+    "gamg_fdic": ("jcube16", dict(solver="GAMG", smoother="FDIC", tolerance=1e-9, relTol=0.0)),
+    "pbicg_dilu": ("cd10", dict(solver="PBiCG", preconditioner="DILU", tolerance=1e-9, relTol=0.0,
+                                maxIter=2000)),
+    "pbicg_diagonal": ("cd6", dict(solver="PBiCG", preconditioner="diagonal", tolerance=1e-8, relTol=0.0,
+                                   maxIter=2000)),
+    "pbicg_none_reltol": ("cd6", dict(solver="PBiCG", preconditioner="none", tolerance=0.0, relTol=1e-4)),
     "pcg_gamg_direct": ("jcube14", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
                                         preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel",
                                                             directSolveCoarsest=True,

@@ -27,11 +27,11 @@ RTOL_FP64 = 1e-10
 
 
 def _iters_ok(solver, ours, ref, n_sweeps=1):
-    """PCG and GAMG: +-1 iteration.  PBiCGStab on the asymmetric upwind
-    matrix is sensitive to the order of its six reductions per iteration
-    (the GPU sums in a fixed tree, the reference sequentially), so its count
-    may move by a few: within 10% (and 4) of the reference's."""
-    if solver == "PBiCGStab":
+    """PCG and GAMG: +-1 iteration.  PBiCGStab and PBiCG on the asymmetric
+    upwind matrix are sensitive to the order of their reductions per
+    iteration (the GPU sums in a fixed tree, the reference sequentially), so
+    their count may move by a few: within 10% (and 4) of the reference's."""
+    if solver in ("PBiCGStab", "PBiCG"):
         return abs(ours - ref) <= max(4, ref // 10)
     if solver == "smoothSolver":
         # sweeps are bit-exact; the residual check sums in a tree, so the
@@ -48,7 +48,7 @@ def _residual_ok(s, psi, tol):
 
 
 _PLUGIN_NAMES = {"PCG": "cudaPCG", "PBiCGStab": "cudaPBiCGStab", "GAMG": "cudaGAMG",
-                 "smoothSolver": "cudaSmoothSolver"}
+                 "smoothSolver": "cudaSmoothSolver", "PBiCG": "cudaPBiCG"}
 
 
 def _ctl(ctl):
@@ -72,14 +72,15 @@ def test_golden_solves(name):
     assert perf.initialResidual == pytest.approx(float(g["initialResidual"][0]), rel=1e-12)
     assert perf.converged == bool(g["converged"][0])
     assert not perf.singular
-    if perf.nIterations == int(g["nIterations"][0]) and ctl["solver"] != "PBiCGStab":
+    if perf.nIterations == int(g["nIterations"][0]) and ctl["solver"] not in ("PBiCGStab", "PBiCG"):
         assert _rel(psi, g["psi"]) <= RTOL_FP64, _rel(psi, g["psi"])
     else:
         # a different iteration count: both solutions meet the tolerance (the
         # residual of ours is recomputed by the oracle in FP64); on the
         # ill-conditioned upwind system that still allows a relative
         # difference of order tolerance*condition
-        _residual_ok(s, psi, ctl.get("tolerance", 1e-6))
+        # the convergence criterion: tolerance, or relTol x initial residual
+        _residual_ok(s, psi, max(ctl.get("tolerance", 1e-6), ctl.get("relTol", 0.0) * perf.initialResidual))
         assert _rel(psi, g["psi"]) <= 1e-4, _rel(psi, g["psi"])
 
 
@@ -331,3 +332,43 @@ def test_gamg_direct_coarsest_against_oracle(n_coarsest):
     perf = ldu.solve(s, psi, dict(ctl, precision="mixed"))
     assert perf.converged
     _residual_ok(s, psi, 1e-9)
+
+
+def test_diagonal_matrix_uses_diagonal_solver():
+    """A diagonal matrix (no off-diagonal coefficients) is solved by
+    diagonalSolver: psi = source/diag bit for bit, "diagonal", 0 iterations,
+    converged, whatever solver the dictionary names."""
+    s = cases.pcg_cube(6, seed=2)
+    mesh = ldu.LduMesh(ldu.default_context(), s["diag"].size, s["l"], s["u"])
+    A = ldu.LduMatrix(mesh, s["diag"])
+    assert A.diagonal() and not A.symmetric()
+    for name in ("cudaPCG", "cudaGAMG", "PBiCG"):
+        psi = np.zeros_like(s["source"])
+        perf = ldu.solver_new("p", A, {"solver": name}).solve(psi, s["source"])
+        np.testing.assert_array_equal(psi, s["source"] / s["diag"])
+        assert perf.solverName == "diagonal" and perf.nIterations == 0 and perf.converged
+        assert perf.initialResidual == 0 and perf.finalResidual == 0
+
+
+def test_pbicg_against_oracle_and_its_errors():
+    """cudaPBiCG with DILU (its preconditionT on the transpose's packs),
+    diagonal and none against the oracle; refused on a symmetric matrix, with
+    the GAMG preconditioner (no preconditionT) and in mixed precision."""
+    cd = cases.convection_diffusion(cases.box_mesh(12, 9, 7, jitter=0.1, seed=5), [1.0, 0.4, 0.1], 2e-2)
+    cd["source"] = cases.uniform(33, cd["diag"].size)
+    for pre in ("DILU", "diagonal", "none"):
+        ref = np.zeros_like(cd["source"])
+        rp = orc.pbicg(cd, ref, tol=1e-9, max_iter=3000, precond=pre)
+        psi = np.zeros_like(cd["source"])
+        perf = ldu.solve(cd, psi, {"solver": "cudaPBiCG", "preconditioner": pre, "tolerance": 1e-9, "relTol": 0,
+                                   "maxIter": 3000})
+        assert perf.solverName == pre + "PBiCG" and perf.converged, pre
+        assert _iters_ok("PBiCG", perf.nIterations, rp.nIterations), (pre, perf.nIterations, rp.nIterations)
+        _residual_ok(cd, psi, 1e-9)
+        assert _rel(psi, ref) <= 1e-6, pre
+    s = cases.pcg_cube(6, seed=1)
+    with pytest.raises(ldu.FatalError, match="Unknown symmetric matrix solver"):
+        ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaPBiCG", "preconditioner": "diagonal"})
+    with pytest.raises(ldu.FatalError, match="mixed"):
+        ldu.solve(cd, np.zeros_like(cd["source"]), {"solver": "cudaPBiCG", "preconditioner": "DILU",
+                                                    "precision": "mixed"})

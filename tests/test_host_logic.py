@@ -61,6 +61,23 @@ def test_unknown_solver_is_fatal_like_the_reference():
         ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaGAMG", "agglomerator": "algebraicPair"})
 
 
+class _FakeDiagonal:
+    def diagonal(self):
+        return True
+
+    def symmetric(self):
+        return False
+
+
+def test_diagonal_matrix_selects_diagonal_solver_before_the_name():
+    """lduMatrix::solver::New (lduMatrixSolver.C:52-66): a diagonal matrix
+    gets diagonalSolver whatever the solver name; the keyword must exist."""
+    s = ldu.solver_new("p", _FakeDiagonal(), {"solver": "PBiCG", "preconditioner": "ILU0"})
+    assert s.c.solver == ldu.SOLVER_PCG  # unused: the library solves psi = source/diag
+    with pytest.raises(ldu.FatalError, match="keyword solver is undefined"):
+        ldu.solver_new("p", _FakeDiagonal(), {"tolerance": 1e-6})
+
+
 def test_smooth_solver_controls_parse():
     s = ldu.solver_new("p", _FakeMatrix(True), {"solver": "cudaSmoothSolver", "smoother": "symGaussSeidel",
                                                 "nSweeps": 2, "tolerance": 1e-7})

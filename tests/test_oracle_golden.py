@@ -74,6 +74,8 @@ def _run_oracle(s, ctl):
                          pre_rel_tol=pre.get("relTol", 0.0), **kw, **gamg_kwargs(pre))
     elif ctl["solver"] == "PCG":
         p = orc.pcg(s, psi, precond=ctl["preconditioner"], **kw)
+    elif ctl["solver"] == "PBiCG":
+        p = orc.pbicg(s, psi, precond=ctl["preconditioner"], **kw)
     elif ctl["solver"] == "PBiCGStab":
         p = orc.pbicgstab(s, psi, precond=ctl["preconditioner"], **kw)
     elif ctl["solver"] == "smoothSolver":

@@ -178,11 +178,61 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
 /* Re-upload coefficients (a new fvMatrix on the same mesh, every solve). */
 cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper,
                              const double* lower);
+/* A matrix of zero coefficients (symmetric: no lower triangle), to be filled
+ * on the device by cfx_fvm_assemble or cfx_matrix_update_device. */
+cfx_status cfx_matrix_create_empty(cfx_mesh* mesh, int symmetric, cfx_matrix** mat);
+
+/* ---- finite-volume assembly on the device ------------------------------- */
+/* Face geometry of the fvMesh behind an lduMesh, uploaded once (host
+ * arrays): per internal face (lduAddressing order) magSf, the snGrad
+ * scheme's deltaCoeffs and the linear interpolation weights (may be NULL
+ * when no linear div term is assembled); per cell V; per boundary face, in
+ * patch order, its cell, magSf and deltaCoeffs. */
+cfx_status cfx_fv_geometry(cfx_mesh* mesh, const double* magSf, const double* deltaCoeffs, const double* weights,
+                           const double* V, int32_t nBoundaryFaces, const int32_t* boundaryCells,
+                           const double* magSfB, const double* deltaCoeffsB);
+
+enum { CFX_DIV_UPWIND = 0, CFX_DIV_LINEAR = 1 };
+enum { CFX_BC_ZERO_GRADIENT = 0, CFX_BC_FIXED_VALUE = 1, CFX_BC_FIXED_GRADIENT = 2 };
+
+/* fvm::ddt(psi) + fvm::div(phi, psi) + lapSign*fvm::laplacian(gamma, psi)
+ * == su, every pointer a device array, every term optional:
+ *   ddt (Euler, EulerDdtScheme.C:466-497) when rDeltaT > 0, psi0 = old psi;
+ *   div (gaussConvectionScheme.C:121-152) when phi != NULL: face fluxes of
+ *     the internal faces and phiB of the boundary faces; divScheme
+ *     CFX_DIV_UPWIND (pos0(phi)) or CFX_DIV_LINEAR (the mesh weights);
+ *   laplacian (gaussLaplacianScheme.C:47-89) when lapSign = +1 or -1:
+ *     gamma/gammaB per face, or gammaUniform when gamma == NULL;
+ *   su (NULL: none): operator==, source += V*su.
+ * psi's boundary conditions per boundary face: bcType CFX_BC_* and bcValue
+ * (the fixed value or the fixed gradient). */
+typedef struct {
+    double rDeltaT;
+    const double* psi0;
+    const double* phi;
+    const double* phiB;
+    int divScheme;
+    int lapSign;
+    double gammaUniform;
+    const double* gamma;
+    const double* gammaB;
+    const int32_t* bcType;
+    const double* bcValue;
+    const double* su;
+} cfx_fvm_terms;
+
+/* Assembles the equation into mat's coefficients (on the device; as
+ * fvMatrix::solveSegregated hands them to the solver, boundary diagonal
+ * included) and its source into d_source (device, nCells).  A div term makes
+ * the matrix asymmetric: mat must then have been created asymmetric. */
+cfx_status cfx_fvm_assemble(cfx_matrix* mat, const cfx_fvm_terms* terms, double* d_source);
+
 /* Same with device pointers (coefficients already in HBM). */
 cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* d_diag, const double* d_upper,
                                     const double* d_lower);
 cfx_status cfx_matrix_destroy(cfx_matrix* mat);
-/* Coarse-level coefficients assembled on the device (level >= 1), copied out. */
+/* Coefficients of level `level` copied out: 0 the matrix itself (e.g. after
+ * cfx_fvm_assemble), >= 1 the coarse levels assembled on the device. */
 cfx_status cfx_matrix_coarse(cfx_matrix* mat, int level, double* diag, double* upper, double* lower);
 
 /* ---- solve (lduMatrix::solver::solve) ------------------------------------ */

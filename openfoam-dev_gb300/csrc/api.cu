@@ -50,6 +50,9 @@ struct cfx_mesh {
     };
     std::vector<Scheds> sched;
     Arena schedArena;
+    FvGeom fv;  // finite-volume face geometry (cfx_fv_geometry)
+    bool hasFv = false;
+    Arena fvArena;
 };
 
 template <class T>
@@ -335,6 +338,12 @@ void prepare_levels(cfx_matrix* mat, bool want32) {
 
 void invalidate_packs(cfx_matrix* mat);
 
+void coefficients_changed(cfx_matrix* mat) {
+    Ops<double>::permute(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0]);
+    mat->coarse64 = mat->coarse32 = mat->fine32 = false;
+    invalidate_packs(mat);
+}
+
 void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, const double* lower,
                       cudaMemcpyKind kind) {
     cfx_mesh* mesh = mat->mesh;
@@ -345,9 +354,7 @@ void set_coefficients(cfx_matrix* mat, const double* diag, const double* upper, 
     if (m.nf && upper) CK(cudaMemcpyAsync(c.upper, upper, sizeof(double) * m.nf, kind, s));
     if (m.nf && !upper) CK(cudaMemsetAsync(c.upper, 0, sizeof(double) * m.nf, s));  // diagonal matrix
     if (!mat->sym && m.nf) CK(cudaMemcpyAsync(c.lower, lower, sizeof(double) * m.nf, kind, s));
-    Ops<double>::permute(s, m, c);
-    mat->coarse64 = mat->coarse32 = mat->fine32 = false;
-    invalidate_packs(mat);
+    coefficients_changed(mat);
 }
 
 // ---- packed sweep schedules and coefficients ------------------------------
@@ -1625,6 +1632,125 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
     });
 }
 
+cfx_status cfx_matrix_create_empty(cfx_mesh* mesh, int symmetric, cfx_matrix** out) {
+    if (!mesh || !out) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        auto mat = std::make_unique<cfx_matrix>();
+        mat->mesh = mesh;
+        mat->sym = symmetric != 0;
+        LevelCoeffs<double> c;
+        alloc_coeffs(mat->arena, mesh->dev[0], mat->sym, c);
+        mat->c64.push_back(c);
+        const LevelMesh& m = mesh->dev[0];
+        mat->d_psi = mat->arena.get<double>(m.n);
+        mat->d_src = mat->arena.get<double>(m.n);
+        cudaStream_t s = mesh->ctx->stream;
+        CK(cudaMemsetAsync(c.diag, 0, sizeof(double) * m.n, s));
+        if (m.nf) CK(cudaMemsetAsync(c.upper, 0, sizeof(double) * m.nf, s));
+        if (m.nf && !mat->sym) CK(cudaMemsetAsync(c.lower, 0, sizeof(double) * m.nf, s));
+        coefficients_changed(mat.get());
+        CK(cudaStreamSynchronize(s));
+        *out = mat.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_fv_geometry(cfx_mesh* mesh, const double* magSf, const double* deltaCoeffs, const double* weights,
+                           const double* V, int32_t nB, const int32_t* bCell, const double* magSfB,
+                           const double* deltaCoeffsB) {
+    if (!mesh || !V || nB < 0) return CFX_ERR_ARG;
+    const HostLevel& h = mesh->host[0];
+    if (h.nf && (!magSf || !deltaCoeffs)) return CFX_ERR_ARG;
+    if (nB && (!bCell || !magSfB || !deltaCoeffsB)) return CFX_ERR_ARG;
+    for (int b = 0; b < nB; ++b)
+        if (bCell[b] < 0 || bCell[b] >= h.n) {
+            set_error("cfx_fv_geometry: boundary face cell out of range");
+            return CFX_ERR_ADDRESSING;
+        }
+    return guard([&]() -> cfx_status {
+        cudaStream_t s = mesh->ctx->stream;
+        CK(cudaStreamSynchronize(s));
+        mesh->fvArena.release();
+        FvGeom g;
+        auto up = [&](const double* p, int n) -> double* {
+            if (!p) return nullptr;
+            double* d = mesh->fvArena.get<double>(n);
+            if (n) CK(cudaMemcpyAsync(d, p, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            return d;
+        };
+        g.nBoundary = nB;
+        g.magSf = up(magSf, h.nf);
+        g.deltaCoeffs = up(deltaCoeffs, h.nf);
+        g.weights = up(weights, h.nf);
+        g.V = up(V, h.n);
+        g.magSfB = up(magSfB, nB);
+        g.deltaCoeffsB = up(deltaCoeffsB, nB);
+        // cell -> boundary faces, ascending (a stable counting sort)
+        std::vector<int> start(h.n + 1, 0), face(nB), cell(bCell, bCell + nB);
+        for (int b = 0; b < nB; ++b) start[bCell[b] + 1]++;
+        for (int c = 0; c < h.n; ++c) start[c + 1] += start[c];
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int b = 0; b < nB; ++b) face[fill[bCell[b]]++] = b;
+        g.bCell = mesh->fvArena.upload(cell, s);
+        g.bStart = mesh->fvArena.upload(start, s);
+        g.bFace = mesh->fvArena.upload(face, s);
+        CK(cudaStreamSynchronize(s));
+        mesh->fv = g;
+        mesh->hasFv = true;
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_fvm_assemble(cfx_matrix* mat, const cfx_fvm_terms* t, double* d_source) {
+    if (!mat || !t || !d_source) return CFX_ERR_ARG;
+    cfx_mesh* mesh = mat->mesh;
+    if (!mesh->hasFv) {
+        set_error("cfx_fvm_assemble: no face geometry (cfx_fv_geometry)");
+        return CFX_ERR_STATE;
+    }
+    const FvGeom& g = mesh->fv;
+    const bool ddt = t->rDeltaT > 0, div = t->phi != nullptr, lap = t->lapSign != 0;
+    const int nB = g.nBoundary;
+    std::string why;
+    if (!ddt && !div && !lap) why = "no term";
+    else if (ddt && !t->psi0) why = "ddt without psi0";
+    else if (div && nB && !t->phiB) why = "div without boundary fluxes";
+    else if (div && t->divScheme != CFX_DIV_UPWIND && t->divScheme != CFX_DIV_LINEAR) why = "unknown div scheme";
+    else if (div && t->divScheme == CFX_DIV_LINEAR && !g.weights) why = "linear div without weights";
+    else if (lap && t->lapSign != 1 && t->lapSign != -1) why = "lapSign must be +1, -1 or 0";
+    else if (lap && t->gamma && nB && !t->gammaB) why = "laplacian gamma without boundary values";
+    else if (nB && (!t->bcType || !t->bcValue)) why = "boundary conditions missing";
+    else if (div == mat->sym) why = div ? "a div term needs an asymmetric matrix" : "an asymmetric matrix without a div term";
+    if (!why.empty()) {
+        set_error("cfx_fvm_assemble: " + why);
+        return CFX_ERR_ARG;
+    }
+    return guard([&]() -> cfx_status {
+        FvmArgs a{};
+        a.rDeltaT = t->rDeltaT;
+        a.psi0 = t->psi0;
+        a.phi = t->phi;
+        a.phiB = t->phiB;
+        a.divScheme = t->divScheme;
+        a.lapSign = t->lapSign;
+        a.gammaUniform = t->gammaUniform;
+        a.gamma = t->gamma;
+        a.gammaB = t->gammaB;
+        a.bcType = t->bcType;
+        a.bcValue = t->bcValue;
+        a.su = t->su;
+        a.hasDdt = ddt;
+        a.hasDiv = div;
+        LevelCoeffs<double>& c = mat->c64[0];
+        launch_fvm_assemble(mesh->ctx->stream, mesh->dev[0], g, a, c.diag, c.upper, mat->sym ? nullptr : c.lower,
+                            d_source);
+        CK(cudaGetLastError());
+        mat->diagonal = false;
+        coefficients_changed(mat);
+        return CFX_OK;
+    });
+}
+
 cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper, const double* lower) {
     if (!mat || !diag || (mat->sym != (lower == nullptr)) || (mat->diagonal != (upper == nullptr))) {
         set_error("cfx_matrix_update: symmetry of the coefficients changed or null diag");
@@ -1654,9 +1780,9 @@ cfx_status cfx_matrix_destroy(cfx_matrix* mat) {
 }
 
 cfx_status cfx_matrix_coarse(cfx_matrix* mat, int level, double* diag, double* upper, double* lower) {
-    if (!mat || level < 1 || level > mat->mesh->nCoarseLevels) return CFX_ERR_ARG;
+    if (!mat || level < 0 || level > mat->mesh->nCoarseLevels) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
-        prepare_levels(mat, false);
+        if (level > 0) prepare_levels(mat, false);
         const LevelMesh& m = mat->mesh->dev[level];
         cudaStream_t s = mat->mesh->ctx->stream;
         const LevelCoeffs<double>& c = mat->c64[level];

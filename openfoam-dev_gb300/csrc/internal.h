@@ -155,6 +155,40 @@ struct Ops {
     static void diag_solve(cudaStream_t s, int n, const T* diag, const T* b, T* x);
 };
 
+// ---- finite-volume assembly (fvm.cu) -------------------------------------
+// Resident face geometry of an fvMesh: internal faces in lduAddressing order,
+// boundary faces in patch order; cell -> boundary faces (ascending).
+struct FvGeom {
+    int nBoundary = 0;
+    double *magSf = nullptr, *deltaCoeffs = nullptr, *weights = nullptr, *V = nullptr;
+    int* bCell = nullptr;
+    double *magSfB = nullptr, *deltaCoeffsB = nullptr;
+    int *bStart = nullptr, *bFace = nullptr;  // [n+1], [nBoundary]
+};
+
+// The terms of one assembly (device pointers; see cfx_fvm_terms).  first:
+// the term that starts the fvMatrix (FVM_*), sgnDiv/sgnLap the signs the
+// others enter with (0: absent).
+enum { FVM_DDT = 0, FVM_DIV = 1, FVM_LAP = 2 };
+struct FvmArgs {
+    double rDeltaT;
+    const double* psi0;
+    const double *phi, *phiB;
+    int divScheme;
+    int lapSign;
+    double gammaUniform;
+    const double *gamma, *gammaB;
+    const int* bcType;
+    const double* bcValue;
+    const double* su;
+    int hasDdt, hasDiv;
+};
+
+// diag, upper, lower (asymmetric results) and source of the assembled
+// equation as fvMatrix::solveSegregated hands them to the solver.
+void launch_fvm_assemble(cudaStream_t s, const LevelMesh& m, const FvGeom& g, const FvmArgs& a, double* diag,
+                         double* upper, double* lower, double* source);
+
 void launch_cast_d2f(cudaStream_t s, int64_t n, const double* in, float* out);
 void launch_cast_f2d(cudaStream_t s, int64_t n, const float* in, double* out);
 

@@ -98,6 +98,18 @@ class ServerStats(ctypes.Structure):
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _d = ctypes.c_double
+class FvmTerms(ctypes.Structure):
+    """cfx_fvm_terms: the terms of a device-side fvMatrix assembly."""
+    _fields_ = [("rDeltaT", ctypes.c_double), ("psi0", ctypes.c_void_p), ("phi", ctypes.c_void_p),
+                ("phiB", ctypes.c_void_p), ("divScheme", ctypes.c_int), ("lapSign", ctypes.c_int),
+                ("gammaUniform", ctypes.c_double), ("gamma", ctypes.c_void_p), ("gammaB", ctypes.c_void_p),
+                ("bcType", ctypes.c_void_p), ("bcValue", ctypes.c_void_p), ("su", ctypes.c_void_p)]
+
+
+DIV_SCHEMES = {"upwind": 0, "linear": 1}
+BC_TYPES = {"zeroGradient": 0, "fixedValue": 1, "fixedGradient": 2}
+
+
 _SIG = {
     "cfx_default_controls": (None, [ctypes.POINTER(Controls)]),
     "cfx_last_error": (ctypes.c_char_p, []),
@@ -118,6 +130,9 @@ _SIG = {
     "cfx_matrix_create": (_i, [_vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "cfx_matrix_update": (_i, [_vp, _vp, _vp, _vp]),
     "cfx_matrix_update_device": (_i, [_vp, _vp, _vp, _vp]),
+    "cfx_matrix_create_empty": (_i, [_vp, _i, ctypes.POINTER(_vp)]),
+    "cfx_fv_geometry": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
+    "cfx_fvm_assemble": (_i, [_vp, ctypes.POINTER(FvmTerms), _vp]),
     "cfx_matrix_destroy": (_i, [_vp]),
     "cfx_matrix_coarse": (_i, [_vp, _i, _vp, _vp, _vp]),
     "cfx_solve": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, ctypes.POINTER(Perf)]),
@@ -322,6 +337,16 @@ class LduMesh:
                "level_info")
         return ra, fra, fl, nc.value, ncf.value, cl, cu
 
+    def fv_geometry(self, magSf, deltaCoeffs, V, bCell, magSfB, deltaCoeffsB, weights=None):
+        """Face geometry for device-side assembly (host arrays, uploaded once):
+        internal faces in lduAddressing order, boundary faces in patch order."""
+        f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        self._fv = [f(magSf), f(deltaCoeffs), f(weights), f(V), np.ascontiguousarray(bCell, np.int32),
+                    f(magSfB), f(deltaCoeffsB)]
+        a = self._fv
+        _check(lib().cfx_fv_geometry(self.h, _hp(a[0]), _hp(a[1]), _hp(a[2]), _hp(a[3]), len(a[4]), _hp(a[4]),
+                                     _hp(a[5]), _hp(a[6])), "cfx_fv_geometry")
+
     def close(self):
         h, self.h = getattr(self, "h", None), None
         if h:
@@ -348,6 +373,32 @@ class LduMatrix:
                "cfx_matrix_create")
         self.h = h
         _track("matrix", self)
+
+    @classmethod
+    def empty(cls, mesh, symmetric):
+        """A matrix of zero coefficients to be assembled on the device."""
+        A = cls.__new__(cls)
+        A.mesh = mesh
+        A.diag = np.zeros(0)
+        A.upper = np.zeros(0)
+        A.lower = None if symmetric else np.zeros(0)
+        h = ctypes.c_void_p()
+        _check(lib().cfx_matrix_create_empty(mesh.h, int(bool(symmetric)), ctypes.byref(h)), "cfx_matrix_create_empty")
+        A.h = h
+        _track("matrix", A)
+        return A
+
+    def assemble(self, source, rDeltaT=0.0, psi0=None, phi=None, phiB=None, div="upwind", lapSign=0, gamma=1.0,
+                 gammaB=None, bcType=None, bcValue=None, su=None):
+        """fvm::ddt(psi) + fvm::div(phi, psi) + lapSign*fvm::laplacian(gamma, psi) == su into this
+        matrix and `source` (CUDA float64 tensors; gamma a float or per-face tensors gamma/gammaB;
+        bcType an int32 tensor of BC_TYPES values)."""
+        import torch
+        uniform = not isinstance(gamma, torch.Tensor)
+        t = FvmTerms(float(rDeltaT), _dp(psi0), _dp(phi), _dp(phiB), DIV_SCHEMES[div], int(lapSign),
+                     float(gamma) if uniform else 0.0, None if uniform else _dp(gamma), _dp(gammaB),
+                     _dp(bcType), _dp(bcValue), _dp(su))
+        _check(lib().cfx_fvm_assemble(self.h, ctypes.byref(t), _dp(source)), "cfx_fvm_assemble")
 
     def diagonal(self):
         return self.upper is None and self.lower is None

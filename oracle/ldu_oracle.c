@@ -1299,3 +1299,236 @@ int ldu_pcg_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi,
     free(rA);
     return 0;
 }
+
+/* ------------------------------------------------ finite-volume assembly */
+
+/* An fvMatrix under construction: lduMatrix coefficient arrays (NULL while
+ * unallocated, lduMatrix.C:168-212), the source and the patch
+ * internal/boundary coefficients (zero-initialised, as fvMatrix's
+ * constructor does). */
+typedef struct {
+    int nCells, nFaces, nB;
+    double *diag, *upper, *lower;
+    double *src, *ic, *bc;
+} fvm_mat;
+
+static void fvm_init(fvm_mat* m, const ldu_fv_geom* g) {
+    m->nCells = g->nCells;
+    m->nFaces = g->nFaces;
+    m->nB = g->nBoundary;
+    m->diag = m->upper = m->lower = NULL;
+    m->src = (double*)calloc(g->nCells ? g->nCells : 1, sizeof(double));
+    m->ic = (double*)calloc(g->nBoundary ? g->nBoundary : 1, sizeof(double));
+    m->bc = (double*)calloc(g->nBoundary ? g->nBoundary : 1, sizeof(double));
+}
+
+static void fvm_free(fvm_mat* m) {
+    free(m->diag);
+    free(m->upper);
+    free(m->lower);
+    free(m->src);
+    free(m->ic);
+    free(m->bc);
+}
+
+static double* dup_or_zero(const double* a, int n) {
+    double* p = (double*)calloc(n ? n : 1, sizeof(double));
+    if (a) memcpy(p, a, sizeof(double) * n);
+    return p;
+}
+
+/* lduMatrix::diag() / upper() / lower(): allocate on first use (a copy of
+ * the other triangle when it exists) */
+static double* fvm_diag(fvm_mat* m) {
+    if (!m->diag) m->diag = dup_or_zero(NULL, m->nCells);
+    return m->diag;
+}
+static double* fvm_upper(fvm_mat* m) {
+    if (!m->upper) m->upper = dup_or_zero(m->lower, m->nFaces);
+    return m->upper;
+}
+static double* fvm_lower(fvm_mat* m) {
+    if (!m->lower) m->lower = dup_or_zero(m->upper, m->nFaces);
+    return m->lower;
+}
+
+/* lduMatrix::negSumDiag, lduMatrixOperations.C:55-74 */
+static void fvm_neg_sum_diag(fvm_mat* m, const ldu_fv_geom* g) {
+    if (!m->lower && !m->upper) return;
+    const double* Lower = m->lower ? m->lower : m->upper;
+    const double* Upper = m->upper ? m->upper : m->lower;
+    double* d = fvm_diag(m);
+    for (int f = 0; f < g->nFaces; ++f) {
+        d[g->l[f]] -= Lower[f];
+        d[g->u[f]] -= Upper[f];
+    }
+}
+
+/* fvMatrix::negate, fvMatrix.C:1079-1090 */
+static void fvm_negate(fvm_mat* m) {
+    if (m->lower)
+        for (int f = 0; f < m->nFaces; ++f) m->lower[f] = -m->lower[f];
+    if (m->upper)
+        for (int f = 0; f < m->nFaces; ++f) m->upper[f] = -m->upper[f];
+    if (m->diag)
+        for (int c = 0; c < m->nCells; ++c) m->diag[c] = -m->diag[c];
+    for (int c = 0; c < m->nCells; ++c) m->src[c] = -m->src[c];
+    for (int b = 0; b < m->nB; ++b) {
+        m->ic[b] = -m->ic[b];
+        m->bc[b] = -m->bc[b];
+    }
+}
+
+static void axpy_sign(int n, double s, const double* a, double* y) {
+    if (s > 0)
+        for (int i = 0; i < n; ++i) y[i] += a[i];
+    else
+        for (int i = 0; i < n; ++i) y[i] -= a[i];
+}
+
+/* fvMatrix::operator+= / -= (s = +1 / -1): lduMatrix::operator+=/-=
+ * (lduMatrixOperations.C:159-318) on the coefficients, then the source and
+ * the patch coefficients */
+static void fvm_add(fvm_mat* C, const fvm_mat* A, double s) {
+    const int nf = C->nFaces;
+    if (A->diag) axpy_sign(C->nCells, s, A->diag, fvm_diag(C));
+    const int cSym = C->diag && !C->lower && C->upper, cAsym = C->diag && C->lower && C->upper;
+    const int cDiagonal = C->diag && !C->lower && !C->upper;
+    const int aSym = A->diag && !A->lower && A->upper, aAsym = A->diag && A->lower && A->upper;
+    if (cSym && aSym) {
+        axpy_sign(nf, s, A->upper, fvm_upper(C));
+    } else if (cSym && aAsym) {
+        fvm_lower(C);
+        axpy_sign(nf, s, A->upper, fvm_upper(C));
+        axpy_sign(nf, s, A->lower, fvm_lower(C));
+    } else if (cAsym && aSym) {
+        const double* a = A->upper ? A->upper : A->lower;
+        axpy_sign(nf, s, a, fvm_lower(C));
+        axpy_sign(nf, s, a, fvm_upper(C));
+    } else if (cAsym && aAsym) {
+        axpy_sign(nf, s, A->lower, fvm_lower(C));
+        axpy_sign(nf, s, A->upper, fvm_upper(C));
+    } else if (cDiagonal) {
+        if (A->upper) {
+            double* u = fvm_upper(C);
+            for (int f = 0; f < nf; ++f) u[f] = s > 0 ? A->upper[f] : -A->upper[f];
+        }
+        if (A->lower) {
+            double* l = fvm_lower(C);
+            for (int f = 0; f < nf; ++f) l[f] = s > 0 ? A->lower[f] : -A->lower[f];
+        }
+    }
+    axpy_sign(C->nCells, s, A->src, C->src);
+    axpy_sign(C->nB, s, A->ic, C->ic);
+    axpy_sign(C->nB, s, A->bc, C->bc);
+}
+
+/* EulerDdtScheme::fvmDdt, EulerDdtScheme.C:466-497 (static mesh) */
+static void fvm_ddt(fvm_mat* m, const ldu_fv_geom* g, double rDeltaT, const double* psi0) {
+    double* d = fvm_diag(m);
+    for (int c = 0; c < g->nCells; ++c) {
+        d[c] = rDeltaT * g->V[c];
+        m->src[c] = rDeltaT * psi0[c] * g->V[c];
+    }
+}
+
+/* gaussConvectionScheme::fvmDiv, gaussConvectionScheme.C:121-152, with the
+ * upwind (upwind.H: pos0(faceFlux)) or linear (mesh weights) interpolation
+ * weights; the patch value coefficients of fixedValue (0, value),
+ * zeroGradient (1, 0) and fixedGradient (1, gradient/deltaCoeffs) */
+static void fvm_div(fvm_mat* m, const ldu_fv_geom* g, const ldu_fvm_terms* t) {
+    double* lo = fvm_lower(m);
+    for (int f = 0; f < g->nFaces; ++f) {
+        const double w = t->divScheme == LDU_DIV_UPWIND ? (t->phi[f] >= 0.0 ? 1.0 : 0.0) : g->weights[f];
+        lo[f] = -w * t->phi[f];
+    }
+    double* up = fvm_upper(m);
+    for (int f = 0; f < g->nFaces; ++f) up[f] = lo[f] + t->phi[f];
+    fvm_neg_sum_diag(m, g);
+    for (int b = 0; b < g->nBoundary; ++b) {
+        const int type = t->bcType[b];
+        const double vic = type == LDU_BC_FIXED_VALUE ? 0.0 : 1.0;
+        const double vbc = type == LDU_BC_FIXED_VALUE ? t->bcValue[b]
+                           : type == LDU_BC_FIXED_GRADIENT ? t->bcValue[b] / g->deltaCoeffsB[b]
+                                                           : 0.0;
+        m->ic[b] = t->phiB[b] * vic;
+        m->bc[b] = -t->phiB[b] * vbc;
+    }
+}
+
+/* gaussLaplacianScheme::fvmLaplacian (gaussLaplacianSchemes.C:35-90) with
+ * fvmLaplacianUncorrected (gaussLaplacianScheme.C:47-89): gammaMagSf =
+ * gamma*magSf; the patch gradient coefficients of fixedValue
+ * (-deltaCoeffs, deltaCoeffs*value), zeroGradient (0, 0) and fixedGradient
+ * (0, gradient) */
+static void fvm_laplacian(fvm_mat* m, const ldu_fv_geom* g, const ldu_fvm_terms* t) {
+    double* up = fvm_upper(m);
+    for (int f = 0; f < g->nFaces; ++f) {
+        const double gms = (t->gamma ? t->gamma[f] : t->gammaUniform) * g->magSf[f];
+        up[f] = g->deltaCoeffs[f] * gms;
+    }
+    fvm_neg_sum_diag(m, g);
+    for (int b = 0; b < g->nBoundary; ++b) {
+        const double gms = (t->gammaB ? t->gammaB[b] : t->gammaUniform) * g->magSfB[b];
+        const int type = t->bcType[b];
+        const double gic = type == LDU_BC_FIXED_VALUE ? -1.0 * g->deltaCoeffsB[b] : 0.0;
+        const double gbc = type == LDU_BC_FIXED_VALUE ? g->deltaCoeffsB[b] * t->bcValue[b]
+                           : type == LDU_BC_FIXED_GRADIENT ? t->bcValue[b]
+                                                           : 0.0;
+        m->ic[b] = gms * gic;
+        m->bc[b] = -gms * gbc;
+    }
+}
+
+int ldu_fvm_assemble(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper, double* lower,
+                     double* source) {
+    fvm_mat C, A;
+    int have = 0;
+    fvm_init(&C, g);
+    if (t->rDeltaT > 0) {
+        fvm_ddt(&C, g, t->rDeltaT, t->psi0);
+        have = 1;
+    }
+    if (t->phi) {
+        if (!have) {
+            fvm_div(&C, g, t);
+        } else {
+            fvm_init(&A, g);
+            fvm_div(&A, g, t);
+            fvm_add(&C, &A, 1.0);
+            fvm_free(&A);
+        }
+        have = 1;
+    }
+    if (t->lapSign) {
+        if (!have) {
+            fvm_laplacian(&C, g, t);
+            if (t->lapSign < 0) fvm_negate(&C);
+        } else {
+            fvm_init(&A, g);
+            fvm_laplacian(&A, g, t);
+            fvm_add(&C, &A, t->lapSign > 0 ? 1.0 : -1.0);
+            fvm_free(&A);
+        }
+        have = 1;
+    }
+    if (!have) {
+        fvm_free(&C);
+        return -1;
+    }
+    /* operator==(fvMatrix, field): source += V*su */
+    if (t->su)
+        for (int c = 0; c < g->nCells; ++c) C.src[c] += g->V[c] * t->su[c];
+    /* fvMatrix::solveSegregated: addBoundarySource, addBoundaryDiag */
+    memcpy(diag, fvm_diag(&C), sizeof(double) * g->nCells);
+    memcpy(source, C.src, sizeof(double) * g->nCells);
+    for (int b = 0; b < g->nBoundary; ++b) {
+        diag[g->bCell[b]] += C.ic[b];
+        source[g->bCell[b]] += C.bc[b];
+    }
+    const double* U = C.upper ? C.upper : C.lower;
+    if (U) memcpy(upper, U, sizeof(double) * g->nFaces);
+    if (lower && C.lower) memcpy(lower, C.lower, sizeof(double) * g->nFaces);
+    fvm_free(&C);
+    return 0;
+}

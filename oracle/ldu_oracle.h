@@ -163,6 +163,51 @@ int ldu_pcg_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi,
                  const ldu_controls* c, const ldu_gamg_controls* g, const ldu_controls* pc, int nVcycles,
                  ldu_perf* perf);
 
+/* ---- finite-volume assembly (fvMatrix of a scalar transport equation) ----
+ * Face geometry of an fvMesh: internal faces (lowerAddr/upperAddr = owner /
+ * neighbour) with magSf, the snGrad scheme's deltaCoeffs and the linear
+ * interpolation weights; boundary faces in patch order with their cell,
+ * magSf and deltaCoeffs; cell volumes. */
+typedef struct {
+    int nCells, nFaces, nBoundary;
+    const int *l, *u;
+    const double *magSf, *deltaCoeffs, *weights, *V;
+    const int* bCell;
+    const double *magSfB, *deltaCoeffsB;
+} ldu_fv_geom;
+
+enum { LDU_DIV_UPWIND = 0, LDU_DIV_LINEAR = 1 };
+enum { LDU_BC_ZERO_GRADIENT = 0, LDU_BC_FIXED_VALUE = 1, LDU_BC_FIXED_GRADIENT = 2 };
+
+/* fvm::ddt(psi) + fvm::div(phi, psi) + lapSign*fvm::laplacian(gamma, psi)
+ * == su, each term optional: ddt when rDeltaT > 0 (Euler: psi0 the old
+ * value), div when phi != NULL (upwind or linear weights), laplacian when
+ * lapSign != 0 (gamma per face, or gammaUniform when gamma == NULL); psi's
+ * boundary conditions per boundary face (type, value or gradient). */
+typedef struct {
+    double rDeltaT;
+    const double* psi0;
+    const double *phi, *phiB;
+    int divScheme;
+    int lapSign;
+    double gammaUniform;
+    const double *gamma, *gammaB;
+    const int* bcType;
+    const double* bcValue;
+    const double* su;
+} ldu_fvm_terms;
+
+/* The lduMatrix and source fvMatrix::solveSegregated hands to the solver:
+ * each term built as EulerDdtScheme.C:466-497, gaussConvectionScheme.C:
+ * 121-152 and gaussLaplacianScheme.C:47-89 build it, combined with
+ * fvMatrix::operator+=/-= (fvMatrix.C:1094-1148, lduMatrixOperations.C:
+ * 140-318), operator==(fvMatrix, field) adding V*su (fvMatrix.C:1705-1715),
+ * then addBoundaryDiag / addBoundarySource (fvMatrix.C:112-174).  lower is
+ * written when the result is asymmetric (a div term).  Returns -1 when no
+ * term is given. */
+int ldu_fvm_assemble(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper, double* lower,
+                     double* source);
+
 #ifdef __cplusplus
 }
 #endif

@@ -354,3 +354,47 @@ def coarse_matrix(fine, agg, i):
                                  _p(ra, i32p), _p(fra, i32p), _p(flip, i32p), nc, ncf,
                                  _p(cd), _p(cu), _p(cl))
     return cd, cu[:ncf], (None if cl is None else cl[:ncf])
+
+
+class LduFvGeom(ctypes.Structure):
+    _fields_ = [("nCells", ctypes.c_int), ("nFaces", ctypes.c_int), ("nBoundary", ctypes.c_int),
+                ("l", i32p), ("u", i32p), ("magSf", f64p), ("deltaCoeffs", f64p), ("weights", f64p),
+                ("V", f64p), ("bCell", i32p), ("magSfB", f64p), ("deltaCoeffsB", f64p)]
+
+
+class LduFvmTerms(ctypes.Structure):
+    _fields_ = [("rDeltaT", ctypes.c_double), ("psi0", f64p), ("phi", f64p), ("phiB", f64p),
+                ("divScheme", ctypes.c_int), ("lapSign", ctypes.c_int), ("gammaUniform", ctypes.c_double),
+                ("gamma", f64p), ("gammaB", f64p), ("bcType", i32p), ("bcValue", f64p), ("su", f64p)]
+
+
+DIV_SCHEMES = {"upwind": 0, "linear": 1}
+
+
+def fvm_assemble(l, u, geom, rDeltaT=0.0, psi0=None, phi=None, phiB=None, div="upwind", lapSign=0, gamma=1.0,
+                 gammaB=None, bcType=None, bcValue=None, su=None):
+    """The lduMatrix (diag, upper, lower or None) and source that
+    fvMatrix::solveSegregated hands to the solver for
+    fvm::ddt + fvm::div - or + fvm::laplacian == su (ldu_fvm_assemble).
+    geom: magSf, deltaCoeffs, weights, V, bCell, magSfB, deltaCoeffsB."""
+    f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+    i = lambda a: None if a is None else np.ascontiguousarray(a, np.int32)
+    l, u = i(l), i(u)
+    g = {k: f(geom[k]) if k != "bCell" else i(geom[k]) for k in geom}
+    nC, nF, nB = g["V"].size, l.size, g["bCell"].size
+    keep = [l, u, g]
+    gc = LduFvGeom(nC, nF, nB, _p(l, i32p), _p(u, i32p), _p(g["magSf"]), _p(g["deltaCoeffs"]),
+                   _p(g.get("weights")), _p(g["V"]), _p(g["bCell"], i32p), _p(g["magSfB"]), _p(g["deltaCoeffsB"]))
+    uniform = np.isscalar(gamma)
+    arrs = dict(psi0=f(psi0), phi=f(phi), phiB=f(phiB), gamma=None if uniform else f(gamma), gammaB=f(gammaB),
+                bcType=i(bcType), bcValue=f(bcValue), su=f(su))
+    keep.append(arrs)
+    t = LduFvmTerms(float(rDeltaT), _p(arrs["psi0"]), _p(arrs["phi"]), _p(arrs["phiB"]), DIV_SCHEMES[div],
+                    int(lapSign), float(gamma) if uniform else 0.0, _p(arrs["gamma"]), _p(arrs["gammaB"]),
+                    _p(arrs["bcType"], i32p), _p(arrs["bcValue"]), _p(arrs["su"]))
+    diag, upper, source = np.empty(nC), np.empty(max(nF, 1)), np.empty(nC)
+    lower = np.empty(max(nF, 1)) if phi is not None else None
+    if lib().ldu_fvm_assemble(ctypes.byref(gc), ctypes.byref(t), _p(diag), _p(upper), _p(lower), _p(source)) != 0:
+        raise ValueError("no term")
+    del keep
+    return diag, upper[:nF], None if lower is None else lower[:nF], source

@@ -4,6 +4,7 @@ library's tuning knobs so every form is checked on small systems:
 * small   -- one CTA, vector in global memory
 * cta     -- one CTA, vector in shared memory (the default for small levels)
 * cluster -- a 16-CTA cluster, vector in distributed shared memory
+* cluster_global -- a 16-CTA cluster, vector in global memory (L2)
 * grid    -- the persistent grid, wavefront: each 32-slot group waits for the
              groups it reads (vector in global memory)
 * levels  -- the persistent grid with whole-level counters (the default grid form)
@@ -16,6 +17,7 @@ FORMS = {
     "small": {ldu.TUNE_SMALL_SWEEP: 1 << 30, ldu.TUNE_SMEM_BYTES: 0},
     "cta": {},
     "cluster": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 8192},
+    "cluster_global": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_CLUSTER_GLOBAL: 1 << 30},
     "grid": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 1},
     "levels": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 0},
 }

@@ -123,6 +123,64 @@ def fv_geometry(mesh):
                 deltaCoeffsB=1.0 / mag(delta))
 
 
+def cyclic_x(s, mesh, gamma=1.0, U=None):
+    """Couples a box system's xmin and xmax patches as a cyclic pair (face k
+    of one with face k of the other): two coupled interfaces, the cells and
+    neighbour cells of their faces, interfaceBouCoeffs (result -= bou*psi_nbr,
+    so the coupling coefficient is -bou) and interfaceIntCoeffs (the
+    transpose's, for Tmul).  The coupling is diffusion gamma*magSf/d across
+    the periodic face and, with U, the upwind flux U.Sf; the diagonals take
+    the matching internal coefficients.  The system must have been built
+    with xmin and xmax as non-Dirichlet patches (their boundary terms are
+    replaced)."""
+    ps = mesh["patchStart"]
+    own = mesh["owner"]
+    nF = mesh["nFaces"]
+    Sf = mesh["Sf"].reshape(nF, 3)
+    Cf = mesh["Cf"].reshape(nF, 3)
+    C = mesh["C"].reshape(-1, 3)
+    fa, fb = np.arange(ps[0], ps[1]), np.arange(ps[1], ps[2])
+    a, b = own[fa], own[fb]
+    dist = lambda v: np.sqrt(v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2])  # noqa: E731
+    d = dist(Cf[fa] - C[a]) + dist(Cf[fb] - C[b])
+    g = gamma * 0.5 * (mesh["magSf"][fa] + mesh["magSf"][fb]) / d
+    diag = s["diag"].copy()
+    if U is None:
+        bouA, bouB = g, g.copy()
+        diag[a] += g
+        diag[b] += g
+    else:
+        Uv = np.asarray(U, np.float64)
+        F = Sf[fb] @ Uv  # flux out through xmax = into the cell on xmin
+        # the generator's zeroGradient outflow terms on both patches are replaced
+        diag[a] -= Sf[fa] @ Uv
+        diag[b] -= F
+        Fp, Fm = np.maximum(F, 0.0), np.maximum(-F, 0.0)
+        diag[a] += g + Fm
+        diag[b] += g + Fp
+        bouA, bouB = g + Fp, g + Fm
+    n = len(fa)
+    out = dict(s)
+    out.update(diag=diag, ifSize=np.array([n, n], np.int32), ifCell=np.concatenate([a, b]).astype(np.int32),
+               ifNbr=np.concatenate([b, a]).astype(np.int32), ifBou=np.concatenate([bouA, bouB]),
+               ifInt=np.concatenate([bouB, bouA]))
+    return out
+
+
+def cyclic_cube(n, jitter=0.2, seed=1, U=None, gamma=1.0):
+    """An n^3 box, periodic in x (a cyclic pair), Dirichlet on ymin: the
+    Laplacian, or with U the upwind convection-diffusion operator."""
+    m = box_mesh(n, n, n, jitter=jitter, seed=seed)
+    if U is None:
+        s = laplacian(m, gamma=gamma, dirichlet=("ymin",))
+    else:
+        s = convection_diffusion(m, U, gamma, dirichlet=("ymin",))
+    s = cyclic_x(s, m, gamma=gamma, U=U)
+    s["source"] = uniform(seed + 7, s["diag"].size)
+    s["name"] = f"cyclic-{n}"
+    return s
+
+
 def _mask(dirichlet):
     m = 0
     for p in dirichlet:

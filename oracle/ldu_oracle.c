@@ -64,9 +64,22 @@ void ldu_free_addr(ldu_matrix* m) {
 
 static const double* lowerOf(const ldu_matrix* m) { return m->lower ? m->lower : m->upper; }
 
+/* lduMatrix::updateMatrixInterfaces (lduMatrixUpdateMatrixInterfaces.C:96-
+ * 266) with cyclic interfaces (cyclicFvPatchField.C:150-174, a scalar field:
+ * no transform): result[faceCells] -= coeffs*psi[nbrFaceCells], patch by
+ * patch.  neg: the callers that pass the negated coefficients (residual,
+ * the Gauss-Seidel smoothers' mBouCoeffs). */
+static void update_interfaces(const ldu_matrix* m, const double* coeffs, int neg, const double* psi,
+                              double* result) {
+    for (int k = 0; k < m->nIf; ++k) {
+        const double c = neg ? -coeffs[k] : coeffs[k];
+        result[m->ifCell[k]] -= c * psi[m->ifNbr[k]];
+    }
+}
+
 /* ------------------------------------------------------------- matrix ops */
 
-/* lduMatrix::Amul, lduMatrixATmul.C:34-92 (no interfaces) */
+/* lduMatrix::Amul, lduMatrixATmul.C:34-92 */
 void ldu_amul(const ldu_matrix* m, const double* x, double* y) {
     const double* lo = lowerOf(m);
     for (int c = 0; c < m->nCells; ++c) y[c] = m->diag[c] * x[c];
@@ -74,6 +87,7 @@ void ldu_amul(const ldu_matrix* m, const double* x, double* y) {
         y[m->u[f]] += lo[f] * x[m->l[f]];
         y[m->l[f]] += m->upper[f] * x[m->u[f]];
     }
+    update_interfaces(m, m->ifBou, 0, x, y);
 }
 
 /* lduMatrix::Tmul, lduMatrixATmul.C:95-151 */
@@ -84,6 +98,7 @@ void ldu_tmul(const ldu_matrix* m, const double* x, double* y) {
         y[m->u[f]] += m->upper[f] * x[m->l[f]];
         y[m->l[f]] += lo[f] * x[m->u[f]];
     }
+    update_interfaces(m, m->ifInt, 0, x, y);
 }
 
 /* lduMatrix::sumA, lduMatrixATmul.C:154-200 */
@@ -94,6 +109,7 @@ void ldu_sumA(const ldu_matrix* m, double* s) {
         s[m->u[f]] += lo[f];
         s[m->l[f]] += m->upper[f];
     }
+    for (int k = 0; k < m->nIf; ++k) s[m->ifCell[k]] -= m->ifBou[k];
 }
 
 /* lduMatrix::residual, lduMatrixATmul.C:203-280 */
@@ -104,6 +120,7 @@ void ldu_residual(const ldu_matrix* m, const double* x, const double* b, double*
         r[m->u[f]] -= lo[f] * x[m->l[f]];
         r[m->l[f]] -= m->upper[f] * x[m->u[f]];
     }
+    update_interfaces(m, m->ifBou, 1, x, r);
 }
 
 /* ------------------------------------------------------------- reductions */
@@ -243,6 +260,7 @@ void ldu_gs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSweep
     double* bPrime = (double*)xmalloc(sizeof(double) * n);
     for (int sweep = 0; sweep < nSweeps; ++sweep) {
         memcpy(bPrime, b, sizeof(double) * n);
+        update_interfaces(m, m->ifBou, 1, psi, bPrime);  /* the Jacobi interface term */
         int fEnd = m->ownerStart[0];
         for (int c = 0; c < n; ++c) {
             const int fStart = fEnd;
@@ -287,6 +305,7 @@ void ldu_symgs_smooth(const ldu_matrix* m, double* psi, const double* b, int nSw
     double* bPrime = (double*)xmalloc(sizeof(double) * n);
     for (int sweep = 0; sweep < nSweeps; ++sweep) {
         memcpy(bPrime, b, sizeof(double) * n);
+        update_interfaces(m, m->ifBou, 1, psi, bPrime);  /* the Jacobi interface term */
         int fEnd = m->ownerStart[0];
         for (int c = 0; c < n; ++c) {
             const int fStart = fEnd;

@@ -26,6 +26,12 @@ typedef struct {
     int *ownerStart;             /* [nCells+1] */
     int *losort;                 /* [nFaces] */
     int *losortStart;            /* [nCells+1] */
+    /* coupled (cyclic) interfaces, faces concatenated in patch order: the
+     * cell on this side, the neighbour patch's cell, interfaceBouCoeffs and
+     * interfaceIntCoeffs (nIf = 0: none) */
+    int nIf;
+    const int *ifCell, *ifNbr;
+    const double *ifBou, *ifInt;
 } ldu_matrix;
 
 typedef struct {

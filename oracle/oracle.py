@@ -29,7 +29,8 @@ f64p = ctypes.POINTER(ctypes.c_double)
 class LduMatrix(ctypes.Structure):
     _fields_ = [("nCells", ctypes.c_int), ("nFaces", ctypes.c_int),
                 ("l", i32p), ("u", i32p), ("diag", f64p), ("upper", f64p), ("lower", f64p),
-                ("ownerStart", i32p), ("losort", i32p), ("losortStart", i32p)]
+                ("ownerStart", i32p), ("losort", i32p), ("losortStart", i32p),
+                ("nIf", ctypes.c_int), ("ifCell", i32p), ("ifNbr", i32p), ("ifBou", f64p), ("ifInt", f64p)]
 
 
 class LduPerf(ctypes.Structure):
@@ -110,6 +111,14 @@ class Matrix:
         self.lower = None if lo is None else np.ascontiguousarray(lo, np.float64)
         self.c = LduMatrix(self.diag.size, self.l.size, _p(self.l, i32p), _p(self.u, i32p),
                            _p(self.diag), _p(self.upper), _p(self.lower), None, None, None)
+        if s.get("ifCell") is not None:
+            # coupled (cyclic) interfaces, faces concatenated in patch order
+            self.ifc = [np.ascontiguousarray(s["ifCell"], np.int32), np.ascontiguousarray(s["ifNbr"], np.int32),
+                        np.ascontiguousarray(s["ifBou"], np.float64),
+                        np.ascontiguousarray(s.get("ifInt", s["ifBou"]), np.float64)]
+            self.c.nIf = self.ifc[0].size
+            self.c.ifCell, self.c.ifNbr = _p(self.ifc[0], i32p), _p(self.ifc[1], i32p)
+            self.c.ifBou, self.c.ifInt = _p(self.ifc[2]), _p(self.ifc[3])
         lib().ldu_init_addr(ctypes.byref(self.c))
         self.n = self.diag.size
 

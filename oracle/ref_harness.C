@@ -48,6 +48,8 @@
 #include "FieldField.H"
 #include "lduMatrix.H"
 #include "lduPrimitiveMesh.H"
+#include "lduInterfaceField.H"
+#include "lduSchedule.H"
 #include "DICPreconditioner.H"
 #include "DILUPreconditioner.H"
 #include "pairGAMGAgglomeration.H"
@@ -191,6 +193,137 @@ public:
 };
 
 
+// Coupled (cyclic) interfaces for the solver path: an lduInterface holding
+// a patch's face cells, and an lduInterfaceField whose update is
+// cyclicFvPatchField::updateInterfaceMatrix (cyclicFvPatchField.C:150-174)
+// for a scalar field (no transform): result[faceCells] -= coeffs*psi[nbr].
+// Like the cyclic field it never marks itself updated, so the reference's
+// nonBlocking consume loop applies it once per update, in patch order.
+class harnessInterface
+:
+    public lduInterface
+{
+    labelList faceCells_;
+
+public:
+
+    explicit harnessInterface(const labelList& fc)
+    :
+        faceCells_(fc)
+    {}
+
+    virtual const labelUList& faceCells() const { return faceCells_; }
+
+    virtual tmp<labelField> interfaceInternalField
+    (
+        const labelUList& internalData
+    ) const
+    {
+        return tmp<labelField>(new labelField(internalData, faceCells_));
+    }
+
+    virtual tmp<labelField> internalFieldTransfer
+    (
+        const Pstream::commsTypes,
+        const labelUList& iF
+    ) const
+    {
+        return tmp<labelField>(new labelField(iF, faceCells_));
+    }
+};
+
+
+class harnessCyclicField
+:
+    public lduInterfaceField
+{
+    labelList nbrCells_;
+
+public:
+
+    harnessCyclicField(const lduInterface& i, const labelList& nbr)
+    :
+        lduInterfaceField(i),
+        nbrCells_(nbr)
+    {}
+
+    virtual void updateInterfaceMatrix
+    (
+        scalarField& result,
+        const scalarField& psiInternal,
+        const scalarField& coeffs,
+        const direction,
+        const Pstream::commsTypes
+    ) const
+    {
+        const scalarField pnf(psiInternal, nbrCells_);
+        const labelUList& faceCells = interface().faceCells();
+        forAll(faceCells, elemI)
+        {
+            result[faceCells[elemI]] -= coeffs[elemI]*pnf[elemI];
+        }
+    }
+};
+
+
+// The interfaces given by the records ifSize (faces per patch), ifCell,
+// ifNbr, ifBou and ifInt (faces concatenated in patch order), added to the
+// mesh; empty lists without them.
+struct harnessInterfaces
+{
+    // owned by the mesh once added (lduPrimitiveMesh::primitiveInterfaces_)
+    UPtrList<harnessInterface> patches;
+    PtrList<harnessCyclicField> fields;
+    lduInterfacePtrsList ilist;
+    lduInterfaceFieldPtrsList ifs;
+    Field<Field<scalar>> bou, intc;
+
+    harnessInterfaces(const RecMap& in, harnessMesh& mesh)
+    :
+        patches(0),
+        fields(0),
+        ilist(0),
+        ifs(0),
+        bou(0),
+        intc(0)
+    {
+        if (!has(in, "ifSize")) return;
+        const labelList sz(getL(in, "ifSize"));
+        const labelList fc(getL(in, "ifCell")), nb(getL(in, "ifNbr"));
+        const scalarField b(getF(in, "ifBou"));
+        const scalarField ic(has(in, "ifInt") ? getF(in, "ifInt") : getF(in, "ifBou"));
+        const label np = sz.size();
+        patches.setSize(np);
+        fields.setSize(np);
+        ilist.setSize(np);
+        ifs.setSize(np);
+        bou.setSize(np);
+        intc.setSize(np);
+        label o = 0;
+        for (label p = 0; p < np; p++)
+        {
+            labelList f(sz[p]), n(sz[p]);
+            scalarField pb(sz[p]), pi(sz[p]);
+            for (label k = 0; k < sz[p]; k++)
+            {
+                f[k] = fc[o + k];
+                n[k] = nb[o + k];
+                pb[k] = b[o + k];
+                pi[k] = ic[o + k];
+            }
+            patches.set(p, new harnessInterface(f));
+            fields.set(p, new harnessCyclicField(patches[p], n));
+            ilist.set(p, &patches[p]);
+            ifs.set(p, &fields[p]);
+            bou[p] = pb;
+            intc[p] = pi;
+            o += sz[p];
+        }
+        mesh.addInterfaces(ilist, lduSchedule());
+    }
+};
+
+
 // pairGAMGAgglomeration driven by explicit face weights: the faceAreaPair
 // weights (faceAreaPairGAMGAgglomeration.C:55-80) computed from the given
 // face-area vectors, then the reference pairing (pairGAMGAgglomerate.C).
@@ -275,16 +408,18 @@ int runOps(const RecMap& in, Writer& out, Time& runTime)
     const scalarField x(getF(in, "x")), b(getF(in, "b"));
     const label nCells = x.size(), nFaces = l.size();
     harnessMesh mesh(runTime, nCells, l, u);
+    harnessInterfaces hi(in, mesh);
     lduMatrix A(mesh);
     buildMatrix(A, in, nCells, nFaces);
 
-    Field<Field<scalar>> bou(0), intc(0);
-    lduInterfaceFieldPtrsList ifs(0);
+    Field<Field<scalar>>& bou = hi.bou;
+    Field<Field<scalar>>& intc = hi.intc;
+    lduInterfaceFieldPtrsList& ifs = hi.ifs;
 
     scalarField y(nCells);
     A.Amul(y, x, bou, ifs, 0);
     out.f8("Amul", y);
-    A.Tmul(y, x, bou, ifs, 0);
+    A.Tmul(y, x, intc, ifs, 0);
     out.f8("Tmul", y);
     A.residual(y, x, b, bou, ifs, 0);
     out.f8("residual", y);
@@ -403,14 +538,16 @@ int runSolve(const RecMap& in, Writer& out, Time& runTime)
     scalarField psi(getF(in, "psi"));
     const label nCells = source.size(), nFaces = l.size();
     harnessMesh mesh(runTime, nCells, l, u);
+    harnessInterfaces hi(in, mesh);
     lduMatrix A(mesh);
     buildMatrix(A, in, nCells, nFaces);
 
     IStringStream is(getS(in, "dict"));
     dictionary dict(is);
 
-    Field<Field<scalar>> bou(0), intc(0);
-    lduInterfaceFieldPtrsList ifs(0);
+    Field<Field<scalar>>& bou = hi.bou;
+    Field<Field<scalar>>& intc = hi.intc;
+    lduInterfaceFieldPtrsList& ifs = hi.ifs;
 
     const word solverName(dict.lookup("solver"));
     // GAMG, or a solver preconditioned by GAMG (a preconditioner

@@ -38,6 +38,9 @@ def _ldu(s):
     d = dict(l=s["l"], u=s["u"], diag=s["diag"], upper=s["upper"])
     if s.get("lower") is not None:
         d["lower"] = s["lower"]
+    if s.get("ifCell") is not None:  # coupled (cyclic) interfaces
+        for k in ("ifSize", "ifCell", "ifNbr", "ifBou", "ifInt"):
+            d[k] = s[k]
     return d
 
 

@@ -47,6 +47,9 @@ SYSTEMS = {
     "cd6": ("bicgstab_cube", dict(n=6, seed=4)),
     "cd10": ("bicgstab_cube", dict(n=10, seed=4)),
     "box": ("box", dict(nx=9, ny=5, nz=13, dirichlet="zmax", seed=11)),
+    # periodic in x: a cyclic interface pair (symmetric / upwind asymmetric)
+    "cyc7": ("cyclic_cube", dict(n=7, jitter=0.2, seed=6)),
+    "cycd7": ("cyclic_cube", dict(n=7, jitter=0.1, seed=8, U=[1.0, 0.4, 0.2], gamma=0.05)),
 }
 
 SOLVES = {
@@ -116,6 +119,18 @@ SOLVES = {
     "pbicg_diagonal": ("cd6", dict(solver="PBiCG", preconditioner="diagonal", tolerance=1e-8, relTol=0.0,
                                    maxIter=2000)),
     "pbicg_none_reltol": ("cd6", dict(solver="PBiCG", preconditioner="none", tolerance=0.0, relTol=1e-4)),
+    "pcg_cyc": ("cyc7", dict(solver="PCG", preconditioner="DIC", tolerance=1e-10, relTol=0.0)),
+    "pcg_cyc_diagonal": ("cyc7", dict(solver="PCG", preconditioner="diagonal", tolerance=1e-9, relTol=0.0)),
+    "bicgstab_cyc": ("cycd7", dict(solver="PBiCGStab", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
+    "pbicg_cyc": ("cycd7", dict(solver="PBiCG", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
+    "smooth_cyc_gs": ("cyc7", dict(solver="smoothSolver", smoother="GaussSeidel", nSweeps=2, tolerance=1e-7,
+                                   relTol=0.0, maxIter=5000)),
+    "smooth_cyc_symgs": ("cycd7", dict(solver="smoothSolver", smoother="symGaussSeidel", tolerance=1e-9,
+                                       relTol=0.0)),
+    "smooth_cyc_dic": ("cyc7", dict(solver="smoothSolver", smoother="DIC", tolerance=1e-7, relTol=0.0,
+                                    maxIter=5000)),
+    "smooth_cyc_dilugs": ("cycd7", dict(solver="smoothSolver", smoother="DILUGaussSeidel", tolerance=1e-9,
+                                        relTol=0.0)),
     "pcg_gamg_direct": ("jcube14", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
                                         preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel",
                                                             directSolveCoarsest=True,
@@ -150,7 +165,7 @@ def main():
                         **{k: g[k] for k in ("Sf", "Cf", "magSf", "C", "V")})
 
     sums = {}
-    for name in ("cube6", "jcube7", "cd6", "box"):
+    for name in ("cube6", "jcube7", "cd6", "box", "cyc7", "cycd7"):
         s = build(*SYSTEMS[name])
         sums[name] = checksum(s)
         x = cases.uniform(99, s["diag"].size)

@@ -25,7 +25,7 @@ def test_geometry_matches_polymesh():
         np.testing.assert_array_equal(m[k], g[k], err_msg=k)
 
 
-@pytest.mark.parametrize("name", ["cube6", "jcube7", "cd6", "box"])
+@pytest.mark.parametrize("name", ["cube6", "jcube7", "cd6", "box", "cyc7", "cycd7"])
 def test_single_operations(name):
     s = system(name)
     g = load(f"ops_{name}.npz")

@@ -178,6 +178,23 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
 /* Re-upload coefficients (a new fvMatrix on the same mesh, every solve). */
 cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* upper,
                              const double* lower);
+/* Coupled (cyclic) interfaces of the mesh (lduInterfaceFieldPtrsList with
+ * cyclic fields): nPatches patches, faces concatenated in patch order, for
+ * each face the cell on this side (faceCells) and the neighbour patch's cell
+ * (nbrFaceCells).  Amul, Tmul, residual, sumA/normFactor and the
+ * Gauss-Seidel smoothers then add the interface terms as
+ * lduMatrix::updateMatrixInterfaces does with cyclicFvPatchField
+ * (cyclicFvPatchField.C:150-174: result[faceCells] -= coeffs*psi[nbr]);
+ * the DIC/DILU factorisations ignore them, as the reference's do.  PCG,
+ * PBiCGStab, PBiCG and smoothSolver solve such systems (FP64); GAMG is
+ * refused.  nPatches = 0 removes them.  Set the interfaces before the
+ * matrices' interface coefficients. */
+cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32_t* patchSize,
+                                   const int32_t* faceCells, const int32_t* nbrFaceCells);
+/* interfaceBouCoeffs and interfaceIntCoeffs (host, faces concatenated in patch
+ * order; intCoeffs NULL: the same as bouCoeffs). */
+cfx_status cfx_matrix_set_interface_coeffs(cfx_matrix* mat, const double* bouCoeffs, const double* intCoeffs);
+
 /* A matrix of zero coefficients (symmetric: no lower triangle), to be filled
  * on the device by cfx_fvm_assemble or cfx_matrix_update_device. */
 cfx_status cfx_matrix_create_empty(cfx_mesh* mesh, int symmetric, cfx_matrix** mat);

@@ -53,6 +53,11 @@ struct cfx_mesh {
     FvGeom fv;  // finite-volume face geometry (cfx_fv_geometry)
     bool hasFv = false;
     Arena fvArena;
+    // coupled interfaces (cfx_mesh_set_interfaces): the CSR position of each
+    // interface face given in patch order
+    int nIf = 0;
+    std::vector<int> ifPos;
+    Arena ifArena;
 };
 
 template <class T>
@@ -110,6 +115,7 @@ struct cfx_matrix {
     BlockSys<float>* d_blk32 = nullptr;
     int* luPiv = nullptr;  // directSolveCoarsest pivots
     int luPivN = 0;
+    int ifN = 0;  // interface coefficients held (cfx_matrix_set_interface_coeffs)
     GraphCache gPCG, gBiCG, gGAMG, gMixed;
 };
 
@@ -666,7 +672,8 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
     }
     const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
-                               reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD)});
+                               reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
+                               reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
     auto body = [&]() {
         if (solver == CFX_SOLVER_PCG) {
             const int np = precondition<T>(mat, lv, precond, r, w, done, true);
@@ -739,12 +746,35 @@ void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b,
         // symGaussSeidelSmoother.C:130-199: a forward pass, then a backward
         // pass over the reverse order starting from the forward bPrime, which
         // is the same per-cell formula on the upper-neighbour DAG
+        // With coupled interfaces both passes start from bPrime = source
+        // minus the (negated) interface terms of psi at the sweep's start.
         const DevSched& f = sched(mat->mesh, lv, SCHED_GS, 1);
         const DevSched& g = sched(mat->mesh, lv, SCHED_GSB, 1);
+        const Iface<T> itf = if_bou(m, c);
         for (int k = 0; k < nSweeps; ++k) {
-            if (run_sweep<T>(s, f, OP_GS, packed<T>(mat, lv, OP_GS, 1, f), b, psi, nullptr, nullptr, nullptr,
+            const T* bk = b;
+            if (itf.start) {
+                T* bp = LW.get(2, m.n);
+                Ops<T>::iface_bprime(s, m.n, itf, b, psi, bp);
+                bk = bp;
+            }
+            if (run_sweep<T>(s, f, OP_GS, packed<T>(mat, lv, OP_GS, 1, f), bk, psi, nullptr, nullptr, nullptr,
                              ctx->d_status) != CFX_OK ||
-                run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, -1, g), b, psi, nullptr, nullptr, nullptr,
+                run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, -1, g), bk, psi, nullptr, nullptr, nullptr,
+                             ctx->d_status) != CFX_OK)
+                throw CudaError(last_error());
+        }
+        return;
+    }
+    if (kind == CFX_SMOOTH_GS && if_bou(m, c).start) {
+        // GaussSeidelSmoother.C:118-177 with coupled interfaces: each sweep
+        // starts from bPrime = source - (-bou)*psi[nbr] (psi at the sweep's
+        // start), so the sweeps are not fused
+        const DevSched& g = sched(mat->mesh, lv, SCHED_GS, 1);
+        T* bp = LW.get(2, m.n);
+        for (int k = 0; k < nSweeps; ++k) {
+            Ops<T>::iface_bprime(s, m.n, if_bou(m, c), b, psi, bp);
+            if (run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, 1, g), bp, psi, nullptr, nullptr, nullptr,
                              ctx->d_status) != CFX_OK)
                 throw CudaError(last_error());
         }
@@ -781,11 +811,17 @@ void prepare_smooth(cfx_matrix* mat, int lv, int kind, int nSweeps, Work<T>& LW)
         prepare_smooth<T>(mat, lv, CFX_SMOOTH_GS, nSweeps, LW);
         return;
     }
+    const bool itf = if_bou(mat->mesh->dev[lv], coeffs<T>(mat, lv)).start != nullptr;
+    if (itf && (kind == CFX_SMOOTH_SYMGS || kind == CFX_SMOOTH_GS)) LW.get(2, mat->mesh->dev[lv].n);
     if (kind == CFX_SMOOTH_SYMGS) {
         prepare_gs<T>(mat, lv, 1);
         const DevSched& g = sched(mat->mesh, lv, SCHED_GSB, 1);
         Packed<T>& p = packed<T>(mat, lv, OP_GS, -1, g);
         if (!p.valid) pack_sweep<T>(mat->mesh->ctx->stream, g, OP_GS, coeffs<T>(mat, lv), p);
+        return;
+    }
+    if (kind == CFX_SMOOTH_GS && itf) {
+        prepare_gs<T>(mat, lv, 1);
         return;
     }
     if (kind == CFX_SMOOTH_GS) {
@@ -1354,6 +1390,22 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         set_error("Unknown asymmetric matrix solver cudaPCG");
         return CFX_ERR_CONFIG;
     }
+    if (mat->mesh->nIf) {
+        // coupled interfaces: the lduMatrix operations, the Krylov solvers and
+        // smoothSolver; GAMG's interface agglomeration is not built
+        if (c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) {
+            set_error("coupled interfaces are not supported by cudaGAMG or the GAMG preconditioner");
+            return CFX_ERR_CONFIG;
+        }
+        if (c->precision == CFX_MIXED) {
+            set_error("precision mixed is not available with coupled interfaces");
+            return CFX_ERR_CONFIG;
+        }
+        if (mat->ifN != mat->mesh->nIf) {
+            set_error("the interface coefficients are not set (cfx_matrix_set_interface_coeffs)");
+            return CFX_ERR_STATE;
+        }
+    }
     if (c->solver == CFX_SOLVER_PBICG && mat->sym) {
         set_error("Unknown symmetric matrix solver cudaPBiCG");  // PBiCG.C:34-35: asymmetric only
         return CFX_ERR_CONFIG;
@@ -1628,6 +1680,82 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
         set_coefficients(mat.get(), diag, upper, lower, cudaMemcpyHostToDevice);
         CK(cudaStreamSynchronize(mesh->ctx->stream));
         *out = mat.release();
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32_t* patchSize,
+                                   const int32_t* faceCells, const int32_t* nbrCells) {
+    if (!mesh || nPatches < 0 || (nPatches && (!patchSize || !faceCells || !nbrCells))) return CFX_ERR_ARG;
+    const int n = mesh->host[0].n;
+    int64_t nIf = 0;
+    for (int p = 0; p < nPatches; ++p) {
+        if (patchSize[p] < 0) return CFX_ERR_ARG;
+        nIf += patchSize[p];
+    }
+    if (nIf > (int64_t(1) << 30)) return CFX_ERR_ARG;
+    for (int64_t k = 0; k < nIf; ++k)
+        if (faceCells[k] < 0 || faceCells[k] >= n || nbrCells[k] < 0 || nbrCells[k] >= n) {
+            set_error("cfx_mesh_set_interfaces: a face cell is out of range");
+            return CFX_ERR_ADDRESSING;
+        }
+    return guard([&]() -> cfx_status {
+        cudaStream_t s = mesh->ctx->stream;
+        CK(cudaStreamSynchronize(s));
+        mesh->ifArena.release();
+        LevelMesh& m = mesh->dev[0];
+        m.nIf = int(nIf);
+        m.ifStart = m.ifNbr = m.ifCells = nullptr;
+        mesh->ifPos.assign(size_t(nIf), 0);
+        mesh->nIf = int(nIf);
+        if (nIf) {
+            // CSR over cells, each cell's faces in patch-then-face order (a
+            // stable counting sort): the order updateMatrixInterfaces adds them
+            std::vector<int> start(n + 1, 0);
+            std::vector<int> nbr(static_cast<size_t>(nIf), 0);
+            for (int64_t k = 0; k < nIf; ++k) start[faceCells[k] + 1]++;
+            for (int c = 0; c < n; ++c) start[c + 1] += start[c];
+            std::vector<int> fill(start.begin(), start.end() - 1);
+            for (int64_t k = 0; k < nIf; ++k) {
+                const int j = fill[faceCells[k]]++;
+                nbr[j] = nbrCells[k];
+                mesh->ifPos[size_t(k)] = j;
+            }
+            m.ifStart = mesh->ifArena.upload(start, s);
+            m.ifNbr = mesh->ifArena.upload(nbr, s);
+        }
+        mesh->version++;  // captured graphs hold the interface pointers
+        CK(cudaStreamSynchronize(s));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_matrix_set_interface_coeffs(cfx_matrix* mat, const double* bouCoeffs, const double* intCoeffs) {
+    if (!mat) return CFX_ERR_ARG;
+    cfx_mesh* mesh = mat->mesh;
+    const int nIf = mesh->nIf;
+    if (nIf && !bouCoeffs) return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        cudaStream_t s = mesh->ctx->stream;
+        LevelCoeffs<double>& c = mat->c64[0];
+        if (!nIf) {
+            c.ifBou = c.ifInt = nullptr;
+            mat->ifN = 0;
+            return CFX_OK;
+        }
+        if (mat->ifN != nIf || !c.ifBou) {
+            c.ifBou = mat->arena.get<double>(nIf);
+            c.ifInt = mat->arena.get<double>(nIf);
+        }
+        std::vector<double> b(nIf), ic(nIf);
+        for (int k = 0; k < nIf; ++k) {
+            b[mesh->ifPos[k]] = bouCoeffs[k];
+            ic[mesh->ifPos[k]] = intCoeffs ? intCoeffs[k] : bouCoeffs[k];
+        }
+        CK(cudaMemcpyAsync(c.ifBou, b.data(), sizeof(double) * nIf, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c.ifInt, ic.data(), sizeof(double) * nIf, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));  // b and ic are host temporaries
+        mat->ifN = nIf;
         return CFX_OK;
     });
 }

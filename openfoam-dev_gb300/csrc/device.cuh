@@ -6,6 +6,8 @@
 
 #include <cfloat>
 
+#include "internal.h"
+
 namespace cfx {
 
 constexpr double VSMALL = DBL_MIN;  // doubleScalarVSmall
@@ -29,6 +31,28 @@ __device__ __forceinline__ T row_amul(int c, const int* __restrict__ os, const i
     return acc;
 }
 
+
+// lduMatrix::updateMatrixInterfaces with cyclic fields
+// (cyclicFvPatchField.C:150-174): acc -= coeffs*psi[nbr], face by face.
+template <class T>
+__device__ __forceinline__ T iface_sub(const Iface<T>& f, int c, const T* __restrict__ x, T acc) {
+    if (f.start) {
+        const int j1 = f.start[c + 1];
+        for (int j = f.start[c]; j < j1; ++j) acc -= f.coef[j] * x[f.nbr[j]];
+    }
+    return acc;
+}
+
+// The same with the negated coefficients (lduMatrix::residual's and the
+// Gauss-Seidel smoothers' mBouCoeffs).
+template <class T>
+__device__ __forceinline__ T iface_sub_neg(const Iface<T>& f, int c, const T* __restrict__ x, T acc) {
+    if (f.start) {
+        const int j1 = f.start[c + 1];
+        for (int j = f.start[c]; j < j1; ++j) acc -= (-f.coef[j]) * x[f.nbr[j]];
+    }
+    return acc;
+}
 
 // Fixed-order warp tree (xor-free shuffle down): the same inputs always give
 // the same sum, whatever the launch.

@@ -89,6 +89,13 @@ struct LevelMesh {
     int* coarseFaceFine = nullptr;    // fine faces of each coarse face, ascending
     int* intFaceStart = nullptr;      // [nCoarse+1]
     int* intFaceFine = nullptr;       // fine faces inside each coarse cell, ascending
+    // coupled (cyclic) interfaces: CSR over cells of the interface faces in
+    // patch-then-face order (neighbour cell per entry), and the cells that
+    // have any (ascending)
+    int nIf = 0, nIfCells = 0;
+    int* ifStart = nullptr;  // [n+1]
+    int* ifNbr = nullptr;    // [nIf]
+    int* ifCells = nullptr;  // [nIfCells]
 };
 
 template <class T>
@@ -97,6 +104,9 @@ struct LevelCoeffs {
     T *diag = nullptr, *upper = nullptr, *lower = nullptr;
     T *lowerPerm = nullptr, *upperPerm = nullptr;
     T* rD = nullptr;
+    // interfaceBouCoeffs / interfaceIntCoeffs in the mesh's interface CSR
+    // order (null: none set)
+    T *ifBou = nullptr, *ifInt = nullptr;
 };
 
 // Device-resident scalars of one solve.  Kernels read and update them so the
@@ -119,6 +129,40 @@ struct Scratch {
     double* chunkPartials = nullptr;  // per-chunk partial sums of fused sweeps
     size_t chunkPartialsCap = 0;
 };
+
+// Coupled (cyclic) interface faces of one cell, in patch-then-face order:
+// the neighbour cells and coefficients, CSR over the cells (start == null:
+// no interfaces).
+template <class T>
+struct Iface {
+    const int* start = nullptr;
+    const int* nbr = nullptr;
+    const T* coef = nullptr;
+};
+
+// interfaceBouCoeffs (Amul, residual, sumA, smoothers) and
+// interfaceIntCoeffs (Tmul) of a level, when both the mesh's interfaces and
+// the matrix's coefficients are set
+template <class T>
+inline Iface<T> if_bou(const LevelMesh& m, const LevelCoeffs<T>& a) {
+    Iface<T> f;
+    if (m.ifStart && a.ifBou) {
+        f.start = m.ifStart;
+        f.nbr = m.ifNbr;
+        f.coef = a.ifBou;
+    }
+    return f;
+}
+template <class T>
+inline Iface<T> if_int(const LevelMesh& m, const LevelCoeffs<T>& a) {
+    Iface<T> f;
+    if (m.ifStart && a.ifInt) {
+        f.start = m.ifStart;
+        f.nbr = m.ifNbr;
+        f.coef = a.ifInt;
+    }
+    return f;
+}
 
 // ---- launchers (kernels.cu) ----------------------------------------------
 template <class T>
@@ -153,6 +197,9 @@ struct Ops {
     static void lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T* b, T* x);
     // x = b / diag (diagonalSolver)
     static void diag_solve(cudaStream_t s, int n, const T* diag, const T* b, T* x);
+    // bp = b - (-bou)*psi[nbr] over the coupled interfaces (the Gauss-Seidel
+    // smoothers' bPrime before a sweep)
+    static void iface_bprime(cudaStream_t s, int n, const Iface<T>& itf, const T* b, const T* psi, T* bp);
 };
 
 // ---- finite-volume assembly (fvm.cu) -------------------------------------

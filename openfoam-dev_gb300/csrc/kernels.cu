@@ -42,14 +42,14 @@ __global__ void __launch_bounds__(RED_NT) amul_k(int n, const int* __restrict__ 
                                                  const int* __restrict__ losortL, const int* __restrict__ u,
                                                  const T* __restrict__ diag, const T* __restrict__ lp,
                                                  const T* __restrict__ upper, const T* __restrict__ x,
-                                                 T* __restrict__ y) {
+                                                 T* __restrict__ y, Iface<T> itf) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         T acc = diag[c] * x[c];
         const int k1 = losortStart[c + 1];
         for (int k = losortStart[c]; k < k1; ++k) acc += lp[k] * x[losortL[k]];
         const int f1 = ownerStart[c + 1];
         for (int f = ownerStart[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
-        y[c] = acc;
+        y[c] = iface_sub(itf, c, x, acc);
     }
 }
 
@@ -59,14 +59,14 @@ __global__ void __launch_bounds__(RED_NT) residual_k(int n, const int* __restric
                                                      const int* __restrict__ losortL, const int* __restrict__ u,
                                                      const T* __restrict__ diag, const T* __restrict__ lp,
                                                      const T* __restrict__ upper, const T* __restrict__ x,
-                                                     const T* __restrict__ b, T* __restrict__ r) {
+                                                     const T* __restrict__ b, T* __restrict__ r, Iface<T> itf) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         T acc = b[c] - diag[c] * x[c];
         const int k1 = losortStart[c + 1];
         for (int k = losortStart[c]; k < k1; ++k) acc -= lp[k] * x[losortL[k]];
         const int f1 = ownerStart[c + 1];
         for (int f = ownerStart[c]; f < f1; ++f) acc -= upper[f] * x[u[f]];
-        r[c] = acc;
+        r[c] = iface_sub_neg(itf, c, x, acc);
     }
 }
 
@@ -74,13 +74,17 @@ template <class T>
 __global__ void __launch_bounds__(RED_NT) sumA_k(int n, const int* __restrict__ ownerStart,
                                                  const int* __restrict__ losortStart, const T* __restrict__ diag,
                                                  const T* __restrict__ lp, const T* __restrict__ upper,
-                                                 T* __restrict__ s) {
+                                                 T* __restrict__ s, Iface<T> itf) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         T acc = diag[c];
         const int k1 = losortStart[c + 1];
         for (int k = losortStart[c]; k < k1; ++k) acc += lp[k];
         const int f1 = ownerStart[c + 1];
         for (int f = ownerStart[c]; f < f1; ++f) acc += upper[f];
+        // lduMatrix::sumA (lduMatrixATmul.C:185-198): minus the interface
+        // boundary coefficients
+        if (itf.start)
+            for (int j = itf.start[c]; j < itf.start[c + 1]; ++j) acc -= itf.coef[j];
         s[c] = acc;
     }
 }
@@ -337,6 +341,13 @@ __global__ void lu_solve_k(int n, const T* __restrict__ LUg, const int* __restri
 }
 
 template <class T>
+__global__ void iface_bprime_k(int n, Iface<T> itf, const T* __restrict__ b, const T* __restrict__ psi,
+                               T* __restrict__ bp) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        bp[c] = iface_sub_neg(itf, c, psi, b[c]);
+}
+
+template <class T>
 __global__ void diag_solve_k(int n, const T* __restrict__ diag, const T* __restrict__ b, T* __restrict__ x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i] / diag[i];
 }
@@ -386,7 +397,7 @@ __global__ void __launch_bounds__(RED_NT) reduce_k(int n, const T* __restrict__ 
 template <class T>
 void Ops<T>::amul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
     amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                               a.lowerPerm, a.upper, x, y);
+                                               a.lowerPerm, a.upper, x, y, if_bou(m, a));
     count_launch();
 }
 
@@ -394,7 +405,8 @@ template <class T>
 void Ops<T>::tmul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
     // Tmul (lduMatrixATmul.C:95-151): y[u] += upper*x[l]; y[l] += lower*x[u]
     amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                               a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower, x, y);
+                                               a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower, x, y,
+                                               if_int(m, a));
     count_launch();
 }
 
@@ -402,14 +414,14 @@ template <class T>
 void Ops<T>::residual(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, const T* b,
                       T* r) {
     residual_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                   a.lowerPerm, a.upper, x, b, r);
+                                                   a.lowerPerm, a.upper, x, b, r, if_bou(m, a));
     count_launch();
 }
 
 template <class T>
 void Ops<T>::sumA(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, T* out) {
     sumA_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, a.diag, a.lowerPerm, a.upper,
-                                               out);
+                                               out, if_bou(m, a));
     count_launch();
 }
 
@@ -473,6 +485,12 @@ void Ops<T>::lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T
         lu_solve_k<T, true><<<1, 128, sm, s>>>(n, A, piv, b, x);
     else
         lu_solve_k<T, false><<<1, 32, 0, s>>>(n, A, piv, b, x);
+    count_launch();
+}
+
+template <class T>
+void Ops<T>::iface_bprime(cudaStream_t s, int n, const Iface<T>& itf, const T* b, const T* psi, T* bp) {
+    iface_bprime_k<T><<<grid_all(n), RED_NT, 0, s>>>(n, itf, b, psi, bp);
     count_launch();
 }
 

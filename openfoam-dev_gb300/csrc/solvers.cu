@@ -88,13 +88,15 @@ __global__ void __launch_bounds__(RED_NT) norm_init_k(int n, const int* os, cons
                                                       const T* diag, const T* lp, const T* upper,
                                                       const T* __restrict__ Apsi, const T* __restrict__ b,
                                                       T* __restrict__ r, T* __restrict__ r0, SolveState* st,
-                                                      Red2 red) {
+                                                      Red2 red, Iface<T> itf) {
     const double avg = n > 0 ? st->red0 / n : 0.0;
     double nf = 0.0, mg = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
         T sA = diag[c];
         for (int k = ls[c]; k < ls[c + 1]; ++k) sA += lp[k];
         for (int f = os[c]; f < os[c + 1]; ++f) sA += upper[f];
+        if (itf.start)  // sumA's interface boundary coefficients
+            for (int j = itf.start[c]; j < itf.start[c + 1]; ++j) sA -= itf.coef[j];
         const T t = sA * T(avg);
         nf += double(fabs(Apsi[c] - t) + fabs(b[c] - t));
         const T rc = b[c] - Apsi[c];
@@ -162,11 +164,11 @@ template <class T>
 __global__ void __launch_bounds__(RED_NT) pcg_amul_k(int n, const int* os, const int* ls, const int* lL,
                                                      const int* u, const T* diag, const T* lp, const T* upper,
                                                      const T* __restrict__ p, T* __restrict__ wA, SolveState* st,
-                                                     Red2 red) {
+                                                     Red2 red, Iface<T> itf) {
     if (st->done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, p);
+        const T v = iface_sub(itf, c, p, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, p));
         wA[c] = v;
         d += double(v) * double(p[c]);
     }
@@ -227,11 +229,12 @@ template <class T>
 __global__ void __launch_bounds__(RED_NT) pbicg_tmul_k(int n, const int* os, const int* ls, const int* lL,
                                                        const int* u, const T* diag, const T* upPerm, const T* lower,
                                                        const T* __restrict__ pT, T* __restrict__ wT,
-                                                       const T* __restrict__ wA, SolveState* st, Red2 red) {
+                                                       const T* __restrict__ wA, SolveState* st, Red2 red,
+                                                       Iface<T> itf) {
     if (st->done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        wT[c] = row_amul<T>(c, os, ls, lL, u, diag, upPerm, lower, pT);
+        wT[c] = iface_sub(itf, c, pT, row_amul<T>(c, os, ls, lL, u, diag, upPerm, lower, pT));
         d += double(wA[c]) * double(pT[c]);
     }
     double s, dummy;
@@ -310,11 +313,11 @@ __global__ void __launch_bounds__(RED_NT) bicg_amul_alpha_k(int n, const int* os
                                                             const int* u, const T* diag, const T* lp,
                                                             const T* upper, const T* __restrict__ yA,
                                                             T* __restrict__ AyA, const T* __restrict__ r0,
-                                                            SolveState* st, Red2 red) {
+                                                            SolveState* st, Red2 red, Iface<T> itf) {
     if (st->done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, yA);
+        const T v = iface_sub(itf, c, yA, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, yA));
         AyA[c] = v;
         d += double(r0[c]) * double(v);
     }
@@ -360,11 +363,11 @@ __global__ void __launch_bounds__(RED_NT) bicg_amul_omega_k(int n, const int* os
                                                             const int* u, const T* diag, const T* lp,
                                                             const T* upper, const T* __restrict__ zA,
                                                             T* __restrict__ tA, const T* __restrict__ sA,
-                                                            SolveState* st, Red2 red) {
+                                                            SolveState* st, Red2 red, Iface<T> itf) {
     if (st->done) return;
     double tt = 0.0, ts = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, zA);
+        const T v = iface_sub(itf, c, zA, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, zA));
         tA[c] = v;
         tt += double(v) * double(v);
         ts += double(v) * double(sA[c]);
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int
                                                                 const int* u, const T* diag, const T* lp,
                                                                 const T* upper, const T* __restrict__ psi,
                                                                 const T* __restrict__ b, T* __restrict__ r,
-                                                                SolveState* st, Red2 red, int inc) {
+                                                                SolveState* st, Red2 red, int inc, Iface<T> itf) {
     if (st->done) return;
     double mg = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
@@ -453,9 +456,9 @@ __global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int
             T acc = b[c] - diag[c] * psi[c];
             for (int k = ls[c]; k < ls[c + 1]; ++k) acc -= lp[k] * psi[lL[k]];
             for (int f = os[c]; f < os[c + 1]; ++f) acc -= upper[f] * psi[u[f]];
-            v = acc;
+            v = iface_sub_neg(itf, c, psi, acc);
         } else {
-            v = b[c] - row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi);
+            v = b[c] - iface_sub(itf, c, psi, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi));
         }
         r[c] = v;
         mg += fabs(double(v));
@@ -505,7 +508,8 @@ template <class T>
 void Kern<T>::norm_init(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* Apsi,
                         const T* b, T* r, T* r0, SolveState* st) {
     norm_init_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.u, a.diag, a.lowerPerm,
-                                                    a.upper, Apsi, b, r, r0, st, Red2{sc.partials, sc.counters});
+                                                    a.upper, Apsi, b, r, r0, st, Red2{sc.partials, sc.counters},
+                                                    if_bou(m, a));
     count_launch();
 }
 
@@ -532,7 +536,8 @@ template <class T>
 void Kern<T>::pcg_amul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* p, T* wA,
                        SolveState* st) {
     pcg_amul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                   a.lowerPerm, a.upper, p, wA, st, Red2{sc.partials, sc.counters});
+                                                   a.lowerPerm, a.upper, p, wA, st, Red2{sc.partials, sc.counters},
+                                                   if_bou(m, a));
     count_launch();
 }
 
@@ -553,7 +558,7 @@ void Kern<T>::pbicg_tmul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const 
                          T* wT, const T* wA, SolveState* st) {
     pbicg_tmul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                      a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower,
-                                                     pT, wT, wA, st, Red2{sc.partials, sc.counters});
+                                                     pT, wT, wA, st, Red2{sc.partials, sc.counters}, if_int(m, a));
     count_launch();
 }
 
@@ -581,7 +586,7 @@ void Kern<T>::bicg_amul_alpha(cudaStream_t s, Scratch& sc, const LevelMesh& m, c
                               T* AyA, const T* r0, SolveState* st) {
     bicg_amul_alpha_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                           a.lowerPerm, a.upper, yA, AyA, r0, st,
-                                                          Red2{sc.partials, sc.counters});
+                                                          Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
 
@@ -603,7 +608,7 @@ void Kern<T>::bicg_amul_omega(cudaStream_t s, Scratch& sc, const LevelMesh& m, c
                               T* tA, const T* sA, SolveState* st) {
     bicg_amul_omega_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                           a.lowerPerm, a.upper, zA, tA, sA, st,
-                                                          Red2{sc.partials, sc.counters});
+                                                          Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
 
@@ -636,11 +641,11 @@ void Kern<T>::gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& 
     if (inc > 0)
         gamg_residual_check_k<T, true><<<grid_for(m.n), RED_NT, 0, s>>>(
             m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
-            Red2{sc.partials, sc.counters}, inc);
+            Red2{sc.partials, sc.counters}, inc, if_bou(m, a));
     else
         gamg_residual_check_k<T, false><<<grid_for(m.n), RED_NT, 0, s>>>(
             m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
-            Red2{sc.partials, sc.counters}, 1);
+            Red2{sc.partials, sc.counters}, 1, if_bou(m, a));
     count_launch();
 }
 

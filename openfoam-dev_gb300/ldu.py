@@ -131,6 +131,8 @@ _SIG = {
     "cfx_matrix_update": (_i, [_vp, _vp, _vp, _vp]),
     "cfx_matrix_update_device": (_i, [_vp, _vp, _vp, _vp]),
     "cfx_matrix_create_empty": (_i, [_vp, _i, ctypes.POINTER(_vp)]),
+    "cfx_mesh_set_interfaces": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "cfx_matrix_set_interface_coeffs": (_i, [_vp, _vp, _vp]),
     "cfx_fv_geometry": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
     "cfx_fvm_assemble": (_i, [_vp, ctypes.POINTER(FvmTerms), _vp]),
     "cfx_matrix_destroy": (_i, [_vp]),
@@ -337,6 +339,12 @@ class LduMesh:
                "level_info")
         return ra, fra, fl, nc.value, ncf.value, cl, cu
 
+    def set_interfaces(self, patchSizes, faceCells, nbrFaceCells):
+        """Coupled (cyclic) interfaces: faces concatenated in patch order."""
+        self._if = [np.ascontiguousarray(a, np.int32) for a in (patchSizes, faceCells, nbrFaceCells)]
+        _check(lib().cfx_mesh_set_interfaces(self.h, len(self._if[0]), _hp(self._if[0]), _hp(self._if[1]),
+                                             _hp(self._if[2])), "cfx_mesh_set_interfaces")
+
     def fv_geometry(self, magSf, deltaCoeffs, V, bCell, magSfB, deltaCoeffsB, weights=None):
         """Face geometry for device-side assembly (host arrays, uploaded once):
         internal faces in lduAddressing order, boundary faces in patch order."""
@@ -373,6 +381,13 @@ class LduMatrix:
                "cfx_matrix_create")
         self.h = h
         _track("matrix", self)
+
+    def set_interface_coeffs(self, bou, intc=None):
+        """interfaceBouCoeffs / interfaceIntCoeffs, faces concatenated in patch order."""
+        self._ifc = [np.ascontiguousarray(bou, np.float64), None if intc is None else
+                     np.ascontiguousarray(intc, np.float64)]
+        _check(lib().cfx_matrix_set_interface_coeffs(self.h, _hp(self._ifc[0]), _hp(self._ifc[1])),
+               "cfx_matrix_set_interface_coeffs")
 
     @classmethod
     def empty(cls, mesh, symmetric):
@@ -616,7 +631,11 @@ def system_matrix(s, ctx=None):
     if "_cfx" not in s:
         ctx = ctx or default_context()
         mesh = LduMesh(ctx, s["diag"].size, s["l"], s["u"])
+        if s.get("ifCell") is not None:  # coupled (cyclic) interfaces
+            mesh.set_interfaces(s["ifSize"], s["ifCell"], s["ifNbr"])
         A = LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
+        if s.get("ifCell") is not None:
+            A.set_interface_coeffs(s["ifBou"], s.get("ifInt"))
         s["_cfx"] = (mesh, A)
     return s["_cfx"]
 

@@ -26,6 +26,7 @@
 
 #include "lduMatrix.H"
 #include "GAMGAgglomeration.H"
+#include "cyclicLduInterface.H"
 #include "addToRunTimeSelectionTable.H"
 
 #include "cfx.h"
@@ -49,6 +50,7 @@ protected:
         label nFaces = -1;
         bool sym = true;
         bool gamg = false;
+        bool interfaces = false;  // the mesh's cyclic interfaces are set
     };
 
     static cfx_ctx* context()
@@ -81,13 +83,33 @@ protected:
     //  coefficients uploaded now
     Entry& deviceMatrix() const
     {
+        // coupled interfaces: cyclic ones (faceCells, the neighbour patch's
+        // faceCells, in interface order); processor interfaces are not
+        // supported on one GPU
+        DynamicList<label> ifSize, ifCells, ifNbr;
+        DynamicList<scalar> ifBou, ifInt;
         forAll(interfaces_, patchi)
         {
-            if (interfaces_.set(patchi))
+            if (!interfaces_.set(patchi)) continue;
+            const lduInterface& li = interfaces_[patchi].interface();
+            if (!isA<cyclicLduInterface>(li))
             {
                 FatalErrorInFunction
-                    << "cudaLduSolvers: coupled interfaces are not supported"
+                    << "cudaLduSolvers: only cyclic coupled interfaces are "
+                    << "supported (patch " << patchi << ")"
                     << exit(FatalError);
+            }
+            const label nbrI =
+                refCast<const cyclicLduInterface>(li).nbrPatchIndex();
+            const labelUList& fc = li.faceCells();
+            const labelUList& nc = interfaces_[nbrI].interface().faceCells();
+            ifSize.append(fc.size());
+            forAll(fc, i)
+            {
+                ifCells.append(fc[i]);
+                ifNbr.append(nc[i]);
+                ifBou.append(interfaceBouCoeffs_[patchi][i]);
+                ifInt.append(interfaceIntCoeffs_[patchi][i]);
             }
         }
 
@@ -118,6 +140,19 @@ protected:
             e.nCells = nCells;
             e.nFaces = nFaces;
         }
+        if (ifSize.size() && !e.interfaces)
+        {
+            check
+            (
+                cfx_mesh_set_interfaces
+                (
+                    e.mesh, ifSize.size(), ifSize.cdata(), ifCells.cdata(),
+                    ifNbr.cdata()
+                ),
+                "cfx_mesh_set_interfaces"
+            );
+            e.interfaces = true;
+        }
 
         const scalar* lower = sym ? nullptr : matrix_.lower().cdata();
         if (!e.mat || e.sym != sym)
@@ -143,6 +178,17 @@ protected:
                     e.mat, matrix_.diag().cdata(), matrix_.upper().cdata(), lower
                 ),
                 "cfx_matrix_update"
+            );
+        }
+        if (ifSize.size())
+        {
+            check
+            (
+                cfx_matrix_set_interface_coeffs
+                (
+                    e.mat, ifBou.cdata(), ifInt.cdata()
+                ),
+                "cfx_matrix_set_interface_coeffs"
             );
         }
         return e;

@@ -41,6 +41,8 @@ SYSTEMS = {
     "jcube7": lambda: system("jcube7"),
     "cd6": lambda: system("cd6"),
     "box": lambda: system("box"),
+    "cyc7": lambda: system("cyc7"),    # cyclic interfaces, symmetric
+    "cycd7": lambda: system("cycd7"),  # cyclic interfaces, upwind asymmetric
     "cube24": lambda: cases.pcg_cube(24, seed=3),
     "perm_lap": lambda: _permuted("gamg_cube", 5),
     "perm_cd": lambda: _permuted("bicgstab_cube", 6),
@@ -55,7 +57,12 @@ def sweep_form(request):
 
 def _fresh(s):
     mesh = ldu.LduMesh(ldu.default_context(), s["diag"].size, s["l"], s["u"])
-    return mesh, ldu.LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
+    if s.get("ifCell") is not None:
+        mesh.set_interfaces(s["ifSize"], s["ifCell"], s["ifNbr"])
+    A = ldu.LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
+    if s.get("ifCell") is not None:
+        A.set_interface_coeffs(s["ifBou"], s.get("ifInt"))
+    return mesh, A
 
 
 @pytest.mark.parametrize("name", sorted(SYSTEMS))

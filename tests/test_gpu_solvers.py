@@ -372,3 +372,26 @@ def test_pbicg_against_oracle_and_its_errors():
     with pytest.raises(ldu.FatalError, match="mixed"):
         ldu.solve(cd, np.zeros_like(cd["source"]), {"solver": "cudaPBiCG", "preconditioner": "DILU",
                                                     "precision": "mixed"})
+
+
+def test_cyclic_interfaces_refusals_and_larger_system():
+    """With coupled interfaces GAMG and mixed precision are refused; a 16^3
+    periodic system solves like the oracle with PCG+DIC and PBiCG+DILU."""
+    s = cases.cyclic_cube(16, jitter=0.2, seed=4)
+    with pytest.raises(ldu.FatalError, match="interfaces"):
+        ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaPCG", "preconditioner": "DIC",
+                                                  "precision": "mixed"})
+    ref = np.zeros_like(s["source"])
+    rp = orc.pcg(s, ref, tol=1e-10, max_iter=2000)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-10, "relTol": 0,
+                              "maxIter": 2000})
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1
+    assert _rel(psi, ref) <= (RTOL_FP64 if perf.nIterations == rp.nIterations else 1e-6)
+    cd = cases.cyclic_cube(12, jitter=0.1, seed=5, U=[1.0, 0.3, 0.2], gamma=0.05)
+    ref = np.zeros_like(cd["source"])
+    rp = orc.pbicg(cd, ref, tol=1e-10, precond="DILU")
+    psi = np.zeros_like(cd["source"])
+    perf = ldu.solve(cd, psi, {"solver": "cudaPBiCG", "preconditioner": "DILU", "tolerance": 1e-10, "relTol": 0})
+    assert perf.converged and _iters_ok("PBiCG", perf.nIterations, rp.nIterations)
+    _residual_ok(cd, psi, 1e-10)

@@ -1401,6 +1401,13 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
             set_error("precision mixed is not available with coupled interfaces");
             return CFX_ERR_CONFIG;
         }
+        // nonBlockingGaussSeidel splits its sweep at the first interface cell
+        // (nonBlockingGaussSeidelSmoother.C:56-78); only GaussSeidel's
+        // arithmetic (no interfaces) is built
+        if ((c->solver == CFX_SOLVER_SMOOTH) && c->smoother == CFX_SMOOTH_NBGS) {
+            set_error("nonBlockingGaussSeidel with coupled interfaces is not supported");
+            return CFX_ERR_CONFIG;
+        }
         if (mat->ifN != mat->mesh->nIf) {
             set_error("the interface coefficients are not set (cfx_matrix_set_interface_coeffs)");
             return CFX_ERR_STATE;
@@ -2158,6 +2165,7 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, i
     if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
     if (kind < CFX_SMOOTH_GS || kind > CFX_SMOOTH_NBGS) return CFX_ERR_CONFIG;
     if (kind == CFX_SMOOTH_FDIC && !mat->sym) return CFX_ERR_CONFIG;
+    if (kind == CFX_SMOOTH_NBGS && mat->mesh->nIf) return CFX_ERR_CONFIG;  // its interface split is not built
     if (kind == CFX_SMOOTH_FDIC) kind = CFX_SMOOTH_DIC;  // the same arithmetic (FDICSmoother.C:40-160)
     if (kind == CFX_SMOOTH_NBGS) kind = CFX_SMOOTH_GS;   // no coupled interfaces
     if ((kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) && !mat->sym) return CFX_ERR_CONFIG;

@@ -88,18 +88,6 @@ __device__ __forceinline__ void face_combined(const FvmArgs& a, const FaceTerms&
     }
 }
 
-__global__ void __launch_bounds__(FV_NT) fvm_faces_k(int nf, FvGeom g, FvmArgs a, double* __restrict__ upper,
-                                                     double* __restrict__ lower) {
-    for (int f = blockIdx.x * FV_NT + threadIdx.x; f < nf; f += gridDim.x * FV_NT) {
-        const FaceTerms t = face_terms(a, g, f);
-        double U, L;
-        bool hasU, hasL;
-        face_combined(a, t, U, L, hasU, hasL);
-        upper[f] = U;
-        if (lower) lower[f] = L;
-    }
-}
-
 // One boundary face's combined internal and boundary coefficients.
 __device__ __forceinline__ void boundary_combined(const FvmArgs& a, const FvGeom& g, int b, double& ic, double& bc) {
     const int type = a.bcType[b];
@@ -147,10 +135,13 @@ __device__ __forceinline__ void boundary_combined(const FvmArgs& a, const FvGeom
     }
 }
 
+// One thread per cell: the diagonal and source of the cell, and the
+// combined upper/lower of the faces it owns (each face has one owner).
 __global__ void __launch_bounds__(FV_NT) fvm_cells_k(int n, const int* __restrict__ ownerStart,
                                                      const int* __restrict__ losortStart,
                                                      const int* __restrict__ losort, FvGeom g, FvmArgs a,
-                                                     double* __restrict__ diag, double* __restrict__ source) {
+                                                     double* __restrict__ diag, double* __restrict__ source,
+                                                     double* __restrict__ upper, double* __restrict__ lower) {
     for (int c = blockIdx.x * FV_NT + threadIdx.x; c < n; c += gridDim.x * FV_NT) {
         // each term's negSumDiag: faces c neighbours (ascending, they precede
         // the faces c owns), subtracting Upper; then owned faces, Lower
@@ -166,6 +157,11 @@ __global__ void __launch_bounds__(FV_NT) fvm_cells_k(int n, const int* __restric
             const FaceTerms t = face_terms(a, g, f);
             dDiv -= t.divL;
             dLap -= t.lapU;
+            double U, L;
+            bool hasU, hasL;
+            face_combined(a, t, U, L, hasU, hasL);
+            upper[f] = U;
+            if (lower) lower[f] = L;
         }
         double D = 0.0, S = 0.0;
         bool started = false;
@@ -221,9 +217,9 @@ inline int fv_grid(int n) {
 
 void launch_fvm_assemble(cudaStream_t s, const LevelMesh& m, const FvGeom& g, const FvmArgs& a, double* diag,
                          double* upper, double* lower, double* source) {
-    if (m.nf) fvm_faces_k<<<fv_grid(m.nf), FV_NT, 0, s>>>(m.nf, g, a, upper, lower);
-    fvm_cells_k<<<fv_grid(m.n), FV_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losort, g, a, diag, source);
-    count_launch(m.nf ? 2 : 1);
+    fvm_cells_k<<<fv_grid(m.n), FV_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losort, g, a, diag, source,
+                                               upper, lower);
+    count_launch();
 }
 
 }  // namespace cfx

@@ -327,6 +327,7 @@ def run_ours(args, rank, world, local, pg):
     }
 
     assembly = fvm_assembly_measure(ctx, ev_time, stream, local) if world == 1 else None
+    krylov = krylov_configs(ctx, stream, local) if world == 1 else None
 
     tm = reduce_max(pg, statistics.median(t_mixed))
     t64 = reduce_max(pg, statistics.median(t_fp64))
@@ -369,6 +370,10 @@ def run_ours(args, rank, world, local, pg):
     if assembly:
         assembly["frac"] = assembly["GB_s"] / peak
         line["assembly"] = assembly
+    if krylov:
+        for v in krylov.values():
+            v["FP64"]["frac"] = v["FP64"]["GB_s"] / peak
+        line["krylov"] = krylov
     if not args.no_cpu_baseline and world == 1:
         r = cpu_reference_sample(s, cycles_hint=p_fp64.nIterations)
         line["cpu_baseline"] = {
@@ -381,6 +386,56 @@ def run_ours(args, rank, world, local, pg):
         line.update(run_batch_serve(args, local, True, True))
     print(json.dumps(line), flush=True)
     return 0
+
+
+def krylov_configs(ctx, stream, local, reps=3):
+    """The Krylov configurations: PCG+DIC on the uniform 64^3 cube and
+    PBiCGStab+DILU on the 128^3 jittered, permuted-then-CM-renumbered upwind
+    system, each to 1e-8 in FP64 and FP32-inner/FP64-refined, resident
+    vectors, CUDA events on the library's stream (median of reps).  GB/s:
+    the per-iteration algorithmic bytes (PCG+DIC 23sN + 3sF + 24F,
+    PBiCGStab+DILU 41sN + 8sF + 56F, s = 8) times the iterations, over the
+    solve time."""
+    import torch
+    from openfoam_dev_gb300 import cases, ldu
+    out = {}
+    for name, s, ctl, per_iter in (
+            ("pcg_dic_64", cases.pcg_cube(64, seed=1),
+             {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-8, "relTol": 0, "maxIter": 2000},
+             lambda N, F: 23 * 8 * N + 3 * 8 * F + 24 * F),
+            ("pbicgstab_dilu_128", cases.bicgstab_cube(128, seed=1),
+             {"solver": "cudaPBiCGStab", "preconditioner": "DILU", "tolerance": 1e-8, "relTol": 0,
+              "maxIter": 2000},
+             lambda N, F: 41 * 8 * N + 8 * 8 * F + 56 * F)):
+        mesh = ldu.LduMesh(ctx, s["diag"].size, s["l"], s["u"])
+        A = ldu.LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
+        N, F = s["diag"].size, s["l"].size
+        src = torch.from_numpy(s["source"]).to(f"cuda:{local}")
+        psi = torch.zeros_like(src)
+        res = {"cells": N, "faces": F, "bytes_per_iteration": per_iter(N, F)}
+        for prec in ("FP64", "mixed"):
+            sol = ldu.solver_new("x", A, dict(ctl, precision=prec))
+            ts, perf = [], None
+            for r in range(reps + 1):
+                with torch.cuda.stream(stream):
+                    psi.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                perf = sol.solve(psi, src)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if r:
+                    ts.append(e0.elapsed_time(e1) / 1e3)
+            t = statistics.median(ts)
+            res[prec] = {"s": t, "iterations": perf.nIterations, "final_residual": perf.finalResidual,
+                         "converged": bool(perf.converged)}
+            if prec == "FP64":
+                res[prec]["GB_s"] = per_iter(N, F) * perf.nIterations / t / 1e9
+        res["mixed_speedup"] = res["FP64"]["s"] / res["mixed"]["s"]
+        out[name] = res
+        A.close()
+        mesh.close()
+    return out
 
 
 def fvm_assembly_measure(ctx, ev_time, stream, local, n=128):

@@ -1282,12 +1282,18 @@ cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, c
         h = read_state(ctx, 0);
         int inner = 0, outer = 0;
         const double innerRelTol = 1e-3;
+        // An FP32 inner solve that has not reduced its residual by
+        // innerRelTol within innerCap iterations has stalled (FP32 rounding
+        // on an ill-conditioned system): the solve then finishes in FP64 from
+        // the current psi.
+        const int innerCap = std::max(100, ctl.maxIter / 10);
+        bool stalled = false;
         while (!h.done) {
             launch_cast_d2f(s, n, r64, r32);
             Kern<float>::fill(s, n, 0.0f, e32, nullptr);
             SolveState hi{};
             CFX_TRY(krylov<float>(mat, mat->w32, ctl.solver == CFX_SOLVER_PCG ? mat->gPCG : mat->gBiCG, 0, ctl.solver,
-                                  ctl.preconditioner, e32, r32, 1, 0.0, innerRelTol, ctl.maxIter, 0, ctl, &hi));
+                                  ctl.preconditioner, e32, r32, 1, 0.0, innerRelTol, innerCap, 0, ctl, &hi));
             inner += hi.nIterations;
             launch_add_f2d(s, n, e32, psi, nullptr);
             // outer: r = b - A psi, |r|/normFactor, one refinement step
@@ -1295,6 +1301,22 @@ cfx_status krylov_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, c
             h = read_state(ctx, 0);
             ++outer;
             if (hi.singular || hi.nIterations == 0) break;
+            if (!hi.converged) {
+                stalled = true;
+                break;
+            }
+        }
+        if (stalled && !h.done) {
+            // the FP64 Krylov solve from here; its test keeps the original
+            // initial residual: final < max(tolerance, relTol * initial)
+            SolveState h64{};
+            const double tol = std::max(ctl.tolerance, ctl.relTol * h.initialResidual);
+            CFX_TRY(krylov<double>(mat, mat->w64, ctl.solver == CFX_SOLVER_PCG ? mat->gPCG : mat->gBiCG, 0,
+                                   ctl.solver, ctl.preconditioner, psi, b, 0, tol, 0.0, ctl.maxIter, 0, ctl, &h64));
+            inner += h64.nIterations;
+            h.finalResidual = h64.finalResidual;
+            h.converged = h64.converged;
+            h.singular = h64.singular;
         }
         h.nIterations = inner;
         perf->nOuter = outer;

@@ -327,7 +327,7 @@ def run_ours(args, rank, world, local, pg):
     }
 
     assembly = fvm_assembly_measure(ctx, ev_time, stream, local) if world == 1 else None
-    krylov = krylov_configs(ctx, stream, local) if world == 1 else None
+    krylov = krylov_configs(ctx, stream, local, cpu=not args.no_cpu_baseline) if world == 1 else None
 
     tm = reduce_max(pg, statistics.median(t_mixed))
     t64 = reduce_max(pg, statistics.median(t_fp64))
@@ -388,7 +388,27 @@ def run_ours(args, rank, world, local, pg):
     return 0
 
 
-def krylov_configs(ctx, stream, local, reps=3):
+def krylov_cpu_sample(s, solver, iterations):
+    """The oracle (serial C restatement, bit-exact with the reference build)
+    on the same system: PCG+DIC to convergence, PBiCGStab+DILU for 10
+    iterations extrapolated to the GPU FP64 solve's count (one Grace core)."""
+    from oracle import oracle as orc
+    psi = np.zeros_like(s["source"])
+    if solver == "PCG":
+        t0 = time.perf_counter()
+        p = orc.pcg(s, psi, tol=1e-8, max_iter=2000, precond="DIC")
+        t = time.perf_counter() - t0
+        return {"value": t, "unit": "s", "cores": 1, "kind": "port", "iterations": p.nIterations,
+                "sample": "oracle PCG+DIC, full solve to 1e-8"}
+    k = 10
+    t0 = time.perf_counter()
+    orc.pbicgstab(s, psi, tol=1e-30, max_iter=k, precond="DILU")
+    t = time.perf_counter() - t0
+    return {"value": t * iterations / k, "unit": "s", "cores": 1, "kind": "port", "iterations": iterations,
+            "sample": f"oracle PBiCGStab+DILU, {k} iterations ({t:.2f} s) extrapolated to {iterations}"}
+
+
+def krylov_configs(ctx, stream, local, reps=3, cpu=True):
     """The Krylov configurations: PCG+DIC on the uniform 64^3 cube and
     PBiCGStab+DILU on the 128^3 jittered, permuted-then-CM-renumbered upwind
     system, each to 1e-8 in FP64 and FP32-inner/FP64-refined, resident
@@ -432,6 +452,9 @@ def krylov_configs(ctx, stream, local, reps=3):
             if prec == "FP64":
                 res[prec]["GB_s"] = per_iter(N, F) * perf.nIterations / t / 1e9
         res["mixed_speedup"] = res["FP64"]["s"] / res["mixed"]["s"]
+        if cpu:
+            res["cpu_baseline"] = krylov_cpu_sample(s, "PCG" if name.startswith("pcg") else "PBiCGStab",
+                                                    res["FP64"]["iterations"])
         out[name] = res
         A.close()
         mesh.close()

@@ -670,7 +670,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1163,7 +1163,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2032,6 +2032,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value > 1) return CFX_ERR_ARG;
             set_sweep_wave(value);
             return CFX_OK;
+        case CFX_TUNE_CLUSTER_PRE:
+            if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16) return CFX_ERR_ARG;
+            set_sweep_cluster_pre(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2042,6 +2046,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_SMALL_SWEEP: *value = small_sweep_threshold(); return CFX_OK;
         case CFX_TUNE_CLUSTER_GLOBAL: *value = cluster_global_cells(); return CFX_OK;
         case CFX_TUNE_CLUSTER_SIZE: *value = sweep_cluster_size(); return CFX_OK;
+        case CFX_TUNE_CLUSTER_PRE: *value = sweep_cluster_pre(); return CFX_OK;
         case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
         case CFX_TUNE_SMEM_BYTES: *value = int(sweep_smem_cap()); return CFX_OK;
         case CFX_TUNE_GRID_WAVE: *value = sweep_wave(); return CFX_OK;

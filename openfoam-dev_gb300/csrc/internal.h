@@ -322,6 +322,8 @@ void set_sweep_wave(int on);
 void set_sweep_smem_cap(size_t b);
 int sweep_cluster_size();
 void set_sweep_cluster_size(int cs);
+int sweep_cluster_pre();
+void set_sweep_cluster_pre(int cs);
 int cluster_global_cells();
 void set_cluster_global_cells(int n);
 

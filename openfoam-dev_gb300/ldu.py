@@ -503,6 +503,7 @@ class SolverPerformance:
 
 TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS, TUNE_SMEM_BYTES = 0, 1, 2, 3, 4
 TUNE_GRID_WAVE = 5
+TUNE_CLUSTER_PRE = 6
 
 
 def tune_set(key, value):

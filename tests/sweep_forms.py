@@ -5,6 +5,8 @@ library's tuning knobs so every form is checked on small systems:
 * cta     -- one CTA, vector in shared memory (the default for small levels)
 * cluster -- a 16-CTA cluster, vector in distributed shared memory
 * cluster_global -- a 16-CTA cluster, vector in global memory (L2)
+* cluster_pre -- the default split: DIC/DILU sweeps in a 16-CTA cluster's
+             shared memory, Gauss-Seidel sweeps on the persistent grid
 * grid    -- the persistent grid, wavefront: each 32-slot group waits for the
              groups it reads (vector in global memory)
 * levels  -- the persistent grid with whole-level counters (the default grid form)
@@ -18,11 +20,13 @@ FORMS = {
     "cta": {},
     "cluster": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 8192},
     "cluster_global": {ldu.TUNE_CLUSTER_SIZE: 16, ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_CLUSTER_GLOBAL: 1 << 30},
+    # the default split: DIC/DILU sweeps on a 16-CTA cluster, Gauss-Seidel on the grid
+    "cluster_pre": {ldu.TUNE_SMEM_BYTES: 8192, ldu.TUNE_CLUSTER_PRE: 16},
     "grid": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 1},
     "levels": {ldu.TUNE_SMEM_BYTES: 0, ldu.TUNE_GRID_WAVE: 0},
 }
 KNOBS = (ldu.TUNE_SMALL_SWEEP, ldu.TUNE_CLUSTER_GLOBAL, ldu.TUNE_CLUSTER_SIZE, ldu.TUNE_SMEM_BYTES,
-         ldu.TUNE_GRID_WAVE)
+         ldu.TUNE_GRID_WAVE, ldu.TUNE_CLUSTER_PRE)
 
 
 @contextlib.contextmanager

@@ -141,7 +141,7 @@ def main():
         fh.write(f"all: {harness}\n")
         fh.write(f"{lib}: {' '.join(objs)}\n"
                  f"\t$(CXX) -shared -fuse-ld=bfd -o $@ $^ -lz -lpthread -ldl -lm\n")
-        fh.write(f"{harness}: {harness_src} {lib}\n"
+        fh.write(f"{harness}: {harness_src} {os.path.join(HERE, 'harness_io.H')} {lib}\n"
                  f"\t$(CXX) $(FLAGS) -o $@ {harness_src} -L{OUT} -lOpenFOAM "
                  f"-Wl,-rpath,{OUT} -lz -lpthread -ldl -lm\n")
         fh.write("\n".join(rules))

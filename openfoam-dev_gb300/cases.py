@@ -99,12 +99,16 @@ def box_mesh(nx, ny, nz, L=(1.0, 1.0, 1.0), jitter=0.0, seed=0):
                 Sf=Sf, Cf=Cf, magSf=magSf, C=C, V=V)
 
 
-def fv_geometry(mesh):
+def fv_geometry(mesh, snGrad="uncorrected"):
     """The face geometry an fvMesh hands to device-side assembly, by the
-    reference's surfaceInterpolation (surfaceInterpolation.C:160-268) and
-    fvPatch::delta (fvPatch.C:159-164): internal magSf, deltaCoeffs
-    1/|C_N - C_P|, weights SfdNei/(SfdOwn + SfdNei); boundary faces (patch
-    order) with their cell, magSf and 1/|n (n . (Cf - C_P))|; cell volumes."""
+    reference's surfaceInterpolation (surfaceInterpolation.C:160-330) and
+    fvPatch::delta (fvPatch.C:159-164): internal magSf; the snGrad scheme's
+    deltaCoeffs -- nonOrthDeltaCoeffs 1/max(n . d, 0.05 |d|) for corrected
+    and uncorrected (surfaceInterpolation.C:302-318), the plain
+    deltaCoeffs 1/|d| for orthogonal -- with d = C_N - C_P; weights
+    SfdNei/(SfdOwn + SfdNei); boundary faces (patch order) with their cell,
+    magSf and 1/|n (n . (Cf - C_P))| (fvPatch::deltaCoeffs, which the
+    boundary gradient coefficients use); cell volumes."""
     nI, nF = mesh["nInternalFaces"], mesh["nFaces"]
     own, nei = mesh["owner"], mesh["neighbour"]
     Sf = mesh["Sf"].reshape(nF, 3)
@@ -113,12 +117,20 @@ def fv_geometry(mesh):
     mag = lambda v: np.sqrt(v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2])
     dot = lambda a, b: a[:, 0] * b[:, 0] + a[:, 1] * b[:, 1] + a[:, 2] * b[:, 2]
     d = C[nei] - C[own[:nI]]
+    if snGrad == "orthogonal":
+        dc = 1.0 / mag(d)
+    elif snGrad in ("corrected", "uncorrected"):
+        unitArea = Sf[:nI] / mesh["magSf"][:nI, None]
+        a, b = dot(unitArea, d), 0.05 * mag(d)
+        dc = 1.0 / np.where(a > b, a, b)
+    else:
+        raise ValueError("snGrad scheme " + snGrad)
     sOwn = np.abs(dot(Sf[:nI], Cf[:nI] - C[own[:nI]]))
     sNei = np.abs(dot(Sf[:nI], C[nei] - Cf[:nI]))
     bo = own[nI:]
     nHat = Sf[nI:] / mesh["magSf"][nI:, None]
     delta = nHat * dot(nHat, Cf[nI:] - C[bo])[:, None]
-    return dict(magSf=mesh["magSf"][:nI].copy(), deltaCoeffs=1.0 / mag(d), weights=sNei / (sOwn + sNei),
+    return dict(magSf=mesh["magSf"][:nI].copy(), deltaCoeffs=dc, weights=sNei / (sOwn + sNei),
                 V=mesh["V"].copy(), bCell=bo.astype(np.int32), magSfB=mesh["magSf"][nI:].copy(),
                 deltaCoeffsB=1.0 / mag(delta))
 

@@ -74,3 +74,66 @@ def solve(s, ctl, psi0=None, weights=None):
     if weights is not None:
         recs["weights"] = weights
     return run(recs)
+
+
+FV_HARNESS = os.path.join(HERE, "_ref", "fv_harness")
+
+_FOAM_HEADER = "FoamFile\n{\n    format ascii;\n    class dictionary;\n    object %s;\n}\n"
+
+
+def fv_available():
+    return os.path.exists(FV_HARNESS) and available()
+
+
+def _fv_case(td, div):
+    """system/ of the case fv_harness runs in: Euler, Gauss <div> for
+    div(phi,T), Gauss linear uncorrected for the Laplacian (the face-normal
+    gradient without the non-orthogonal correction, as the device assembly
+    has it)."""
+    sysdir = os.path.join(td, "cfxcase", "system")
+    os.makedirs(sysdir, exist_ok=True)
+    files = {
+        "fvSchemes": ("ddtSchemes { default Euler; }\n"
+                      "gradSchemes { default Gauss linear; }\n"
+                      "divSchemes { default none; div(phi,T) Gauss %s; }\n"
+                      "laplacianSchemes { default Gauss linear uncorrected; }\n"
+                      "interpolationSchemes { default linear; }\n"
+                      "snGradSchemes { default uncorrected; }\n" % div),
+        "fvSolution": "solvers { }\n",
+        "controlDict": ("application none;\nstartFrom startTime;\nstartTime 0;\nstopAt endTime;\n"
+                        "endTime 1;\ndeltaT 1;\nwriteControl timeStep;\nwriteInterval 1;\n"),
+    }
+    for name, body in files.items():
+        with open(os.path.join(sysdir, name), "w") as fh:
+            fh.write(_FOAM_HEADER % name + body)
+
+
+def fvm(mesh, patchBC, bcValue, deltaT=None, psi0=None, phi=None, phiB=None, div="upwind", lapSign=0,
+        gamma=None, gammaB=None, gammaUniform=None, su=None):
+    """The reference's fvm::ddt(T) + fvm::div(phi, T) +/- fvm::laplacian(gamma, T)
+    == su on a hex mesh, each term optional (fv_harness): the diag (with
+    addBoundaryDiag), upper, lower (when asymmetric) and source (with
+    addBoundarySource) the solver receives, and the geometry the schemes used.
+    patchBC per patch: 0 zeroGradient, 1 fixedValue, 2 fixedGradient; bcValue
+    per boundary face (value or gradient)."""
+    recs = dict(points=mesh["points"], faces=mesh["faces"], owner=mesh["owner"], neighbour=mesh["neighbour"],
+                patchStart=mesh["patchStart"], patchBC=np.asarray(patchBC, np.int32),
+                bcValue=np.asarray(bcValue, np.float64))
+    if deltaT is not None:
+        recs["deltaT"] = np.array([deltaT], np.float64)
+    opt = dict(psi0=psi0, phi=phi, phiB=phiB, gamma=gamma, gammaB=gammaB, su=su)
+    recs.update({k: np.asarray(v, np.float64) for k, v in opt.items() if v is not None})
+    if gammaUniform is not None:
+        recs["gammaUniform"] = np.array([gammaUniform], np.float64)
+    if lapSign:
+        recs["lapSign"] = np.array([lapSign], np.int32)
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.rec"), os.path.join(td, "out.rec")
+        records.write(fin, recs)
+        _fv_case(td, div)
+        env = dict(os.environ, WM_PROJECT_DIR=REF_ROOT, WM_PROJECT="OpenFOAM",
+                   WM_PROJECT_VERSION="dev", CFX_HARNESS_ROOT=td)
+        r = subprocess.run([FV_HARNESS, fin, fout], env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("fv harness failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
+        return records.read(fout)

@@ -13,6 +13,11 @@ harness).  Every fixture is produced by the reference's own code:
 * solve_*.npz  lduMatrix::solver::New(...)->solve for PCG, PBiCGStab, GAMG
                (with the agglomeration levels and coarse matrices) and
                smoothSolver with each smoother of the run-time table
+* fvm_*.npz    finiteVolume's fvm::ddt + fvm::div +/- fvm::laplacian == su
+               on a jittered hex box (oracle/fv_harness, linked against the
+               reference's libfiniteVolume): the inputs (in_*), the geometry
+               the schemes used, and the diag/upper/lower/source handed to
+               the solver
 
 Inputs are regenerated by the tests from the stored case parameters with
 openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
@@ -138,6 +143,61 @@ SOLVES = {
 }
 
 
+# fvMatrix assembly cases: psi's patch conditions on the 6 box patches
+# (0 zeroGradient, 1 fixedValue, 2 fixedGradient) and the terms of each.
+FVM_MESH = dict(nx=7, ny=6, nz=5, jitter=0.25, seed=3)
+FVM_PATCH_BC = [1, 0, 2, 1, 0, 2]
+FVM = {
+    # scalarTransportFoam: ddt + div(phi,T) - laplacian(DT,T) == su
+    "transport_upwind": dict(deltaT=0.01, div="upwind", lapSign=-1, gammaUniform=0.05, su=True),
+    "transport_linear_face_gamma": dict(deltaT=0.02, div="linear", lapSign=-1, gamma=True),
+    # pressure equation: laplacian(rAU, p) == div(phiHbyA)
+    "pressure": dict(lapSign=1, gamma=True, su=True),
+    "minus_laplacian": dict(lapSign=-1, gammaUniform=0.7),
+    # laplacianFoam: ddt(T) - laplacian(DT,T)
+    "ddt_laplacian": dict(deltaT=0.005, lapSign=-1, gammaUniform=0.3),
+    "div_only": dict(div="upwind"),
+    "ddt_div": dict(deltaT=0.01, div="linear"),
+}
+
+
+def fvm_inputs(mesh, seed=11):
+    """Seeded fields on the mesh: psi's boundary values/gradients, the old
+    value, a flux phi = Sf.U + noise, a face diffusivity and a source."""
+    rng = np.random.default_rng(seed)
+    nI, nF, nC = mesh["nInternalFaces"], mesh["nFaces"], mesh["V"].size
+    Sf = mesh["Sf"].reshape(nF, 3)
+    phi = Sf @ np.array([0.8, -0.35, 0.2]) + 0.05 * rng.uniform(-1, 1, nF) * mesh["magSf"]
+    gam = rng.uniform(0.2, 1.5, nF)
+    return dict(bcValue=rng.uniform(-2, 2, nF - nI), psi0=rng.uniform(-1, 1, nC), phi=phi[:nI], phiB=phi[nI:],
+                gamma=gam[:nI], gammaB=gam[nI:], su=rng.uniform(-3, 3, nC))
+
+
+def fvm_cases():
+    m = cases.box_mesh(**FVM_MESH)
+    inp = fvm_inputs(m)
+    nI = m["nInternalFaces"]
+    for name, spec in FVM.items():
+        kw = dict(patchBC=FVM_PATCH_BC, bcValue=inp["bcValue"], lapSign=spec.get("lapSign", 0))
+        if "deltaT" in spec:
+            kw.update(deltaT=spec["deltaT"], psi0=inp["psi0"])
+        if "div" in spec:
+            kw.update(phi=inp["phi"], phiB=inp["phiB"], div=spec["div"])
+        if spec.get("gamma"):
+            kw.update(gamma=inp["gamma"], gammaB=inp["gammaB"])
+        elif "gammaUniform" in spec:
+            kw.update(gammaUniform=spec["gammaUniform"])
+        if spec.get("su"):
+            kw.update(su=inp["su"])
+        r = ref.fvm(m, **kw)
+        out = {k: v for k, v in r.items() if not isinstance(v, str)}
+        ins = {"in_" + k: np.asarray(v) for k, v in kw.items() if k not in ("div",)}
+        ins["in_div"] = np.frombuffer(kw.get("div", "none").encode(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"fvm_{name}.npz"), l=m["owner"][:nI], u=m["neighbour"],
+                            patchStart=m["patchStart"], **ins, **out)
+        print(name, float(np.abs(out["diag"]).sum()), float(np.abs(out["source"]).sum()))
+
+
 def build(kind, params):
     return getattr(cases, kind)(**params)
 
@@ -155,6 +215,8 @@ def main():
         print("reference harness not built (python oracle/build_ref.py) or sources absent")
         return 1
     specs = {"systems": SYSTEMS, "solves": SOLVES}
+    if ref.fv_available():
+        specs["fvm"] = dict(mesh=FVM_MESH, patchBC=FVM_PATCH_BC, cases=FVM)
     with open(os.path.join(HERE, "specs.json"), "w") as fh:
         json.dump(specs, fh, indent=1, sort_keys=True)
 
@@ -184,6 +246,11 @@ def main():
         out["solverName"] = np.frombuffer(r["solverName"].encode(), np.uint8)
         np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **out)
         print(name, r["solverName"], int(r["nIterations"][0]), float(r["finalResidual"][0]))
+
+    if ref.fv_available():
+        fvm_cases()
+    else:
+        print("fv_harness not built (python oracle/build_ref_fv.py): fvm_*.npz kept")
 
     with open(os.path.join(HERE, "checksums.json"), "w") as fh:
         json.dump(sums, fh, indent=1, sort_keys=True)

@@ -8,7 +8,7 @@ GPU parity test compares against.
 import numpy as np
 import pytest
 
-from golden_cases import CHECKSUMS, SPECS, checksum, gamg_kwargs, load, solve_case, system
+from golden_cases import CHECKSUMS, SPECS, checksum, fvm_case, fvm_names, gamg_kwargs, load, solve_case, system
 from oracle import oracle as orc
 from openfoam_dev_gb300 import cases
 
@@ -131,3 +131,32 @@ def test_lu_restatement_solves_and_detects_singular_rows():
     A[7, :] = 0.0
     with pytest.raises(ValueError, match="Singular matrix"):
         orc.lu_solve(A, b)
+
+
+@pytest.mark.parametrize("name", fvm_names())
+def test_fvm_assembly_bit_exact(name):
+    """fvm::ddt + fvm::div +/- fvm::laplacian == su as the reference's
+    finiteVolume library assembles it (fixedValue, zeroGradient and
+    fixedGradient patches; upwind and linear; face and uniform diffusivity)
+    and as the oracle restates it, from the same geometry: diag, upper,
+    lower and source equal bit for bit."""
+    l, u, geom, terms, ref = fvm_case(name)
+    d, up, lo, src = orc.fvm_assemble(l, u, geom, **terms)
+    np.testing.assert_array_equal(d, ref["diag"])
+    np.testing.assert_array_equal(up, ref["upper"])
+    assert (lo is None) == (ref["lower"] is None)
+    if lo is not None:
+        np.testing.assert_array_equal(lo, ref["lower"])
+    np.testing.assert_array_equal(src, ref["source"])
+
+
+@pytest.mark.skipif(not fvm_names(), reason="no fvm fixtures")
+def test_fv_geometry_matches_surface_interpolation():
+    """cases.fv_geometry (the geometry handed to the device assembly)
+    against the reference's surfaceInterpolation and fvPatch on the same
+    mesh, bit for bit: magSf, nonOrthDeltaCoeffs, weights, V and the
+    boundary faces' cells, magSf and deltaCoeffs."""
+    _, _, geom, _, _ = fvm_case(fvm_names()[0])
+    g = cases.fv_geometry(cases.box_mesh(**SPECS["fvm"]["mesh"]))
+    for k in geom:
+        np.testing.assert_array_equal(g[k], geom[k], err_msg=k)

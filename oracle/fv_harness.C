@@ -17,7 +17,12 @@
   lduMatrix and source that fvMatrix::solveSegregated hands to the linear
   solver (diag with addBoundaryDiag, source with addBoundarySource), and the
   geometry the schemes used (magSf, nonOrthDeltaCoeffs, weights, V, the
-  patches' magSf and deltaCoeffs).
+  patches' magSf and deltaCoeffs).  With a "dict" record it then solves the
+  equation as a solver application does, fvMatrix::solve(dict) (segregated:
+  addBoundaryDiag/Source, lduMatrix::solver::New on the fvMesh, so GAMG
+  agglomerates with faceAreaPair from the mesh's own Sf), starting from psi0
+  (or zero), and writes psi, the solver performance and, for GAMG, the
+  agglomeration levels.
 \*---------------------------------------------------------------------------*/
 
 #include "Time.H"
@@ -32,6 +37,8 @@
 #include "fixedValueFvPatchFields.H"
 #include "zeroGradientFvPatchFields.H"
 #include "fixedGradientFvPatchFields.H"
+#include "GAMGAgglomeration.H"
+#include "IStringStream.H"
 #include "harness_io.H"
 
 using namespace Foam;
@@ -258,6 +265,38 @@ int runFvm(const RecMap& in, Writer& out, Time& runTime)
     out.i4("bCell", labelList(bCell));
     out.f8("magSfB", scalarField(magSfB));
     out.f8("deltaCoeffsB", scalarField(deltaCoeffsB));
+
+    if (has(in, "dict"))
+    {
+        IStringStream is(getS(in, "dict"));
+        const dictionary dict(is);
+        if (!has(in, "psi0")) T.primitiveFieldRef() = 0;
+        const solverPerformance perf = tM.ref().solve(dict);
+        out.f8("psi", T.primitiveField());
+        out.f8("initialResidual", perf.initialResidual());
+        out.f8("finalResidual", perf.finalResidual());
+        out.i4("nIterations", perf.nIterations());
+        out.i4("converged", perf.converged() ? 1 : 0);
+        out.put("solverName", "s", perf.solverName().c_str(), perf.solverName().size(), 1);
+        const objectRegistry& db = static_cast<const lduMesh&>(mesh).db();
+        if (db.foundObject<GAMGAgglomeration>(GAMGAgglomeration::typeName))
+        {
+            const GAMGAgglomeration& agg =
+                db.lookupObject<GAMGAgglomeration>(GAMGAgglomeration::typeName);
+            out.i4("nLevels", agg.size());
+            for (label i = 0; i < agg.size(); i++)
+            {
+                const std::string k = std::to_string(i);
+                out.i4("restrict" + k, agg.restrictAddressing(i));
+                out.i4("faceRestrict" + k, agg.faceRestrictAddressing(i));
+                const boolList& fl = agg.faceFlipMap(i);
+                labelList fli(fl.size());
+                forAll(fl, j) fli[j] = fl[j] ? 1 : 0;
+                out.i4("faceFlip" + k, fli);
+                out.i4("nCells" + k, agg.nCells(i));
+            }
+        }
+    }
     return 0;
 }
 

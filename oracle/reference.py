@@ -109,13 +109,15 @@ def _fv_case(td, div):
 
 
 def fvm(mesh, patchBC, bcValue, deltaT=None, psi0=None, phi=None, phiB=None, div="upwind", lapSign=0,
-        gamma=None, gammaB=None, gammaUniform=None, su=None):
+        gamma=None, gammaB=None, gammaUniform=None, su=None, solve=None):
     """The reference's fvm::ddt(T) + fvm::div(phi, T) +/- fvm::laplacian(gamma, T)
     == su on a hex mesh, each term optional (fv_harness): the diag (with
     addBoundaryDiag), upper, lower (when asymmetric) and source (with
     addBoundarySource) the solver receives, and the geometry the schemes used.
     patchBC per patch: 0 zeroGradient, 1 fixedValue, 2 fixedGradient; bcValue
-    per boundary face (value or gradient)."""
+    per boundary face (value or gradient).  With solve (a solver control
+    dict) the harness then runs fvMatrix::solve with it from psi0 (or zero)
+    and adds psi, the solver performance and GAMG's agglomeration levels."""
     recs = dict(points=mesh["points"], faces=mesh["faces"], owner=mesh["owner"], neighbour=mesh["neighbour"],
                 patchStart=mesh["patchStart"], patchBC=np.asarray(patchBC, np.int32),
                 bcValue=np.asarray(bcValue, np.float64))
@@ -127,6 +129,8 @@ def fvm(mesh, patchBC, bcValue, deltaT=None, psi0=None, phi=None, phiB=None, div
         recs["gammaUniform"] = np.array([gammaUniform], np.float64)
     if lapSign:
         recs["lapSign"] = np.array([lapSign], np.int32)
+    if solve is not None:
+        recs["dict"] = dict_text(solve)
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.rec"), os.path.join(td, "out.rec")
         records.write(fin, recs)

@@ -18,6 +18,10 @@ harness).  Every fixture is produced by the reference's own code:
                reference's libfiniteVolume): the inputs (in_*), the geometry
                the schemes used, and the diag/upper/lower/source handed to
                the solver
+* fvsolve_*.npz  fvMatrix::solve of those equations on a larger box (GAMG
+               with faceAreaPair on the fvMesh, PCG with GAMG, PCG, PBiCGStab,
+               smoothSolver): psi, the solver performance, GAMG's levels and
+               a digest of the assembled matrix
 
 Inputs are regenerated by the tests from the stored case parameters with
 openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
@@ -35,12 +39,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
+sys.path.insert(0, os.path.dirname(HERE))
 import __graft_entry__ as ge  # noqa: E402
 
 ge.load_package()
 from openfoam_dev_gb300 import cases  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 from oracle import reference as ref  # noqa: E402
+import golden_cases as gc  # noqa: E402
 
 # Case specs: (kind, params).  Shared with tests/golden_cases.py via JSON.
 SYSTEMS = {
@@ -159,36 +165,28 @@ FVM = {
     "div_only": dict(div="upwind"),
     "ddt_div": dict(deltaT=0.01, div="linear"),
 }
-
-
-def fvm_inputs(mesh, seed=11):
-    """Seeded fields on the mesh: psi's boundary values/gradients, the old
-    value, a flux phi = Sf.U + noise, a face diffusivity and a source."""
-    rng = np.random.default_rng(seed)
-    nI, nF, nC = mesh["nInternalFaces"], mesh["nFaces"], mesh["V"].size
-    Sf = mesh["Sf"].reshape(nF, 3)
-    phi = Sf @ np.array([0.8, -0.35, 0.2]) + 0.05 * rng.uniform(-1, 1, nF) * mesh["magSf"]
-    gam = rng.uniform(0.2, 1.5, nF)
-    return dict(bcValue=rng.uniform(-2, 2, nF - nI), psi0=rng.uniform(-1, 1, nC), phi=phi[:nI], phiB=phi[nI:],
-                gamma=gam[:nI], gammaB=gam[nI:], su=rng.uniform(-3, 3, nC))
+# fvMatrix::solve of some of those equations on a 14x12x10 box
+FVSOLVE = dict(mesh=dict(nx=14, ny=12, nz=10, jitter=0.25, seed=5), seed=13, patchBC=FVM_PATCH_BC, cases={
+    "pressure_gamg": ("pressure", dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-9, relTol=0.0)),
+    "pressure_gamg_dic": ("pressure", dict(solver="GAMG", smoother="DIC", nPreSweeps=1, tolerance=1e-9,
+                                           relTol=0.0)),
+    "pressure_pcg_gamg": ("pressure", dict(solver="PCG", tolerance=1e-9, relTol=0.0,
+                                           preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel"))),
+    "ddt_laplacian_pcg": ("ddt_laplacian", dict(solver="PCG", preconditioner="DIC", tolerance=1e-10,
+                                                relTol=0.0)),
+    "transport_pbicgstab": ("transport_upwind", dict(solver="PBiCGStab", preconditioner="DILU",
+                                                     tolerance=1e-10, relTol=0.0)),
+    "transport_smooth": ("transport_upwind", dict(solver="smoothSolver", smoother="symGaussSeidel",
+                                                  tolerance=1e-9, relTol=0.0)),
+})
 
 
 def fvm_cases():
     m = cases.box_mesh(**FVM_MESH)
-    inp = fvm_inputs(m)
+    inp = gc.fvm_inputs(m)
     nI = m["nInternalFaces"]
     for name, spec in FVM.items():
-        kw = dict(patchBC=FVM_PATCH_BC, bcValue=inp["bcValue"], lapSign=spec.get("lapSign", 0))
-        if "deltaT" in spec:
-            kw.update(deltaT=spec["deltaT"], psi0=inp["psi0"])
-        if "div" in spec:
-            kw.update(phi=inp["phi"], phiB=inp["phiB"], div=spec["div"])
-        if spec.get("gamma"):
-            kw.update(gamma=inp["gamma"], gammaB=inp["gammaB"])
-        elif "gammaUniform" in spec:
-            kw.update(gammaUniform=spec["gammaUniform"])
-        if spec.get("su"):
-            kw.update(su=inp["su"])
+        kw = gc.fvm_ref_kwargs(spec, inp, FVM_PATCH_BC)
         r = ref.fvm(m, **kw)
         out = {k: v for k, v in r.items() if not isinstance(v, str)}
         ins = {"in_" + k: np.asarray(v) for k, v in kw.items() if k not in ("div",)}
@@ -196,6 +194,26 @@ def fvm_cases():
         np.savez_compressed(os.path.join(HERE, f"fvm_{name}.npz"), l=m["owner"][:nI], u=m["neighbour"],
                             patchStart=m["patchStart"], **ins, **out)
         print(name, float(np.abs(out["diag"]).sum()), float(np.abs(out["source"]).sum()))
+
+
+def fvsolve_cases():
+    """The equation assembled and solved by fvMatrix::solve on a larger
+    jittered box: psi, the solver performance and GAMG's levels (faceAreaPair
+    on the fvMesh's own Sf); the assembled matrix is kept as a digest."""
+    m = cases.box_mesh(**FVSOLVE["mesh"])
+    inp = gc.fvm_inputs(m, seed=FVSOLVE["seed"])
+    for name, (eq, ctl) in FVSOLVE["cases"].items():
+        kw = gc.fvm_ref_kwargs(FVM[eq], inp, FVSOLVE["patchBC"])
+        r = ref.fvm(m, solve=ctl, **kw)
+        out = {k: v for k, v in r.items() if not isinstance(v, str)}
+        for k in ("diag", "upper", "lower", "source", "magSf", "deltaCoeffs", "weights", "V", "bCell", "magSfB",
+                  "deltaCoeffsB"):
+            out.pop(k, None)
+        out["matrixDigest"] = np.frombuffer(gc.matrix_digest(r["diag"], r["upper"], r.get("lower"),
+                                                             r["source"]).encode(), np.uint8)
+        out["solverName"] = np.frombuffer(r["solverName"].encode(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"fvsolve_{name}.npz"), **out)
+        print(name, r["solverName"], int(r["nIterations"][0]), float(r["finalResidual"][0]))
 
 
 def build(kind, params):
@@ -217,6 +235,7 @@ def main():
     specs = {"systems": SYSTEMS, "solves": SOLVES}
     if ref.fv_available():
         specs["fvm"] = dict(mesh=FVM_MESH, patchBC=FVM_PATCH_BC, cases=FVM)
+        specs["fvsolve"] = FVSOLVE
     with open(os.path.join(HERE, "specs.json"), "w") as fh:
         json.dump(specs, fh, indent=1, sort_keys=True)
 
@@ -249,6 +268,7 @@ def main():
 
     if ref.fv_available():
         fvm_cases()
+        fvsolve_cases()
     else:
         print("fv_harness not built (python oracle/build_ref_fv.py): fvm_*.npz kept")
 

@@ -75,3 +75,76 @@ def fvm_case(name):
         terms["gamma"] = float(g["in_gammaUniform"])
     ref = dict(diag=g["diag"], upper=g["upper"], lower=g.get("lower"), source=g["source"])
     return g["l"], g["u"], geom, terms, ref
+
+
+def fvm_inputs(mesh, seed=11):
+    """Seeded fields on the mesh: psi's boundary values/gradients, the old
+    value, a flux phi = Sf.U + noise, a face diffusivity and a source."""
+    rng = np.random.default_rng(seed)
+    nI, nF, nC = mesh["nInternalFaces"], mesh["nFaces"], mesh["V"].size
+    Sf = mesh["Sf"].reshape(nF, 3)
+    phi = Sf @ np.array([0.8, -0.35, 0.2]) + 0.05 * rng.uniform(-1, 1, nF) * mesh["magSf"]
+    gam = rng.uniform(0.2, 1.5, nF)
+    return dict(bcValue=rng.uniform(-2, 2, nF - nI), psi0=rng.uniform(-1, 1, nC), phi=phi[:nI], phiB=phi[nI:],
+                gamma=gam[:nI], gammaB=gam[nI:], su=rng.uniform(-3, 3, nC))
+
+
+def fvm_ref_kwargs(spec, inp, patchBC):
+    """An equation spec's arguments to the reference harness (oracle.reference.fvm)."""
+    kw = dict(patchBC=patchBC, bcValue=inp["bcValue"], lapSign=spec.get("lapSign", 0))
+    if "deltaT" in spec:
+        kw.update(deltaT=spec["deltaT"], psi0=inp["psi0"])
+    if "div" in spec:
+        kw.update(phi=inp["phi"], phiB=inp["phiB"], div=spec["div"])
+    if spec.get("gamma"):
+        kw.update(gamma=inp["gamma"], gammaB=inp["gammaB"])
+    elif "gammaUniform" in spec:
+        kw.update(gammaUniform=spec["gammaUniform"])
+    if spec.get("su"):
+        kw.update(su=inp["su"])
+    return kw
+
+
+def fvm_terms(spec, inp, bcType):
+    """The same equation in the oracle's / device's assembly arguments."""
+    t = dict(rDeltaT=1.0 / spec["deltaT"] if "deltaT" in spec else 0.0, div=spec.get("div", "upwind"),
+             lapSign=spec.get("lapSign", 0), bcType=bcType, bcValue=inp["bcValue"])
+    if "deltaT" in spec:
+        t["psi0"] = inp["psi0"]
+    if "div" in spec:
+        t.update(phi=inp["phi"], phiB=inp["phiB"])
+    if spec.get("gamma"):
+        t.update(gamma=inp["gamma"], gammaB=inp["gammaB"])
+    elif "gammaUniform" in spec:
+        t["gamma"] = spec["gammaUniform"]
+    if spec.get("su"):
+        t["su"] = inp["su"]
+    return t
+
+
+def matrix_digest(diag, upper, lower, source):
+    h = hashlib.sha256()
+    for a in (diag, upper, lower, source):
+        if a is not None:
+            h.update(np.ascontiguousarray(a, np.float64).tobytes())
+    return h.hexdigest()
+
+
+def fvsolve_names():
+    return sorted(f[8:-4] for f in os.listdir(GOLDEN) if f.startswith("fvsolve_") and f.endswith(".npz"))
+
+
+def fvsolve_case(name):
+    """One fvMatrix::solve fixture: (mesh, the equation's assembly terms,
+    the solver controls, the reference's results)."""
+    spec = SPECS["fvsolve"]
+    eq, ctl = spec["cases"][name]
+    m = cases.box_mesh(**spec["mesh"])
+    nI = m["nInternalFaces"]
+    inp = fvm_inputs(m, seed=spec["seed"])
+    bcType = np.repeat(np.asarray(spec["patchBC"], np.int32), np.diff(m["patchStart"])).astype(np.int32)
+    g = load(f"fvsolve_{name}.npz")
+    g["solverName"] = bytes(g["solverName"]).decode()
+    g["matrixDigest"] = bytes(g["matrixDigest"]).decode()
+    m["Sf_internal"] = m["Sf"][: 3 * nI].reshape(nI, 3).copy()
+    return m, fvm_terms(SPECS["fvm"]["cases"][eq], inp, bcType), dict(ctl), g

@@ -8,14 +8,10 @@ PISO/PIMPLE step assembles, on a jittered mesh with fixedValue,
 zeroGradient and fixedGradient patches.  Re-assembly with new fluxes
 replaces the resident coefficients (no stale packs), and an assembled
 system solves to the same answer as the same system uploaded from the host.
-The fixtures written by the reference's own finiteVolume library
-(tests/golden/fvm_*.npz) are reproduced bit for bit from the geometry the
-reference's schemes used.
 """
 import numpy as np
 import pytest
 
-from golden_cases import fvm_case, fvm_names
 from oracle import oracle as orc
 from openfoam_dev_gb300 import cases, ldu
 
@@ -95,27 +91,6 @@ def test_assembly_bit_exact_against_the_oracle(name):
     if lo is not None:
         np.testing.assert_array_equal(got_l, lo)
     np.testing.assert_array_equal(source.cpu().numpy(), src)
-
-
-@pytest.mark.parametrize("name", fvm_names())
-def test_assembly_bit_exact_against_the_reference_fixtures(name):
-    l, u, geom, terms, ref = fvm_case(name)
-    n = geom["V"].size
-    mesh = ldu.LduMesh(ldu.default_context(), n, l, u)
-    mesh.fv_geometry(geom["magSf"], geom["deltaCoeffs"], geom["V"], geom["bCell"], geom["magSfB"],
-                     geom["deltaCoeffsB"], weights=geom["weights"])
-    A = ldu.LduMatrix.empty(mesh, symmetric=ref["lower"] is None)
-    source = torch.empty(n, dtype=torch.float64, device="cuda")
-    kw = {k: (_dev(v, torch.int32 if k == "bcType" else torch.float64) if isinstance(v, np.ndarray) else v)
-          for k, v in terms.items()}
-    A.assemble(source, **kw)
-    torch.cuda.synchronize()
-    got_d, got_u, got_l = A.coarse(0, n, l.size)
-    np.testing.assert_array_equal(got_d, ref["diag"])
-    np.testing.assert_array_equal(got_u, ref["upper"])
-    if ref["lower"] is not None:
-        np.testing.assert_array_equal(got_l, ref["lower"])
-    np.testing.assert_array_equal(source.cpu().numpy(), ref["source"])
 
 
 def test_reassembly_replaces_coefficients_and_solves_like_an_upload():

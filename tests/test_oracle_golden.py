@@ -8,7 +8,8 @@ GPU parity test compares against.
 import numpy as np
 import pytest
 
-from golden_cases import CHECKSUMS, SPECS, checksum, fvm_case, fvm_names, gamg_kwargs, load, solve_case, system
+from golden_cases import (CHECKSUMS, SPECS, checksum, fvm_case, fvm_names, fvsolve_case, fvsolve_names, gamg_kwargs,
+                          load, matrix_digest, solve_case, system)
 from oracle import oracle as orc
 from openfoam_dev_gb300 import cases
 
@@ -64,8 +65,8 @@ def test_single_operations(name):
         np.testing.assert_array_equal(m.smooth(sm, x, b, 2), g[f"{sm}_smooth2"], err_msg=sm)
 
 
-def _run_oracle(s, ctl):
-    psi = np.zeros_like(s["source"])
+def _run_oracle(s, ctl, psi0=None):
+    psi = np.zeros_like(s["source"]) if psi0 is None else np.array(psi0, np.float64)
     kw = dict(tol=ctl.get("tolerance", 1e-6), rel_tol=ctl.get("relTol", 0.0), max_iter=ctl.get("maxIter", 1000),
               min_iter=ctl.get("minIter", 0))
     pre = ctl.get("preconditioner")
@@ -160,3 +161,40 @@ def test_fv_geometry_matches_surface_interpolation():
     g = cases.fv_geometry(cases.box_mesh(**SPECS["fvm"]["mesh"]))
     for k in geom:
         np.testing.assert_array_equal(g[k], geom[k], err_msg=k)
+
+
+def _fvsolve_system(name):
+    m, terms, ctl, g = fvsolve_case(name)
+    nI = m["nInternalFaces"]
+    d, up, lo, src = orc.fvm_assemble(m["owner"][:nI], m["neighbour"], cases.fv_geometry(m), **terms)
+    s = dict(l=m["owner"][:nI], u=m["neighbour"], diag=d, upper=up, lower=lo, source=src, Sf=m["Sf_internal"])
+    return s, terms, ctl, g
+
+
+@pytest.mark.parametrize("name", fvsolve_names())
+def test_fvmatrix_solve_bit_exact(name):
+    """The equation as a solver application solves it (fvMatrix::solve on
+    the fvMesh, GAMG agglomerating with faceAreaPair from the mesh's own Sf):
+    the oracle's assembly from cases.fv_geometry gives the reference's
+    matrix (digest), its faceAreaPair levels and its solve give the
+    reference's psi, iteration count and residuals bit for bit."""
+    s, terms, ctl, g = _fvsolve_system(name)
+    assert matrix_digest(s["diag"], s["upper"], s["lower"], s["source"]) == g["matrixDigest"]
+    if "nLevels" in g:
+        pre = ctl.get("preconditioner")
+        gctl = pre if isinstance(pre, dict) else ctl
+        agg = orc.Agglomeration(s, n_coarsest=gctl.get("nCellsInCoarsestLevel", 10))
+        assert agg.n_levels == g["nLevels"][0]
+        for i in range(agg.n_levels):
+            ra, fra, flip, nc, _, _, _ = agg.level(i)
+            np.testing.assert_array_equal(ra, g[f"restrict{i}"])
+            np.testing.assert_array_equal(fra, g[f"faceRestrict{i}"])
+            np.testing.assert_array_equal(flip, g[f"faceFlip{i}"])
+            assert nc == g[f"nCells{i}"][0]
+    start = terms.get("psi0")
+    psi, p = _run_oracle(s, ctl, psi0=start)
+    np.testing.assert_array_equal(psi, g["psi"])
+    assert p.nIterations == g["nIterations"][0]
+    assert p.initialResidual == g["initialResidual"][0]
+    assert p.finalResidual == g["finalResidual"][0]
+    assert p.converged == bool(g["converged"][0])

@@ -71,8 +71,10 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
-def box_mesh(nx, ny, nz, L=(1.0, 1.0, 1.0), jitter=0.0, seed=0):
-    """Hex box mesh with OpenFOAM face geometry (points, faces, owner, ...)."""
+def box_mesh(nx, ny, nz, L=(1.0, 1.0, 1.0), jitter=0.0, seed=0, periodic_x=False):
+    """Hex box mesh with OpenFOAM face geometry (points, faces, owner, ...).
+    periodic_x: the xmax plane's points take the y, z of the xmin plane's, so
+    the two patches are translations of each other (a cyclic pair)."""
     L_ = lib()
     c = [ctypes.c_int64() for _ in range(4)]
     _chk(L_.cfxc_box_counts(nx, ny, nz, *[ctypes.byref(x) for x in c]), "box_counts")
@@ -80,6 +82,9 @@ def box_mesh(nx, ny, nz, L=(1.0, 1.0, 1.0), jitter=0.0, seed=0):
     nF = nI + nB
     pts = np.empty(3 * nP)
     _chk(L_.cfxc_box_points(nx, ny, nz, L[0], L[1], L[2], jitter, seed, pts), "box_points")
+    if periodic_x:
+        P = pts.reshape(nz + 1, ny + 1, nx + 1, 3)
+        P[:, :, nx, 1:] = P[:, :, 0, 1:]
     faces = np.empty(4 * nF, np.int32)
     owner = np.empty(nF, np.int32)
     nei = np.empty(max(nI, 1), np.int32)

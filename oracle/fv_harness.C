@@ -7,7 +7,8 @@
   (harness_io.H) describing a hex mesh (points, faces, owner, neighbour,
   patchStart), psi's boundary condition per patch (patchBC: 0 zeroGradient,
   1 fixedValue, 2 fixedGradient, with bcValue per boundary face: the value
-  or the gradient), the fields and the terms, builds an fvMesh and
+  or the gradient; 3 cyclic, patches 2i and 2i+1 coupled face by face), the
+  fields and the terms, builds an fvMesh and
   volScalarField T in the case directory (whose system/fvSchemes selects
   Euler, Gauss upwind or linear, Gauss linear uncorrected), assembles
 
@@ -15,7 +16,10 @@
 
   with each term optional, as a solver application writes it, and writes the
   lduMatrix and source that fvMatrix::solveSegregated hands to the linear
-  solver (diag with addBoundaryDiag, source with addBoundarySource), and the
+  solver (diag with addBoundaryDiag, source with addBoundarySource without
+  the coupled patches), the cyclic patches' interfaces (face cells, the
+  partner's face cells, boundaryCoeffs and internalCoeffs, which the solver
+  receives as interfaceBouCoeffs and interfaceIntCoeffs), and the
   geometry the schemes used (magSf, nonOrthDeltaCoeffs, weights, V, the
   patches' magSf and deltaCoeffs).  With a "dict" record it then solves the
   equation as a solver application does, fvMatrix::solve(dict) (segregated:
@@ -37,6 +41,8 @@
 #include "fixedValueFvPatchFields.H"
 #include "zeroGradientFvPatchFields.H"
 #include "fixedGradientFvPatchFields.H"
+#include "cyclicPolyPatch.H"
+#include "cyclicFvPatchFields.H"
 #include "GAMGAgglomeration.H"
 #include "IStringStream.H"
 #include "harness_io.H"
@@ -110,13 +116,25 @@ int runFvm(const RecMap& in, Writer& out, Time& runTime)
     List<polyPatch*> patches(ps.size() - 1);
     forAll(patches, p)
     {
-        patches[p] = new polyPatch
-        (
-            "patch" + Foam::name(p), ps[p+1] - ps[p], ps[p], p,
-            static_cast<const polyMesh&>(mesh).boundary()
-        );
+        if (patchBC[p] == 3)
+        {
+            patches[p] = new cyclicPolyPatch
+            (
+                "patch" + Foam::name(p), ps[p+1] - ps[p], ps[p], p,
+                static_cast<const polyMesh&>(mesh).boundary(),
+                "patch" + Foam::name(p % 2 ? p - 1 : p + 1)
+            );
+        }
+        else
+        {
+            patches[p] = new polyPatch
+            (
+                "patch" + Foam::name(p), ps[p+1] - ps[p], ps[p], p,
+                static_cast<const polyMesh&>(mesh).boundary()
+            );
+        }
     }
-    mesh.addFvPatches(patches, false);
+    mesh.addFvPatches(patches, true);
     const label nI = mesh.nInternalFaces();
 
     // psi with its boundary conditions and old-time value (fixedGradient
@@ -126,8 +144,8 @@ int runFvm(const RecMap& in, Writer& out, Time& runTime)
     forAll(types, p)
     {
         types[p] =
-            patchBC[p] == 1
-          ? fixedValueFvPatchScalarField::typeName
+            patchBC[p] == 1 ? fixedValueFvPatchScalarField::typeName
+          : patchBC[p] == 3 ? cyclicFvPatchScalarField::typeName
           : zeroGradientFvPatchScalarField::typeName;
     }
     volScalarField T
@@ -235,11 +253,39 @@ int runFvm(const RecMap& in, Writer& out, Time& runTime)
     scalarField diag(M.diag());
     (M.*get(fvmAddBoundaryDiag()))(diag, 0);
     scalarField source(M.source());
-    (M.*get(fvmAddBoundarySource()))(source, true);
+    (M.*get(fvmAddBoundarySource()))(source, false);
     out.f8("diag", diag);
     out.f8("upper", M.upper());
     if (M.hasLower()) out.f8("lower", M.lower());
     out.f8("source", source);
+    {
+        fvScalarMatrix& Mw = tM.ref();  // the coefficient accessors are non-const
+        DynamicList<label> ifSize, ifCell, ifNbr;
+        DynamicList<scalar> ifBou, ifInt;
+        forAll(mesh.boundary(), p)
+        {
+            if (patchBC[p] != 3) continue;
+            const labelUList& fc = mesh.boundary()[p].faceCells();
+            const labelUList& nc =
+                mesh.boundary()[p % 2 ? p - 1 : p + 1].faceCells();
+            ifSize.append(fc.size());
+            forAll(fc, k)
+            {
+                ifCell.append(fc[k]);
+                ifNbr.append(nc[k]);
+                ifBou.append(Mw.boundaryCoeffs()[p][k]);
+                ifInt.append(Mw.internalCoeffs()[p][k]);
+            }
+        }
+        if (ifSize.size())
+        {
+            out.i4("ifSize", labelList(ifSize));
+            out.i4("ifCell", labelList(ifCell));
+            out.i4("ifNbr", labelList(ifNbr));
+            out.f8("ifBou", scalarField(ifBou));
+            out.f8("ifInt", scalarField(ifInt));
+        }
+    }
 
     // the geometry the schemes used
     out.f8("magSf", mesh.magSf().primitiveField());

@@ -22,6 +22,9 @@ harness).  Every fixture is produced by the reference's own code:
                with faceAreaPair on the fvMesh, PCG with GAMG, PCG, PBiCGStab,
                smoothSolver): psi, the solver performance, GAMG's levels and
                a digest of the assembled matrix
+* fvcyc_*.npz  fvMatrix::solve with a cyclic patch pair (the reference's own
+               cyclicPolyPatch / cyclicFvPatchField, GAMG's cyclicGAMGInterface):
+               the lduMatrix and interfaces the solver received and its results
 
 Inputs are regenerated by the tests from the stored case parameters with
 openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
@@ -216,6 +219,41 @@ def fvsolve_cases():
         print(name, r["solverName"], int(r["nIterations"][0]), float(r["finalResidual"][0]))
 
 
+# fvMatrix::solve with a cyclic pair (x periodic, patches 0 and 1) on a box
+# whose xmin and xmax points match: the lduMatrix, the interfaces and the
+# reference's solve (psi, performance, GAMG levels)
+FVCYC = dict(mesh=dict(nx=10, ny=9, nz=8, jitter=0.25, seed=4, periodic_x=True), seed=21,
+             patchBC=[3, 3, 1, 0, 2, 0], cases={
+    "laplacian_pcg": (dict(lapSign=-1, gammaUniform=0.6, su=True),
+                      dict(solver="PCG", preconditioner="DIC", tolerance=1e-10, relTol=0.0)),
+    "laplacian_gamg": (dict(lapSign=-1, gammaUniform=0.6, su=True),
+                       dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-9, relTol=0.0)),
+    "laplacian_gamg_dic": (dict(lapSign=-1, gammaUniform=0.6, su=True),
+                           dict(solver="GAMG", smoother="DIC", nPreSweeps=1, tolerance=1e-9, relTol=0.0)),
+    "transport_pbicgstab": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
+                            dict(solver="PBiCGStab", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
+    "transport_pbicg": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
+                        dict(solver="PBiCG", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
+    "transport_smooth": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
+                         dict(solver="smoothSolver", smoother="symGaussSeidel", tolerance=1e-9, relTol=0.0)),
+})
+
+
+def fvcyc_cases():
+    m = cases.box_mesh(**FVCYC["mesh"])
+    inp = gc.fvcyc_inputs(m, FVCYC["seed"])
+    nI = m["nInternalFaces"]
+    for name, (eq, ctl) in FVCYC["cases"].items():
+        kw = gc.fvm_ref_kwargs(eq, inp, FVCYC["patchBC"])
+        r = ref.fvm(m, solve=ctl, **kw)
+        out = {k: v for k, v in r.items() if not isinstance(v, str)}
+        for k in ("magSf", "deltaCoeffs", "weights", "V", "bCell", "magSfB", "deltaCoeffsB"):
+            out.pop(k, None)
+        out["solverName"] = np.frombuffer(r["solverName"].encode(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"fvcyc_{name}.npz"), l=m["owner"][:nI], u=m["neighbour"], **out)
+        print(name, r["solverName"], int(r["nIterations"][0]), float(r["finalResidual"][0]))
+
+
 def build(kind, params):
     return getattr(cases, kind)(**params)
 
@@ -236,6 +274,7 @@ def main():
     if ref.fv_available():
         specs["fvm"] = dict(mesh=FVM_MESH, patchBC=FVM_PATCH_BC, cases=FVM)
         specs["fvsolve"] = FVSOLVE
+        specs["fvcyc"] = FVCYC
     with open(os.path.join(HERE, "specs.json"), "w") as fh:
         json.dump(specs, fh, indent=1, sort_keys=True)
 
@@ -269,6 +308,7 @@ def main():
     if ref.fv_available():
         fvm_cases()
         fvsolve_cases()
+        fvcyc_cases()
     else:
         print("fv_harness not built (python oracle/build_ref_fv.py): fvm_*.npz kept")
 

@@ -148,3 +148,36 @@ def fvsolve_case(name):
     g["matrixDigest"] = bytes(g["matrixDigest"]).decode()
     m["Sf_internal"] = m["Sf"][: 3 * nI].reshape(nI, 3).copy()
     return m, fvm_terms(SPECS["fvm"]["cases"][eq], inp, bcType), dict(ctl), g
+
+
+def fvcyc_inputs(mesh, seed):
+    """fvm_inputs with the cyclic pair's face values made periodic: the flux
+    through an xmax face is minus that through its xmin partner, and both
+    carry the same diffusivity."""
+    inp = fvm_inputs(mesh, seed=seed)
+    nI, ps = mesh["nInternalFaces"], mesh["patchStart"]
+    a = slice(ps[0] - nI, ps[1] - nI)
+    b = slice(ps[1] - nI, ps[2] - nI)
+    inp["phiB"][b] = -inp["phiB"][a]
+    inp["gammaB"][b] = inp["gammaB"][a]
+    return inp
+
+
+def fvcyc_names():
+    return sorted(f[6:-4] for f in os.listdir(GOLDEN) if f.startswith("fvcyc_") and f.endswith(".npz"))
+
+
+def fvcyc_case(name):
+    """(the lduMatrix system with its cyclic interfaces as the solver
+    received it, the starting psi, the solver controls, the reference's
+    results)."""
+    eq, ctl = SPECS["fvcyc"]["cases"][name]
+    g = load(f"fvcyc_{name}.npz")
+    g["solverName"] = bytes(g["solverName"]).decode()
+    s = dict(l=g["l"], u=g["u"], diag=g["diag"], upper=g["upper"], lower=g.get("lower"), source=g["source"],
+             ifSize=g["ifSize"], ifCell=g["ifCell"], ifNbr=g["ifNbr"], ifBou=g["ifBou"], ifInt=g["ifInt"])
+    psi0 = None
+    if "deltaT" in eq:
+        m = cases.box_mesh(**SPECS["fvcyc"]["mesh"])
+        psi0 = fvcyc_inputs(m, SPECS["fvcyc"]["seed"])["psi0"]
+    return s, psi0, dict(ctl), g

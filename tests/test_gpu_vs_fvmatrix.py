@@ -14,11 +14,15 @@ The fixtures come from the reference's own finiteVolume library
   bit) gives the same matrix (digest); solving it gives the solution within
   relative L2 1e-10 and the iteration count within +-1 (PBiCGStab: within
   10 % and 4; its per-iteration reductions are summed in another order).
+* fvcyc_*.npz: fvMatrix::solve on an x-periodic box with the reference's
+  own cyclic patches.  The lduMatrix and interfaces the reference's solver
+  received, solved through the plugin solvers with coupled interfaces, give
+  the reference's psi within the same bounds.
 """
 import numpy as np
 import pytest
 
-from golden_cases import fvm_case, fvm_names, fvsolve_case, fvsolve_names, matrix_digest
+from golden_cases import SPECS, fvcyc_case, fvcyc_names, fvm_case, fvm_names, fvsolve_case, fvsolve_names, matrix_digest
 from oracle import oracle as orc
 from openfoam_dev_gb300 import cases, ldu
 
@@ -26,7 +30,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 _PLUGIN_NAMES = {"PCG": "cudaPCG", "PBiCGStab": "cudaPBiCGStab", "GAMG": "cudaGAMG",
-                 "smoothSolver": "cudaSmoothSolver"}
+                 "smoothSolver": "cudaSmoothSolver", "PBiCG": "cudaPBiCG"}
 
 
 def _dev(a, dtype=torch.float64):
@@ -102,3 +106,31 @@ def test_assemble_and_solve_match_fvmatrix_solve(name):
         nf = om.norm_factor(start, b)
         assert np.abs(om.residual(x, b)).sum() / nf < 1.5 * ctl["tolerance"]
         assert rel <= 1e-6, rel
+
+
+def _check_against(perf, x, g, ctl, om, b, start):
+    ref_it = int(g["nIterations"][0])
+    assert perf.solverName == g["solverName"]
+    assert perf.converged == bool(g["converged"][0])
+    assert perf.initialResidual == pytest.approx(float(g["initialResidual"][0]), rel=1e-12)
+    rel = float(np.linalg.norm(x - g["psi"]) / np.linalg.norm(g["psi"]))
+    krylov_bicg = ctl["solver"] in ("PBiCGStab", "PBiCG")
+    if krylov_bicg:
+        assert abs(perf.nIterations - ref_it) <= max(4, ref_it // 10), (perf, ref_it)
+    else:
+        assert abs(perf.nIterations - ref_it) <= 1, (perf, ref_it)
+    if perf.nIterations == ref_it and not krylov_bicg:
+        assert rel <= 1e-10, rel
+    else:
+        r = om.residual(x, b)
+        assert np.abs(r).sum() / om.norm_factor(start, b) < 1.5 * ctl["tolerance"]
+        assert rel <= 1e-6, rel
+
+
+@pytest.mark.parametrize("name", [n for n in fvcyc_names() if SPECS["fvcyc"]["cases"][n][1]["solver"] != "GAMG"])
+def test_cyclic_solve_matches_fvmatrix_solve(name):
+    s, psi0, ctl, g = fvcyc_case(name)
+    start = np.zeros_like(s["source"]) if psi0 is None else np.array(psi0)
+    x = start.copy()
+    perf = ldu.solve(s, x, dict(ctl, solver=_PLUGIN_NAMES[ctl["solver"]]))
+    _check_against(perf, x, g, ctl, orc.Matrix(s), s["source"], start)

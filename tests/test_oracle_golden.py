@@ -8,8 +8,8 @@ GPU parity test compares against.
 import numpy as np
 import pytest
 
-from golden_cases import (CHECKSUMS, SPECS, checksum, fvm_case, fvm_names, fvsolve_case, fvsolve_names, gamg_kwargs,
-                          load, matrix_digest, solve_case, system)
+from golden_cases import (CHECKSUMS, SPECS, checksum, fvcyc_case, fvcyc_names, fvm_case, fvm_names, fvsolve_case,
+                          fvsolve_names, gamg_kwargs, load, matrix_digest, solve_case, system)
 from oracle import oracle as orc
 from openfoam_dev_gb300 import cases
 
@@ -193,6 +193,22 @@ def test_fvmatrix_solve_bit_exact(name):
             assert nc == g[f"nCells{i}"][0]
     start = terms.get("psi0")
     psi, p = _run_oracle(s, ctl, psi0=start)
+    np.testing.assert_array_equal(psi, g["psi"])
+    assert p.nIterations == g["nIterations"][0]
+    assert p.initialResidual == g["initialResidual"][0]
+    assert p.finalResidual == g["finalResidual"][0]
+    assert p.converged == bool(g["converged"][0])
+
+
+@pytest.mark.parametrize("name", [n for n in fvcyc_names() if SPECS["fvcyc"]["cases"][n][1]["solver"] != "GAMG"])
+def test_cyclic_fvmatrix_solve_bit_exact(name):
+    """The reference's own cyclicPolyPatch / cyclicFvPatchField on an
+    x-periodic box: from the lduMatrix and interfaces its fvMatrix handed to
+    the solver (interfaceBouCoeffs = boundaryCoeffs, interfaceIntCoeffs =
+    internalCoeffs), the oracle's PCG, PBiCGStab, PBiCG and smoothSolver
+    reproduce psi, iterations and residuals bit for bit."""
+    s, psi0, ctl, g = fvcyc_case(name)
+    psi, p = _run_oracle(s, ctl, psi0=psi0)
     np.testing.assert_array_equal(psi, g["psi"])
     assert p.nIterations == g["nIterations"][0]
     assert p.initialResidual == g["initialResidual"][0]

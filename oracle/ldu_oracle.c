@@ -917,7 +917,57 @@ typedef struct {
     double* upper;
     double* lower;
     double* rD; /* DIC smoother */
+    /* the level's coupled interfaces (cyclicGAMGInterface) */
+    int *ifCell, *ifNbr, *ifPatchSize;
+    double *ifBou, *ifInt;
 } level_matrix;
+
+/* Coarse cyclic interfaces of one GAMG level from the finer level's and its
+ * restriction map R: cyclicGAMGInterface's constructor
+ * (cyclicGAMGInterface.C:87-151) groups each patch's faces by the pair
+ * (coarse cell, coarse neighbour cell) in order of first appearance, the
+ * neighbour cells coming from the partner patch (internalFieldTransfer of
+ * the restrict map, cyclicGAMGInterface.C:172-189: the same pair read from
+ * the other side); the coefficients are summed over each coarse face's fine
+ * faces in face order (GAMGSolverAgglomerateMatrix.C:196-268 restrictField,
+ * GAMGInterface.C:90-115). */
+static void coarse_interfaces(const ldu_matrix* fine, const int* R, level_matrix* L) {
+    const int nIf = fine->nIf;
+    const int nP = fine->nIfPatch > 0 ? fine->nIfPatch : 1;
+    L->ifCell = (int*)xmalloc(sizeof(int) * nIf);
+    L->ifNbr = (int*)xmalloc(sizeof(int) * nIf);
+    L->ifBou = (double*)xmalloc(sizeof(double) * nIf);
+    L->ifInt = (double*)xmalloc(sizeof(double) * nIf);
+    L->ifPatchSize = (int*)xmalloc(sizeof(int) * nP);
+    int off = 0, nc = 0;
+    for (int p = 0; p < nP; ++p) {
+        const int np = fine->nIfPatch > 0 ? fine->ifPatchSize[p] : nIf;
+        const int c0 = nc;
+        for (int k = off; k < off + np; ++k) {
+            const int a = R[fine->ifCell[k]], b = R[fine->ifNbr[k]];
+            int j = c0;
+            while (j < nc && !(L->ifCell[j] == a && L->ifNbr[j] == b)) ++j;
+            if (j == nc) {
+                L->ifCell[nc] = a;
+                L->ifNbr[nc] = b;
+                L->ifBou[nc] = 0.0;
+                L->ifInt[nc] = 0.0;
+                ++nc;
+            }
+            L->ifBou[j] += fine->ifBou[k];
+            L->ifInt[j] += fine->ifInt ? fine->ifInt[k] : fine->ifBou[k];
+        }
+        L->ifPatchSize[p] = nc - c0;
+        off += np;
+    }
+    L->m.nIf = nc;
+    L->m.ifCell = L->ifCell;
+    L->m.ifNbr = L->ifNbr;
+    L->m.ifBou = L->ifBou;
+    L->m.ifInt = L->ifInt;
+    L->m.nIfPatch = nP;
+    L->m.ifPatchSize = L->ifPatchSize;
+}
 
 /* GAMG's smoother on one level (any smoother of the table; rD as smoother_rD) */
 static void smooth(const ldu_matrix* m, const double* rD, int kind, double* psi, const double* b, int n) {
@@ -1077,6 +1127,7 @@ static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeratio
         L->m.diag = L->diag;
         L->m.upper = L->upper;
         L->m.lower = L->lower;
+        if (fine->nIf) coarse_interfaces(fine, agg->restrictAddr[i], L);
         ldu_init_addr(&L->m);
         fine = &L->m;
     }
@@ -1110,6 +1161,11 @@ static void gamg_free(gamg_hier* H) {
         free(H->lv[i].diag);
         free(H->lv[i].upper);
         free(H->lv[i].lower);
+        free(H->lv[i].ifCell);
+        free(H->lv[i].ifNbr);
+        free(H->lv[i].ifPatchSize);
+        free(H->lv[i].ifBou);
+        free(H->lv[i].ifInt);
         ldu_free_addr(&H->lv[i].m);
     }
     free(H->corr);
@@ -1134,6 +1190,8 @@ static void gamg_interpolate(const ldu_matrix* m, double* psi, double* Apsi, con
         Apsi[m->u[f]] += lower[f] * psi[m->l[f]];
         Apsi[m->l[f]] += m->upper[f] * psi[m->u[f]];
     }
+    /* the interfaces' updateMatrixInterfaces (GAMGSolverInterpolate.C:60-67) */
+    update_interfaces(m, m->ifBou, 0, psi, Apsi);
     for (int c = 0; c < n; ++c) psi[c] = -Apsi[c] / m->diag[c];
     double* corrC = (double*)calloc(nCC ? nCC : 1, sizeof(double));
     double* diagC = (double*)calloc(nCC ? nCC : 1, sizeof(double));
@@ -1216,11 +1274,14 @@ static void gamg_vcycle(gamg_hier* H, double* psi, const double* b, double* Apsi
 }
 
 /* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
- * GAMGSolverSolve.C:31-552 (no interfaces). */
+ * GAMGSolverSolve.C:31-552, with the coupled interfaces agglomerated level
+ * by level (coarse_interfaces).  directSolveCoarsest with interfaces is not
+ * restated (returns -3). */
 int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
              const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
     const int n = m->nCells;
     if (agg->nLevels < 1) return -1;
+    if (m->nIf && gc->directSolveCoarsest) return -3;
     memset(perf, 0, sizeof(*perf));
     gamg_hier H;
     gamg_setup(&H, m, agg, gc);

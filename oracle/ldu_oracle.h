@@ -32,6 +32,10 @@ typedef struct {
     int nIf;
     const int *ifCell, *ifNbr;
     const double *ifBou, *ifInt;
+    /* the interfaces' patch sizes (GAMG groups each patch's faces on its
+     * own); nIfPatch = 0 with nIf > 0: one patch of nIf faces */
+    int nIfPatch;
+    const int* ifPatchSize;
 } ldu_matrix;
 
 typedef struct {

@@ -30,7 +30,8 @@ class LduMatrix(ctypes.Structure):
     _fields_ = [("nCells", ctypes.c_int), ("nFaces", ctypes.c_int),
                 ("l", i32p), ("u", i32p), ("diag", f64p), ("upper", f64p), ("lower", f64p),
                 ("ownerStart", i32p), ("losort", i32p), ("losortStart", i32p),
-                ("nIf", ctypes.c_int), ("ifCell", i32p), ("ifNbr", i32p), ("ifBou", f64p), ("ifInt", f64p)]
+                ("nIf", ctypes.c_int), ("ifCell", i32p), ("ifNbr", i32p), ("ifBou", f64p), ("ifInt", f64p),
+                ("nIfPatch", ctypes.c_int), ("ifPatchSize", i32p)]
 
 
 class LduPerf(ctypes.Structure):
@@ -119,6 +120,9 @@ class Matrix:
             self.c.nIf = self.ifc[0].size
             self.c.ifCell, self.c.ifNbr = _p(self.ifc[0], i32p), _p(self.ifc[1], i32p)
             self.c.ifBou, self.c.ifInt = _p(self.ifc[2]), _p(self.ifc[3])
+            if s.get("ifSize") is not None:
+                self.ifc.append(np.ascontiguousarray(s["ifSize"], np.int32))
+                self.c.nIfPatch, self.c.ifPatchSize = self.ifc[4].size, _p(self.ifc[4], i32p)
         lib().ldu_init_addr(ctypes.byref(self.c))
         self.n = self.diag.size
 

@@ -176,8 +176,8 @@ def fvcyc_case(name):
     g["solverName"] = bytes(g["solverName"]).decode()
     s = dict(l=g["l"], u=g["u"], diag=g["diag"], upper=g["upper"], lower=g.get("lower"), source=g["source"],
              ifSize=g["ifSize"], ifCell=g["ifCell"], ifNbr=g["ifNbr"], ifBou=g["ifBou"], ifInt=g["ifInt"])
-    psi0 = None
-    if "deltaT" in eq:
-        m = cases.box_mesh(**SPECS["fvcyc"]["mesh"])
-        psi0 = fvcyc_inputs(m, SPECS["fvcyc"]["seed"])["psi0"]
+    m = cases.box_mesh(**SPECS["fvcyc"]["mesh"])
+    nI = m["nInternalFaces"]
+    s["Sf"] = m["Sf"][: 3 * nI].reshape(nI, 3).copy()  # faceAreaPair weights
+    psi0 = fvcyc_inputs(m, SPECS["fvcyc"]["seed"])["psi0"] if "deltaT" in eq else None
     return s, psi0, dict(ctl), g

@@ -200,14 +200,22 @@ def test_fvmatrix_solve_bit_exact(name):
     assert p.converged == bool(g["converged"][0])
 
 
-@pytest.mark.parametrize("name", [n for n in fvcyc_names() if SPECS["fvcyc"]["cases"][n][1]["solver"] != "GAMG"])
+@pytest.mark.parametrize("name", fvcyc_names())
 def test_cyclic_fvmatrix_solve_bit_exact(name):
     """The reference's own cyclicPolyPatch / cyclicFvPatchField on an
     x-periodic box: from the lduMatrix and interfaces its fvMatrix handed to
     the solver (interfaceBouCoeffs = boundaryCoeffs, interfaceIntCoeffs =
-    internalCoeffs), the oracle's PCG, PBiCGStab, PBiCG and smoothSolver
-    reproduce psi, iterations and residuals bit for bit."""
+    internalCoeffs), the oracle's PCG, PBiCGStab, PBiCG, smoothSolver and
+    GAMG (its cyclicGAMGInterface levels restated) reproduce psi, iterations
+    and residuals bit for bit, and GAMG's levels."""
     s, psi0, ctl, g = fvcyc_case(name)
+    if "nLevels" in g:
+        agg = orc.Agglomeration(s, n_coarsest=ctl.get("nCellsInCoarsestLevel", 10))
+        assert agg.n_levels == g["nLevels"][0]
+        for i in range(agg.n_levels):
+            ra, fra, flip, nc, _, _, _ = agg.level(i)
+            np.testing.assert_array_equal(ra, g[f"restrict{i}"])
+            np.testing.assert_array_equal(fra, g[f"faceRestrict{i}"])
     psi, p = _run_oracle(s, ctl, psi0=psi0)
     np.testing.assert_array_equal(psi, g["psi"])
     assert p.nIterations == g["nIterations"][0]

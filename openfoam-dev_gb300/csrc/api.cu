@@ -58,6 +58,10 @@ struct cfx_mesh {
     int nIf = 0;
     std::vector<int> ifPos;
     Arena ifArena;
+    // the same interfaces on the host (patch sizes, face cells, partner
+    // cells, patch order) and the GAMG levels' coarse interfaces
+    std::vector<int> ifPatchSize, ifFaceCell, ifNbrCell;
+    Arena ifCoarseArena;
 };
 
 template <class T>
@@ -212,6 +216,8 @@ void alloc_coeffs(Arena& ar, const LevelMesh& m, bool sym, LevelCoeffs<T>& c) {
 }
 
 // GAMG hierarchy from level-0 restriction maps (host), then upload.
+void build_coarse_interfaces(cfx_mesh* mesh);
+
 cfx_status build_hierarchy(cfx_mesh* mesh, const std::vector<std::vector<int>>& maps, const std::vector<int>& nCoarse) {
     cudaStream_t s = mesh->ctx->stream;
     mesh->host.resize(1);
@@ -248,7 +254,81 @@ cfx_status build_hierarchy(cfx_mesh* mesh, const std::vector<std::vector<int>>& 
         if (mesh->host[i].nCoarse > 0) upload_restriction(mesh->arena, s, mesh->host[i], m);
         mesh->dev.push_back(m);
     }
+    build_coarse_interfaces(mesh);
     return CFX_OK;
+}
+
+// The GAMG levels' cyclic interfaces (cyclicGAMGInterface.C:87-151): on
+// each coarse level every patch's faces are grouped by the pair (coarse cell,
+// coarse partner cell) in order of first appearance, the partner cell read
+// through the partner patch's restricted face cells (its
+// internalFieldTransfer); per level, the coarse faces' CSR over cells (in
+// patch-then-face order, as updateMatrixInterfaces adds them) and, for the
+// coefficient sums (GAMGInterface::agglomerateCoeffs), each coarse face's
+// fine faces in ascending order.
+void build_coarse_interfaces(cfx_mesh* mesh) {
+    cudaStream_t s = mesh->ctx->stream;
+    CK(cudaStreamSynchronize(s));
+    mesh->ifCoarseArena.release();
+    const int nl = int(mesh->dev.size());
+    for (int i = 1; i < nl; ++i) {
+        LevelMesh& m = mesh->dev[i];
+        m.nIf = 0;
+        m.ifStart = m.ifNbr = m.ifcStart = m.ifcFine = nullptr;
+    }
+    if (!mesh->nIf) return;
+    std::vector<int> size = mesh->ifPatchSize, cell = mesh->ifFaceCell, nbr = mesh->ifNbrCell, pos = mesh->ifPos;
+    for (int i = 1; i < nl; ++i) {
+        const std::vector<int>& R = mesh->host[i - 1].restrictAddr;
+        const int nFine = int(cell.size());
+        std::vector<int> cSize, cCell, cNbr, toCoarse(static_cast<size_t>(nFine));
+        int off = 0;
+        for (size_t p = 0; p < size.size(); ++p) {
+            const int c0 = int(cCell.size());
+            std::map<std::pair<int, int>, int> seen;
+            for (int k = off; k < off + size[p]; ++k) {
+                const std::pair<int, int> key(R[cell[k]], R[nbr[k]]);
+                auto it = seen.find(key);
+                if (it == seen.end()) {
+                    const int j = int(cCell.size());
+                    seen.emplace(key, j);
+                    cCell.push_back(key.first);
+                    cNbr.push_back(key.second);
+                    toCoarse[k] = j;
+                } else {
+                    toCoarse[k] = it->second;
+                }
+            }
+            cSize.push_back(int(cCell.size()) - c0);
+            off += size[p];
+        }
+        const int n = mesh->host[i].n, nc = int(cCell.size());
+        std::vector<int> start(static_cast<size_t>(n) + 1, 0), cnbr(nc), cpos(nc);
+        for (int k = 0; k < nc; ++k) start[cCell[k] + 1]++;
+        for (int c = 0; c < n; ++c) start[c + 1] += start[c];
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int k = 0; k < nc; ++k) {
+            const int j = fill[cCell[k]]++;
+            cnbr[j] = cNbr[k];
+            cpos[k] = j;
+        }
+        std::vector<int> gStart(static_cast<size_t>(nc) + 1, 0), gFine(static_cast<size_t>(nFine));
+        for (int k = 0; k < nFine; ++k) gStart[cpos[toCoarse[k]] + 1]++;
+        for (int j = 0; j < nc; ++j) gStart[j + 1] += gStart[j];
+        std::vector<int> gfill(gStart.begin(), gStart.end() - 1);
+        for (int k = 0; k < nFine; ++k) gFine[gfill[cpos[toCoarse[k]]]++] = pos[k];
+        LevelMesh& m = mesh->dev[i];
+        m.nIf = nc;
+        m.ifStart = mesh->ifCoarseArena.upload(start, s);
+        m.ifNbr = mesh->ifCoarseArena.upload(cnbr, s);
+        m.ifcStart = mesh->ifCoarseArena.upload(gStart, s);
+        m.ifcFine = mesh->ifCoarseArena.upload(gFine, s);
+        size.swap(cSize);
+        cell.swap(cCell);
+        nbr.swap(cNbr);
+        pos.swap(cpos);
+    }
+    CK(cudaStreamSynchronize(s));  // the host vectors are temporaries
 }
 
 void set_state(cfx_ctx* ctx, int slot, const cfx_controls& c, double tol, double relTol, int maxIter, int minIter) {
@@ -313,7 +393,25 @@ void prepare_levels(cfx_matrix* mat, bool want32) {
         mat->coarse64 = false;
     }
     if (!mat->coarse64) {
-        for (int i = 1; i < nl; ++i) Ops<double>::coarsen(s, mesh->dev[i - 1], mat->c64[i - 1], mesh->dev[i], mat->c64[i]);
+        for (int i = 1; i < nl; ++i) {
+            Ops<double>::coarsen(s, mesh->dev[i - 1], mat->c64[i - 1], mesh->dev[i], mat->c64[i]);
+            // the coarse interfaces' coefficients
+            // (GAMGSolverAgglomerateMatrix.C:196-268)
+            const LevelMesh& cm = mesh->dev[i];
+            LevelCoeffs<double>& cc = mat->c64[i];
+            const LevelCoeffs<double>& fc = mat->c64[i - 1];
+            if (cm.nIf && fc.ifBou) {
+                if (cc.ifCap < cm.nIf) {
+                    cc.ifBou = mat->arena.get<double>(cm.nIf);
+                    cc.ifInt = mat->arena.get<double>(cm.nIf);
+                    cc.ifCap = cm.nIf;
+                }
+                Ops<double>::iface_restrict(s, cm, fc.ifBou, cc.ifBou);
+                Ops<double>::iface_restrict(s, cm, fc.ifInt ? fc.ifInt : fc.ifBou, cc.ifInt);
+            } else {
+                cc.ifBou = cc.ifInt = nullptr;
+            }
+        }
         mat->coarse64 = true;
     }
     if (want32) {
@@ -1030,6 +1128,7 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
     h.lp = c.lowerPerm;
     h.upper = c.upper;
     h.rD = c.rD;
+    h.itf = if_bou(m, c);  // the coarsest level's interfaces (solveCoarsestLevel)
     h.b = cy.src[lc - 1];
     h.psi = cy.corr[lc - 1];
     h.r = W.get(G0 + 3, m.n);
@@ -1413,10 +1512,15 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         return CFX_ERR_CONFIG;
     }
     if (mat->mesh->nIf) {
-        // coupled interfaces: the lduMatrix operations, the Krylov solvers and
-        // smoothSolver; GAMG's interface agglomeration is not built
-        if (c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) {
-            set_error("coupled interfaces are not supported by cudaGAMG or the GAMG preconditioner");
+        // coupled interfaces: the lduMatrix operations, the Krylov solvers,
+        // smoothSolver and GAMG (cyclicGAMGInterface levels); the direct
+        // coarsest-level solve's dense matrix does not take them
+        if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->directSolveCoarsest) {
+            set_error("directSolveCoarsest with coupled interfaces is not supported");
+            return CFX_ERR_CONFIG;
+        }
+        if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->smoother == CFX_SMOOTH_NBGS) {
+            set_error("nonBlockingGaussSeidel with coupled interfaces is not supported");
             return CFX_ERR_CONFIG;
         }
         if (c->precision == CFX_MIXED) {
@@ -1753,6 +1857,10 @@ cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32
             m.ifStart = mesh->ifArena.upload(start, s);
             m.ifNbr = mesh->ifArena.upload(nbr, s);
         }
+        mesh->ifPatchSize.assign(patchSize, patchSize + nPatches);
+        mesh->ifFaceCell.assign(faceCells, faceCells + nIf);
+        mesh->ifNbrCell.assign(nbrCells, nbrCells + nIf);
+        build_coarse_interfaces(mesh);
         mesh->version++;  // captured graphs hold the interface pointers
         CK(cudaStreamSynchronize(s));
         return CFX_OK;
@@ -1785,6 +1893,7 @@ cfx_status cfx_matrix_set_interface_coeffs(cfx_matrix* mat, const double* bouCoe
         CK(cudaMemcpyAsync(c.ifInt, ic.data(), sizeof(double) * nIf, cudaMemcpyHostToDevice, s));
         CK(cudaStreamSynchronize(s));  // b and ic are host temporaries
         mat->ifN = nIf;
+        mat->coarse64 = mat->coarse32 = false;  // the GAMG levels' interface sums
         return CFX_OK;
     });
 }

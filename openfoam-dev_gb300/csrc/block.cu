@@ -22,8 +22,11 @@ namespace {
 
 template <class G, class T>
 __device__ void blk_amul(G& g, const BlockSys<T>& S, const T* x, T* y) {
+    // Amul with the interfaces (lduMatrixATmul.C:34-92): internal faces,
+    // then each interface face's -coeffs*x[nbr]
     for (int c = g.rank(); c < S.n; c += g.size())
-        y[c] = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, x);
+        y[c] = iface_sub(S.itf, c, x,
+                         row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, x));
     g.sync();
 }
 
@@ -113,6 +116,9 @@ __device__ void blk_solve(G& g, BlockSys<T>& S) {
         T sA = S.diag[c];
         for (int k = S.losortStart[c]; k < S.losortStart[c + 1]; ++k) sA += S.lp[k];
         for (int f = S.ownerStart[c]; f < S.ownerStart[c + 1]; ++f) sA += S.upper[f];
+        // sumA's interface terms (lduMatrixATmul.C:238-254)
+        if (S.itf.start)
+            for (int j = S.itf.start[c]; j < S.itf.start[c + 1]; ++j) sA -= S.itf.coef[j];
         const T t = sA * T(avg);
         nf += double(fabs(S.q[c] - t) + fabs(S.b[c] - t));
         const T rc = S.b[c] - S.q[c];
@@ -197,7 +203,9 @@ __device__ void blk_solve(G& g, BlockSys<T>& S) {
                 // tA = A zA, kept in r (r is rewritten below from s and tA)
                 double tt = 0.0, ts = 0.0;
                 for (int c = r0_; c < n; c += st_) {
-                    const T v = row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp, S.upper, S.t);
+                    const T v = iface_sub(S.itf, c, S.t,
+                                          row_amul<T>(c, S.ownerStart, S.losortStart, S.losortL, S.u, S.diag, S.lp,
+                                                      S.upper, S.t));
                     S.r[c] = v;
                     tt += double(v) * double(v);
                     ts += double(v) * double(S.s[c]);

@@ -96,6 +96,11 @@ struct LevelMesh {
     int* ifStart = nullptr;  // [n+1]
     int* ifNbr = nullptr;    // [nIf]
     int* ifCells = nullptr;  // [nIfCells]
+    // coarse levels: the finer level's interface faces (their CSR
+    // positions, in ascending patch-then-face order) summed into each of this
+    // level's interface faces (CSR order)
+    int* ifcStart = nullptr;  // [nIf+1]
+    int* ifcFine = nullptr;   // [the finer level's nIf]
 };
 
 template <class T>
@@ -107,6 +112,7 @@ struct LevelCoeffs {
     // interfaceBouCoeffs / interfaceIntCoeffs in the mesh's interface CSR
     // order (null: none set)
     T *ifBou = nullptr, *ifInt = nullptr;
+    int ifCap = 0;  // allocated length of ifBou / ifInt (coarse levels)
 };
 
 // Device-resident scalars of one solve.  Kernels read and update them so the
@@ -200,6 +206,9 @@ struct Ops {
     // bp = b - (-bou)*psi[nbr] over the coupled interfaces (the Gauss-Seidel
     // smoothers' bPrime before a sweep)
     static void iface_bprime(cudaStream_t s, int n, const Iface<T>& itf, const T* b, const T* psi, T* bp);
+    // GAMGInterface::agglomerateCoeffs: coarse interface coefficients (CSR
+    // order of level m) from the finer level's
+    static void iface_restrict(cudaStream_t s, const LevelMesh& m, const T* fine, T* coarse);
 };
 
 // ---- finite-volume assembly (fvm.cu) -------------------------------------

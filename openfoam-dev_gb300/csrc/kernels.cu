@@ -168,14 +168,29 @@ template <class T>
 __global__ void offdiag_amul_k(int n, const int* __restrict__ ownerStart, const int* __restrict__ losortStart,
                                const int* __restrict__ losortL, const int* __restrict__ u,
                                const T* __restrict__ lp, const T* __restrict__ upper, const T* __restrict__ x,
-                               T* __restrict__ y) {
+                               T* __restrict__ y, Iface<T> itf) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         T acc = T(0);
         const int k1 = losortStart[c + 1];
         for (int k = losortStart[c]; k < k1; ++k) acc += lp[k] * x[losortL[k]];
         const int f1 = ownerStart[c + 1];
         for (int f = ownerStart[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
-        y[c] = acc;
+        // the interfaces' updateMatrixInterfaces (GAMGSolverInterpolate.C:60-67)
+        y[c] = iface_sub(itf, c, x, acc);
+    }
+}
+
+// GAMGInterface::agglomerateCoeffs (GAMGInterface.C:90-115) through
+// restrictField: each coarse interface face sums its fine faces'
+// coefficients from zero in the fine faces' order.
+template <class T>
+__global__ void iface_restrict_k(int nc, const int* __restrict__ start, const int* __restrict__ fineFaces,
+                                 const T* __restrict__ fine, T* __restrict__ coarse) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc; j += gridDim.x * blockDim.x) {
+        T v = T(0);
+        const int t1 = start[j + 1];
+        for (int t = start[j]; t < t1; ++t) v += fine[fineFaces[t]];
+        coarse[j] = v;
     }
 }
 
@@ -464,7 +479,7 @@ template <class T>
 void Ops<T>::interpolate(cudaStream_t s, const LevelMesh& f, const LevelCoeffs<T>& a, T* psi, T* Apsi,
                          const T* psiC) {
     offdiag_amul_k<T><<<grid_all(f.n), RED_NT, 0, s>>>(f.n, f.ownerStart, f.losortStart, f.losortL, f.u,
-                                                       a.lowerPerm, a.upper, psi, Apsi);
+                                                       a.lowerPerm, a.upper, psi, Apsi, if_bou(f, a));
     interp_coarse_k<T><<<grid_for(f.nCoarse), RED_NT, 0, s>>>(f.nCoarse, f.coarseCellStart, f.coarseCellFine,
                                                              a.diag, Apsi, psiC, psi);
     count_launch(2);
@@ -485,6 +500,12 @@ void Ops<T>::lu_solve(cudaStream_t s, int n, const T* A, const int* piv, const T
         lu_solve_k<T, true><<<1, 128, sm, s>>>(n, A, piv, b, x);
     else
         lu_solve_k<T, false><<<1, 32, 0, s>>>(n, A, piv, b, x);
+    count_launch();
+}
+
+template <class T>
+void Ops<T>::iface_restrict(cudaStream_t s, const LevelMesh& m, const T* fine, T* coarse) {
+    iface_restrict_k<T><<<grid_all(m.nIf), RED_NT, 0, s>>>(m.nIf, m.ifcStart, m.ifcFine, fine, coarse);
     count_launch();
 }
 

@@ -409,11 +409,13 @@ template <class T>
 __global__ void __launch_bounds__(RED_NT) gamg_scale_sf_k(int n, const int* os, const int* ls, const int* lL,
                                                           const int* u, const T* diag, const T* lp, const T* upper,
                                                           const T* __restrict__ field, T* __restrict__ Acf,
-                                                          const T* __restrict__ source, SolveState* st, Red2 red) {
+                                                          const T* __restrict__ source, SolveState* st, Red2 red,
+                                                          Iface<T> itf) {
     if (st->done) return;
     double num = 0.0, den = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = row_amul<T>(c, os, ls, lL, u, diag, lp, upper, field);
+        // Amul with the level's interfaces (GAMGSolverScale.C:42-50)
+        const T v = iface_sub(itf, c, field, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, field));
         Acf[c] = v;
         num += double(source[c]) * double(field[c]);
         den += double(v) * double(field[c]);
@@ -624,7 +626,7 @@ void Kern<T>::gamg_scale_sf(cudaStream_t s, Scratch& sc, const LevelMesh& m, con
                             T* Acf, const T* source, SolveState* st) {
     gamg_scale_sf_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
                                                         a.lowerPerm, a.upper, field, Acf, source, st,
-                                                        Red2{sc.partials, sc.counters});
+                                                        Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
 

@@ -14,6 +14,7 @@ struct BlockSys {
     int nFwd, nBwd;
     const T *diag, *lp, *upper, *rD;
     const T* upPerm;  // upper[losort] for the DILU reciprocal diagonal (null: lp)
+    Iface<T> itf;     // the level's coupled interfaces (start null: none)
     const T* b;
     T* psi;
     T *r, *w, *p, *q, *s, *t, *r0;  // work vectors (s, t, r0: PBiCGStab)

@@ -20,8 +20,11 @@
   fvMatrix::solve (fvScalarMatrix.C:162-170); the device copies of the
   addressing, level schedules and GAMG hierarchy live in a process-wide
   cache keyed by the lduMesh, and the coefficients are re-uploaded on every
-  solve.  Coupled interfaces are not supported: a matrix with any set
-  interface is refused with FatalError.
+  solve.  Cyclic coupled interfaces are passed through (each patch's face
+  cells, its partner's face cells, interfaceBouCoeffs and
+  interfaceIntCoeffs); the library builds GAMG's coarse cyclic interfaces
+  itself.  Any other coupled interface (processor) is refused with
+  FatalError.
 \*---------------------------------------------------------------------------*/
 
 #include "lduMatrix.H"

@@ -375,7 +375,7 @@ def test_pbicg_against_oracle_and_its_errors():
 
 
 def test_cyclic_interfaces_refusals_and_larger_system():
-    """With coupled interfaces GAMG and mixed precision are refused; a 16^3
+    """With coupled interfaces mixed precision is refused; a 16^3
     periodic system solves like the oracle with PCG+DIC and PBiCG+DILU."""
     s = cases.cyclic_cube(16, jitter=0.2, seed=4)
     with pytest.raises(ldu.FatalError, match="interfaces"):

@@ -16,14 +16,19 @@ The fixtures come from the reference's own finiteVolume library
   10 % and 4; its per-iteration reductions are summed in another order).
 * fvcyc_*.npz: fvMatrix::solve on an x-periodic box with the reference's
   own cyclic patches.  The lduMatrix and interfaces the reference's solver
-  received, solved through the plugin solvers with coupled interfaces, give
-  the reference's psi within the same bounds.
+  received, solved through the plugin solvers with coupled interfaces (GAMG
+  with its cyclicGAMGInterface levels included), give the reference's psi
+  within the same bounds.
+GAMG and the GAMG preconditioner with cyclic interfaces also follow the
+oracle on a 16^3 periodic cube; directSolveCoarsest with interfaces is
+refused.
 """
 import numpy as np
 import pytest
 
 from golden_cases import SPECS, fvcyc_case, fvcyc_names, fvm_case, fvm_names, fvsolve_case, fvsolve_names, matrix_digest
 from oracle import oracle as orc
+from golden_cases import gamg_kwargs
 from openfoam_dev_gb300 import cases, ldu
 
 pytestmark = pytest.mark.gpu
@@ -127,10 +132,40 @@ def _check_against(perf, x, g, ctl, om, b, start):
         assert rel <= 1e-6, rel
 
 
-@pytest.mark.parametrize("name", [n for n in fvcyc_names() if SPECS["fvcyc"]["cases"][n][1]["solver"] != "GAMG"])
+@pytest.mark.parametrize("name", fvcyc_names())
 def test_cyclic_solve_matches_fvmatrix_solve(name):
     s, psi0, ctl, g = fvcyc_case(name)
     start = np.zeros_like(s["source"]) if psi0 is None else np.array(psi0)
     x = start.copy()
     perf = ldu.solve(s, x, dict(ctl, solver=_PLUGIN_NAMES[ctl["solver"]]))
     _check_against(perf, x, g, ctl, orc.Matrix(s), s["source"], start)
+
+
+@pytest.mark.parametrize("ctl", [
+    dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-9, relTol=0.0),
+    dict(solver="GAMG", smoother="DIC", nPreSweeps=1, interpolateCorrection=True, tolerance=1e-9, relTol=0.0),
+    dict(solver="PCG", tolerance=1e-9, relTol=0.0,
+         preconditioner=dict(preconditioner="GAMG", smoother="symGaussSeidel")),
+], ids=["gamg_gs", "gamg_dic_interp", "pcg_gamg"])
+def test_gamg_with_cyclic_interfaces_against_the_oracle(ctl):
+    s = cases.cyclic_cube(16, jitter=0.2, seed=4)
+    ref = np.zeros_like(s["source"])
+    pre = ctl.get("preconditioner")
+    if ctl["solver"] == "GAMG":
+        rp = orc.gamg(s, ref, tol=ctl["tolerance"], **gamg_kwargs(ctl))
+    else:
+        rp = orc.pcg_gamg(s, ref, tol=ctl["tolerance"], **gamg_kwargs(pre))
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, dict(ctl, solver=_PLUGIN_NAMES[ctl["solver"]]))
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1, (perf, rp)
+    rel = float(np.linalg.norm(psi - ref) / np.linalg.norm(ref))
+    if perf.nIterations == rp.nIterations:
+        assert rel <= 1e-10, rel
+    else:
+        assert rel <= 1e-6, rel
+
+
+def test_direct_coarsest_solve_with_interfaces_is_refused():
+    s = cases.cyclic_cube(8, jitter=0.2, seed=2)
+    with pytest.raises(ldu.FatalError, match="directSolveCoarsest"):
+        ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaGAMG", "directSolveCoarsest": True})

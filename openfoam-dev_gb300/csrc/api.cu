@@ -433,7 +433,20 @@ void prepare_levels(cfx_matrix* mat, bool want32) {
                     launch_cast_d2f(s, m.nf, mat->c64[i].lower, mat->c32[i].lower);
                     launch_cast_d2f(s, m.nf, mat->c64[i].upperPerm, mat->c32[i].upperPerm);
                 }
-                count_launch(mat->sym ? 3 : 5);
+                // the interface coefficients of the FP32 inner solves
+                LevelCoeffs<float>& f32 = mat->c32[i];
+                const LevelCoeffs<double>& f64 = mat->c64[i];
+                if (m.nIf && f64.ifBou) {
+                    if (f32.ifCap < m.nIf) {
+                        f32.ifBou = mat->arena.get<float>(m.nIf);
+                        f32.ifInt = mat->arena.get<float>(m.nIf);
+                        f32.ifCap = m.nIf;
+                    }
+                    launch_cast_d2f(s, m.nIf, f64.ifBou, f32.ifBou);
+                    launch_cast_d2f(s, m.nIf, f64.ifInt ? f64.ifInt : f64.ifBou, f32.ifInt);
+                } else {
+                    f32.ifBou = f32.ifInt = nullptr;
+                }
             }
             mat->fine32 = mat->coarse32 = true;
         }
@@ -1521,10 +1534,6 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         }
         if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->smoother == CFX_SMOOTH_NBGS) {
             set_error("nonBlockingGaussSeidel with coupled interfaces is not supported");
-            return CFX_ERR_CONFIG;
-        }
-        if (c->precision == CFX_MIXED) {
-            set_error("precision mixed is not available with coupled interfaces");
             return CFX_ERR_CONFIG;
         }
         // nonBlockingGaussSeidel splits its sweep at the first interface cell

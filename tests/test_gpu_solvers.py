@@ -374,13 +374,10 @@ def test_pbicg_against_oracle_and_its_errors():
                                                     "precision": "mixed"})
 
 
-def test_cyclic_interfaces_refusals_and_larger_system():
-    """With coupled interfaces mixed precision is refused; a 16^3
-    periodic system solves like the oracle with PCG+DIC and PBiCG+DILU."""
+def test_cyclic_interfaces_larger_system():
+    """A 16^3 periodic system solves like the oracle with PCG+DIC and
+    PBiCG+DILU."""
     s = cases.cyclic_cube(16, jitter=0.2, seed=4)
-    with pytest.raises(ldu.FatalError, match="interfaces"):
-        ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaPCG", "preconditioner": "DIC",
-                                                  "precision": "mixed"})
     ref = np.zeros_like(s["source"])
     rp = orc.pcg(s, ref, tol=1e-10, max_iter=2000)
     psi = np.zeros_like(s["source"])

@@ -21,7 +21,9 @@ The fixtures come from the reference's own finiteVolume library
   within the same bounds.
 GAMG and the GAMG preconditioner with cyclic interfaces also follow the
 oracle on a 16^3 periodic cube; directSolveCoarsest with interfaces is
-refused.
+refused.  Mixed precision (FP32 inner solves, FP64 refinement) with
+interfaces reaches the FP64 tolerance by the oracle's FP64 residual and
+stays within relative L2 1e-6 of the FP64 solution.
 """
 import numpy as np
 import pytest
@@ -169,3 +171,21 @@ def test_direct_coarsest_solve_with_interfaces_is_refused():
     s = cases.cyclic_cube(8, jitter=0.2, seed=2)
     with pytest.raises(ldu.FatalError, match="directSolveCoarsest"):
         ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaGAMG", "directSolveCoarsest": True})
+
+
+@pytest.mark.parametrize("ctl", [
+    {"solver": "cudaPCG", "preconditioner": "DIC"},
+    {"solver": "cudaPBiCGStab", "preconditioner": "DIC"},
+    {"solver": "cudaGAMG", "smoother": "GaussSeidel"},
+], ids=["pcg", "pbicgstab", "gamg"])
+def test_mixed_precision_with_cyclic_interfaces(ctl):
+    s = cases.cyclic_cube(16, jitter=0.2, seed=4)
+    ref = np.zeros_like(s["source"])
+    orc.pcg(s, ref, tol=1e-12, max_iter=5000)
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, dict(ctl, tolerance=1e-8, relTol=0.0, precision="mixed"))
+    assert perf.converged
+    om = orc.Matrix(s)
+    nf = om.norm_factor(np.zeros_like(psi), s["source"])
+    assert np.abs(om.residual(psi, s["source"])).sum() / nf < 1.5e-8
+    assert float(np.linalg.norm(psi - ref) / np.linalg.norm(ref)) <= 1e-6

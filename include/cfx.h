@@ -165,6 +165,20 @@ cfx_status cfx_gamg_level_info(cfx_mesh* mesh, int level, int* nCells, int* nFac
                                int32_t* restrictAddr, int32_t* faceRestrict, int32_t* faceFlip,
                                int32_t* coarseL, int32_t* coarseU);
 cfx_status cfx_gamg_n_levels(cfx_mesh* mesh, int* nLevels);
+/* GAMG's coarse cyclic interfaces of one level, on the host
+ * (cyclicGAMGInterface.C:87-151; GAMGAgglomerateLduAddressing.C:250-340
+ * creates them): from the finer level's interfaces (nPatches patches of
+ * patchSize faces in patch order, their cells and partner cells) and the
+ * restriction map, each patch's faces grouped by (coarse cell, coarse partner
+ * cell) in order of first appearance.  Out: the coarse patch sizes
+ * [nPatches], coarse face cells and partner cells [sum of patchSize at
+ * most], each fine face's coarse face (patch-order index) and the coarse
+ * face count.  cfx_mesh_set_interfaces' GAMG levels are built this way. */
+cfx_status cfx_gamg_coarse_interfaces(int32_t nFineCells, const int32_t* restrictAddr, int32_t nPatches,
+                                      const int32_t* patchSize, const int32_t* faceCells,
+                                      const int32_t* nbrCells, int32_t* coarsePatchSize,
+                                      int32_t* coarseFaceCells, int32_t* coarseNbrCells,
+                                      int32_t* fineToCoarse, int32_t* nCoarseFaces);
 
 /* ---- matrix (lduMatrix coefficients) ------------------------------------ */
 /* Host coefficients; lower == NULL means symmetric (lduMatrix::symmetric()).

@@ -266,6 +266,37 @@ cfx_status build_hierarchy(cfx_mesh* mesh, const std::vector<std::vector<int>>& 
 // patch-then-face order, as updateMatrixInterfaces adds them) and, for the
 // coefficient sums (GAMGInterface::agglomerateCoeffs), each coarse face's
 // fine faces in ascending order.
+// One level's grouping (cyclicGAMGInterface.C:87-151): size/cell/nbr of the
+// finer level in patch order and its restriction map R.
+void coarse_interface_faces(const int* R, const std::vector<int>& size, const std::vector<int>& cell,
+                            const std::vector<int>& nbr, std::vector<int>& cSize, std::vector<int>& cCell,
+                            std::vector<int>& cNbr, std::vector<int>& toCoarse) {
+    cSize.clear();
+    cCell.clear();
+    cNbr.clear();
+    toCoarse.assign(cell.size(), 0);
+    int off = 0;
+    for (size_t p = 0; p < size.size(); ++p) {
+        const int c0 = int(cCell.size());
+        std::map<std::pair<int, int>, int> seen;
+        for (int k = off; k < off + size[p]; ++k) {
+            const std::pair<int, int> key(R[cell[k]], R[nbr[k]]);
+            auto it = seen.find(key);
+            if (it == seen.end()) {
+                const int j = int(cCell.size());
+                seen.emplace(key, j);
+                cCell.push_back(key.first);
+                cNbr.push_back(key.second);
+                toCoarse[k] = j;
+            } else {
+                toCoarse[k] = it->second;
+            }
+        }
+        cSize.push_back(int(cCell.size()) - c0);
+        off += size[p];
+    }
+}
+
 void build_coarse_interfaces(cfx_mesh* mesh) {
     cudaStream_t s = mesh->ctx->stream;
     CK(cudaStreamSynchronize(s));
@@ -279,29 +310,9 @@ void build_coarse_interfaces(cfx_mesh* mesh) {
     if (!mesh->nIf) return;
     std::vector<int> size = mesh->ifPatchSize, cell = mesh->ifFaceCell, nbr = mesh->ifNbrCell, pos = mesh->ifPos;
     for (int i = 1; i < nl; ++i) {
-        const std::vector<int>& R = mesh->host[i - 1].restrictAddr;
         const int nFine = int(cell.size());
-        std::vector<int> cSize, cCell, cNbr, toCoarse(static_cast<size_t>(nFine));
-        int off = 0;
-        for (size_t p = 0; p < size.size(); ++p) {
-            const int c0 = int(cCell.size());
-            std::map<std::pair<int, int>, int> seen;
-            for (int k = off; k < off + size[p]; ++k) {
-                const std::pair<int, int> key(R[cell[k]], R[nbr[k]]);
-                auto it = seen.find(key);
-                if (it == seen.end()) {
-                    const int j = int(cCell.size());
-                    seen.emplace(key, j);
-                    cCell.push_back(key.first);
-                    cNbr.push_back(key.second);
-                    toCoarse[k] = j;
-                } else {
-                    toCoarse[k] = it->second;
-                }
-            }
-            cSize.push_back(int(cCell.size()) - c0);
-            off += size[p];
-        }
+        std::vector<int> cSize, cCell, cNbr, toCoarse;
+        coarse_interface_faces(mesh->host[i - 1].restrictAddr.data(), size, cell, nbr, cSize, cCell, cNbr, toCoarse);
         const int n = mesh->host[i].n, nc = int(cCell.size());
         std::vector<int> start(static_cast<size_t>(n) + 1, 0), cnbr(nc), cpos(nc);
         for (int k = 0; k < nc; ++k) start[cCell[k] + 1]++;
@@ -1780,6 +1791,39 @@ cfx_status cfx_gamg_set_levels(cfx_mesh* mesh, int nLevels, const int32_t* const
         }
         CFX_TRY(build_hierarchy(mesh, maps, nCoarse));
         CK(cudaStreamSynchronize(mesh->ctx->stream));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_gamg_coarse_interfaces(int32_t nFineCells, const int32_t* restrictAddr, int32_t nPatches,
+                                      const int32_t* patchSize, const int32_t* faceCells,
+                                      const int32_t* nbrCells, int32_t* coarsePatchSize,
+                                      int32_t* coarseFaceCells, int32_t* coarseNbrCells,
+                                      int32_t* fineToCoarse, int32_t* nCoarseFaces) {
+    if (nFineCells < 0 || nPatches < 0 || !nCoarseFaces || (nPatches && (!patchSize || !coarsePatchSize)) ||
+        (nFineCells && !restrictAddr))
+        return CFX_ERR_ARG;
+    int64_t nIf = 0;
+    for (int p = 0; p < nPatches; ++p) {
+        if (patchSize[p] < 0) return CFX_ERR_ARG;
+        nIf += patchSize[p];
+    }
+    if (nIf > (int64_t(1) << 30)) return CFX_ERR_ARG;
+    if (nIf && (!faceCells || !nbrCells || !coarseFaceCells || !coarseNbrCells || !fineToCoarse)) return CFX_ERR_ARG;
+    for (int64_t k = 0; k < nIf; ++k)
+        if (faceCells[k] < 0 || faceCells[k] >= nFineCells || nbrCells[k] < 0 || nbrCells[k] >= nFineCells) {
+            set_error("cfx_gamg_coarse_interfaces: a face cell is out of range");
+            return CFX_ERR_ADDRESSING;
+        }
+    return guard([&]() -> cfx_status {
+        std::vector<int> size(patchSize, patchSize + nPatches), cell(faceCells, faceCells + nIf),
+            nbr(nbrCells, nbrCells + nIf), cSize, cCell, cNbr, toCoarse;
+        coarse_interface_faces(restrictAddr, size, cell, nbr, cSize, cCell, cNbr, toCoarse);
+        std::copy(cSize.begin(), cSize.end(), coarsePatchSize);
+        std::copy(cCell.begin(), cCell.end(), coarseFaceCells);
+        std::copy(cNbr.begin(), cNbr.end(), coarseNbrCells);
+        std::copy(toCoarse.begin(), toCoarse.end(), fineToCoarse);
+        *nCoarseFaces = int32_t(cCell.size());
         return CFX_OK;
     });
 }

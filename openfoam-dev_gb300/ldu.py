@@ -124,6 +124,7 @@ _SIG = {
     "cfx_mesh_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cfx_face_area_pair_weights": (_i, [_i, _vp, _vp]),
     "cfx_gamg_agglomerate": (_i, [_vp, _vp, _i, _i]),
+    "cfx_gamg_coarse_interfaces": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfx_gamg_set_levels": (_i, [_vp, _i, _vp, _vp]),
     "cfx_gamg_level_info": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp, _vp, _vp, _vp, _vp]),
     "cfx_gamg_n_levels": (_i, [_vp, ctypes.POINTER(_i)]),
@@ -514,6 +515,21 @@ def tune_get(key):
     v = ctypes.c_int()
     _check(lib().cfx_tune_get(int(key), ctypes.byref(v)), "cfx_tune_get")
     return v.value
+
+
+def gamg_coarse_interfaces(restrictAddr, patchSize, faceCells, nbrCells):
+    """One GAMG level's coarse cyclic interfaces (cfx_gamg_coarse_interfaces,
+    host only): (coarse patch sizes, face cells, partner cells, each fine
+    face's coarse face)."""
+    R = np.ascontiguousarray(restrictAddr, np.int32)
+    ps = np.ascontiguousarray(patchSize, np.int32)
+    fc = np.ascontiguousarray(faceCells, np.int32)
+    nc = np.ascontiguousarray(nbrCells, np.int32)
+    cps, cfc, cnc, f2c = (np.zeros(max(a, 1), np.int32) for a in (ps.size, fc.size, fc.size, fc.size))
+    n = ctypes.c_int32()
+    _check(lib().cfx_gamg_coarse_interfaces(R.size, _hp(R), ps.size, _hp(ps), _hp(fc), _hp(nc), _hp(cps), _hp(cfc),
+                                            _hp(cnc), _hp(f2c), ctypes.byref(n)), "cfx_gamg_coarse_interfaces")
+    return cps[:ps.size], cfc[:n.value], cnc[:n.value], f2c[:fc.size]
 
 
 def face_area_pair_weights(Sf):

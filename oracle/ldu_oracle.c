@@ -931,7 +931,7 @@ typedef struct {
  * the other side); the coefficients are summed over each coarse face's fine
  * faces in face order (GAMGSolverAgglomerateMatrix.C:196-268 restrictField,
  * GAMGInterface.C:90-115). */
-static void coarse_interfaces(const ldu_matrix* fine, const int* R, level_matrix* L) {
+static void coarse_interfaces(const ldu_matrix* fine, const int* R, level_matrix* L, int* toCoarse) {
     const int nIf = fine->nIf;
     const int nP = fine->nIfPatch > 0 ? fine->nIfPatch : 1;
     L->ifCell = (int*)xmalloc(sizeof(int) * nIf);
@@ -956,6 +956,7 @@ static void coarse_interfaces(const ldu_matrix* fine, const int* R, level_matrix
             }
             L->ifBou[j] += fine->ifBou[k];
             L->ifInt[j] += fine->ifInt ? fine->ifInt[k] : fine->ifBou[k];
+            if (toCoarse) toCoarse[k] = j;
         }
         L->ifPatchSize[p] = nc - c0;
         off += np;
@@ -990,6 +991,38 @@ static void gamg_scale(const ldu_matrix* A, double* field, double* Acf, const do
 }
 
 static int imin(int a, int b) { return a < b ? a : b; }
+
+int ldu_gamg_coarse_interfaces(const int* R, int nPatch, const int* patchSize, const int* faceCells,
+                               const int* nbrCells, const double* bou, int* coarsePatchSize, int* coarseFaceCells,
+                               int* coarseNbrCells, double* coarseBou, int* toCoarse) {
+    ldu_matrix f;
+    memset(&f, 0, sizeof(f));
+    int nIf = 0;
+    for (int p = 0; p < nPatch; ++p) nIf += patchSize[p];
+    f.nIf = nIf;
+    f.ifCell = faceCells;
+    f.ifNbr = nbrCells;
+    f.ifBou = bou;
+    f.ifInt = bou;
+    f.nIfPatch = nPatch;
+    f.ifPatchSize = patchSize;
+    level_matrix L;
+    memset(&L, 0, sizeof(L));
+    if (nIf) coarse_interfaces(&f, R, &L, toCoarse);
+    const int nc = L.m.nIf;
+    for (int p = 0; p < nPatch && nIf; ++p) coarsePatchSize[p] = L.ifPatchSize[p];
+    for (int j = 0; j < nc; ++j) {
+        coarseFaceCells[j] = L.ifCell[j];
+        coarseNbrCells[j] = L.ifNbr[j];
+        coarseBou[j] = L.ifBou[j];
+    }
+    free(L.ifCell);
+    free(L.ifNbr);
+    free(L.ifPatchSize);
+    free(L.ifBou);
+    free(L.ifInt);
+    return nc;
+}
 
 /* The GAMG hierarchy of one solve: coarse matrices (GAMGSolver ctor,
  * GAMGSolver.C:204-206), the smoothers' reciprocal diagonals and the coarse
@@ -1127,7 +1160,7 @@ static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeratio
         L->m.diag = L->diag;
         L->m.upper = L->upper;
         L->m.lower = L->lower;
-        if (fine->nIf) coarse_interfaces(fine, agg->restrictAddr[i], L);
+        if (fine->nIf) coarse_interfaces(fine, agg->restrictAddr[i], L, NULL);
         ldu_init_addr(&L->m);
         fine = &L->m;
     }

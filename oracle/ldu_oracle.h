@@ -133,6 +133,13 @@ int ldu_gamg_agglomerate(int nCells, int nFaces, const int* l, const int* u,
                          ldu_agglomeration* agg);
 void ldu_gamg_free(ldu_agglomeration* agg);
 
+/* One GAMG level's coarse cyclic interfaces (cyclicGAMGInterface.C:87-151)
+ * and summed coefficients (GAMGInterface.C:90-115) from the finer level's
+ * (patch order) and restriction map R; returns the coarse face count. */
+int ldu_gamg_coarse_interfaces(const int* R, int nPatch, const int* patchSize, const int* faceCells,
+                               const int* nbrCells, const double* bou, int* coarsePatchSize, int* coarseFaceCells,
+                               int* coarseNbrCells, double* coarseBou, int* toCoarse);
+
 /* faceAreaPairGAMGAgglomeration.C:55-80 weights from face-area vectors. */
 void ldu_face_area_pair_weights(int nFaces, const double* Sf, double* w);
 

@@ -260,6 +260,21 @@ def pbicgstab(s, psi, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, precond=
     return _perf(perf)
 
 
+def gamg_coarse_interfaces(R, patchSize, faceCells, nbrCells, bou):
+    """One GAMG level's coarse cyclic interfaces: (patch sizes, face cells,
+    partner cells, summed coefficients, each fine face's coarse face)."""
+    i = lambda a: np.ascontiguousarray(a, np.int32)  # noqa: E731
+    R, ps, fc, nc = i(R), i(patchSize), i(faceCells), i(nbrCells)
+    bou = np.ascontiguousarray(bou, np.float64)
+    n = max(fc.size, 1)
+    cps, cfc, cnc, f2c = np.zeros(max(ps.size, 1), np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32), \
+        np.zeros(n, np.int32)
+    cb = np.zeros(n)
+    k = lib().ldu_gamg_coarse_interfaces(_p(R, i32p), ps.size, _p(ps, i32p), _p(fc, i32p), _p(nc, i32p), _p(bou),
+                                         _p(cps, i32p), _p(cfc, i32p), _p(cnc, i32p), _p(cb), _p(f2c, i32p))
+    return cps[:ps.size], cfc[:k], cnc[:k], cb[:k], f2c[:fc.size]
+
+
 def face_area_pair_weights(Sf):
     Sf = np.ascontiguousarray(Sf, np.float64).reshape(-1)
     w = np.empty(Sf.size // 3)

@@ -199,3 +199,30 @@ def test_fvm_oracle_agrees_with_the_case_generator_on_an_orthogonal_mesh():
     np.testing.assert_allclose(up, cd["upper"], rtol=1e-13, atol=1e-16)
     np.testing.assert_allclose(lo, cd["lower"], rtol=1e-13, atol=1e-16)
     assert np.all(src == 0)
+
+
+@pytest.mark.parametrize("which", ["cube16", "channel"])
+def test_coarse_cyclic_interfaces_match_the_oracle(which):
+    """The library's GAMG coarse cyclic interfaces (the host grouping the
+    device levels are built from) equal the oracle's restatement of
+    cyclicGAMGInterface on every level, and summing each coarse face's fine
+    coefficients in ascending fine-face order (the device gather) gives the
+    oracle's coarse coefficients bit for bit."""
+    if which == "cube16":
+        s = cases.cyclic_cube(16, jitter=0.2, seed=4)
+    else:
+        s = cases.cyclic_cube(12, jitter=0.1, seed=5, U=[1.0, 0.3, 0.2], gamma=0.05)
+    agg = orc.Agglomeration(s)
+    size, cell, nbr, bou = s["ifSize"], s["ifCell"], s["ifNbr"], s["ifBou"]
+    for i in range(agg.n_levels):
+        R = agg.level(i)[0]
+        ps, fc, nc, f2c = ldu.gamg_coarse_interfaces(R, size, cell, nbr)
+        ops, ofc, onc, ob, of2c = orc.gamg_coarse_interfaces(R, size, cell, nbr, bou)
+        for a, b in ((ps, ops), (fc, ofc), (nc, onc), (f2c, of2c)):
+            np.testing.assert_array_equal(a, b)
+        summed = np.zeros(fc.size)
+        for k in range(f2c.size):
+            summed[f2c[k]] += bou[k]
+        np.testing.assert_array_equal(summed, ob)
+        assert fc.size <= cell.size and ps.sum() == fc.size
+        size, cell, nbr, bou = ps, fc, nc, ob

@@ -230,6 +230,11 @@ FVCYC = dict(mesh=dict(nx=10, ny=9, nz=8, jitter=0.25, seed=4, periodic_x=True),
                        dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-9, relTol=0.0)),
     "laplacian_gamg_dic": (dict(lapSign=-1, gammaUniform=0.6, su=True),
                            dict(solver="GAMG", smoother="DIC", nPreSweeps=1, tolerance=1e-9, relTol=0.0)),
+    "laplacian_pcg_gamg": (dict(lapSign=-1, gammaUniform=0.6, su=True),
+                           dict(solver="PCG", tolerance=1e-9, relTol=0.0,
+                                preconditioner=dict(preconditioner="GAMG", smoother="GaussSeidel"))),
+    "transport_gamg": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
+                       dict(solver="GAMG", smoother="GaussSeidel", tolerance=1e-10, relTol=0.0)),
     "transport_pbicgstab": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
                             dict(solver="PBiCGStab", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
     "transport_pbicg": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),

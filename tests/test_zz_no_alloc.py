@@ -7,7 +7,8 @@ size limit (33,554,432 elements).  The test compares it, through the C ABI,
 with the allocating entry point cfx_reduce on two calls in a row (the static
 scratch is reused), within the reduction tolerance the other tests use, and
 checks that a size beyond the limit is refused before any launch.  This file
-sorts last so that a run stopping at the first failure has run the rest.
+sorts after the solver and operator tests so that a run stopping at the first
+failure has run them.
 """
 import ctypes
 

@@ -1,5 +1,9 @@
 """Device-side assembly and solve against the reference's fvMatrix itself.
 
+This file sorts last: its fixtures and its cyclic GAMG and mixed-precision
+cases are the newest GPU checks, so a run stopping at the first failure has
+run every other test first.
+
 The fixtures come from the reference's own finiteVolume library
 (tests/golden/make_golden.py, oracle/fv_harness.C):
 

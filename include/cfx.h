@@ -3,7 +3,7 @@
  *
  * The library replaces, for one GPU, the reference's lduMatrix::solver path:
  * an OpenFOAM plugin class (cudaPCG, cudaPBiCGStab, cudaGAMG deriving
- * Foam::lduMatrix::solver, see INTEGRATION.md) holds a cfx_mesh per lduMesh,
+ * Foam::lduMatrix::solver) holds a cfx_mesh per lduMesh,
  * re-uploads coefficients on every solve and calls cfx_solve().  All entry
  * points take plain pointers and sizes; labels are int32 (WM_LABEL_SIZE=32)
  * and scalars double (WM_DP).  Every function returns a cfx_status.
@@ -432,8 +432,8 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* d_psi, const double* d_
 
 /* ---- reduction that allocates nothing ------------------------------------
  * No counterpart in the reference: an extra entry point for callers that
- * cannot call cudaMalloc (code enqueuing work during CUDA-graph stream
- * capture, hosts that give all GPU memory to their own pool).  Same
+ * cannot call cudaMalloc (a host application whose own memory pool reserves
+ * the whole GPU, or one held to a fixed device-memory budget).  Same
  * operations as cfx_reduce (which: 0 sum, 1 sumMag, 2 sumSqr, 3 sumProd), no
  * context: d_a, d_b (device, n doubles) in, the result to the device double
  * d_out, enqueued on `stream` (a cudaStream_t; NULL = the default stream)

@@ -36,7 +36,11 @@ using namespace cfx;
 // ------------------------------------------------------------------ objects
 
 struct cfx_mesh {
-    cfx_ctx* ctx = nullptr;
+    cfx_ctx* ctx = nullptr;  // retained while the mesh lives
+    // The creator's handle plus one reference per matrix on this mesh:
+    // cfx_mesh_destroy drops the creator's and the mesh is freed with its
+    // last matrix, so matrices may be destroyed after their mesh.
+    std::atomic<int> refs{1};
     Arena arena;
     std::vector<HostLevel> host;   // [0] = the mesh, then GAMG coarse levels
     std::vector<LevelMesh> dev;
@@ -1612,6 +1616,31 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
 }  // namespace
 
 // ===================================================================== C ABI
+namespace cfx {
+void ctx_retain(cfx_ctx* ctx) { ctx->refs.fetch_add(1, std::memory_order_relaxed); }
+
+void ctx_release(cfx_ctx* ctx) {
+    if (ctx->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFreeHost(ctx->h_state);
+    cudaFreeHost(ctx->h_red);
+    ctx->arena.release();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+void mesh_retain(cfx_mesh* mesh) { mesh->refs.fetch_add(1, std::memory_order_relaxed); }
+
+void mesh_release(cfx_mesh* mesh) {
+    if (mesh->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
+    cfx_ctx* ctx = mesh->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    delete mesh;
+    ctx_release(ctx);
+}
+}  // namespace cfx
+
 extern "C" {
 
 void cfx_default_controls(cfx_controls* c) {
@@ -1668,14 +1697,10 @@ cfx_status cfx_ctx_create(int device, cfx_ctx** out) {
     });
 }
 
+
 cfx_status cfx_ctx_destroy(cfx_ctx* ctx) {
     if (!ctx) return CFX_ERR_ARG;
-    cudaStreamSynchronize(ctx->stream);
-    cudaFreeHost(ctx->h_state);
-    cudaFreeHost(ctx->h_red);
-    ctx->arena.release();
-    cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    ctx_release(ctx);
     return CFX_OK;
 }
 
@@ -1715,6 +1740,7 @@ cfx_status cfx_mesh_create(cfx_ctx* ctx, int nCells, int nFaces, const int32_t* 
         upload_level(mesh->arena, ctx->stream, mesh->host[0], m);
         mesh->dev.push_back(m);
         CK(cudaStreamSynchronize(ctx->stream));
+        ctx_retain(ctx);
         *out = mesh.release();
         return CFX_OK;
     });
@@ -1722,8 +1748,7 @@ cfx_status cfx_mesh_create(cfx_ctx* ctx, int nCells, int nFaces, const int32_t* 
 
 cfx_status cfx_mesh_destroy(cfx_mesh* mesh) {
     if (!mesh) return CFX_ERR_ARG;
-    cudaStreamSynchronize(mesh->ctx->stream);
-    delete mesh;
+    mesh_release(mesh);
     return CFX_OK;
 }
 
@@ -1865,6 +1890,7 @@ cfx_status cfx_matrix_create(cfx_mesh* mesh, const double* diag, const double* u
         mat->d_src = mat->arena.get<double>(n);
         set_coefficients(mat.get(), diag, upper, lower, cudaMemcpyHostToDevice);
         CK(cudaStreamSynchronize(mesh->ctx->stream));
+        mesh_retain(mesh);
         *out = mat.release();
         return CFX_OK;
     });
@@ -1969,6 +1995,7 @@ cfx_status cfx_matrix_create_empty(cfx_mesh* mesh, int symmetric, cfx_matrix** o
         if (m.nf && !mat->sym) CK(cudaMemsetAsync(c.lower, 0, sizeof(double) * m.nf, s));
         coefficients_changed(mat.get());
         CK(cudaStreamSynchronize(s));
+        mesh_retain(mesh);
         *out = mat.release();
         return CFX_OK;
     });
@@ -2092,9 +2119,11 @@ cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* diag, const d
 
 cfx_status cfx_matrix_destroy(cfx_matrix* mat) {
     if (!mat) return CFX_ERR_ARG;
-    cudaStreamSynchronize(mat->mesh->ctx->stream);
+    cfx_mesh* mesh = mat->mesh;  // alive: the matrix holds a reference
+    cudaStreamSynchronize(mesh->ctx->stream);
     pc_gamg_free(mat->pcGamg);
     delete mat;
+    mesh_release(mesh);
     return CFX_OK;
 }
 

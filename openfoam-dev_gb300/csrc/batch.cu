@@ -540,6 +540,7 @@ cfx_status cfx_batch_create(cfx_ctx* ctx, int nSystems, const int32_t* nCells, c
         CK(cudaMallocHost(&bt->h64, sizeof(SlotSys<double>) * nSystems));
         CK(cudaMallocHost(&bt->h32, sizeof(SlotSys<float>) * nSystems));
         CK(cudaStreamSynchronize(ctx->stream));
+        ctx_retain(ctx);
         *out = bt.release();
         return CFX_OK;
     });
@@ -547,8 +548,10 @@ cfx_status cfx_batch_create(cfx_ctx* ctx, int nSystems, const int32_t* nCells, c
 
 cfx_status cfx_batch_destroy(cfx_batch* bt) {
     if (!bt) return CFX_ERR_ARG;
-    cudaStreamSynchronize(bt->ctx->stream);
+    cfx_ctx* ctx = bt->ctx;  // alive: the batch holds a reference
+    cudaStreamSynchronize(ctx->stream);
     delete bt;
+    ctx_release(ctx);
     return CFX_OK;
 }
 

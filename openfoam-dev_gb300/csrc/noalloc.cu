@@ -1,13 +1,15 @@
 // noalloc.cu - a reduction entry point that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: code that enqueues work while a stream
-// is being captured into a CUDA graph (an allocation there breaks the
-// capture), and host codes that hand the whole GPU memory to their own pool
-// or run under a fixed memory budget with no room for a library's
-// allocations.  cfx_reduce_noalloc serves them: its only scratch is the
-// file-scope array below, which the CUDA runtime places when the library's
-// device code is loaded and which every GPU that loads the library holds
-// until the process exits.
+// Some callers cannot call cudaMalloc: a host application whose own memory
+// pool has reserved the whole GPU up front (a cudaMalloc from a library then
+// fails, or takes memory the pool accounts for), or one that runs under a
+// fixed device-memory budget with no room for a library's allocations.
+// cfx_reduce_noalloc serves them: its only scratch is the file-scope array
+// below, which the CUDA runtime places when the library's device code is
+// loaded and which every GPU that loads the library holds until the process
+// exits.  The first call on a device looks up the array's device address
+// (once, with that device current); make that first call before any stream
+// capture.
 //
 // Scratch: NA_MAX_BLOCKS fixed-order block partials plus a completion
 // counter.  Each block reduces exactly NA_NT*NA_ITEMS consecutive elements,
@@ -102,7 +104,9 @@ extern "C" cfx_status cfx_reduce_noalloc(int which, int n, const double* d_a, co
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_na_scratch);
             if (e != cudaSuccess || !p) {
-                set_error(std::string("cfx_reduce_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+                set_error(std::string("cfx_reduce_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e) +
+                          " (a device's first call looks up the scratch address and must be made outside "
+                          "stream capture)");
                 return CFX_ERR_CUDA;
             }
             g_na_ptr[dev] = static_cast<NaScratch*>(p);

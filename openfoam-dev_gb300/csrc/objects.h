@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -76,7 +77,17 @@ struct cfx_ctx {
     int* d_status = nullptr;
     double* d_red = nullptr;        // [8] reduction outputs
     double* h_red = nullptr;        // pinned
+    // The creator's handle plus one reference per mesh, batch and server
+    // built on this context: cfx_ctx_destroy drops the creator's, and the
+    // context is freed when the last user goes, in whatever order the
+    // caller (or a garbage collector) destroys them.
+    std::atomic<int> refs{1};
 };
+
+namespace cfx {
+void ctx_retain(cfx_ctx* ctx);
+void ctx_release(cfx_ctx* ctx);
+}  // namespace cfx
 
 struct GraphCache {
     cudaGraphExec_t exec = nullptr;

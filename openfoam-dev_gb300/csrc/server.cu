@@ -372,6 +372,7 @@ cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_ser
         CK(cudaMalloc(&sv->d_next, 2 * sizeof(unsigned)));
         sv->t0 = Clock::now();
         sv->worker = std::thread(worker_loop, sv.get());
+        ctx_retain(ctx);
         *out = sv.release();
         return CFX_OK;
     });
@@ -399,7 +400,9 @@ cfx_status cfx_server_destroy(cfx_server* sv) {
     cudaStreamDestroy(sv->copyStream);
     if (sv->ctxLarge) cfx_ctx_destroy(sv->ctxLarge);
     sv->cvDone.notify_all();
+    cfx_ctx* ctx = sv->ctx;  // alive: the server holds a reference
     delete sv;
+    ctx_release(ctx);
     return CFX_OK;
 }
 

@@ -20,13 +20,16 @@ plain C++ (its VERSION_STRING/BUILD_STRING placeholders stay literal).
 The harness ``oracle/ref_harness.C`` (our own code) is then linked against it.
 Outputs go only to ``oracle/_ref/``; nothing is written to the reference tree.
 
-Usage: python oracle/build_ref.py [--ref /root/reference] [-j N]
+Usage: python oracle/build_ref.py [--ref DIR] [-j N]   (DIR defaults to $OPENFOAM_REF_DIR)
 """
 import argparse
 import os
 import re
 import subprocess
 import sys
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from refpath import REF_ROOT  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
@@ -104,7 +107,7 @@ def make_farm(src_dir, farm):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=REF_ROOT)
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     args = ap.parse_args()
     ref = os.path.abspath(args.ref)

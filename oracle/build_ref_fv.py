@@ -15,7 +15,7 @@ compiled; the link leaves their two symbols unresolved in the shared library
 (nothing on the assembly path reads STL).  Outputs go only to
 ``oracle/_ref/``.
 
-Usage: python oracle/build_ref_fv.py [--ref /root/reference] [-j N] [--lib-only]
+Usage: python oracle/build_ref_fv.py [--ref DIR] [-j N] [--lib-only]   (DIR defaults to $OPENFOAM_REF_DIR)
 """
 import argparse
 import os
@@ -38,7 +38,7 @@ FV_LIBS = [
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=br.REF_ROOT)
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--lib-only", action="store_true", help="build the library, not the harness")
     args = ap.parse_args()

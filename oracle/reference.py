@@ -11,10 +11,10 @@ import tempfile
 import numpy as np
 
 from . import records
+from .refpath import REF_ROOT
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 HARNESS = os.path.join(HERE, "_ref", "ref_harness")
-REF_ROOT = "/root/reference"
 
 
 def available():

@@ -1,8 +1,8 @@
 """cfx_reduce_noalloc: the reduction entry point that allocates nothing.
 
-It exists for callers that cannot call cudaMalloc (work enqueued while a
-stream is captured into a CUDA graph; host codes whose memory pool owns the
-whole GPU).  Its block partials live in a static device array, so it has a
+It exists for callers that cannot call cudaMalloc: a host application whose
+own memory pool has reserved the whole GPU, or one held to a fixed
+device-memory budget.  Its block partials live in a static device array, so it has a
 size limit (33,554,432 elements).  The test compares it, through the C ABI,
 with the allocating entry point cfx_reduce on two calls in a row (the static
 scratch is reused), within the reduction tolerance the other tests use, and

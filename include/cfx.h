@@ -125,7 +125,19 @@ void cfx_default_controls(cfx_controls* c);
 const char* cfx_last_error(void);
 int cfx_version(void);
 
-/* ---- context ------------------------------------------------------------ */
+/* ---- context ------------------------------------------------------------
+ * Handles are reference counted: a mesh holds its context and a matrix its
+ * mesh (batches and servers hold their context), so the *_destroy calls may
+ * come in any order; memory goes with the last handle that uses it.
+ *
+ * Stream order: a context enqueues on its own non-blocking stream.  Entry
+ * points that take the caller's device pointers first order that stream
+ * after the work already on the legacy default stream (where CUDA runtime
+ * code and PyTorch produce arrays by default), and those that return before
+ * their work completes (cfx_fvm_assemble, cfx_matrix_update_device, the
+ * diagonal solve) order the default stream after it.  A caller producing or
+ * consuming arrays on another stream synchronises that stream itself, or
+ * enqueues on the context's stream (cfx_ctx_stream). */
 cfx_status cfx_ctx_create(int device, cfx_ctx** ctx);
 cfx_status cfx_ctx_destroy(cfx_ctx* ctx);
 /* The cudaStream_t all work of this context is enqueued on. */

@@ -1626,6 +1626,8 @@ void ctx_release(cfx_ctx* ctx) {
     cudaFreeHost(ctx->h_state);
     cudaFreeHost(ctx->h_red);
     ctx->arena.release();
+    if (ctx->evIn) cudaEventDestroy(ctx->evIn);
+    if (ctx->evOut) cudaEventDestroy(ctx->evOut);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1679,6 +1681,8 @@ cfx_status cfx_ctx_create(int device, cfx_ctx** out) {
         ctx->device = device;
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->evIn, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->evOut, cudaEventDisableTiming));
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
         sweeps_init(sms);
@@ -2088,9 +2092,11 @@ cfx_status cfx_fvm_assemble(cfx_matrix* mat, const cfx_fvm_terms* t, double* d_s
         a.hasDdt = ddt;
         a.hasDiv = div;
         LevelCoeffs<double>& c = mat->c64[0];
+        after_caller(mesh->ctx);
         launch_fvm_assemble(mesh->ctx->stream, mesh->dev[0], g, a, c.diag, c.upper, mat->sym ? nullptr : c.lower,
                             d_source);
         CK(cudaGetLastError());
+        to_caller(mesh->ctx);
         mat->diagonal = false;
         coefficients_changed(mat);
         return CFX_OK;
@@ -2112,7 +2118,9 @@ cfx_status cfx_matrix_update_device(cfx_matrix* mat, const double* diag, const d
     if (!mat || !diag || (mat->sym != (lower == nullptr)) || (mat->diagonal != (upper == nullptr)))
         return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         set_coefficients(mat, diag, upper, lower, cudaMemcpyDeviceToDevice);
+        to_caller(mat->mesh->ctx);
         return CFX_OK;
     });
 }
@@ -2152,7 +2160,9 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
         if (!ctl) return CFX_ERR_ARG;
         std::memset(perf, 0, sizeof(*perf));
         const cfx_status st = guard([&]() -> cfx_status {
+            after_caller(mat->mesh->ctx);
             Ops<double>::diag_solve(mat->mesh->ctx->stream, mat->mesh->dev[0].n, mat->c64[0].diag, d_source, d_psi);
+            to_caller(mat->mesh->ctx);
             return CFX_OK;
         });
         std::snprintf(perf->solverName, sizeof(perf->solverName), "diagonal");
@@ -2171,6 +2181,7 @@ cfx_status cfx_solve_device(cfx_matrix* mat, const cfx_controls* ctl, double* d_
     if (c.smoother == CFX_SMOOTH_FDIC) c.smoother = CFX_SMOOTH_DIC;
     if (c.smoother == CFX_SMOOTH_NBGS) c.smoother = CFX_SMOOTH_GS;
     const cfx_status st = guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         CK(cudaMemsetAsync(mat->mesh->ctx->d_status, 0, sizeof(int), mat->mesh->ctx->stream));
         if (c.solver == CFX_SOLVER_GAMG) return gamg_solve(mat, c, d_psi, d_source, perf);
         if (c.solver == CFX_SOLVER_SMOOTH) return smooth_solve(mat, c, d_psi, d_source, perf);
@@ -2249,6 +2260,7 @@ cfx_status cfx_tune_get(int key, int* value) {
 cfx_status cfx_amul(cfx_matrix* mat, const double* x, double* y) {
     if (!mat || !x || !y) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         Ops<double>::amul(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, y);
         CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
         return CFX_OK;
@@ -2258,6 +2270,7 @@ cfx_status cfx_amul(cfx_matrix* mat, const double* x, double* y) {
 cfx_status cfx_tmul(cfx_matrix* mat, const double* x, double* y) {
     if (!mat || !x || !y) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         Ops<double>::tmul(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, y);
         CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
         return CFX_OK;
@@ -2267,6 +2280,7 @@ cfx_status cfx_tmul(cfx_matrix* mat, const double* x, double* y) {
 cfx_status cfx_residual(cfx_matrix* mat, const double* x, const double* b, double* r) {
     if (!mat || !x || !b || !r) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         Ops<double>::residual(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], x, b, r);
         CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
         return CFX_OK;
@@ -2276,6 +2290,7 @@ cfx_status cfx_residual(cfx_matrix* mat, const double* x, const double* b, doubl
 cfx_status cfx_sumA(cfx_matrix* mat, double* s) {
     if (!mat || !s) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(mat->mesh->ctx);
         Ops<double>::sumA(mat->mesh->ctx->stream, mat->mesh->dev[0], mat->c64[0], s);
         CK(cudaStreamSynchronize(mat->mesh->ctx->stream));
         return CFX_OK;
@@ -2285,6 +2300,7 @@ cfx_status cfx_sumA(cfx_matrix* mat, double* s) {
 cfx_status cfx_reduce(cfx_ctx* ctx, int which, int n, const double* a, const double* b, double* out) {
     if (!ctx || !a || !out || which < 0 || which > 3 || (which == 3 && !b) || n < 0) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
+        after_caller(ctx);
         launch_reduce<double>(ctx->stream, ctx->sc, which, n, a, b, ctx->d_red);
         count_launch();
         CK(cudaMemcpyAsync(ctx->h_red, ctx->d_red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2298,6 +2314,7 @@ cfx_status cfx_norm_factor(cfx_matrix* mat, const double* psi, const double* b, 
     if (!mat || !psi || !b || !out) return CFX_ERR_ARG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
+        after_caller(ctx);
         cudaStream_t s = ctx->stream;
         const LevelMesh& m = mat->mesh->dev[0];
         Work<double>& W = mat->w64;
@@ -2324,6 +2341,7 @@ cfx_status cfx_reciprocal_d(cfx_matrix* mat, int kind, double* rD) {
         return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
+        after_caller(ctx);
         const LevelMesh& m = mat->mesh->dev[0];
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
         setup_preconditioner<double>(mat, 0, kind);
@@ -2344,6 +2362,7 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
         return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
+        after_caller(ctx);
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
         setup_preconditioner<double>(mat, 0, kind);
         precondition<double>(mat, 0, kind, r, w, nullptr, false);
@@ -2390,6 +2409,7 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* psi, const double* b, i
     if ((kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) && mat->sym) return CFX_ERR_CONFIG;
     return guard([&]() -> cfx_status {
         cfx_ctx* ctx = mat->mesh->ctx;
+        after_caller(ctx);
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
         if ((int)mat->lv64.size() < 1) mat->lv64.resize(1);
         if (kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) setup_preconditioner<double>(mat, 0, CFX_PRE_DIC);

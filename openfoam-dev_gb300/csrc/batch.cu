@@ -579,6 +579,7 @@ cfx_status cfx_batch_solve_device(cfx_batch* bt, const cfx_controls* ctl, cfx_pe
     if (!bt) return CFX_ERR_ARG;
     CFX_TRY(batch_check(bt, ctl));
     return guard([&]() -> cfx_status {
+        after_caller(bt->ctx);  // the caller may have filled the vectors on its stream
         batch_enqueue(bt, *ctl);
         batch_results(bt, *ctl, perf);
         return CFX_OK;

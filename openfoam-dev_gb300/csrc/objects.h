@@ -82,11 +82,30 @@ struct cfx_ctx {
     // context is freed when the last user goes, in whatever order the
     // caller (or a garbage collector) destroys them.
     std::atomic<int> refs{1};
+    // Stream order with the caller: entry points that take the caller's
+    // device pointers first make this context's (non-blocking) stream wait
+    // for the work already enqueued on the legacy default stream, where
+    // CUDA runtime callers and PyTorch produce their arrays by default, and
+    // the asynchronous ones make that stream wait for their results.
+    cudaEvent_t evIn = nullptr, evOut = nullptr;
 };
 
 namespace cfx {
 void ctx_retain(cfx_ctx* ctx);
 void ctx_release(cfx_ctx* ctx);
+
+// The caller's inputs are ready before this context's stream reads them.
+inline void after_caller(cfx_ctx* ctx) {
+    CK(cudaEventRecord(ctx->evIn, cudaStreamLegacy));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->evIn, 0));
+}
+
+// The caller's later work on the default stream sees this stream's results
+// (and may reuse the input arrays it passed).
+inline void to_caller(cfx_ctx* ctx) {
+    CK(cudaEventRecord(ctx->evOut, ctx->stream));
+    CK(cudaStreamWaitEvent(cudaStreamLegacy, ctx->evOut, 0));
+}
 }  // namespace cfx
 
 struct GraphCache {

@@ -30,6 +30,8 @@ Inputs are regenerated by the tests from the stored case parameters with
 openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
 
 Usage:  python tests/golden/make_golden.py
+        (flux_fvsolve.npz alone, on the machine that made the fvsolve
+        fixtures: python tests/golden/make_golden.py --fvsolve-inputs)
 """
 import hashlib
 import json
@@ -199,12 +201,20 @@ def fvm_cases():
         print(name, float(np.abs(out["diag"]).sum()), float(np.abs(out["source"]).sum()))
 
 
+def write_fvsolve_inputs(inp):
+    """The face flux the fvsolve cases are assembled from, as computed here:
+    Sf.U goes through the host BLAS, whose rounding is machine-dependent, so
+    the tests read these bits instead of recomputing them."""
+    np.savez_compressed(os.path.join(HERE, "flux_fvsolve.npz"), phi=np.concatenate([inp["phi"], inp["phiB"]]))
+
+
 def fvsolve_cases():
     """The equation assembled and solved by fvMatrix::solve on a larger
     jittered box: psi, the solver performance and GAMG's levels (faceAreaPair
     on the fvMesh's own Sf); the assembled matrix is kept as a digest."""
     m = cases.box_mesh(**FVSOLVE["mesh"])
     inp = gc.fvm_inputs(m, seed=FVSOLVE["seed"])
+    write_fvsolve_inputs(inp)
     for name, (eq, ctl) in FVSOLVE["cases"].items():
         kw = gc.fvm_ref_kwargs(FVM[eq], inp, FVSOLVE["patchBC"])
         r = ref.fvm(m, solve=ctl, **kw)
@@ -314,6 +324,9 @@ def main():
         fvm_cases()
         fvsolve_cases()
         fvcyc_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--fvsolve-inputs":
+        m = cases.box_mesh(**FVSOLVE["mesh"])
+        write_fvsolve_inputs(gc.fvm_inputs(m, seed=FVSOLVE["seed"]))
     else:
         print("fv_harness not built (python oracle/build_ref_fv.py): fvm_*.npz kept")
 

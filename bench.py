@@ -16,7 +16,16 @@ reference-facing call a plugin makes per solve: coefficient upload, psi and
 source host->device from pinned memory, the solve, psi device->host.
 
 --impl reference times the C restatement of the reference solver (oracle/,
-the reference itself is not built on this machine) on the host cores.
+bit-exact with the reference built from its sources, compiled with the
+reference's own optimisation flags) on the host cores: every step is one
+complete serial solve from psi = 0 to 1e-8, the steps run concurrently, one
+process per host core.  Its inputs are the same seeded arrays, written to a
+file by a separate generator process, so the timed processes load only the
+oracle.
+
+Parity: oracle processes started before the first GPU call solve the same
+systems (256^3 GAMG, 64^3 PCG+DIC, 128^3 PBiCGStab+DILU) to 1e-8, then on to
+1e-12; the line states each GPU solution's relative L2 error against both.
 
 Multi-GPU: replicas only (one independent system per rank, no collective on
 the data path); launch with torchrun, value = max over ranks.
@@ -52,8 +61,11 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=256, help="cube cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel-only", choices=["gs"], default=None,
-                    help="only run the finest-level fused 2-sweep Gauss-Seidel (for profiling)")
+    ap.add_argument("--kernel-only", choices=["gs", "level1", "solves"], default=None,
+                    help="profiling: gs = the finest level's fused 2-sweep Gauss-Seidel alone, level1 = the "
+                         "first agglomerated level's, solves = one FP64 and one mixed headline solve inside "
+                         "the NVTX range 'profiled' (after one warm-up solve of each)")
+    ap.add_argument("--write-case", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--workload", choices=["all", "gamg", "batch", "serve"], default="all",
                     help="all: the GAMG headline line with the batch and serving measurements added")
     ap.add_argument("--batch-count", type=int, default=512)
@@ -92,10 +104,129 @@ def reduce_max(pg, v):
 
 
 def workload(n):
+    """The configuration both arms report (identical dicts)."""
     return {"workload": f"cudaGAMG faceAreaPair GaussSeidel nPre2/nPost2, Laplacian of a {n}^3 cube jittered "
                         f"+-20%, Dirichlet x=0, tolerance 1e-8 relTol 0",
             "n_cells": n ** 3, "n_faces": 3 * n * n * (n - 1), "solve": "psi=0 to residual 1e-8",
-            "l2": "inputs larger than L2 (no flush): the resident system is several GB"}
+            "seed": 1, "l2": "inputs larger than L2 (no flush): the resident system is several GB"}
+
+
+# ------------------------------------------------------------ oracle (CPU) legs
+# These run in processes started with the spawn method before the first GPU
+# call.  They load the oracle built with the reference's optimisation flags
+# (CFX_ORACLE_TIMED=1; bit-identical results to the build the tests pin).
+
+GAMG_ORACLE = dict(smoother="GaussSeidel", nPreSweeps=2, nPostSweeps=2)
+
+
+def _oracle_case(kind, n, seed):
+    ge.load_package()
+    from openfoam_dev_gb300 import cases
+    if kind == "gamg":
+        return cases.gamg_cube(n, jitter=0.2, seed=seed)
+    if kind == "pcg":
+        return cases.pcg_cube(n, seed=seed)
+    return cases.bicgstab_cube(n, seed=seed)
+
+
+def _oracle_solve(kind, s, psi, tol, agg=None, max_iter=None):
+    from oracle import oracle as orc
+    if kind == "gamg":
+        return orc.gamg(s, psi, agg, tol=tol, rel_tol=0.0, max_iter=max_iter or 200, **GAMG_ORACLE)
+    if kind == "pcg":
+        return orc.pcg(s, psi, tol=tol, rel_tol=0.0, max_iter=max_iter or 2000, precond="DIC")
+    return orc.pbicgstab(s, psi, tol=tol, rel_tol=0.0, max_iter=max_iter or 2000, precond="DILU")
+
+
+def oracle_job(kind, n, seed, outdir):
+    """One configuration in the oracle (serial): the solve from psi = 0 to
+    1e-8, timed (GAMG: the agglomeration, cached per mesh as the reference
+    caches it, timed apart), then continued from that psi to 1e-12 (the FP64
+    truth every result is measured against).  Both solutions are written to
+    outdir; the statistics are returned."""
+    os.environ["CFX_ORACLE_TIMED"] = "1"
+    from oracle import oracle as orc
+    s = _oracle_case(kind, n, seed)
+    agg, t_agg = None, 0.0
+    if kind == "gamg":
+        t0 = time.perf_counter()
+        agg = orc.Agglomeration(s, n_coarsest=10)
+        t_agg = time.perf_counter() - t0
+    psi = np.zeros_like(s["source"])
+    t0 = time.perf_counter()
+    p = _oracle_solve(kind, s, psi, 1e-8, agg)
+    t = time.perf_counter() - t0
+    np.save(os.path.join(outdir, f"{kind}{n}_psi8.npy"), psi)
+    psi12 = psi.copy()
+    q = _oracle_solve(kind, s, psi12, 1e-12, agg, max_iter=4000)
+    np.save(os.path.join(outdir, f"{kind}{n}_psi12.npy"), psi12)
+    return {"kind": kind, "n": n, "seed": seed, "s": t, "iterations": p.nIterations,
+            "final_residual": p.finalResidual, "converged": bool(p.converged), "agglomeration_s": t_agg,
+            "truth_iterations": q.nIterations, "truth_final_residual": q.finalResidual,
+            "truth_converged": bool(q.converged)}
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+def parity_of(job, outdir, psi_fp64, it_fp64, psi_mixed=None):
+    """The GPU solutions against the oracle's: FP64 against its 1e-8 solve
+    (the drop-in bar: rel L2 <= 1e-10, iterations +-1) and both precisions
+    against its 1e-12 solution (the error each result states)."""
+    p8 = np.load(os.path.join(outdir, f"{job['kind']}{job['n']}_psi8.npy"))
+    p12 = np.load(os.path.join(outdir, f"{job['kind']}{job['n']}_psi12.npy"))
+    out = {"oracle_iterations": job["iterations"], "fp64_iterations": it_fp64,
+           "fp64_vs_oracle_1e-8_rel_l2": _rel_l2(psi_fp64, p8),
+           "fp64_vs_truth_1e-12_rel_l2": _rel_l2(psi_fp64, p12),
+           "oracle_1e-8_vs_truth_rel_l2": _rel_l2(p8, p12),
+           "truth": f"oracle FP64 continued to {job['truth_final_residual']:.2e} "
+                    f"({job['truth_iterations']} more iterations)"}
+    if psi_mixed is not None:
+        out["mixed_vs_truth_1e-12_rel_l2"] = _rel_l2(psi_mixed, p12)
+    out["fp64_drop_in_ok"] = bool(out["fp64_vs_oracle_1e-8_rel_l2"] <= 1e-10 and
+                                  abs(it_fp64 - job["iterations"]) <= 1)
+    return out
+
+
+def write_case(path, n, seed=1):
+    """The headline system (256^3 jittered Laplacian) as the oracle takes it,
+    with its faceAreaPair weights: written by a separate process so that the
+    timed reference processes load the oracle only."""
+    os.environ["CFX_ORACLE_TIMED"] = "1"
+    from oracle import oracle as orc
+    s = _oracle_case("gamg", n, seed)
+    w = orc.face_area_pair_weights(s["Sf"])
+    np.savez(path, l=s["l"], u=s["u"], diag=s["diag"], upper=s["upper"], source=s["source"], weights=w)
+
+
+def reference_step(path, i):
+    """One step of the reference arm: one complete serial solve of the case
+    file's system from psi = 0 to 1e-8 (coarse-level set-up included, the
+    cached agglomeration not), timed in this process."""
+    os.environ["CFX_ORACLE_TIMED"] = "1"
+    from oracle import oracle as orc
+    z = np.load(path)
+    s = {k: z[k] for k in ("l", "u", "diag", "upper", "source")}
+    s["lower"] = None
+    agg = orc.Agglomeration(s, weights=z["weights"], n_coarsest=10)
+    psi = np.zeros_like(s["source"])
+    t0 = time.perf_counter()
+    p = _oracle_solve("gamg", s, psi, 1e-8, agg)
+    t = time.perf_counter() - t0
+    return {"step": i, "s": t, "iterations": p.nIterations, "final_residual": p.finalResidual,
+            "converged": bool(p.converged)}
+
+
+def _mem_available():
+    try:
+        with open("/proc/meminfo") as fh:
+            for line in fh:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
 
 
 class Clocks:
@@ -151,73 +282,122 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference_sample(s, cycles_hint=None):
-    """The oracle (C restatement of GAMGSolver, serial) on a bounded sample of
-    the same workload: agglomeration plus 2 V-cycles, extrapolated to the
-    V-cycles a full solve takes (from the observed per-cycle reduction, or the
-    GPU solve's count, which matches the reference's within one)."""
-    from oracle import oracle as orc
-    t0 = time.perf_counter()
-    agg = orc.Agglomeration(s, n_coarsest=10)
-    t_agg = time.perf_counter() - t0
-    psi = np.zeros_like(s["source"])
-    kw = dict(tol=TOL, rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=2, nPostSweeps=2)
-    t0 = time.perf_counter()
-    p1 = orc.gamg(s, psi, agg, max_iter=1, **kw)
-    t1 = time.perf_counter() - t0
-    psi = np.zeros_like(s["source"])
-    t0 = time.perf_counter()
-    p2 = orc.gamg(s, psi, agg, max_iter=2, **kw)
-    t2 = time.perf_counter() - t0
-    t_cycle = max(t2 - t1, 1e-9)
-    if cycles_hint:
-        cycles = int(cycles_hint)
-    else:
-        rho = p2.finalResidual / max(p1.finalResidual, 1e-300)
-        cycles = 2 + max(0, math.ceil(math.log(TOL / p2.finalResidual) / math.log(rho))) if rho < 1 else 1000
-    # setup (coarse matrices, smoother set-up) is t1 - t_cycle
-    total = (t1 - t_cycle) + cycles * t_cycle
-    return {"value": total, "cycles": cycles, "t_cycle": t_cycle, "t_setup": t1 - t_cycle,
-            "t_agglomeration": t_agg, "sample_s": t_agg + t1 + t2}
-
-
 def run_reference(args, rank, world, pg):
+    """The reference arm: the oracle (the reference's solver restated,
+    bit-exact with its own build, compiled with its optimisation flags) on
+    the host cores.  Every step is one complete serial solve of the headline
+    system to 1e-8, timed directly; the warm-up and timed steps run
+    concurrently, one process per host core (as many as the host memory
+    holds), so the run ends within minutes.  Rank 0 alone runs it."""
     if rank != 0:
         return 0
-    ge.load_package()
-    from openfoam_dev_gb300 import cases
-    s = cases.gamg_cube(args.n, jitter=0.2, seed=1)
-    # the V-cycle count of the full serial solve, measured once before the
-    # timed steps (the early cycles reduce the residual faster than the
-    # rest, so a rate from the first two under-counts)
-    from oracle import oracle as orc
-    psi = np.zeros_like(s["source"])
-    cycles = orc.gamg(s, psi, tol=TOL, rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=2,
-                      nPostSweeps=2).nIterations
-    samples = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_reference_sample(s, cycles_hint=cycles)
-        if i >= args.warmup:
-            samples.append(r)
-    v = statistics.median([r["value"] for r in samples])
+    import multiprocessing as mp
+    import shutil
+    import tempfile
+    tmp = tempfile.mkdtemp(prefix="cfx_ref_")
+    try:
+        path = os.path.join(tmp, "case.npz")
+        t0 = time.perf_counter()
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--write-case", path, "--n", str(args.n)],
+                       check=True)
+        t_case = time.perf_counter() - t0
+        case_bytes = os.path.getsize(path)
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        # a solve holds the case, the agglomeration and coarse levels and its
+        # vectors: 4.3x the case file measured at 128^3; budget 5x per process
+        # and at most half the free host memory
+        per_proc = 5 * case_bytes
+        fit = max(1, int(0.5 * _mem_available() // per_proc)) if _mem_available() else 1
+        nsteps = args.warmup + args.steps
+        procs = max(1, min(cores, nsteps, fit))
+        ctx = mp.get_context("spawn")
+        t0 = time.perf_counter()
+        with ctx.Pool(procs) as pool:
+            res = pool.starmap(reference_step, [(path, i) for i in range(nsteps)])
+        wall = time.perf_counter() - t0
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    timed = [r for r in res if r["step"] >= args.warmup]
+    v = statistics.median(r["s"] for r in timed)
+    sample = (f"oracle/ldu_oracle.c GAMG (serial C restatement of GAMGSolver, bit-exact with the reference "
+              f"built from source; -O3 with the reference's flags): each of the {nsteps} steps is one complete "
+              f"solve from psi=0 to 1e-8 at {args.n}^3, run {procs} at a time on {cores} host cores "
+              f"(value = median of the {len(timed)} timed steps; {wall:.0f} s wall); the reference is serial "
+              f"(no MPI on this host)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": workload(args.n),
-            "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
-                             "sample": "oracle/ldu_oracle.c GAMG (serial C restatement of GAMGSolver, "
-                                       "bit-exact with the reference built from source): agglomeration + "
-                                       f"1 and 2 V-cycles at {args.n}^3, extrapolated to "
-                                       f"the {samples[-1]['cycles']} V-cycles of the full solve (counted by "
-                                       "one full serial solve before the timed steps); the reference is "
-                                       "serial (no MPI on this host)"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "detail": samples[-1]}
+            "detail": {"steps": res, "case_write_s": t_case, "concurrent_processes": procs,
+                       "wall_s": wall, "min_s": min(r["s"] for r in timed), "max_s": max(r["s"] for r in timed),
+                       "iterations": sorted({r["iterations"] for r in res}),
+                       "converged": all(r["converged"] for r in res)}}
     print(json.dumps(line), flush=True)
     return 0
 
 
+def gs_sweeps(level):
+    """Gauss-Seidel sweeps of a V-cycle smoothing on a level (0 = the mesh):
+    nFinestSweeps 2 on the finest; nPre/PostSweeps 2 plus one per coarser
+    level, at most 4 (GAMGSolver.C:70-80, GAMGSolverSolve.C)."""
+    return 2 if level == 0 else min(2 + (level - 1), 4)
+
+
+def gs_bytes(N, F, s=8):
+    """Algorithmic bytes of one Gauss-Seidel sweep: 7sN + sF + 4F + 4N."""
+    return 7 * s * N + s * F + 4 * F + 4 * N
+
+
+def level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells):
+    """Every GAMG level's smoothing timed alone (FP64, the V-cycle's sweep
+    count): each coarse level's matrix, assembled on the device, read back
+    and swept through its own cfx_smooth, CUDA events on the library's
+    stream.  Returns one row per level with its algorithmic bytes and GB/s."""
+    import torch
+    from openfoam_dev_gb300 import ldu
+    rows = []
+    nc_prev, nf_prev = N, F
+    levels = [(0, N, F, None, None)]
+    for i in range(mesh.n_levels()):
+        _, _, _, nc, ncf, cl, cu = mesh.level(i, nc_prev, nf_prev)
+        levels.append((i + 1, nc, ncf, cl, cu))
+        nc_prev, nf_prev = nc, ncf
+    rng = np.random.default_rng(7)
+    for lv, nc, ncf, cl, cu in levels:
+        S = gs_sweeps(lv)
+        if lv == 0:
+            Al, ml = A, None
+        else:
+            d, up, _ = A.coarse(lv, nc, ncf)
+            ml = ldu.LduMesh(ctx, nc, cl, cu)
+            Al = ldu.LduMatrix(ml, d, up)
+        b = torch.from_numpy(rng.uniform(-1, 1, nc)).to(f"cuda:{local}")
+        x = torch.zeros_like(b)
+        t = ev_time(lambda: Al.smooth("GaussSeidel", x, b, S))
+        by = S * gs_bytes(nc, ncf)
+        rows.append({"level": lv, "cells": nc, "faces": ncf, "sweeps": S, "s": t, "algorithmic_bytes": by,
+                     "GB_s": by / t / 1e9, "form": "one CTA, vector in shared memory" if nc <= smem_cells
+                     else "persistent grid"})
+        if ml is not None:
+            Al.close()
+            ml.close()
+    return rows
+
+
 def run_ours(args, rank, world, local, pg):
+    # the oracle legs start first, in spawned processes, before any GPU call
+    cpu = not args.no_cpu_baseline and world == 1 and rank == 0
+    pool, jobs, outdir = None, {}, None
+    if cpu:
+        import multiprocessing as mp
+        import tempfile
+        outdir = tempfile.mkdtemp(prefix="cfx_oracle_")
+        pool = mp.get_context("spawn").Pool(2)
+        jobs["gamg"] = pool.apply_async(oracle_job, ("gamg", args.n, 1, outdir))
+        jobs["pcg"] = pool.apply_async(oracle_job, ("pcg", 64, 1, outdir))
+        jobs["bicgstab"] = pool.apply_async(oracle_job, ("bicgstab", 128, 1, outdir))
     import torch
     torch.cuda.set_device(local)
     ge.load_package()
@@ -232,6 +412,7 @@ def run_ours(args, rank, world, local, pg):
     N, F = s["diag"].size, s["l"].size
     d_src = torch.from_numpy(s["source"]).to(f"cuda:{local}")
     d_psi = torch.zeros_like(d_src)
+    torch.cuda.synchronize()
     mixed = ldu.solver_new("T", A, dict(GAMG, precision="mixed"))
     fp64 = ldu.solver_new("T", A, dict(GAMG, precision="FP64"))
 
@@ -264,8 +445,10 @@ def run_ours(args, rank, world, local, pg):
         t_mixed, p_mixed = timed(mixed, args.steps)
     launches = ctx.launch_count() - launches0
     torch.cuda.synchronize()
+    psi_mixed = d_psi.cpu().numpy()
     barrier(pg)
     t_fp64, p_fp64 = timed(fp64, args.steps)
+    psi_fp64 = d_psi.cpu().numpy()
     barrier(pg)
 
     # e2e: what a plugin does per fvMatrix::solve, host buffers (pinned)
@@ -282,32 +465,6 @@ def run_ours(args, rank, world, local, pg):
         if i >= args.warmup:
             e2e.append(dt)
 
-    # roofline of the largest single kernel: the fused 2-sweep Gauss-Seidel of
-    # the finest level (gather of b into slot order + the level-scheduled
-    # sweep), FP64, timed alone with events on the library's stream
-    d_b = d_src.clone()
-    d_x = torch.zeros_like(d_src)
-    A.smooth("GaussSeidel", d_x, d_b, 2)
-    torch.cuda.synchronize()
-    reps = 5
-    gs = []
-    for _ in range(reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        A.smooth("GaussSeidel", d_x, d_b, 2)
-        e1.record(stream)
-        gs.append((e0, e1))
-    torch.cuda.synchronize()
-    t_gs = statistics.median([a.elapsed_time(b) / 1e3 for a, b in gs])
-    # algorithmic bytes of one GS sweep (7sN + sF + 4F + 4N, s = 8): diag, b,
-    # psi read+write, bPrime, upper once, upperAddr, ownerStart
-    gs_bytes = 2 * (7 * 8 * N + 8 * F + 4 * F + 4 * N)
-
-    # the streaming kernels of the path (HBM-bound, no level chain), FP64 at
-    # the same size, each timed alone: Amul (3sN + sF + 8F), residual
-    # (4sN + sF + 8F), and a dot product (2sN)
-    d_y = torch.empty_like(d_src)
-
     def ev_time(fn, reps=5):
         fn()
         torch.cuda.synchronize()
@@ -321,13 +478,23 @@ def run_ours(args, rank, world, local, pg):
         torch.cuda.synchronize()
         return statistics.median([a.elapsed_time(b) / 1e3 for a, b in out])
 
+    # every level's smoothing alone (FP64): the dominant kernels by device
+    # time are the Gauss-Seidel sweeps of the agglomerated levels
+    smem_cells = ldu.tune_get(ldu.TUNE_SMEM_BYTES) // 8
+    levels = level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells)
+
+    # the streaming kernels of the path (HBM-bound, no level chain), FP64 at
+    # the same size, each timed alone: Amul (3sN + sF + 8F), residual
+    # (4sN + sF + 8F)
+    d_b = d_src.clone()
+    d_y = torch.empty_like(d_src)
     streaming = {
         "amul": (ev_time(lambda: A.Amul(d_b, d_y)), 3 * 8 * N + 8 * F + 8 * F),
         "residual": (ev_time(lambda: A.residual(d_b, d_src, d_y)), 4 * 8 * N + 8 * F + 8 * F),
     }
 
     assembly = fvm_assembly_measure(ctx, ev_time, stream, local) if world == 1 else None
-    krylov = krylov_configs(ctx, stream, local, cpu=not args.no_cpu_baseline) if world == 1 else None
+    krylov, krylov_psi = krylov_configs(ctx, stream, local) if world == 1 else (None, None)
 
     tm = reduce_max(pg, statistics.median(t_mixed))
     t64 = reduce_max(pg, statistics.median(t_fp64))
@@ -341,31 +508,48 @@ def run_ours(args, rank, world, local, pg):
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = gs_bytes / t_gs / 1e9
+    # roofline: the agglomerated levels' persistent-grid Gauss-Seidel sweeps
+    # (the largest share of device time), bytes and time summed over their
+    # launches = average bytes per launch / average launch time
+    dom = [r for r in levels if r["level"] > 0 and r["form"] == "persistent grid"]
+    dom_bytes = sum(r["algorithmic_bytes"] for r in dom)
+    dom_time = sum(r["s"] for r in dom)
+    achieved = dom_bytes / dom_time / 1e9
+    cycle_sweeps = 2 * sum(r["s"] for r in levels)  # pre and post smoothing per V-cycle
     traffic = None
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
-        traffic = tr.get(f"gs2_finest_{n}")
+        per_byte = tr.get("gs_coarse_dram_per_algorithmic_byte")
+        if per_byte:
+            traffic = per_byte * dom_bytes / max(len(dom), 1)
     except (OSError, ValueError):
         pass
+    for r in levels:
+        r["frac"] = r["GB_s"] / peak
     line = {"metric": METRIC, "value": tm, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tm * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-inner/f64-refined", "data": "synthetic (seeded)",
-            "config": dict(workload(n), parallelism="replicas" if world > 1 else "1 GPU"),
+            "config": workload(n), "parallelism": "replicas" if world > 1 else "1 GPU",
             "fp64_time_s": t64, "mixed_speedup": t64 / tm, "v_cycles_mixed": p_mixed.nIterations,
             "v_cycles_fp64": p_fp64.nIterations, "final_residual_mixed": p_mixed.finalResidual,
             "final_residual_fp64": p_fp64.finalResidual,
             "e2e": {"value": te, "unit": "s", "h2d_bytes_per_step": 8 * (N + F) + 16 * N,
                     "d2h_bytes_per_step": 8 * N},
             "gpu_launches": int(launches),
-            "streaming_kernels": {k: {"s": t, "algorithmic_bytes": b, "GB_s": b / t / 1e9,
-                                      "frac": b / t / 1e9 / float(peaks.get("hbm_gbs", 6800.0))}
+            "streaming_kernels": {k: {"s": t, "algorithmic_bytes": b, "GB_s": b / t / 1e9, "frac": b / t / 1e9 / peak}
                                   for k, (t, b) in streaming.items()},
-            "roofline": {"bound": "hbm", "kernel": "fused 2-sweep GaussSeidel, finest level (FP64)",
+            "roofline": {"bound": "hbm",
+                         "kernel": "Gauss-Seidel sweeps of the agglomerated GAMG levels, persistent grid form "
+                                   f"(FP64; levels {dom[0]['level']}-{dom[-1]['level']}, the V-cycle's sweep counts)"
+                         if dom else "none",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "algorithmic_bytes": gs_bytes, "launch_s": t_gs,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes / max(len(dom), 1),
+                         "launch_s": dom_time / max(len(dom), 1), "launches": len(dom),
                          "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "gamg_levels_fp64": levels,
+            "v_cycle_fp64_s": t64 / max(p_fp64.nIterations, 1),
+            "v_cycle_smoothing_fp64_s": cycle_sweeps,
             "clocks": clk.summary()}
     if assembly:
         assembly["frac"] = assembly["GB_s"] / peak
@@ -374,51 +558,49 @@ def run_ours(args, rank, world, local, pg):
         for v in krylov.values():
             v["FP64"]["frac"] = v["FP64"]["GB_s"] / peak
         line["krylov"] = krylov
-    if not args.no_cpu_baseline and world == 1:
-        r = cpu_reference_sample(s, cycles_hint=p_fp64.nIterations)
+    if cpu:
+        res = {k: j.get() for k, j in jobs.items()}
+        pool.close()
+        pool.join()
+        g = res["gamg"]
+        line["parity"] = parity_of(g, outdir, psi_fp64, p_fp64.nIterations, psi_mixed)
         line["cpu_baseline"] = {
-            "value": r["value"], "unit": "s", "cores": 1, "kind": "port",
-            "sample": f"oracle GAMG (serial C restatement, bit-exact with the reference build) at {n}^3: "
-                      f"agglomeration + 1 and 2 V-cycles timed, extrapolated to the {r['cycles']} V-cycles "
-                      f"of the FP64 solve ({r['sample_s']:.1f} s of CPU work)",
-            "detail": r}
+            "value": g["s"], "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"oracle GAMG (serial C restatement of GAMGSolver, bit-exact with the reference build, "
+                      f"-O3 with the reference's flags) at {n}^3: one complete solve from psi=0 to 1e-8 "
+                      f"({g['iterations']} V-cycles), timed directly, agglomeration ({g['agglomeration_s']:.1f} s, "
+                      f"cached per mesh as in the reference) excluded",
+            "detail": g}
+        if krylov:
+            for name, key in (("pcg_dic_64", "pcg"), ("pbicgstab_dilu_128", "bicgstab")):
+                r = res[key]
+                k = krylov[name]
+                k["parity"] = parity_of(r, outdir, krylov_psi[name]["FP64"], k["FP64"]["iterations"],
+                                        krylov_psi[name]["mixed"])
+                k["cpu_baseline"] = {"value": r["s"], "unit": "s", "cores": 1, "kind": "port",
+                                     "iterations": r["iterations"],
+                                     "sample": "oracle, one complete solve to 1e-8, timed directly"}
+                k["speedup_fp64_vs_cpu"] = r["s"] / k["FP64"]["s"]
+        import shutil
+        shutil.rmtree(outdir, ignore_errors=True)
     if world == 1 and args.workload == "all":
         line.update(run_batch_serve(args, local, True, True))
     print(json.dumps(line), flush=True)
     return 0
 
 
-def krylov_cpu_sample(s, solver, iterations):
-    """The oracle (serial C restatement, bit-exact with the reference build)
-    on the same system: PCG+DIC to convergence, PBiCGStab+DILU for 10
-    iterations extrapolated to the GPU FP64 solve's count (one Grace core)."""
-    from oracle import oracle as orc
-    psi = np.zeros_like(s["source"])
-    if solver == "PCG":
-        t0 = time.perf_counter()
-        p = orc.pcg(s, psi, tol=1e-8, max_iter=2000, precond="DIC")
-        t = time.perf_counter() - t0
-        return {"value": t, "unit": "s", "cores": 1, "kind": "port", "iterations": p.nIterations,
-                "sample": "oracle PCG+DIC, full solve to 1e-8"}
-    k = 10
-    t0 = time.perf_counter()
-    orc.pbicgstab(s, psi, tol=1e-30, max_iter=k, precond="DILU")
-    t = time.perf_counter() - t0
-    return {"value": t * iterations / k, "unit": "s", "cores": 1, "kind": "port", "iterations": iterations,
-            "sample": f"oracle PBiCGStab+DILU, {k} iterations ({t:.2f} s) extrapolated to {iterations}"}
-
-
-def krylov_configs(ctx, stream, local, reps=3, cpu=True):
+def krylov_configs(ctx, stream, local, reps=3):
     """The Krylov configurations: PCG+DIC on the uniform 64^3 cube and
     PBiCGStab+DILU on the 128^3 jittered, permuted-then-CM-renumbered upwind
     system, each to 1e-8 in FP64 and FP32-inner/FP64-refined, resident
     vectors, CUDA events on the library's stream (median of reps).  GB/s:
     the per-iteration algorithmic bytes (PCG+DIC 23sN + 3sF + 24F,
     PBiCGStab+DILU 41sN + 8sF + 56F, s = 8) times the iterations, over the
-    solve time."""
+    solve time.  Returns the measurements and each precision's solution
+    (host arrays, for the parity against the oracle)."""
     import torch
     from openfoam_dev_gb300 import cases, ldu
-    out = {}
+    out, sols = {}, {}
     for name, s, ctl, per_iter in (
             ("pcg_dic_64", cases.pcg_cube(64, seed=1),
              {"solver": "cudaPCG", "preconditioner": "DIC", "tolerance": 1e-8, "relTol": 0, "maxIter": 2000},
@@ -433,6 +615,7 @@ def krylov_configs(ctx, stream, local, reps=3, cpu=True):
         src = torch.from_numpy(s["source"]).to(f"cuda:{local}")
         psi = torch.zeros_like(src)
         res = {"cells": N, "faces": F, "bytes_per_iteration": per_iter(N, F)}
+        sols[name] = {}
         for prec in ("FP64", "mixed"):
             sol = ldu.solver_new("x", A, dict(ctl, precision=prec))
             ts, perf = [], None
@@ -447,18 +630,16 @@ def krylov_configs(ctx, stream, local, reps=3, cpu=True):
                 if r:
                     ts.append(e0.elapsed_time(e1) / 1e3)
             t = statistics.median(ts)
+            sols[name][prec] = psi.cpu().numpy()
             res[prec] = {"s": t, "iterations": perf.nIterations, "final_residual": perf.finalResidual,
                          "converged": bool(perf.converged)}
             if prec == "FP64":
                 res[prec]["GB_s"] = per_iter(N, F) * perf.nIterations / t / 1e9
         res["mixed_speedup"] = res["FP64"]["s"] / res["mixed"]["s"]
-        if cpu:
-            res["cpu_baseline"] = krylov_cpu_sample(s, "PCG" if name.startswith("pcg") else "PBiCGStab",
-                                                    res["FP64"]["iterations"])
         out[name] = res
         A.close()
         mesh.close()
-    return out
+    return out, sols
 
 
 def fvm_assembly_measure(ctx, ev_time, stream, local, n=128):
@@ -594,14 +775,46 @@ def run_batch_serve(args, local, want_batch, want_serve):
 
 
 def run_kernel_only(args):
-    """The finest-level fused 2-sweep GaussSeidel alone, warmup + steps times."""
+    """One Gauss-Seidel smoothing alone, warmup + steps times (for profiling
+    under ncu): gs = the finest level's fused 2 sweeps, level1 = the first
+    agglomerated level's (the persistent grid form, the V-cycle's 2 sweeps)."""
     import torch
     ge.load_package()
     from openfoam_dev_gb300 import cases, ldu
     s = cases.gamg_cube(args.n, jitter=0.2, seed=1)
     mesh, A = ldu.system_matrix(s)
-    d_b = torch.from_numpy(s["source"]).cuda()
+    N, F = s["diag"].size, s["l"].size
+    if args.kernel_only == "solves":
+        mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=10)
+        d_src = torch.from_numpy(s["source"]).cuda()
+        d_psi = torch.zeros_like(d_src)
+        torch.cuda.synchronize()
+        sol = {p: ldu.solver_new("T", A, dict(GAMG, precision=p)) for p in ("FP64", "mixed")}
+        out = {}
+        for prof in (False, True):
+            if prof:
+                torch.cuda.nvtx.range_push("profiled")
+            for p in ("FP64", "mixed"):
+                d_psi.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                perf = sol[p].solve(d_psi, d_src)
+                out[p] = {"s": time.perf_counter() - t0, "v_cycles": perf.nIterations}
+            if prof:
+                torch.cuda.synchronize()
+                torch.cuda.nvtx.range_pop()
+        print(json.dumps({"kernel": "solves", "n": args.n, **out}), flush=True)
+        return 0
+    if args.kernel_only == "level1":
+        mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=10)
+        _, _, _, nc, ncf, cl, cu = mesh.level(0, N, F)
+        d, up, _ = A.coarse(1, nc, ncf)
+        mesh = ldu.LduMesh(mesh.ctx, nc, cl, cu)
+        A = ldu.LduMatrix(mesh, d, up)
+        N, F = nc, ncf
+    d_b = torch.from_numpy(np.random.default_rng(7).uniform(-1, 1, N)).cuda()
     d_x = torch.zeros_like(d_b)
+    torch.cuda.synchronize()
     t = []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
@@ -610,12 +823,16 @@ def run_kernel_only(args):
         torch.cuda.synchronize()
         if i >= args.warmup:
             t.append(time.perf_counter() - t0)
-    print(json.dumps({"kernel": "gs2_finest", "n": args.n, "s": statistics.median(t)}), flush=True)
+    print(json.dumps({"kernel": args.kernel_only, "n": args.n, "cells": N, "faces": F,
+                      "algorithmic_bytes": 2 * gs_bytes(N, F), "s": statistics.median(t)}), flush=True)
     return 0
 
 
 def main():
     args = parse()
+    if args.write_case:
+        write_case(args.write_case, args.n)
+        return 0
     if args.kernel_only:
         return run_kernel_only(args)
     rank, world, local, pg = dist()

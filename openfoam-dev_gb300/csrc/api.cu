@@ -518,28 +518,58 @@ DevSched upload_sched(Arena& ar, cudaStream_t s, const HostSched& h) {
     d.waveOk = h.waveOk ? 1 : 0;
     d.sync = ar.get<int>(2 + std::max(h.nLevels, 1));
     CK(cudaMemsetAsync(d.sync, 0, sizeof(int) * (2 + std::max(h.nLevels, 1)), s));
+    if (h.tiled) {
+        d.tiled = 1;
+        d.nTiles = h.nTiles;
+        d.nSegs = h.nSegs;
+        d.grid = h.grid;
+        d.maxTileCells = h.maxTileCells;
+        d.pubEvery = h.pubEvery;
+        d.nChunks = h.grid;  // dot partials: one per CTA
+        d.tileSeg = ar.upload(h.tileSeg, s);
+        d.segGroup = ar.upload(h.segGroup, s);
+        d.segWait = ar.upload(h.segWait, s);
+        d.waitTile = ar.upload(h.waitTile, s);
+        d.waitNeed = ar.upload(h.waitNeed, s);
+        d.ctaTile = ar.upload(h.ctaTile, s);
+        d.ctaTiles = ar.upload(h.ctaTiles, s);
+        d.slotLocal = ar.upload(h.slotLocal, s);
+        d.progress = ar.get<int>(std::max(h.nTiles, 1));
+        d.seen = ar.get<int>(std::max<size_t>(size_t(h.grid) * h.nTiles, 1));
+    }
     return d;
+}
+
+// A level's schedule: tiled when its vector does not fit one CTA's shared
+// memory (and the tile form is on), else level-ordered.  A tile holds at
+// most the FP64 values that fit that shared memory, and a band of levels has
+// at most as many tiles as CTAs can be resident.
+DevSched build_and_upload(cfx_mesh* mesh, int lv, int kind, int S) {
+    const HostLevel& hl = mesh->host[lv];
+    cudaStream_t s = mesh->ctx->stream;
+    HostSched h;
+    const size_t cap = sweep_smem_cap();
+    const bool tiled = sweep_tile() && cap >= 256 * sizeof(double) && size_t(hl.n) * sizeof(double) > cap &&
+                       build_sched_tiled(hl, kind, S, int(cap / sizeof(double)), sweep_tile_ctas(),
+                                         sweep_tile_pub(), h);
+    if (!tiled) build_sched(hl, kind, S, h, sweep_wave() != 0);
+    return upload_sched(mesh->schedArena, s, h);
 }
 
 // Schedule of level lv (kind SCHED_*, S combined Gauss-Seidel sweeps).
 const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     if ((int)mesh->sched.size() < (int)mesh->host.size()) mesh->sched.resize(mesh->host.size());
     cfx_mesh::Scheds& sc = mesh->sched[lv];
-    cudaStream_t s = mesh->ctx->stream;
     if (kind == SCHED_FWD) {
         if (!sc.hasFwd) {
-            HostSched h;
-            build_sched(mesh->host[lv], SCHED_FWD, 1, h, sweep_wave() != 0);
-            sc.fwd = upload_sched(mesh->schedArena, s, h);
+            sc.fwd = build_and_upload(mesh, lv, SCHED_FWD, 1);
             sc.hasFwd = true;
         }
         return sc.fwd;
     }
     if (kind == SCHED_BWD) {
         if (!sc.hasBwd) {
-            HostSched h;
-            build_sched(mesh->host[lv], SCHED_BWD, 1, h, sweep_wave() != 0);
-            sc.bwd = upload_sched(mesh->schedArena, s, h);
+            sc.bwd = build_and_upload(mesh, lv, SCHED_BWD, 1);
             sc.hasBwd = true;
         }
         return sc.bwd;
@@ -547,14 +577,9 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     // Gauss-Seidel schedules by sweep count; key -1 = the backward pass
     if (kind == SCHED_GSB) S = -1;
     auto it = sc.gs.find(S);
-    if (it == sc.gs.end()) {
-        HostSched h;
-        if (S < 0)
-            build_sched(mesh->host[lv], SCHED_GSB, 1, h, sweep_wave() != 0);
-        else
-            build_sched(mesh->host[lv], SCHED_GS, S, h, sweep_wave() != 0);
-        it = sc.gs.emplace(S, upload_sched(mesh->schedArena, s, h)).first;
-    }
+    if (it == sc.gs.end())
+        it = sc.gs.emplace(S, S < 0 ? build_and_upload(mesh, lv, SCHED_GSB, 1)
+                                    : build_and_upload(mesh, lv, SCHED_GS, S)).first;
     return it->second;
 }
 
@@ -2238,6 +2263,14 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16) return CFX_ERR_ARG;
             set_sweep_cluster_pre(value);
             return CFX_OK;
+        case CFX_TUNE_TILE:
+            if (value > 1) return CFX_ERR_ARG;
+            set_sweep_tile(value);
+            return CFX_OK;
+        case CFX_TUNE_TILE_PUBLISH:
+            if (value < 1 || value > 64) return CFX_ERR_ARG;
+            set_sweep_tile_pub(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2252,6 +2285,8 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
         case CFX_TUNE_SMEM_BYTES: *value = int(sweep_smem_cap()); return CFX_OK;
         case CFX_TUNE_GRID_WAVE: *value = sweep_wave(); return CFX_OK;
+        case CFX_TUNE_TILE: *value = sweep_tile(); return CFX_OK;
+        case CFX_TUNE_TILE_PUBLISH: *value = sweep_tile_pub(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2369,6 +2404,35 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);
         return stc ? cfx_status(stc) : CFX_OK;
+    });
+}
+
+cfx_status cfx_sched_tiled_check(int nCells, int nFaces, const int32_t* l, const int32_t* u, int kind, int nSweeps,
+                                 int tileCells, int maxCtas, int pubEvery, int32_t* stats) {
+    if (nCells < 1 || nFaces < 0 || (nFaces && (!l || !u)) || kind < SCHED_FWD || kind > SCHED_GSB || !stats)
+        return CFX_ERR_ARG;
+    return guard([&]() -> cfx_status {
+        HostLevel h;
+        CFX_TRY(build_host_level(nCells, nFaces, l, u, h, true));
+        HostSched o;
+        if (!build_sched_tiled(h, kind, nSweeps, tileCells, maxCtas, pubEvery, o)) {
+            set_error("cfx_sched_tiled_check: the levels are too wide for the tiles");
+            return CFX_ERR_STATE;
+        }
+        std::string why;
+        if (!check_sched_tiled(h, o, why)) {
+            set_error("cfx_sched_tiled_check: " + why);
+            return CFX_ERR_STATE;
+        }
+        stats[0] = o.nTiles;
+        stats[1] = o.grid;
+        stats[2] = o.nSegs;
+        stats[3] = o.maxTileCells;
+        stats[4] = int32_t(o.waitTile.size());
+        stats[5] = int32_t(o.cell.size());
+        stats[6] = o.nLevels;
+        stats[7] = o.maxK;
+        return CFX_OK;
     });
 }
 

@@ -37,6 +37,16 @@
 //                 Launched cooperatively so all CTAs are resident.  A wait
 //                 that exceeds its deadline sets the abort flag and an error
 //                 status; every CTA then returns.
+//   sweep_tile_k  persistent CTAs on a tiled schedule (build_sched_tiled):
+//                 each tile (a band of levels x a range of cells) runs on
+//                 one CTA level by level with block barriers, the values it
+//                 produces held in shared memory; values of other tiles are
+//                 read from global memory after waiting for the producing
+//                 tile's published progress (cached per CTA, so a wait that
+//                 is already satisfied costs nothing).  Most dependencies
+//                 stay inside a CTA, and the cross-CTA ones are pipelined
+//                 instead of paid at every level.  Launched cooperatively;
+//                 waits bounded like the grid form's.
 
 #include <cooperative_groups.h>
 
@@ -54,6 +64,7 @@ constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
 constexpr int GRID_NT = 256;                            // 8 warps = one chunk
 constexpr int CTA_NT = 256;
 constexpr int CL_NT = 256;                              // threads per cluster CTA
+constexpr int TILE_NT = 512;                            // threads per tile CTA
 constexpr int PF_SMALL = 8, PF_LARGE = 16, PF_GRID_XL = 32;  // entries held in registers per slot
 namespace cg = cooperative_groups;
 
@@ -68,6 +79,9 @@ int g_wave_grid[2][8][3];   // resident CTAs of sweep_wave_k, the same
 int g_wave = 0;             // grid form: wavefront (1) or whole-level counters (0, default)
 size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
+int g_tile = 0;             // build large schedules tiled (the tile form)
+int g_tile_pub = 2;         // tile form: progress published every this many levels
+int g_tile_ctas = 152;      // tile CTAs that can be resident at once
 
 template <class T>
 struct SweepCtx {
@@ -517,6 +531,163 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
     }
 }
 
+// Tile form.  Shared memory: the tile's values at tile-local indices.  Each
+// CTA keeps, in its own row of s.seen (global memory, touched by its warp 0
+// only), the progress it has observed of every tile, its own tiles' final
+// counts included.  Warp 0 does the waits for the next level before the
+// level barrier, which also votes on the abort: every thread leaves at the
+// same barrier.
+template <class T>
+__host__ __device__ __forceinline__ size_t tile_x_bytes(int maxTileCells) {
+    return (sizeof(T) * size_t(maxTileCells > 0 ? maxTileCells : 1) + 15) & ~size_t(15);
+}
+
+template <class T, int OP, int PF>
+__global__ void __launch_bounds__(TILE_NT, 1) sweep_tile_k(DevSched s, SweepCtx<T> a, int* status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double sh[TILE_NT / 32];
+    if (a.done && *a.done) return;
+    T* X = reinterpret_cast<T*>(smem_raw);
+    int* seen = s.seen + size_t(blockIdx.x) * s.nTiles;
+    for (int i = threadIdx.x; i < s.nTiles; i += TILE_NT) seen[i] = 0;
+    int* abortf = s.sync;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int NW = TILE_NT / 32;
+    double dot = 0.0;
+    __syncthreads();
+    // warp 0: wait until every tile segment q reads from has published
+    auto wait_seg = [&](int q) -> bool {
+        bool ok = true;
+        for (int k = s.segWait[q] + lane; k < s.segWait[q + 1]; k += 32) {
+            const int p = s.waitTile[k], need = s.waitNeed[k];
+            if (seen[p] >= need) continue;
+            uint64_t t0 = 0;
+            unsigned spins = 0;
+            int v;
+            while ((v = ld_acquire(s.progress + p)) < need) {
+                if ((++spins & 63u) == 0) {
+                    if (*(volatile int*)abortf) {
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t t = globaltimer_ns();
+                    if (t0 == 0) {
+                        t0 = t;
+                    } else if (t - t0 > a.timeoutNs) {
+                        atomicExch(abortf, 1);
+                        atomicExch(status, int(CFX_ERR_TIMEOUT));
+                        ok = false;
+                        break;
+                    }
+                }
+            }
+            if (!ok) break;
+            seen[p] = v;
+        }
+        return ok;
+    };
+    auto xat = [&](int e) -> T { return e >= 0 ? X[e] : ldcg(a.x + (-e - 1)); };
+    for (int ti = s.ctaTile[blockIdx.x]; ti < s.ctaTile[blockIdx.x + 1]; ++ti) {
+        const int t = s.ctaTiles[ti];
+        const int q0 = s.tileSeg[t], q1 = s.tileSeg[t + 1];
+        // header of this warp's first group in segment q (and the slot's
+        // tile-local index), issued two levels ahead
+        auto hdr = [&](int q, SlotRegs<T, PF>& r, int& loc) {
+            int g = 0;
+            bool okg = false;
+            if (q < q1) {
+                g = s.segGroup[q] + w;
+                okg = g < s.segGroup[q + 1];
+            }
+            load_header<T, OP, PF>(s, a, g, okg, lane, r);
+            loc = okg ? s.slotLocal[g * 32 + lane] : 0;
+        };
+        bool ok = true;
+        if (w == 0) ok = wait_seg(q0);
+        if (!__syncthreads_and(ok)) return;
+        // one entry set (the level being computed, then refilled with the
+        // next level's before the barrier) and two headers in flight
+        SlotRegs<T, PF> E;
+        SlotRegs<T, 1> H;  // header of level q + 1 (only its header fields are used)
+        int locE = 0, locH = 0;
+        {
+            SlotRegs<T, PF> tmp;
+            hdr(q0, E, locE);
+            load_entries<T, PF>(s, a.coef, E);
+            hdr(q0 + 1, tmp, locH);
+            H.c = tmp.c;
+            H.n = tmp.n;
+            H.e0 = tmp.e0;
+            H.sc = tmp.sc;
+            H.in = tmp.in;
+        }
+        for (int q = q0; q < q1; ++q) {
+            if (E.c >= 0) {
+                T acc = sw_init<OP>(E.sc, E.in, OP == OP_BWD ? ldcg(a.x + E.c) : T(0));
+#pragma unroll
+                for (int k = 0; k < PF; ++k)
+                    if (k < E.n) acc = sw_step<OP>(acc, E.cf[k], xat(E.nbr[k]));
+                acc = tail_entries<T, OP>(s, a.coef, E.e0, PF, E.n, acc, xat);
+                const T v = sw_fini<OP>(acc, E.sc);
+                X[locE] = v;
+                a.x[E.c] = v;
+                if (a.dotWith) dot += double(v) * double(a.dotWith[E.c]);
+            }
+            // further groups of this warp in a wide level, loaded directly
+            for (int g = s.segGroup[q] + w + NW; g < s.segGroup[q + 1]; g += NW) {
+                const int slot = g * 32 + lane;
+                const int c = s.cell[slot];
+                if (c < 0) continue;
+                const int cnt = s.cnt[slot];
+                const int e0 = s.groupEntry[g] + lane;
+                const T sc = a.scalar[slot];
+                const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+                T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
+                acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
+                const T v = sw_fini<OP>(acc, sc);
+                X[s.slotLocal[slot]] = v;
+                a.x[c] = v;
+                if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
+            }
+            // level q + 1: its header (issued a level ago) becomes current and
+            // its entries are issued now; the header of q + 2 is issued
+            E.c = H.c;
+            E.n = H.n;
+            E.e0 = H.e0;
+            E.sc = H.sc;
+            E.in = H.in;
+            locE = locH;
+            load_entries<T, PF>(s, a.coef, E);
+            {
+                SlotRegs<T, 1> tmp;
+                int g = 0;
+                bool okg = false;
+                if (q + 2 < q1) {
+                    g = s.segGroup[q + 2] + w;
+                    okg = g < s.segGroup[q + 3];
+                }
+                load_header<T, OP, 1>(s, a, g, okg, lane, tmp);
+                locH = okg ? s.slotLocal[g * 32 + lane] : 0;
+                H = tmp;
+            }
+            ok = true;
+            if (w == 0 && q + 1 < q1) ok = wait_seg(q + 1);
+            if (!__syncthreads_and(ok)) return;
+            if (threadIdx.x == 0) {
+                const int done = q - q0 + 1;
+                if (done % s.pubEvery == 0 || q + 1 == q1) {
+                    st_release(s.progress + t, done);
+                    seen[t] = done;
+                }
+            }
+        }
+    }
+    if (a.dotWith) {
+        dot = block_sum<TILE_NT>(dot, sh);
+        if (threadIdx.x == 0) a.partials[blockIdx.x] = dot;
+    }
+}
+
 // Right-hand side gathered into slot order, so the sweeps load it without
 // first loading the slot's cell index.
 template <class T>
@@ -565,7 +736,7 @@ inline int prec_index<double>() { return 0; }
 template <>
 inline int prec_index<float>() { return 1; }
 
-enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4 };
+enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4, M_TILE = 5 };
 
 // Execution form of a schedule: the vector in one CTA's shared memory, in a
 // cluster's distributed shared memory, or in global memory with a single CTA,
@@ -582,6 +753,7 @@ inline int cluster_of(const DevSched& s) {
 
 template <class T>
 int mode_of(const DevSched& s) {
+    if (s.tiled) return M_TILE;
     const size_t xbytes = sizeof(T) * size_t(s.n);
     if (xbytes <= g_smem_cap) return M_CTA;
     const int cs = cluster_of(s);
@@ -599,9 +771,41 @@ constexpr int pf_index(int pf) { return pf == PF_SMALL ? 0 : pf == PF_LARGE ? 1 
 template <class T, int OP, int PF>
 cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status);
 
+template <class T>
+size_t tile_smem_bytes(const DevSched& s) {
+    return tile_x_bytes<T>(s.maxTileCells);
+}
+
+// The tile form: one cooperative launch of s.grid CTAs (all resident), the
+// progress counters and the abort flag cleared first.
+template <class T, int OP, int PF>
+cfx_status launch_tile(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
+    const size_t smem = tile_smem_bytes<T>(s);
+    if (smem > g_smem_cap_max || s.grid > g_tile_ctas) {
+        set_error("tiled sweep: schedule exceeds the shared memory or the resident CTAs");
+        return CFX_ERR_STATE;
+    }
+    CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * 2, st));
+    CFX_CUDA(cudaMemsetAsync(s.progress, 0, sizeof(int) * size_t(s.nTiles), st));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(s.grid);
+    cfg.blockDim = dim3(TILE_NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_tile_k<T, OP, PF>, s, a, status));
+    count_launch();
+    return CFX_OK;
+}
+
 template <class T, int OP, int PF>
 cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
     if (s.nSlots == 0) return CFX_OK;
+    if (s.tiled) return launch_tile<T, OP, PF>(st, s, a, status);
     const size_t xbytes = sizeof(T) * size_t(s.n);
     const int cs = cluster_of(s);
     const int per = cs ? (s.n + cs - 1) / cs : 0;
@@ -706,6 +910,7 @@ void init_op_pf() {
     per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_wave_k<T, OP, PF>, GRID_NT, 0);
     g_wave_grid[prec_index<T>()][OP][pf_index(PF)] = g_num_sms * (per > 0 ? per : 1);
+    cudaFuncSetAttribute(sweep_tile_k<T, OP, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(g_smem_cap));
@@ -773,6 +978,14 @@ void sweeps_init(int numSms) {
     g_smem_cap_max = g_smem_cap;
     init_attrs<double>();
     init_attrs<float>();
+    // resident tile CTAs with a full shared-memory partition each
+    {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_tile_k<double, OP_GS, PF_LARGE>, TILE_NT,
+                                                      g_smem_cap);
+        g_tile_ctas = g_num_sms * (per > 0 ? per : 1);
+        cudaGetLastError();
+    }
     // The cluster forms are kept behind CFX_TUNE_CLUSTER_SIZE: on GB300 the
     // persistent grid form sweeps the mid-size levels faster (a cluster
     // barrier per level costs more than the grid's per-level counters).
@@ -801,6 +1014,11 @@ int wave_grid(const DevSched& s) {
 
 int sweep_wave() { return g_wave; }
 void set_sweep_wave(int on) { g_wave = on ? 1 : 0; }
+int sweep_tile() { return g_tile; }
+void set_sweep_tile(int on) { g_tile = on ? 1 : 0; }
+int sweep_tile_pub() { return g_tile_pub; }
+void set_sweep_tile_pub(int k) { g_tile_pub = k < 1 ? 1 : k; }
+int sweep_tile_ctas() { return g_tile_ctas; }
 
 template <class T>
 bool sweep_is_grid(const DevSched& s) {
@@ -810,6 +1028,7 @@ bool sweep_is_grid(const DevSched& s) {
 template <class T>
 int sweep_partials(const DevSched& s) {
     const int m = mode_of<T>(s);
+    if (m == M_TILE) return s.grid;
     if (m == M_GRID) return g_wave && s.waveOk ? wave_grid<T>(s) : s.nChunks;
     return (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) ? cluster_of(s) : 1;
 }
@@ -844,8 +1063,8 @@ cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>
 template <class T>
 cfx_status run_sweep_stalled(cudaStream_t st, const DevSched& s, const Packed<T>& p, const T* in, T* x,
                              unsigned long long timeoutNs, int* status) {
-    if (s.nLevels < 2 || s.nSlots == 0) {
-        set_error("stalled sweep: the schedule needs at least two levels");
+    if (s.nLevels < 2 || s.nSlots == 0 || s.tiled) {
+        set_error("stalled sweep: the schedule needs at least two levels (level-ordered, not tiled)");
         return CFX_ERR_ARG;
     }
     int blocks = (s.nSlots + 255) / 256;

@@ -13,6 +13,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libldu_oracle.so")
+# the same source built with the reference's optimisation flags (bit-identical
+# results; loaded instead of LIB when CFX_ORACLE_TIMED=1, by the timed CPU legs)
+LIB_TIMED = os.path.join(HERE, "_build", "libldu_oracle_timed.so")
 
 # FDIC (preconditioner and smoother) is DIC's arithmetic and
 # nonBlockingGaussSeidel without coupled interfaces is GaussSeidel's: the
@@ -72,9 +75,10 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            raise RuntimeError(f"{LIB} missing: run `make -C oracle`")
-        _lib = ctypes.CDLL(LIB)
+        path = LIB_TIMED if os.environ.get("CFX_ORACLE_TIMED") == "1" else LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} missing: run `make -C oracle`")
+        _lib = ctypes.CDLL(path)
         for name in ("ldu_sum", "ldu_sum_mag", "ldu_sum_sqr", "ldu_average"):
             getattr(_lib, name).restype = ctypes.c_double
         _lib.ldu_sum_prod.restype = ctypes.c_double

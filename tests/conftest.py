@@ -29,7 +29,8 @@ def _ensure_built():
     if not (os.path.exists(os.path.join(lib_dir, "libcudaLduSolvers.so"))
             and os.path.exists(os.path.join(lib_dir, "libcfxcase.so"))):
         importlib.import_module("openfoam_dev_gb300.build").build()
-    if not os.path.exists(os.path.join(REPO, "oracle", "_build", "libldu_oracle.so")):
+    if not all(os.path.exists(os.path.join(REPO, "oracle", "_build", f))
+               for f in ("libldu_oracle.so", "libldu_oracle_timed.so")):
         subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
 
 

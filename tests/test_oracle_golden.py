@@ -222,3 +222,36 @@ def test_cyclic_fvmatrix_solve_bit_exact(name):
     assert p.initialResidual == g["initialResidual"][0]
     assert p.finalResidual == g["finalResidual"][0]
     assert p.converged == bool(g["converged"][0])
+
+
+_TIMED_CHILD = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import __graft_entry__ as ge
+ge.load_package()
+from openfoam_dev_gb300 import cases
+from oracle import oracle as orc
+s = cases.gamg_cube(12, jitter=0.2, seed=4)
+psi = np.zeros_like(s["source"])
+p = orc.gamg(s, psi, tol=1e-10, rel_tol=0.0, smoother="GaussSeidel", nPreSweeps=2, nPostSweeps=2)
+t = cases.bicgstab_cube(10, seed=2)
+x = np.zeros_like(t["source"])
+q = orc.pbicgstab(t, x, tol=1e-10, precond="DILU")
+np.save(sys.argv[2], np.concatenate([psi, x, [p.nIterations, q.nIterations]]))
+"""
+
+
+def test_timed_oracle_build_is_bit_identical(tmp_path):
+    """The oracle built with the reference's optimisation flags (the one the
+    bench times) gives the same bits as the build the tests pin."""
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for timed in ("0", "1"):
+        f = str(tmp_path / f"r{timed}.npy")
+        env = dict(os.environ, CFX_ORACLE_TIMED=timed)
+        subprocess.run([sys.executable, "-c", _TIMED_CHILD, repo, f], env=env, check=True)
+        out[timed] = np.load(f)
+    np.testing.assert_array_equal(out["0"], out["1"])

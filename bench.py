@@ -65,6 +65,8 @@ def parse():
                     help="profiling: gs = the finest level's fused 2-sweep Gauss-Seidel alone, level1 = the "
                          "first agglomerated level's, solves = one FP64 and one mixed headline solve inside "
                          "the NVTX range 'profiled' (after one warm-up solve of each)")
+    ap.add_argument("--form", choices=["default", "grid", "flow"], default="default",
+                    help="profiling modes: the sweep form of the levels larger than one CTA")
     ap.add_argument("--write-case", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--workload", choices=["all", "gamg", "batch", "serve"], default="all",
                     help="all: the GAMG headline line with the batch and serving measurements added")
@@ -781,6 +783,8 @@ def run_kernel_only(args):
     import torch
     ge.load_package()
     from openfoam_dev_gb300 import cases, ldu
+    if args.form != "default":
+        ldu.tune_set(ldu.TUNE_FLOW, int(args.form == "flow"))
     s = cases.gamg_cube(args.n, jitter=0.2, seed=1)
     mesh, A = ldu.system_matrix(s)
     N, F = s["diag"].size, s["l"].size

@@ -315,16 +315,10 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
         * memory is swept there (default 16 where the GPU allows it: PCG+DIC
         * 64^3 1.5x faster than the grid form); 0 keeps the grid */
        CFX_TUNE_CLUSTER_PRE = 6,
-       /* 1: a mesh level whose vector does not fit one CTA's
-        * shared memory gets tiled schedules, swept by the tile form: each
-        * tile (a band of levels x a range of cells) on one CTA, its values
-        * in shared memory, waiting only on the tiles it reads from; 0
-        * (default): the level-ordered forms above.  Read when a schedule is first built
-        * (schedules are kept per mesh). */
-       CFX_TUNE_TILE = 7,
-       /* tile form: a tile publishes its progress every this many levels
-        * (default 2; 1..64) */
-       CFX_TUNE_TILE_PUBLISH = 8 };
+       CFX_TUNE_FLOW = 7,
+       /* dataflow form: warps launched for this many levels of the
+        * schedule's average width (default 4; 1..64) */
+       CFX_TUNE_FLOW_AHEAD = 8 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 
@@ -466,20 +460,6 @@ cfx_status cfx_smooth(cfx_matrix* mat, int kind, double* d_psi, const double* d_
  * overlap on the GPU race. */
 cfx_status cfx_reduce_noalloc(int which, int n, const double* d_a, const double* d_b, double* d_out,
                               void* stream);
-
-/* ---- schedule check (host only; no reference counterpart) ----------------
- * Builds the tiled form of a sweep schedule of the mesh (l, u) -- kind 0
- * forward (DIC/DILU), 1 backward, 2 Gauss-Seidel with nSweeps fused sweeps,
- * 3 the backward pass of symGaussSeidel -- with tiles of at most tileCells
- * cells, at most maxCtas tiles per band of levels and progress published
- * every pubEvery levels, and checks it against the sequential sweep: every
- * (sweep, cell) once, each cell's terms in the reference's order, every
- * value read either produced earlier in the same tile or waited for, every
- * wait on a lower tile (no deadlock with all CTAs resident).  stats[8]:
- * tiles, CTAs, segments, largest tile (cells), waits, slots, levels, largest
- * entry count.  CFX_ERR_STATE with the reason when a check fails. */
-cfx_status cfx_sched_tiled_check(int nCells, int nFaces, const int32_t* l, const int32_t* u, int kind, int nSweeps,
-                                 int tileCells, int maxCtas, int pubEvery, int32_t* stats);
 
 /* ---- diagnostics (no reference counterpart) -------------------------------
  * Exercises the failure path of the bounded device waits without any fault:

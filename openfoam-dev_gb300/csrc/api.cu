@@ -514,46 +514,20 @@ DevSched upload_sched(Arena& ar, cudaStream_t s, const HostSched& h) {
     d.levelChunks = ar.upload(h.levelChunks, s);
     d.depStart = ar.upload(h.depStart, s);
     d.dep = ar.upload(h.dep, s);
+    d.slotSweep = ar.upload(h.slotSweep, s);
+    d.slotLower = ar.upload(h.slotLower, s);
     d.gdone = ar.get<int>(std::max(d.nGroups, 1));
     d.waveOk = h.waveOk ? 1 : 0;
     d.sync = ar.get<int>(2 + std::max(h.nLevels, 1));
     CK(cudaMemsetAsync(d.sync, 0, sizeof(int) * (2 + std::max(h.nLevels, 1)), s));
-    if (h.tiled) {
-        d.tiled = 1;
-        d.nTiles = h.nTiles;
-        d.nSegs = h.nSegs;
-        d.grid = h.grid;
-        d.maxTileCells = h.maxTileCells;
-        d.pubEvery = h.pubEvery;
-        d.nChunks = h.grid;  // dot partials: one per CTA
-        d.tileSeg = ar.upload(h.tileSeg, s);
-        d.segGroup = ar.upload(h.segGroup, s);
-        d.segWait = ar.upload(h.segWait, s);
-        d.waitTile = ar.upload(h.waitTile, s);
-        d.waitNeed = ar.upload(h.waitNeed, s);
-        d.ctaTile = ar.upload(h.ctaTile, s);
-        d.ctaTiles = ar.upload(h.ctaTiles, s);
-        d.slotLocal = ar.upload(h.slotLocal, s);
-        d.progress = ar.get<int>(std::max(h.nTiles, 1));
-        d.seen = ar.get<int>(std::max<size_t>(size_t(h.grid) * h.nTiles, 1));
-    }
     return d;
 }
 
-// A level's schedule: tiled when its vector does not fit one CTA's shared
-// memory (and the tile form is on), else level-ordered.  A tile holds at
-// most the FP64 values that fit that shared memory, and a band of levels has
-// at most as many tiles as CTAs can be resident.
+// A level's schedule, built on first use and kept with the mesh.
 DevSched build_and_upload(cfx_mesh* mesh, int lv, int kind, int S) {
-    const HostLevel& hl = mesh->host[lv];
-    cudaStream_t s = mesh->ctx->stream;
     HostSched h;
-    const size_t cap = sweep_smem_cap();
-    const bool tiled = sweep_tile() && cap >= 256 * sizeof(double) && size_t(hl.n) * sizeof(double) > cap &&
-                       build_sched_tiled(hl, kind, S, int(cap / sizeof(double)), sweep_tile_ctas(),
-                                         sweep_tile_pub(), h);
-    if (!tiled) build_sched(hl, kind, S, h, sweep_wave() != 0);
-    return upload_sched(mesh->schedArena, s, h);
+    build_sched(mesh->host[lv], kind, S, h, sweep_wave() != 0);
+    return upload_sched(mesh->schedArena, mesh->ctx->stream, h);
 }
 
 // Schedule of level lv (kind SCHED_*, S combined Gauss-Seidel sweeps).
@@ -605,6 +579,8 @@ Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd) {
         p->scalar = mat->arena.get<T>(sd.nSlots);
         p->inS = mat->arena.get<T>(sd.nSlots);
     }
+    const size_t fv = sweep_flow_values(sd, op);
+    if (fv && !p->flow) p->flow = mat->arena.get<T>(fv);
     return *p;
 }
 
@@ -620,6 +596,8 @@ Packed<T>& packedT(cfx_matrix* mat, int lv, int op, const DevSched& sd) {
         p->scalar = mat->arena.get<T>(sd.nSlots);
         p->inS = mat->arena.get<T>(sd.nSlots);
     }
+    const size_t fv = sweep_flow_values(sd, op);
+    if (fv && !p->flow) p->flow = mat->arena.get<T>(fv);
     return *p;
 }
 
@@ -653,7 +631,10 @@ void compute_rD(cfx_matrix* mat, int lv) {
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
     const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
-    ensure_chunk_partials(ctx, std::max(f.nChunks, b.nChunks));
+    // dot partials of the fused backward sweep: one per chunk or per
+    // dataflow CTA, whichever form runs
+    ensure_chunk_partials(ctx, std::max({size_t(f.nChunks), size_t(b.nChunks), size_t(sweep_partials<T>(b)),
+                                         size_t(sweep_partials<T>(f))}));
     Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f);
     pack_sweep<T>(s, f, OP_RD, c, prd);
     if (run_sweep<T>(s, f, OP_RD, prd, nullptr, c.rD, nullptr, nullptr, nullptr, ctx->d_status) != CFX_OK)
@@ -821,7 +802,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1315,7 +1296,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2263,13 +2244,13 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16) return CFX_ERR_ARG;
             set_sweep_cluster_pre(value);
             return CFX_OK;
-        case CFX_TUNE_TILE:
-            if (value > 1) return CFX_ERR_ARG;
-            set_sweep_tile(value);
+        case CFX_TUNE_FLOW:
+            if (value > 2) return CFX_ERR_ARG;
+            set_sweep_flow(value);
             return CFX_OK;
-        case CFX_TUNE_TILE_PUBLISH:
+        case CFX_TUNE_FLOW_AHEAD:
             if (value < 1 || value > 64) return CFX_ERR_ARG;
-            set_sweep_tile_pub(value);
+            set_sweep_flow_ahead(value);
             return CFX_OK;
         default: return CFX_ERR_ARG;
     }
@@ -2285,8 +2266,8 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_BATCH_INNER_DIGITS: *value = batch_inner_digits(); return CFX_OK;
         case CFX_TUNE_SMEM_BYTES: *value = int(sweep_smem_cap()); return CFX_OK;
         case CFX_TUNE_GRID_WAVE: *value = sweep_wave(); return CFX_OK;
-        case CFX_TUNE_TILE: *value = sweep_tile(); return CFX_OK;
-        case CFX_TUNE_TILE_PUBLISH: *value = sweep_tile_pub(); return CFX_OK;
+        case CFX_TUNE_FLOW: *value = sweep_flow(); return CFX_OK;
+        case CFX_TUNE_FLOW_AHEAD: *value = sweep_flow_ahead(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2404,35 +2385,6 @@ cfx_status cfx_precondition(cfx_matrix* mat, int kind, int transpose, const doub
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);
         return stc ? cfx_status(stc) : CFX_OK;
-    });
-}
-
-cfx_status cfx_sched_tiled_check(int nCells, int nFaces, const int32_t* l, const int32_t* u, int kind, int nSweeps,
-                                 int tileCells, int maxCtas, int pubEvery, int32_t* stats) {
-    if (nCells < 1 || nFaces < 0 || (nFaces && (!l || !u)) || kind < SCHED_FWD || kind > SCHED_GSB || !stats)
-        return CFX_ERR_ARG;
-    return guard([&]() -> cfx_status {
-        HostLevel h;
-        CFX_TRY(build_host_level(nCells, nFaces, l, u, h, true));
-        HostSched o;
-        if (!build_sched_tiled(h, kind, nSweeps, tileCells, maxCtas, pubEvery, o)) {
-            set_error("cfx_sched_tiled_check: the levels are too wide for the tiles");
-            return CFX_ERR_STATE;
-        }
-        std::string why;
-        if (!check_sched_tiled(h, o, why)) {
-            set_error("cfx_sched_tiled_check: " + why);
-            return CFX_ERR_STATE;
-        }
-        stats[0] = o.nTiles;
-        stats[1] = o.grid;
-        stats[2] = o.nSegs;
-        stats[3] = o.maxTileCells;
-        stats[4] = int32_t(o.waitTile.size());
-        stats[5] = int32_t(o.cell.size());
-        stats[6] = o.nLevels;
-        stats[7] = o.maxK;
-        return CFX_OK;
     });
 }
 

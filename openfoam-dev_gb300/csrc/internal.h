@@ -269,20 +269,9 @@ struct HostSched {
     // form waits on exactly these
     std::vector<int> depStart, dep;
     bool waveOk = false;
-    // Tiled form (build_sched_tiled): slots ordered tile by tile, each tile's
-    // slots by level (a segment per level, whole groups of 32).  nb holds the
-    // tile-local index of the value read (>= 0, shared memory) or -(cell + 1)
-    // (global memory).  Tiles of one band of levels run on distinct CTAs;
-    // CTA j takes tile j of every band that has one, bands in order.
-    bool tiled = false;
-    int nTiles = 0, nSegs = 0, grid = 0, maxTileCells = 0, pubEvery = 1;
-    std::vector<int> tileSeg;            // [nTiles + 1] first segment of each tile
-    std::vector<int> segGroup;           // [nSegs + 1] first group of each segment
-    std::vector<int> segWait;            // [nSegs + 1] wait list of each segment (CSR)
-    std::vector<int> waitTile, waitNeed; // producer tile, its segments that must be done
-    std::vector<int> ctaTile;            // [grid + 1] CSR over ctaTiles: each CTA's tiles
-    std::vector<int> ctaTiles;
-    std::vector<int> slotLocal;          // [nSlots] tile-local index of the slot's cell
+    // per slot: its sweep (combined Gauss-Seidel schedules) and its number
+    // of lower-neighbour entries (the losort ones, first in its entries)
+    std::vector<int> slotSweep, slotLower;
 };
 
 struct DevSched {
@@ -296,12 +285,7 @@ struct DevSched {
     int *depStart = nullptr, *dep = nullptr;  // group dependencies (wavefront form)
     int* gdone = nullptr;                // [nGroups] group finished flags
     int waveOk = 0;                      // dependencies verified to point backwards
-    // tiled form (see HostSched)
-    int tiled = 0, nTiles = 0, nSegs = 0, grid = 0, maxTileCells = 0, pubEvery = 1;
-    int *tileSeg = nullptr, *segGroup = nullptr, *segWait = nullptr, *waitTile = nullptr, *waitNeed = nullptr;
-    int *ctaTile = nullptr, *ctaTiles = nullptr, *slotLocal = nullptr;
-    int* progress = nullptr;             // [nTiles] segments each tile has published
-    int* seen = nullptr;                 // [grid * nTiles] progress each CTA has observed
+    int *slotSweep = nullptr, *slotLower = nullptr;  // [nSlots] (level-ordered schedules)
 };
 
 // coefficients packed for one schedule and one operation
@@ -310,18 +294,12 @@ struct Packed {
     T* coef = nullptr;    // [nEntries]
     T* scalar = nullptr;  // [nSlots]
     T* inS = nullptr;     // [nSlots] right-hand side in slot order (scratch)
+    T* flow = nullptr;    // [nSweeps * n] the dataflow form's per-sweep values (scratch)
     bool valid = false;
 };
 
 // withDeps: also the group dependency lists of the wavefront form
 void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps);
-// The tiled form of the same schedule: tiles of at most tileCells distinct
-// cells, at most maxCtas tiles per band, progress published every pubEvery
-// segments.  Returns false (o untouched) when the levels are too wide.
-bool build_sched_tiled(const HostLevel& h, int kind, int nSweeps, int tileCells, int maxCtas, int pubEvery,
-                       HostSched& o);
-// Structural check of a tiled schedule (see host.cpp); false with a reason.
-bool check_sched_tiled(const HostLevel& h, const HostSched& o, std::string& why);
 
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {
@@ -355,12 +333,13 @@ size_t sweep_smem_cap();
 size_t sweep_smem_cap_max();
 int sweep_wave();
 void set_sweep_wave(int on);
-// tiled schedules (built for meshes whose vector does not fit one CTA)
-int sweep_tile();
-void set_sweep_tile(int on);
-int sweep_tile_pub();
-void set_sweep_tile_pub(int k);
-int sweep_tile_ctas();
+// dataflow sweeps (level-ordered schedules larger than one CTA)
+int sweep_flow();
+void set_sweep_flow(int on);
+int sweep_flow_ahead();
+void set_sweep_flow_ahead(int k);
+// the dataflow form's value buffers: sweeps x cells of the schedule (0: none)
+size_t sweep_flow_values(const DevSched& s, int op);
 void set_sweep_smem_cap(size_t b);
 int sweep_cluster_size();
 void set_sweep_cluster_size(int cs);

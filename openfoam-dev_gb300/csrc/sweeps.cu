@@ -37,20 +37,19 @@
 //                 Launched cooperatively so all CTAs are resident.  A wait
 //                 that exceeds its deadline sets the abort flag and an error
 //                 status; every CTA then returns.
-//   sweep_tile_k  persistent CTAs on a tiled schedule (build_sched_tiled):
-//                 each tile (a band of levels x a range of cells) runs on
-//                 one CTA level by level with block barriers, the values it
-//                 produces held in shared memory; values of other tiles are
-//                 read from global memory after waiting for the producing
-//                 tile's published progress (cached per CTA, so a wait that
-//                 is already satisfied costs nothing).  Most dependencies
-//                 stay inside a CTA, and the cross-CTA ones are pipelined
-//                 instead of paid at every level.  Launched cooperatively;
-//                 waits bounded like the grid form's.
+//   sweep_flow_k  dataflow: persistent warps take the level-ordered groups
+//                 round-robin; every value a sweep produces goes to a buffer
+//                 filled beforehand with a sentinel (all bits set, a NaN no
+//                 arithmetic produces), and a slot spins, with a bounded and
+//                 backed-off wait, on exactly the neighbour values it reads
+//                 until they are no longer the sentinel.  The value is its own
+//                 flag: no counters, release fences or block barriers, so a
+//                 dependency costs one store-to-load trip through L2.
 
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "device.cuh"
 #include "internal.h"
@@ -64,7 +63,6 @@ constexpr uint64_t SWEEP_TIMEOUT_NS = 2000000000ull;  // 2 s per wait
 constexpr int GRID_NT = 256;                            // 8 warps = one chunk
 constexpr int CTA_NT = 256;
 constexpr int CL_NT = 256;                              // threads per cluster CTA
-constexpr int TILE_NT = 512;                            // threads per tile CTA
 constexpr int PF_SMALL = 8, PF_LARGE = 16, PF_GRID_XL = 32;  // entries held in registers per slot
 namespace cg = cooperative_groups;
 
@@ -75,13 +73,13 @@ int g_cluster_avail = 0;    // largest cluster the GPU can hold (16 or 8; 0: non
 int g_small_threshold = 0;  // <= this many cells: single-CTA even without smem fit
 int g_cluster_global = 0;   // <= this many cells: one cluster with the vector in global memory
 int g_grid[2][8][3];        // resident CTAs of sweep_grid_k per (precision, op, PF 8/16/32)
+int g_flow_grid[2][4];      // resident CTAs of sweep_flow_k per (precision, op)
 int g_wave_grid[2][8][3];   // resident CTAs of sweep_wave_k, the same
 int g_wave = 0;             // grid form: wavefront (1) or whole-level counters (0, default)
 size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
-int g_tile = 0;             // build large schedules tiled (the tile form)
-int g_tile_pub = 2;         // tile form: progress published every this many levels
-int g_tile_ctas = 152;      // tile CTAs that can be resident at once
+int g_flow = 2;             // the dataflow form: 0 off, 1 on, 2 for schedules of <= PF_SMALL entries
+int g_flow_ahead = 4;       // dataflow form: levels of groups in flight (warps launched)
 
 template <class T>
 struct SweepCtx {
@@ -174,8 +172,9 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
                 const int* d = done + L - 1;
                 uint64_t t0 = 0;
                 unsigned spins = 0;
-                // relaxed poll, then a fence: the acquire pattern
-                while (*(volatile const int*)d < target) {
+                // acquire loads: the load that sees the count orders the
+                // reads of the previous level's values after it
+                while (ld_acquire(d) < target) {
                     if (*(volatile int*)abortf) {
                         ok = 0;
                         break;
@@ -192,7 +191,6 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
                         }
                     }
                 }
-                __threadfence();
             } else if (*(volatile int*)abortf) {
                 ok = 0;
             }
@@ -531,161 +529,184 @@ __global__ void __launch_bounds__(CL_NT) sweep_cluster_k(DevSched s, SweepCtx<T>
     }
 }
 
-// Tile form.  Shared memory: the tile's values at tile-local indices.  Each
-// CTA keeps, in its own row of s.seen (global memory, touched by its warp 0
-// only), the progress it has observed of every tile, its own tiles' final
-// counts included.  Warp 0 does the waits for the next level before the
-// level barrier, which also votes on the abort: every thread leaves at the
-// same barrier.
+// Dataflow form.
+constexpr int FLOW_NT = 256;
+constexpr int FLOW_B = 8;  // entries per batch (all of a hexahedral cell's)
+
 template <class T>
-__host__ __device__ __forceinline__ size_t tile_x_bytes(int maxTileCells) {
-    return (sizeof(T) * size_t(maxTileCells > 0 ? maxTileCells : 1) + 15) & ~size_t(15);
+__device__ __forceinline__ T ld_flow(const T* p);
+template <>
+__device__ __forceinline__ double ld_flow<double>(const double* p) {
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ float ld_flow<float>(const float* p) {
+    float v;
+    asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+template <class T>
+__device__ __forceinline__ void st_flow(T* p, T v);
+template <>
+__device__ __forceinline__ void st_flow<double>(double* p, double v) {
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+template <>
+__device__ __forceinline__ void st_flow<float>(float* p, float v) {
+    asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+// the sentinel: all bits set
+__device__ __forceinline__ bool flow_unset(double v) { return __double_as_longlong(v) == -1LL; }
+__device__ __forceinline__ bool flow_unset(float v) { return __float_as_int(v) == -1; }
+// a computed value that happens to have the sentinel's bits (a NaN) is
+// stored as the canonical quiet NaN instead
+__device__ __forceinline__ double flow_value(double v) {
+    return flow_unset(v) ? __longlong_as_double(0x7ff8000000000000LL) : v;
+}
+__device__ __forceinline__ float flow_value(float v) { return flow_unset(v) ? __int_as_float(0x7fc00000) : v; }
+
+// Wait for the value at p: relaxed loads (the value is the flag; nothing
+// else is published with it), backing off with nanosleep, bounded by
+// timeoutNs of %globaltimer; on expiry the abort flag and CFX_ERR_TIMEOUT
+// are set and ok is cleared.
+template <class T>
+__device__ __forceinline__ T flow_wait(const T* p, int* abortf, int* status, unsigned long long timeoutNs, bool& ok) {
+    T v = ld_flow(p);
+    if (!flow_unset(v)) return v;
+    uint64_t t0 = 0;
+    unsigned spins = 0;
+    while (flow_unset(v)) {
+        // poll back to back at first (the value is usually a level away),
+        // then back off
+        if (spins > 32) __nanosleep(64);
+        if ((++spins & 15u) == 0) {
+            if (*(volatile int*)abortf) {
+                ok = false;
+                return T(0);
+            }
+            const uint64_t t = globaltimer_ns();
+            if (t0 == 0) {
+                t0 = t;
+            } else if (t - t0 > timeoutNs) {
+                atomicExch(abortf, 1);
+                atomicExch(status, int(CFX_ERR_TIMEOUT));
+                ok = false;
+                return T(0);
+            }
+        }
+        v = ld_flow(p);
+    }
+    return v;
 }
 
-template <class T, int OP, int PF>
-__global__ void __launch_bounds__(TILE_NT, 1) sweep_tile_k(DevSched s, SweepCtx<T> a, int* status) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double sh[TILE_NT / 32];
+// out: [nSweeps][n] values (sentinel-filled); for the forward and pivot
+// sweeps out is x itself.  Reads: Gauss-Seidel, a slot of sweep sw takes
+// its lower neighbours from out[sw] and its upper ones from out[sw - 1] (x,
+// the values before the launch, for sw = 0); the backward Gauss-Seidel pass
+// takes its lower neighbours from x and its upper ones from out; the
+// forward, pivot and backward sweeps take every neighbour from out (the
+// backward one its own previous value from x).  Warps take groups W, W + NW,
+// ... in level order, and every group reads only groups of earlier levels:
+// with all warps resident (cooperative launch) the lowest unfinished group
+// can always proceed.  The dot partial (when requested) is summed per warp
+// in its group order, then per CTA (nPartials = gridDim.x).
+template <class T, int OP>
+__global__ void __launch_bounds__(FLOW_NT) sweep_flow_k(DevSched s, SweepCtx<T> a, T* out, int* status) {
+    __shared__ double sh[FLOW_NT / 32];
     if (a.done && *a.done) return;
-    T* X = reinterpret_cast<T*>(smem_raw);
-    int* seen = s.seen + size_t(blockIdx.x) * s.nTiles;
-    for (int i = threadIdx.x; i < s.nTiles; i += TILE_NT) seen[i] = 0;
     int* abortf = s.sync;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    constexpr int NW = TILE_NT / 32;
+    const int n = s.n;
+    const int lane = threadIdx.x & 31;
+    const int W = blockIdx.x * (FLOW_NT / 32) + (threadIdx.x >> 5);
+    const int NW = gridDim.x * (FLOW_NT / 32);
+    const bool gs = s.kind == SCHED_GS, gsb = s.kind == SCHED_GSB;
     double dot = 0.0;
-    __syncthreads();
-    // warp 0: wait until every tile segment q reads from has published
-    auto wait_seg = [&](int q) -> bool {
-        bool ok = true;
-        for (int k = s.segWait[q] + lane; k < s.segWait[q + 1]; k += 32) {
-            const int p = s.waitTile[k], need = s.waitNeed[k];
-            if (seen[p] >= need) continue;
-            uint64_t t0 = 0;
-            unsigned spins = 0;
-            int v;
-            while ((v = ld_acquire(s.progress + p)) < need) {
-                if ((++spins & 63u) == 0) {
-                    if (*(volatile int*)abortf) {
-                        ok = false;
-                        break;
-                    }
-                    const uint64_t t = globaltimer_ns();
-                    if (t0 == 0) {
-                        t0 = t;
-                    } else if (t - t0 > a.timeoutNs) {
-                        atomicExch(abortf, 1);
-                        atomicExch(status, int(CFX_ERR_TIMEOUT));
-                        ok = false;
-                        break;
-                    }
-                }
+    bool ok = true;
+    for (int g = W; g < s.nGroups; g += NW) {
+        // the warp's lanes finish a group together, so no lane runs ahead
+        // into a later group and competes with the ones still on this level
+        __syncwarp();
+        if (!__all_sync(0xffffffffu, ok)) break;
+        const int slot = g * 32 + lane;
+        const int c = s.cell[slot];
+        if (c < 0) continue;
+        const int cnt = s.cnt[slot];
+        const int e0 = s.groupEntry[g] + lane;
+        const T sc = a.scalar[slot];
+        const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+        const int sw = gs ? s.slotSweep[slot] : 0;
+        const int nLow = (gs || gsb) ? s.slotLower[slot] : 0;
+        const T* cur = out + size_t(sw) * n;
+        const T* prev = sw > 0 ? out + size_t(sw - 1) * n : a.x;
+        T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
+        // where entry k's value lives and whether it is produced in this launch
+        auto src_of = [&](int k, int nbk, bool& live) -> const T* {
+            if (gs) {
+                live = k < nLow || sw > 0;
+                return (k < nLow ? cur : prev) + nbk;
             }
-            if (!ok) break;
-            seen[p] = v;
-        }
-        return ok;
-    };
-    auto xat = [&](int e) -> T { return e >= 0 ? X[e] : ldcg(a.x + (-e - 1)); };
-    for (int ti = s.ctaTile[blockIdx.x]; ti < s.ctaTile[blockIdx.x + 1]; ++ti) {
-        const int t = s.ctaTiles[ti];
-        const int q0 = s.tileSeg[t], q1 = s.tileSeg[t + 1];
-        // header of this warp's first group in segment q (and the slot's
-        // tile-local index), issued two levels ahead
-        auto hdr = [&](int q, SlotRegs<T, PF>& r, int& loc) {
-            int g = 0;
-            bool okg = false;
-            if (q < q1) {
-                g = s.segGroup[q] + w;
-                okg = g < s.segGroup[q + 1];
+            if (gsb) {
+                live = k >= nLow;
+                return (k < nLow ? a.x : cur) + nbk;
             }
-            load_header<T, OP, PF>(s, a, g, okg, lane, r);
-            loc = okg ? s.slotLocal[g * 32 + lane] : 0;
+            live = true;
+            return cur + nbk;
         };
-        bool ok = true;
-        if (w == 0) ok = wait_seg(q0);
-        if (!__syncthreads_and(ok)) return;
-        // one entry set (the level being computed, then refilled with the
-        // next level's before the barrier) and two headers in flight
-        SlotRegs<T, PF> E;
-        SlotRegs<T, 1> H;  // header of level q + 1 (only its header fields are used)
-        int locE = 0, locH = 0;
-        {
-            SlotRegs<T, PF> tmp;
-            hdr(q0, E, locE);
-            load_entries<T, PF>(s, a.coef, E);
-            hdr(q0 + 1, tmp, locH);
-            H.c = tmp.c;
-            H.n = tmp.n;
-            H.e0 = tmp.e0;
-            H.sc = tmp.sc;
-            H.in = tmp.in;
-        }
-        for (int q = q0; q < q1; ++q) {
-            if (E.c >= 0) {
-                T acc = sw_init<OP>(E.sc, E.in, OP == OP_BWD ? ldcg(a.x + E.c) : T(0));
+        // batches of FLOW_B entries: every value load of a batch is issued
+        // before the first is waited on, so a slot pays one trip through L2
+        // per batch plus the wait for the values still being produced
+        for (int kb = 0; kb < cnt && ok; kb += FLOW_B) {
+            int nb[FLOW_B];
+            T cf[FLOW_B], v[FLOW_B];
 #pragma unroll
-                for (int k = 0; k < PF; ++k)
-                    if (k < E.n) acc = sw_step<OP>(acc, E.cf[k], xat(E.nbr[k]));
-                acc = tail_entries<T, OP>(s, a.coef, E.e0, PF, E.n, acc, xat);
-                const T v = sw_fini<OP>(acc, E.sc);
-                X[locE] = v;
-                a.x[E.c] = v;
-                if (a.dotWith) dot += double(v) * double(a.dotWith[E.c]);
-            }
-            // further groups of this warp in a wide level, loaded directly
-            for (int g = s.segGroup[q] + w + NW; g < s.segGroup[q + 1]; g += NW) {
-                const int slot = g * 32 + lane;
-                const int c = s.cell[slot];
-                if (c < 0) continue;
-                const int cnt = s.cnt[slot];
-                const int e0 = s.groupEntry[g] + lane;
-                const T sc = a.scalar[slot];
-                const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
-                T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
-                acc = tail_entries<T, OP>(s, a.coef, e0, 0, cnt, acc, xat);
-                const T v = sw_fini<OP>(acc, sc);
-                X[s.slotLocal[slot]] = v;
-                a.x[c] = v;
-                if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
-            }
-            // level q + 1: its header (issued a level ago) becomes current and
-            // its entries are issued now; the header of q + 2 is issued
-            E.c = H.c;
-            E.n = H.n;
-            E.e0 = H.e0;
-            E.sc = H.sc;
-            E.in = H.in;
-            locE = locH;
-            load_entries<T, PF>(s, a.coef, E);
-            {
-                SlotRegs<T, 1> tmp;
-                int g = 0;
-                bool okg = false;
-                if (q + 2 < q1) {
-                    g = s.segGroup[q + 2] + w;
-                    okg = g < s.segGroup[q + 3];
+            for (int j = 0; j < FLOW_B; ++j)
+                if (kb + j < cnt) {
+                    nb[j] = s.nb[e0 + 32 * (kb + j)];
+                    cf[j] = a.coef[e0 + 32 * (kb + j)];
                 }
-                load_header<T, OP, 1>(s, a, g, okg, lane, tmp);
-                locH = okg ? s.slotLocal[g * 32 + lane] : 0;
-                H = tmp;
-            }
-            ok = true;
-            if (w == 0 && q + 1 < q1) ok = wait_seg(q + 1);
-            if (!__syncthreads_and(ok)) return;
-            if (threadIdx.x == 0) {
-                const int done = q - q0 + 1;
-                if (done % s.pubEvery == 0 || q + 1 == q1) {
-                    st_release(s.progress + t, done);
-                    seen[t] = done;
+#pragma unroll
+            for (int j = 0; j < FLOW_B; ++j)
+                if (kb + j < cnt) {
+                    bool live;
+                    const T* p = src_of(kb + j, nb[j], live);
+                    v[j] = live ? ld_flow(p) : ldcg(p);
                 }
-            }
+#pragma unroll
+            for (int j = 0; j < FLOW_B; ++j)
+                if (kb + j < cnt && ok) {
+                    bool live;
+                    const T* p = src_of(kb + j, nb[j], live);
+                    if (live && flow_unset(v[j])) v[j] = flow_wait(p, abortf, status, a.timeoutNs, ok);
+                    acc = sw_step<OP>(acc, cf[j], v[j]);
+                }
         }
+        if (!ok) continue;
+        const T v = flow_value(sw_fini<OP>(acc, sc));
+        st_flow(out + size_t(sw) * n + c, v);
+        if (a.dotWith) dot += double(v) * double(a.dotWith[c]);
     }
+    __syncwarp();
     if (a.dotWith) {
-        dot = block_sum<TILE_NT>(dot, sh);
+        dot = block_sum<FLOW_NT>(dot, sh);
         if (threadIdx.x == 0) a.partials[blockIdx.x] = dot;
     }
+}
+
+// The dataflow form's buffers: filled with the sentinel before the sweep,
+// and the last sweep's values copied back into x after it.
+template <class T>
+__global__ void flow_fill_k(int64_t nv, T* out, const int* done) {
+    if (done && *done) return;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = sizeof(T) == 8 ? T(__longlong_as_double(-1LL)) : T(__int_as_float(-1));
+}
+
+template <class T>
+__global__ void flow_copy_k(int n, const T* __restrict__ src, T* __restrict__ x, const int* done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = src[i];
 }
 
 // Right-hand side gathered into slot order, so the sweeps load it without
@@ -736,7 +757,7 @@ inline int prec_index<double>() { return 0; }
 template <>
 inline int prec_index<float>() { return 1; }
 
-enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4, M_TILE = 5 };
+enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4, M_FLOW = 5 };
 
 // Execution form of a schedule: the vector in one CTA's shared memory, in a
 // cluster's distributed shared memory, or in global memory with a single CTA,
@@ -753,7 +774,6 @@ inline int cluster_of(const DevSched& s) {
 
 template <class T>
 int mode_of(const DevSched& s) {
-    if (s.tiled) return M_TILE;
     const size_t xbytes = sizeof(T) * size_t(s.n);
     if (xbytes <= g_smem_cap) return M_CTA;
     const int cs = cluster_of(s);
@@ -763,6 +783,10 @@ int mode_of(const DevSched& s) {
     }
     if (s.n <= g_small_threshold) return M_CTA_GLOBAL;
     if (g_cluster && s.n <= g_cluster_global) return M_CLUSTER_GLOBAL;
+    // the dataflow form: forced (1), or by default (2) for schedules of at
+    // most PF_SMALL entries per slot, where it measured faster than the
+    // level counters (the finest hexahedral level; triangular sweeps)
+    if (g_flow == 1 || (g_flow == 2 && s.maxK <= PF_SMALL)) return M_FLOW;
     return M_GRID;
 }
 
@@ -771,41 +795,9 @@ constexpr int pf_index(int pf) { return pf == PF_SMALL ? 0 : pf == PF_LARGE ? 1 
 template <class T, int OP, int PF>
 cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status);
 
-template <class T>
-size_t tile_smem_bytes(const DevSched& s) {
-    return tile_x_bytes<T>(s.maxTileCells);
-}
-
-// The tile form: one cooperative launch of s.grid CTAs (all resident), the
-// progress counters and the abort flag cleared first.
-template <class T, int OP, int PF>
-cfx_status launch_tile(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
-    const size_t smem = tile_smem_bytes<T>(s);
-    if (smem > g_smem_cap_max || s.grid > g_tile_ctas) {
-        set_error("tiled sweep: schedule exceeds the shared memory or the resident CTAs");
-        return CFX_ERR_STATE;
-    }
-    CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * 2, st));
-    CFX_CUDA(cudaMemsetAsync(s.progress, 0, sizeof(int) * size_t(s.nTiles), st));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(s.grid);
-    cfg.blockDim = dim3(TILE_NT);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_tile_k<T, OP, PF>, s, a, status));
-    count_launch();
-    return CFX_OK;
-}
-
 template <class T, int OP, int PF>
 cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, int* status) {
     if (s.nSlots == 0) return CFX_OK;
-    if (s.tiled) return launch_tile<T, OP, PF>(st, s, a, status);
     const size_t xbytes = sizeof(T) * size_t(s.n);
     const int cs = cluster_of(s);
     const int per = cs ? (s.n + cs - 1) / cs : 0;
@@ -910,7 +902,6 @@ void init_op_pf() {
     per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_wave_k<T, OP, PF>, GRID_NT, 0);
     g_wave_grid[prec_index<T>()][OP][pf_index(PF)] = g_num_sms * (per > 0 ? per : 1);
-    cudaFuncSetAttribute(sweep_tile_k<T, OP, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g_smem_cap));
     cudaFuncSetAttribute(sweep_cluster_k<T, OP, true, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(g_smem_cap));
@@ -956,12 +947,23 @@ int probe_cluster() {
     return 0;
 }
 
+template <class T, int OP>
+void init_flow() {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_flow_k<T, OP>, FLOW_NT, 0);
+    g_flow_grid[prec_index<T>()][OP] = g_num_sms * (per > 0 ? per : 1);
+}
+
 template <class T>
 void init_attrs() {
     init_op<T, OP_FWD>();
     init_op<T, OP_BWD>();
     init_op<T, OP_GS>();
     init_op<T, OP_RD>();
+    init_flow<T, OP_FWD>();
+    init_flow<T, OP_BWD>();
+    init_flow<T, OP_GS>();
+    init_flow<T, OP_RD>();
 }
 
 }  // namespace
@@ -978,14 +980,6 @@ void sweeps_init(int numSms) {
     g_smem_cap_max = g_smem_cap;
     init_attrs<double>();
     init_attrs<float>();
-    // resident tile CTAs with a full shared-memory partition each
-    {
-        int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_tile_k<double, OP_GS, PF_LARGE>, TILE_NT,
-                                                      g_smem_cap);
-        g_tile_ctas = g_num_sms * (per > 0 ? per : 1);
-        cudaGetLastError();
-    }
     // The cluster forms are kept behind CFX_TUNE_CLUSTER_SIZE: on GB300 the
     // persistent grid form sweeps the mid-size levels faster (a cluster
     // barrier per level costs more than the grid's per-level counters).
@@ -1014,11 +1008,21 @@ int wave_grid(const DevSched& s) {
 
 int sweep_wave() { return g_wave; }
 void set_sweep_wave(int on) { g_wave = on ? 1 : 0; }
-int sweep_tile() { return g_tile; }
-void set_sweep_tile(int on) { g_tile = on ? 1 : 0; }
-int sweep_tile_pub() { return g_tile_pub; }
-void set_sweep_tile_pub(int k) { g_tile_pub = k < 1 ? 1 : k; }
-int sweep_tile_ctas() { return g_tile_ctas; }
+int sweep_flow() { return g_flow; }
+void set_sweep_flow(int mode) { g_flow = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+int sweep_flow_ahead() { return g_flow_ahead; }
+void set_sweep_flow_ahead(int k) { g_flow_ahead = k < 1 ? 1 : k; }
+
+// Value buffers a pack of s needs in the dataflow form: the level-ordered
+// schedules whose vector does not fit one CTA (FP64), for the sweeps that do
+// not write their values straight into x.
+size_t sweep_flow_values(const DevSched& s, int op) {
+    if (s.n == 0 || sizeof(double) * size_t(s.n) <= g_smem_cap) return 0;
+    if (op == OP_FWD || op == OP_RD) return 0;
+    return size_t(s.nSweeps > 0 ? s.nSweeps : 1) * size_t(s.n);
+}
+
+
 
 template <class T>
 bool sweep_is_grid(const DevSched& s) {
@@ -1028,13 +1032,59 @@ bool sweep_is_grid(const DevSched& s) {
 template <class T>
 int sweep_partials(const DevSched& s) {
     const int m = mode_of<T>(s);
-    if (m == M_TILE) return s.grid;
+    if (m == M_FLOW) return flow_ctas(prec_index<T>(), OP_BWD, s);
     if (m == M_GRID) return g_wave && s.waveOk ? wave_grid<T>(s) : s.nChunks;
     return (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) ? cluster_of(s) : 1;
 }
 
 int cluster_global_cells() { return g_cluster_global; }
 void set_cluster_global_cells(int n) { g_cluster_global = n; }
+
+// CTAs of a dataflow launch: enough warps for g_flow_ahead levels of the
+// schedule's average width (warps further ahead would only spin), at most
+// the resident maximum.
+inline int flow_ctas(int prec, int op, const DevSched& s) {
+    const double perLevel = double(s.nGroups) / double(s.nLevels > 0 ? s.nLevels : 1);
+    const int want = int(std::ceil(perLevel * g_flow_ahead / double(FLOW_NT / 32)));
+    return std::max(1, std::min(want, g_flow_grid[prec][op]));
+}
+
+// The dataflow form of one sweep: fill the value buffers with the sentinel,
+// one cooperative launch of every resident CTA, copy the last sweep's
+// values into x (Gauss-Seidel and the backward sweeps; the forward and
+// pivot sweeps write x directly).
+template <class T, int OP>
+cfx_status launch_flow(cudaStream_t st, const DevSched& s, const Packed<T>& p, SweepCtx<T> a, int* status) {
+    const bool own = OP == OP_FWD || OP == OP_RD;
+    T* out = own ? a.x : p.flow;
+    if (!out) {
+        set_error("dataflow sweep: no value buffer");
+        return CFX_ERR_STATE;
+    }
+    const int64_t nv = own ? int64_t(s.n) : int64_t(s.nSweeps) * s.n;
+    const int fb = int(std::min<int64_t>((nv + 255) / 256, 4096));
+    flow_fill_k<T><<<fb, 256, 0, st>>>(nv, out, a.done);
+    count_launch();
+    CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * 2, st));
+    const int grid = flow_ctas(prec_index<T>(), OP, s);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid > 0 ? grid : 1);
+    cfg.blockDim = dim3(FLOW_NT);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_flow_k<T, OP>, s, a, out, status));
+    count_launch();
+    if (!own) {
+        const int cb = std::min((s.n + 255) / 256, 4096);
+        flow_copy_k<T><<<cb, 256, 0, st>>>(s.n, out + size_t(s.nSweeps - 1) * s.n, a.x, a.done);
+        count_launch();
+    }
+    return CFX_OK;
+}
 
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
@@ -1046,6 +1096,15 @@ cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>
         count_launch();
     }
     SweepCtx<T> a{p.coef, p.scalar, in, p.inS, x, dotWith, partials, done, SWEEP_TIMEOUT_NS};
+    if (s.nSlots > 0 && mode_of<T>(s) == M_FLOW) {
+        switch (op) {
+            case OP_FWD: return launch_flow<T, OP_FWD>(st, s, p, a, status);
+            case OP_BWD: return launch_flow<T, OP_BWD>(st, s, p, a, status);
+            case OP_GS: return launch_flow<T, OP_GS>(st, s, p, a, status);
+            case OP_RD: return launch_flow<T, OP_RD>(st, s, p, a, status);
+            default: set_error("unknown sweep"); return CFX_ERR_ARG;
+        }
+    }
     switch (op) {
         case OP_FWD: return launch<T, OP_FWD>(st, s, a, status);
         case OP_BWD: return launch<T, OP_BWD>(st, s, a, status);
@@ -1063,8 +1122,8 @@ cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>
 template <class T>
 cfx_status run_sweep_stalled(cudaStream_t st, const DevSched& s, const Packed<T>& p, const T* in, T* x,
                              unsigned long long timeoutNs, int* status) {
-    if (s.nLevels < 2 || s.nSlots == 0 || s.tiled) {
-        set_error("stalled sweep: the schedule needs at least two levels (level-ordered, not tiled)");
+    if (s.nLevels < 2 || s.nSlots == 0) {
+        set_error("stalled sweep: the schedule needs at least two levels");
         return CFX_ERR_ARG;
     }
     int blocks = (s.nSlots + 255) / 256;

@@ -141,7 +141,6 @@ _SIG = {
     "cfx_solve": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, ctypes.POINTER(Perf)]),
     "cfx_solve_device": (_i, [_vp, ctypes.POINTER(Controls), _vp, _vp, ctypes.POINTER(Perf)]),
     "cfx_tune_set": (_i, [_i, _i]),
-    "cfx_sched_tiled_check": (_i, [_i, _i, _vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "cfx_tune_get": (_i, [_i, ctypes.POINTER(_i)]),
     "cfx_amul": (_i, [_vp, _vp, _vp]),
     "cfx_tmul": (_i, [_vp, _vp, _vp]),
@@ -506,8 +505,8 @@ class SolverPerformance:
 TUNE_SMALL_SWEEP, TUNE_CLUSTER_GLOBAL, TUNE_CLUSTER_SIZE, TUNE_BATCH_INNER_DIGITS, TUNE_SMEM_BYTES = 0, 1, 2, 3, 4
 TUNE_GRID_WAVE = 5
 TUNE_CLUSTER_PRE = 6
-TUNE_TILE = 7
-TUNE_TILE_PUBLISH = 8
+TUNE_FLOW = 7
+TUNE_FLOW_AHEAD = 8
 
 
 def tune_set(key, value):
@@ -518,21 +517,6 @@ def tune_get(key):
     v = ctypes.c_int()
     _check(lib().cfx_tune_get(int(key), ctypes.byref(v)), "cfx_tune_get")
     return v.value
-
-
-SCHED_KINDS = {"forward": 0, "backward": 1, "GaussSeidel": 2, "symGaussSeidelBackward": 3}
-
-
-def sched_tiled_check(nCells, lowerAddr, upperAddr, kind, nSweeps=1, tileCells=4096, maxCtas=152, pubEvery=2):
-    """Build and check the tiled form of a sweep schedule (host only, no
-    GPU); returns its statistics or raises CfxError with the reason."""
-    l = np.ascontiguousarray(lowerAddr, np.int32)
-    u = np.ascontiguousarray(upperAddr, np.int32)
-    st = np.zeros(8, np.int32)
-    _check(lib().cfx_sched_tiled_check(int(nCells), l.size, _hp(l), _hp(u), SCHED_KINDS[kind], int(nSweeps),
-                                       int(tileCells), int(maxCtas), int(pubEvery), _hp(st)), "cfx_sched_tiled_check")
-    return dict(zip(("tiles", "ctas", "segments", "maxTileCells", "waits", "slots", "levels", "maxK"),
-                    (int(x) for x in st)))
 
 
 def gamg_coarse_interfaces(restrictAddr, patchSize, faceCells, nbrCells):

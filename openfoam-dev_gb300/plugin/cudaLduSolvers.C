@@ -232,6 +232,119 @@ protected:
         e.gamg = true;
     }
 
+    //- The preconditioner's name as lduMatrix::preconditioner::New reads
+    //  it (lduMatrixPreconditioner.C:60-75; the keyword is required), checked
+    //  against the reference's own run-time tables with its error text
+    //  (lduMatrixPreconditioner.C:96-136), then against what the device
+    //  implements
+    word preconditionerName() const
+    {
+        const entry& pe =
+            controlDict_.lookupEntry("preconditioner", false, false);
+        word name;
+        if (pe.isDict())
+        {
+            pe.dict().lookup("preconditioner") >> name;
+        }
+        else
+        {
+            pe.stream() >> name;
+        }
+        const dictionary& pc = pe.isDict() ? pe.dict() : dictionary::null;
+        if (matrix_.diagonal()) return name;
+        if (matrix_.symmetric())
+        {
+            if (!lduMatrix::preconditioner::symMatrixConstructorTablePtr_->found(name))
+            {
+                FatalIOErrorInFunction(pc)
+                    << "Unknown symmetric matrix preconditioner "
+                    << name << nl << nl
+                    << "Valid symmetric matrix preconditioners :" << endl
+                    << lduMatrix::preconditioner::symMatrixConstructorTablePtr_->sortedToc()
+                    << exit(FatalIOError);
+            }
+        }
+        else if
+        (
+            !lduMatrix::preconditioner::asymMatrixConstructorTablePtr_->found(name)
+        )
+        {
+            FatalIOErrorInFunction(pc)
+                << "Unknown asymmetric matrix preconditioner "
+                << name << nl << nl
+                << "Valid asymmetric matrix preconditioners :" << endl
+                << lduMatrix::preconditioner::asymMatrixConstructorTablePtr_->sortedToc()
+                << exit(FatalIOError);
+        }
+        static const wordList onDevice
+        ({"none", "diagonal", "DIC", "FDIC", "DILU", "GAMG"});
+        if (findIndex(onDevice, name) < 0)
+        {
+            FatalIOErrorInFunction(controlDict_)
+                << "cudaLduSolvers: preconditioner " << name
+                << " is not available on the GPU; available: " << onDevice
+                << exit(FatalIOError);
+        }
+        return name;
+    }
+
+    //- The smoother's name as lduMatrix::smoother::New reads it
+    //  (lduMatrixSmoother.C:40-60, the keyword required), checked against
+    //  the reference's run-time tables with its error text
+    //  (lduMatrixSmoother.C:102-147), then against what the device implements
+    word smootherName(const dictionary& d) const
+    {
+        const entry& se = d.lookupEntry("smoother", false, false);
+        word name;
+        if (se.isDict())
+        {
+            se.dict().lookup("smoother") >> name;
+        }
+        else
+        {
+            se.stream() >> name;
+        }
+        if (matrix_.diagonal()) return name;
+        if (matrix_.symmetric())
+        {
+            if (!lduMatrix::smoother::symMatrixConstructorTablePtr_->found(name))
+            {
+                FatalIOErrorInFunction(d)
+                    << "Unknown symmetric matrix smoother "
+                    << name << nl << nl
+                    << "Valid symmetric matrix smoothers are :" << endl
+                    << lduMatrix::smoother::symMatrixConstructorTablePtr_->sortedToc()
+                    << exit(FatalIOError);
+            }
+        }
+        else if
+        (
+            !lduMatrix::smoother::asymMatrixConstructorTablePtr_->found(name)
+        )
+        {
+            FatalIOErrorInFunction(d)
+                << "Unknown asymmetric matrix smoother "
+                << name << nl << nl
+                << "Valid asymmetric matrix smoothers are :" << endl
+                << lduMatrix::smoother::asymMatrixConstructorTablePtr_->sortedToc()
+                << exit(FatalIOError);
+        }
+        static const wordList onDevice
+        ({
+            "GaussSeidel", "symGaussSeidel", "nonBlockingGaussSeidel", "DIC",
+            "FDIC", "DILU", "DICGaussSeidel", "DILUGaussSeidel"
+        });
+        if (findIndex(onDevice, name) < 0)
+        {
+            FatalIOErrorInFunction(d)
+                << "cudaLduSolvers: smoother " << name
+                << " is not available on the GPU; available: " << onDevice
+                << exit(FatalIOError);
+        }
+        return name;
+    }
+
+    //- The solver controls, read and checked before any device work
     cfx_controls controls(int solverType) const
     {
         cfx_controls c;
@@ -242,12 +355,12 @@ protected:
         c.maxIter = maxIter_;
         c.minIter = minIter_;
         const dictionary* pd = preconditionerDict();
-        const word pre
-        (
-            pd
-          ? pd->lookup<word>("preconditioner")
-          : controlDict_.lookupOrDefault<word>("preconditioner", "none")
-        );
+        // Krylov solvers construct a preconditioner (PCG.C:104-112,
+        // PBiCGStab.C:104-112, PBiCG.C:104-112); GAMG and smoothSolver do not
+        const bool krylov =
+            solverType == CFX_SOLVER_PCG || solverType == CFX_SOLVER_PBICGSTAB
+         || solverType == CFX_SOLVER_PBICG;
+        const word pre(krylov ? preconditionerName() : word("none"));
         c.preconditioner =
             pre == "DIC" ? CFX_PRE_DIC
           : pre == "FDIC" ? CFX_PRE_FDIC
@@ -267,9 +380,14 @@ protected:
             c.pcTolerance = gd.lookupOrDefault<scalar>("tolerance", 1e-6);
             c.pcRelTol = gd.lookupOrDefault<scalar>("relTol", 0);
         }
+        // GAMG (GAMGSolver.C:67-93) and smoothSolver (smoothSolver.C:
+        // 84-94) construct smoothers; the GAMG preconditioner's cycles too
+        const bool smoothed =
+            solverType == CFX_SOLVER_GAMG || solverType == CFX_SOLVER_SMOOTH
+         || pcGamg;
         const word sm
         (
-            gd.lookupOrDefault<word>("smoother", "GaussSeidel")
+            smoothed ? smootherName(gd) : word("GaussSeidel")
         );
         c.smoother =
             sm == "DIC" ? CFX_SMOOTH_DIC
@@ -299,9 +417,17 @@ protected:
             gd.lookupOrDefault<bool>("interpolateCorrection", false);
         c.directSolveCoarsest =
             gd.lookupOrDefault<bool>("directSolveCoarsest", false);
-        c.precision =
-            controlDict_.lookupOrDefault<word>("precision", "FP64") == "mixed"
-          ? CFX_MIXED : CFX_FP64;
+        const word precision
+        (
+            controlDict_.lookupOrDefault<word>("precision", "FP64")
+        );
+        if (precision != "FP64" && precision != "mixed")
+        {
+            FatalIOErrorInFunction(controlDict_)
+                << "cudaLduSolvers: unknown precision " << precision
+                << " (FP64 or mixed)" << exit(FatalIOError);
+        }
+        c.precision = precision == "mixed" ? CFX_MIXED : CFX_FP64;
         return c;
     }
 
@@ -422,8 +548,8 @@ solverPerformance cudaPCG::solve
     const direction
 ) const
 {
-    Entry& e = deviceMatrix();
     const cfx_controls c = controls(CFX_SOLVER_PCG);
+    Entry& e = deviceMatrix();
     if (c.preconditioner == CFX_PRE_GAMG) gamgLevels(e, *preconditionerDict());
     return run(e, c, psi, source);
 }
@@ -436,8 +562,8 @@ solverPerformance cudaPBiCGStab::solve
     const direction
 ) const
 {
-    Entry& e = deviceMatrix();
     const cfx_controls c = controls(CFX_SOLVER_PBICGSTAB);
+    Entry& e = deviceMatrix();
     if (c.preconditioner == CFX_PRE_GAMG) gamgLevels(e, *preconditionerDict());
     return run(e, c, psi, source);
 }
@@ -450,8 +576,9 @@ solverPerformance cudaPBiCG::solve
     const direction
 ) const
 {
+    const cfx_controls c = controls(CFX_SOLVER_PBICG);
     Entry& e = deviceMatrix();
-    return run(e, controls(CFX_SOLVER_PBICG), psi, source);
+    return run(e, c, psi, source);
 }
 
 
@@ -462,8 +589,9 @@ solverPerformance cudaSmoothSolver::solve
     const direction
 ) const
 {
+    const cfx_controls c = controls(CFX_SOLVER_SMOOTH);
     Entry& e = deviceMatrix();
-    return run(e, controls(CFX_SOLVER_SMOOTH), psi, source);
+    return run(e, c, psi, source);
 }
 
 
@@ -474,9 +602,10 @@ solverPerformance cudaGAMG::solve
     const direction
 ) const
 {
+    const cfx_controls c = controls(CFX_SOLVER_GAMG);
     Entry& e = deviceMatrix();
     gamgLevels(e, controlDict_);
-    return run(e, controls(CFX_SOLVER_GAMG), psi, source);
+    return run(e, c, psi, source);
 }
 
 } // End namespace Foam

@@ -137,16 +137,27 @@ def main():
     lib = os.path.join(OUT, "libOpenFOAM.so")
     harness_src = os.path.join(HERE, "ref_harness.C")
     harness = os.path.join(OUT, "ref_harness")
+    # the OpenFOAM-side plugin of the solver library, built against this
+    # reference build so that a test can load it as controlDict's libs
+    # entry would (the harness's plugin mode)
+    repo = os.path.dirname(HERE)
+    plugin_src = os.path.join(repo, "openfoam-dev_gb300", "plugin", "cudaLduSolvers.C")
+    solver_lib_dir = os.path.join(repo, "openfoam-dev_gb300", "lib")
+    plugin = os.path.join(OUT, "libcudaLduSolvers_OpenFOAM.so")
     mk = os.path.join(OUT, "Makefile")
     with open(mk, "w") as fh:
         fh.write("CXX = g++\n")
         fh.write("FLAGS = " + " ".join(CXXFLAGS + inc) + "\n")
-        fh.write(f"all: {harness}\n")
+        fh.write(f"all: {harness} {plugin}\n")
         fh.write(f"{lib}: {' '.join(objs)}\n"
                  f"\t$(CXX) -shared -fuse-ld=bfd -o $@ $^ -lz -lpthread -ldl -lm\n")
         fh.write(f"{harness}: {harness_src} {os.path.join(HERE, 'harness_io.H')} {lib}\n"
                  f"\t$(CXX) $(FLAGS) -o $@ {harness_src} -L{OUT} -lOpenFOAM "
                  f"-Wl,-rpath,{OUT} -lz -lpthread -ldl -lm\n")
+        fh.write(f"{plugin}: {plugin_src} {os.path.join(repo, 'include', 'cfx.h')} {lib}\n"
+                 f"\t$(CXX) $(FLAGS) -shared -I{os.path.join(repo, 'include')} -o $@ {plugin_src} "
+                 f"-L{OUT} -lOpenFOAM -L{solver_lib_dir} -lcudaLduSolvers "
+                 f"-Wl,-rpath,{OUT} -Wl,-rpath,{solver_lib_dir}\n")
         fh.write("\n".join(rules))
     r = subprocess.call(["make", "-f", mk, f"-j{args.j}", "-k"])
     return r

@@ -18,6 +18,12 @@
            registered first (the faceAreaPair weights need an fvMesh; the
            pairing itself is the reference code path), and the level
            hierarchy and coarse matrices are written too.
+    plugin the run-time loading path of a solver library: libs.open(library)
+           (dlLibraryTable, as controlDict's libs entry does), then
+           lduMatrix::solver::New for the dictionary given as text and
+           solve(psi, source), with FatalError thrown as an exception; writes
+           whether the library loaded, the selected type, the solver
+           performance, or the FatalError message.
 
   Record file: "CFXREC1\n", then records of
     char name[32]; char dtype[8] ("i4"|"f8"|"s"); int64 count; data
@@ -58,6 +64,8 @@
 #include "IStringStream.H"
 #include "SolverPerformance.H"
 #include "GAMGSolver.H"
+#include "dlLibraryTable.H"
+#include "error.H"
 #include "harness_io.H"
 
 using namespace Foam;
@@ -520,6 +528,45 @@ int runSolve(const RecMap& in, Writer& out, Time& runTime)
     return 0;
 }
 
+int runPlugin(const RecMap& in, Writer& out, Time& runTime)
+{
+    labelList l(getL(in, "l")), u(getL(in, "u"));
+    const scalarField source(getF(in, "source"));
+    scalarField psi(getF(in, "psi"));
+    const label nCells = source.size(), nFaces = l.size();
+    harnessMesh mesh(runTime, nCells, l, u);
+    harnessInterfaces hi(in, mesh);
+    lduMatrix A(mesh);
+    buildMatrix(A, in, nCells, nFaces);
+
+    const std::string lib = getS(in, "library");
+    const bool loaded = lib.empty() ? false : libs.open(fileName(lib));
+    out.i4("loaded", loaded ? 1 : 0);
+
+    FatalError.throwExceptions();
+    FatalIOError.throwExceptions();
+    try
+    {
+        IStringStream is(getS(in, "dict"));
+        dictionary dict(is);
+        autoPtr<lduMatrix::solver> s =
+            lduMatrix::solver::New("psi", A, hi.bou, hi.intc, hi.ifs, dict);
+        const std::string type(s->type());
+        out.put("type", "s", type.c_str(), type.size(), 1);
+        solverPerformance perf = s->solve(psi, source, 0);
+        out.f8("psi", psi);
+        out.f8("finalResidual", perf.finalResidual());
+        out.i4("nIterations", perf.nIterations());
+        out.put("solverName", "s", perf.solverName().c_str(), perf.solverName().size(), 1);
+    }
+    catch (const Foam::error& e)
+    {
+        const std::string msg(e.message());
+        out.put("fatal", "s", msg.c_str(), msg.size(), 1);
+    }
+    return 0;
+}
+
 } // namespace
 
 
@@ -541,6 +588,7 @@ int main(int argc, char* argv[])
     if (mode == "geom") return runGeom(in, out, runTime);
     if (mode == "ops") return runOps(in, out, runTime);
     if (mode == "solve") return runSolve(in, out, runTime);
+    if (mode == "plugin") return runPlugin(in, out, runTime);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -76,6 +76,24 @@ def solve(s, ctl, psi0=None, weights=None):
     return run(recs)
 
 
+PLUGIN = os.path.join(HERE, "_ref", "libcudaLduSolvers_OpenFOAM.so")
+
+
+def plugin_available():
+    return os.path.exists(PLUGIN) and available()
+
+
+def plugin_solve(s, ctl, library=PLUGIN, psi0=None):
+    """The reference's run-time loading path: libs.open(library), then
+    lduMatrix::solver::New with the dictionary and solve; returns the
+    records (loaded, type, psi and performance, or the FatalError message
+    as "fatal")."""
+    recs = dict(mode="plugin", source=s["source"],
+                psi=np.zeros_like(s["source"]) if psi0 is None else psi0,
+                dict=dict_text(ctl), library=library or "", **_ldu(s))
+    return run(recs)
+
+
 FV_HARNESS = os.path.join(HERE, "_ref", "fv_harness")
 
 _FOAM_HEADER = "FoamFile\n{\n    format ascii;\n    class dictionary;\n    object %s;\n}\n"

@@ -71,9 +71,13 @@ def parse():
     ap.add_argument("--workload", choices=["all", "gamg", "batch", "serve"], default="all",
                     help="all: the GAMG headline line with the batch and serving measurements added")
     ap.add_argument("--batch-count", type=int, default=512)
-    ap.add_argument("--serve-duration", type=float, default=15.0, help="seconds of Poisson arrivals per precision")
-    ap.add_argument("--serve-rate", type=float, default=0.0, help="requests/s (0: 60%% of the estimated capacity)")
-    ap.add_argument("--serve-sweep", action="store_true", help="sweep the rate for the largest with p99 <= 2x unloaded")
+    ap.add_argument("--serve-duration", type=float, default=60.0,
+                    help="seconds of Poisson arrivals of the serving stream, per precision")
+    ap.add_argument("--serve-rate", type=float, default=0.0,
+                    help="requests/s of the serving stream (0: the largest rate of the sweep at which every "
+                         "request kind's p99 stays within 2x its unloaded p99)")
+    ap.add_argument("--serve-sweep-duration", type=float, default=15.0,
+                    help="seconds per rate of the sweep that picks the serving rate (0: no sweep)")
     ap.add_argument("--serve-large", type=int, default=200, help="cells per axis of the large GAMG requests")
     return ap.parse_args()
 
@@ -751,23 +755,30 @@ def run_batch_serve(args, local, want_batch, want_serve):
         for prec in ("mixed", "FP64"):
             mix.run(mix.draw(), prec)  # warm the drivers
             mix.run(("large", None, 1), prec)
-            un = loadgen.serve_unloaded(mix, 24, prec)
+            un = loadgen.serve_unloaded(mix, 32, prec)
             t_large = un["by_kind_p50_ms"].get("large", 1000.0) / 1e3
-            rate = args.serve_rate or 0.6 / (0.1 * t_large + 0.9 * 0.01)
-            r = {"unloaded": un}
-            if args.serve_sweep:
-                sweep = []
-                for f in (0.4, 0.6, 0.8, 1.0, 1.2):
-                    q = loadgen.serve_stream(mix, rate / 0.6 * f, args.serve_duration, prec)
-                    q["p99_over_unloaded"] = q["p99_ms"] / un["p99_ms"]
-                    sweep.append(q)
-                ok = [q for q in sweep if q["p99_over_unloaded"] <= 2.0]
-                r["sweep"] = sweep
-                r["max_sustainable_solves_per_s"] = max((q["solves_per_s"] for q in ok), default=None)
-            else:
-                q = loadgen.serve_stream(mix, rate, args.serve_duration, prec)
-                q["p99_over_unloaded"] = q["p99_ms"] / un["p99_ms"]
-                r["stream"] = q
+            t_small = un["by_kind_p50_ms"].get("resident", 10.0) / 1e3
+            # requests/s the GPU could take if nothing overlapped
+            capacity = 1.0 / (0.1 * t_large + 0.9 * t_small)
+            r = {"unloaded": un, "capacity_estimate_per_s": capacity}
+            rate = args.serve_rate
+            if not rate:
+                rate = 0.3 * capacity
+                if args.serve_sweep_duration > 0:
+                    sweep = []
+                    for f in (0.3, 0.5, 0.7, 0.9):
+                        q = loadgen.serve_stream(mix, f * capacity, args.serve_sweep_duration, prec)
+                        q["by_kind_ratio"], q["worst_kind_p99_over_unloaded_p99"] = loadgen.per_kind_ratio(q, un)
+                        sweep.append(q)
+                        if q["worst_kind_p99_over_unloaded_p99"] is not None and \
+                                q["worst_kind_p99_over_unloaded_p99"] <= 2.0:
+                            rate = f * capacity
+                    r["sweep"] = sweep
+            q = loadgen.serve_stream(mix, rate, args.serve_duration, prec)
+            q["by_kind_ratio"], q["worst_kind_p99_over_unloaded_p99"] = loadgen.per_kind_ratio(q, un)
+            q["p99_over_unloaded_p99_all"] = q["p99_ms"] / un["p99_ms"]
+            r["stream"] = q
+            r["sustained_solves_per_s"] = q["solves_per_s"]
             srv[prec] = r
         sv.close()
         out["serve"] = srv

@@ -855,6 +855,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
             set_error("iteration loop did not terminate");
             return CFX_ERR_STATE;
         }
+        if (ctx->yield && !h.done) ctx->yield(ctx->yieldArg);
     }
     *out = h;
     return CFX_OK;
@@ -1319,6 +1320,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
             h = read_state(ctx, 0);
             const int stc = read_status(ctx);
             if (stc != 0) return cfx_status(stc);
+            if (ctx->yield && !h.done) ctx->yield(ctx->yieldArg);
         }
     } else {
         // FP32 V-cycle on the residual equation A e = r inside an FP64
@@ -1341,6 +1343,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
             h = read_state(ctx, 0);
             const int stc = read_status(ctx);
             if (stc != 0) return cfx_status(stc);
+            if (ctx->yield && !h.done) ctx->yield(ctx->yieldArg);
         }
     }
     std::snprintf(perf->solverName, sizeof(perf->solverName), "GAMG");

@@ -88,6 +88,11 @@ struct cfx_ctx {
     // CUDA runtime callers and PyTorch produce their arrays by default, and
     // the asynchronous ones make that stream wait for their results.
     cudaEvent_t evIn = nullptr, evOut = nullptr;
+    // Called by the solve drivers between iterations (V-cycles, batches of
+    // Krylov iterations), when the device is idle: lets an owner such as the
+    // solve server run other work there.  Not part of the C ABI.
+    void (*yield)(void*) = nullptr;
+    void* yieldArg = nullptr;
 };
 
 namespace cfx {

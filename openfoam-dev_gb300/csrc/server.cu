@@ -12,11 +12,18 @@
 //     count against an HBM budget.  A matrix or request that alone exceeds
 //     the budget is refused (CFX_ERR_ADMISSION); one that does not fit now
 //     waits (the submitting thread blocks) until completions free space.
-//   * One worker thread runs the GPU.  Whenever it is free it takes every
-//     queued small request (at most one per matrix, up to maxBatch) and
-//     solves them in one persistent launch, one CTA or one thread-block
-//     cluster per system; requests that arrive meanwhile go into the next
-//     launch.  Large requests run alone through the whole-GPU drivers.
+//   * Two worker threads share the GPU.  The batch worker takes every queued
+//     small request (at most one per matrix, up to maxBatch) and solves them
+//     in one persistent launch, one CTA or one thread-block cluster per
+//     system; requests that arrive meanwhile go into the next launch.  The
+//     large worker runs large requests one at a time through the whole-GPU
+//     drivers on its own context.  The whole-GPU drivers launch cooperative
+//     grids that must have the device to themselves, so the two do not run
+//     kernels at the same time; instead a large solve yields between its
+//     V-cycles (or batches of Krylov iterations) whenever small requests are
+//     waiting, the batch worker runs one launch in that gap, and the large
+//     solve resumes.  A small request waits at most one cycle of a large
+//     solve, not all of it.
 //   * Completion is signalled per request; a request can be cancelled while
 //     it is queued (or its result dropped later), and requests whose client
 //     never collects them are freed at release or shutdown.
@@ -89,7 +96,14 @@ struct cfx_server {
     int64_t nextMat = 1, nextReq = 1;
     size_t used = 0;                  // bytes admitted (matrices + request vectors)
     bool stop = false;
-    std::thread worker;
+    std::thread worker;               // batches of small requests
+    std::thread largeWorker;          // large requests
+    // who runs kernels now (mu held): 0 nobody, 1 a batch, 2 a large solve;
+    // largeActive: a large solve is in progress (possibly yielding);
+    // yieldOpen: it has yielded for one batch; batchGen counts batches
+    int owner = 0;
+    bool largeActive = false, yieldOpen = false;
+    int64_t batchGen = 0, yields = 0;
     // launch buffers
     SlotSys<double>* d64 = nullptr;
     SlotSys<float>* d32 = nullptr;
@@ -252,82 +266,142 @@ void run_batch(cfx_server* sv, std::vector<SrvRequest*>& rs, std::vector<SrvMatr
 
 namespace {
 
-// The worker: large requests alone, small ones batched (one precision per
-// launch, at most one request per matrix), until stopped.
-void worker_loop(cfx_server* sv) {
+enum { GPU_FREE = 0, GPU_BATCH = 1, GPU_LARGE = 2 };
+
+// A queued request of the kind the worker serves whose matrix is idle
+// (mu held).
+SrvRequest* next_ready(cfx_server* sv, bool large) {
+    for (int64_t id : sv->queue) {
+        SrvRequest* r = sv->reqs[id].get();
+        SrvMatrix* m = sv->mats[r->matrixId].get();
+        if (m->large == large && !m->busy) return r;
+    }
+    return nullptr;
+}
+
+void finish_all(cfx_server* sv, std::vector<SrvRequest*>& rs, cfx_status st, const std::string& err) {
+    for (SrvRequest* r : rs) {
+        r->status = st;
+        r->error = err;
+        r->perf.status = st;
+        finish(sv, *r, st == CFX_OK ? Q_DONE : Q_FAILED);
+    }
+    drop_detached(sv);
+    reap(sv);
+    sv->cvDone.notify_all();
+    sv->cvWork.notify_all();
+}
+
+// The batch worker: while no large solve runs (or one has yielded), every
+// queued small request of the oldest one's precision, at most one per
+// matrix, in one launch.
+void batch_worker(cfx_server* sv) {
     cudaSetDevice(sv->ctx->device);
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
-        sv->cvWork.wait(lk, [&] { return sv->stop || !sv->queue.empty(); });
+        sv->cvWork.wait(lk, [&] {
+            return sv->stop ||
+                   (sv->owner == GPU_FREE && (!sv->largeActive || sv->yieldOpen) && next_ready(sv, false));
+        });
         if (sv->stop) return;
-        // the oldest request decides: large -> alone; small -> a batch of
-        // its precision
-        SrvRequest* head = sv->reqs[sv->queue.front()].get();
-        SrvMatrix* hm = sv->mats[head->matrixId].get();
+        sv->owner = GPU_BATCH;
+        sv->yieldOpen = false;
+        const int prec = next_ready(sv, false)->ctl.precision;
         std::vector<SrvRequest*> rs;
         std::vector<SrvMatrix*> ms;
-        if (hm->large) {
-            if (hm->busy) {  // cannot happen with one worker, kept for clarity
-                sv->cvWork.wait_for(lk, std::chrono::milliseconds(1));
-                continue;
-            }
-            rs.push_back(head);
-            ms.push_back(hm);
+        std::deque<int64_t> keep;
+        while (!sv->queue.empty()) {
+            const int64_t id = sv->queue.front();
             sv->queue.pop_front();
-        } else {
-            const int prec = head->ctl.precision;
-            std::deque<int64_t> keep;
-            while (!sv->queue.empty()) {
-                const int64_t id = sv->queue.front();
-                sv->queue.pop_front();
-                SrvRequest* r = sv->reqs[id].get();
-                SrvMatrix* m = sv->mats[r->matrixId].get();
-                if (!m->large && !m->busy && r->ctl.precision == prec && int(rs.size()) < sv->cfg.maxBatch) {
-                    m->busy = true;
-                    rs.push_back(r);
-                    ms.push_back(m);
-                } else {
-                    keep.push_back(id);
-                }
+            SrvRequest* r = sv->reqs[id].get();
+            SrvMatrix* m = sv->mats[r->matrixId].get();
+            if (!m->large && !m->busy && r->ctl.precision == prec && int(rs.size()) < sv->cfg.maxBatch) {
+                m->busy = true;
+                rs.push_back(r);
+                ms.push_back(m);
+            } else {
+                keep.push_back(id);
             }
-            sv->queue.swap(keep);
         }
+        sv->queue.swap(keep);
         for (SrvRequest* r : rs) r->state = Q_RUNNING;
-        sv->running = int64_t(rs.size());
+        sv->running += int64_t(rs.size());
         lk.unlock();
         cfx_status st = CFX_OK;
         std::string err;
         try {
-            if (ms[0]->large) {
-                cfx_perf perf;
-                std::memset(&perf, 0, sizeof(perf));
-                st = cfx_solve_device(ms[0]->mat, &rs[0]->ctl, rs[0]->d_psi, rs[0]->d_b, &perf);
-                if (st != CFX_OK) err = cfx_last_error();
-                rs[0]->perf = perf;
-            } else {
-                run_batch(sv, rs, ms);
-            }
+            run_batch(sv, rs, ms);
         } catch (const std::exception& e) {
             st = CFX_ERR_CUDA;
             err = e.what();
         }
         lk.lock();
-        sv->running = 0;
-        if (ms[0]->large) {
-            ++sv->largeSolves;
-        } else {
-            ++sv->batches;
-            sv->batchedSolves += int64_t(rs.size());
+        sv->running -= int64_t(rs.size());
+        ++sv->batches;
+        sv->batchedSolves += int64_t(rs.size());
+        sv->owner = GPU_FREE;
+        ++sv->batchGen;
+        finish_all(sv, rs, st, err);
+    }
+}
+
+// Called by the large worker's solve between iterations (lock not held, the
+// device idle): when small requests wait, hand the GPU to the batch worker
+// for one launch and take it back after.
+void large_yield(void* arg) {
+    cfx_server* sv = static_cast<cfx_server*>(arg);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (sv->stop || !next_ready(sv, false)) return;
+    const int64_t gen = sv->batchGen;
+    sv->owner = GPU_FREE;
+    sv->yieldOpen = true;
+    ++sv->yields;
+    sv->cvWork.notify_all();
+    sv->cvWork.wait(lk, [&] {
+        return sv->stop || (sv->owner == GPU_FREE && (sv->batchGen != gen || !next_ready(sv, false)));
+    });
+    sv->yieldOpen = false;
+    sv->owner = GPU_LARGE;
+}
+
+// The large worker: one large request at a time through the whole-GPU
+// drivers on the large context, yielding to batches between iterations.
+void large_worker(cfx_server* sv) {
+    cudaSetDevice(sv->ctxLarge->device);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        sv->cvWork.wait(lk, [&] {
+            return sv->stop || (sv->owner == GPU_FREE && !sv->largeActive && next_ready(sv, true));
+        });
+        if (sv->stop) return;
+        SrvRequest* r = next_ready(sv, true);
+        SrvMatrix* m = sv->mats[r->matrixId].get();
+        sv->queue.erase(std::find(sv->queue.begin(), sv->queue.end(), r->id));
+        m->busy = true;
+        r->state = Q_RUNNING;
+        sv->owner = GPU_LARGE;
+        sv->largeActive = true;
+        sv->running += 1;
+        lk.unlock();
+        cfx_status st = CFX_OK;
+        std::string err;
+        try {
+            cfx_perf perf;
+            std::memset(&perf, 0, sizeof(perf));
+            st = cfx_solve_device(m->mat, &r->ctl, r->d_psi, r->d_b, &perf);
+            if (st != CFX_OK) err = cfx_last_error();
+            r->perf = perf;
+        } catch (const std::exception& e) {
+            st = CFX_ERR_CUDA;
+            err = e.what();
         }
-        for (SrvRequest* r : rs) {
-            r->status = st;
-            r->error = err;
-            r->perf.status = st;
-            finish(sv, *r, st == CFX_OK ? Q_DONE : Q_FAILED);
-        }
-        drop_detached(sv);
-        reap(sv);
-        sv->cvDone.notify_all();
+        lk.lock();
+        sv->running -= 1;
+        ++sv->largeSolves;
+        sv->owner = GPU_FREE;
+        sv->largeActive = false;
+        std::vector<SrvRequest*> rs{r};
+        finish_all(sv, rs, st, err);
     }
 }
 
@@ -371,7 +445,10 @@ cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_ser
         CFX_TRY(cfx_ctx_create(ctx->device, &sv->ctxLarge));
         CK(cudaMalloc(&sv->d_next, 2 * sizeof(unsigned)));
         sv->t0 = Clock::now();
-        sv->worker = std::thread(worker_loop, sv.get());
+        sv->ctxLarge->yield = large_yield;
+        sv->ctxLarge->yieldArg = sv.get();
+        sv->worker = std::thread(batch_worker, sv.get());
+        sv->largeWorker = std::thread(large_worker, sv.get());
         ctx_retain(ctx);
         *out = sv.release();
         return CFX_OK;
@@ -386,6 +463,7 @@ cfx_status cfx_server_destroy(cfx_server* sv) {
     }
     sv->cvWork.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    if (sv->largeWorker.joinable()) sv->largeWorker.join();
     cudaStreamSynchronize(sv->ctx->stream);
     for (auto& kv : sv->reqs) free_request_buffers(sv, *kv.second);
     sv->reqs.clear();
@@ -549,7 +627,7 @@ cfx_status cfx_server_submit(cfx_server* sv, int64_t matrixId, const cfx_control
     }
     *requestId = rp->id;
     sv->queue.push_back(rp->id);
-    sv->cvWork.notify_one();
+    sv->cvWork.notify_all();
     return CFX_OK;
 }
 
@@ -671,6 +749,7 @@ cfx_status cfx_server_stats(cfx_server* sv, cfx_server_stats_t* o) {
         for (double x : v) sum += x;
         o->meanMs = sum / double(v.size());
     }
+    o->largeYields = sv->yields;
     return CFX_OK;
 }
 
@@ -679,7 +758,7 @@ cfx_status cfx_server_reset_stats(cfx_server* sv) {
     std::lock_guard<std::mutex> lk(sv->mu);
     sv->t0 = Clock::now();
     sv->submitted = sv->completed = sv->cancelled = sv->failed = sv->refused = 0;
-    sv->batches = sv->batchedSolves = sv->largeSolves = 0;
+    sv->batches = sv->batchedSolves = sv->largeSolves = sv->yields = 0;
     sv->latMs.clear();
     return CFX_OK;
 }

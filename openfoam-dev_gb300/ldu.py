@@ -88,7 +88,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "cancelled", "failed", "refused", "batches",
                                               "batchedSolves", "largeSolves", "queueDepth", "running",
                                               "residentMatrices", "hbmInUse", "hbmBudget")] + \
-               [(k, ctypes.c_double) for k in ("elapsedS", "solvesPerS", "p50Ms", "p99Ms", "meanMs", "maxMs")]
+               [(k, ctypes.c_double) for k in ("elapsedS", "solvesPerS", "p50Ms", "p99Ms", "meanMs", "maxMs")] + \
+               [("largeYields", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -181,7 +181,22 @@ def serve_unloaded(mix, count, precision, seed=7):
         lat.setdefault(k, []).append(t)
     del rng
     return {"requests": count, "p50_ms": 1e3 * _pct(lat["all"], 0.5), "p99_ms": 1e3 * _pct(lat["all"], 0.99),
-            "by_kind_p50_ms": {k: 1e3 * _pct(v, 0.5) for k, v in lat.items() if k != "all"}}
+            "by_kind_p50_ms": {k: 1e3 * _pct(v, 0.5) for k, v in lat.items() if k != "all"},
+            "by_kind_p99_ms": {k: 1e3 * _pct(v, 0.99) for k, v in lat.items() if k != "all"},
+            "by_kind_n": {k: len(v) for k, v in lat.items() if k != "all"}}
+
+
+def per_kind_ratio(stream, unloaded):
+    """Each request kind's p99 under load over its p99 one at a time (and
+    over its median one at a time), and the worst of the first."""
+    out = {}
+    for k, v in stream["by_kind"].items():
+        u99 = unloaded["by_kind_p99_ms"].get(k)
+        u50 = unloaded["by_kind_p50_ms"].get(k)
+        out[k] = {"p99_over_unloaded_p99": v["p99_ms"] / u99 if u99 else None,
+                  "p99_over_unloaded_p50": v["p99_ms"] / u50 if u50 else None}
+    worst = [r["p99_over_unloaded_p99"] for r in out.values() if r["p99_over_unloaded_p99"] is not None]
+    return out, (max(worst) if worst else None)
 
 
 def serve_stream(mix, rate, duration, precision, seed=11, clients=64):
@@ -230,5 +245,5 @@ def serve_stream(mix, rate, duration, precision, seed=11, clients=64):
             "by_kind": {k: {"n": len(v), "p50_ms": 1e3 * _pct(v, 0.5), "p99_ms": 1e3 * _pct(v, 0.99)}
                         for k, v in by.items()},
             "converged": all(r[2] for r in results),
-            "server": {k: st[k] for k in ("batches", "batchedSolves", "largeSolves", "hbmInUse", "hbmBudget",
-                                          "refused", "failed")}}
+            "server": {k: st[k] for k in ("batches", "batchedSolves", "largeSolves", "largeYields", "hbmInUse",
+                                          "hbmBudget", "refused", "failed")}}

@@ -213,3 +213,40 @@ def test_server_asymmetric_requests_and_metrics():
     for k in ("solvesPerS", "p50Ms", "p99Ms", "queueDepth", "hbmInUse", "hbmBudget"):
         assert k in m
     sv.close()
+
+
+def test_small_requests_run_between_the_cycles_of_a_large_solve():
+    """Continuous batching across kinds: small requests that arrive while a
+    large GAMG solve runs are served in the gaps between its V-cycles (the
+    large solve yields the GPU to one batch at a time), finish long before
+    it, and every result equals the one computed alone."""
+    s = cases.gamg_cube(40, jitter=0.2, seed=4)
+    gctl = {"solver": "cudaGAMG", "smoother": "GaussSeidel", "nPreSweeps": 2, "tolerance": 1e-10, "relTol": 0.0}
+    sv = ldu.Server(largeCells=10000, groupCells=700)
+    big = sv.add_matrix(s, gamg=True)
+    systems = _boxes()
+    mids = [sv.add_matrix(x) for x in systems]
+    alone = [sv.wait(sv.submit(m, x["source"], CTL))[0] for m, x in zip(mids, systems)]
+    psi_big_alone, p_alone = sv.wait(sv.submit(big, s["source"], gctl))
+    sv.reset_stats()
+    import time
+    rid_big = sv.submit(big, s["source"], gctl)
+    t0 = time.perf_counter()
+    while sv.stats()["running"] < 1 and time.perf_counter() - t0 < 5.0:
+        time.sleep(0.0002)  # the large solve has started
+    t_small = []
+    rids = [sv.submit(m, x["source"], CTL) for m, x in zip(mids, systems)]
+    for k, rid in enumerate(rids):
+        psi, p = sv.wait(rid)
+        t_small.append(time.perf_counter())
+        np.testing.assert_array_equal(psi, alone[k])
+    psi_big, p_big = sv.wait(rid_big)
+    t_big = time.perf_counter()
+    np.testing.assert_array_equal(psi_big, psi_big_alone)
+    assert p_big.nIterations == p_alone.nIterations
+    st = sv.stats()
+    assert st["largeSolves"] == 1 and st["batchedSolves"] == len(systems)
+    # the small requests were served inside the large solve, not after it
+    assert st["largeYields"] >= 1
+    assert max(t_small) <= t_big
+    sv.close()

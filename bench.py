@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=0.0,
                     help="requests/s of the serving stream (0: the largest rate of the sweep at which every "
                          "request kind's p99 stays within 2x its unloaded p99)")
-    ap.add_argument("--serve-sweep-duration", type=float, default=15.0,
+    ap.add_argument("--serve-sweep-duration", type=float, default=10.0,
                     help="seconds per rate of the sweep that picks the serving rate (0: no sweep)")
     ap.add_argument("--serve-large", type=int, default=200, help="cells per axis of the large GAMG requests")
     return ap.parse_args()
@@ -766,7 +766,7 @@ def run_batch_serve(args, local, want_batch, want_serve):
                 rate = 0.3 * capacity
                 if args.serve_sweep_duration > 0:
                     sweep = []
-                    for f in (0.3, 0.5, 0.7, 0.9):
+                    for f in (0.3, 0.5, 0.7):
                         q = loadgen.serve_stream(mix, f * capacity, args.serve_sweep_duration, prec)
                         q["by_kind_ratio"], q["worst_kind_p99_over_unloaded_p99"] = loadgen.per_kind_ratio(q, un)
                         sweep.append(q)

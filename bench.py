@@ -490,14 +490,22 @@ def run_ours(args, rank, world, local, pg):
     levels = level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells)
 
     # the streaming kernels of the path (HBM-bound, no level chain), FP64 at
-    # the same size, each timed alone: Amul (3sN + sF + 8F), residual
-    # (4sN + sF + 8F)
+    # the same size, each timed alone: Amul (3sN + 2sF), residual
+    # (4sN + 2sF); rows read from the sliced ELL copy (the default) and,
+    # for comparison, through the losort/owner gathers
     d_b = d_src.clone()
     d_y = torch.empty_like(d_src)
     streaming = {
         "amul": (ev_time(lambda: A.Amul(d_b, d_y)), 3 * 8 * N + 8 * F + 8 * F),
         "residual": (ev_time(lambda: A.residual(d_b, d_src, d_y)), 4 * 8 * N + 8 * F + 8 * F),
     }
+    sell_was = ldu.tune_get(ldu.TUNE_AMUL_SELL)
+    ldu.tune_set(ldu.TUNE_AMUL_SELL, 0)
+    try:
+        streaming["amul_gather"] = (ev_time(lambda: A.Amul(d_b, d_y)), 3 * 8 * N + 8 * F + 8 * F)
+        streaming["residual_gather"] = (ev_time(lambda: A.residual(d_b, d_src, d_y)), 4 * 8 * N + 8 * F + 8 * F)
+    finally:
+        ldu.tune_set(ldu.TUNE_AMUL_SELL, sell_was)
 
     assembly = fvm_assembly_measure(ctx, ev_time, stream, local) if world == 1 else None
     krylov, krylov_psi = krylov_configs(ctx, stream, local) if world == 1 else (None, None)

@@ -156,6 +156,11 @@ cfx_status cfx_mesh_create(cfx_ctx* ctx, int nCells, int nFaces, const int32_t* 
 cfx_status cfx_mesh_destroy(cfx_mesh* mesh);
 /* Level-schedule depth of the forward (lower) DAG. */
 cfx_status cfx_mesh_info(cfx_mesh* mesh, int* nFwdLevels, int* nBwdLevels);
+/* The finest level's sliced ELL rows used by the A x products (no reference
+ * counterpart: the reference's products loop over faces): slices of 32 rows,
+ * how many are offset-pattern slices (no columns stored), and the entries
+ * including padding.  slices 0: not built (a row with over 255 neighbours). */
+cfx_status cfx_mesh_sell_info(cfx_mesh* mesh, int* slices, int* patternSlices, int64_t* entries);
 
 /* faceAreaPair weights |(Sf/sqrt|Sf|) * (1, 1.01, 1.02)|
  * (faceAreaPairGAMGAgglomeration.C:55-80) from face-area vectors Sf[nFaces*3]. */
@@ -318,7 +323,13 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
        CFX_TUNE_FLOW = 7,
        /* dataflow form: warps launched for this many levels of the
         * schedule's average width (default 4; 1..64) */
-       CFX_TUNE_FLOW_AHEAD = 8 };
+       CFX_TUNE_FLOW_AHEAD = 8,
+       /* A x products (Amul, residual, the solvers' fused products): 0
+        * gathers each row through losort/ownerStart; 1 and 2 (default) read
+        * it from the level's sliced ELL copy, 2 with the slices whose rows
+        * share at most 8 neighbour offsets stored without columns (1 or 2
+        * is read when a mesh is created).  The results are identical */
+       CFX_TUNE_AMUL_SELL = 9 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 
@@ -373,13 +384,15 @@ cfx_status cfx_batch_tune(cfx_batch* batch, const cfx_controls* ctl, int* best, 
  * (solver instances of several cases, a parametric study driver, a service
  * front end).  Matrices are registered once and stay resident in HBM;
  * requests bring a right-hand side (and initial psi) for a resident matrix,
- * so re-solving one (a PISO corrector) uploads two vectors.  One worker
- * thread drives the GPU: requests on small matrices are solved together in
- * one persistent launch whenever the GPU is free (continuous batching, one
- * precision per launch, at most one request per matrix at a time, up to
- * maxBatch); requests on large matrices (more than largeCells cells) run
- * alone through the whole-GPU drivers, with cudaGAMG when the matrix was
- * registered with face weights.  Admission: resident matrices and the
+ * so re-solving one (a PISO corrector) uploads two vectors.  Requests on
+ * small matrices are solved together in persistent launches (continuous
+ * batching: up to `lanes` launches run at once, each on its own stream and
+ * taking the queued requests of one precision and one size class, at most one
+ * request per matrix at a time, up to maxBatch), so a request that arrives
+ * while a launch runs starts on an idle lane at once; requests on large
+ * matrices (more than largeCells cells) run alone through the whole-GPU
+ * drivers, with cudaGAMG when the matrix was registered with face weights,
+ * yielding the GPU to the lanes between V-cycles.  Admission: resident matrices and the
  * requests' device vectors count against hbmBudget bytes; a matrix that does
  * not fit, or a request that alone exceeds the budget, is refused with
  * CFX_ERR_ADMISSION; a request that does not fit now blocks the submitting
@@ -394,6 +407,8 @@ typedef struct {
     int groupSize;              /* a thread-block cluster of groupSize CTAs (defaults 100,000 and 4;
                                  * 0: one CTA each); a result depends on its matrix only, never on
                                  * the rest of the launch */
+    int lanes;                  /* batch launches that may run at once, each on its own stream
+                                 * (default 4, 1..16) */
 } cfx_server_config;
 typedef struct {
     int64_t submitted, completed, cancelled, failed, refused;

@@ -158,6 +158,22 @@ void upload_schedule(Arena& ar, cudaStream_t s, const std::vector<int>& cells, c
     CK(cudaMemsetAsync(sch.sync, 0, sizeof(int) * (2 + std::max(nl, 1)), s));
 }
 
+// The level's rows in sliced ELL form (build_sell), when every row has at
+// most 255 neighbours.
+void upload_sell(Arena& ar, cudaStream_t s, const HostLevel& h, LevelMesh& m) {
+    HostSell hs;
+    if (!build_sell(h, amul_sell() == 2, hs)) return;
+    m.sellStart = ar.upload(hs.start, s);
+    m.sellCnt = ar.upload(hs.cnt, s);
+    m.sellCol = ar.upload(hs.col, s);
+    m.sellSrc = ar.upload(hs.src, s);
+    m.sellPat = ar.upload(hs.pat, s);
+    m.sellOffs = hs.offs.empty() ? nullptr : ar.upload(hs.offs, s);
+    m.sellEntries = hs.entries;
+    m.sellPatterns = hs.patterns;
+    m.sellPatternSlices = hs.patternSlices;
+}
+
 void upload_level(Arena& ar, cudaStream_t s, const HostLevel& h, LevelMesh& m) {
     m.n = h.n;
     m.nf = h.nf;
@@ -169,6 +185,7 @@ void upload_level(Arena& ar, cudaStream_t s, const HostLevel& h, LevelMesh& m) {
     m.losortL = ar.upload(h.losortL, s);
     upload_schedule(ar, s, h.fwdCells, h.fwdLevelStart, m.fwd);
     upload_schedule(ar, s, h.bwdCells, h.bwdLevelStart, m.bwd);
+    upload_sell(ar, s, h, m);
 }
 
 // Inverse restriction maps of level h (fine) -> coarse, for the gathers.
@@ -217,6 +234,7 @@ void alloc_coeffs(Arena& ar, const LevelMesh& m, bool sym, LevelCoeffs<T>& c) {
     c.lowerPerm = ar.get<T>(m.nf);
     c.upperPerm = sym ? nullptr : ar.get<T>(m.nf);
     c.rD = ar.get<T>(m.n);
+    c.sellCoef = m.sellCol ? ar.get<T>(m.sellEntries) : nullptr;
 }
 
 // GAMG hierarchy from level-0 restriction maps (host), then upload.
@@ -444,6 +462,7 @@ void prepare_levels(cfx_matrix* mat, bool want32) {
                 launch_cast_d2f(s, m.n, mat->c64[i].diag, mat->c32[i].diag);
                 launch_cast_d2f(s, m.nf, mat->c64[i].upper, mat->c32[i].upper);
                 launch_cast_d2f(s, m.nf, mat->c64[i].lowerPerm, mat->c32[i].lowerPerm);
+                if (m.sellCol) launch_cast_d2f(s, m.sellEntries, mat->c64[i].sellCoef, mat->c32[i].sellCoef);
                 if (!mat->sym) {
                     launch_cast_d2f(s, m.nf, mat->c64[i].lower, mat->c32[i].lower);
                     launch_cast_d2f(s, m.nf, mat->c64[i].upperPerm, mat->c32[i].upperPerm);
@@ -718,6 +737,7 @@ void setup_preconditioner_t(cfx_matrix* mat, int lv, int kind) {
     t.upper = c.lower;
     t.lowerPerm = c.upperPerm;
     t.upperPerm = c.lowerPerm;
+    t.sellCoef = nullptr;
     const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
     const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
     pack_sweep<T>(s, f, OP_FWD, t, packedT<T>(mat, lv, OP_FWD, f));
@@ -802,7 +822,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1297,7 +1317,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -1769,6 +1789,15 @@ cfx_status cfx_mesh_info(cfx_mesh* mesh, int* nFwd, int* nBwd) {
     if (!mesh) return CFX_ERR_ARG;
     if (nFwd) *nFwd = mesh->dev[0].fwd.nLevels;
     if (nBwd) *nBwd = mesh->dev[0].bwd.nLevels;
+    return CFX_OK;
+}
+
+cfx_status cfx_mesh_sell_info(cfx_mesh* mesh, int* slices, int* patternSlices, int64_t* entries) {
+    if (!mesh) return CFX_ERR_ARG;
+    const LevelMesh& m = mesh->dev[0];
+    if (slices) *slices = m.sellCol ? (m.n + 31) / 32 : 0;
+    if (patternSlices) *patternSlices = m.sellCol ? m.sellPatternSlices : 0;
+    if (entries) *entries = m.sellCol ? m.sellEntries : 0;
     return CFX_OK;
 }
 
@@ -2255,6 +2284,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value < 1 || value > 64) return CFX_ERR_ARG;
             set_sweep_flow_ahead(value);
             return CFX_OK;
+        case CFX_TUNE_AMUL_SELL:
+            if (value < 0 || value > 2) return CFX_ERR_ARG;
+            set_amul_sell(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2271,6 +2304,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_GRID_WAVE: *value = sweep_wave(); return CFX_OK;
         case CFX_TUNE_FLOW: *value = sweep_flow(); return CFX_OK;
         case CFX_TUNE_FLOW_AHEAD: *value = sweep_flow_ahead(); return CFX_OK;
+        case CFX_TUNE_AMUL_SELL: *value = amul_sell(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

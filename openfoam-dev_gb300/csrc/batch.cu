@@ -123,9 +123,30 @@ size_t coef_layout(BSys& sys, char* base, size_t* coefPart) {
 
 }  // namespace
 
+namespace {
+
+void* bsys_alloc(const BSys& sys, size_t bytes) {
+    void* d = nullptr;
+    if (sys.pool)
+        CK(cudaMallocFromPoolAsync(&d, bytes, sys.pool, sys.poolStream));
+    else
+        CK(cudaMalloc(&d, bytes));
+    return d;
+}
+
+void bsys_free(const BSys& sys, void* p) {
+    if (!p) return;
+    if (sys.pool)
+        cudaFreeAsync(p, sys.poolStream);
+    else
+        cudaFree(p);
+}
+
+}  // namespace
+
 BSys::~BSys() {
-    if (dAddr) cudaFree(dAddr);
-    if (dCoef) cudaFree(dCoef);
+    bsys_free(*this, dAddr);
+    bsys_free(*this, dCoef);
 }
 
 size_t bsys_bytes_estimate(int n, int nf, bool sym) {
@@ -212,9 +233,7 @@ cfx_status bsys_create(cudaStream_t s, int n, int nf, const int32_t* l, const in
     std::vector<char> img(sys.addrBytes, 0);
     Carve hc{img.data()};
     Carve dc{nullptr};
-    void* d = nullptr;
-    CK(cudaMalloc(&d, sys.addrBytes));
-    sys.dAddr = static_cast<char*>(d);
+    sys.dAddr = static_cast<char*>(bsys_alloc(sys, sys.addrBytes));
     dc.base = sys.dAddr;
     auto put = [&](const std::vector<int>& v, size_t count) -> const int* {
         int* hp = hc.take<int>(count);
@@ -261,16 +280,14 @@ void bsys_set_coeffs(cudaStream_t s, BSys& sys, const double* diag, const double
     const bool sym = lower == nullptr;
     if (sys.dCoef && sys.sym != sym) {
         CK(cudaStreamSynchronize(s));
-        cudaFree(sys.dCoef);
+        bsys_free(sys, sys.dCoef);
         sys.dCoef = nullptr;
     }
     sys.sym = sym;
     size_t part = 0;
     if (!sys.dCoef) {
         sys.coefBytes = coef_layout<false>(sys, nullptr, nullptr);
-        void* d = nullptr;
-        CK(cudaMalloc(&d, sys.coefBytes));
-        sys.dCoef = static_cast<char*>(d);
+        sys.dCoef = static_cast<char*>(bsys_alloc(sys, sys.coefBytes));
     }
     coef_layout<true>(sys, sys.dCoef, &part);
     // host image of the uploaded part, in the device layout

@@ -24,6 +24,10 @@ struct BSys {
     bool sym = true, hasCoeffs = false;
     char* dAddr = nullptr;    // addressing allocation
     char* dCoef = nullptr;    // coefficients + work allocation
+    // with a pool, both allocations are stream-ordered on poolStream (no
+    // device-wide synchronisation when they are made or freed)
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t poolStream = nullptr;
     size_t addrBytes = 0, coefBytes = 0;
     SlotSys<double> h64{};    // pointers into the allocations (bCell, psiCell unset)
     SlotSys<float> h32{};

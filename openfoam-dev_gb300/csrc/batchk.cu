@@ -576,10 +576,25 @@ __device__ __forceinline__ void store_results(SlotSys<double>* s64, int i, const
     o.tEnd = globaltimer_ns();
 }
 
+// The finished system's result to host-mapped memory, flag last (one
+// thread, after every thread of the system's CTAs fenced its stores).
+__device__ __forceinline__ void publish(BatchDone* done, int i, const SlotSys<double>& a) {
+    BatchDone& d = done[i];
+    d.initialResidual = a.initialResidual;
+    d.finalResidual = a.finalResidual;
+    d.nIterations = a.nIterations;
+    d.converged = a.converged;
+    d.singular = a.singular;
+    d.nOuter = a.nOuter;
+    __threadfence_system();
+    *reinterpret_cast<volatile unsigned*>(&d.flag) = 1u;
+}
+
 // Persistent batch, one CTA per system: each CTA takes the next system from
 // next[1] until all are done (the host orders them largest first).
 __global__ void __launch_bounds__(BLK_NT, 2) batch_k(SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int mixed,
-                                                     double innerRelTol, int maxOuter, unsigned* next) {
+                                                     double innerRelTol, int maxOuter, unsigned* next,
+                                                     BatchDone* done) {
     __shared__ double sh[BLK_NT / 32 + 1];
     __shared__ int sIdx;
     __shared__ SlotSys<double> rec;
@@ -594,7 +609,14 @@ __global__ void __launch_bounds__(BLK_NT, 2) batch_k(SlotSys<double>* s64, SlotS
         const unsigned long long t0 = globaltimer_ns();
         load_records(s64, s32, i, rec, rec32);
         batch_one(g, rec, &rec32, mixed, innerRelTol, maxOuter);
-        if (threadIdx.x == 0) store_results(s64, i, rec, t0);
+        if (done) {
+            __threadfence_system();
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            store_results(s64, i, rec, t0);
+            if (done) publish(done, i, rec);
+        }
         __syncthreads();
     }
 }
@@ -606,7 +628,7 @@ __global__ void __launch_bounds__(BLK_NT, 2) batch_k(SlotSys<double>* s64, SlotS
 // touches another's shared memory after phase 1's last cluster barrier.
 __global__ void __launch_bounds__(BLK_NT, 2) batch_cluster_k(SlotSys<double>* s64, SlotSys<float>* s32, int nSys,
                                                              int nBig, int mixed, double innerRelTol, int maxOuter,
-                                                             unsigned* next) {
+                                                             unsigned* next, BatchDone* done) {
     __shared__ double sh[BLK_NT / 32 + 1];
     __shared__ double slot[2];
     __shared__ int sIdx;
@@ -623,7 +645,14 @@ __global__ void __launch_bounds__(BLK_NT, 2) batch_cluster_k(SlotSys<double>* s6
         const unsigned long long t0 = globaltimer_ns();
         load_records(s64, s32, i, rec, rec32);
         batch_one(cgp, rec, &rec32, mixed, innerRelTol, maxOuter);
-        if (cgp.leader()) store_results(s64, i, rec, t0);
+        if (done) {
+            __threadfence_system();
+            cl.sync();
+        }
+        if (cgp.leader()) {
+            store_results(s64, i, rec, t0);
+            if (done) publish(done, i, rec);
+        }
         __syncthreads();
     }
     CtaGroup g{sh};
@@ -636,21 +665,28 @@ __global__ void __launch_bounds__(BLK_NT, 2) batch_cluster_k(SlotSys<double>* s6
         const unsigned long long t0 = globaltimer_ns();
         load_records(s64, s32, i, rec, rec32);
         batch_one(g, rec, &rec32, mixed, innerRelTol, maxOuter);
-        if (threadIdx.x == 0) store_results(s64, i, rec, t0);
+        if (done) {
+            __threadfence_system();
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            store_results(s64, i, rec, t0);
+            if (done) publish(done, i, rec);
+        }
         __syncthreads();
     }
 }
 }  // namespace
 
 void launch_batch(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nCta, int mixed,
-                  double innerRelTol, int maxOuter, unsigned* next) {
-    batch_k<<<nCta, BLK_NT, 0, s>>>(s64, s32, nSys, mixed, innerRelTol, maxOuter, next);
+                  double innerRelTol, int maxOuter, unsigned* next, BatchDone* done) {
+    batch_k<<<nCta, BLK_NT, 0, s>>>(s64, s32, nSys, mixed, innerRelTol, maxOuter, next, done);
     count_launch();
 }
 
 cudaError_t launch_batch_cluster(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nBig,
                                  int clusterSize, int nClusters, int mixed, double innerRelTol, int maxOuter,
-                                 unsigned* next) {
+                                 unsigned* next, BatchDone* done) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(clusterSize * nClusters);
     cfg.blockDim = dim3(BLK_NT);
@@ -664,7 +700,7 @@ cudaError_t launch_batch_cluster(cudaStream_t s, SlotSys<double>* s64, SlotSys<f
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const cudaError_t e =
-        cudaLaunchKernelEx(&cfg, batch_cluster_k, s64, s32, nSys, nBig, mixed, innerRelTol, maxOuter, next);
+        cudaLaunchKernelEx(&cfg, batch_cluster_k, s64, s32, nSys, nBig, mixed, innerRelTol, maxOuter, next, done);
     if (e == cudaSuccess) count_launch();
     return e;
 }

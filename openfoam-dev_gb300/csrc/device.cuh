@@ -32,6 +32,143 @@ __device__ __forceinline__ T row_amul(int c, const int* __restrict__ os, const i
 }
 
 
+// The rows of A in sliced ELL form: slices of 32 rows (one warp), each
+// row's entries in the order above (lower terms in losort order, then upper
+// terms in face order), stored in pairs so that a lane reads two entries of
+// its row with one 128-bit (FP64) coefficient load, and a warp reads 512
+// contiguous bytes: entry k of row c (lane j of slice s) sits at
+// start[s] + 64*(k/2) + 2*j + (k%2); a slice's width K is even.
+//
+// Two kinds of slice.  Explicit: cnt[c] entries, columns in col.  Pattern
+// (pat[s] >= 0): the slice's rows draw their neighbours from one ascending
+// list of at most 8 offsets, offs[8*pat[s] + k] (cell-index differences);
+// cnt[c] is then a mask of the offsets row c has, entry k holds the
+// coefficient of neighbour c + offs[k], and no column is read.  A row's
+// terms come in ascending column order either way (lower neighbours before
+// upper ones, each in face order), so both kinds keep the reference's order.
+// col == nullptr: not built (rows with more than 255 entries); the kernels
+// then gather through losort/ownerStart.
+template <class T>
+struct Sell {
+    const int* start = nullptr;          // [slices + 1] first entry of each slice
+    const unsigned char* cnt = nullptr;  // [n] entries of each row, or its offset mask
+    const int* col = nullptr;
+    const T* coef = nullptr;
+    const int* pat = nullptr;   // [slices] offset list of each slice, -1 explicit (null: all explicit)
+    const int* offs = nullptr;  // [8 x lists]
+};
+
+template <class T>
+inline Sell<T> sell_of(const LevelMesh& m, const LevelCoeffs<T>& a) {
+    Sell<T> S;
+    const int form = amul_sell();
+    if (m.sellCol && a.sellCoef && form) {
+        S.start = m.sellStart;
+        S.cnt = m.sellCnt;
+        S.col = m.sellCol;
+        S.coef = a.sellCoef;
+        S.pat = m.sellPat;
+        S.offs = m.sellOffs;
+    }
+    return S;
+}
+
+template <class T>
+struct Pair2;
+template <>
+struct Pair2<double> {
+    using type = double2;
+};
+template <>
+struct Pair2<float> {
+    using type = float2;
+};
+
+template <int OP, class T>
+__device__ __forceinline__ T sell_acc(T acc, T a, T x) {
+    return OP == 0 ? acc + a * x : acc - a * x;
+}
+
+// acc op= the row's terms in order: OP 0 adds coef*x[col], OP 1 subtracts.
+// Slices up to 8 wide issue every load of the row before the first product
+// (two dependent rounds: coefficients and columns, then x).
+template <class T, int OP>
+__device__ __forceinline__ T sell_row(int c, const Sell<T>& S, const T* __restrict__ x, T acc) {
+    using P2 = typename Pair2<T>::type;
+    const int sl = c >> 5;
+    const int s0 = __ldg(S.start + sl);
+    const int K = (__ldg(S.start + sl + 1) - s0) >> 5;
+    const int e0 = s0 + 2 * (c & 31);
+    const int k1 = __ldg(S.cnt + c);
+    const int p = S.pat ? __ldg(S.pat + sl) : -1;
+    if (K <= 8) {
+        P2 cf[4];
+        T xv[8];
+        if (p >= 0) {
+            const int* __restrict__ off = S.offs + 8 * p;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (2 * q < K) cf[q] = __ldg(reinterpret_cast<const P2*>(S.coef + e0 + 64 * q));
+#pragma unroll
+            for (int k = 0; k < 8; ++k) xv[k] = (k < K && ((k1 >> k) & 1)) ? x[c + __ldg(off + k)] : T(0);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < K && ((k1 >> k) & 1)) acc = sell_acc<OP>(acc, (k & 1) ? cf[k >> 1].y : cf[k >> 1].x, xv[k]);
+            return acc;
+        }
+        int2 cl[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (2 * q < K) {
+                cf[q] = __ldg(reinterpret_cast<const P2*>(S.coef + e0 + 64 * q));
+                cl[q] = __ldg(reinterpret_cast<const int2*>(S.col + e0 + 64 * q));
+            }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (2 * q < k1) xv[2 * q] = x[cl[q].x];
+            if (2 * q + 1 < k1) xv[2 * q + 1] = x[cl[q].y];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < k1) acc = sell_acc<OP>(acc, (k & 1) ? cf[k >> 1].y : cf[k >> 1].x, xv[k]);
+        return acc;
+    }
+    // wider explicit slices (pattern slices are at most 8 wide)
+    for (int k = 0; k < k1; k += 2) {
+        const int e = e0 + 32 * k;
+        const P2 cf = __ldg(reinterpret_cast<const P2*>(S.coef + e));
+        const int2 cl = __ldg(reinterpret_cast<const int2*>(S.col + e));
+        acc = sell_acc<OP>(acc, cf.x, x[cl.x]);
+        if (k + 1 < k1) acc = sell_acc<OP>(acc, cf.y, x[cl.y]);
+    }
+    return acc;
+}
+
+// One row of A x from whichever form the level has.
+template <class T>
+__device__ __forceinline__ T row_ax(int c, const int* __restrict__ os, const int* __restrict__ ls,
+                                    const int* __restrict__ lL, const int* __restrict__ u,
+                                    const T* __restrict__ diag, const T* __restrict__ lp,
+                                    const T* __restrict__ upper, const Sell<T>& S, const T* __restrict__ x) {
+    if (S.col) return sell_row<T, 0>(c, S, x, diag[c] * x[c]);
+    return row_amul<T>(c, os, ls, lL, u, diag, lp, upper, x);
+}
+
+// lduMatrix::residual's order for one row (lduMatrixATmul.C:203-280):
+// b - diag*x, then minus each neighbour product.
+template <class T>
+__device__ __forceinline__ T row_res(int c, const int* __restrict__ os, const int* __restrict__ ls,
+                                     const int* __restrict__ lL, const int* __restrict__ u,
+                                     const T* __restrict__ diag, const T* __restrict__ lp,
+                                     const T* __restrict__ upper, const Sell<T>& S, const T* __restrict__ x,
+                                     const T* __restrict__ b) {
+    T acc = b[c] - diag[c] * x[c];
+    if (S.col) return sell_row<T, 1>(c, S, x, acc);
+    for (int k = ls[c]; k < ls[c + 1]; ++k) acc -= lp[k] * x[lL[k]];
+    for (int f = os[c]; f < os[c + 1]; ++f) acc -= upper[f] * x[u[f]];
+    return acc;
+}
+
 // lduMatrix::updateMatrixInterfaces with cyclic fields
 // (cyclicFvPatchField.C:150-174): acc -= coeffs*psi[nbr], face by face.
 template <class T>

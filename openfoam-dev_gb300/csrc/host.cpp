@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <map>
 
 #include "internal.h"
 
@@ -417,6 +418,113 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
         for (int d : ds) o.dep.push_back(d);
         o.depStart.push_back(int(o.dep.size()));
     }
+}
+
+// The level's rows in sliced ELL form (Sell in device.cuh): slices of 32
+// rows, each row's entries in the reference's order (losort slots, then
+// owner faces), stored in pairs: entry k of row c at
+// start[c/32] + 64*(k/2) + 2*(c%32) + k%2.  With patterns, a slice whose
+// rows' neighbour offsets are each ascending and together take at most 8
+// values becomes a pattern slice: its entries sit at the offsets' positions
+// in the slice's sorted offset list, cnt[c] is the row's offset mask, and no
+// column is read.  False (nothing built) when a row has more than 255
+// entries or the entries overflow 32-bit indices.
+bool build_sell(const HostLevel& h, bool patterns, HostSell& out) {
+    const int n = h.n;
+    const int ns = (n + 31) / 32;
+    out = HostSell();
+    std::vector<unsigned char>& cnt = out.cnt;
+    cnt.assign(n, 0);
+    for (int c = 0; c < n; ++c) {
+        const int k = (h.losortStart[c + 1] - h.losortStart[c]) + (h.ownerStart[c + 1] - h.ownerStart[c]);
+        if (k > 255) return false;
+        cnt[c] = static_cast<unsigned char>(k);
+    }
+    // each row's neighbours in the product's order: (column, coefficient source)
+    auto row = [&](int c, std::vector<std::pair<int, int>>& nb) {
+        nb.clear();
+        for (int q = h.losortStart[c]; q < h.losortStart[c + 1]; ++q) nb.emplace_back(h.losortL[q], q);
+        for (int f = h.ownerStart[c]; f < h.ownerStart[c + 1]; ++f) nb.emplace_back(h.u[f], f | SRC_UPPER);
+    };
+    std::vector<int>& start = out.start;
+    std::vector<int>& pat = out.pat;
+    start.assign(ns + 1, 0);
+    pat.assign(ns, -1);
+    std::map<std::vector<int>, int> patIndex;
+    std::vector<std::vector<int>> slicePat(ns);
+    std::vector<std::pair<int, int>> nb;
+    int64_t nE = 0;
+    for (int sl = 0; sl < ns; ++sl) {
+        const int c0 = 32 * sl, c1 = std::min(n, c0 + 32);
+        int K = 0;
+        for (int c = c0; c < c1; ++c) K = std::max(K, int(cnt[c]));
+        std::vector<int> u;
+        bool ok = patterns;
+        for (int c = c0; c < c1 && ok; ++c) {
+            row(c, nb);
+            for (size_t k = 0; k < nb.size(); ++k) {
+                if (k && nb[k].first <= nb[k - 1].first) ok = false;
+                u.push_back(nb[k].first - c);
+            }
+        }
+        if (ok) {
+            std::sort(u.begin(), u.end());
+            u.erase(std::unique(u.begin(), u.end()), u.end());
+            ok = !u.empty() && u.size() <= 8;
+        }
+        if (ok) {
+            if (u.size() & 1) u.push_back(u.back());  // pad to the pair width (sorted); its bit is never set
+            auto it = patIndex.find(u);
+            if (it == patIndex.end()) {
+                const int idx = int(patIndex.size());
+                it = patIndex.emplace(u, idx).first;
+                std::vector<int> o(8, 0);
+                std::copy(u.begin(), u.end(), o.begin());
+                out.offs.insert(out.offs.end(), o.begin(), o.end());
+            }
+            pat[sl] = it->second;
+            K = int(u.size());
+            slicePat[sl] = u;
+        }
+        K = (K + 1) & ~1;
+        nE += 32 * int64_t(K);
+        if (nE > std::numeric_limits<int>::max()) return false;  // entry indices are 32-bit
+        start[sl + 1] = int(nE);
+    }
+    out.col.assign(std::max<int64_t>(nE, 1), 0);
+    out.src.assign(std::max<int64_t>(nE, 1), -1);
+    int nPat = 0;
+    for (int sl = 0; sl < ns; ++sl) {
+        const int K = (start[sl + 1] - start[sl]) / 32;
+        const bool isPat = pat[sl] >= 0;
+        nPat += isPat;
+        for (int c = 32 * sl; c < std::min(n, 32 * sl + 32); ++c) {
+            const int j = c & 31;
+            auto at = [&](int k) { return int64_t(start[sl]) + 64 * (k >> 1) + 2 * j + (k & 1); };
+            for (int k = 0; k < K; ++k) out.col[at(k)] = c;  // padding: a valid column, never read
+            row(c, nb);
+            if (isPat) {
+                const std::vector<int>& u = slicePat[sl];
+                unsigned mask = 0;
+                for (const auto& e : nb) {
+                    const int k = int(std::lower_bound(u.begin(), u.end(), e.first - c) - u.begin());
+                    out.col[at(k)] = e.first;
+                    out.src[at(k)] = e.second;
+                    mask |= 1u << k;
+                }
+                cnt[c] = static_cast<unsigned char>(mask);
+            } else {
+                for (size_t k = 0; k < nb.size(); ++k) {
+                    out.col[at(int(k))] = nb[k].first;
+                    out.src[at(int(k))] = nb[k].second;
+                }
+            }
+        }
+    }
+    out.entries = nE;
+    out.patterns = int(patIndex.size());
+    out.patternSlices = nPat;
+    return true;
 }
 
 }  // namespace cfx

@@ -77,6 +77,15 @@ struct LevelMesh {
     int n = 0, nf = 0;
     int *l = nullptr, *u = nullptr, *ownerStart = nullptr, *losortStart = nullptr;
     int *losort = nullptr, *losortL = nullptr;
+    // the rows in sliced ELL form (Sell in device.cuh): slice starts, entry
+    // counts, columns and each entry's coefficient source (a losort slot, or
+    // an owner face | SRC_UPPER; -1 padding); sellCol null when not built
+    int* sellStart = nullptr;
+    unsigned char* sellCnt = nullptr;
+    int *sellCol = nullptr, *sellSrc = nullptr;
+    int *sellPat = nullptr, *sellOffs = nullptr;  // offset-pattern slices
+    int64_t sellEntries = 0;
+    int sellPatterns = 0, sellPatternSlices = 0;
     Schedule fwd, bwd;
     // restriction to the next coarser level (valid when nCoarse > 0)
     int nCoarse = 0, nCoarseFaces = 0;
@@ -108,6 +117,7 @@ struct LevelCoeffs {
     bool sym = true;
     T *diag = nullptr, *upper = nullptr, *lower = nullptr;
     T *lowerPerm = nullptr, *upperPerm = nullptr;
+    T* sellCoef = nullptr;  // the coefficients in the level's sliced ELL order
     T* rD = nullptr;
     // interfaceBouCoeffs / interfaceIntCoeffs in the mesh's interface CSR
     // order (null: none set)
@@ -338,6 +348,11 @@ int sweep_flow();
 void set_sweep_flow(int on);
 int sweep_flow_ahead();
 void set_sweep_flow_ahead(int k);
+// A x products: 0 the losort/owner gathers, 1 the sliced ELL rows with
+// explicit columns, 2 (default) sliced ELL with offset-pattern slices (1/2
+// read when a level's rows are uploaded)
+int amul_sell();
+void set_amul_sell(int on);
 // the dataflow form's value buffers: sweeps x cells of the schedule (0: none)
 size_t sweep_flow_values(const DevSched& s, int op);
 void set_sweep_smem_cap(size_t b);
@@ -350,6 +365,14 @@ void set_cluster_global_cells(int n);
 
 // ---- host addressing (host.cpp) ----------------------------------------------
 cfx_status build_host_level(int n, int nf, const int* l, const int* u, HostLevel& h, bool validate);
+// A level's rows in sliced ELL form (Sell in device.cuh), built on the host.
+struct HostSell {
+    std::vector<int> start, pat, offs, col, src;
+    std::vector<unsigned char> cnt;
+    int64_t entries = 0;
+    int patterns = 0, patternSlices = 0;
+};
+bool build_sell(const HostLevel& h, bool patterns, HostSell& out);
 void build_schedules(HostLevel& h);
 int pair_agglomerate(int nFine, int nFaces, const int* l, const int* u, const double* w,
                      bool& forward, std::vector<int>& map);

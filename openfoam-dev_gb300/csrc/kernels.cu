@@ -41,16 +41,10 @@ __global__ void __launch_bounds__(RED_NT) amul_k(int n, const int* __restrict__ 
                                                  const int* __restrict__ losortStart,
                                                  const int* __restrict__ losortL, const int* __restrict__ u,
                                                  const T* __restrict__ diag, const T* __restrict__ lp,
-                                                 const T* __restrict__ upper, const T* __restrict__ x,
+                                                 const T* __restrict__ upper, Sell<T> S, const T* __restrict__ x,
                                                  T* __restrict__ y, Iface<T> itf) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        T acc = diag[c] * x[c];
-        const int k1 = losortStart[c + 1];
-        for (int k = losortStart[c]; k < k1; ++k) acc += lp[k] * x[losortL[k]];
-        const int f1 = ownerStart[c + 1];
-        for (int f = ownerStart[c]; f < f1; ++f) acc += upper[f] * x[u[f]];
-        y[c] = iface_sub(itf, c, x, acc);
-    }
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        y[c] = iface_sub(itf, c, x, row_ax<T>(c, ownerStart, losortStart, losortL, u, diag, lp, upper, S, x));
 }
 
 template <class T>
@@ -58,16 +52,11 @@ __global__ void __launch_bounds__(RED_NT) residual_k(int n, const int* __restric
                                                      const int* __restrict__ losortStart,
                                                      const int* __restrict__ losortL, const int* __restrict__ u,
                                                      const T* __restrict__ diag, const T* __restrict__ lp,
-                                                     const T* __restrict__ upper, const T* __restrict__ x,
-                                                     const T* __restrict__ b, T* __restrict__ r, Iface<T> itf) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        T acc = b[c] - diag[c] * x[c];
-        const int k1 = losortStart[c + 1];
-        for (int k = losortStart[c]; k < k1; ++k) acc -= lp[k] * x[losortL[k]];
-        const int f1 = ownerStart[c + 1];
-        for (int f = ownerStart[c]; f < f1; ++f) acc -= upper[f] * x[u[f]];
-        r[c] = iface_sub_neg(itf, c, x, acc);
-    }
+                                                     const T* __restrict__ upper, Sell<T> S,
+                                                     const T* __restrict__ x, const T* __restrict__ b,
+                                                     T* __restrict__ r, Iface<T> itf) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        r[c] = iface_sub_neg(itf, c, x, row_res<T>(c, ownerStart, losortStart, losortL, u, diag, lp, upper, S, x, b));
 }
 
 template <class T>
@@ -96,6 +85,17 @@ __global__ void permute_k(int nf, const int* __restrict__ losort, const T* __res
         const int f = losort[k];
         lowerPerm[k] = lower[f];
         if (upperPerm) upperPerm[k] = upper[f];
+    }
+}
+
+// The coefficients in the level's sliced ELL order: a lower term from the
+// losort-permuted lower coefficients, an upper term from upper.
+template <class T>
+__global__ void sell_pack_k(int64_t nE, const int* __restrict__ src, const T* __restrict__ lowerPerm,
+                            const T* __restrict__ upper, T* __restrict__ coef) {
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < nE; e += int64_t(gridDim.x) * blockDim.x) {
+        const int sc = src[e];
+        coef[e] = sc < 0 ? T(0) : (sc & SRC_UPPER) ? upper[sc & (SRC_UPPER - 1)] : lowerPerm[sc];
     }
 }
 
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(RED_NT) reduce_k(int n, const T* __restrict__ 
 template <class T>
 void Ops<T>::amul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
     amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                               a.lowerPerm, a.upper, x, y, if_bou(m, a));
+                                               a.lowerPerm, a.upper, sell_of(m, a), x, y, if_bou(m, a));
     count_launch();
 }
 
@@ -420,8 +420,8 @@ template <class T>
 void Ops<T>::tmul(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, T* y) {
     // Tmul (lduMatrixATmul.C:95-151): y[u] += upper*x[l]; y[l] += lower*x[u]
     amul_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                               a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower, x, y,
-                                               if_int(m, a));
+                                               a.sym ? a.lowerPerm : a.upperPerm, a.sym ? a.upper : a.lower,
+                                               a.sym ? sell_of(m, a) : Sell<T>{}, x, y, if_int(m, a));
     count_launch();
 }
 
@@ -429,7 +429,7 @@ template <class T>
 void Ops<T>::residual(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, const T* x, const T* b,
                       T* r) {
     residual_k<T><<<grid_all(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                   a.lowerPerm, a.upper, x, b, r, if_bou(m, a));
+                                                   a.lowerPerm, a.upper, sell_of(m, a), x, b, r, if_bou(m, a));
     count_launch();
 }
 
@@ -440,12 +440,23 @@ void Ops<T>::sumA(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, T
     count_launch();
 }
 
+namespace {
+int g_amul_sell = 2;
+}
+int amul_sell() { return g_amul_sell; }
+void set_amul_sell(int on) { g_amul_sell = on; }
+
 template <class T>
 void Ops<T>::permute(cudaStream_t s, const LevelMesh& m, LevelCoeffs<T>& a) {
     if (m.nf == 0) return;
     permute_k<T><<<grid_for(m.nf), RED_NT, 0, s>>>(m.nf, m.losort, a.sym ? a.upper : a.lower, a.upper,
                                                    a.lowerPerm, a.sym ? nullptr : a.upperPerm);
     count_launch();
+    if (m.sellCol && a.sellCoef) {
+        sell_pack_k<T><<<grid_all(m.sellEntries), RED_NT, 0, s>>>(m.sellEntries, m.sellSrc, a.lowerPerm, a.upper,
+                                                                  a.sellCoef);
+        count_launch();
+    }
 }
 
 template <class T>

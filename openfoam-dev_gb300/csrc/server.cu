@@ -12,18 +12,25 @@
 //     count against an HBM budget.  A matrix or request that alone exceeds
 //     the budget is refused (CFX_ERR_ADMISSION); one that does not fit now
 //     waits (the submitting thread blocks) until completions free space.
-//   * Two worker threads share the GPU.  The batch worker takes every queued
-//     small request (at most one per matrix, up to maxBatch) and solves them
-//     in one persistent launch, one CTA or one thread-block cluster per
-//     system; requests that arrive meanwhile go into the next launch.  The
-//     large worker runs large requests one at a time through the whole-GPU
-//     drivers on its own context.  The whole-GPU drivers launch cooperative
-//     grids that must have the device to themselves, so the two do not run
-//     kernels at the same time; instead a large solve yields between its
-//     V-cycles (or batches of Krylov iterations) whenever small requests are
-//     waiting, the batch worker runs one launch in that gap, and the large
-//     solve resumes.  A small request waits at most one cycle of a large
-//     solve, not all of it.
+//   * Batch lanes and a large worker share the GPU.  A lane (a thread with
+//     its own stream and launch buffers) takes the queued small requests of
+//     the oldest one's precision and size class (cluster-sized systems or
+//     one-CTA systems), at most one per matrix, up to maxBatch, and solves
+//     them in one persistent launch, one CTA or one thread-block cluster per
+//     system.  Lanes run concurrently: the batch kernels never wait on each
+//     other (each CTA or cluster finishes its systems alone), so a request
+//     that arrives while a long launch runs starts at once on an idle lane
+//     on the SMs that launch leaves free, and one-CTA systems never wait for
+//     a cluster-sized one launched with them.  The large worker runs large
+//     requests one at a time through the whole-GPU drivers on its own
+//     context.  Those launch cooperative grids that must have the device to
+//     themselves, so large kernels and batch kernels never run at the same
+//     time: a large solve starts once the lanes are idle (lanes start
+//     nothing new while one waits), and yields between its V-cycles (or
+//     batches of Krylov iterations) whenever small requests are waiting:
+//     the idle lanes start launches in that gap, the gap closes when the
+//     first of them finishes, and the large solve resumes when all have.  A
+//     small request waits at most one cycle of a large solve, not all of it.
 //   * Completion is signalled per request; a request can be cancelled while
 //     it is queued (or its result dropped later), and requests whose client
 //     never collects them are freed at release or shutdown.
@@ -81,12 +88,28 @@ struct SrvRequest {
 
 }  // namespace
 
+// A batch lane: one launch at a time on its own stream.
+struct SrvLane {
+    cudaStream_t stream = nullptr;
+    SlotSys<double>* d64 = nullptr;
+    SlotSys<float>* d32 = nullptr;
+    SlotSys<double>* h64 = nullptr;
+    SlotSys<float>* h32 = nullptr;
+    BatchDone* hDone = nullptr;  // host-mapped per-system results ...
+    BatchDone* dDone = nullptr;  // ... and the kernels' view of them
+    unsigned* d_next = nullptr;
+    int cap = 0;
+    std::thread th;
+};
+
 struct cfx_server {
-    cfx_ctx* ctx = nullptr;           // batches run on its stream
+    cfx_ctx* ctx = nullptr;           // the device; batch lanes have their own streams
     cfx_ctx* ctxLarge = nullptr;      // large matrices: their uploads and solves
     cudaStream_t copyStream = nullptr;  // request vectors and small-matrix uploads
+    cudaMemPool_t pool = nullptr;       // their device memory, stream-ordered on copyStream
     cfx_server_config cfg{};
     int sms = 0;
+    int clusterMax = 0;  // clusters of cfg.groupSize CTAs resident at once (0: no cluster form)
     std::mutex mu;
     std::condition_variable cvWork;   // worker: something to do
     std::condition_variable cvDone;   // clients: a request finished / space freed
@@ -96,22 +119,14 @@ struct cfx_server {
     int64_t nextMat = 1, nextReq = 1;
     size_t used = 0;                  // bytes admitted (matrices + request vectors)
     bool stop = false;
-    std::thread worker;               // batches of small requests
-    std::thread largeWorker;          // large requests
-    // who runs kernels now (mu held): 0 nobody, 1 a batch, 2 a large solve;
-    // largeActive: a large solve is in progress (possibly yielding);
-    // yieldOpen: it has yielded for one batch; batchGen counts batches
-    int owner = 0;
+    std::vector<std::unique_ptr<SrvLane>> lanes;  // batches of small requests
+    std::thread largeWorker;                       // large requests
+    // (mu held) activeLanes: lanes running a launch; largeActive: a large
+    // solve is in progress (possibly yielding); yieldOpen: it has yielded
+    // and lanes may start; batchGen counts finished launches
+    int activeLanes = 0;
     bool largeActive = false, yieldOpen = false;
     int64_t batchGen = 0, yields = 0;
-    // launch buffers
-    SlotSys<double>* d64 = nullptr;
-    SlotSys<float>* d32 = nullptr;
-    SlotSys<double>* h64 = nullptr;
-    SlotSys<float>* h32 = nullptr;
-    unsigned* d_next = nullptr;
-    int cap = 0;
-    std::map<int, int> maxClusters;
     // statistics
     Clock::time_point t0;
     int64_t submitted = 0, completed = 0, cancelled = 0, failed = 0, refused = 0;
@@ -123,17 +138,13 @@ namespace {
 
 size_t large_estimate(int n, int nf) {
     // fine level + GAMG hierarchy (< the fine level again), FP64 and FP32
-    // coefficients, schedules and the drivers' work vectors
-    return size_t(n) * 420 + size_t(nf) * 96 + (size_t(64) << 20);
-}
-
-int max_clusters(cfx_server* sv, int cs) {
-    auto it = sv->maxClusters.find(cs);
-    if (it == sv->maxClusters.end()) it = sv->maxClusters.emplace(cs, batch_max_clusters(cs)).first;
-    return it->second;
+    // coefficients, the sliced ELL rows (about 2.3 entries a face of column,
+    // source and both coefficient copies), schedules and work vectors
+    return size_t(n) * 420 + size_t(nf) * 150 + (size_t(64) << 20);
 }
 
 void finish(cfx_server* sv, SrvRequest& r, ReqState st) {
+    const bool ran = r.state == Q_RUNNING;
     r.state = st;
     r.tDone = Clock::now();
     if (st == Q_DONE) {
@@ -144,7 +155,9 @@ void finish(cfx_server* sv, SrvRequest& r, ReqState st) {
     }
     auto m = sv->mats.find(r.matrixId);
     if (m != sv->mats.end()) {
-        m->second->busy = false;
+        // only the running request holds its matrix: cancelling a queued one
+        // must not free the matrix for a second launch while one runs on it
+        if (ran) m->second->busy = false;
         m->second->pending--;
     }
 }
@@ -191,82 +204,118 @@ void reap(cfx_server* sv) {
     }
 }
 
-void ensure_cap(cfx_server* sv, int k) {
-    if (k <= sv->cap) return;
-    const int c = std::max(k, 2 * sv->cap);
-    if (sv->d64) cudaFree(sv->d64);
-    if (sv->d32) cudaFree(sv->d32);
-    if (sv->h64) cudaFreeHost(sv->h64);
-    if (sv->h32) cudaFreeHost(sv->h32);
-    sv->d64 = nullptr;
-    sv->d32 = nullptr;
-    sv->h64 = nullptr;
-    sv->h32 = nullptr;
-    sv->cap = 0;
-    CK(cudaMalloc(&sv->d64, sizeof(SlotSys<double>) * c));
-    CK(cudaMalloc(&sv->d32, sizeof(SlotSys<float>) * c));
-    CK(cudaMallocHost(&sv->h64, sizeof(SlotSys<double>) * c));
-    CK(cudaMallocHost(&sv->h32, sizeof(SlotSys<float>) * c));
-    sv->cap = c;
+void ensure_cap(SrvLane& ln, int k) {
+    if (k <= ln.cap) return;
+    const int c = std::max(k, 2 * ln.cap);
+    if (ln.d64) cudaFree(ln.d64);
+    if (ln.d32) cudaFree(ln.d32);
+    if (ln.h64) cudaFreeHost(ln.h64);
+    if (ln.h32) cudaFreeHost(ln.h32);
+    if (ln.hDone) cudaFreeHost(ln.hDone);
+    ln.d64 = nullptr;
+    ln.d32 = nullptr;
+    ln.h64 = nullptr;
+    ln.h32 = nullptr;
+    ln.hDone = ln.dDone = nullptr;
+    ln.cap = 0;
+    CK(cudaMalloc(&ln.d64, sizeof(SlotSys<double>) * c));
+    CK(cudaMalloc(&ln.d32, sizeof(SlotSys<float>) * c));
+    CK(cudaMallocHost(&ln.h64, sizeof(SlotSys<double>) * c));
+    CK(cudaMallocHost(&ln.h32, sizeof(SlotSys<float>) * c));
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&ln.hDone), sizeof(BatchDone) * c, cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&ln.dDone), ln.hDone, 0));
+    ln.cap = c;
 }
 
-// Runs one batch of small requests (worker thread, lock not held): systems
-// of at least groupCells cells on clusters of groupSize CTAs, the others one
-// CTA each, largest first.
-void run_batch(cfx_server* sv, std::vector<SrvRequest*>& rs, std::vector<SrvMatrix*>& ms) {
+// A small matrix's size class: solved by a cluster of groupSize CTAs (1) or
+// by one CTA (0), by its size alone, so that a request's result does not
+// depend on what else is in the launch.
+int size_class(const cfx_server* sv, const SrvMatrix& m) {
+    return sv->cfg.groupSize > 1 && sv->clusterMax > 0 && m.n >= sv->cfg.groupCells;
+}
+
+// Runs one batch of small requests of one size class on a lane (lane
+// thread, lock not held), largest first.  Each system's result is published
+// by the kernel the moment it finishes (BatchDone in host-mapped memory):
+// the lane polls the flags while the launch runs and hands every finished
+// request to complete() at once, so a small system does not wait for the
+// largest of its launch.  done[i] marks the requests handed over.
+template <class Complete>
+void run_batch(cfx_server* sv, SrvLane& ln, std::vector<SrvRequest*>& rs, std::vector<SrvMatrix*>& ms,
+               std::vector<char>& done, Complete&& complete) {
     const int k = int(rs.size());
     std::vector<int> order(k);
     for (int i = 0; i < k; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ms[a]->n > ms[b]->n; });
-    ensure_cap(sv, k);
+    ensure_cap(ln, k);
     int mixed = 0;
     for (int j = 0; j < k; ++j) {
         const int i = order[j];
-        bsys_records(*ms[i]->bs, rs[i]->ctl, rs[i]->d_psi, rs[i]->d_b, sv->h64[j], sv->h32[j]);
+        bsys_records(*ms[i]->bs, rs[i]->ctl, rs[i]->d_psi, rs[i]->d_b, ln.h64[j], ln.h32[j]);
         mixed |= rs[i]->ctl.precision == CFX_MIXED;
     }
-    cudaStream_t s = sv->ctx->stream;
-    CK(cudaMemcpyAsync(sv->d64, sv->h64, sizeof(SlotSys<double>) * k, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(sv->d32, sv->h32, sizeof(SlotSys<float>) * k, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(sv->d_next, 0, 2 * sizeof(unsigned), s));
-    // group size by system size alone, so that a request's result does not
-    // depend on what else is in the launch
-    int cs = 0, nBig = 0;
-    if (sv->cfg.groupSize > 1 && max_clusters(sv, sv->cfg.groupSize) > 0) {
-        for (int j = 0; j < k; ++j)
-            if (ms[order[j]]->n >= sv->cfg.groupCells) nBig = j + 1;
-        if (nBig) cs = sv->cfg.groupSize;
-    }
+    std::memset(ln.hDone, 0, sizeof(BatchDone) * k);
+    cudaStream_t s = ln.stream;
+    CK(cudaMemcpyAsync(ln.d64, ln.h64, sizeof(SlotSys<double>) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ln.d32, ln.h32, sizeof(SlotSys<float>) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(ln.d_next, 0, 2 * sizeof(unsigned), s));
+    const bool clusters = size_class(sv, *ms[0]);
     const double innerRelTol = std::pow(10.0, -double(batch_inner_digits()));
-    // a mixed launch solves every system of it in mixed precision; the
-    // worker only batches requests of one precision together
-    if (cs)
-        CK(launch_batch_cluster(s, sv->d64, mixed ? sv->d32 : nullptr, k, nBig, cs, max_clusters(sv, cs), mixed,
-                                innerRelTol, 50, sv->d_next));
+    // a mixed launch solves every system of it in mixed precision; a lane
+    // only batches requests of one precision together
+    if (clusters)
+        CK(launch_batch_cluster(s, ln.d64, mixed ? ln.d32 : nullptr, k, k, sv->cfg.groupSize, sv->clusterMax, mixed,
+                                innerRelTol, 50, ln.d_next, ln.dDone));
     else
-        launch_batch(s, sv->d64, mixed ? sv->d32 : nullptr, k, std::min(k, sv->sms * batch_ctas_per_sm()), mixed,
-                     innerRelTol, 50, sv->d_next);
-    CK(cudaMemcpyAsync(sv->h64, sv->d64, sizeof(SlotSys<double>) * k, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    for (int j = 0; j < k; ++j) {
-        const SlotSys<double>& r = sv->h64[j];
+        launch_batch(s, ln.d64, mixed ? ln.d32 : nullptr, k, std::min(k, sv->sms * batch_ctas_per_sm()), mixed,
+                     innerRelTol, 50, ln.d_next, ln.dDone);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ln.h64, ln.d64, sizeof(SlotSys<double>) * k, cudaMemcpyDeviceToHost, s));
+    auto set_perf = [&](int j, double ini, double fin, int it, int conv, int sing, int outer) {
         SrvRequest& q = *rs[order[j]];
         std::memset(&q.perf, 0, sizeof(q.perf));
         std::snprintf(q.perf.solverName, sizeof(q.perf.solverName), "%s", bsys_solver_name(q.ctl));
-        q.perf.initialResidual = r.initialResidual;
-        q.perf.finalResidual = r.finalResidual;
-        q.perf.nIterations = r.nIterations;
-        q.perf.converged = r.converged;
-        q.perf.singular = r.singular;
-        q.perf.nOuter = mixed ? r.nOuter : 0;
+        q.perf.initialResidual = ini;
+        q.perf.finalResidual = fin;
+        q.perf.nIterations = it;
+        q.perf.converged = conv;
+        q.perf.singular = sing;
+        q.perf.nOuter = mixed ? outer : 0;
+    };
+    std::vector<SrvRequest*> now;
+    int left = k;
+    for (;;) {
+        now.clear();
+        for (int j = 0; j < k; ++j) {
+            if (done[order[j]] || !__atomic_load_n(&ln.hDone[j].flag, __ATOMIC_ACQUIRE)) continue;
+            const BatchDone& d = ln.hDone[j];
+            set_perf(j, d.initialResidual, d.finalResidual, d.nIterations, d.converged, d.singular, d.nOuter);
+            done[order[j]] = 1;
+            now.push_back(rs[order[j]]);
+        }
+        left -= int(now.size());
+        if (!now.empty()) complete(now);
+        if (left == 0) break;
+        const cudaError_t q = cudaStreamQuery(s);
+        if (q == cudaSuccess) break;  // the launch is over: the rest from its records
+        if (q != cudaErrorNotReady) CK(q);
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
+    CK(cudaStreamSynchronize(s));
+    now.clear();
+    for (int j = 0; j < k; ++j) {
+        if (done[order[j]]) continue;
+        const SlotSys<double>& r = ln.h64[j];
+        set_perf(j, r.initialResidual, r.finalResidual, r.nIterations, r.converged, r.singular, r.nOuter);
+        done[order[j]] = 1;
+        now.push_back(rs[order[j]]);
+    }
+    if (!now.empty()) complete(now);
 }
 
 }  // namespace
 
 namespace {
-
-enum { GPU_FREE = 0, GPU_BATCH = 1, GPU_LARGE = 2 };
 
 // A queued request of the kind the worker serves whose matrix is idle
 // (mu held).
@@ -292,21 +341,26 @@ void finish_all(cfx_server* sv, std::vector<SrvRequest*>& rs, cfx_status st, con
     sv->cvWork.notify_all();
 }
 
-// The batch worker: while no large solve runs (or one has yielded), every
-// queued small request of the oldest one's precision, at most one per
-// matrix, in one launch.
-void batch_worker(cfx_server* sv) {
+// Whether a lane may start a launch now (mu held): small requests are
+// ready, and either no large solve is in progress and none waits to start,
+// or the running one has yielded.
+bool lane_may_start(cfx_server* sv) {
+    if (!next_ready(sv, false)) return false;
+    if (sv->largeActive) return sv->yieldOpen;
+    return next_ready(sv, true) == nullptr;
+}
+
+// A batch lane: every queued small request of the oldest ready one's
+// precision and size class, at most one per matrix, in one launch.
+void lane_worker(cfx_server* sv, SrvLane* ln) {
     cudaSetDevice(sv->ctx->device);
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
-        sv->cvWork.wait(lk, [&] {
-            return sv->stop ||
-                   (sv->owner == GPU_FREE && (!sv->largeActive || sv->yieldOpen) && next_ready(sv, false));
-        });
+        sv->cvWork.wait(lk, [&] { return sv->stop || lane_may_start(sv); });
         if (sv->stop) return;
-        sv->owner = GPU_BATCH;
-        sv->yieldOpen = false;
-        const int prec = next_ready(sv, false)->ctl.precision;
+        SrvRequest* first = next_ready(sv, false);
+        const int prec = first->ctl.precision;
+        const int cls = size_class(sv, *sv->mats[first->matrixId]);
         std::vector<SrvRequest*> rs;
         std::vector<SrvMatrix*> ms;
         std::deque<int64_t> keep;
@@ -315,7 +369,8 @@ void batch_worker(cfx_server* sv) {
             sv->queue.pop_front();
             SrvRequest* r = sv->reqs[id].get();
             SrvMatrix* m = sv->mats[r->matrixId].get();
-            if (!m->large && !m->busy && r->ctl.precision == prec && int(rs.size()) < sv->cfg.maxBatch) {
+            if (!m->large && !m->busy && r->ctl.precision == prec && size_class(sv, *m) == cls &&
+                int(rs.size()) < sv->cfg.maxBatch) {
                 m->busy = true;
                 rs.push_back(r);
                 ms.push_back(m);
@@ -326,42 +381,51 @@ void batch_worker(cfx_server* sv) {
         sv->queue.swap(keep);
         for (SrvRequest* r : rs) r->state = Q_RUNNING;
         sv->running += int64_t(rs.size());
+        ++sv->activeLanes;
         lk.unlock();
+        std::vector<char> done(rs.size(), 0);
+        auto complete = [&](std::vector<SrvRequest*>& fin) {
+            std::lock_guard<std::mutex> g(sv->mu);
+            sv->running -= int64_t(fin.size());
+            finish_all(sv, fin, CFX_OK, std::string());
+        };
         cfx_status st = CFX_OK;
         std::string err;
         try {
-            run_batch(sv, rs, ms);
+            run_batch(sv, *ln, rs, ms, done, complete);
         } catch (const std::exception& e) {
             st = CFX_ERR_CUDA;
             err = e.what();
         }
         lk.lock();
-        sv->running -= int64_t(rs.size());
+        std::vector<SrvRequest*> rest;
+        for (size_t i = 0; i < rs.size(); ++i)
+            if (!done[i]) rest.push_back(rs[i]);
+        sv->running -= int64_t(rest.size());
         ++sv->batches;
         sv->batchedSolves += int64_t(rs.size());
-        sv->owner = GPU_FREE;
+        --sv->activeLanes;
         ++sv->batchGen;
-        finish_all(sv, rs, st, err);
+        sv->yieldOpen = false;  // a yield's gap closes at its first finished launch
+        finish_all(sv, rest, st, err);
     }
 }
 
 // Called by the large worker's solve between iterations (lock not held, the
-// device idle): when small requests wait, hand the GPU to the batch worker
-// for one launch and take it back after.
+// device idle): when small requests wait, open a gap for the lanes and take
+// the GPU back once the launches started in it have finished.
 void large_yield(void* arg) {
     cfx_server* sv = static_cast<cfx_server*>(arg);
     std::unique_lock<std::mutex> lk(sv->mu);
     if (sv->stop || !next_ready(sv, false)) return;
     const int64_t gen = sv->batchGen;
-    sv->owner = GPU_FREE;
     sv->yieldOpen = true;
     ++sv->yields;
     sv->cvWork.notify_all();
     sv->cvWork.wait(lk, [&] {
-        return sv->stop || (sv->owner == GPU_FREE && (sv->batchGen != gen || !next_ready(sv, false)));
+        return sv->stop || (sv->activeLanes == 0 && (sv->batchGen != gen || !next_ready(sv, false)));
     });
     sv->yieldOpen = false;
-    sv->owner = GPU_LARGE;
 }
 
 // The large worker: one large request at a time through the whole-GPU
@@ -371,7 +435,7 @@ void large_worker(cfx_server* sv) {
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         sv->cvWork.wait(lk, [&] {
-            return sv->stop || (sv->owner == GPU_FREE && !sv->largeActive && next_ready(sv, true));
+            return sv->stop || (sv->activeLanes == 0 && !sv->largeActive && next_ready(sv, true));
         });
         if (sv->stop) return;
         SrvRequest* r = next_ready(sv, true);
@@ -379,7 +443,6 @@ void large_worker(cfx_server* sv) {
         sv->queue.erase(std::find(sv->queue.begin(), sv->queue.end(), r->id));
         m->busy = true;
         r->state = Q_RUNNING;
-        sv->owner = GPU_LARGE;
         sv->largeActive = true;
         sv->running += 1;
         lk.unlock();
@@ -398,7 +461,6 @@ void large_worker(cfx_server* sv) {
         lk.lock();
         sv->running -= 1;
         ++sv->largeSolves;
-        sv->owner = GPU_FREE;
         sv->largeActive = false;
         std::vector<SrvRequest*> rs{r};
         finish_all(sv, rs, st, err);
@@ -419,6 +481,7 @@ void cfx_server_default_config(cfx_server_config* c) {
     c->nCellsInCoarsestLevel = 10;
     c->groupCells = 100000;
     c->groupSize = 4;
+    c->lanes = 4;
 }
 
 cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_server** out) {
@@ -435,19 +498,34 @@ cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_ser
             cfx_server_default_config(&sv->cfg);
         }
         if (sv->cfg.hbmBudget <= 0 || sv->cfg.largeCells < 1 || sv->cfg.maxBatch < 1 || sv->cfg.groupSize < 0 ||
-            sv->cfg.groupSize > 16) {
+            sv->cfg.groupSize > 16 || sv->cfg.lanes < 1 || sv->cfg.lanes > 16) {
             set_error("cfx_server_create: bad configuration");
             return CFX_ERR_ARG;
         }
         CK(cudaSetDevice(ctx->device));
         CK(cudaDeviceGetAttribute(&sv->sms, cudaDevAttrMultiProcessorCount, ctx->device));
         CK(cudaStreamCreateWithFlags(&sv->copyStream, cudaStreamNonBlocking));
+        // a pool of its own that keeps freed memory for reuse: registering,
+        // removing and serving small matrices never waits for the device
+        cudaMemPoolProps pp = {};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = ctx->device;
+        CK(cudaMemPoolCreate(&sv->pool, &pp));
+        uint64_t keep = UINT64_MAX;
+        CK(cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep));
         CFX_TRY(cfx_ctx_create(ctx->device, &sv->ctxLarge));
-        CK(cudaMalloc(&sv->d_next, 2 * sizeof(unsigned)));
+        if (sv->cfg.groupSize > 1) sv->clusterMax = batch_max_clusters(sv->cfg.groupSize);
+        for (int i = 0; i < sv->cfg.lanes; ++i) {
+            auto ln = std::make_unique<SrvLane>();
+            CK(cudaStreamCreateWithFlags(&ln->stream, cudaStreamNonBlocking));
+            CK(cudaMalloc(&ln->d_next, 2 * sizeof(unsigned)));
+            sv->lanes.push_back(std::move(ln));
+        }
         sv->t0 = Clock::now();
         sv->ctxLarge->yield = large_yield;
         sv->ctxLarge->yieldArg = sv.get();
-        sv->worker = std::thread(batch_worker, sv.get());
+        for (auto& ln : sv->lanes) ln->th = std::thread(lane_worker, sv.get(), ln.get());
         sv->largeWorker = std::thread(large_worker, sv.get());
         ctx_retain(ctx);
         *out = sv.release();
@@ -462,20 +540,27 @@ cfx_status cfx_server_destroy(cfx_server* sv) {
         sv->stop = true;
     }
     sv->cvWork.notify_all();
-    if (sv->worker.joinable()) sv->worker.join();
+    for (auto& ln : sv->lanes)
+        if (ln->th.joinable()) ln->th.join();
     if (sv->largeWorker.joinable()) sv->largeWorker.join();
-    cudaStreamSynchronize(sv->ctx->stream);
+    for (auto& ln : sv->lanes) cudaStreamSynchronize(ln->stream);
     for (auto& kv : sv->reqs) free_request_buffers(sv, *kv.second);
     sv->reqs.clear();
     for (auto& kv : sv->mats) free_matrix(sv, *kv.second);
     sv->mats.clear();
     cudaStreamSynchronize(sv->copyStream);
-    if (sv->d64) cudaFree(sv->d64);
-    if (sv->d32) cudaFree(sv->d32);
-    if (sv->h64) cudaFreeHost(sv->h64);
-    if (sv->h32) cudaFreeHost(sv->h32);
-    if (sv->d_next) cudaFree(sv->d_next);
+    for (auto& ln : sv->lanes) {
+        if (ln->d64) cudaFree(ln->d64);
+        if (ln->d32) cudaFree(ln->d32);
+        if (ln->h64) cudaFreeHost(ln->h64);
+        if (ln->h32) cudaFreeHost(ln->h32);
+        if (ln->hDone) cudaFreeHost(ln->hDone);
+        if (ln->d_next) cudaFree(ln->d_next);
+        if (ln->stream) cudaStreamDestroy(ln->stream);
+    }
+    sv->lanes.clear();
     cudaStreamDestroy(sv->copyStream);
+    if (sv->pool) cudaMemPoolDestroy(sv->pool);
     if (sv->ctxLarge) cfx_ctx_destroy(sv->ctxLarge);
     sv->cvDone.notify_all();
     cfx_ctx* ctx = sv->ctx;  // alive: the server holds a reference
@@ -518,6 +603,8 @@ cfx_status cfx_server_add_matrix(cfx_server* sv, int nCells, int nFaces, const i
             m->bytes = est;
         } else {
             m->bs = std::make_unique<BSys>();
+            m->bs->pool = sv->pool;
+            m->bs->poolStream = sv->copyStream;
             CFX_TRY(bsys_create(sv->copyStream, nCells, nFaces, l, u, *m->bs));
             bsys_set_coeffs(sv->copyStream, *m->bs, diag, upper, lower);
             m->bytes = m->bs->addrBytes + m->bs->coefBytes;
@@ -606,8 +693,8 @@ cfx_status cfx_server_submit(cfx_server* sv, int64_t matrixId, const cfx_control
     // device vectors and uploads outside the lock (the request is not queued yet)
     const cfx_status st = guard([&]() -> cfx_status {
         const size_t b = sizeof(double) * size_t(rp->n);
-        CK(cudaMallocAsync(&rp->d_psi, b, sv->copyStream));
-        CK(cudaMallocAsync(&rp->d_b, b, sv->copyStream));
+        CK(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&rp->d_psi), b, sv->pool, sv->copyStream));
+        CK(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&rp->d_b), b, sv->pool, sv->copyStream));
         if (psi0)
             CK(cudaMemcpyAsync(rp->d_psi, psi0, b, cudaMemcpyHostToDevice, sv->copyStream));
         else

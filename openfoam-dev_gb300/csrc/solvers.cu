@@ -162,13 +162,13 @@ __global__ void pcg_p_k(int n, const T* __restrict__ w, T* __restrict__ p, const
 
 template <class T>
 __global__ void __launch_bounds__(RED_NT) pcg_amul_k(int n, const int* os, const int* ls, const int* lL,
-                                                     const int* u, const T* diag, const T* lp, const T* upper,
+                                                     const int* u, const T* diag, const T* lp, const T* upper, Sell<T> S,
                                                      const T* __restrict__ p, T* __restrict__ wA, SolveState* st,
                                                      Red2 red, Iface<T> itf) {
     if (st->done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = iface_sub(itf, c, p, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, p));
+        const T v = iface_sub(itf, c, p, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, p));
         wA[c] = v;
         d += double(v) * double(p[c]);
     }
@@ -311,13 +311,13 @@ __global__ void bicg_p_k(int n, const T* __restrict__ r, const T* __restrict__ A
 template <class T>
 __global__ void __launch_bounds__(RED_NT) bicg_amul_alpha_k(int n, const int* os, const int* ls, const int* lL,
                                                             const int* u, const T* diag, const T* lp,
-                                                            const T* upper, const T* __restrict__ yA,
+                                                            const T* upper, Sell<T> S, const T* __restrict__ yA,
                                                             T* __restrict__ AyA, const T* __restrict__ r0,
                                                             SolveState* st, Red2 red, Iface<T> itf) {
     if (st->done) return;
     double d = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = iface_sub(itf, c, yA, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, yA));
+        const T v = iface_sub(itf, c, yA, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, yA));
         AyA[c] = v;
         d += double(r0[c]) * double(v);
     }
@@ -361,13 +361,13 @@ __global__ void bicg_phase_k(SolveState* st) {
 template <class T>
 __global__ void __launch_bounds__(RED_NT) bicg_amul_omega_k(int n, const int* os, const int* ls, const int* lL,
                                                             const int* u, const T* diag, const T* lp,
-                                                            const T* upper, const T* __restrict__ zA,
+                                                            const T* upper, Sell<T> S, const T* __restrict__ zA,
                                                             T* __restrict__ tA, const T* __restrict__ sA,
                                                             SolveState* st, Red2 red, Iface<T> itf) {
     if (st->done) return;
     double tt = 0.0, ts = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
-        const T v = iface_sub(itf, c, zA, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, zA));
+        const T v = iface_sub(itf, c, zA, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, zA));
         tA[c] = v;
         tt += double(v) * double(v);
         ts += double(v) * double(sA[c]);
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(RED_NT) bicg_update_k(int n, const T* __restri
 // GAMGSolverScale.C:42-75
 template <class T>
 __global__ void __launch_bounds__(RED_NT) gamg_scale_sf_k(int n, const int* os, const int* ls, const int* lL,
-                                                          const int* u, const T* diag, const T* lp, const T* upper,
+                                                          const int* u, const T* diag, const T* lp, const T* upper, Sell<T> S,
                                                           const T* __restrict__ field, T* __restrict__ Acf,
                                                           const T* __restrict__ source, SolveState* st, Red2 red,
                                                           Iface<T> itf) {
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(RED_NT) gamg_scale_sf_k(int n, const int* os, 
     double num = 0.0, den = 0.0;
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
         // Amul with the level's interfaces (GAMGSolverScale.C:42-50)
-        const T v = iface_sub(itf, c, field, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, field));
+        const T v = iface_sub(itf, c, field, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, field));
         Acf[c] = v;
         num += double(source[c]) * double(field[c]);
         den += double(v) * double(field[c]);
@@ -447,7 +447,7 @@ __global__ void gamg_scale_apply_k(int n, T* __restrict__ field, const T* __rest
 template <class T, bool RES>
 __global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int* os, const int* ls, const int* lL,
                                                                 const int* u, const T* diag, const T* lp,
-                                                                const T* upper, const T* __restrict__ psi,
+                                                                const T* upper, Sell<T> S, const T* __restrict__ psi,
                                                                 const T* __restrict__ b, T* __restrict__ r,
                                                                 SolveState* st, Red2 red, int inc, Iface<T> itf) {
     if (st->done) return;
@@ -455,12 +455,9 @@ __global__ void __launch_bounds__(RED_NT) gamg_residual_check_k(int n, const int
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
         T v;
         if (RES) {
-            T acc = b[c] - diag[c] * psi[c];
-            for (int k = ls[c]; k < ls[c + 1]; ++k) acc -= lp[k] * psi[lL[k]];
-            for (int f = os[c]; f < os[c + 1]; ++f) acc -= upper[f] * psi[u[f]];
-            v = iface_sub_neg(itf, c, psi, acc);
+            v = iface_sub_neg(itf, c, psi, row_res<T>(c, os, ls, lL, u, diag, lp, upper, S, psi, b));
         } else {
-            v = b[c] - iface_sub(itf, c, psi, row_amul<T>(c, os, ls, lL, u, diag, lp, upper, psi));
+            v = b[c] - iface_sub(itf, c, psi, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, psi));
         }
         r[c] = v;
         mg += fabs(double(v));
@@ -538,7 +535,7 @@ template <class T>
 void Kern<T>::pcg_amul(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* p, T* wA,
                        SolveState* st) {
     pcg_amul_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                   a.lowerPerm, a.upper, p, wA, st, Red2{sc.partials, sc.counters},
+                                                   a.lowerPerm, a.upper, sell_of(m, a), p, wA, st, Red2{sc.partials, sc.counters},
                                                    if_bou(m, a));
     count_launch();
 }
@@ -587,7 +584,7 @@ template <class T>
 void Kern<T>::bicg_amul_alpha(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* yA,
                               T* AyA, const T* r0, SolveState* st) {
     bicg_amul_alpha_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                          a.lowerPerm, a.upper, yA, AyA, r0, st,
+                                                          a.lowerPerm, a.upper, sell_of(m, a), yA, AyA, r0, st,
                                                           Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
@@ -609,7 +606,7 @@ template <class T>
 void Kern<T>::bicg_amul_omega(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* zA,
                               T* tA, const T* sA, SolveState* st) {
     bicg_amul_omega_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                          a.lowerPerm, a.upper, zA, tA, sA, st,
+                                                          a.lowerPerm, a.upper, sell_of(m, a), zA, tA, sA, st,
                                                           Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
@@ -625,7 +622,7 @@ template <class T>
 void Kern<T>::gamg_scale_sf(cudaStream_t s, Scratch& sc, const LevelMesh& m, const LevelCoeffs<T>& a, const T* field,
                             T* Acf, const T* source, SolveState* st) {
     gamg_scale_sf_k<T><<<grid_for(m.n), RED_NT, 0, s>>>(m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag,
-                                                        a.lowerPerm, a.upper, field, Acf, source, st,
+                                                        a.lowerPerm, a.upper, sell_of(m, a), field, Acf, source, st,
                                                         Red2{sc.partials, sc.counters}, if_bou(m, a));
     count_launch();
 }
@@ -642,11 +639,11 @@ void Kern<T>::gamg_residual_check(cudaStream_t s, Scratch& sc, const LevelMesh& 
                                   const T* psi, const T* b, T* r, SolveState* st, int inc) {
     if (inc > 0)
         gamg_residual_check_k<T, true><<<grid_for(m.n), RED_NT, 0, s>>>(
-            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
+            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, sell_of(m, a), psi, b, r, st,
             Red2{sc.partials, sc.counters}, inc, if_bou(m, a));
     else
         gamg_residual_check_k<T, false><<<grid_for(m.n), RED_NT, 0, s>>>(
-            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, psi, b, r, st,
+            m.n, m.ownerStart, m.losortStart, m.losortL, m.u, a.diag, a.lowerPerm, a.upper, sell_of(m, a), psi, b, r, st,
             Red2{sc.partials, sc.counters}, 1, if_bou(m, a));
     count_launch();
 }

@@ -108,12 +108,26 @@ struct SlotSys {
     unsigned long long tStart, tEnd;  // %globaltimer at the system's start / end (ns)
 };
 
+// A system's result as the batch kernels publish it, when asked, to
+// host-mapped memory the moment the system finishes: the fields, then a
+// system-scope fence, then flag = 1 (so the system's psiCell and the fields
+// are visible once the host sees the flag), letting a host thread complete
+// the system while the launch runs on.  The host zeroes the flags before
+// the launch.
+struct BatchDone {
+    double initialResidual, finalResidual;
+    int nIterations, converged, singular, nOuter;
+    unsigned flag, pad;
+};
+
 // Batched solves of independent systems: nCta persistent CTAs take systems
 // in array order from the counter next[1] (zero at launch), one CTA per
 // system.  Preconditioner set-up runs in the kernel.  mixed: FP32 inner
-// solves in FP64 iterative refinement (nOuter = refinement steps).
+// solves in FP64 iterative refinement (nOuter = refinement steps).  done
+// (device view of host-mapped memory, [nSys], or null): per-system results
+// published as each system finishes.
 void launch_batch(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nCta, int mixed,
-                  double innerRelTol, int maxOuter, unsigned* next);
+                  double innerRelTol, int maxOuter, unsigned* next, BatchDone* done = nullptr);
 // resident batch CTAs per SM (occupancy of the batch kernel)
 int batch_ctas_per_sm();
 // Cluster form: the first nBig systems (in array order) are solved by whole
@@ -121,7 +135,7 @@ int batch_ctas_per_sm();
 // persistent clusters; next[0], next[1] zero at launch.
 cudaError_t launch_batch_cluster(cudaStream_t s, SlotSys<double>* s64, SlotSys<float>* s32, int nSys, int nBig,
                                  int clusterSize, int nClusters, int mixed, double innerRelTol, int maxOuter,
-                                 unsigned* next);
+                                 unsigned* next, BatchDone* done = nullptr);
 // co-resident clusters of the cluster form (0: clusters unavailable)
 int batch_max_clusters(int clusterSize);
 

@@ -81,7 +81,8 @@ class Controls(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbmBudget", ctypes.c_int64), ("largeCells", ctypes.c_int), ("maxBatch", ctypes.c_int),
-                ("nCellsInCoarsestLevel", ctypes.c_int), ("groupCells", ctypes.c_int), ("groupSize", ctypes.c_int)]
+                ("nCellsInCoarsestLevel", ctypes.c_int), ("groupCells", ctypes.c_int), ("groupSize", ctypes.c_int),
+                ("lanes", ctypes.c_int)]
 
 
 class ServerStats(ctypes.Structure):
@@ -123,6 +124,7 @@ _SIG = {
     "cfx_mesh_create": (_i, [_vp, _i, _i, _vp, _vp, ctypes.POINTER(_vp)]),
     "cfx_mesh_destroy": (_i, [_vp]),
     "cfx_mesh_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "cfx_mesh_sell_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_int64)]),
     "cfx_face_area_pair_weights": (_i, [_i, _vp, _vp]),
     "cfx_gamg_agglomerate": (_i, [_vp, _vp, _i, _i]),
     "cfx_gamg_coarse_interfaces": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -305,6 +307,13 @@ class LduMesh:
         a, b = ctypes.c_int(), ctypes.c_int()
         _check(lib().cfx_mesh_info(self.h, ctypes.byref(a), ctypes.byref(b)), "cfx_mesh_info")
         return a.value, b.value
+
+    def sell_info(self):
+        """(slices, pattern slices, entries) of the finest level's sliced rows."""
+        a, b, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+        _check(lib().cfx_mesh_sell_info(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(e)),
+               "cfx_mesh_sell_info")
+        return a.value, b.value, e.value
 
     def agglomerate(self, weights=None, Sf=None, nCellsInCoarsestLevel=10, forward=True):
         """faceAreaPair agglomeration (weights from Sf when not given)."""
@@ -508,6 +517,7 @@ TUNE_GRID_WAVE = 5
 TUNE_CLUSTER_PRE = 6
 TUNE_FLOW = 7
 TUNE_FLOW_AHEAD = 8
+TUNE_AMUL_SELL = 9
 
 
 def tune_set(key, value):

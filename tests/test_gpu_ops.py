@@ -7,6 +7,12 @@ residual, sumA, the DIC/DILU reciprocal diagonals and preconditioners, and the
 GaussSeidel / DIC smoothers are exact.  Both sweep forms (one CTA with block
 barriers, and the multi-CTA level scheduler) are exercised, on the natural
 lexicographic order and on randomly permuted meshes (many short levels).
+
+The A x products read each row either from the level's sliced ELL copy (the
+default, with offset-pattern slices where the rows share their neighbour
+offsets; or with explicit columns only) or through the losort/owner gathers;
+all three are checked, and a row with more than 255 neighbours (no sliced
+copy) falls back to the gathers.
 """
 import numpy as np
 import pytest
@@ -46,7 +52,42 @@ SYSTEMS = {
     "cube24": lambda: cases.pcg_cube(24, seed=3),
     "perm_lap": lambda: _permuted("gamg_cube", 5),
     "perm_cd": lambda: _permuted("bicgstab_cube", 6),
+    "hub": lambda: _hub(300),     # a row of 299 entries: no sliced copy
+    "hub255": lambda: _hub(256),  # a row of 255 entries: a wide explicit slice
 }
+
+
+def _hub(n, seed=4):
+    """Cell 0 neighbours every other cell (a row of n-1 > 255 entries), the
+    others form a chain: faces in owner order, asymmetric, diagonally
+    dominant."""
+    faces = [(0, k) for k in range(1, n)] + [(k, k + 1) for k in range(1, n - 1)]
+    faces.sort()
+    l = np.array([f[0] for f in faces], np.int32)
+    u = np.array([f[1] for f in faces], np.int32)
+    rng = np.random.default_rng(seed)
+    upper = -rng.uniform(0.1, 1.0, l.size)
+    lower = -rng.uniform(0.1, 1.0, l.size)
+    diag = np.zeros(n)
+    np.add.at(diag, l, -upper)
+    np.add.at(diag, u, -lower)
+    diag += rng.uniform(0.5, 1.0, n)
+    return {"name": "hub", "l": l, "u": u, "diag": diag, "upper": upper, "lower": lower,
+            "source": rng.uniform(-1, 1, n)}
+
+
+AMUL_FORMS = {"gather": 0, "explicit": 1, "pattern": 2}
+
+
+@pytest.fixture(params=sorted(AMUL_FORMS))
+def amul_form(request):
+    """The product form, set before the test builds its mesh."""
+    old = ldu.tune_get(ldu.TUNE_AMUL_SELL)
+    ldu.tune_set(ldu.TUNE_AMUL_SELL, AMUL_FORMS[request.param])
+    try:
+        yield request.param
+    finally:
+        ldu.tune_set(ldu.TUNE_AMUL_SELL, old)
 
 
 @pytest.fixture(params=sorted(FORMS))
@@ -66,7 +107,7 @@ def _fresh(s):
 
 
 @pytest.mark.parametrize("name", sorted(SYSTEMS))
-def test_matrix_products_exact(name):
+def test_matrix_products_exact(name, amul_form):
     s = SYSTEMS[name]()
     _, A = _fresh(s)
     m = orc.Matrix(s)
@@ -84,7 +125,55 @@ def test_matrix_products_exact(name):
     np.testing.assert_array_equal(host(dy), m.sumA())
 
 
-@pytest.mark.parametrize("name", sorted(SYSTEMS))
+def test_sliced_rows_layout():
+    """Pattern slices where the rows share their offsets (a lexicographic
+    cube: every slice), explicit ones on a randomly renumbered mesh, none
+    with a row of more than 255 neighbours."""
+    old = ldu.tune_get(ldu.TUNE_AMUL_SELL)
+    try:
+        ldu.tune_set(ldu.TUNE_AMUL_SELL, 2)
+        mesh, _ = _fresh(SYSTEMS["cube24"]())
+        slices, pat, entries = mesh.sell_info()
+        assert slices == 24 ** 3 // 32 and pat == slices and entries == 32 * 6 * slices
+        mesh, _ = _fresh(SYSTEMS["perm_lap"]())
+        slices, pat, entries = mesh.sell_info()
+        assert slices == (9 ** 3 + 31) // 32 and pat < slices
+        ldu.tune_set(ldu.TUNE_AMUL_SELL, 1)
+        mesh, _ = _fresh(SYSTEMS["cube24"]())
+        assert mesh.sell_info()[1] == 0
+        mesh, _ = _fresh(SYSTEMS["hub"]())
+        assert mesh.sell_info() == (0, 0, 0)
+        mesh, _ = _fresh(SYSTEMS["hub255"]())
+        assert mesh.sell_info()[:2] == (8, 0)
+    finally:
+        ldu.tune_set(ldu.TUNE_AMUL_SELL, old)
+
+
+@pytest.mark.parametrize("name", ["cube24", "cd6", "cycd7", "perm_cd", "hub"])
+def test_products_follow_coefficient_updates(name, amul_form):
+    """cfx_matrix_update rewrites every copy of the coefficients the products
+    read (the sliced rows included)."""
+    s = SYSTEMS[name]()
+    _, A = _fresh(s)
+    n = s["diag"].size
+    rng = np.random.default_rng(11)
+    s2 = dict(s)
+    s2["upper"] = s["upper"] * rng.uniform(0.5, 1.5, s["upper"].size)
+    if s.get("lower") is not None:
+        s2["lower"] = s["lower"] * rng.uniform(0.5, 1.5, s["lower"].size)
+    s2["diag"] = s["diag"] * rng.uniform(1.0, 1.5, n)
+    x = cases.uniform(9, n)
+    dx, db, dy = dev(x), dev(s["source"]), torch.empty(n, dtype=torch.float64, device="cuda")
+    A.Amul(dx, dy)
+    A.update(s2["diag"], s2["upper"], s2.get("lower"))
+    m2 = orc.Matrix(s2)
+    A.Amul(dx, dy)
+    np.testing.assert_array_equal(host(dy), m2.amul(x))
+    A.residual(dx, db, dy)
+    np.testing.assert_array_equal(host(dy), m2.residual(x, s["source"]))
+
+
+@pytest.mark.parametrize("name", sorted(set(SYSTEMS) - {"hub", "hub255"}))
 def test_sweeps_exact(name, sweep_form):
     s = SYSTEMS[name]()
     _, A = _fresh(s)

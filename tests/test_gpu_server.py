@@ -250,3 +250,72 @@ def test_small_requests_run_between_the_cycles_of_a_large_solve():
     assert st["largeYields"] >= 1
     assert max(t_small) <= t_big
     sv.close()
+
+
+def test_small_requests_do_not_wait_for_a_long_launch():
+    """Batch lanes: a small request submitted while a long launch (one
+    cluster-sized system) runs starts on an idle lane at once and finishes
+    first; both results equal the ones computed alone."""
+    long_sys = cases.box(64, 64, 48, dirichlet="xmin", seed=21)
+    ctl_long = dict(CTL, tolerance=1e-12)
+    sv = ldu.Server(groupCells=100000)
+    big = sv.add_matrix(long_sys)
+    systems = _boxes()[:4]
+    mids = [sv.add_matrix(x) for x in systems]
+    alone = [sv.wait(sv.submit(m, x["source"], CTL))[0] for m, x in zip(mids, systems)]
+    big_alone, _ = sv.wait(sv.submit(big, long_sys["source"], ctl_long))
+    import time
+    rid_big = sv.submit(big, long_sys["source"], ctl_long)
+    t0 = time.perf_counter()
+    while sv.stats()["running"] < 1 and time.perf_counter() - t0 < 5.0:
+        time.sleep(0.0002)
+    rids = [sv.submit(m, x["source"], CTL) for m, x in zip(mids, systems)]
+    done_small = []
+    for k, rid in enumerate(rids):
+        psi, _ = sv.wait(rid)
+        done_small.append(time.perf_counter())
+        np.testing.assert_array_equal(psi, alone[k])
+    psi_big, _ = sv.wait(rid_big)
+    t_big = time.perf_counter()
+    np.testing.assert_array_equal(psi_big, big_alone)
+    assert max(done_small) < t_big
+    st = sv.stats()
+    assert st["batches"] >= 2
+    sv.close()
+
+
+def test_a_small_request_completes_before_the_largest_of_its_launch():
+    """Per-system completion: with one lane, a small request that shares a
+    launch with a large one is handed back as soon as its own system
+    finishes (the kernel publishes each system's result), not when the
+    launch ends; both results equal the ones computed alone."""
+    sv = ldu.Server(lanes=1, groupCells=10 ** 9)
+    blocker = cases.box(40, 40, 40, dirichlet="xmin", seed=31)
+    big = cases.box(40, 40, 40, dirichlet="ymin", seed=32)
+    small = cases.box(8, 8, 8, dirichlet="zmin", seed=33)
+    ctl = dict(CTL, tolerance=1e-12)
+    m_blk, m_big, m_small = sv.add_matrix(blocker), sv.add_matrix(big), sv.add_matrix(small)
+    big_alone, _ = sv.wait(sv.submit(m_big, big["source"], ctl))
+    small_alone, _ = sv.wait(sv.submit(m_small, small["source"], ctl))
+    import time
+    rid_blk = sv.submit(m_blk, blocker["source"], ctl)
+    t0 = time.perf_counter()
+    while sv.stats()["running"] < 1 and time.perf_counter() - t0 < 5.0:
+        time.sleep(0.0002)
+    rid_big = sv.submit(m_big, big["source"], ctl)
+    rid_small = sv.submit(m_small, small["source"], ctl)
+    done = {}
+
+    def waiter(name, rid):
+        done[name] = (sv.wait(rid)[0], time.perf_counter())
+
+    ts = [threading.Thread(target=waiter, args=a) for a in (("big", rid_big), ("small", rid_small))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    sv.wait(rid_blk)
+    np.testing.assert_array_equal(done["big"][0], big_alone)
+    np.testing.assert_array_equal(done["small"][0], small_alone)
+    assert done["small"][1] < done["big"][1]
+    sv.close()

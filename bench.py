@@ -61,10 +61,11 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=256, help="cube cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel-only", choices=["gs", "level1", "solves"], default=None,
+    ap.add_argument("--kernel-only", choices=["gs", "level1", "solves", "amul"], default=None,
                     help="profiling: gs = the finest level's fused 2-sweep Gauss-Seidel alone, level1 = the "
                          "first agglomerated level's, solves = one FP64 and one mixed headline solve inside "
-                         "the NVTX range 'profiled' (after one warm-up solve of each)")
+                         "the NVTX range 'profiled' (after one warm-up solve of each), amul = Amul on the "
+                         "finest level, FP64 then FP32 (warmup + steps launches each)")
     ap.add_argument("--form", choices=["default", "grid", "flow"], default="default",
                     help="profiling modes: the sweep form of the levels larger than one CTA")
     ap.add_argument("--write-case", default=None, help=argparse.SUPPRESS)
@@ -356,6 +357,21 @@ def gs_bytes(N, F, s=8):
     return 7 * s * N + s * F + 4 * F + 4 * N
 
 
+# GB300's FP64 rate: 1.25 TFLOP/s nominal counting a fused multiply-add as
+# two, i.e. 0.625e12 FP64 instructions/s.  The products here are not
+# contracted (the reference's rounding), so every multiply and every add is
+# one FP64 instruction.
+FP64_OPS_PEAK = 0.625e12
+
+
+def fp64_ops(kernel, N, F):
+    """FP64 instructions of one Amul (diag*x, then a multiply and an add per
+    off-diagonal entry: 2F entries) or residual (b - diag*x, then a multiply
+    and a subtract per entry)."""
+    base = kernel.split("_")[0]
+    return (N if base == "amul" else 2 * N) + 2 * 2 * F
+
+
 def level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells):
     """Every GAMG level's smoothing timed alone (FP64, the V-cycle's sweep
     count): each coarse level's matrix, assembled on the device, read back
@@ -551,7 +567,10 @@ def run_ours(args, rank, world, local, pg):
             "e2e": {"value": te, "unit": "s", "h2d_bytes_per_step": 8 * (N + F) + 16 * N,
                     "d2h_bytes_per_step": 8 * N},
             "gpu_launches": int(launches),
-            "streaming_kernels": {k: {"s": t, "algorithmic_bytes": b, "GB_s": b / t / 1e9, "frac": b / t / 1e9 / peak}
+            "streaming_kernels": {k: {"s": t, "algorithmic_bytes": b, "GB_s": b / t / 1e9, "frac": b / t / 1e9 / peak,
+                                      "fp64_ops": fp64_ops(k, N, F),
+                                      "fp64_Gops_s": fp64_ops(k, N, F) / t / 1e9,
+                                      "fp64_pipe_frac": fp64_ops(k, N, F) / t / FP64_OPS_PEAK}
                                   for k, (t, b) in streaming.items()},
             "roofline": {"bound": "hbm",
                          "kernel": "Gauss-Seidel sweeps of the agglomerated GAMG levels, persistent grid form "
@@ -827,6 +846,25 @@ def run_kernel_only(args):
                 torch.cuda.synchronize()
                 torch.cuda.nvtx.range_pop()
         print(json.dumps({"kernel": "solves", "n": args.n, **out}), flush=True)
+        return 0
+    if args.kernel_only == "amul":
+        # cfx_amul and cfx_residual run in FP64 (the FP32 copies of the
+        # coefficients are reached only inside mixed-precision solves)
+        d_b = torch.from_numpy(np.random.default_rng(7).uniform(-1, 1, N)).cuda()
+        d_y = torch.empty_like(d_b)
+        torch.cuda.synchronize()
+        t = {}
+        for name, fn in (("amul", lambda: A.Amul(d_b, d_y)), ("residual", lambda: A.residual(d_b, d_b, d_y))):
+            ts = []
+            for i in range(args.warmup + args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                if i >= args.warmup:
+                    ts.append(time.perf_counter() - t0)
+            t[name] = statistics.median(ts)
+        print(json.dumps({"kernel": "amul", "n": args.n, "cells": N, "faces": F, **t}), flush=True)
         return 0
     if args.kernel_only == "level1":
         mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=10)

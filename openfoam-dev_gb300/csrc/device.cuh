@@ -90,50 +90,29 @@ __device__ __forceinline__ T sell_acc(T acc, T a, T x) {
 }
 
 // acc op= the row's terms in order: OP 0 adds coef*x[col], OP 1 subtracts.
-// Slices up to 8 wide issue every load of the row before the first product
-// (two dependent rounds: coefficients and columns, then x).
+// One 16-byte (FP64) or 8-byte (FP32) coefficient load per pair of entries;
+// a pattern slice computes each column from the slice's offset list (an L1
+// broadcast) instead of loading it.  In FP64 the row's products and sums
+// (the reference's rounding, no contraction) keep the FP64 pipe busy rather
+// than HBM; in FP32 the pattern slices move the fewest bytes.
 template <class T, int OP>
 __device__ __forceinline__ T sell_row(int c, const Sell<T>& S, const T* __restrict__ x, T acc) {
     using P2 = typename Pair2<T>::type;
     const int sl = c >> 5;
     const int s0 = __ldg(S.start + sl);
-    const int K = (__ldg(S.start + sl + 1) - s0) >> 5;
     const int e0 = s0 + 2 * (c & 31);
     const int k1 = __ldg(S.cnt + c);
     const int p = S.pat ? __ldg(S.pat + sl) : -1;
-    if (K <= 8) {
-        P2 cf[4];
-        T xv[8];
-        if (p >= 0) {
-            const int* __restrict__ off = S.offs + 8 * p;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (2 * q < K) cf[q] = __ldg(reinterpret_cast<const P2*>(S.coef + e0 + 64 * q));
-#pragma unroll
-            for (int k = 0; k < 8; ++k) xv[k] = (k < K && ((k1 >> k) & 1)) ? x[c + __ldg(off + k)] : T(0);
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (k < K && ((k1 >> k) & 1)) acc = sell_acc<OP>(acc, (k & 1) ? cf[k >> 1].y : cf[k >> 1].x, xv[k]);
-            return acc;
+    if (p >= 0) {
+        const int K = (__ldg(S.start + sl + 1) - s0) >> 5;
+        const int* __restrict__ off = S.offs + 8 * p;
+        for (int k = 0; k < K; k += 2) {
+            const P2 cf = __ldg(reinterpret_cast<const P2*>(S.coef + e0 + 32 * k));
+            if ((k1 >> k) & 1) acc = sell_acc<OP>(acc, cf.x, x[c + __ldg(off + k)]);
+            if ((k1 >> (k + 1)) & 1) acc = sell_acc<OP>(acc, cf.y, x[c + __ldg(off + k + 1)]);
         }
-        int2 cl[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (2 * q < K) {
-                cf[q] = __ldg(reinterpret_cast<const P2*>(S.coef + e0 + 64 * q));
-                cl[q] = __ldg(reinterpret_cast<const int2*>(S.col + e0 + 64 * q));
-            }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (2 * q < k1) xv[2 * q] = x[cl[q].x];
-            if (2 * q + 1 < k1) xv[2 * q + 1] = x[cl[q].y];
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (k < k1) acc = sell_acc<OP>(acc, (k & 1) ? cf[k >> 1].y : cf[k >> 1].x, xv[k]);
         return acc;
     }
-    // wider explicit slices (pattern slices are at most 8 wide)
     for (int k = 0; k < k1; k += 2) {
         const int e = e0 + 32 * k;
         const P2 cf = __ldg(reinterpret_cast<const P2*>(S.coef + e));

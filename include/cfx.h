@@ -217,11 +217,20 @@ cfx_status cfx_matrix_update(cfx_matrix* mat, const double* diag, const double* 
  * lduMatrix::updateMatrixInterfaces does with cyclicFvPatchField
  * (cyclicFvPatchField.C:150-174: result[faceCells] -= coeffs*psi[nbr]);
  * the DIC/DILU factorisations ignore them, as the reference's do.  PCG,
- * PBiCGStab, PBiCG and smoothSolver solve such systems (FP64); GAMG is
- * refused.  nPatches = 0 removes them.  Set the interfaces before the
- * matrices' interface coefficients. */
+ * PBiCGStab, PBiCG, smoothSolver and GAMG (cyclicGAMGInterface levels, and
+ * GAMG as PCG's preconditioner) solve such systems, FP64 and mixed; the
+ * direct coarsest-level solve also needs cfx_mesh_set_interface_partners;
+ * the nonBlockingGaussSeidel smoother is refused.  nPatches = 0 removes
+ * them.  Set the interfaces before the matrices' interface coefficients. */
 cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32_t* patchSize,
                                    const int32_t* faceCells, const int32_t* nbrFaceCells);
+/* Each interface patch's partner patch (cyclicLduInterface::nbrPatchIndex,
+ * cyclicLduInterface.H, in the numbering of cfx_mesh_set_interfaces), which
+ * LUscalarMatrix::convert (LUscalarMatrix.C:205-265) reads for the direct
+ * coarsest-level solve: it subtracts the partner's interfaceBouCoeffs.  A
+ * partner must have as many faces.  Needed only by directSolveCoarsest with
+ * interfaces; cfx_mesh_set_interfaces forgets it. */
+cfx_status cfx_mesh_set_interface_partners(cfx_mesh* mesh, const int32_t* nbrPatch);
 /* interfaceBouCoeffs and interfaceIntCoeffs (host, faces concatenated in patch
  * order; intCoeffs NULL: the same as bouCoeffs). */
 cfx_status cfx_matrix_set_interface_coeffs(cfx_matrix* mat, const double* bouCoeffs, const double* intCoeffs);

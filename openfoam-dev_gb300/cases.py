@@ -180,7 +180,7 @@ def cyclic_x(s, mesh, gamma=1.0, U=None):
     out = dict(s)
     out.update(diag=diag, ifSize=np.array([n, n], np.int32), ifCell=np.concatenate([a, b]).astype(np.int32),
                ifNbr=np.concatenate([b, a]).astype(np.int32), ifBou=np.concatenate([bouA, bouB]),
-               ifInt=np.concatenate([bouB, bouA]))
+               ifInt=np.concatenate([bouB, bouA]), ifNbrPatch=np.array([1, 0], np.int32))
     return out
 
 

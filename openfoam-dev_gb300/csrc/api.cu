@@ -63,8 +63,9 @@ struct cfx_mesh {
     std::vector<int> ifPos;
     Arena ifArena;
     // the same interfaces on the host (patch sizes, face cells, partner
-    // cells, patch order) and the GAMG levels' coarse interfaces
-    std::vector<int> ifPatchSize, ifFaceCell, ifNbrCell;
+    // cells, patch order) and the GAMG levels' coarse interfaces; each
+    // patch's partner patch when known (cfx_mesh_set_interface_partners)
+    std::vector<int> ifPatchSize, ifFaceCell, ifNbrCell, ifNbrPatch;
     Arena ifCoarseArena;
 };
 
@@ -319,18 +320,62 @@ void coarse_interface_faces(const int* R, const std::vector<int>& size, const st
     }
 }
 
+// LUscalarMatrix::convert's interface entries (LUscalarMatrix.C:236-262) of
+// one level: per patch p with partner q and face f, row faceCells_p[f],
+// column faceCells_q[f], coefficient interfaceBouCoeffs_q[f] (its CSR
+// position).  False when a partner is unknown or of another size.
+bool lu_interface_entries(const std::vector<int>& partner, const std::vector<int>& size,
+                          const std::vector<int>& cell, const std::vector<int>& pos, std::vector<int>& row,
+                          std::vector<int>& col, std::vector<int>& src) {
+    const int nP = int(size.size());
+    if (int(partner.size()) != nP) return false;
+    std::vector<int> off(static_cast<size_t>(nP) + 1, 0);
+    for (int p = 0; p < nP; ++p) off[p + 1] = off[p] + size[p];
+    row.clear();
+    col.clear();
+    src.clear();
+    for (int p = 0; p < nP; ++p) {
+        const int q = partner[p];
+        if (q < 0 || q >= nP || size[q] != size[p]) return false;
+        for (int f = 0; f < size[p]; ++f) {
+            row.push_back(cell[off[p] + f]);
+            col.push_back(cell[off[q] + f]);
+            src.push_back(pos[off[q] + f]);
+        }
+    }
+    return true;
+}
+
+void set_lu_interfaces(cfx_mesh* mesh, LevelMesh& m, const std::vector<int>& size, const std::vector<int>& cell,
+                       const std::vector<int>& pos, cudaStream_t s) {
+    std::vector<int> row, col, src;
+    m.luIfRow = m.luIfCol = m.luIfSrc = nullptr;
+    if (!lu_interface_entries(mesh->ifNbrPatch, size, cell, pos, row, col, src)) {
+        m.luIfN = -1;
+        return;
+    }
+    m.luIfN = int(row.size());
+    m.luIfRow = mesh->ifCoarseArena.upload(row, s);
+    m.luIfCol = mesh->ifCoarseArena.upload(col, s);
+    m.luIfSrc = mesh->ifCoarseArena.upload(src, s);
+}
+
 void build_coarse_interfaces(cfx_mesh* mesh) {
     cudaStream_t s = mesh->ctx->stream;
     CK(cudaStreamSynchronize(s));
     mesh->ifCoarseArena.release();
     const int nl = int(mesh->dev.size());
-    for (int i = 1; i < nl; ++i) {
+    for (int i = 0; i < nl; ++i) {
         LevelMesh& m = mesh->dev[i];
+        m.luIfN = 0;
+        m.luIfRow = m.luIfCol = m.luIfSrc = nullptr;
+        if (i == 0) continue;
         m.nIf = 0;
         m.ifStart = m.ifNbr = m.ifcStart = m.ifcFine = nullptr;
     }
     if (!mesh->nIf) return;
     std::vector<int> size = mesh->ifPatchSize, cell = mesh->ifFaceCell, nbr = mesh->ifNbrCell, pos = mesh->ifPos;
+    set_lu_interfaces(mesh, mesh->dev[0], size, cell, pos, s);
     for (int i = 1; i < nl; ++i) {
         const int nFine = int(cell.size());
         std::vector<int> cSize, cCell, cNbr, toCoarse;
@@ -360,6 +405,7 @@ void build_coarse_interfaces(cfx_mesh* mesh) {
         cell.swap(cCell);
         nbr.swap(cNbr);
         pos.swap(cpos);
+        set_lu_interfaces(mesh, m, size, cell, pos, s);
     }
     CK(cudaStreamSynchronize(s));  // the host vectors are temporaries
 }
@@ -1150,6 +1196,9 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
         // solver construction (here: per solve), in the cycle's precision
         if (m.n > 8192) throw StatusError(CFX_ERR_CONFIG, "directSolveCoarsest: the coarsest level has more "
                                                           "than 8192 cells");
+        if (m.nIf && m.luIfN < 0)
+            throw StatusError(CFX_ERR_CONFIG, "directSolveCoarsest: a coarsest-level interface has no partner "
+                                              "patch of its size");
         cy.lu = W.get(G0 + 700, m.n * m.n);
         T* vv = W.get(G0 + 701, m.n);
         if (mat->luPivN < m.n) {
@@ -1572,8 +1621,10 @@ cfx_status check_controls(const cfx_matrix* mat, const cfx_controls* c) {
         // coupled interfaces: the lduMatrix operations, the Krylov solvers,
         // smoothSolver and GAMG (cyclicGAMGInterface levels); the direct
         // coarsest-level solve's dense matrix does not take them
-        if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->directSolveCoarsest) {
-            set_error("directSolveCoarsest with coupled interfaces is not supported");
+        if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->directSolveCoarsest &&
+            mat->mesh->ifNbrPatch.empty()) {
+            set_error("directSolveCoarsest with coupled interfaces needs the interfaces' partner patches "
+                      "(cfx_mesh_set_interface_partners)");
             return CFX_ERR_CONFIG;
         }
         if ((c->solver == CFX_SOLVER_GAMG || c->preconditioner == CFX_PRE_GAMG) && c->smoother == CFX_SMOOTH_NBGS) {
@@ -1981,9 +2032,27 @@ cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32
         mesh->ifPatchSize.assign(patchSize, patchSize + nPatches);
         mesh->ifFaceCell.assign(faceCells, faceCells + nIf);
         mesh->ifNbrCell.assign(nbrCells, nbrCells + nIf);
+        mesh->ifNbrPatch.clear();
         build_coarse_interfaces(mesh);
         mesh->version++;  // captured graphs hold the interface pointers
         CK(cudaStreamSynchronize(s));
+        return CFX_OK;
+    });
+}
+
+cfx_status cfx_mesh_set_interface_partners(cfx_mesh* mesh, const int32_t* nbrPatch) {
+    if (!mesh || !nbrPatch) return CFX_ERR_ARG;
+    const int nP = int(mesh->ifPatchSize.size());
+    for (int p = 0; p < nP; ++p)
+        if (nbrPatch[p] < 0 || nbrPatch[p] >= nP || mesh->ifPatchSize[nbrPatch[p]] != mesh->ifPatchSize[p]) {
+            set_error("cfx_mesh_set_interface_partners: patch " + std::to_string(p) +
+                      ": the partner patch is out of range or of another size");
+            return CFX_ERR_ARG;
+        }
+    return guard([&]() -> cfx_status {
+        mesh->ifNbrPatch.assign(nbrPatch, nbrPatch + nP);
+        build_coarse_interfaces(mesh);
+        mesh->version++;
         return CFX_OK;
     });
 }

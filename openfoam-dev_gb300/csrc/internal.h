@@ -110,6 +110,12 @@ struct LevelMesh {
     // level's interface faces (CSR order)
     int* ifcStart = nullptr;  // [nIf+1]
     int* ifcFine = nullptr;   // [the finer level's nIf]
+    // the dense (direct coarsest) matrix's interface entries, in patch then
+    // face order: A[luIfRow[k]][luIfCol[k]] -= ifBou[luIfSrc[k]] (the
+    // partner patch's coefficient, a CSR position); luIfN < 0: the
+    // interfaces' partner patches are not known
+    int luIfN = 0;
+    int *luIfRow = nullptr, *luIfCol = nullptr, *luIfSrc = nullptr;
 };
 
 template <class T>

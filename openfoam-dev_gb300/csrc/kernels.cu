@@ -234,8 +234,10 @@ template <class T>
 __global__ void __launch_bounds__(LU_NT) lu_factor_k(int n, int nf, const int* __restrict__ l,
                                                      const int* __restrict__ u, const T* __restrict__ diag,
                                                      const T* __restrict__ upper, const T* __restrict__ lower,
-                                                     T* __restrict__ A, T* __restrict__ vv, int* __restrict__ piv,
-                                                     int* status) {
+                                                     int nIf, const int* __restrict__ ifRow,
+                                                     const int* __restrict__ ifCol, const int* __restrict__ ifSrc,
+                                                     const T* __restrict__ ifBou, T* __restrict__ A,
+                                                     T* __restrict__ vv, int* __restrict__ piv, int* status) {
     __shared__ int singular, pivRow;
     const int t = threadIdx.x;
     const size_t nn = size_t(n) * n;
@@ -247,6 +249,11 @@ __global__ void __launch_bounds__(LU_NT) lu_factor_k(int n, int nf, const int* _
         A[size_t(u[f]) * n + l[f]] = lower[f];
         A[size_t(l[f]) * n + u[f]] = upper[f];
     }
+    __syncthreads();
+    // the cyclic interfaces, in the reference's patch then face order (one
+    // thread: two faces may meet on one entry)
+    if (t == 0)
+        for (int k = 0; k < nIf; ++k) A[size_t(ifRow[k]) * n + ifCol[k]] -= ifBou[ifSrc[k]];
     __syncthreads();
     for (int i = t; i < n; i += LU_NT) {
         T big = T(0);
@@ -499,7 +506,9 @@ void Ops<T>::interpolate(cudaStream_t s, const LevelMesh& f, const LevelCoeffs<T
 template <class T>
 void Ops<T>::lu_factor(cudaStream_t s, const LevelMesh& m, const LevelCoeffs<T>& a, T* A, T* vv, int* piv,
                        int* status) {
-    lu_factor_k<T><<<1, LU_NT, 0, s>>>(m.n, m.nf, m.l, m.u, a.diag, a.upper, a.sym ? a.upper : a.lower, A, vv, piv,
+    const bool itf = m.nIf > 0 && m.luIfN > 0 && a.ifBou;
+    lu_factor_k<T><<<1, LU_NT, 0, s>>>(m.n, m.nf, m.l, m.u, a.diag, a.upper, a.sym ? a.upper : a.lower,
+                                       itf ? m.luIfN : 0, m.luIfRow, m.luIfCol, m.luIfSrc, a.ifBou, A, vv, piv,
                                        status);
     count_launch();
 }

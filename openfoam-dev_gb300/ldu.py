@@ -123,6 +123,7 @@ _SIG = {
     "cfx_ctx_launch_count": (_i, [_vp, ctypes.POINTER(ctypes.c_int64)]),
     "cfx_mesh_create": (_i, [_vp, _i, _i, _vp, _vp, ctypes.POINTER(_vp)]),
     "cfx_mesh_destroy": (_i, [_vp]),
+    "cfx_mesh_set_interface_partners": (_i, [_vp, _vp]),
     "cfx_mesh_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cfx_mesh_sell_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_int64)]),
     "cfx_face_area_pair_weights": (_i, [_i, _vp, _vp]),
@@ -350,11 +351,17 @@ class LduMesh:
                "level_info")
         return ra, fra, fl, nc.value, ncf.value, cl, cu
 
-    def set_interfaces(self, patchSizes, faceCells, nbrFaceCells):
-        """Coupled (cyclic) interfaces: faces concatenated in patch order."""
+    def set_interfaces(self, patchSizes, faceCells, nbrFaceCells, nbrPatch=None):
+        """Coupled (cyclic) interfaces: faces concatenated in patch order;
+        nbrPatch: each patch's partner patch (the direct coarsest-level
+        solve needs it)."""
         self._if = [np.ascontiguousarray(a, np.int32) for a in (patchSizes, faceCells, nbrFaceCells)]
         _check(lib().cfx_mesh_set_interfaces(self.h, len(self._if[0]), _hp(self._if[0]), _hp(self._if[1]),
                                              _hp(self._if[2])), "cfx_mesh_set_interfaces")
+        if nbrPatch is not None:
+            self._if.append(np.ascontiguousarray(nbrPatch, np.int32))
+            _check(lib().cfx_mesh_set_interface_partners(self.h, _hp(self._if[3])),
+                   "cfx_mesh_set_interface_partners")
 
     def fv_geometry(self, magSf, deltaCoeffs, V, bCell, magSfB, deltaCoeffsB, weights=None):
         """Face geometry for device-side assembly (host arrays, uploaded once):
@@ -662,7 +669,7 @@ def system_matrix(s, ctx=None):
         ctx = ctx or default_context()
         mesh = LduMesh(ctx, s["diag"].size, s["l"], s["u"])
         if s.get("ifCell") is not None:  # coupled (cyclic) interfaces
-            mesh.set_interfaces(s["ifSize"], s["ifCell"], s["ifNbr"])
+            mesh.set_interfaces(s["ifSize"], s["ifCell"], s["ifNbr"], s.get("ifNbrPatch"))
         A = LduMatrix(mesh, s["diag"], s["upper"], s.get("lower"))
         if s.get("ifCell") is not None:
             A.set_interface_coeffs(s["ifBou"], s.get("ifInt"))

@@ -89,8 +89,17 @@ protected:
         // coupled interfaces: cyclic ones (faceCells, the neighbour patch's
         // faceCells, in interface order); processor interfaces are not
         // supported on one GPU
-        DynamicList<label> ifSize, ifCells, ifNbr;
+        DynamicList<label> ifSize, ifCells, ifNbr, ifPartner;
         DynamicList<scalar> ifBou, ifInt;
+        // the library numbers the set interfaces only
+        labelList libIndex(interfaces_.size(), -1);
+        {
+            label k = 0;
+            forAll(interfaces_, patchi)
+            {
+                if (interfaces_.set(patchi)) libIndex[patchi] = k++;
+            }
+        }
         forAll(interfaces_, patchi)
         {
             if (!interfaces_.set(patchi)) continue;
@@ -107,6 +116,7 @@ protected:
             const labelUList& fc = li.faceCells();
             const labelUList& nc = interfaces_[nbrI].interface().faceCells();
             ifSize.append(fc.size());
+            ifPartner.append(libIndex[nbrI]);
             forAll(fc, i)
             {
                 ifCells.append(fc[i]);
@@ -153,6 +163,13 @@ protected:
                     ifNbr.cdata()
                 ),
                 "cfx_mesh_set_interfaces"
+            );
+            // the direct coarsest-level solve reads the partner patches'
+            // coefficients (LUscalarMatrix::convert)
+            check
+            (
+                cfx_mesh_set_interface_partners(e.mesh, ifPartner.cdata()),
+                "cfx_mesh_set_interface_partners"
             );
             e.interfaces = true;
         }

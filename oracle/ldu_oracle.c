@@ -968,6 +968,7 @@ static void coarse_interfaces(const ldu_matrix* fine, const int* R, level_matrix
     L->m.ifInt = L->ifInt;
     L->m.nIfPatch = nP;
     L->m.ifPatchSize = L->ifPatchSize;
+    L->m.ifNbrPatch = fine->nIfPatch > 0 ? fine->ifNbrPatch : NULL;  /* the same patches */
 }
 
 /* GAMG's smoother on one level (any smoother of the table; rD as smoother_rD) */
@@ -1118,6 +1119,22 @@ typedef struct {
 
 /* LUscalarMatrix::convert (LUscalarMatrix.C:205-266, no interfaces): the
  * dense row-major matrix of an LDU matrix (lower = upper when symmetric). */
+/* The direct coarsest solve takes interfaces when every patch names a
+ * partner patch with as many faces (at most 64 patches). */
+static int lu_interfaces_ok(const ldu_matrix* m) {
+    if (!m->nIf) return 1;
+    if (m->nIfPatch <= 0 || m->nIfPatch > 64 || !m->ifNbrPatch) return 0;
+    for (int p = 0; p < m->nIfPatch; ++p) {
+        const int q = m->ifNbrPatch[p];
+        if (q < 0 || q >= m->nIfPatch || m->ifPatchSize[q] != m->ifPatchSize[p]) return 0;
+    }
+    return 1;
+}
+
+/* LUscalarMatrix::convert (LUscalarMatrix.C:205-265): the dense matrix,
+ * then per cyclic patch p and face f, A[faceCells_p[f]][faceCells_q[f]] -=
+ * interfaceBouCoeffs_q[f] with q the partner patch (the partner's
+ * coefficient, as the reference takes it), in patch then face order. */
 static void lu_dense(const ldu_matrix* m, double* A) {
     const int n = m->nCells;
     const double* lower = m->lower ? m->lower : m->upper;
@@ -1127,7 +1144,20 @@ static void lu_dense(const ldu_matrix* m, double* A) {
         A[(size_t)m->u[f] * n + m->l[f]] = lower[f];
         A[(size_t)m->l[f] * n + m->u[f]] = m->upper[f];
     }
+    if (!m->nIf || !lu_interfaces_ok(m)) return;
+    int off[64];
+    for (int p = 0, o = 0; p < m->nIfPatch && p < 64; ++p) {
+        off[p] = o;
+        o += m->ifPatchSize[p];
+    }
+    for (int p = 0; p < m->nIfPatch; ++p) {
+        const int q = m->ifNbrPatch[p];
+        for (int f = 0; f < m->ifPatchSize[p]; ++f)
+            A[(size_t)m->ifCell[off[p] + f] * n + m->ifCell[off[q] + f]] -= m->ifBou[off[q] + f];
+    }
 }
+
+
 
 static void gamg_setup(gamg_hier* H, const ldu_matrix* m, const ldu_agglomeration* agg,
                        const ldu_gamg_controls* gc) {
@@ -1308,13 +1338,13 @@ static void gamg_vcycle(gamg_hier* H, double* psi, const double* b, double* Apsi
 
 /* GAMGSolver::solve / Vcycle / initVcycle / solveCoarsestLevel,
  * GAMGSolverSolve.C:31-552, with the coupled interfaces agglomerated level
- * by level (coarse_interfaces).  directSolveCoarsest with interfaces is not
- * restated (returns -3). */
+ * by level (coarse_interfaces).  directSolveCoarsest with interfaces needs
+ * each patch's partner (ifNbrPatch); without it returns -3. */
 int ldu_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi, const double* b,
              const ldu_controls* c, const ldu_gamg_controls* gc, ldu_perf* perf) {
     const int n = m->nCells;
     if (agg->nLevels < 1) return -1;
-    if (m->nIf && gc->directSolveCoarsest) return -3;
+    if (m->nIf && gc->directSolveCoarsest && !lu_interfaces_ok(m)) return -3;
     memset(perf, 0, sizeof(*perf));
     gamg_hier H;
     gamg_setup(&H, m, agg, gc);
@@ -1356,6 +1386,7 @@ int ldu_pcg_gamg(const ldu_matrix* m, const ldu_agglomeration* agg, double* psi,
                  ldu_perf* perf) {
     const int n = m->nCells;
     if (agg->nLevels < 1) return -1;
+    if (m->nIf && gc->directSolveCoarsest && !lu_interfaces_ok(m)) return -3;
     double* pA = (double*)xmalloc(sizeof(double) * n);
     double* wA = (double*)xmalloc(sizeof(double) * n);
     double* rA = (double*)xmalloc(sizeof(double) * n);

@@ -36,6 +36,9 @@ typedef struct {
      * own); nIfPatch = 0 with nIf > 0: one patch of nIf faces */
     int nIfPatch;
     const int* ifPatchSize;
+    /* each patch's partner patch (cyclicLduInterface::nbrPatchIndex), or
+     * NULL: needed only by the direct coarsest-level solve */
+    const int* ifNbrPatch;
 } ldu_matrix;
 
 typedef struct {

@@ -34,7 +34,7 @@ class LduMatrix(ctypes.Structure):
                 ("l", i32p), ("u", i32p), ("diag", f64p), ("upper", f64p), ("lower", f64p),
                 ("ownerStart", i32p), ("losort", i32p), ("losortStart", i32p),
                 ("nIf", ctypes.c_int), ("ifCell", i32p), ("ifNbr", i32p), ("ifBou", f64p), ("ifInt", f64p),
-                ("nIfPatch", ctypes.c_int), ("ifPatchSize", i32p)]
+                ("nIfPatch", ctypes.c_int), ("ifPatchSize", i32p), ("ifNbrPatch", i32p)]
 
 
 class LduPerf(ctypes.Structure):
@@ -127,6 +127,9 @@ class Matrix:
             if s.get("ifSize") is not None:
                 self.ifc.append(np.ascontiguousarray(s["ifSize"], np.int32))
                 self.c.nIfPatch, self.c.ifPatchSize = self.ifc[4].size, _p(self.ifc[4], i32p)
+                if s.get("ifNbrPatch") is not None:
+                    self.ifc.append(np.ascontiguousarray(s["ifNbrPatch"], np.int32))
+                    self.c.ifNbrPatch = _p(self.ifc[5], i32p)
         lib().ldu_init_addr(ctypes.byref(self.c))
         self.n = self.diag.size
 
@@ -344,6 +347,8 @@ def gamg(s, psi, agg=None, tol=1e-6, rel_tol=0.0, max_iter=1000, min_iter=0, smo
                         ctypes.byref(g), ctypes.byref(perf))
     if rc == -2:
         raise ValueError("Singular matrix")
+    if rc == -3:
+        raise ValueError("directSolveCoarsest with interfaces needs each patch's partner patch")
     if rc != 0:
         raise ValueError("GAMG failed")
     return _perf(perf)

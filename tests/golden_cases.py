@@ -179,8 +179,12 @@ def fvcyc_case(name):
     eq, ctl = SPECS["fvcyc"]["cases"][name]
     g = load(f"fvcyc_{name}.npz")
     g["solverName"] = bytes(g["solverName"]).decode()
+    # the harness lists the cyclic patches in pairs (xmin, xmax): each
+    # other's partner (cyclicLduInterface::nbrPatchIndex)
+    nbr_patch = np.arange(len(g["ifSize"]), dtype=np.int32) ^ 1
     s = dict(l=g["l"], u=g["u"], diag=g["diag"], upper=g["upper"], lower=g.get("lower"), source=g["source"],
-             ifSize=g["ifSize"], ifCell=g["ifCell"], ifNbr=g["ifNbr"], ifBou=g["ifBou"], ifInt=g["ifInt"])
+             ifSize=g["ifSize"], ifCell=g["ifCell"], ifNbr=g["ifNbr"], ifBou=g["ifBou"], ifInt=g["ifInt"],
+             ifNbrPatch=nbr_patch)
     m = cases.box_mesh(**SPECS["fvcyc"]["mesh"])
     nI = m["nInternalFaces"]
     s["Sf"] = m["Sf"][: 3 * nI].reshape(nI, 3).copy()  # faceAreaPair weights

@@ -255,3 +255,22 @@ def test_timed_oracle_build_is_bit_identical(tmp_path):
         subprocess.run([sys.executable, "-c", _TIMED_CHILD, repo, f], env=env, check=True)
         out[timed] = np.load(f)
     np.testing.assert_array_equal(out["0"], out["1"])
+
+
+@pytest.mark.parametrize("U", [None, (1.0, 0.3, 0.0)], ids=["laplacian", "upwind"])
+def test_direct_coarsest_with_interfaces(U):
+    """LUscalarMatrix::convert with cyclic interfaces (LUscalarMatrix.C:236-262)
+    in the oracle: it needs each patch's partner patch, and the GAMG solve
+    with the direct coarsest solve reaches the iterative coarsest solve's
+    answer."""
+    s = cases.cyclic_cube(12, jitter=0.2, seed=4, U=U)
+    a = np.zeros_like(s["source"])
+    pa = orc.gamg(s, a, tol=1e-9, directSolveCoarsest=True)
+    b = np.zeros_like(s["source"])
+    orc.gamg(s, b, tol=1e-9)
+    assert pa.converged
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-8
+    t = dict(s)
+    t.pop("ifNbrPatch")
+    with pytest.raises(ValueError, match="partner"):
+        orc.gamg(t, np.zeros_like(s["source"]), tol=1e-9, directSolveCoarsest=True)

@@ -171,10 +171,28 @@ def test_gamg_with_cyclic_interfaces_against_the_oracle(ctl):
         assert rel <= 1e-6, rel
 
 
-def test_direct_coarsest_solve_with_interfaces_is_refused():
+def test_direct_coarsest_solve_with_interfaces_needs_the_partner_patches():
     s = cases.cyclic_cube(8, jitter=0.2, seed=2)
+    s.pop("ifNbrPatch")
     with pytest.raises(ldu.FatalError, match="directSolveCoarsest"):
         ldu.solve(s, np.zeros_like(s["source"]), {"solver": "cudaGAMG", "directSolveCoarsest": True})
+
+
+@pytest.mark.parametrize("U", [None, (1.0, 0.3, 0.0)], ids=["laplacian", "upwind"])
+def test_direct_coarsest_solve_with_interfaces_against_the_oracle(U):
+    """LUscalarMatrix::convert with cyclic interfaces: the coarsest level's
+    dense matrix takes each patch's faces with the partner patch's
+    coefficients (LUscalarMatrix.C:236-262), on the device as in the
+    oracle."""
+    s = cases.cyclic_cube(16, jitter=0.2, seed=4, U=U)
+    ctl = dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True, tolerance=1e-9, relTol=0.0)
+    ref = np.zeros_like(s["source"])
+    rp = orc.gamg(s, ref, tol=ctl["tolerance"], **gamg_kwargs(ctl))
+    psi = np.zeros_like(s["source"])
+    perf = ldu.solve(s, psi, dict(ctl, solver="cudaGAMG"))
+    assert perf.converged and abs(perf.nIterations - rp.nIterations) <= 1, (perf, rp)
+    rel = float(np.linalg.norm(psi - ref) / np.linalg.norm(ref))
+    assert rel <= (1e-10 if perf.nIterations == rp.nIterations else 1e-6), rel
 
 
 @pytest.mark.parametrize("ctl", [

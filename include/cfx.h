@@ -427,6 +427,8 @@ typedef struct {
     double elapsedS, solvesPerS;   /* since creation or the last reset */
     double p50Ms, p99Ms, meanMs, maxMs;  /* submit-to-completion latency */
     int64_t largeYields;           /* times a large solve yielded the GPU to a batch */
+    double queueP50Ms, queueP99Ms; /* submit to start of its launch or solve */
+    double runP50Ms, runP99Ms;     /* start to completion */
 } cfx_server_stats_t;
 void cfx_server_default_config(cfx_server_config* cfg);
 /* cfg NULL: defaults.  The server runs on ctx's device. */

@@ -83,7 +83,7 @@ struct SrvRequest {
     cfx_status status = CFX_OK;
     std::string error;
     cfx_perf perf{};
-    Clock::time_point tSubmit, tDone;
+    Clock::time_point tSubmit, tStart, tDone;
 };
 
 }  // namespace
@@ -131,7 +131,7 @@ struct cfx_server {
     Clock::time_point t0;
     int64_t submitted = 0, completed = 0, cancelled = 0, failed = 0, refused = 0;
     int64_t batches = 0, batchedSolves = 0, largeSolves = 0, running = 0;
-    std::vector<double> latMs;
+    std::vector<double> latMs, queueMs, runMs;  // submit-to-done, submit-to-start, start-to-done
 };
 
 namespace {
@@ -150,6 +150,8 @@ void finish(cfx_server* sv, SrvRequest& r, ReqState st) {
     if (st == Q_DONE) {
         ++sv->completed;
         sv->latMs.push_back(std::chrono::duration<double, std::milli>(r.tDone - r.tSubmit).count());
+        sv->queueMs.push_back(std::chrono::duration<double, std::milli>(r.tStart - r.tSubmit).count());
+        sv->runMs.push_back(std::chrono::duration<double, std::milli>(r.tDone - r.tStart).count());
     } else if (st == Q_FAILED) {
         ++sv->failed;
     }
@@ -379,7 +381,11 @@ void lane_worker(cfx_server* sv, SrvLane* ln) {
             }
         }
         sv->queue.swap(keep);
-        for (SrvRequest* r : rs) r->state = Q_RUNNING;
+        const Clock::time_point now = Clock::now();
+        for (SrvRequest* r : rs) {
+            r->state = Q_RUNNING;
+            r->tStart = now;
+        }
         sv->running += int64_t(rs.size());
         ++sv->activeLanes;
         lk.unlock();
@@ -443,6 +449,7 @@ void large_worker(cfx_server* sv) {
         sv->queue.erase(std::find(sv->queue.begin(), sv->queue.end(), r->id));
         m->busy = true;
         r->state = Q_RUNNING;
+        r->tStart = Clock::now();
         sv->largeActive = true;
         sv->running += 1;
         lk.unlock();
@@ -822,21 +829,25 @@ cfx_status cfx_server_stats(cfx_server* sv, cfx_server_stats_t* o) {
     o->hbmBudget = sv->cfg.hbmBudget;
     o->elapsedS = std::chrono::duration<double>(Clock::now() - sv->t0).count();
     o->solvesPerS = o->elapsedS > 0 ? double(sv->completed) / o->elapsedS : 0.0;
-    if (!sv->latMs.empty()) {
-        std::vector<double> v = sv->latMs;
+    auto pct = [](std::vector<double> v, double q) {
+        if (v.empty()) return 0.0;
         std::sort(v.begin(), v.end());
-        auto pct = [&](double q) {
-            const size_t i = std::min(v.size() - 1, size_t(std::ceil(q * double(v.size()))) - (q > 0 ? 1 : 0));
-            return v[i];
-        };
-        o->p50Ms = pct(0.50);
-        o->p99Ms = pct(0.99);
-        o->maxMs = v.back();
+        const size_t i = std::min(v.size() - 1, size_t(std::ceil(q * double(v.size()))) - (q > 0 ? 1 : 0));
+        return v[i];
+    };
+    if (!sv->latMs.empty()) {
+        o->p50Ms = pct(sv->latMs, 0.50);
+        o->p99Ms = pct(sv->latMs, 0.99);
+        o->maxMs = *std::max_element(sv->latMs.begin(), sv->latMs.end());
         double sum = 0.0;
-        for (double x : v) sum += x;
-        o->meanMs = sum / double(v.size());
+        for (double x : sv->latMs) sum += x;
+        o->meanMs = sum / double(sv->latMs.size());
     }
     o->largeYields = sv->yields;
+    o->queueP50Ms = pct(sv->queueMs, 0.50);
+    o->queueP99Ms = pct(sv->queueMs, 0.99);
+    o->runP50Ms = pct(sv->runMs, 0.50);
+    o->runP99Ms = pct(sv->runMs, 0.99);
     return CFX_OK;
 }
 
@@ -847,6 +858,8 @@ cfx_status cfx_server_reset_stats(cfx_server* sv) {
     sv->submitted = sv->completed = sv->cancelled = sv->failed = sv->refused = 0;
     sv->batches = sv->batchedSolves = sv->largeSolves = sv->yields = 0;
     sv->latMs.clear();
+    sv->queueMs.clear();
+    sv->runMs.clear();
     return CFX_OK;
 }
 

@@ -90,7 +90,8 @@ class ServerStats(ctypes.Structure):
                                               "batchedSolves", "largeSolves", "queueDepth", "running",
                                               "residentMatrices", "hbmInUse", "hbmBudget")] + \
                [(k, ctypes.c_double) for k in ("elapsedS", "solvesPerS", "p50Ms", "p99Ms", "meanMs", "maxMs")] + \
-               [("largeYields", ctypes.c_int64)]
+               [("largeYields", ctypes.c_int64)] + \
+               [(k, ctypes.c_double) for k in ("queueP50Ms", "queueP99Ms", "runP50Ms", "runP99Ms")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

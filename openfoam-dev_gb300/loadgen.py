@@ -146,25 +146,37 @@ class ServeMix:
                 return ("resident", self.resident[int(self.rng.integers(len(self.resident)))], seed)
             return ("new", int(self.rng.integers(len(self.pool))), seed)
 
-    def run(self, req, precision):
-        """One client request; returns (kind, latency_s, converged)."""
+    def run(self, req, precision, phases=None):
+        """One client request; returns (kind, latency_s, converged).  phases
+        (a dict, optional) receives the seconds spent registering, solving
+        (submit to the end of wait) and removing."""
         kind, what, seed = req
         t0 = time.perf_counter()
         sv = self.server
+        ph = {} if phases is None else phases
         if kind == "large":
             src = cases.uniform(seed, self.large["diag"].size)
+            t1 = time.perf_counter()
             _, p = sv.wait(sv.submit(self.large_mid, src, dict(GAMG, precision=precision)))
+            ph["solve"] = time.perf_counter() - t1
         elif kind == "resident":
             i, mid = what
             src = cases.uniform(seed, self.pool[i]["diag"].size)
+            t1 = time.perf_counter()
             _, p = sv.wait(sv.submit(mid, src, dict(PCG, precision=precision)))
+            ph["solve"] = time.perf_counter() - t1
         else:
             s = self.pool[what]
             mid = sv.add_matrix(s)
+            t1 = time.perf_counter()
+            ph["add"] = t1 - t0
             try:
                 _, p = sv.wait(sv.submit(mid, s["source"], dict(PCG, precision=precision)))
             finally:
+                t2 = time.perf_counter()
+                ph["solve"] = t2 - t1
                 sv.remove_matrix(mid)
+                ph["remove"] = time.perf_counter() - t2
         return kind, time.perf_counter() - t0, bool(p.converged)
 
 
@@ -217,12 +229,19 @@ def serve_stream(mix, rate, duration, precision, seed=11, clients=64):
     lock = threading.Lock()
     start = time.perf_counter()
 
+    phases = {}
+
     def handle(i):
         # latency from the scheduled arrival (includes any client-side delay)
-        k, _, ok = mix.run(reqs[i], precision)
+        t_begin = time.perf_counter()
+        ph = {}
+        k, _, ok = mix.run(reqs[i], precision, ph)
         done = time.perf_counter()
+        ph["client_wait"] = t_begin - (start + arrivals[i])
         with lock:
             results.append((k, done - (start + arrivals[i]), ok, done))
+            for name, v in ph.items():
+                phases.setdefault(k, {}).setdefault(name, []).append(v)
 
     with ThreadPoolExecutor(max_workers=clients) as ex:
         futs = []
@@ -245,5 +264,8 @@ def serve_stream(mix, rate, duration, precision, seed=11, clients=64):
             "by_kind": {k: {"n": len(v), "p50_ms": 1e3 * _pct(v, 0.5), "p99_ms": 1e3 * _pct(v, 0.99)}
                         for k, v in by.items()},
             "converged": all(r[2] for r in results),
+            # where the time goes, per kind: p99 of each phase of the client's request
+            "phases_p99_ms": {k: {n: 1e3 * _pct(v, 0.99) for n, v in d.items()} for k, d in phases.items()},
             "server": {k: st[k] for k in ("batches", "batchedSolves", "largeSolves", "largeYields", "hbmInUse",
-                                          "hbmBudget", "refused", "failed")}}
+                                          "hbmBudget", "refused", "failed", "queueP50Ms", "queueP99Ms",
+                                          "runP50Ms", "runP99Ms")}}

@@ -417,7 +417,7 @@ typedef struct {
                                  * 0: one CTA each); a result depends on its matrix only, never on
                                  * the rest of the launch */
     int lanes;                  /* batch launches that may run at once, each on its own stream
-                                 * (default 4, 1..16) */
+                                 * (default 8, 1..16) */
 } cfx_server_config;
 typedef struct {
     int64_t submitted, completed, cancelled, failed, refused;

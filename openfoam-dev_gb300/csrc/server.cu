@@ -26,7 +26,8 @@
 //     context.  Those launch cooperative grids that must have the device to
 //     themselves, so large kernels and batch kernels never run at the same
 //     time: a large solve starts once the lanes are idle (lanes start
-//     nothing new while one waits), and yields between its V-cycles (or
+//     nothing new once a large request has waited 100 ms), and yields
+//     between its V-cycles (or
 //     batches of Krylov iterations) whenever small requests are waiting:
 //     the idle lanes start launches in that gap, the gap closes when the
 //     first of them finishes, and the large solve resumes when all have.  A
@@ -343,13 +344,18 @@ void finish_all(cfx_server* sv, std::vector<SrvRequest*>& rs, cfx_status st, con
     sv->cvWork.notify_all();
 }
 
+// A large request waits this long for the lanes to go idle on their own
+// before the lanes stop starting launches for it.
+constexpr auto LARGE_HOLD = std::chrono::milliseconds(100);
+
 // Whether a lane may start a launch now (mu held): small requests are
-// ready, and either no large solve is in progress and none waits to start,
-// or the running one has yielded.
+// ready, and either no large solve is in progress and no large request has
+// waited LARGE_HOLD for the lanes, or the running one has yielded.
 bool lane_may_start(cfx_server* sv) {
     if (!next_ready(sv, false)) return false;
     if (sv->largeActive) return sv->yieldOpen;
-    return next_ready(sv, true) == nullptr;
+    const SrvRequest* big = next_ready(sv, true);
+    return !big || Clock::now() - big->tSubmit < LARGE_HOLD;
 }
 
 // A batch lane: every queued small request of the oldest ready one's
@@ -358,7 +364,8 @@ void lane_worker(cfx_server* sv, SrvLane* ln) {
     cudaSetDevice(sv->ctx->device);
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
-        sv->cvWork.wait(lk, [&] { return sv->stop || lane_may_start(sv); });
+        // timed: a waiting large request's hold runs out without a notify
+        while (!sv->stop && !lane_may_start(sv)) sv->cvWork.wait_for(lk, std::chrono::milliseconds(10));
         if (sv->stop) return;
         SrvRequest* first = next_ready(sv, false);
         const int prec = first->ctl.precision;
@@ -488,7 +495,7 @@ void cfx_server_default_config(cfx_server_config* c) {
     c->nCellsInCoarsestLevel = 10;
     c->groupCells = 100000;
     c->groupSize = 4;
-    c->lanes = 4;
+    c->lanes = 8;
 }
 
 cfx_status cfx_server_create(cfx_ctx* ctx, const cfx_server_config* cfg, cfx_server** out) {

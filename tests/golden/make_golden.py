@@ -31,7 +31,8 @@ openfoam-dev_gb300/cases.py; their checksums are stored to catch drift.
 
 Usage:  python tests/golden/make_golden.py
         (flux_fvsolve.npz alone, on the machine that made the fvsolve
-        fixtures: python tests/golden/make_golden.py --fvsolve-inputs)
+        fixtures: python tests/golden/make_golden.py --fvsolve-inputs;
+        some fvcyc_*.npz alone: python tests/golden/make_golden.py --fvcyc NAME...)
 """
 import hashlib
 import json
@@ -251,14 +252,23 @@ FVCYC = dict(mesh=dict(nx=10, ny=9, nz=8, jitter=0.25, seed=4, periodic_x=True),
                         dict(solver="PBiCG", preconditioner="DILU", tolerance=1e-10, relTol=0.0)),
     "transport_smooth": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
                          dict(solver="smoothSolver", smoother="symGaussSeidel", tolerance=1e-9, relTol=0.0)),
+    # the direct coarsest-level solve with the cyclic interfaces in its dense matrix
+    "laplacian_gamg_direct": (dict(lapSign=-1, gammaUniform=0.6, su=True),
+                              dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True,
+                                   tolerance=1e-9, relTol=0.0)),
+    "transport_gamg_direct": (dict(deltaT=0.004, div="upwind", lapSign=-1, gamma=True, su=True),
+                              dict(solver="GAMG", smoother="GaussSeidel", directSolveCoarsest=True,
+                                   tolerance=1e-10, relTol=0.0)),
 })
 
 
-def fvcyc_cases():
+def fvcyc_cases(only=None):
     m = cases.box_mesh(**FVCYC["mesh"])
     inp = gc.fvcyc_inputs(m, FVCYC["seed"])
     nI = m["nInternalFaces"]
     for name, (eq, ctl) in FVCYC["cases"].items():
+        if only and name not in only:
+            continue
         kw = gc.fvm_ref_kwargs(eq, inp, FVCYC["patchBC"])
         r = ref.fvm(m, solve=ctl, **kw)
         out = {k: v for k, v in r.items() if not isinstance(v, str)}
@@ -292,6 +302,13 @@ def main():
         specs["fvcyc"] = FVCYC
     with open(os.path.join(HERE, "specs.json"), "w") as fh:
         json.dump(specs, fh, indent=1, sort_keys=True)
+    if len(sys.argv) > 2 and sys.argv[1] == "--fvcyc":
+        # only the named cyclic fvMatrix::solve fixtures (the others kept)
+        if not ref.fv_available():
+            print("fv_harness not built (python oracle/build_ref_fv.py)")
+            return 1
+        fvcyc_cases(only=set(sys.argv[2:]))
+        return 0
 
     # geometry of a jittered box
     m = cases.box_mesh(5, 6, 7, jitter=0.3, seed=11)

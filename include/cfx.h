@@ -250,7 +250,7 @@ cfx_status cfx_fv_geometry(cfx_mesh* mesh, const double* magSf, const double* de
                            const double* magSfB, const double* deltaCoeffsB);
 
 enum { CFX_DIV_UPWIND = 0, CFX_DIV_LINEAR = 1 };
-enum { CFX_BC_ZERO_GRADIENT = 0, CFX_BC_FIXED_VALUE = 1, CFX_BC_FIXED_GRADIENT = 2 };
+enum { CFX_BC_ZERO_GRADIENT = 0, CFX_BC_FIXED_VALUE = 1, CFX_BC_FIXED_GRADIENT = 2, CFX_BC_CYCLIC = 3 };
 
 /* fvm::ddt(psi) + fvm::div(phi, psi) + lapSign*fvm::laplacian(gamma, psi)
  * == su, every pointer a device array, every term optional:
@@ -262,7 +262,15 @@ enum { CFX_BC_ZERO_GRADIENT = 0, CFX_BC_FIXED_VALUE = 1, CFX_BC_FIXED_GRADIENT =
  *     gamma/gammaB per face, or gammaUniform when gamma == NULL;
  *   su (NULL: none): operator==, source += V*su.
  * psi's boundary conditions per boundary face: bcType CFX_BC_* and bcValue
- * (the fixed value or the fixed gradient). */
+ * (the fixed value or the fixed gradient).  CFX_BC_CYCLIC marks a face of a
+ * cyclic patch (cyclicFvPatchField): the coupled patch coefficients
+ * (coupledFvPatchField.C:157-205: value w, 1 - w with the upwind weight;
+ * gradient -deltaCoeffs, deltaCoeffs with deltaCoeffsB of that face the
+ * snGrad scheme's, nonOrthDeltaCoeffs), internalCoeffs added to the
+ * diagonal, boundaryCoeffs kept out of the source, and both written as the
+ * matrix's interface coefficients; the cyclic faces, in boundary order, must
+ * be the faces given to cfx_mesh_set_interfaces, in their order (else
+ * CFX_ERR_ARG), and a div term with them must be upwind. */
 typedef struct {
     double rDeltaT;
     const double* psi0;

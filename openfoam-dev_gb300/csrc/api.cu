@@ -61,6 +61,7 @@ struct cfx_mesh {
     // interface face given in patch order
     int nIf = 0;
     std::vector<int> ifPos;
+    int* d_ifPos = nullptr;  // the same on the device (device assembly of cyclic faces)
     Arena ifArena;
     // the same interfaces on the host (patch sizes, face cells, partner
     // cells, patch order) and the GAMG levels' coarse interfaces; each
@@ -2012,6 +2013,7 @@ cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32
         m.nIf = int(nIf);
         m.ifStart = m.ifNbr = m.ifCells = nullptr;
         mesh->ifPos.assign(size_t(nIf), 0);
+        mesh->d_ifPos = nullptr;
         mesh->nIf = int(nIf);
         if (nIf) {
             // CSR over cells, each cell's faces in patch-then-face order (a
@@ -2027,6 +2029,7 @@ cfx_status cfx_mesh_set_interfaces(cfx_mesh* mesh, int32_t nPatches, const int32
                 mesh->ifPos[size_t(k)] = j;
             }
             m.ifStart = mesh->ifArena.upload(start, s);
+            mesh->d_ifPos = mesh->ifArena.upload(mesh->ifPos, s);
             m.ifNbr = mesh->ifArena.upload(nbr, s);
         }
         mesh->ifPatchSize.assign(patchSize, patchSize + nPatches);
@@ -2199,11 +2202,31 @@ cfx_status cfx_fvm_assemble(cfx_matrix* mat, const cfx_fvm_terms* t, double* d_s
         a.hasDdt = ddt;
         a.hasDiv = div;
         LevelCoeffs<double>& c = mat->c64[0];
-        after_caller(mesh->ctx);
-        launch_fvm_assemble(mesh->ctx->stream, mesh->dev[0], g, a, c.diag, c.upper, mat->sym ? nullptr : c.lower,
+        cfx_ctx* ctx = mesh->ctx;
+        const int nIf = mesh->nIf;
+        if (nIf && (mat->ifN != nIf || !c.ifBou)) {
+            c.ifBou = mat->arena.get<double>(nIf);
+            c.ifInt = mat->arena.get<double>(nIf);
+        }
+        after_caller(ctx);
+        launch_fvm_assemble(ctx->stream, mesh->dev[0], g, a, c.diag, c.upper, mat->sym ? nullptr : c.lower,
                             d_source);
         CK(cudaGetLastError());
-        to_caller(mesh->ctx);
+        if (nIf) {
+            // the cyclic faces' coefficients become the interface coefficients
+            CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+            launch_fvm_interfaces(ctx->stream, g, a, nIf, mesh->d_ifPos, c.ifBou, c.ifInt, ctx->d_status);
+            CK(cudaGetLastError());
+            if (read_status(ctx) != 0) {
+                CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+                set_error("cfx_fvm_assemble: the cyclic boundary faces (bcType CFX_BC_CYCLIC) are not the "
+                          "interfaces' faces, or a linear div term meets them");
+                return CFX_ERR_ARG;
+            }
+            mat->ifN = nIf;
+            mat->coarse64 = mat->coarse32 = false;  // the GAMG levels' interface sums
+        }
+        to_caller(ctx);
         mat->diagonal = false;
         coefficients_changed(mat);
         return CFX_OK;

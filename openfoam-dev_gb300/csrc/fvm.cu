@@ -18,7 +18,10 @@
 //   * operator==(fvMatrix, field): source += V*su (fvMatrix.C:1705-1715);
 //   * fvMatrix::solveSegregated's addBoundaryDiag / addBoundarySource
 //     (fvMatrix.C:112-174): each cell adds its boundary faces' coefficients
-//     in patch-then-face order.
+//     in patch-then-face order, the cyclic faces' internalCoeffs to the
+//     diagonal only; their boundaryCoeffs and internalCoeffs become the
+//     solver's interfaceBouCoeffs / interfaceIntCoeffs (coupledFvPatchField
+//     coefficients, coupledFvPatchField.C:157-205).
 // Compiled with --fmad=false like the rest of the library: no contraction.
 
 #include "internal.h"
@@ -88,20 +91,31 @@ __device__ __forceinline__ void face_combined(const FvmArgs& a, const FaceTerms&
     }
 }
 
-// One boundary face's combined internal and boundary coefficients.
+constexpr int BC_CYCLIC = 3;
+
+// One boundary face's combined internal and boundary coefficients.  A
+// cyclic face takes the coupled patch coefficients: value (w, 1 - w) with the
+// upwind weight pos0(phi), gradient (-deltaCoeffs, deltaCoeffs).
 __device__ __forceinline__ void boundary_combined(const FvmArgs& a, const FvGeom& g, int b, double& ic, double& bc) {
     const int type = a.bcType[b];
     double divIc = 0.0, divBc = 0.0, lapIc = 0.0, lapBc = 0.0;
     if (a.hasDiv) {
-        const double vic = type == 1 ? 0.0 : 1.0;
-        const double vbc = type == 1 ? a.bcValue[b] : type == 2 ? a.bcValue[b] / g.deltaCoeffsB[b] : 0.0;
-        divIc = a.phiB[b] * vic;
-        divBc = -a.phiB[b] * vbc;
+        if (type == BC_CYCLIC) {
+            const double w = a.phiB[b] >= 0.0 ? 1.0 : 0.0;
+            divIc = a.phiB[b] * (1.0 * w);
+            divBc = -a.phiB[b] * (1.0 * (1.0 - w));
+        } else {
+            const double vic = type == 1 ? 0.0 : 1.0;
+            const double vbc = type == 1 ? a.bcValue[b] : type == 2 ? a.bcValue[b] / g.deltaCoeffsB[b] : 0.0;
+            divIc = a.phiB[b] * vic;
+            divBc = -a.phiB[b] * vbc;
+        }
     }
     if (a.lapSign) {
         const double gms = (a.gammaB ? a.gammaB[b] : a.gammaUniform) * g.magSfB[b];
-        const double gic = type == 1 ? -1.0 * g.deltaCoeffsB[b] : 0.0;
-        const double gbc = type == 1 ? g.deltaCoeffsB[b] * a.bcValue[b] : type == 2 ? a.bcValue[b] : 0.0;
+        const double gic = type == 1 || type == BC_CYCLIC ? -1.0 * g.deltaCoeffsB[b] : 0.0;
+        const double gbc = type == BC_CYCLIC ? -gic
+                           : type == 1 ? g.deltaCoeffsB[b] * a.bcValue[b] : type == 2 ? a.bcValue[b] : 0.0;
         lapIc = gms * gic;
         lapBc = -gms * gbc;
     }
@@ -199,13 +213,57 @@ __global__ void __launch_bounds__(FV_NT) fvm_cells_k(int n, const int* __restric
         const int b1 = g.bStart[c + 1];
         for (int k = g.bStart[c]; k < b1; ++k) {
             double ic, bc;
-            boundary_combined(a, g, g.bFace[k], ic, bc);
+            const int b = g.bFace[k];
+            boundary_combined(a, g, b, ic, bc);
             D += ic;
-            S += bc;
+            if (a.bcType[b] != BC_CYCLIC) S += bc;
         }
         diag[c] = D;
         source[c] = S;
     }
+}
+
+// The cyclic faces' coefficients as the solver's interface coefficients:
+// one CTA walks the boundary faces in order, numbering the cyclic ones with
+// a block-wide prefix count.
+constexpr int FVI_NT = 1024;
+
+__global__ void __launch_bounds__(FVI_NT) fvm_iface_k(FvGeom g, FvmArgs a, int nIf, const int* __restrict__ ifPos,
+                                                      double* __restrict__ ifBou, double* __restrict__ ifInt,
+                                                      int* status) {
+    __shared__ int warpCount[FVI_NT / 32];
+    __shared__ int base;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < g.nBoundary; b0 += FVI_NT) {
+        const int b = b0 + threadIdx.x;
+        const bool cyc = b < g.nBoundary && a.bcType[b] == BC_CYCLIC;
+        const unsigned m = __ballot_sync(0xffffffffu, cyc);
+        if (lane == 0) warpCount[w] = __popc(m);
+        __syncthreads();
+        int before = base;
+        for (int i = 0; i < w; ++i) before += warpCount[i];
+        const int k = before + __popc(m & ((1u << lane) - 1u));
+        if (cyc) {
+            if (a.hasDiv && a.divScheme != 0) {
+                *status = CFX_ERR_ARG;  // linear weights of a cyclic patch are not given
+            } else if (k < nIf) {
+                double ic, bc;
+                boundary_combined(a, g, b, ic, bc);
+                ifBou[ifPos[k]] = bc;
+                ifInt[ifPos[k]] = ic;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == FVI_NT - 1) {
+            int total = 0;
+            for (int i = 0; i < FVI_NT / 32; ++i) total += warpCount[i];
+            base += total;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && base != nIf) *status = CFX_ERR_ARG;
 }
 
 inline int fv_grid(int n) {
@@ -214,6 +272,12 @@ inline int fv_grid(int n) {
 }
 
 }  // namespace
+
+void launch_fvm_interfaces(cudaStream_t s, const FvGeom& g, const FvmArgs& a, int nIf, const int* ifPos,
+                           double* ifBou, double* ifInt, int* status) {
+    fvm_iface_k<<<1, FVI_NT, 0, s>>>(g, a, nIf, ifPos, ifBou, ifInt, status);
+    count_launch();
+}
 
 void launch_fvm_assemble(cudaStream_t s, const LevelMesh& m, const FvGeom& g, const FvmArgs& a, double* diag,
                          double* upper, double* lower, double* source) {

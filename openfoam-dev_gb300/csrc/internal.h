@@ -258,6 +258,12 @@ struct FvmArgs {
 
 // diag, upper, lower (asymmetric results) and source of the assembled
 // equation as fvMatrix::solveSegregated hands them to the solver.
+// The cyclic boundary faces (bcType 3), in boundary order the interfaces'
+// faces in patch order: their boundaryCoeffs and internalCoeffs written to
+// ifBou/ifInt at the faces' CSR positions ifPos; *status = CFX_ERR_ARG when
+// their count is not nIf or a linear div meets one (one CTA, in order).
+void launch_fvm_interfaces(cudaStream_t s, const FvGeom& g, const FvmArgs& a, int nIf, const int* ifPos,
+                           double* ifBou, double* ifInt, int* status);
 void launch_fvm_assemble(cudaStream_t s, const LevelMesh& m, const FvGeom& g, const FvmArgs& a, double* diag,
                          double* upper, double* lower, double* source);
 

@@ -110,7 +110,7 @@ class FvmTerms(ctypes.Structure):
 
 
 DIV_SCHEMES = {"upwind": 0, "linear": 1}
-BC_TYPES = {"zeroGradient": 0, "fixedValue": 1, "fixedGradient": 2}
+BC_TYPES = {"zeroGradient": 0, "fixedValue": 1, "fixedGradient": 2, "cyclic": 3}
 
 
 _SIG = {

@@ -300,7 +300,15 @@ int runFvm(const RecMap& in, Writer& out, Time& runTime)
     {
         const fvPatch& fp = mesh.boundary()[p];
         const labelUList& fc = fp.faceCells();
-        const scalarField dc(fp.deltaCoeffs());
+        // the Laplacian takes a coupled patch's coefficients from the snGrad
+        // scheme's deltaCoeffs (nonOrthDeltaCoeffs), an uncoupled patch's
+        // from the patch's own deltaCoeffs (gaussLaplacianScheme.C:64-86)
+        const scalarField dc
+        (
+            fp.coupled()
+          ? scalarField(mesh.nonOrthDeltaCoeffs().boundaryField()[p])
+          : scalarField(fp.deltaCoeffs())
+        );
         forAll(fc, k)
         {
             bCell.append(fc[k]);

@@ -1591,6 +1591,14 @@ static void fvm_div(fvm_mat* m, const ldu_fv_geom* g, const ldu_fvm_terms* t) {
     fvm_neg_sum_diag(m, g);
     for (int b = 0; b < g->nBoundary; ++b) {
         const int type = t->bcType[b];
+        if (type == LDU_BC_CYCLIC) {
+            /* coupledFvPatchField::valueInternalCoeffs / valueBoundaryCoeffs:
+             * (w, 1 - w), upwind w = pos0(phi) */
+            const double w = t->phiB[b] >= 0.0 ? 1.0 : 0.0;
+            m->ic[b] = t->phiB[b] * (1.0 * w);
+            m->bc[b] = -t->phiB[b] * (1.0 * (1.0 - w));
+            continue;
+        }
         const double vic = type == LDU_BC_FIXED_VALUE ? 0.0 : 1.0;
         const double vbc = type == LDU_BC_FIXED_VALUE ? t->bcValue[b]
                            : type == LDU_BC_FIXED_GRADIENT ? t->bcValue[b] / g->deltaCoeffsB[b]
@@ -1615,8 +1623,11 @@ static void fvm_laplacian(fvm_mat* m, const ldu_fv_geom* g, const ldu_fvm_terms*
     for (int b = 0; b < g->nBoundary; ++b) {
         const double gms = (t->gammaB ? t->gammaB[b] : t->gammaUniform) * g->magSfB[b];
         const int type = t->bcType[b];
-        const double gic = type == LDU_BC_FIXED_VALUE ? -1.0 * g->deltaCoeffsB[b] : 0.0;
-        const double gbc = type == LDU_BC_FIXED_VALUE ? g->deltaCoeffsB[b] * t->bcValue[b]
+        /* coupled: gradientInternalCoeffs(deltaCoeffs) = -deltaCoeffs,
+         * gradientBoundaryCoeffs = minus that */
+        const double gic = type == LDU_BC_FIXED_VALUE || type == LDU_BC_CYCLIC ? -1.0 * g->deltaCoeffsB[b] : 0.0;
+        const double gbc = type == LDU_BC_CYCLIC ? -gic
+                           : type == LDU_BC_FIXED_VALUE ? g->deltaCoeffsB[b] * t->bcValue[b]
                            : type == LDU_BC_FIXED_GRADIENT ? t->bcValue[b]
                                                            : 0.0;
         m->ic[b] = gms * gic;
@@ -1626,8 +1637,16 @@ static void fvm_laplacian(fvm_mat* m, const ldu_fv_geom* g, const ldu_fvm_terms*
 
 int ldu_fvm_assemble(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper, double* lower,
                      double* source) {
+    return ldu_fvm_assemble_coupled(g, t, diag, upper, lower, source, NULL, NULL);
+}
+
+int ldu_fvm_assemble_coupled(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper,
+                             double* lower, double* source, double* ifBou, double* ifInt) {
     fvm_mat C, A;
     int have = 0;
+    if (t->phi && t->divScheme != LDU_DIV_UPWIND)
+        for (int b = 0; b < g->nBoundary; ++b)
+            if (t->bcType[b] == LDU_BC_CYCLIC) return -2;
     fvm_init(&C, g);
     if (t->rDeltaT > 0) {
         fvm_ddt(&C, g, t->rDeltaT, t->psi0);
@@ -1666,9 +1685,16 @@ int ldu_fvm_assemble(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag,
     /* fvMatrix::solveSegregated: addBoundarySource, addBoundaryDiag */
     memcpy(diag, fvm_diag(&C), sizeof(double) * g->nCells);
     memcpy(source, C.src, sizeof(double) * g->nCells);
+    int k = 0;
     for (int b = 0; b < g->nBoundary; ++b) {
         diag[g->bCell[b]] += C.ic[b];
-        source[g->bCell[b]] += C.bc[b];
+        if (t->bcType[b] != LDU_BC_CYCLIC) {
+            source[g->bCell[b]] += C.bc[b];
+        } else {
+            if (ifBou) ifBou[k] = C.bc[b];
+            if (ifInt) ifInt[k] = C.ic[b];
+            ++k;
+        }
     }
     const double* U = C.upper ? C.upper : C.lower;
     if (U) memcpy(upper, U, sizeof(double) * g->nFaces);

@@ -197,7 +197,7 @@ typedef struct {
 } ldu_fv_geom;
 
 enum { LDU_DIV_UPWIND = 0, LDU_DIV_LINEAR = 1 };
-enum { LDU_BC_ZERO_GRADIENT = 0, LDU_BC_FIXED_VALUE = 1, LDU_BC_FIXED_GRADIENT = 2 };
+enum { LDU_BC_ZERO_GRADIENT = 0, LDU_BC_FIXED_VALUE = 1, LDU_BC_FIXED_GRADIENT = 2, LDU_BC_CYCLIC = 3 };
 
 /* fvm::ddt(psi) + fvm::div(phi, psi) + lapSign*fvm::laplacian(gamma, psi)
  * == su, each term optional: ddt when rDeltaT > 0 (Euler: psi0 the old
@@ -227,6 +227,18 @@ typedef struct {
  * term is given. */
 int ldu_fvm_assemble(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper, double* lower,
                      double* source);
+/* The same with cyclic (coupled) boundary faces (bcType LDU_BC_CYCLIC): their
+ * internalCoeffs join the diagonal (addBoundaryDiag), their boundaryCoeffs
+ * stay out of the source (addBoundarySource(source, false)), and both are
+ * returned, in boundary-face order, as the solver's interfaceBouCoeffs
+ * (ifBou) and interfaceIntCoeffs (ifInt).  Coupled patches take the
+ * coupledFvPatchField coefficients (coupledFvPatchField.C:157-205): value
+ * (w, 1 - w) with the upwind weight pos0(phi), gradient (-deltaCoeffs,
+ * deltaCoeffs) with the snGrad scheme's deltaCoeffs in deltaCoeffsB.
+ * Returns -1 when no term is given, -2 for linear div with cyclic faces
+ * (the patch weights are not given). */
+int ldu_fvm_assemble_coupled(const ldu_fv_geom* g, const ldu_fvm_terms* t, double* diag, double* upper,
+                             double* lower, double* source, double* ifBou, double* ifInt);
 
 #ifdef __cplusplus
 }

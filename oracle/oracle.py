@@ -409,11 +409,13 @@ DIV_SCHEMES = {"upwind": 0, "linear": 1}
 
 
 def fvm_assemble(l, u, geom, rDeltaT=0.0, psi0=None, phi=None, phiB=None, div="upwind", lapSign=0, gamma=1.0,
-                 gammaB=None, bcType=None, bcValue=None, su=None):
+                 gammaB=None, bcType=None, bcValue=None, su=None, coupled=False):
     """The lduMatrix (diag, upper, lower or None) and source that
     fvMatrix::solveSegregated hands to the solver for
     fvm::ddt + fvm::div - or + fvm::laplacian == su (ldu_fvm_assemble).
-    geom: magSf, deltaCoeffs, weights, V, bCell, magSfB, deltaCoeffsB."""
+    geom: magSf, deltaCoeffs, weights, V, bCell, magSfB, deltaCoeffsB.
+    coupled: also return the cyclic faces' (bcType 3) interfaceBouCoeffs
+    and interfaceIntCoeffs, in boundary-face order."""
     f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
     i = lambda a: None if a is None else np.ascontiguousarray(a, np.int32)
     l, u = i(l), i(u)
@@ -431,7 +433,14 @@ def fvm_assemble(l, u, geom, rDeltaT=0.0, psi0=None, phi=None, phiB=None, div="u
                     _p(arrs["bcType"], i32p), _p(arrs["bcValue"]), _p(arrs["su"]))
     diag, upper, source = np.empty(nC), np.empty(max(nF, 1)), np.empty(nC)
     lower = np.empty(max(nF, 1)) if phi is not None else None
-    if lib().ldu_fvm_assemble(ctypes.byref(gc), ctypes.byref(t), _p(diag), _p(upper), _p(lower), _p(source)) != 0:
+    nCyc = int(np.count_nonzero(arrs["bcType"] == 3)) if arrs["bcType"] is not None else 0
+    ifBou, ifInt = np.empty(max(nCyc, 1)), np.empty(max(nCyc, 1))
+    rc = lib().ldu_fvm_assemble_coupled(ctypes.byref(gc), ctypes.byref(t), _p(diag), _p(upper), _p(lower),
+                                        _p(source), _p(ifBou), _p(ifInt))
+    if rc == -2:
+        raise ValueError("linear div with cyclic faces")
+    if rc != 0:
         raise ValueError("no term")
     del keep
-    return diag, upper[:nF], None if lower is None else lower[:nF], source
+    out = (diag, upper[:nF], None if lower is None else lower[:nF], source)
+    return out + (ifBou[:nCyc], ifInt[:nCyc]) if coupled else out

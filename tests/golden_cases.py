@@ -172,6 +172,23 @@ def fvcyc_names():
     return sorted(f[6:-4] for f in os.listdir(GOLDEN) if f.startswith("fvcyc_") and f.endswith(".npz"))
 
 
+def fvcyc_assembly_case(name):
+    """One cyclic fvMatrix fixture as an assembly case: (l, u, the
+    reference's geometry (the cyclic faces' deltaCoeffsB the snGrad
+    scheme's), the terms with the cyclic pair as bcType 3, and the
+    reference's diag/upper/lower/source and interfaceBou/IntCoeffs)."""
+    eq, _ = SPECS["fvcyc"]["cases"][name]
+    g = load(f"fvcyc_{name}.npz")
+    m = cases.box_mesh(**SPECS["fvcyc"]["mesh"])
+    inp = fvcyc_inputs(m, SPECS["fvcyc"]["seed"])
+    inp["phi"], inp["phiB"] = g["in_phi"], g["in_phiB"]  # the fluxes the reference was given
+    bcType = np.repeat(np.asarray(SPECS["fvcyc"]["patchBC"], np.int32), np.diff(g["patchStart"])).astype(np.int32)
+    geom = {k: g[k] for k in FVM_GEOMETRY_KEYS}
+    ref = dict(diag=g["diag"], upper=g["upper"], lower=g.get("lower"), source=g["source"], ifBou=g["ifBou"],
+               ifInt=g["ifInt"], ifSize=g["ifSize"], ifCell=g["ifCell"], ifNbr=g["ifNbr"])
+    return g["l"], g["u"], geom, fvm_terms(eq, inp, bcType), ref
+
+
 def fvcyc_case(name):
     """(the lduMatrix system with its cyclic interfaces as the solver
     received it, the starting psi, the solver controls, the reference's

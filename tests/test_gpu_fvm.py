@@ -127,3 +127,63 @@ def test_assembly_errors():
     other = ldu.LduMesh(ldu.default_context(), n, m["owner"][:m["nInternalFaces"]], m["neighbour"])
     with pytest.raises(ldu.CfxError):  # no geometry
         ldu.LduMatrix.empty(other, symmetric=True).assemble(source, **_terms(CASES["minus_laplacian"], f, dev=True))
+
+
+def _cyclic_names():
+    from golden_cases import fvcyc_names
+    return fvcyc_names()
+
+
+@pytest.mark.parametrize("name", _cyclic_names())
+def test_cyclic_assembly_matches_the_reference(name):
+    """A cyclic patch pair assembled on the device (CFX_BC_CYCLIC): the
+    lduMatrix and source equal the reference's fvMatrix bit for bit, and the
+    interface coefficients written by the assembly give the reference's A x
+    and A^T x (interfaceBouCoeffs in Amul, interfaceIntCoeffs in Tmul)."""
+    from golden_cases import fvcyc_assembly_case
+    l, u, geom, terms, ref = fvcyc_assembly_case(name)
+    n, nI = geom["V"].size, l.size
+    mesh = ldu.LduMesh(ldu.default_context(), n, l, u)
+    mesh.set_interfaces(ref["ifSize"], ref["ifCell"], ref["ifNbr"],
+                        np.arange(len(ref["ifSize"]), dtype=np.int32) ^ 1)
+    mesh.fv_geometry(geom["magSf"], geom["deltaCoeffs"], geom["V"], geom["bCell"], geom["magSfB"],
+                     geom["deltaCoeffsB"], weights=geom["weights"])
+    A = ldu.LduMatrix.empty(mesh, symmetric=ref["lower"] is None)
+    source = torch.empty(n, dtype=torch.float64, device="cuda")
+    dev = {k: (_dev(v, torch.int32 if k == "bcType" else torch.float64) if isinstance(v, np.ndarray) else v)
+           for k, v in terms.items()}
+    A.assemble(source, **dev)
+    torch.cuda.synchronize()
+    got_d, got_u, got_l = A.coarse(0, n, nI)
+    np.testing.assert_array_equal(got_d, ref["diag"])
+    np.testing.assert_array_equal(got_u, ref["upper"])
+    if ref["lower"] is not None:
+        np.testing.assert_array_equal(got_l, ref["lower"])
+    np.testing.assert_array_equal(source.cpu().numpy(), ref["source"])
+    s = dict(l=l, u=u, diag=ref["diag"], upper=ref["upper"], lower=ref["lower"], ifSize=ref["ifSize"],
+             ifCell=ref["ifCell"], ifNbr=ref["ifNbr"], ifBou=ref["ifBou"], ifInt=ref["ifInt"])
+    om = orc.Matrix(s)
+    x = cases.uniform(5, n)
+    dx, dy = _dev(x), torch.empty(n, dtype=torch.float64, device="cuda")
+    A.Amul(dx, dy)
+    np.testing.assert_array_equal(dy.cpu().numpy(), om.amul(x))
+    A.Tmul(dx, dy)
+    np.testing.assert_array_equal(dy.cpu().numpy(), om.tmul(x))
+
+
+def test_cyclic_faces_must_be_the_interfaces():
+    from golden_cases import fvcyc_assembly_case
+    l, u, geom, terms, ref = fvcyc_assembly_case("laplacian_pcg")
+    n = geom["V"].size
+    mesh = ldu.LduMesh(ldu.default_context(), n, l, u)
+    # one patch's faces only: the assembly finds twice as many cyclic faces
+    k = int(ref["ifSize"][0])
+    mesh.set_interfaces(ref["ifSize"][:1], ref["ifCell"][:k], ref["ifNbr"][:k])
+    mesh.fv_geometry(geom["magSf"], geom["deltaCoeffs"], geom["V"], geom["bCell"], geom["magSfB"],
+                     geom["deltaCoeffsB"], weights=geom["weights"])
+    A = ldu.LduMatrix.empty(mesh, symmetric=True)
+    source = torch.empty(n, dtype=torch.float64, device="cuda")
+    dev = {k2: (_dev(v, torch.int32 if k2 == "bcType" else torch.float64) if isinstance(v, np.ndarray) else v)
+           for k2, v in terms.items()}
+    with pytest.raises(ldu.CfxError, match="cyclic"):
+        A.assemble(source, **dev)

@@ -274,3 +274,22 @@ def test_direct_coarsest_with_interfaces(U):
     t.pop("ifNbrPatch")
     with pytest.raises(ValueError, match="partner"):
         orc.gamg(t, np.zeros_like(s["source"]), tol=1e-9, directSolveCoarsest=True)
+
+
+@pytest.mark.parametrize("name", fvcyc_names())
+def test_cyclic_fvmatrix_assembly_bit_exact(name):
+    """The reference's assembly with a cyclicFvPatchField pair
+    (coupledFvPatchField's value and gradient coefficients; addBoundaryDiag
+    over every patch, addBoundarySource over the uncoupled ones): the
+    oracle reproduces the lduMatrix, the source and the interfaceBouCoeffs /
+    interfaceIntCoeffs the solver received, bit for bit."""
+    from golden_cases import fvcyc_assembly_case
+    l, u, geom, terms, ref = fvcyc_assembly_case(name)
+    d, up, lo, src, ib, ii = orc.fvm_assemble(l, u, geom, coupled=True, **terms)
+    np.testing.assert_array_equal(d, ref["diag"])
+    np.testing.assert_array_equal(up, ref["upper"])
+    if ref["lower"] is not None:
+        np.testing.assert_array_equal(lo, ref["lower"])
+    np.testing.assert_array_equal(src, ref["source"])
+    np.testing.assert_array_equal(ib, ref["ifBou"])
+    np.testing.assert_array_equal(ii, ref["ifInt"])

@@ -346,7 +346,15 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
         * it from the level's sliced ELL copy, 2 with the slices whose rows
         * share at most 8 neighbour offsets stored without columns (1 or 2
         * is read when a mesh is created).  The results are identical */
-       CFX_TUNE_AMUL_SELL = 9 };
+       CFX_TUNE_AMUL_SELL = 9,
+       /* level-counter grid form of the sweeps: the spacing of the per-level
+        * completion counters in ints (1..32; 32 puts each in its own 128-byte
+        * line) and the back-off of the waiting CTAs' polls in ns (0..1000) */
+       CFX_TUNE_GRID_STRIDE = 10, CFX_TUNE_GRID_POLL_NS = 11,
+       /* groups of 32 slots per chunk of the level-counter grid form (1..8,
+        * default 2), read when a level's schedule is built: smaller chunks
+        * spread a DAG level's arithmetic over more SMs */
+       CFX_TUNE_CHUNK_GROUPS = 12 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -280,7 +280,10 @@ void launch_reduce(cudaStream_t s, Scratch& sc, int which, int n, const T* a, co
 // entries, levels of the upper-neighbour DAG, cells in reverse order)
 enum { SCHED_FWD = 0, SCHED_BWD = 1, SCHED_GS = 2, SCHED_GSB = 3 };
 constexpr int SRC_UPPER = 1 << 30;       // entry coefficient from upper[f]
-constexpr int SCHED_CHUNK_GROUPS = 8;    // groups of 32 slots per grid chunk
+constexpr int SCHED_CHUNK_GROUPS = 8;    // most groups of 32 slots per grid chunk (one CTA)
+// groups per grid chunk of the schedules built from now on (1..8)
+int sched_chunk_groups();
+void set_sched_chunk_groups(int g);
 
 struct HostSched {
     int kind = 0, nSweeps = 1, nLevels = 0, n = 0, maxK = 0;
@@ -303,12 +306,15 @@ struct DevSched {
     int *levelSlot = nullptr, *levelEntry = nullptr, *groupEntry = nullptr;
     int *cell = nullptr, *cnt = nullptr, *nb = nullptr, *src = nullptr;
     int *chunkGroup = nullptr, *chunkLevel = nullptr, *levelChunks = nullptr;
-    int* sync = nullptr;                 // [2 + nLevels]: abort, pad, done[level]
+    int* sync = nullptr;                 // [2 + LVL_STRIDE_MAX*nLevels]: abort, pad, done[level*lvlStride]
+    int lvlStride = 1, pollNs = 0;       // set per launch: counter spacing (ints), poll back-off (ns)
     int *depStart = nullptr, *dep = nullptr;  // group dependencies (wavefront form)
     int* gdone = nullptr;                // [nGroups] group finished flags
     int waveOk = 0;                      // dependencies verified to point backwards
     int *slotSweep = nullptr, *slotLower = nullptr;  // [nSlots] (level-ordered schedules)
 };
+
+constexpr int LVL_STRIDE_MAX = 32;  // level counters up to one 128-byte line apart
 
 // coefficients packed for one schedule and one operation
 template <class T>
@@ -360,6 +366,12 @@ int sweep_flow();
 void set_sweep_flow(int on);
 int sweep_flow_ahead();
 void set_sweep_flow_ahead(int k);
+// level-counter grid form: counter spacing in ints (1..LVL_STRIDE_MAX) and
+// the back-off of its polls (ns, 0: none)
+int sweep_grid_stride();
+void set_sweep_grid_stride(int k);
+int sweep_grid_poll_ns();
+void set_sweep_grid_poll_ns(int ns);
 // A x products: 0 the losort/owner gathers, 1 the sliced ELL rows with
 // explicit columns, 2 (default) sliced ELL with offset-pattern slices (1/2
 // read when a level's rows are uploaded)

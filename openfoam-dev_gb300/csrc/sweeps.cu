@@ -80,6 +80,8 @@ size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
 int g_flow = 2;             // the dataflow form: 0 off, 1 on, 2 for schedules of <= PF_SMALL entries
 int g_flow_ahead = 4;       // dataflow form: levels of groups in flight (warps launched)
+int g_lvl_stride = 1;       // level-counter grid form: ints between consecutive level counters
+int g_poll_ns = 0;          // and the back-off of its waiting polls (ns)
 
 template <class T>
 struct SweepCtx {
@@ -141,6 +143,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
     if (a.done && *a.done) return;
     int* abortf = s.sync;
     int* done = s.sync + 2;
+    const int stride = s.lvlStride;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int J = blockIdx.x; J < s.nChunks; J += gridDim.x) {
         const int L = s.chunkLevel[J];
@@ -169,12 +172,13 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
             int ok = 1;
             if (L > 0) {
                 const int target = s.levelChunks[L - 1];
-                const int* d = done + L - 1;
+                const int* d = done + size_t(L - 1) * stride;
                 uint64_t t0 = 0;
                 unsigned spins = 0;
                 // acquire loads: the load that sees the count orders the
                 // reads of the previous level's values after it
                 while (ld_acquire(d) < target) {
+                    if (s.pollNs) __nanosleep(s.pollNs);
                     if (*(volatile int*)abortf) {
                         ok = 0;
                         break;
@@ -214,7 +218,7 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
             if (threadIdx.x == 0) a.partials[J] = p;
         }
         __syncthreads();
-        if (threadIdx.x == 0) red_release_add(done + L, 1);
+        if (threadIdx.x == 0) red_release_add(done + size_t(L) * stride, 1);
     }
 }
 
@@ -867,7 +871,10 @@ cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a,
         return CFX_OK;
     }
     {
-        CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + s.nLevels), st));
+        DevSched g = s;
+        g.lvlStride = g_lvl_stride;
+        g.pollNs = g_poll_ns;
+        CFX_CUDA(cudaMemsetAsync(s.sync, 0, sizeof(int) * (2 + size_t(g.lvlStride) * s.nLevels), st));
         const int grid = std::min(s.nChunks, g_grid[prec_index<T>()][OP][pf_index(PF)]);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
@@ -879,7 +886,7 @@ cfx_status launch_grid(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a,
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_grid_k<T, OP, PF>, s, a, status));
+        CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_grid_k<T, OP, PF>, g, a, status));
     }
     count_launch();
     return CFX_OK;
@@ -1010,6 +1017,10 @@ int sweep_wave() { return g_wave; }
 void set_sweep_wave(int on) { g_wave = on ? 1 : 0; }
 int sweep_flow() { return g_flow; }
 void set_sweep_flow(int mode) { g_flow = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+int sweep_grid_stride() { return g_lvl_stride; }
+void set_sweep_grid_stride(int k) { g_lvl_stride = k < 1 ? 1 : k > LVL_STRIDE_MAX ? LVL_STRIDE_MAX : k; }
+int sweep_grid_poll_ns() { return g_poll_ns; }
+void set_sweep_grid_poll_ns(int ns) { g_poll_ns = ns < 0 ? 0 : ns; }
 int sweep_flow_ahead() { return g_flow_ahead; }
 void set_sweep_flow_ahead(int k) { g_flow_ahead = k < 1 ? 1 : k; }
 

@@ -399,9 +399,14 @@ def level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells):
         x = torch.zeros_like(b)
         t = ev_time(lambda: Al.smooth("GaussSeidel", x, b, S))
         by = S * gs_bytes(nc, ncf)
+        # the form the library picks: one CTA when the vector fits its shared
+        # memory, else the dataflow form for the hexahedral finest level (at
+        # most 8 entries per slot) and the level-counter grid for the
+        # agglomerated levels (more entries per slot)
+        form = ("one CTA, vector in shared memory" if nc <= smem_cells
+                else "dataflow" if lv == 0 else "persistent grid")
         rows.append({"level": lv, "cells": nc, "faces": ncf, "sweeps": S, "s": t, "algorithmic_bytes": by,
-                     "GB_s": by / t / 1e9, "form": "one CTA, vector in shared memory" if nc <= smem_cells
-                     else "persistent grid"})
+                     "GB_s": by / t / 1e9, "form": form})
         if ml is not None:
             Al.close()
             ml.close()
@@ -786,7 +791,7 @@ def run_batch_serve(args, local, want_batch, want_serve):
         for prec in ("mixed", "FP64"):
             mix.run(mix.draw(), prec)  # warm the drivers
             mix.run(("large", None, 1), prec)
-            un = loadgen.serve_unloaded(mix, 32, prec)
+            un = loadgen.serve_unloaded(mix, 48, prec)
             t_large = un["by_kind_p50_ms"].get("large", 1000.0) / 1e3
             t_small = un["by_kind_p50_ms"].get("resident", 10.0) / 1e3
             # requests/s the GPU could take if nothing overlapped
@@ -805,11 +810,23 @@ def run_batch_serve(args, local, want_batch, want_serve):
                                 q["worst_kind_p99_over_unloaded_p99"] <= 2.0:
                             rate = f * capacity
                     r["sweep"] = sweep
-            q = loadgen.serve_stream(mix, rate, args.serve_duration, prec)
-            q["by_kind_ratio"], q["worst_kind_p99_over_unloaded_p99"] = loadgen.per_kind_ratio(q, un)
-            q["p99_over_unloaded_p99_all"] = q["p99_ms"] / un["p99_ms"]
-            r["stream"] = q
-            r["sustained_solves_per_s"] = q["solves_per_s"]
+            # the long stream; a 10 s sweep window sees few tail requests, so
+            # when the long stream misses the 2x target at the chosen rate it
+            # runs once more at 0.7x that rate (both kept)
+            attempts = []
+            for _ in range(2):
+                q = loadgen.serve_stream(mix, rate, args.serve_duration, prec)
+                q["by_kind_ratio"], q["worst_kind_p99_over_unloaded_p99"] = loadgen.per_kind_ratio(q, un)
+                q["p99_over_unloaded_p99_all"] = q["p99_ms"] / un["p99_ms"]
+                attempts.append(q)
+                w = q["worst_kind_p99_over_unloaded_p99"]
+                if args.serve_rate or w is None or w <= 2.0:
+                    break
+                rate *= 0.7
+            r["stream"] = attempts[-1]
+            if len(attempts) > 1:
+                r["stream_attempts"] = attempts[:-1]
+            r["sustained_solves_per_s"] = attempts[-1]["solves_per_s"]
             srv[prec] = r
         sv.close()
         out["serve"] = srv

@@ -354,7 +354,11 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
        /* groups of 32 slots per chunk of the level-counter grid form (1..8,
         * default 2), read when a level's schedule is built: smaller chunks
         * spread a DAG level's arithmetic over more SMs */
-       CFX_TUNE_CHUNK_GROUPS = 12 };
+       CFX_TUNE_CHUNK_GROUPS = 12,
+       /* single-CTA form in FP32: hold 32 (1, default) or 16 (0) entries per
+        * slot in registers when a schedule's slots have more than 16 (256^3
+        * mixed GAMG 1.77 -> 1.71 s; in FP64 the larger set spills) */
+       CFX_TUNE_CTA_XL = 13 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -368,6 +368,10 @@ int sweep_flow_ahead();
 void set_sweep_flow_ahead(int k);
 // level-counter grid form: counter spacing in ints (1..LVL_STRIDE_MAX) and
 // the back-off of its polls (ns, 0: none)
+// single-CTA form in FP32: 32 entries per slot held in registers for
+// schedules with more than 16 (1, default) or 16 (0)
+int sweep_cta_xl();
+void set_sweep_cta_xl(int on);
 int sweep_grid_stride();
 void set_sweep_grid_stride(int k);
 int sweep_grid_poll_ns();

@@ -22,16 +22,18 @@
 // in sweep s-1, so S sweeps take D + 2(S-1) levels instead of S*D.
 //
 // Execution forms:
-//   sweep_cta_k   one CTA of 1024 threads walks the levels with block
-//                 barriers; the vector lives in shared memory when it fits.
-//                 Used for coarse levels and small meshes.
+//   sweep_cta_k   one CTA of 256 threads walks the levels with block
+//                 barriers, each warp's next group prefetched into registers
+//                 (up to 32 entries per slot); the vector lives in shared
+//                 memory when it fits.  Used for coarse levels and small
+//                 meshes.
 //   sweep_cluster_k  a cluster of up to 16 CTAs (one GPC) holds the vector in
 //                 distributed shared memory (cell c in CTA c / per) and
 //                 separates levels with the hardware cluster barrier; each
 //                 warp prefetches its next group's packed data into registers
 //                 before the barrier.  Used up to ~16x the single-CTA size.
-//   sweep_grid_k  persistent CTAs, chunk J (8 groups of 32 slots, level
-//                 order) on CTA J mod grid; each CTA loads its next chunk's
+//   sweep_grid_k  persistent CTAs, chunk J (by default 2 groups of 32
+//                 slots, level order) on CTA J mod grid; each CTA loads its next chunk's
 //                 packed data, then waits (bounded spin, acquire) for every
 //                 chunk of the previous level to release its done-counter.
 //                 Launched cooperatively so all CTAs are resident.  A wait
@@ -80,6 +82,7 @@ size_t g_smem_cap = 200 * 1024;
 size_t g_smem_cap_max = 200 * 1024;
 int g_flow = 2;             // the dataflow form: 0 off, 1 on, 2 for schedules of <= PF_SMALL entries
 int g_flow_ahead = 4;       // dataflow form: levels of groups in flight (warps launched)
+int g_cta_xl = 1;           // single-CTA form, FP32: PF_GRID_XL entries per slot in registers when slots have more than PF_LARGE
 int g_lvl_stride = 1;       // level-counter grid form: ints between consecutive level counters
 int g_poll_ns = 0;          // and the back-off of its waiting polls (ns)
 
@@ -807,7 +810,17 @@ cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, i
     const int per = cs ? (s.n + cs - 1) / cs : 0;
     const int m = mode_of<T>(s);
     if (m == M_CTA) {
-        sweep_cta_k<T, OP, true, PF><<<1, CTA_NT, xbytes, st>>>(s, a);
+        // FP32: the single CTA holds the larger register set (the next
+        // level's entries prefetched, up to PF_GRID_XL per slot); in FP64 that
+        // set spills and is slower
+        bool xl = false;
+        if constexpr (sizeof(T) == 4) {
+            if (PF == PF_LARGE && s.maxK > PF_LARGE && g_cta_xl) {
+                sweep_cta_k<T, OP, true, PF_GRID_XL><<<1, CTA_NT, xbytes, st>>>(s, a);
+                xl = true;
+            }
+        }
+        if (!xl) sweep_cta_k<T, OP, true, PF><<<1, CTA_NT, xbytes, st>>>(s, a);
     } else if (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) {
         const bool ds = m == M_CLUSTER_DS;
         cudaLaunchConfig_t cfg = {};
@@ -920,6 +933,9 @@ template <class T, int OP>
 void init_op() {
     init_op_pf<T, OP, PF_SMALL>();
     init_op_pf<T, OP, PF_LARGE>();
+    if constexpr (sizeof(T) == 4)
+        cudaFuncSetAttribute(sweep_cta_k<T, OP, true, PF_GRID_XL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(g_smem_cap));
     if (sizeof(T) == 4) {
         constexpr int XL = sizeof(T) == 4 ? PF_GRID_XL : PF_LARGE;
         int per = 0;
@@ -1017,6 +1033,8 @@ int sweep_wave() { return g_wave; }
 void set_sweep_wave(int on) { g_wave = on ? 1 : 0; }
 int sweep_flow() { return g_flow; }
 void set_sweep_flow(int mode) { g_flow = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+int sweep_cta_xl() { return g_cta_xl; }
+void set_sweep_cta_xl(int on) { g_cta_xl = on ? 1 : 0; }
 int sweep_grid_stride() { return g_lvl_stride; }
 void set_sweep_grid_stride(int k) { g_lvl_stride = k < 1 ? 1 : k > LVL_STRIDE_MAX ? LVL_STRIDE_MAX : k; }
 int sweep_grid_poll_ns() { return g_poll_ns; }

@@ -226,3 +226,50 @@ def test_coarse_cyclic_interfaces_match_the_oracle(which):
         np.testing.assert_array_equal(summed, ob)
         assert fc.size <= cell.size and ps.sum() == fc.size
         size, cell, nbr, bou = ps, fc, nc, ob
+
+
+def _ldu_file(path, s):
+    with open(path, "wb") as fh:
+        np.array([s["diag"].size, s["l"].size], np.int32).tofile(fh)
+        np.ascontiguousarray(s["l"], np.int32).tofile(fh)
+        np.ascontiguousarray(s["u"], np.int32).tofile(fh)
+
+
+def test_sliced_rows_layout_on_the_host(tmp_path):
+    """build_sell (csrc/host.cpp), compiled on its own with a checker that reads
+    the rows back as the device does: every row's entries in the product's
+    order with their coefficient sources, valid padding columns, pattern
+    slices on a lexicographic cube, explicit ones on a renumbered mesh, none
+    with a row of more than 255 entries."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    csrc = os.path.join(repo, "openfoam-dev_gb300", "csrc")
+    cuda_inc = [d for d in ("/usr/local/cuda/include",) if os.path.isdir(d)]
+    exe = str(tmp_path / "sell_check")
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", csrc, "-I", INCLUDE_DIR] + [f"-I{d}" for d in cuda_inc] +
+                       [os.path.join(repo, "tests", "sell_layout_check.cpp"), os.path.join(csrc, "host.cpp"),
+                        "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0 and "cuda_runtime.h" in r.stderr:
+        pytest.skip("no CUDA headers")
+    assert r.returncode == 0, r.stderr[-3000:]
+    cube = cases.pcg_cube(12, seed=1)
+    perm = cases.gamg_cube(9, seed=5)
+    cases.renumber(perm, cases.random_order(5, perm["diag"].size))
+    n = 300
+    faces = sorted([(0, k) for k in range(1, n)] + [(k, k + 1) for k in range(1, n - 1)])
+    hub = {"l": np.array([a for a, _ in faces]), "u": np.array([b for _, b in faces]), "diag": np.zeros(n)}
+    out = {}
+    for name, s in (("cube", cube), ("perm", perm), ("hub", hub)):
+        path = str(tmp_path / f"{name}.bin")
+        _ldu_file(path, s)
+        p = subprocess.run([exe, path], capture_output=True, text=True)
+        assert p.returncode == 0, (name, p.stdout, p.stderr)
+        out[name] = p.stdout
+    assert "patterns=1 slices=54 patternSlices=54" in out["cube"]
+    assert "patterns=0 slices=54 patternSlices=0" in out["cube"]
+    assert "ok" in out["perm"]
+    assert out["hub"].count("not built") == 2

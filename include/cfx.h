@@ -358,7 +358,15 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
        /* single-CTA form in FP32: hold 32 (1, default) or 16 (0) entries per
         * slot in registers when a schedule's slots have more than 16 (256^3
         * mixed GAMG 1.77 -> 1.71 s; in FP64 the larger set spills) */
-       CFX_TUNE_CTA_XL = 13 };
+       CFX_TUNE_CTA_XL = 13,
+       /* Gauss-Seidel smoothing order: 0 the reference's cell order
+        * everywhere; 1 (default) a multicolour order (a greedy colouring of
+        * each level's cells, smaller colours first: about sweeps x colours
+        * dependent steps instead of the cell order's thousands) in the FP32
+        * inner cycles of mixed-precision solves, whose FP64 refinement still
+        * reaches the FP64 tolerance; the FP64 solves keep the reference's
+        * order bit for bit; 2 the multicolour order everywhere (tests) */
+       CFX_TUNE_COLORED_GS = 14 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -623,6 +623,30 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     return it->second;
 }
 
+// The multicolour Gauss-Seidel schedule of level lv (S combined sweeps),
+// built on first use; kept under key COLORED_KEY + S.
+constexpr int COLORED_KEY = 1 << 16;
+const DevSched& sched_colored(cfx_mesh* mesh, int lv, int S) {
+    if ((int)mesh->sched.size() < (int)mesh->host.size()) mesh->sched.resize(mesh->host.size());
+    cfx_mesh::Scheds& sc = mesh->sched[lv];
+    auto it = sc.gs.find(COLORED_KEY + S);
+    if (it == sc.gs.end()) {
+        std::vector<int> color;
+        greedy_colors(mesh->host[lv], color);
+        HostSched h;
+        build_sched(mesh->host[lv], SCHED_GS, S, h, false, &color);
+        it = sc.gs.emplace(COLORED_KEY + S, upload_sched(mesh->schedArena, mesh->ctx->stream, h)).first;
+    }
+    return it->second;
+}
+
+// Whether precision T's Gauss-Seidel smoothing takes the multicolour order
+// (colored_gs(): 1 for the FP32 inner cycles, 2 for every smoothing).
+template <class T>
+bool gs_colored() {
+    return colored_gs() == 2 || (colored_gs() == 1 && sizeof(T) == 4);
+}
+
 template <class T>
 std::vector<LevelPack<T>>& packs_of(cfx_matrix* mat);
 template <>
@@ -804,11 +828,12 @@ void setup_preconditioner(cfx_matrix* mat, int lv, int kind) {
     ensure_chunk_partials(ctx, RED_MAXB);
 }
 
-// Gauss-Seidel coefficients for S fused sweeps on level lv.
+// Gauss-Seidel coefficients for S fused sweeps on level lv (colored: the
+// multicolour schedule's).
 template <class T>
-void prepare_gs(cfx_matrix* mat, int lv, int S) {
-    const DevSched& g = sched(mat->mesh, lv, SCHED_GS, S);
-    Packed<T>& p = packed<T>(mat, lv, OP_GS, S, g);
+void prepare_gs(cfx_matrix* mat, int lv, int S, bool colored = false) {
+    const DevSched& g = colored ? sched_colored(mat->mesh, lv, S) : sched(mat->mesh, lv, SCHED_GS, S);
+    Packed<T>& p = packed<T>(mat, lv, OP_GS, colored ? COLORED_KEY + S : S, g);
     if (!p.valid) pack_sweep<T>(mat->mesh->ctx->stream, g, OP_GS, coeffs<T>(mat, lv), p);
 }
 
@@ -869,7 +894,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -981,12 +1006,14 @@ void smooth(cfx_ctx* ctx, cfx_matrix* mat, int lv, int kind, T* psi, const T* b,
         return;
     }
     if (kind == CFX_SMOOTH_GS) {
-        // GaussSeidelSmoother.C:125-177
+        // GaussSeidelSmoother.C:125-177; the FP32 inner cycles of the
+        // mixed-precision solves (by default) in the multicolour order
+        const bool colored = gs_colored<T>();
         for (int left = nSweeps; left > 0;) {
             const int S = std::min(left, MAX_FUSED_SWEEPS);
-            const DevSched& g = sched(mat->mesh, lv, SCHED_GS, S);
-            if (run_sweep<T>(s, g, OP_GS, packed<T>(mat, lv, OP_GS, S, g), b, psi, nullptr, nullptr, nullptr,
-                             ctx->d_status) != CFX_OK)
+            const DevSched& g = colored ? sched_colored(mat->mesh, lv, S) : sched(mat->mesh, lv, SCHED_GS, S);
+            Packed<T>& p = packed<T>(mat, lv, OP_GS, colored ? COLORED_KEY + S : S, g);
+            if (run_sweep<T>(s, g, OP_GS, p, b, psi, nullptr, nullptr, nullptr, ctx->d_status) != CFX_OK)
                 throw CudaError(last_error());
             left -= S;
         }
@@ -1027,7 +1054,7 @@ void prepare_smooth(cfx_matrix* mat, int lv, int kind, int nSweeps, Work<T>& LW)
     if (kind == CFX_SMOOTH_GS) {
         for (int left = nSweeps; left > 0;) {
             const int S = std::min(left, MAX_FUSED_SWEEPS);
-            prepare_gs<T>(mat, lv, S);
+            prepare_gs<T>(mat, lv, S, gs_colored<T>());
             left -= S;
         }
     } else {
@@ -1367,7 +1394,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2396,6 +2423,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value < 0 || value > 1) return CFX_ERR_ARG;
             set_sweep_cta_xl(value);
             return CFX_OK;
+        case CFX_TUNE_COLORED_GS:
+            if (value < 0 || value > 2) return CFX_ERR_ARG;
+            set_colored_gs(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2417,6 +2448,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_GRID_POLL_NS: *value = sweep_grid_poll_ns(); return CFX_OK;
         case CFX_TUNE_CHUNK_GROUPS: *value = sched_chunk_groups(); return CFX_OK;
         case CFX_TUNE_CTA_XL: *value = sweep_cta_xl(); return CFX_OK;
+        case CFX_TUNE_COLORED_GS: *value = colored_gs(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

@@ -288,13 +288,77 @@ int g_chunk_groups = 2;
 int sched_chunk_groups() { return g_chunk_groups; }
 void set_sched_chunk_groups(int g) { g_chunk_groups = g < 1 ? 1 : g > SCHED_CHUNK_GROUPS ? SCHED_CHUNK_GROUPS : g; }
 
-void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps) {
+namespace {
+int g_colored_gs = 1;
+
+// Colour of each neighbour entry relative to the cell: the multicolour
+// schedule's levels.  Cells are taken colour by colour (ascending cells in a
+// colour); (c, s) waits for its smaller-coloured neighbours in sweep s, its
+// larger-coloured ones in sweep s-1, and itself in sweep s-1.
+void colored_levels(const HostLevel& h, const std::vector<int>& color, int S, std::vector<int>& lev) {
+    const int n = h.n;
+    int nc = 0;
+    for (int c = 0; c < n; ++c) nc = std::max(nc, color[c] + 1);
+    std::vector<int> byColor(n), cstart(nc + 1, 0);
+    for (int c = 0; c < n; ++c) cstart[color[c] + 1]++;
+    for (int k = 0; k < nc; ++k) cstart[k + 1] += cstart[k];
+    {
+        std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+        for (int c = 0; c < n; ++c) byColor[fill[color[c]]++] = c;
+    }
+    lev.assign(size_t(n) * S, 0);
+    std::vector<int> nbs, srcs;
+    for (int s = 0; s < S; ++s) {
+        int* L = lev.data() + size_t(s) * n;
+        const int* P = s > 0 ? lev.data() + size_t(s - 1) * n : nullptr;
+        for (int c : byColor) {
+            int v = P ? P[c] + 1 : 0;
+            sched_entries(h, SCHED_GS, c, nbs, srcs);
+            for (int nb : nbs) {
+                if (color[nb] < color[c]) v = std::max(v, L[nb] + 1);
+                else if (P) v = std::max(v, P[nb] + 1);
+            }
+            L[c] = v;
+        }
+    }
+}
+}  // namespace
+
+int colored_gs() { return g_colored_gs; }
+void set_colored_gs(int v) { g_colored_gs = v < 0 ? 0 : v > 2 ? 2 : v; }
+
+int greedy_colors(const HostLevel& h, std::vector<int>& color) {
+    const int n = h.n;
+    color.assign(n, -1);
+    std::vector<int> seen;  // seen[k] == c: colour k taken by a neighbour of c
+    int nc = 0;
+    for (int c = 0; c < n; ++c) {
+        for (int q = h.losortStart[c]; q < h.losortStart[c + 1]; ++q) {
+            const int k = color[h.losortL[q]];
+            if (k >= int(seen.size())) seen.resize(k + 1, -1);
+            seen[k] = c;
+        }
+        int k = 0;
+        while (k < int(seen.size()) && seen[k] == c) ++k;
+        color[c] = k;
+        nc = std::max(nc, k + 1);
+    }
+    return nc;
+}
+
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps,
+                 const std::vector<int>* color) {
     const int n = h.n;
     const int chunkGroups = g_chunk_groups;
     const int S = kind == SCHED_GS ? std::max(1, nSweeps) : 1;
+    const bool colored = color != nullptr && kind == SCHED_GS;
+    if (colored) withDeps = false;
     // level of every (cell, sweep)
     std::vector<int> lev;
-    sched_levels(h, kind, S, lev);
+    if (colored)
+        colored_levels(h, *color, S, lev);
+    else
+        sched_levels(h, kind, S, lev);
     int nl = 0;
     for (int v : lev) nl = std::max(nl, v + 1);
     if (n == 0) nl = 0;
@@ -326,8 +390,25 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
     o.slotLower.clear();
     o.maxK = 0;
     o.maxLevelBytes8 = 0;
+    std::vector<int> cnb, csrc;
+    int nLowerOf = 0;  // the colored form's lower-entry count of the last cell
     auto entries_of = [&](int c, std::vector<int>& nbs, std::vector<int>& srcs) {
         sched_entries(h, kind, c, nbs, srcs);
+        if (!colored) return;
+        // smaller-coloured neighbours first, then the larger-coloured ones,
+        // each group in the reference's entry order
+        cnb.clear();
+        csrc.clear();
+        for (int pass = 0; pass < 2; ++pass)
+            for (size_t k = 0; k < nbs.size(); ++k)
+                if (((*color)[nbs[k]] < (*color)[c]) == (pass == 0)) {
+                    cnb.push_back(nbs[k]);
+                    csrc.push_back(srcs[k]);
+                }
+        nLowerOf = 0;
+        for (int nb : nbs) nLowerOf += (*color)[nb] < (*color)[c];
+        nbs.swap(cnb);
+        srcs.swap(csrc);
     };
     std::vector<int> nbs, srcs;
     std::vector<std::vector<int>> gnb(32), gsrc(32);
@@ -346,7 +427,8 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
                     o.cell.push_back(c);
                     o.cnt.push_back(int(gnb[j].size()));
                     o.slotSweep.push_back(order[i] / n);
-                    o.slotLower.push_back(kind == SCHED_GS || kind == SCHED_GSB
+                    o.slotLower.push_back(colored ? nLowerOf
+                                          : kind == SCHED_GS || kind == SCHED_GSB
                                               ? h.losortStart[c + 1] - h.losortStart[c] : 0);
                     K = std::max(K, int(gnb[j].size()));
                 } else {

@@ -327,7 +327,22 @@ struct Packed {
 };
 
 // withDeps: also the group dependency lists of the wavefront form
-void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps);
+// color (not null, SCHED_GS only): a multicolour Gauss-Seidel in place of
+// the reference's cell order: a cell's "lower" neighbours are those of a
+// smaller colour (this sweep's values), the others its "upper" ones (the
+// previous sweep's), each group in the reference's entry order; the DAG has
+// about nSweeps x colours levels
+void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps,
+                 const std::vector<int>* color = nullptr);
+// A greedy colouring of a level's cells (ascending cells, smallest colour no
+// neighbour has); returns the number of colours.
+int greedy_colors(const HostLevel& h, std::vector<int>& color);
+// Gauss-Seidel smoothing order: 0 the reference's cell order everywhere; 1
+// (default) the multicolour order for the FP32 inner cycles of the
+// mixed-precision solves; 2 the multicolour order for every Gauss-Seidel
+// smoothing (tests)
+int colored_gs();
+void set_colored_gs(int v);
 
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {

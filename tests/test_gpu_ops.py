@@ -240,3 +240,59 @@ def test_bad_addressing_rejected():
     with pytest.raises(ldu.CfxError) as e:
         ldu.LduMesh(ctx, 4, [0, 1], [1, 4])  # out of range
     assert e.value.status == -2
+
+
+def _colored_gs(s, x, b, sweeps):
+    """The multicolour Gauss-Seidel the FP32 inner cycles use, in FP64 on the
+    host: greedy colours (ascending cells, smallest colour no smaller-index
+    neighbour has); per sweep the colours in ascending order, each cell from
+    b minus its smaller-coloured neighbours' new values, then its
+    larger-coloured neighbours' old values (each group in the reference's
+    entry order: losort faces, then owned faces), divided by the diagonal."""
+    n = s["diag"].size
+    l, u = np.asarray(s["l"]), np.asarray(s["u"])
+    upper = np.asarray(s["upper"], np.float64)
+    lower = upper if s.get("lower") is None else np.asarray(s["lower"], np.float64)
+    entries = [[] for _ in range(n)]
+    for f in np.argsort(u, kind="stable"):  # losort: by neighbour cell, faces in order
+        entries[u[f]].append((int(l[f]), lower[f]))
+    for f in range(l.size):
+        entries[l[f]].append((int(u[f]), upper[f]))
+    color = np.full(n, -1)
+    for c in range(n):
+        taken = {color[nb] for nb, _ in entries[c] if nb < c}
+        k = 0
+        while k in taken:
+            k += 1
+        color[c] = k
+    x = np.array(x, np.float64)
+    order = np.argsort(color, kind="stable")
+    for _ in range(sweeps):
+        for c in order:
+            acc = np.float64(b[c])
+            for first in (True, False):
+                for nb, cf in entries[c]:
+                    if (color[nb] < color[c]) == first:
+                        acc = acc - cf * x[nb]
+            x[c] = acc / s["diag"][c]
+    return x
+
+
+@pytest.mark.parametrize("name", ["cube6", "cd6", "perm_lap", "box"])
+def test_multicolour_gauss_seidel_exact(name):
+    """The multicolour Gauss-Seidel schedule (CFX_TUNE_COLORED_GS 2 runs it in
+    FP64 too) equals the host restatement bit for bit, fused sweeps included."""
+    s = SYSTEMS[name]()
+    old = ldu.tune_get(ldu.TUNE_COLORED_GS)
+    ldu.tune_set(ldu.TUNE_COLORED_GS, 2)
+    try:
+        _, A = _fresh(s)
+        n = s["diag"].size
+        x = cases.uniform(8, n)
+        b = s["source"]
+        for sweeps in (1, 3):
+            psi = dev(x)
+            A.smooth("GaussSeidel", psi, dev(b), sweeps)
+            np.testing.assert_array_equal(host(psi), _colored_gs(s, x, b, sweeps))
+    finally:
+        ldu.tune_set(ldu.TUNE_COLORED_GS, old)

@@ -366,7 +366,14 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
         * inner cycles of mixed-precision solves, whose FP64 refinement still
         * reaches the FP64 tolerance; the FP64 solves keep the reference's
         * order bit for bit; 2 the multicolour order everywhere (tests) */
-       CFX_TUNE_COLORED_GS = 14 };
+       CFX_TUNE_COLORED_GS = 14,
+       /* DIC / DILU order (preconditioners and smoothers), the same three
+        * values: 1 (default) the incomplete factorisation and its sweeps in
+        * the same multicolour order (a cell's smaller-coloured neighbours
+        * are its forward entries, the larger-coloured its backward ones) in
+        * the FP32 inner solves; the FP64 solves and the coarsest level's
+        * one-CTA solve keep the reference's order */
+       CFX_TUNE_COLORED_PRE = 15 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

@@ -50,6 +50,8 @@ struct cfx_mesh {
     struct Scheds {
         DevSched fwd, bwd;
         bool hasFwd = false, hasBwd = false;
+        DevSched fwdC, bwdC;  // the multicolour forward / backward schedules
+        bool hasFwdC = false, hasBwdC = false;
         std::map<int, DevSched> gs;
     };
     std::vector<Scheds> sched;
@@ -74,6 +76,7 @@ template <class T>
 struct LevelPack {
     Packed<T> rd, fwd, bwd;
     Packed<T> fwdT, bwdT;  // DILU preconditionT: the packs of the transpose
+    Packed<T> rdC, fwdC, bwdC, fwdTC, bwdTC;  // the same on the multicolour schedules
     std::map<int, Packed<T>> gs;
 };
 
@@ -623,6 +626,36 @@ const DevSched& sched(cfx_mesh* mesh, int lv, int kind, int S = 1) {
     return it->second;
 }
 
+// The multicolour forward or backward schedule of level lv (kind SCHED_FWD
+// or SCHED_BWD), built on first use.
+const DevSched& sched_pre_colored(cfx_mesh* mesh, int lv, int kind) {
+    if ((int)mesh->sched.size() < (int)mesh->host.size()) mesh->sched.resize(mesh->host.size());
+    cfx_mesh::Scheds& sc = mesh->sched[lv];
+    const bool fwd = kind == SCHED_FWD;
+    if (!(fwd ? sc.hasFwdC : sc.hasBwdC)) {
+        std::vector<int> color;
+        greedy_colors(mesh->host[lv], color);
+        HostSched h;
+        build_sched(mesh->host[lv], kind, 1, h, false, &color);
+        (fwd ? sc.fwdC : sc.bwdC) = upload_sched(mesh->schedArena, mesh->ctx->stream, h);
+        (fwd ? sc.hasFwdC : sc.hasBwdC) = true;
+    }
+    return fwd ? sc.fwdC : sc.bwdC;
+}
+
+// Whether precision T's DIC / DILU take the multicolour order
+// (colored_pre(): 1 for the FP32 inner solves, 2 for every solve).
+template <class T>
+bool pre_colored() {
+    return colored_pre() == 2 || (colored_pre() == 1 && sizeof(T) == 4);
+}
+
+// The forward / backward schedule DIC and DILU of precision T run on.
+template <class T>
+const DevSched& sched_pre(cfx_mesh* mesh, int lv, int kind, bool col = pre_colored<T>()) {
+    return col ? sched_pre_colored(mesh, lv, kind) : sched(mesh, lv, kind);
+}
+
 // The multicolour Gauss-Seidel schedule of level lv (S combined sweeps),
 // built on first use; kept under key COLORED_KEY + S.
 constexpr int COLORED_KEY = 1 << 16;
@@ -659,11 +692,16 @@ std::vector<LevelPack<float>>& packs_of<float>(cfx_matrix* mat) {
 }
 
 template <class T>
-Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd) {
+Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd, bool colPre = pre_colored<T>()) {
     auto& v = packs_of<T>(mat);
     if ((int)v.size() <= lv) v.resize(lv + 1);
     LevelPack<T>& lp = v[lv];
-    Packed<T>* p = op == OP_RD ? &lp.rd : op == OP_FWD ? &lp.fwd : op == OP_BWD ? &lp.bwd : &lp.gs[S];
+    // the forward, backward and pivot packs of the multicolour schedules
+    // are kept apart (their entry counts differ)
+    const bool col = op != OP_GS && colPre;
+    Packed<T>* p = op == OP_RD ? (col ? &lp.rdC : &lp.rd)
+                 : op == OP_FWD ? (col ? &lp.fwdC : &lp.fwd)
+                 : op == OP_BWD ? (col ? &lp.bwdC : &lp.bwd) : &lp.gs[S];
     if (!p->coef) {
         p->coef = mat->arena.get<T>(sd.nEntries);
         p->scalar = mat->arena.get<T>(sd.nSlots);
@@ -680,7 +718,8 @@ template <class T>
 Packed<T>& packedT(cfx_matrix* mat, int lv, int op, const DevSched& sd) {
     auto& v = packs_of<T>(mat);
     if ((int)v.size() <= lv) v.resize(lv + 1);
-    Packed<T>* p = op == OP_FWD ? &v[lv].fwdT : &v[lv].bwdT;
+    const bool col = pre_colored<T>();
+    Packed<T>* p = op == OP_FWD ? (col ? &v[lv].fwdTC : &v[lv].fwdT) : (col ? &v[lv].bwdTC : &v[lv].bwdT);
     if (!p->coef) {
         p->coef = mat->arena.get<T>(sd.nEntries);
         p->scalar = mat->arena.get<T>(sd.nSlots);
@@ -694,10 +733,12 @@ Packed<T>& packedT(cfx_matrix* mat, int lv, int op, const DevSched& sd) {
 void invalidate_packs(cfx_matrix* mat) {
     for (auto& l : mat->p64) {
         l.rd.valid = l.fwd.valid = l.bwd.valid = l.fwdT.valid = l.bwdT.valid = false;
+        l.rdC.valid = l.fwdC.valid = l.bwdC.valid = l.fwdTC.valid = l.bwdTC.valid = false;
         for (auto& kv : l.gs) kv.second.valid = false;
     }
     for (auto& l : mat->p32) {
         l.rd.valid = l.fwd.valid = l.bwd.valid = l.fwdT.valid = l.bwdT.valid = false;
+        l.rdC.valid = l.fwdC.valid = l.bwdC.valid = l.fwdTC.valid = l.bwdTC.valid = false;
         for (auto& kv : l.gs) kv.second.valid = false;
     }
 }
@@ -712,26 +753,28 @@ void ensure_chunk_partials(cfx_ctx* ctx, size_t chunks) {
 
 // rD of DIC / DILU (DICPreconditioner.C:57-84, DILUPreconditioner.C:57-85):
 // pivot sweep in level order, then the reciprocal; then the forward and
-// backward coefficients (rD_c*lower, rD_c*upper) are packed.
+// backward coefficients (rD_c*lower, rD_c*upper) are packed.  col: in the
+// multicolour order (the coarsest level's one-CTA solve sweeps in the
+// reference's order and takes the reference's pivots).
 template <class T>
-void compute_rD(cfx_matrix* mat, int lv) {
+void compute_rD(cfx_matrix* mat, int lv, bool col = pre_colored<T>()) {
     cfx_ctx* ctx = mat->mesh->ctx;
     cudaStream_t s = ctx->stream;
     const LevelMesh& m = mat->mesh->dev[lv];
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
-    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
-    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD, col);
+    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD, col);
     // dot partials of the fused backward sweep: one per chunk or per
     // dataflow CTA, whichever form runs
     ensure_chunk_partials(ctx, std::max({size_t(f.nChunks), size_t(b.nChunks), size_t(sweep_partials<T>(b)),
                                          size_t(sweep_partials<T>(f))}));
-    Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f);
+    Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f, col);
     pack_sweep<T>(s, f, OP_RD, c, prd);
     if (run_sweep<T>(s, f, OP_RD, prd, nullptr, c.rD, nullptr, nullptr, nullptr, ctx->d_status) != CFX_OK)
         throw CudaError(last_error());
     Ops<T>::reciprocal(s, m.n, c.rD);
-    pack_sweep<T>(s, f, OP_FWD, c, packed<T>(mat, lv, OP_FWD, 1, f));
-    pack_sweep<T>(s, b, OP_BWD, c, packed<T>(mat, lv, OP_BWD, 1, b));
+    pack_sweep<T>(s, f, OP_FWD, c, packed<T>(mat, lv, OP_FWD, 1, f, col));
+    pack_sweep<T>(s, b, OP_BWD, c, packed<T>(mat, lv, OP_BWD, 1, b, col));
 }
 
 template <class T>
@@ -756,8 +799,8 @@ int precondition(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int*
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     if (kind == CFX_PRE_GAMG) return pc_gamg_apply<T>(mat, r, w, done, dot);
     if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
-        const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
-        const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+        const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
+        const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
         if (run_sweep<T>(s, f, OP_FWD, packed<T>(mat, lv, OP_FWD, 1, f), r, w, nullptr, nullptr, done,
                          ctx->d_status) != CFX_OK)
             throw CudaError(last_error());
@@ -786,8 +829,8 @@ void preconditionT(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const in
     }
     cfx_ctx* ctx = mat->mesh->ctx;
     cudaStream_t s = ctx->stream;
-    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
-    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
+    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
     if (run_sweep<T>(s, f, OP_FWD, packedT<T>(mat, lv, OP_FWD, f), r, w, nullptr, nullptr, done, ctx->d_status) !=
         CFX_OK)
         throw CudaError(last_error());
@@ -809,8 +852,8 @@ void setup_preconditioner_t(cfx_matrix* mat, int lv, int kind) {
     t.lowerPerm = c.upperPerm;
     t.upperPerm = c.lowerPerm;
     t.sellCoef = nullptr;
-    const DevSched& f = sched(mat->mesh, lv, SCHED_FWD);
-    const DevSched& b = sched(mat->mesh, lv, SCHED_BWD);
+    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
+    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
     pack_sweep<T>(s, f, OP_FWD, t, packedT<T>(mat, lv, OP_FWD, f));
     pack_sweep<T>(s, b, OP_BWD, t, packedT<T>(mat, lv, OP_BWD, b));
 }
@@ -894,7 +937,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1242,7 +1285,7 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
         }
         return;
     }
-    compute_rD<T>(mat, lc);  // coarsest PCG+DIC / PBiCGStab+DILU
+    compute_rD<T>(mat, lc, false);  // coarsest PCG+DIC / PBiCGStab+DILU
     BlockSys<T> h{};
     h.n = m.n;
     h.nf = m.nf;
@@ -1394,7 +1437,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2427,6 +2470,10 @@ cfx_status cfx_tune_set(int key, int value) {
             if (value < 0 || value > 2) return CFX_ERR_ARG;
             set_colored_gs(value);
             return CFX_OK;
+        case CFX_TUNE_COLORED_PRE:
+            if (value < 0 || value > 2) return CFX_ERR_ARG;
+            set_colored_pre(value);
+            return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }
@@ -2449,6 +2496,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_CHUNK_GROUPS: *value = sched_chunk_groups(); return CFX_OK;
         case CFX_TUNE_CTA_XL: *value = sweep_cta_xl(); return CFX_OK;
         case CFX_TUNE_COLORED_GS: *value = colored_gs(); return CFX_OK;
+        case CFX_TUNE_COLORED_PRE: *value = colored_pre(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

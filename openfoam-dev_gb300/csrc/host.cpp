@@ -290,12 +290,15 @@ void set_sched_chunk_groups(int g) { g_chunk_groups = g < 1 ? 1 : g > SCHED_CHUN
 
 namespace {
 int g_colored_gs = 1;
+int g_colored_pre = 1;
 
 // Colour of each neighbour entry relative to the cell: the multicolour
 // schedule's levels.  Cells are taken colour by colour (ascending cells in a
 // colour); (c, s) waits for its smaller-coloured neighbours in sweep s, its
 // larger-coloured ones in sweep s-1, and itself in sweep s-1.
-void colored_levels(const HostLevel& h, const std::vector<int>& color, int S, std::vector<int>& lev) {
+// The triangular sweeps (kind SCHED_FWD / SCHED_BWD) wait for every
+// neighbour of a smaller (forward) or larger (backward) colour.
+void colored_levels(const HostLevel& h, int kind, const std::vector<int>& color, int S, std::vector<int>& lev) {
     const int n = h.n;
     int nc = 0;
     for (int c = 0; c < n; ++c) nc = std::max(nc, color[c] + 1);
@@ -308,6 +311,18 @@ void colored_levels(const HostLevel& h, const std::vector<int>& color, int S, st
     }
     lev.assign(size_t(n) * S, 0);
     std::vector<int> nbs, srcs;
+    if (kind == SCHED_FWD || kind == SCHED_BWD) {
+        const bool fwd = kind == SCHED_FWD;
+        for (int i = 0; i < n; ++i) {
+            const int c = byColor[fwd ? i : n - 1 - i];
+            int v = 0;
+            sched_entries(h, SCHED_GS, c, nbs, srcs);
+            for (int nb : nbs)
+                if (fwd ? color[nb] < color[c] : color[nb] > color[c]) v = std::max(v, lev[nb] + 1);
+            lev[c] = v;
+        }
+        return;
+    }
     for (int s = 0; s < S; ++s) {
         int* L = lev.data() + size_t(s) * n;
         const int* P = s > 0 ? lev.data() + size_t(s - 1) * n : nullptr;
@@ -326,6 +341,8 @@ void colored_levels(const HostLevel& h, const std::vector<int>& color, int S, st
 
 int colored_gs() { return g_colored_gs; }
 void set_colored_gs(int v) { g_colored_gs = v < 0 ? 0 : v > 2 ? 2 : v; }
+int colored_pre() { return g_colored_pre; }
+void set_colored_pre(int v) { g_colored_pre = v < 0 ? 0 : v > 2 ? 2 : v; }
 
 int greedy_colors(const HostLevel& h, std::vector<int>& color) {
     const int n = h.n;
@@ -351,12 +368,12 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
     const int n = h.n;
     const int chunkGroups = g_chunk_groups;
     const int S = kind == SCHED_GS ? std::max(1, nSweeps) : 1;
-    const bool colored = color != nullptr && kind == SCHED_GS;
+    const bool colored = color != nullptr && (kind == SCHED_GS || kind == SCHED_FWD || kind == SCHED_BWD);
     if (colored) withDeps = false;
     // level of every (cell, sweep)
     std::vector<int> lev;
     if (colored)
-        colored_levels(h, *color, S, lev);
+        colored_levels(h, kind, *color, S, lev);
     else
         sched_levels(h, kind, S, lev);
     int nl = 0;
@@ -393,6 +410,23 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
     std::vector<int> cnb, csrc;
     int nLowerOf = 0;  // the colored form's lower-entry count of the last cell
     auto entries_of = [&](int c, std::vector<int>& nbs, std::vector<int>& srcs) {
+        if (colored && kind != SCHED_GS) {
+            // forward: the smaller-coloured neighbours in the Gauss-Seidel
+            // entry order (losort slots, then owned faces); backward: the
+            // larger-coloured ones in the reverse of that order
+            sched_entries(h, SCHED_GS, c, cnb, csrc);
+            nbs.clear();
+            srcs.clear();
+            const int m = int(cnb.size());
+            for (int i = 0; i < m; ++i) {
+                const int k = kind == SCHED_FWD ? i : m - 1 - i;
+                if (kind == SCHED_FWD ? (*color)[cnb[k]] < (*color)[c] : (*color)[cnb[k]] > (*color)[c]) {
+                    nbs.push_back(cnb[k]);
+                    srcs.push_back(csrc[k]);
+                }
+            }
+            return;
+        }
         sched_entries(h, kind, c, nbs, srcs);
         if (!colored) return;
         // smaller-coloured neighbours first, then the larger-coloured ones,
@@ -427,7 +461,7 @@ void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool w
                     o.cell.push_back(c);
                     o.cnt.push_back(int(gnb[j].size()));
                     o.slotSweep.push_back(order[i] / n);
-                    o.slotLower.push_back(colored ? nLowerOf
+                    o.slotLower.push_back(colored && kind == SCHED_GS ? nLowerOf
                                           : kind == SCHED_GS || kind == SCHED_GSB
                                               ? h.losortStart[c + 1] - h.losortStart[c] : 0);
                     K = std::max(K, int(gnb[j].size()));

@@ -327,11 +327,14 @@ struct Packed {
 };
 
 // withDeps: also the group dependency lists of the wavefront form
-// color (not null, SCHED_GS only): a multicolour Gauss-Seidel in place of
-// the reference's cell order: a cell's "lower" neighbours are those of a
-// smaller colour (this sweep's values), the others its "upper" ones (the
-// previous sweep's), each group in the reference's entry order; the DAG has
-// about nSweeps x colours levels
+// color (not null; SCHED_GS, SCHED_FWD or SCHED_BWD): a multicolour order in
+// place of the reference's cell order.  Gauss-Seidel: a cell's "lower"
+// neighbours are those of a smaller colour (this sweep's values), the others
+// its "upper" ones (the previous sweep's), each group in the reference's
+// entry order; the DAG has about nSweeps x colours levels.  Forward: the
+// smaller-coloured neighbours (losort slots, then owned faces); backward: the
+// larger-coloured ones in the reverse of that order; the coefficient of each
+// entry is the matrix entry of the cell's row (src as for Gauss-Seidel)
 void build_sched(const HostLevel& h, int kind, int nSweeps, HostSched& o, bool withDeps,
                  const std::vector<int>* color = nullptr);
 // A greedy colouring of a level's cells (ascending cells, smallest colour no
@@ -343,6 +346,10 @@ int greedy_colors(const HostLevel& h, std::vector<int>& color);
 // smoothing (tests)
 int colored_gs();
 void set_colored_gs(int v);
+// DIC / DILU (preconditioners and smoothers) order, the same three values:
+// the multicolour incomplete factorisation of the same sparsity
+int colored_pre();
+void set_colored_pre(int v);
 
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {

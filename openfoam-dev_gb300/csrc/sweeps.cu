@@ -728,11 +728,16 @@ __global__ void gather_slots_k(int nSlots, const int* __restrict__ cell, const T
     }
 }
 
-// Coefficients of a schedule for one operation (per matrix update).
+// Coefficients of a schedule for one operation (per matrix update).  An
+// entry's matrix coefficient A_cj is lower[losort slot] (lp) or, with
+// SRC_UPPER, upper[face]: the reference's forward entries are all losort
+// slots and its backward ones all owned faces; the multicolour schedules mix
+// both.  The pivot products A_cj*A_jc are up*lp per losort slot (up: upper in
+// losort order) and upper*lower per owned face (lo: lower by face).
 template <class T>
 __global__ void pack_k(DevSched s, int op, const T* __restrict__ lp, const T* __restrict__ up,
-                       const T* __restrict__ upper, const T* __restrict__ diag, const T* __restrict__ rD,
-                       T* __restrict__ coef, T* __restrict__ scalar) {
+                       const T* __restrict__ upper, const T* __restrict__ lo, const T* __restrict__ diag,
+                       const T* __restrict__ rD, T* __restrict__ coef, T* __restrict__ scalar) {
     const int nThreads = s.nGroups * 32;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nThreads; t += gridDim.x * blockDim.x) {
         const int g = t >> 5, lane = t & 31;
@@ -747,10 +752,11 @@ __global__ void pack_k(DevSched s, int op, const T* __restrict__ lp, const T* __
             if (k < n) {
                 const int src = s.src[e];
                 const int i = src & (SRC_UPPER - 1);
-                if (op == OP_FWD) v = rD[c] * lp[i];
-                else if (op == OP_BWD) v = rD[c] * upper[i];
-                else if (op == OP_GS) v = (src & SRC_UPPER) ? upper[i] : lp[i];
-                else v = up[i] * lp[i];  // OP_RD: upper*upper (DIC) / upper*lower (DILU)
+                const bool own = (src & SRC_UPPER) != 0;
+                const T a = own ? upper[i] : lp[i];
+                if (op == OP_FWD || op == OP_BWD) v = rD[c] * a;
+                else if (op == OP_GS) v = a;
+                else v = own ? upper[i] * lo[i] : up[i] * lp[i];  // OP_RD: upper*upper (DIC) / upper*lower (DILU)
             }
             coef[e] = v;
         }
@@ -1188,10 +1194,11 @@ void pack_sweep(cudaStream_t st, const DevSched& s, int op, const LevelCoeffs<T>
         return;
     }
     const T* up = c.sym ? c.lowerPerm : c.upperPerm;
+    const T* lo = c.sym ? c.upper : c.lower;
     const int threads = 256;
     int blocks = (s.nGroups * 32 + threads - 1) / threads;
     if (blocks > 4096) blocks = 4096;
-    pack_k<T><<<blocks, threads, 0, st>>>(s, op, c.lowerPerm, up, c.upper, c.diag, c.rD, p.coef, p.scalar);
+    pack_k<T><<<blocks, threads, 0, st>>>(s, op, c.lowerPerm, up, c.upper, lo, c.diag, c.rD, p.coef, p.scalar);
     count_launch();
     p.valid = true;
 }

@@ -528,6 +528,7 @@ TUNE_FLOW_AHEAD = 8
 TUNE_AMUL_SELL = 9
 TUNE_GRID_STRIDE, TUNE_GRID_POLL_NS, TUNE_CHUNK_GROUPS, TUNE_CTA_XL = 10, 11, 12, 13
 TUNE_COLORED_GS = 14
+TUNE_COLORED_PRE = 15
 
 
 def tune_set(key, value):

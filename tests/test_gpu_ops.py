@@ -278,6 +278,101 @@ def _colored_gs(s, x, b, sweeps):
     return x
 
 
+def _colored_ilu(s, b, transpose=False):
+    """The multicolour DIC / DILU the FP32 inner solves use, in FP64 on the
+    host: the greedy colours of _colored_gs; a cell's forward entries are its
+    smaller-coloured neighbours in the Gauss-Seidel entry order (losort faces,
+    then owned faces), its backward entries the larger-coloured ones in the
+    reverse of that order; each entry's coefficient is the matrix entry of
+    the cell's row (of the transpose's row for preconditionT).  Pivots
+    d_c = diag_c - sum upper*lower / d_j over the forward entries, rD = 1/d;
+    forward w_c = rD_c r_c - sum (rD_c a_cj) w_j, backward
+    w_c -= sum (rD_c a_cj) w_j.  Returns (rD, w)."""
+    n = s["diag"].size
+    l, u = np.asarray(s["l"]), np.asarray(s["u"])
+    upper = np.asarray(s["upper"], np.float64)
+    lower = upper if s.get("lower") is None else np.asarray(s["lower"], np.float64)
+    if transpose:
+        upper, lower = lower, upper
+    entries = [[] for _ in range(n)]  # (neighbour, a_cj, upper*lower)
+    for f in np.argsort(u, kind="stable"):
+        entries[u[f]].append((int(l[f]), lower[f], upper[f] * lower[f]))
+    for f in range(l.size):
+        entries[l[f]].append((int(u[f]), upper[f], upper[f] * lower[f]))
+    color = np.full(n, -1)
+    for c in range(n):
+        taken = {color[nb] for nb, _, _ in entries[c] if nb < c}
+        k = 0
+        while k in taken:
+            k += 1
+        color[c] = k
+    order = np.argsort(color, kind="stable")
+    d = np.array(s["diag"], np.float64)
+    for c in order:
+        acc = d[c]
+        for nb, _, p in entries[c]:
+            if color[nb] < color[c]:
+                acc = acc - p / d[nb]
+        d[c] = acc
+    rD = 1.0 / d
+    w = np.zeros(n)
+    for c in order:
+        acc = rD[c] * b[c]
+        for nb, a, _ in entries[c]:
+            if color[nb] < color[c]:
+                acc = acc - (rD[c] * a) * w[nb]
+        w[c] = acc
+    for c in order[::-1]:
+        acc = w[c]
+        for nb, a, _ in entries[c][::-1]:
+            if color[nb] > color[c]:
+                acc = acc - (rD[c] * a) * w[nb]
+        w[c] = acc
+    return rD, w
+
+
+@pytest.mark.parametrize("name", ["cube6", "cd6", "perm_lap", "perm_cd", "box", "cycd7"])
+def test_multicolour_dic_dilu_exact(name, sweep_form):
+    """The multicolour DIC / DILU schedules (CFX_TUNE_COLORED_PRE 2 runs them
+    in FP64 too) equal the host restatement bit for bit in every sweep form:
+    the pivots, the preconditioner, DILU's preconditionT, and the DIC / DILU
+    smoother's sweeps."""
+    s = SYSTEMS[name]()
+    old = ldu.tune_get(ldu.TUNE_COLORED_PRE)
+    ldu.tune_set(ldu.TUNE_COLORED_PRE, 2)
+    try:
+        _, A = _fresh(s)
+        n = s["diag"].size
+        b = s["source"]
+        db = dev(b)
+        rD = torch.empty(n, dtype=torch.float64, device="cuda")
+        w = torch.empty(n, dtype=torch.float64, device="cuda")
+        kind = "DIC" if A.symmetric() else "DILU"
+        want_rD, want_w = _colored_ilu(s, b)
+        A.reciprocalD(kind, rD)
+        np.testing.assert_array_equal(host(rD), want_rD)
+        A.precondition(kind, db, w)
+        np.testing.assert_array_equal(host(w), want_w)
+        # the smoother: psi += M^-1 (b - A psi), one sweep from psi = 0
+        psi = torch.zeros(n, dtype=torch.float64, device="cuda")
+        A.smooth(kind, psi, db, 1)
+        np.testing.assert_array_equal(host(psi), want_w)
+        if kind == "DILU" and s.get("ifCell") is None:
+            # preconditionT (PBiCG's transpose sweeps) on the multicolour
+            # schedules: PBiCG+DILU still reaches the solution
+            dense = np.diag(np.asarray(s["diag"], np.float64))
+            dense[s["l"], s["u"]] = s["upper"]
+            dense[s["u"], s["l"]] = s["lower"]
+            want = np.linalg.solve(dense, b)
+            psi = np.zeros(n)
+            p = ldu.solve(s, psi, {"solver": "cudaPBiCG", "preconditioner": "DILU", "tolerance": 1e-12,
+                                   "relTol": 0, "maxIter": 1000})
+            assert p.converged
+            assert np.linalg.norm(psi - want) <= 1e-9 * np.linalg.norm(want)
+    finally:
+        ldu.tune_set(ldu.TUNE_COLORED_PRE, old)
+
+
 @pytest.mark.parametrize("name", ["cube6", "cd6", "perm_lap", "box"])
 def test_multicolour_gauss_seidel_exact(name):
     """The multicolour Gauss-Seidel schedule (CFX_TUNE_COLORED_GS 2 runs it in

@@ -367,13 +367,22 @@ enum { CFX_TUNE_SMALL_SWEEP = 0, CFX_TUNE_CLUSTER_GLOBAL = 1, CFX_TUNE_CLUSTER_S
         * reaches the FP64 tolerance; the FP64 solves keep the reference's
         * order bit for bit; 2 the multicolour order everywhere (tests) */
        CFX_TUNE_COLORED_GS = 14,
-       /* DIC / DILU order (preconditioners and smoothers), the same three
-        * values: 1 (default) the incomplete factorisation and its sweeps in
-        * the same multicolour order (a cell's smaller-coloured neighbours
-        * are its forward entries, the larger-coloured its backward ones) in
-        * the FP32 inner solves; the FP64 solves and the coarsest level's
+       /* DIC / DILU order (preconditioners and smoothers): 0 the
+        * reference's everywhere; 1 (default) DIC (symmetric matrices) in the
+        * FP32 inner solves of mixed-precision solves takes the incomplete
+        * factorisation and its sweeps in the multicolour order (a cell's
+        * smaller-coloured neighbours are its forward entries, the
+        * larger-coloured its backward ones): a few dependent steps per sweep
+        * instead of hundreds; 2 DILU there too (on convection-dominated
+        * systems the multicolour DILU is a much weaker preconditioner); 3
+        * both everywhere (tests).  The FP64 solves and the coarsest level's
         * one-CTA solve keep the reference's order */
-       CFX_TUNE_COLORED_PRE = 15 };
+       CFX_TUNE_COLORED_PRE = 15,
+       /* schedules of at most this many DAG levels (0..128, default 96)
+        * whose vector does not fit one CTA's shared memory run level by
+        * level, one ordinary launch per level with no waits: the multicolour
+        * schedules, whose levels are few and wide; 0: never */
+       CFX_TUNE_LEVEL_LAUNCH = 16 };
 cfx_status cfx_tune_set(int key, int value);
 cfx_status cfx_tune_get(int key, int* value);
 

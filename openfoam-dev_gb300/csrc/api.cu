@@ -587,6 +587,17 @@ DevSched upload_sched(Arena& ar, cudaStream_t s, const HostSched& h) {
     d.slotLower = ar.upload(h.slotLower, s);
     d.gdone = ar.get<int>(std::max(d.nGroups, 1));
     d.waveOk = h.waveOk ? 1 : 0;
+    d.levelLaunch = h.nLevels <= LVL_LAUNCH_MAX ? 1 : 0;
+    if (d.levelLaunch) {
+        d.hLvlPart[0] = 0;
+        for (int L = 0; L <= h.nLevels; ++L) {
+            d.hLvlSlot[L] = h.levelSlot[L];
+            if (L < h.nLevels) {
+                const int groups = (h.levelSlot[L + 1] - h.levelSlot[L]) / 32;
+                d.hLvlPart[L + 1] = d.hLvlPart[L] + (groups + LVL_LAUNCH_GROUPS - 1) / LVL_LAUNCH_GROUPS;
+            }
+        }
+    }
     d.sync = ar.get<int>(2 + size_t(LVL_STRIDE_MAX) * std::max(h.nLevels, 1));
     CK(cudaMemsetAsync(d.sync, 0, sizeof(int) * (2 + size_t(LVL_STRIDE_MAX) * std::max(h.nLevels, 1)), s));
     return d;
@@ -643,16 +654,19 @@ const DevSched& sched_pre_colored(cfx_mesh* mesh, int lv, int kind) {
     return fwd ? sc.fwdC : sc.bwdC;
 }
 
-// Whether precision T's DIC / DILU take the multicolour order
-// (colored_pre(): 1 for the FP32 inner solves, 2 for every solve).
+// Whether precision T's DIC (sym) / DILU take the multicolour order
+// (colored_pre(): 1 DIC in the FP32 inner solves, 2 DIC and DILU in the
+// FP32 inner solves, 3 both in every solve).
 template <class T>
-bool pre_colored() {
-    return colored_pre() == 2 || (colored_pre() == 1 && sizeof(T) == 4);
+bool pre_colored(bool sym) {
+    const int k = colored_pre();
+    if (k == 3) return true;
+    return k > 0 && sizeof(T) == 4 && (sym || k == 2);
 }
 
 // The forward / backward schedule DIC and DILU of precision T run on.
 template <class T>
-const DevSched& sched_pre(cfx_mesh* mesh, int lv, int kind, bool col = pre_colored<T>()) {
+const DevSched& sched_pre(cfx_mesh* mesh, int lv, int kind, bool col) {
     return col ? sched_pre_colored(mesh, lv, kind) : sched(mesh, lv, kind);
 }
 
@@ -692,13 +706,13 @@ std::vector<LevelPack<float>>& packs_of<float>(cfx_matrix* mat) {
 }
 
 template <class T>
-Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd, bool colPre = pre_colored<T>()) {
+Packed<T>& packed(cfx_matrix* mat, int lv, int op, int S, const DevSched& sd, int colPre = -1) {
     auto& v = packs_of<T>(mat);
     if ((int)v.size() <= lv) v.resize(lv + 1);
     LevelPack<T>& lp = v[lv];
     // the forward, backward and pivot packs of the multicolour schedules
     // are kept apart (their entry counts differ)
-    const bool col = op != OP_GS && colPre;
+    const bool col = op != OP_GS && (colPre < 0 ? pre_colored<T>(mat->sym) : colPre != 0);
     Packed<T>* p = op == OP_RD ? (col ? &lp.rdC : &lp.rd)
                  : op == OP_FWD ? (col ? &lp.fwdC : &lp.fwd)
                  : op == OP_BWD ? (col ? &lp.bwdC : &lp.bwd) : &lp.gs[S];
@@ -718,7 +732,7 @@ template <class T>
 Packed<T>& packedT(cfx_matrix* mat, int lv, int op, const DevSched& sd) {
     auto& v = packs_of<T>(mat);
     if ((int)v.size() <= lv) v.resize(lv + 1);
-    const bool col = pre_colored<T>();
+    const bool col = pre_colored<T>(mat->sym);
     Packed<T>* p = op == OP_FWD ? (col ? &v[lv].fwdTC : &v[lv].fwdT) : (col ? &v[lv].bwdTC : &v[lv].bwdT);
     if (!p->coef) {
         p->coef = mat->arena.get<T>(sd.nEntries);
@@ -757,7 +771,8 @@ void ensure_chunk_partials(cfx_ctx* ctx, size_t chunks) {
 // multicolour order (the coarsest level's one-CTA solve sweeps in the
 // reference's order and takes the reference's pivots).
 template <class T>
-void compute_rD(cfx_matrix* mat, int lv, bool col = pre_colored<T>()) {
+void compute_rD(cfx_matrix* mat, int lv, int colored = -1) {
+    const bool col = colored < 0 ? pre_colored<T>(mat->sym) : colored != 0;
     cfx_ctx* ctx = mat->mesh->ctx;
     cudaStream_t s = ctx->stream;
     const LevelMesh& m = mat->mesh->dev[lv];
@@ -768,13 +783,13 @@ void compute_rD(cfx_matrix* mat, int lv, bool col = pre_colored<T>()) {
     // dataflow CTA, whichever form runs
     ensure_chunk_partials(ctx, std::max({size_t(f.nChunks), size_t(b.nChunks), size_t(sweep_partials<T>(b)),
                                          size_t(sweep_partials<T>(f))}));
-    Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f, col);
+    Packed<T>& prd = packed<T>(mat, lv, OP_RD, 1, f, int(col));
     pack_sweep<T>(s, f, OP_RD, c, prd);
     if (run_sweep<T>(s, f, OP_RD, prd, nullptr, c.rD, nullptr, nullptr, nullptr, ctx->d_status) != CFX_OK)
         throw CudaError(last_error());
     Ops<T>::reciprocal(s, m.n, c.rD);
-    pack_sweep<T>(s, f, OP_FWD, c, packed<T>(mat, lv, OP_FWD, 1, f, col));
-    pack_sweep<T>(s, b, OP_BWD, c, packed<T>(mat, lv, OP_BWD, 1, b, col));
+    pack_sweep<T>(s, f, OP_FWD, c, packed<T>(mat, lv, OP_FWD, 1, f, int(col)));
+    pack_sweep<T>(s, b, OP_BWD, c, packed<T>(mat, lv, OP_BWD, 1, b, int(col)));
 }
 
 template <class T>
@@ -799,8 +814,8 @@ int precondition(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const int*
     LevelCoeffs<T>& c = coeffs<T>(mat, lv);
     if (kind == CFX_PRE_GAMG) return pc_gamg_apply<T>(mat, r, w, done, dot);
     if (kind == CFX_PRE_DIC || kind == CFX_PRE_DILU) {
-        const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
-        const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
+        const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD, pre_colored<T>(mat->sym));
+        const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD, pre_colored<T>(mat->sym));
         if (run_sweep<T>(s, f, OP_FWD, packed<T>(mat, lv, OP_FWD, 1, f), r, w, nullptr, nullptr, done,
                          ctx->d_status) != CFX_OK)
             throw CudaError(last_error());
@@ -829,8 +844,8 @@ void preconditionT(cfx_matrix* mat, int lv, int kind, const T* r, T* w, const in
     }
     cfx_ctx* ctx = mat->mesh->ctx;
     cudaStream_t s = ctx->stream;
-    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
-    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
+    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD, pre_colored<T>(mat->sym));
+    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD, pre_colored<T>(mat->sym));
     if (run_sweep<T>(s, f, OP_FWD, packedT<T>(mat, lv, OP_FWD, f), r, w, nullptr, nullptr, done, ctx->d_status) !=
         CFX_OK)
         throw CudaError(last_error());
@@ -852,8 +867,8 @@ void setup_preconditioner_t(cfx_matrix* mat, int lv, int kind) {
     t.lowerPerm = c.upperPerm;
     t.upperPerm = c.lowerPerm;
     t.sellCoef = nullptr;
-    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD);
-    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD);
+    const DevSched& f = sched_pre<T>(mat->mesh, lv, SCHED_FWD, pre_colored<T>(mat->sym));
+    const DevSched& b = sched_pre<T>(mat->mesh, lv, SCHED_BWD, pre_colored<T>(mat->sym));
     pack_sweep<T>(s, f, OP_FWD, t, packedT<T>(mat, lv, OP_FWD, f));
     pack_sweep<T>(s, b, OP_BWD, t, packedT<T>(mat, lv, OP_BWD, b));
 }
@@ -937,7 +952,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1285,7 +1300,7 @@ void setup_cycle(GamgCycle<T>& cy, cfx_matrix* mat, const cfx_controls* ctl, Wor
         }
         return;
     }
-    compute_rD<T>(mat, lc, false);  // coarsest PCG+DIC / PBiCGStab+DILU
+    compute_rD<T>(mat, lc, 0);  // coarsest PCG+DIC / PBiCGStab+DILU
     BlockSys<T> h{};
     h.n = m.n;
     h.nf = m.nf;
@@ -1437,7 +1452,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2471,8 +2486,12 @@ cfx_status cfx_tune_set(int key, int value) {
             set_colored_gs(value);
             return CFX_OK;
         case CFX_TUNE_COLORED_PRE:
-            if (value < 0 || value > 2) return CFX_ERR_ARG;
+            if (value < 0 || value > 3) return CFX_ERR_ARG;
             set_colored_pre(value);
+            return CFX_OK;
+        case CFX_TUNE_LEVEL_LAUNCH:
+            if (value < 0 || value > LVL_LAUNCH_MAX) return CFX_ERR_ARG;
+            set_sweep_level_launch(value);
             return CFX_OK;
         default: return CFX_ERR_ARG;
     }
@@ -2497,6 +2516,7 @@ cfx_status cfx_tune_get(int key, int* value) {
         case CFX_TUNE_CTA_XL: *value = sweep_cta_xl(); return CFX_OK;
         case CFX_TUNE_COLORED_GS: *value = colored_gs(); return CFX_OK;
         case CFX_TUNE_COLORED_PRE: *value = colored_pre(); return CFX_OK;
+        case CFX_TUNE_LEVEL_LAUNCH: *value = sweep_level_launch(); return CFX_OK;
         default: return CFX_ERR_ARG;
     }
 }

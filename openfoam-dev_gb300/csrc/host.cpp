@@ -342,7 +342,7 @@ void colored_levels(const HostLevel& h, int kind, const std::vector<int>& color,
 int colored_gs() { return g_colored_gs; }
 void set_colored_gs(int v) { g_colored_gs = v < 0 ? 0 : v > 2 ? 2 : v; }
 int colored_pre() { return g_colored_pre; }
-void set_colored_pre(int v) { g_colored_pre = v < 0 ? 0 : v > 2 ? 2 : v; }
+void set_colored_pre(int v) { g_colored_pre = v < 0 ? 0 : v > 3 ? 3 : v; }
 
 int greedy_colors(const HostLevel& h, std::vector<int>& color) {
     const int n = h.n;

@@ -299,6 +299,9 @@ struct HostSched {
     std::vector<int> slotSweep, slotLower;
 };
 
+constexpr int LVL_LAUNCH_MAX = 128;  // levels a schedule may have for the level-by-level form
+constexpr int LVL_LAUNCH_GROUPS = 8;  // groups (warps) per CTA of the level-by-level form
+
 struct DevSched {
     int kind = 0, nSweeps = 1, nLevels = 0, n = 0, maxK = 0;
     int nSlots = 0, nEntries = 0, nGroups = 0, nChunks = 0;
@@ -312,6 +315,12 @@ struct DevSched {
     int* gdone = nullptr;                // [nGroups] group finished flags
     int waveOk = 0;                      // dependencies verified to point backwards
     int *slotSweep = nullptr, *slotLower = nullptr;  // [nSlots] (level-ordered schedules)
+    // schedules of at most LVL_LAUNCH_MAX levels (the multicolour ones):
+    // each level's first slot and first dot partial, kept on the host for the
+    // level-by-level form (one launch per level)
+    int levelLaunch = 0;
+    int hLvlSlot[LVL_LAUNCH_MAX + 1];
+    int hLvlPart[LVL_LAUNCH_MAX + 1];
 };
 
 constexpr int LVL_STRIDE_MAX = 32;  // level counters up to one 128-byte line apart
@@ -346,10 +355,16 @@ int greedy_colors(const HostLevel& h, std::vector<int>& color);
 // smoothing (tests)
 int colored_gs();
 void set_colored_gs(int v);
-// DIC / DILU (preconditioners and smoothers) order, the same three values:
-// the multicolour incomplete factorisation of the same sparsity
+// DIC / DILU (preconditioners and smoothers) order: 0 the reference's; 1
+// (default) the multicolour incomplete factorisation of the same sparsity
+// for DIC in the FP32 inner solves; 2 for DIC and DILU there; 3 everywhere
+// (tests)
 int colored_pre();
 void set_colored_pre(int v);
+// Schedules of at most this many DAG levels (and too large for one CTA's
+// shared memory) run level by level, one ordinary launch per level (0: never)
+int sweep_level_launch();
+void set_sweep_level_launch(int v);
 
 // ---- sweeps (sweeps.cu) ---------------------------------------------------
 enum SweepOp {

@@ -412,16 +412,19 @@ __global__ void __launch_bounds__(RED_NT) gamg_scale_sf_k(int n, const int* os, 
                                                           const T* __restrict__ source, SolveState* st, Red2 red,
                                                           Iface<T> itf) {
     if (st->done) return;
-    double num = 0.0, den = 0.0;
+    // a thread's partial sums in T (the FP32 inner cycles accumulate their
+    // few cells in FP32 rather than on GB300's slow FP64 pipe), the block and
+    // grid sums in double
+    T num = T(0), den = T(0);
     for (int c = blockIdx.x * RED_NT + threadIdx.x; c < n; c += gridDim.x * RED_NT) {
         // Amul with the level's interfaces (GAMGSolverScale.C:42-50)
         const T v = iface_sub(itf, c, field, row_ax<T>(c, os, ls, lL, u, diag, lp, upper, S, field));
         Acf[c] = v;
-        num += double(source[c]) * double(field[c]);
-        den += double(v) * double(field[c]);
+        num += source[c] * field[c];
+        den += v * field[c];
     }
     double sn, sd;
-    if (reduce2<RED_NT>(num, den, red, sn, sd) && threadIdx.x == 0) {
+    if (reduce2<RED_NT>(double(num), double(den), red, sn, sd) && threadIdx.x == 0) {
         const double stab = sd >= 0 ? sd + VSMALL : sd - VSMALL;  // stabilise(den, vSmall)
         st->sf = sn / stab;
     }

@@ -47,6 +47,11 @@
 //                 until they are no longer the sentinel.  The value is its own
 //                 flag: no counters, release fences or block barriers, so a
 //                 dependency costs one store-to-load trip through L2.
+//   sweep_level_k one ordinary launch per DAG level (a warp per group, no
+//                 waits: the launch order separates the levels), for
+//                 schedules of few, wide levels (the multicolour ones: a few
+//                 colours per sweep), where the persistent forms' per-chunk
+//                 waits and counters cost more than a launch per level.
 
 #include <cooperative_groups.h>
 
@@ -83,6 +88,7 @@ size_t g_smem_cap_max = 200 * 1024;
 int g_flow = 2;             // the dataflow form: 0 off, 1 on, 2 for schedules of <= PF_SMALL entries
 int g_flow_ahead = 4;       // dataflow form: levels of groups in flight (warps launched)
 int g_cta_xl = 1;           // single-CTA form, FP32: PF_GRID_XL entries per slot in registers when slots have more than PF_LARGE
+int g_level_launch = 96;    // schedules of at most this many levels run one launch per level (0: never)
 int g_lvl_stride = 1;       // level-counter grid form: ints between consecutive level counters
 int g_poll_ns = 0;          // and the back-off of its waiting polls (ns)
 
@@ -222,6 +228,42 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
         }
         __syncthreads();
         if (threadIdx.x == 0) red_release_add(done + size_t(L) * stride, 1);
+    }
+}
+
+// Level-by-level form: groups g0..g1 of one DAG level, LVL_LAUNCH_GROUPS
+// warps per CTA, a warp per group.  Every value a slot reads comes from an
+// earlier level (an earlier launch), and the cells of one level are
+// independent, so x is updated in place without waits.  The dot partial
+// (when requested) is one per CTA, at p0 + blockIdx.x.
+template <class T, int OP>
+__global__ void __launch_bounds__(32 * LVL_LAUNCH_GROUPS) sweep_level_k(DevSched s, SweepCtx<T> a, int g0, int g1,
+                                                                       int p0) {
+    constexpr int NT = 32 * LVL_LAUNCH_GROUPS;
+    __shared__ double sh[LVL_LAUNCH_GROUPS];
+    if (a.done && *a.done) return;
+    const int lane = threadIdx.x & 31;
+    const int g = g0 + blockIdx.x * LVL_LAUNCH_GROUPS + (threadIdx.x >> 5);
+    int c = -1;
+    T v = T(0);
+    if (g < g1) {
+        const int slot = g * 32 + lane;
+        c = s.cell[slot];
+        if (c >= 0) {
+            const int n = s.cnt[slot];
+            const int e0 = s.groupEntry[g] + lane;
+            const T sc = a.scalar[slot];
+            const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
+            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? a.x[c] : T(0));
+            acc = tail_entries<T, OP>(s, a.coef, e0, 0, n, acc, [&](int cc) { return a.x[cc]; });
+            v = sw_fini<OP>(acc, sc);
+            a.x[c] = v;
+        }
+    }
+    if (a.dotWith) {
+        double p = c >= 0 ? double(v) * double(a.dotWith[c]) : 0.0;
+        p = block_sum<NT>(p, sh);
+        if (threadIdx.x == 0) a.partials[p0 + blockIdx.x] = p;
     }
 }
 
@@ -770,7 +812,7 @@ inline int prec_index<double>() { return 0; }
 template <>
 inline int prec_index<float>() { return 1; }
 
-enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4, M_FLOW = 5 };
+enum Mode { M_CTA = 0, M_CLUSTER_DS = 1, M_CTA_GLOBAL = 2, M_CLUSTER_GLOBAL = 3, M_GRID = 4, M_FLOW = 5, M_LEVELS = 6 };
 
 // Execution form of a schedule: the vector in one CTA's shared memory, in a
 // cluster's distributed shared memory, or in global memory with a single CTA,
@@ -788,6 +830,12 @@ inline int cluster_of(const DevSched& s) {
 template <class T>
 int mode_of(const DevSched& s) {
     const size_t xbytes = sizeof(T) * size_t(s.n);
+    // few levels: a launch per level, unless the vector fits one CTA's
+    // shared memory and the levels are narrow (fewer than 128 slots on
+    // average: one CTA walks those faster than a launch per level)
+    if (s.levelLaunch && s.nLevels <= g_level_launch &&
+        (xbytes > g_smem_cap || int64_t(s.nSlots) >= 128 * int64_t(s.nLevels)))
+        return M_LEVELS;
     if (xbytes <= g_smem_cap) return M_CTA;
     const int cs = cluster_of(s);
     if (cs) {
@@ -815,6 +863,16 @@ cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, i
     const int cs = cluster_of(s);
     const int per = cs ? (s.n + cs - 1) / cs : 0;
     const int m = mode_of<T>(s);
+    if (m == M_LEVELS) {
+        for (int L = 0; L < s.nLevels; ++L) {
+            const int g0 = s.hLvlSlot[L] / 32, g1 = s.hLvlSlot[L + 1] / 32;
+            const int ctas = (g1 - g0 + LVL_LAUNCH_GROUPS - 1) / LVL_LAUNCH_GROUPS;
+            if (ctas == 0) continue;
+            sweep_level_k<T, OP><<<ctas, 32 * LVL_LAUNCH_GROUPS, 0, st>>>(s, a, g0, g1, s.hLvlPart[L]);
+            count_launch();
+        }
+        return CFX_OK;
+    }
     if (m == M_CTA) {
         // FP32: the single CTA holds the larger register set (the next
         // level's entries prefetched, up to PF_GRID_XL per slot); in FP64 that
@@ -1045,6 +1103,8 @@ int sweep_grid_stride() { return g_lvl_stride; }
 void set_sweep_grid_stride(int k) { g_lvl_stride = k < 1 ? 1 : k > LVL_STRIDE_MAX ? LVL_STRIDE_MAX : k; }
 int sweep_grid_poll_ns() { return g_poll_ns; }
 void set_sweep_grid_poll_ns(int ns) { g_poll_ns = ns < 0 ? 0 : ns; }
+int sweep_level_launch() { return g_level_launch; }
+void set_sweep_level_launch(int v) { g_level_launch = v < 0 ? 0 : v > LVL_LAUNCH_MAX ? LVL_LAUNCH_MAX : v; }
 int sweep_flow_ahead() { return g_flow_ahead; }
 void set_sweep_flow_ahead(int k) { g_flow_ahead = k < 1 ? 1 : k; }
 
@@ -1068,6 +1128,7 @@ template <class T>
 int sweep_partials(const DevSched& s) {
     const int m = mode_of<T>(s);
     if (m == M_FLOW) return flow_ctas(prec_index<T>(), OP_BWD, s);
+    if (m == M_LEVELS) return std::max(1, s.hLvlPart[s.nLevels]);
     if (m == M_GRID) return g_wave && s.waveOk ? wave_grid<T>(s) : s.nChunks;
     return (m == M_CLUSTER_DS || m == M_CLUSTER_GLOBAL) ? cluster_of(s) : 1;
 }

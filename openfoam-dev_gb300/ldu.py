@@ -529,6 +529,7 @@ TUNE_AMUL_SELL = 9
 TUNE_GRID_STRIDE, TUNE_GRID_POLL_NS, TUNE_CHUNK_GROUPS, TUNE_CTA_XL = 10, 11, 12, 13
 TUNE_COLORED_GS = 14
 TUNE_COLORED_PRE = 15
+TUNE_LEVEL_LAUNCH = 16
 
 
 def tune_set(key, value):

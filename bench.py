@@ -61,11 +61,12 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=256, help="cube cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel-only", choices=["gs", "level1", "solves", "amul"], default=None,
+    ap.add_argument("--kernel-only", choices=["gs", "level1", "gs32", "level1_32", "solves", "amul"], default=None,
                     help="profiling: gs = the finest level's fused 2-sweep Gauss-Seidel alone, level1 = the "
-                         "first agglomerated level's, solves = one FP64 and one mixed headline solve inside "
-                         "the NVTX range 'profiled' (after one warm-up solve of each), amul = Amul on the "
-                         "finest level, FP64 then FP32 (warmup + steps launches each)")
+                         "first agglomerated level's, gs32 / level1_32 = the same levels' FP32 inner-cycle "
+                         "smoothing (multicolour order), solves = one FP64 and one mixed headline solve inside "
+                         "the NVTX ranges 'profiled_fp64' / 'profiled_mixed' (after one warm-up solve of each), "
+                         "amul = Amul on the finest level, FP64 then FP32 (warmup + steps launches each)")
     ap.add_argument("--form", choices=["default", "grid", "flow"], default="default",
                     help="profiling modes: the sweep form of the levels larger than one CTA")
     ap.add_argument("--write-case", default=None, help=argparse.SUPPRESS)
@@ -413,6 +414,48 @@ def level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells):
     return rows
 
 
+FORM_NAMES = {0: "one CTA, vector in shared memory", 1: "cluster, distributed shared memory",
+              2: "one CTA, vector in global memory", 3: "cluster, global memory", 4: "persistent grid",
+              5: "dataflow", 6: "one launch per level"}
+
+
+def level_sweeps_f32(ctx, mesh, A, N, F, ev_time, local):
+    """Every GAMG level's smoothing as the FP32 inner cycles of the mixed
+    solve apply it (multicolour Gauss-Seidel on the FP32 coefficient copy,
+    the V-cycle's sweep count), each level's matrix alone through
+    cfx_diag_smooth_f32, CUDA events on the library's stream.  Algorithmic
+    bytes with 4-byte values: 7sN + sF + 4F + 4N per sweep, s = 4."""
+    import torch
+    from openfoam_dev_gb300 import ldu
+    rows = []
+    nc_prev, nf_prev = N, F
+    levels = [(0, N, F, None, None)]
+    for i in range(mesh.n_levels()):
+        _, _, _, nc, ncf, cl, cu = mesh.level(i, nc_prev, nf_prev)
+        levels.append((i + 1, nc, ncf, cl, cu))
+        nc_prev, nf_prev = nc, ncf
+    rng = np.random.default_rng(7)
+    for lv, nc, ncf, cl, cu in levels:
+        S = gs_sweeps(lv)
+        if lv == 0:
+            Al, ml = A, None
+        else:
+            d, up, _ = A.coarse(lv, nc, ncf)
+            ml = ldu.LduMesh(ctx, nc, cl, cu)
+            Al = ldu.LduMatrix(ml, d, up)
+        b = torch.from_numpy(rng.uniform(-1, 1, nc).astype(np.float32)).to(f"cuda:{local}")
+        x = torch.zeros_like(b)
+        form = Al.smooth_f32("GaussSeidel", x, b, S)
+        t = ev_time(lambda: Al.smooth_f32("GaussSeidel", x, b, S))
+        by = S * gs_bytes(nc, ncf, s=4)
+        rows.append({"level": lv, "cells": nc, "faces": ncf, "sweeps": S, "s": t, "algorithmic_bytes": by,
+                     "GB_s": by / t / 1e9, "form": FORM_NAMES.get(form, str(form))})
+        if ml is not None:
+            Al.close()
+            ml.close()
+    return rows
+
+
 def run_ours(args, rank, world, local, pg):
     # the oracle legs start first, in spawned processes, before any GPU call
     cpu = not args.no_cpu_baseline and world == 1 and rank == 0
@@ -509,6 +552,8 @@ def run_ours(args, rank, world, local, pg):
     # time are the Gauss-Seidel sweeps of the agglomerated levels
     smem_cells = ldu.tune_get(ldu.TUNE_SMEM_BYTES) // 8
     levels = level_sweeps(ctx, mesh, A, N, F, ev_time, local, smem_cells)
+    # the mixed solve's smoothing (FP32 inner cycles): its dominant kernel
+    levels32 = level_sweeps_f32(ctx, mesh, A, N, F, ev_time, local)
 
     # the streaming kernels of the path (HBM-bound, no level chain), FP64 at
     # the same size, each timed alone: Amul (3sN + 2sF), residual
@@ -543,24 +588,34 @@ def run_ours(args, rank, world, local, pg):
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    # roofline: the agglomerated levels' persistent-grid Gauss-Seidel sweeps
-    # (the largest share of device time), bytes and time summed over their
-    # launches = average bytes per launch / average launch time
-    dom = [r for r in levels if r["level"] > 0 and r["form"] == "persistent grid"]
+    # roofline: the kernel with the largest share of the headline (mixed)
+    # solve's device time, sweep_level_k<float>: the FP32 multicolour
+    # Gauss-Seidel smoothing of the levels that run one launch per DAG level;
+    # bytes and time summed over those levels' smoothings = average bytes per
+    # smoothing / average smoothing time
+    dom = [r for r in levels32 if r["form"] == FORM_NAMES[6]]
     dom_bytes = sum(r["algorithmic_bytes"] for r in dom)
     dom_time = sum(r["s"] for r in dom)
-    achieved = dom_bytes / dom_time / 1e9
+    achieved = dom_bytes / dom_time / 1e9 if dom else 0.0
+    # the same for the FP64 solve's dominant kernels (the agglomerated
+    # levels' persistent-grid sweeps)
+    dom64 = [r for r in levels if r["level"] > 0 and r["form"] == "persistent grid"]
+    dom64_bytes = sum(r["algorithmic_bytes"] for r in dom64)
+    dom64_time = sum(r["s"] for r in dom64)
     cycle_sweeps = 2 * sum(r["s"] for r in levels)  # pre and post smoothing per V-cycle
-    traffic = None
+    traffic = traffic64 = None
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
-        per_byte = tr.get("gs_coarse_dram_per_algorithmic_byte")
-        if per_byte:
-            traffic = per_byte * dom_bytes / max(len(dom), 1)
+        per_byte = tr.get("gs_level_f32_dram_per_algorithmic_byte")
+        if per_byte and dom:
+            traffic = per_byte * dom_bytes / len(dom)
+        per_byte64 = tr.get("gs_coarse_dram_per_algorithmic_byte")
+        if per_byte64 and dom64:
+            traffic64 = per_byte64 * dom64_bytes / len(dom64)
     except (OSError, ValueError):
         pass
-    for r in levels:
+    for r in levels + levels32:
         r["frac"] = r["GB_s"] / peak
     line = {"metric": METRIC, "value": tm, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tm * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -579,14 +634,26 @@ def run_ours(args, rank, world, local, pg):
                                       "fp64_pipe_frac": fp64_ops(k, N, F) / t / FP64_OPS_PEAK}
                                   for k, (t, b) in streaming.items()},
             "roofline": {"bound": "hbm",
-                         "kernel": "Gauss-Seidel sweeps of the agglomerated GAMG levels, persistent grid form "
-                                   f"(FP64; levels {dom[0]['level']}-{dom[-1]['level']}, the V-cycle's sweep counts)"
-                         if dom else "none",
+                         "kernel": "sweep_level_k<float>: the FP32 inner cycles' multicolour Gauss-Seidel "
+                                   "smoothing, one launch per DAG level "
+                                   f"(levels {', '.join(str(r['level']) for r in dom)}, the V-cycle's sweep counts; "
+                                   "bytes and time per level smoothing)" if dom else "none",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes / max(len(dom), 1),
                          "launch_s": dom_time / max(len(dom), 1), "launches": len(dom),
                          "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "roofline_fp64": {"bound": "hbm",
+                              "kernel": "sweep_grid_k<double>: the FP64 solve's Gauss-Seidel sweeps of the "
+                                        "agglomerated levels, persistent grid form (levels "
+                                        f"{dom64[0]['level']}-{dom64[-1]['level']})" if dom64 else "none",
+                              "achieved": dom64_bytes / dom64_time / 1e9 if dom64 else 0.0, "peak": peak,
+                              "unit": "GB/s",
+                              "frac": dom64_bytes / dom64_time / 1e9 / peak if dom64 else 0.0,
+                              "traffic": traffic64,
+                              "algorithmic_bytes_per_launch": dom64_bytes / max(len(dom64), 1),
+                              "launch_s": dom64_time / max(len(dom64), 1), "launches": len(dom64)},
             "gamg_levels_fp64": levels,
+            "gamg_levels_f32_inner": levels32,
             "v_cycle_fp64_s": t64 / max(p_fp64.nIterations, 1),
             "v_cycle_smoothing_fp64_s": cycle_sweeps,
             "clocks": clk.summary()}
@@ -838,7 +905,9 @@ def run_batch_serve(args, local, want_batch, want_serve):
 def run_kernel_only(args):
     """One Gauss-Seidel smoothing alone, warmup + steps times (for profiling
     under ncu): gs = the finest level's fused 2 sweeps, level1 = the first
-    agglomerated level's (the persistent grid form, the V-cycle's 2 sweeps)."""
+    agglomerated level's (the persistent grid form, the V-cycle's 2 sweeps);
+    gs32 / level1_32 = the same levels' FP32 inner-cycle smoothing
+    (multicolour order, one launch per DAG level)."""
     import torch
     ge.load_package()
     from openfoam_dev_gb300 import cases, ldu
@@ -889,26 +958,34 @@ def run_kernel_only(args):
             t[name] = statistics.median(ts)
         print(json.dumps({"kernel": "amul", "n": args.n, "cells": N, "faces": F, **t}), flush=True)
         return 0
-    if args.kernel_only == "level1":
+    if args.kernel_only in ("level1", "level1_32"):
         mesh.agglomerate(Sf=s["Sf"], nCellsInCoarsestLevel=10)
         _, _, _, nc, ncf, cl, cu = mesh.level(0, N, F)
         d, up, _ = A.coarse(1, nc, ncf)
         mesh = ldu.LduMesh(mesh.ctx, nc, cl, cu)
         A = ldu.LduMatrix(mesh, d, up)
         N, F = nc, ncf
+    f32 = args.kernel_only.endswith("32")
     d_b = torch.from_numpy(np.random.default_rng(7).uniform(-1, 1, N)).cuda()
+    if f32:
+        d_b = d_b.float()
     d_x = torch.zeros_like(d_b)
     torch.cuda.synchronize()
     t = []
+    form = None
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        A.smooth("GaussSeidel", d_x, d_b, 2)
+        if f32:
+            form = A.smooth_f32("GaussSeidel", d_x, d_b, 2)
+        else:
+            A.smooth("GaussSeidel", d_x, d_b, 2)
         torch.cuda.synchronize()
         if i >= args.warmup:
             t.append(time.perf_counter() - t0)
     print(json.dumps({"kernel": args.kernel_only, "n": args.n, "cells": N, "faces": F,
-                      "algorithmic_bytes": 2 * gs_bytes(N, F), "s": statistics.median(t)}), flush=True)
+                      "algorithmic_bytes": 2 * gs_bytes(N, F, s=4 if f32 else 8), "s": statistics.median(t),
+                      "form": FORM_NAMES.get(form) if f32 else None}), flush=True)
     return 0
 
 

@@ -542,6 +542,18 @@ cfx_status cfx_reduce_noalloc(int which, int n, const double* d_a, const double*
  * the matrix needs at least two forward levels. */
 cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status);
 
+/* The smoothing the FP32 inner cycles of a mixed-precision GAMG solve apply
+ * to a level, on its own: nSweeps sweeps of smoother `kind` (the cfx_smooth
+ * kinds GaussSeidel, DIC, DILU and their GaussSeidel combinations) on the
+ * matrix's FP32 coefficient copy, psi and b device FP32 vectors of nCells,
+ * in the order the inner cycles use (CFX_TUNE_COLORED_GS /
+ * CFX_TUNE_COLORED_PRE).  *form (may be NULL) receives the execution form of
+ * the Gauss-Seidel schedule: 0 one CTA (vector in shared memory), 1 a
+ * cluster (distributed shared memory), 2 one CTA (vector in global memory),
+ * 3 a cluster (global memory), 4 the persistent grid, 5 the dataflow form,
+ * 6 one launch per level.  For timing and profiling. */
+cfx_status cfx_diag_smooth_f32(cfx_matrix* mat, int kind, float* psi, const float* b, int nSweeps, int* form);
+
 #ifdef __cplusplus
 }
 #endif

@@ -130,6 +130,7 @@ struct cfx_matrix {
     int luPivN = 0;
     int ifN = 0;  // interface coefficients held (cfx_matrix_set_interface_coeffs)
     GraphCache gPCG, gBiCG, gGAMG, gMixed;
+    GraphCache gDiag32;  // cfx_diag_smooth_f32: the smoothing as the V-cycle graph replays it
 };
 
 // --------------------------------------------------------------- utilities
@@ -952,7 +953,7 @@ cfx_status krylov(cfx_matrix* mat, Work<T>& W, GraphCache& gc, int lv, int solve
                       uint64_t(ctl.interpolateCorrection), uint64_t(ctl.directSolveCoarsest),
                       uint64_t(mat->mesh->nCoarseLevels)});
     }
-    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
+    const uint64_t key = hkey({mat->mesh->version, pcKey, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(sweep_smem_cap()), uint64_t(sweep_wave()), uint64_t(sched_chunk_groups()), uint64_t(lv), uint64_t(solver), uint64_t(precond), uint64_t(slot), uint64_t(n),
                                reinterpret_cast<uint64_t>(psi), reinterpret_cast<uint64_t>(b),
                                reinterpret_cast<uint64_t>(r), reinterpret_cast<uint64_t>(c.rD),
                                reinterpret_cast<uint64_t>(c.ifBou), reinterpret_cast<uint64_t>(m.ifStart)});
@@ -1452,7 +1453,7 @@ cfx_status gamg_solve(cfx_matrix* mat, const cfx_controls& ctl, double* psi, con
     count_launch();
     Ops<double>::amul(s, m0, mat->c64[0], psi, Apsi);
     Kern<double>::norm_init(s, ctx->sc, m0, mat->c64[0], Apsi, b, fres, nullptr, st);
-    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
+    uint64_t key = hkey({mesh->version, uint64_t(small_sweep_threshold()), uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()), uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()), uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()), uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(sweep_smem_cap()), uint64_t(sweep_wave()), uint64_t(sched_chunk_groups()), uint64_t(nl), uint64_t(ctl.smoother), uint64_t(ctl.nPreSweeps), uint64_t(ctl.nPostSweeps),
                          uint64_t(ctl.nFinestSweeps), uint64_t(ctl.maxPreSweeps), uint64_t(ctl.maxPostSweeps),
                          uint64_t(ctl.preSweepsLevelMultiplier), uint64_t(ctl.postSweepsLevelMultiplier),
                          uint64_t(ctl.scaleCorrection + 7), uint64_t(ctl.interpolateCorrection),
@@ -2660,6 +2661,43 @@ cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status) {
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s));
         CK(cudaStreamSynchronize(s));
         return CFX_OK;
+    });
+}
+
+cfx_status cfx_diag_smooth_f32(cfx_matrix* mat, int kind, float* psi, const float* b, int nSweeps, int* form) {
+    if (!mat || !psi || !b || nSweeps < 0) return CFX_ERR_ARG;
+    if (kind != CFX_SMOOTH_GS && kind != CFX_SMOOTH_DIC && kind != CFX_SMOOTH_DILU && kind != CFX_SMOOTH_DICGS &&
+        kind != CFX_SMOOTH_DILUGS)
+        return CFX_ERR_CONFIG;
+    if ((kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) && !mat->sym) return CFX_ERR_CONFIG;
+    if ((kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) && mat->sym) return CFX_ERR_CONFIG;
+    return guard([&]() -> cfx_status {
+        cfx_ctx* ctx = mat->mesh->ctx;
+        after_caller(ctx);
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+        prepare_levels(mat, true);
+        if ((int)mat->lv32.size() < 1) mat->lv32.resize(1);
+        if (kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DICGS) setup_preconditioner<float>(mat, 0, CFX_PRE_DIC);
+        if (kind == CFX_SMOOTH_DILU || kind == CFX_SMOOTH_DILUGS) setup_preconditioner<float>(mat, 0, CFX_PRE_DILU);
+        prepare_smooth<float>(mat, 0, kind, nSweeps, mat->lv32[0]);
+        // captured and replayed as a CUDA graph, as inside the V-cycle
+        const uint64_t key =
+            hkey({mat->mesh->version, uint64_t(kind), uint64_t(nSweeps), uint64_t(reinterpret_cast<uintptr_t>(psi)),
+                  uint64_t(reinterpret_cast<uintptr_t>(b)), uint64_t(small_sweep_threshold()),
+                  uint64_t(cluster_global_cells()), uint64_t(sweep_cluster_size()), uint64_t(sweep_cluster_pre()),
+                  uint64_t(sweep_flow()), uint64_t(sweep_flow_ahead()), uint64_t(amul_sell()),
+                  uint64_t(sweep_grid_stride()), uint64_t(sweep_grid_poll_ns()), uint64_t(sweep_cta_xl()),
+                  uint64_t(colored_gs()), uint64_t(colored_pre()), uint64_t(sweep_level_launch()), uint64_t(sweep_smem_cap()), uint64_t(sweep_wave()), uint64_t(sched_chunk_groups())});
+        graph_launch(mat->gDiag32, key, ctx->stream,
+                     [&] { smooth<float>(ctx, mat, 0, kind, psi, b, nSweeps, mat->lv32[0]); });
+        if (form) {
+            const int S = std::max(nSweeps, 1);
+            *form = sweep_mode<float>(gs_colored<float>() ? sched_colored(mat->mesh, 0, S)
+                                                          : sched(mat->mesh, 0, SCHED_GS, S));
+        }
+        CK(cudaStreamSynchronize(ctx->stream));
+        const int stc = read_status(ctx);
+        return stc ? cfx_status(stc) : CFX_OK;
     });
 }
 

@@ -380,6 +380,11 @@ bool sweep_is_grid(const DevSched& s);
 // number of dot partials a fused backward sweep writes
 template <class T>
 int sweep_partials(const DevSched& s);
+// The execution form a schedule runs in (0 one CTA, 1 cluster in distributed
+// shared memory, 2 one CTA with the vector in global memory, 3 cluster in
+// global memory, 4 persistent grid, 5 dataflow, 6 one launch per level)
+template <class T>
+int sweep_mode(const DevSched& s);
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
                      const T* dotWith, double* partials, const int* done, int* status);

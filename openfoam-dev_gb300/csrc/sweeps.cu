@@ -1125,6 +1125,11 @@ bool sweep_is_grid(const DevSched& s) {
 }
 
 template <class T>
+int sweep_mode(const DevSched& s) {
+    return mode_of<T>(s);
+}
+
+template <class T>
 int sweep_partials(const DevSched& s) {
     const int m = mode_of<T>(s);
     if (m == M_FLOW) return flow_ctas(prec_index<T>(), OP_BWD, s);
@@ -1268,6 +1273,8 @@ template bool sweep_is_grid<double>(const DevSched&);
 template bool sweep_is_grid<float>(const DevSched&);
 template int sweep_partials<double>(const DevSched&);
 template int sweep_partials<float>(const DevSched&);
+template int sweep_mode<double>(const DevSched&);
+template int sweep_mode<float>(const DevSched&);
 template cfx_status run_sweep<double>(cudaStream_t, const DevSched&, int, const Packed<double>&, const double*,
                                       double*, const double*, double*, const int*, int*);
 template cfx_status run_sweep<float>(cudaStream_t, const DevSched&, int, const Packed<float>&, const float*, float*,

@@ -157,6 +157,7 @@ _SIG = {
     "cfx_reciprocal_d": (_i, [_vp, _i, _vp]),
     "cfx_smooth": (_i, [_vp, _i, _vp, _vp, _i]),
     "cfx_diag_sweep_stall": (_i, [_vp, _i, ctypes.POINTER(_i)]),
+    "cfx_diag_smooth_f32": (_i, [_vp, _i, _vp, _vp, _i, ctypes.POINTER(_i)]),
     "cfx_reduce_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
     "cfx_batch_create": (_i, [_vp, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "cfx_batch_destroy": (_i, [_vp]),
@@ -475,6 +476,15 @@ class LduMatrix:
 
     def smooth(self, kind, psi, b, nSweeps):
         _check(lib().cfx_smooth(self.h, SMOOTHERS[kind], _dp(psi), _dp(b), int(nSweeps)), "smooth")
+
+    def smooth_f32(self, kind, psi, b, nSweeps):
+        """The FP32 inner cycles' smoothing of this matrix alone (psi, b:
+        float32 CUDA tensors); returns the Gauss-Seidel schedule's execution
+        form (cfx_diag_smooth_f32)."""
+        form = ctypes.c_int(-1)
+        _check(lib().cfx_diag_smooth_f32(self.h, SMOOTHERS[kind], _dp(psi), _dp(b), int(nSweeps),
+                                         ctypes.byref(form)), "cfx_diag_smooth_f32")
+        return form.value
 
     def diag_sweep_stall(self, timeout_ms):
         """Device status of a sweep whose bounded waits are made to expire."""

@@ -242,17 +242,19 @@ def test_bad_addressing_rejected():
     assert e.value.status == -2
 
 
-def _colored_gs(s, x, b, sweeps):
-    """The multicolour Gauss-Seidel the FP32 inner cycles use, in FP64 on the
-    host: greedy colours (ascending cells, smallest colour no smaller-index
-    neighbour has); per sweep the colours in ascending order, each cell from
-    b minus its smaller-coloured neighbours' new values, then its
-    larger-coloured neighbours' old values (each group in the reference's
+def _colored_gs(s, x, b, sweeps, dt=np.float64):
+    """The multicolour Gauss-Seidel the FP32 inner cycles use, on the host in
+    precision dt: greedy colours (ascending cells, smallest colour no
+    smaller-index neighbour has); per sweep the colours in ascending order,
+    each cell from b minus its smaller-coloured neighbours' new values, then
+    its larger-coloured neighbours' old values (each group in the reference's
     entry order: losort faces, then owned faces), divided by the diagonal."""
     n = s["diag"].size
     l, u = np.asarray(s["l"]), np.asarray(s["u"])
-    upper = np.asarray(s["upper"], np.float64)
-    lower = upper if s.get("lower") is None else np.asarray(s["lower"], np.float64)
+    upper = np.asarray(s["upper"], dt)
+    lower = upper if s.get("lower") is None else np.asarray(s["lower"], dt)
+    diag = np.asarray(s["diag"], dt)
+    b = np.asarray(b, dt)
     entries = [[] for _ in range(n)]
     for f in np.argsort(u, kind="stable"):  # losort: by neighbour cell, faces in order
         entries[u[f]].append((int(l[f]), lower[f]))
@@ -265,16 +267,16 @@ def _colored_gs(s, x, b, sweeps):
         while k in taken:
             k += 1
         color[c] = k
-    x = np.array(x, np.float64)
+    x = np.array(x, dt)
     order = np.argsort(color, kind="stable")
     for _ in range(sweeps):
         for c in order:
-            acc = np.float64(b[c])
+            acc = b[c]
             for first in (True, False):
                 for nb, cf in entries[c]:
                     if (color[nb] < color[c]) == first:
                         acc = acc - cf * x[nb]
-            x[c] = acc / s["diag"][c]
+            x[c] = acc / diag[c]
     return x
 
 
@@ -371,6 +373,24 @@ def test_multicolour_dic_dilu_exact(name, sweep_form):
             assert np.linalg.norm(psi - want) <= 1e-9 * np.linalg.norm(want)
     finally:
         ldu.tune_set(ldu.TUNE_COLORED_PRE, old)
+
+
+@pytest.mark.parametrize("name", ["cube24", "cd6", "perm_lap", "box"])
+def test_fp32_inner_smoothing_exact(name, sweep_form):
+    """cfx_diag_smooth_f32: the FP32 inner cycles' multicolour Gauss-Seidel
+    on the FP32 coefficient copy equals an FP32 host restatement bit for bit
+    in every sweep form, and reports the form it ran in."""
+    s = SYSTEMS[name]()
+    _, A = _fresh(s)
+    n = s["diag"].size
+    x = cases.uniform(8, n).astype(np.float32)
+    b = s["source"].astype(np.float32)
+    for sweeps in (1, 2, 4):
+        psi = torch.from_numpy(x.copy()).cuda()
+        form = A.smooth_f32("GaussSeidel", psi, torch.from_numpy(b).cuda(), sweeps)
+        assert 0 <= form <= 6
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(psi.cpu().numpy(), _colored_gs(s, x, b, sweeps, np.float32))
 
 
 @pytest.mark.parametrize("name", ["cube6", "cd6", "perm_lap", "box"])

@@ -234,34 +234,72 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
 // Level-by-level form: groups g0..g1 of one DAG level, LVL_LAUNCH_GROUPS
 // warps per CTA, a warp per group.  Every value a slot reads comes from an
 // earlier level (an earlier launch), and the cells of one level are
-// independent, so x is updated in place without waits.  The dot partial
-// (when requested) is one per CTA, at p0 + blockIdx.x.
-template <class T, int OP>
-__global__ void __launch_bounds__(32 * LVL_LAUNCH_GROUPS) sweep_level_k(DevSched s, SweepCtx<T> a, int g0, int g1,
+// independent, so x is updated in place without waits.  The levels are
+// launched as programmatic dependents of one another: a level's grid starts
+// while the previous level runs, loads its slots' schedule data (cell,
+// entry count, the first PF columns and coefficients, scalar, right-hand
+// side; all written by kernels that completed before the previous level
+// passed its own wait, read through L2) and only then waits
+// (griddepcontrol.wait) for the previous level's values; it lets its own
+// dependents start once past that wait, so a level's prologue never reads
+// anything a still-running kernel writes.  The dot partial (when requested)
+// is one per CTA, at p0 + blockIdx.x.
+struct LevelView {
+    const int *cell, *cnt, *groupEntry, *nb;
+};
+
+template <class T, int OP, int PF>
+__global__ void __launch_bounds__(32 * LVL_LAUNCH_GROUPS) sweep_level_k(LevelView s, SweepCtx<T> a, int g0, int g1,
                                                                        int p0) {
     constexpr int NT = 32 * LVL_LAUNCH_GROUPS;
     __shared__ double sh[LVL_LAUNCH_GROUPS];
-    if (a.done && *a.done) return;
     const int lane = threadIdx.x & 31;
     const int g = g0 + blockIdx.x * LVL_LAUNCH_GROUPS + (threadIdx.x >> 5);
-    int c = -1;
-    T v = T(0);
+    int c = -1, n = 0, e0 = 0;
+    T sc = T(0), in = T(0);
+    int nbr[PF];
+    T cf[PF];
     if (g < g1) {
         const int slot = g * 32 + lane;
-        c = s.cell[slot];
-        if (c >= 0) {
-            const int n = s.cnt[slot];
-            const int e0 = s.groupEntry[g] + lane;
-            const T sc = a.scalar[slot];
-            const T in = (OP == OP_FWD || OP == OP_GS) ? a.inS[slot] : T(0);
-            T acc = sw_init<OP>(sc, in, OP == OP_BWD ? a.x[c] : T(0));
-            acc = tail_entries<T, OP>(s, a.coef, e0, 0, n, acc, [&](int cc) { return a.x[cc]; });
-            v = sw_fini<OP>(acc, sc);
-            a.x[c] = v;
+        c = ldcg(s.cell + slot);
+        n = ldcg(s.cnt + slot);
+        e0 = ldcg(s.groupEntry + g) + lane;
+        sc = ldcg(a.scalar + slot);
+        if (OP == OP_FWD || OP == OP_GS) in = ldcg(a.inS + slot);
+#pragma unroll
+        for (int k = 0; k < PF; ++k)
+            if (k < n) {
+                nbr[k] = ldcg(s.nb + e0 + 32 * k);
+                cf[k] = ldcg(a.coef + e0 + 32 * k);
+            }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (a.done && ldcg(a.done)) return;
+    T v = T(0);
+    if (c >= 0) {
+        T acc = sw_init<OP>(sc, in, OP == OP_BWD ? ldcg(a.x + c) : T(0));
+#pragma unroll
+        for (int k = 0; k < PF; ++k)
+            if (k < n) acc = sw_step<OP>(acc, cf[k], ldcg(a.x + nbr[k]));
+        for (int kb = PF; kb < n; kb += 8) {
+            int nb[8];
+            T cb[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (kb + j < n) {
+                    nb[j] = ldcg(s.nb + e0 + 32 * (kb + j));
+                    cb[j] = ldcg(a.coef + e0 + 32 * (kb + j));
+                }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (kb + j < n) acc = sw_step<OP>(acc, cb[j], ldcg(a.x + nb[j]));
         }
+        v = sw_fini<OP>(acc, sc);
+        a.x[c] = v;
     }
     if (a.dotWith) {
-        double p = c >= 0 ? double(v) * double(a.dotWith[c]) : 0.0;
+        double p = c >= 0 ? double(v) * double(ldcg(a.dotWith + c)) : 0.0;
         p = block_sum<NT>(p, sh);
         if (threadIdx.x == 0) a.partials[p0 + blockIdx.x] = p;
     }
@@ -864,11 +902,25 @@ cfx_status launch_pf(cudaStream_t st, const DevSched& s, const SweepCtx<T>& a, i
     const int per = cs ? (s.n + cs - 1) / cs : 0;
     const int m = mode_of<T>(s);
     if (m == M_LEVELS) {
+        const LevelView v{s.cell, s.cnt, s.groupEntry, s.nb};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
         for (int L = 0; L < s.nLevels; ++L) {
             const int g0 = s.hLvlSlot[L] / 32, g1 = s.hLvlSlot[L + 1] / 32;
             const int ctas = (g1 - g0 + LVL_LAUNCH_GROUPS - 1) / LVL_LAUNCH_GROUPS;
             if (ctas == 0) continue;
-            sweep_level_k<T, OP><<<ctas, 32 * LVL_LAUNCH_GROUPS, 0, st>>>(s, a, g0, g1, s.hLvlPart[L]);
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(ctas);
+            cfg.blockDim = dim3(32 * LVL_LAUNCH_GROUPS);
+            cfg.stream = st;
+            // the first level follows a kernel that does not signal its
+            // dependents early (gather_slots_k): an ordinary launch
+            cfg.attrs = L > 0 ? attr : nullptr;
+            cfg.numAttrs = L > 0 ? 1 : 0;
+            // PF_SMALL entries prefetched (more registers would cost
+            // occupancy on the wide levels, which stream from HBM)
+            CFX_CUDA(cudaLaunchKernelEx(&cfg, sweep_level_k<T, OP, PF_SMALL>, v, a, g0, g1, s.hLvlPart[L]));
             count_launch();
         }
         return CFX_OK;

@@ -273,3 +273,40 @@ def test_sliced_rows_layout_on_the_host(tmp_path):
     assert "patterns=0 slices=54 patternSlices=0" in out["cube"]
     assert "ok" in out["perm"]
     assert out["hub"].count("not built") == 2
+
+
+def test_sweep_schedules_respect_their_dependencies(tmp_path):
+    """build_sched (csrc/host.cpp), compiled on its own with a checker: in the
+    reference order and in the multicolour order (greedy colours, which must
+    be proper), the forward, backward and fused 1-3-sweep Gauss-Seidel
+    schedules hold every (cell, sweep) once, each entry is the right
+    neighbour in the right order with its face's coefficient source, and
+    every value a slot reads comes from an earlier DAG level."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    csrc = os.path.join(repo, "openfoam-dev_gb300", "csrc")
+    cuda_inc = [d for d in ("/usr/local/cuda/include",) if os.path.isdir(d)]
+    exe = str(tmp_path / "sched_check")
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", csrc, "-I", INCLUDE_DIR] + [f"-I{d}" for d in cuda_inc] +
+                       [os.path.join(repo, "tests", "sched_check.cpp"), os.path.join(csrc, "host.cpp"),
+                        "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0 and "cuda_runtime.h" in r.stderr:
+        pytest.skip("no CUDA headers")
+    assert r.returncode == 0, r.stderr[-3000:]
+    cube = cases.pcg_cube(10, seed=1)
+    perm = cases.gamg_cube(9, seed=5)
+    cases.renumber(perm, cases.random_order(5, perm["diag"].size))
+    cm = cases.bicgstab_cube(10, seed=2)
+    for name, s in (("cube", cube), ("perm", perm), ("cm", cm)):
+        path = str(tmp_path / f"{name}.bin")
+        _ldu_file(path, s)
+        p = subprocess.run([exe, path], capture_output=True, text=True)
+        assert p.returncode == 0, (name, p.stdout[-2000:], p.stderr[-2000:])
+        assert p.stdout.count(" ok") == 10, (name, p.stdout)
+    # the lexicographic hexahedral cube colours in two (red-black)
+    p = subprocess.run([exe, str(tmp_path / "cube.bin")], capture_output=True, text=True)
+    assert "colours=2" in p.stdout

@@ -238,8 +238,8 @@ __global__ void __launch_bounds__(GRID_NT) sweep_grid_k(DevSched s, SweepCtx<T> 
 // launched as programmatic dependents of one another: a level's grid starts
 // while the previous level runs, loads its slots' schedule data (cell,
 // entry count, the first PF columns and coefficients, scalar, right-hand
-// side; all written by kernels that completed before the previous level
-// passed its own wait, read through L2) and only then waits
+// side by cell; all written by kernels that completed before the previous
+// level passed its own wait, read through L2) and only then waits
 // (griddepcontrol.wait) for the previous level's values; it lets its own
 // dependents start once past that wait, so a level's prologue never reads
 // anything a still-running kernel writes.  The dot partial (when requested)
@@ -265,13 +265,13 @@ __global__ void __launch_bounds__(32 * LVL_LAUNCH_GROUPS) sweep_level_k(LevelVie
         n = ldcg(s.cnt + slot);
         e0 = ldcg(s.groupEntry + g) + lane;
         sc = ldcg(a.scalar + slot);
-        if (OP == OP_FWD || OP == OP_GS) in = ldcg(a.inS + slot);
 #pragma unroll
         for (int k = 0; k < PF; ++k)
             if (k < n) {
                 nbr[k] = ldcg(s.nb + e0 + 32 * k);
                 cf[k] = ldcg(a.coef + e0 + 32 * k);
             }
+        if ((OP == OP_FWD || OP == OP_GS) && c >= 0) in = ldcg(a.in + c);
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -1242,7 +1242,9 @@ cfx_status launch_flow(cudaStream_t st, const DevSched& s, const Packed<T>& p, S
 template <class T>
 cfx_status run_sweep(cudaStream_t st, const DevSched& s, int op, const Packed<T>& p, const T* in, T* x,
                      const T* dotWith, double* partials, const int* done, int* status) {
-    if ((op == OP_FWD || op == OP_GS) && s.nSlots > 0) {
+    // the right-hand side in slot order (the level-by-level form reads it by
+    // cell in its prologue instead)
+    if ((op == OP_FWD || op == OP_GS) && s.nSlots > 0 && mode_of<T>(s) != M_LEVELS) {
         int blocks = (s.nSlots + 255) / 256;
         if (blocks > 4096) blocks = 4096;
         gather_slots_k<T><<<blocks, 256, 0, st>>>(s.nSlots, s.cell, in, p.inS, done);

@@ -548,8 +548,9 @@ cfx_status cfx_diag_sweep_stall(cfx_matrix* mat, int timeoutMs, int* status);
  * matrix's FP32 coefficient copy, psi and b device FP32 vectors of nCells,
  * in the order the inner cycles use (CFX_TUNE_COLORED_GS /
  * CFX_TUNE_COLORED_PRE).  *form (may be NULL) receives the execution form of
- * the Gauss-Seidel schedule: 0 one CTA (vector in shared memory), 1 a
- * cluster (distributed shared memory), 2 one CTA (vector in global memory),
+ * the Gauss-Seidel schedule (DIC / DILU: of the forward schedule): 0 one CTA
+ * (vector in shared memory), 1 a cluster (distributed shared memory), 2 one
+ * CTA (vector in global memory),
  * 3 a cluster (global memory), 4 the persistent grid, 5 the dataflow form,
  * 6 one launch per level.  For timing and profiling. */
 cfx_status cfx_diag_smooth_f32(cfx_matrix* mat, int kind, float* psi, const float* b, int nSweeps, int* form);

@@ -2692,8 +2692,11 @@ cfx_status cfx_diag_smooth_f32(cfx_matrix* mat, int kind, float* psi, const floa
                      [&] { smooth<float>(ctx, mat, 0, kind, psi, b, nSweeps, mat->lv32[0]); });
         if (form) {
             const int S = std::max(nSweeps, 1);
-            *form = sweep_mode<float>(gs_colored<float>() ? sched_colored(mat->mesh, 0, S)
-                                                          : sched(mat->mesh, 0, SCHED_GS, S));
+            if (kind == CFX_SMOOTH_DIC || kind == CFX_SMOOTH_DILU)  // no Gauss-Seidel: the forward schedule's
+                *form = sweep_mode<float>(sched_pre<float>(mat->mesh, 0, SCHED_FWD, pre_colored<float>(mat->sym)));
+            else
+                *form = sweep_mode<float>(gs_colored<float>() ? sched_colored(mat->mesh, 0, S)
+                                                              : sched(mat->mesh, 0, SCHED_GS, S));
         }
         CK(cudaStreamSynchronize(ctx->stream));
         const int stc = read_status(ctx);
